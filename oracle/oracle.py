@@ -1,0 +1,253 @@
+"""ctypes bindings for the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+`Oracle` wraps oracle/_build/libqj_oracle.so, the plain-C restatement of the
+reference's hot path (qj_oracle.c).  `Reference` wraps the reference QUIJIBO
+itself, compiled from its own sources into oracle/_ref/ (only where those
+sources are present); it pins the restatement and generates golden fixtures.
+Only tests, the smoke check and the benchmark's CPU-baseline leg use this.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "libqj_oracle.so")
+REF_SO = {"double": os.path.join(HERE, "_ref", "libqjref_double.so"),
+          "ldouble": os.path.join(HERE, "_ref", "libqjref_ldouble.so")}
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+def _ptr(a, t=_dp):
+    return a.ctypes.data_as(t) if a is not None else None
+
+
+def build(ref=False):
+    """Compile the restatement (and, with ref=True, the reference flavours)."""
+    subprocess.run(["make", "-s", "-C", HERE] + (["ref"] if ref else []), check=True)
+
+
+class _Poly(C.Structure):
+    _fields_ = [("n", C.c_int), ("roots", _dp), ("powers", _dp), ("power_scalar", C.c_double)]
+
+
+class _Map(C.Structure):
+    _fields_ = [("top", _Poly), ("bottom", _Poly), ("scale", C.c_double)]
+
+
+class _Grid(C.Structure):
+    _fields_ = [("res", C.c_int * 3), ("center", C.c_double * 3), ("lengths", C.c_double * 3),
+                ("rot", C.c_double * 4), ("slice", C.c_double)]
+
+
+def make_map(rootset):
+    """rootset: object with top_roots (n,4), top_powers, sigma_top, bottom_*, scale."""
+    keep = []
+
+    def poly(r, p, s):
+        r = np.ascontiguousarray(r, dtype=np.float64).reshape(-1, 4)
+        p = np.ascontiguousarray(p, dtype=np.float64).reshape(-1)
+        keep.extend([r, p])
+        return _Poly(len(p), _ptr(r), _ptr(p), float(s))
+
+    m = _Map(poly(rootset.top_roots, rootset.top_powers, rootset.sigma_top),
+             poly(rootset.bottom_roots, rootset.bottom_powers, rootset.sigma_bottom),
+             float(rootset.scale))
+    m._keep = keep
+    return m
+
+
+def make_grid(grid):
+    g = _Grid()
+    g.res[:] = list(grid.res)
+    g.center[:] = list(grid.center)
+    g.lengths[:] = list(grid.lengths)
+    g.rot[:] = list(grid.rot)
+    g.slice = float(grid.slice)
+    return g
+
+
+class Oracle:
+    def __init__(self, path=ORACLE_SO):
+        if not os.path.exists(path):
+            build()
+        L = C.CDLL(path)
+        L.qjo_mt_rand.argtypes = [C.c_uint32, C.c_int, _dp]
+        L.qjo_quat_pow.argtypes = [_dp, C.c_double, _dp]
+        L.qjo_field.argtypes = [C.POINTER(_Map), C.POINTER(_Grid), C.c_int, C.c_double, C.c_int,
+                                C.c_int, _dp, _dp, C.POINTER(C.c_int32), C.c_int]
+        L.qjo_field.restype = C.c_int64
+        L.qjo_nonlinear_value.argtypes = [C.POINTER(_Map), _dp, C.c_double, C.c_int, C.c_double,
+                                          C.c_double]
+        L.qjo_nonlinear_value.restype = C.c_double
+        L.qjo_mesh.argtypes = [C.POINTER(_Map), C.POINTER(_Grid), _dp, C.c_int, C.c_int,
+                               C.c_double, C.c_double, _dp, C.c_int64, C.POINTER(C.c_int32),
+                               C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                               C.POINTER(C.c_int64), C.c_int]
+        L.qjo_trilinear.argtypes = [C.POINTER(_Grid), _dp, _dp]
+        L.qjo_trilinear.restype = C.c_double
+        L.qjo_cell_center.argtypes = [C.POINTER(_Grid), C.c_int, C.c_int, C.c_int, _dp]
+        self.L = L
+
+    def mt_rand(self, seed, n):
+        out = np.empty(n)
+        self.L.qjo_mt_rand(seed, n, _ptr(out))
+        return out
+
+    def quat_pow(self, q, e):
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        out = np.empty(4)
+        self.L.qjo_quat_pow(_ptr(q), e, _ptr(out))
+        return out
+
+    def cell_center(self, grid, x, y, z):
+        out = np.empty(3)
+        self.L.qjo_cell_center(C.byref(make_grid(grid)), x, y, z, _ptr(out))
+        return out
+
+    def field(self, rootset, grid, max_it, escape, z0=0, z1=None, de=False, iters=False,
+              nthreads=0):
+        X, Y, Z = grid.res
+        z1 = Z if z1 is None else z1
+        n = X * Y * (z1 - z0)
+        f = np.empty(n)
+        d = np.empty(n) if de else None
+        it = np.empty(n, dtype=np.int32) if iters else None
+        m, g = make_map(rootset), make_grid(grid)
+        terms = self.L.qjo_field(C.byref(m), C.byref(g), max_it, escape, z0, z1, _ptr(f),
+                                 _ptr(d), _ptr(it, C.POINTER(C.c_int32)), nthreads)
+        shape = (z1 - z0, Y, X)
+        out = {"field": f.reshape(shape), "root_terms": int(terms)}
+        if de:
+            out["de"] = d.reshape(shape)
+        if iters:
+            out["iters"] = it.reshape(shape)
+        return out
+
+    def nonlinear_value(self, rootset, p, slice_, max_it, escape, iso=0.0):
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        return self.L.qjo_nonlinear_value(C.byref(make_map(rootset)), _ptr(p), slice_, max_it,
+                                          escape, iso)
+
+    def mesh(self, rootset, grid, classify, mode, max_it, escape, iso=0.0, nthreads=0):
+        classify = np.ascontiguousarray(classify, dtype=np.float64).reshape(-1)
+        N = classify.size
+        cap_v, cap_t = 3 * N + 16, 5 * N + 16
+        verts = np.empty(3 * cap_v)
+        tris = np.empty(3 * cap_t, dtype=np.int32)
+        nv, nt, nu = C.c_int64(), C.c_int64(), C.c_int64()
+        m = make_map(rootset) if rootset is not None else _Map()
+        rc = self.L.qjo_mesh(C.byref(m), C.byref(make_grid(grid)), _ptr(classify), mode, max_it,
+                             escape, iso, _ptr(verts), cap_v, _ptr(tris, C.POINTER(C.c_int32)),
+                             cap_t, C.byref(nv), C.byref(nt), C.byref(nu), nthreads)
+        assert rc == 0, rc
+        return {"verts": verts[:3 * nv.value].reshape(-1, 3).copy(),
+                "tris": tris[:3 * nt.value].reshape(-1, 3).copy(), "unbracketed": nu.value}
+
+    def trilinear(self, grid, data, p):
+        data = np.ascontiguousarray(data, dtype=np.float64).reshape(-1)
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        return self.L.qjo_trilinear(C.byref(make_grid(grid)), _ptr(data), _ptr(p))
+
+
+class _MapArgs(C.Structure):
+    _fields_ = [("nt", C.c_int), ("troots", _dp), ("tpows", _dp), ("tsig", C.c_double),
+                ("nb", C.c_int), ("broots", _dp), ("bpows", _dp), ("bsig", C.c_double),
+                ("s", C.c_double)]
+
+
+def _map_args(rs):
+    tr = np.ascontiguousarray(rs.top_roots, dtype=np.float64).reshape(-1, 4)
+    tp = np.ascontiguousarray(rs.top_powers, dtype=np.float64)
+    br = np.ascontiguousarray(rs.bottom_roots, dtype=np.float64).reshape(-1, 4)
+    bp = np.ascontiguousarray(rs.bottom_powers, dtype=np.float64)
+    a = _MapArgs(len(tp), _ptr(tr), _ptr(tp), rs.sigma_top, len(bp), _ptr(br), _ptr(bp),
+                 rs.sigma_bottom, rs.scale)
+    a._keep = (tr, tp, br, bp)
+    return a
+
+
+class Reference:
+    """The reference implementation compiled from its own sources."""
+
+    def __init__(self, flavour="double"):
+        path = REF_SO[flavour]
+        if not os.path.exists(path):
+            build(ref=True)
+        L = C.CDLL(path)
+        L.ref_sizeof_real.restype = C.c_int
+        L.ref_mt_rand.argtypes = [C.c_uint, C.c_int, _dp]
+        L.ref_quat_pow.argtypes = [_dp, C.c_double, _dp]
+        A = C.POINTER(_MapArgs)
+        L.ref_field_escape.argtypes = [A, _ip, _dp, _dp, _dp, C.c_double, C.c_int, C.c_double, _dp]
+        L.ref_field_map.argtypes = [A, _ip, _dp, _dp, C.c_double, C.c_int, _dp]
+        L.ref_mesh_stream.argtypes = [A, _ip, _dp, _dp, _dp, C.c_double, C.c_int, C.c_double, _dp,
+                                      C.c_int, _ip, C.c_int, _ip, _ip]
+        L.ref_mesh_field_nonlinear.argtypes = [A, _ip, _dp, _dp, _dp, C.c_double, C.c_int,
+                                               C.c_double, _dp, C.c_int, _ip, C.c_int, _ip, _ip]
+        L.ref_mesh_linear.argtypes = [_ip, _dp, _dp, _dp, _dp, C.c_int, _ip, C.c_int, _ip, _ip]
+        self.L = L
+        self.sizeof_real = L.ref_sizeof_real()
+
+    @staticmethod
+    def _g(grid):
+        res = np.array(grid.res, dtype=np.int32)
+        return (res, np.array(grid.center, dtype=np.float64),
+                np.array(grid.lengths, dtype=np.float64), np.array(grid.rot, dtype=np.float64))
+
+    def mt_rand(self, seed, n):
+        out = np.empty(n)
+        self.L.ref_mt_rand(seed, n, _ptr(out))
+        return out
+
+    def quat_pow(self, q, e):
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        out = np.empty(4)
+        self.L.ref_quat_pow(_ptr(q), e, _ptr(out))
+        return out
+
+    def field_escape(self, rs, grid, max_it, escape):
+        res, c, l, r = self._g(grid)
+        out = np.empty(int(np.prod(res)))
+        self.L.ref_field_escape(C.byref(_map_args(rs)), _ptr(res, _ip), _ptr(c), _ptr(l), _ptr(r),
+                                grid.slice, max_it, escape, _ptr(out))
+        return out.reshape(res[2], res[1], res[0])
+
+    def field_map(self, rs, grid, max_it):
+        res, c, l, _ = self._g(grid)
+        out = np.empty(int(np.prod(res)))
+        self.L.ref_field_map(C.byref(_map_args(rs)), _ptr(res, _ip), _ptr(c), _ptr(l), grid.slice,
+                             max_it, _ptr(out))
+        return out.reshape(res[2], res[1], res[0])
+
+    def _mesh_out(self, fn, *args, n):
+        cap_v, cap_t = 3 * n + 16, 5 * n + 16
+        verts = np.empty(3 * cap_v)
+        tris = np.empty(3 * cap_t, dtype=np.int32)
+        nv, nt = C.c_int(), C.c_int()
+        rc = fn(*args, _ptr(verts), cap_v, _ptr(tris, _ip), cap_t, C.byref(nv), C.byref(nt))
+        assert rc == 0, rc
+        return {"verts": verts[:3 * nv.value].reshape(-1, 3).copy(),
+                "tris": tris[:3 * nt.value].reshape(-1, 3).copy()}
+
+    def mesh_stream(self, rs, grid, max_it, iso=0.0):
+        res, c, l, r = self._g(grid)
+        return self._mesh_out(self.L.ref_mesh_stream, C.byref(_map_args(rs)), _ptr(res, _ip),
+                              _ptr(c), _ptr(l), _ptr(r), grid.slice, max_it, iso,
+                              n=int(np.prod(res)))
+
+    def mesh_field_nonlinear(self, rs, grid, field, max_it, iso=0.0):
+        res, c, l, _ = self._g(grid)
+        f = np.ascontiguousarray(field, dtype=np.float64).reshape(-1)
+        return self._mesh_out(self.L.ref_mesh_field_nonlinear, C.byref(_map_args(rs)),
+                              _ptr(res, _ip), _ptr(c), _ptr(l), _ptr(f), grid.slice, max_it, iso,
+                              n=f.size)
+
+    def mesh_linear(self, grid, field):
+        res, c, l, _ = self._g(grid)
+        f = np.ascontiguousarray(field, dtype=np.float64).reshape(-1)
+        return self._mesh_out(self.L.ref_mesh_linear, _ptr(res, _ip), _ptr(c), _ptr(l), _ptr(f),
+                              n=f.size)

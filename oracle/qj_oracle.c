@@ -1,0 +1,430 @@
+/*
+ * CPU oracle for the QUIJIBO hot path -- TEST INFRASTRUCTURE ONLY (see
+ * qj_oracle.h).  Compile with -ffp-contract=off so that no multiply-add is
+ * fused: the reference's x86-64 double build rounds every product and sum
+ * separately, and so does this file.
+ *
+ * Reference files cited below are paths inside the QUIJIBO project.
+ */
+#include "qj_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../quijibo_gb300/csrc/mc_cases.h"
+
+/* SETTINGS.h:60 -- REAL_MIN is FLT_MIN whatever Real is. */
+#define QJO_REAL_MIN ((double)FLT_MIN)
+
+/* ------------------------------------------------------------------ */
+/* MT19937 as MERSENNETWISTER (src/util/MERSENNETWISTER.h:147, 287-330):
+ * Matsumoto & Nishimura's init_genrand seeding and tempering; rand()
+ * scales a 32-bit draw by 1/(2^32-1). */
+void qjo_mt_rand(uint32_t seed, int n, double* out) {
+  uint32_t mt[624];
+  int idx = 624;
+  mt[0] = seed;
+  for (int i = 1; i < 624; i++)
+    mt[i] = 1812433253u * (mt[i - 1] ^ (mt[i - 1] >> 30)) + (uint32_t)i;
+  for (int k = 0; k < n; k++) {
+    if (idx >= 624) {
+      for (int i = 0; i < 624; i++) {
+        uint32_t y = (mt[i] & 0x80000000u) | (mt[(i + 1) % 624] & 0x7fffffffu);
+        mt[i] = mt[(i + 397) % 624] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+      }
+      idx = 0;
+    }
+    uint32_t y = mt[idx++];
+    y ^= y >> 11;
+    y ^= (y << 7) & 0x9d2c5680u;
+    y ^= (y << 15) & 0xefc60000u;
+    y ^= y >> 18;
+    out[k] = (double)y * (1.0 / 4294967295.0);
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* Quaternion helpers, all (w, x, y, z). */
+
+/* QUATERNION::operator*= and operator*(q, q): QUATERNION.h:51-58,
+ * QUATERNION.cpp:154-162 (identical formulas and order). */
+static inline void qmul(const double a[4], const double b[4], double o[4]) {
+  const double x = a[2] * b[3] - a[3] * b[2] + b[0] * a[1] + a[0] * b[1];
+  const double y = a[3] * b[1] - a[1] * b[3] + b[0] * a[2] + a[0] * b[2];
+  const double z = a[1] * b[2] - a[2] * b[1] + b[0] * a[3] + a[0] * b[3];
+  const double w = a[0] * b[0] - a[1] * b[1] - b[2] * a[2] - a[3] * b[3];
+  o[0] = w; o[1] = x; o[2] = y; o[3] = z;
+}
+
+/* QUATERNION::magnitude, QUATERNION.h:93. */
+static inline double qmag(const double q[4]) {
+  return sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+}
+
+/* operator/(q, q): QUATERNION.cpp:174-182 -- l * (conj(r) * (1/|r|^2)). */
+static inline void qdiv(const double l[4], const double r[4], double o[4]) {
+  const double m2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + r[3] * r[3];
+  const double inv = 1.0 / m2; /* operator/(QUATERNION, Real), QUATERNION.cpp:195-199 */
+  double ri[4] = {r[0] * inv, -r[1] * inv, -r[2] * inv, -r[3] * inv};
+  qmul(l, ri, o);
+}
+
+/* QUATERNION::pow, QUATERNION.cpp:375-393. */
+void qjo_quat_pow(const double q[4], double e, double out[4]) {
+  const double partial = q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+  const double qm = sqrt(partial + q[0] * q[0]);
+  const double vm = sqrt(partial);
+  const double vminv = (vm > 0.0) ? 1.0 / vm : 0.0;
+  const double scale = e * acos(q[0] / qm) * vminv;
+  const double mag = scale * vm;
+  const double maginv = (mag > 0.0) ? 1.0 / mag : 0.0;
+  const double exps = exp(e * log(qm));
+  const double scale2 = scale * exps * maginv * sin(mag);
+  out[0] = exps * cos(mag);
+  out[1] = scale2 * q[1];
+  out[2] = scale2 * q[2];
+  out[3] = scale2 * q[3];
+}
+
+/* POLYNOMIAL_4D::evaluateScaledPowerFactored, POLYNOMIAL_4D.cpp:912-923. */
+void qjo_eval_factored(const qjo_poly* p, const double q[4], double out[4]) {
+  double d[4], t[4], r[4];
+  for (int c = 0; c < 4; c++) d[c] = q[c] - p->roots[c];
+  qjo_quat_pow(d, p->power_scalar * p->powers[0], r);
+  for (int i = 1; i < p->n; i++) {
+    for (int c = 0; c < 4; c++) d[c] = q[c] - p->roots[4 * i + c];
+    qjo_quat_pow(d, p->power_scalar * p->powers[i], t);
+    double o[4];
+    qmul(r, t, o);
+    memcpy(r, o, sizeof r);
+  }
+  memcpy(out, r, sizeof r);
+}
+
+/* One map application as in the escape loop of
+ * OPTIMIZE_3D::computeLogScaledPowerRationalMap (OPTIMIZE_3D.cpp:1331-1350). */
+void qjo_map_apply(const qjo_map* m, const double q[4], double out[4]) {
+  double t[4];
+  qjo_eval_factored(&m->top, q, t);
+  if (m->bottom.n > 0) {
+    double b[4];
+    qjo_eval_factored(&m->bottom, q, b);
+    qdiv(t, b, out);
+  } else {
+    memcpy(out, t, sizeof t);
+  }
+  for (int c = 0; c < 4; c++) out[c] *= m->scale;
+}
+
+/* |grad_q log|R(q)|| for the distance estimate: the norm of
+ * sigma_t sum e_i (q-t_i)/|q-t_i|^2 - sigma_b sum f_j (q-b_j)/|q-b_j|^2.
+ * (No reference counterpart; the reference tracks no derivative for this map.) */
+static double log_gradient_norm(const qjo_map* m, const double q[4]) {
+  double g[4] = {0, 0, 0, 0};
+  for (int side = 0; side < 2; side++) {
+    const qjo_poly* p = side ? &m->bottom : &m->top;
+    const double sgn = side ? -1.0 : 1.0;
+    for (int i = 0; i < p->n; i++) {
+      double d[4];
+      for (int c = 0; c < 4; c++) d[c] = q[c] - p->roots[4 * i + c];
+      const double d2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2] + d[3] * d[3];
+      const double k = sgn * p->power_scalar * p->powers[i] / d2;
+      for (int c = 0; c < 4; c++) g[c] += k * d[c];
+    }
+  }
+  return qmag(g);
+}
+
+/* FIELD_3D::cellCenter, FIELD_3D.cpp:818-841, with the rotation matrix of
+ * QUATERNION::toRotationMatrix (QUATERNION.cpp:395-411) and the row-dot
+ * MATRIX3 * VEC3 of MATRIX3.h:200-201. */
+void qjo_cell_center(const qjo_grid* g, int x, int y, int z, double out[3]) {
+  const double dx[3] = {g->lengths[0] / g->res[0], g->lengths[1] / g->res[1],
+                        g->lengths[2] / g->res[2]};
+  const int idx[3] = {x, y, z};
+  double f[3];
+  for (int c = 0; c < 3; c++) {
+    const double half = g->lengths[c] * 0.5;
+    f[c] = g->center[c] - half;
+    f[c] += idx[c] * dx[c];
+  }
+  for (int c = 0; c < 3; c++) f[c] += dx[c] * 0.5;
+  for (int c = 0; c < 3; c++) f[c] -= g->center[c];
+  const double w = g->rot[0], qx = g->rot[1], qy = g->rot[2], qz = g->rot[3];
+  double R[3][3];
+  R[0][0] = 1 - 2 * qy * qy - 2 * qz * qz;
+  R[0][1] = 2 * qx * qy - 2 * w * qz;
+  R[0][2] = 2 * qx * qz + 2 * w * qy;
+  R[1][0] = 2 * qx * qy + 2 * w * qz;
+  R[1][1] = 1 - 2 * qx * qx - 2 * qz * qz;
+  R[1][2] = 2 * qy * qz - 2 * w * qx;
+  R[2][0] = 2 * qx * qz - 2 * w * qy;
+  R[2][1] = 2 * qy * qz + 2 * w * qx;
+  R[2][2] = 1 - 2 * qx * qx - 2 * qy * qy;
+  double r[3];
+  for (int c = 0; c < 3; c++) r[c] = R[c][0] * f[0] + R[c][1] * f[1] + R[c][2] * f[2];
+  for (int c = 0; c < 3; c++) out[c] = r[c] + g->center[c];
+}
+
+/* The escape-time loop of OPTIMIZE_3D::computeLogScaledPowerRationalMap
+ * (OPTIMIZE_3D.cpp:1317-1362) and TRIANGLE_MESH::nonlinearValue
+ * (TRIANGLE_MESH.cpp:1755-1795) with the escape radius as a parameter.
+ * The initial iterate is QUATERNION(x, y, z, slice): w = x, and the slice is
+ * the k component.  Returns log|q_N|; *de and *iters are optional. */
+static double escape_value(const qjo_map* m, const double p[3], double slice, int max_it,
+                           double escape, double* de, int32_t* iters) {
+  double q[4] = {p[0], p[1], p[2], slice};
+  double mag = qmag(q);
+  int it = 0, executed = 0;
+  double dnorm = 1.0; /* |q_n'| */
+  while (mag < escape && it < max_it) {
+    double nq[4];
+    if (de) dnorm *= log_gradient_norm(m, q);
+    qjo_map_apply(m, q, nq);
+    memcpy(q, nq, sizeof q);
+    mag = qmag(q);
+    if (de) dnorm *= mag;
+    it++;
+    executed++;
+    if (mag < 10.0 * QJO_REAL_MIN) it = max_it;
+  }
+  const double f = log(mag);
+  if (de) *de = mag * f / dnorm;
+  if (iters) *iters = executed;
+  return f;
+}
+
+int64_t qjo_field(const qjo_map* m, const qjo_grid* g, int max_it, double escape, int z0,
+                  int z1, double* field, double* de, int32_t* iters, int nthreads) {
+  const int X = g->res[0], Y = g->res[1];
+  const int64_t slab = (int64_t)X * Y;
+  const int rows = (z1 - z0) * Y;
+  int64_t terms = 0;
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_num_procs();
+#pragma omp parallel for schedule(dynamic) num_threads(nthreads) reduction(+ : terms)
+#endif
+  for (int r = 0; r < rows; r++) {
+    const int z = z0 + r / Y, y = r % Y;
+    for (int x = 0; x < X; x++) {
+      double p[3], d;
+      int32_t n;
+      qjo_cell_center(g, x, y, z, p);
+      const int64_t i = (int64_t)(z - z0) * slab + (int64_t)y * X + x;
+      field[i] = escape_value(m, p, g->slice, max_it, escape, de ? &d : NULL, &n);
+      if (de) de[i] = d;
+      if (iters) iters[i] = n;
+      terms += (int64_t)n * (m->top.n + m->bottom.n);
+    }
+  }
+  return terms;
+}
+
+double qjo_nonlinear_value(const qjo_map* m, const double p[3], double slice, int max_it,
+                           double escape, double iso) {
+  return escape_value(m, p, slice, max_it, escape, NULL, NULL) - iso;
+}
+
+/* ------------------------------------------------------------------ */
+/* Marching cubes. */
+
+/* Edge id -> (lower-endpoint corner offset, axis), TRIANGLE_MESH.cpp:1569-1665. */
+static const int EDGE_OFF[13][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 1}, {0, 1, 0},
+                                    {1, 0, 0}, {1, 0, 0}, {1, 0, 1}, {1, 1, 0}, {0, 1, 0},
+                                    {0, 0, 0}, {0, 0, 1}, {0, 1, 1}};
+static const int EDGE_AXIS[13] = {0, 1, 2, 1, 2, 1, 2, 1, 2, 0, 0, 0, 0};
+
+static inline int cube_flag(const double* v, int X, int64_t slab, int x, int y, int z) {
+  const int64_t i = (int64_t)z * slab + (int64_t)y * X + x;
+  /* corner weights NNN=1 NNP=2 NPN=4 NPP=8 PNN=16 PNP=32 PPN=64 PPP=128,
+   * TRIANGLE_MESH.cpp:4929-4931 (first letter x, then y, then z) */
+  return (v[i] > 0) + 2 * (v[i + slab] > 0) + 4 * (v[i + X] > 0) + 8 * (v[i + X + slab] > 0) +
+         16 * (v[i + 1] > 0) + 32 * (v[i + 1 + slab] > 0) + 64 * (v[i + 1 + X] > 0) +
+         128 * (v[i + 1 + X + slab] > 0);
+}
+
+/* TRIANGLE_MESH::midpointSearch, TRIANGLE_MESH.cpp:2232-2271. */
+static void midpoint_search(const qjo_map* m, double slice, int max_it, double escape,
+                            double iso, const double pv[3], double pval, const double nv[3],
+                            double nval, int rec, double out[3], int* unbracketed) {
+  double mid[3];
+  for (int c = 0; c < 3; c++) mid[c] = pv[c] + nv[c];
+  for (int c = 0; c < 3; c++) mid[c] *= 0.5;
+  if (pval * nval >= 0.0) {
+    *unbracketed = 1;
+    memcpy(out, mid, sizeof mid);
+    return;
+  }
+  if (rec >= 6) {
+    memcpy(out, mid, sizeof mid);
+    return;
+  }
+  const double mval = qjo_nonlinear_value(m, mid, slice, max_it, escape, iso);
+  if (fabs(mval) < 1e-8) {
+    memcpy(out, mid, sizeof mid);
+    return;
+  }
+  if (mval < 0)
+    midpoint_search(m, slice, max_it, escape, iso, pv, pval, mid, mval, rec + 1, out, unbracketed);
+  else
+    midpoint_search(m, slice, max_it, escape, iso, mid, mval, nv, nval, rec + 1, out, unbracketed);
+}
+
+int qjo_mesh(const qjo_map* m, const qjo_grid* g, const double* v, int mode, int max_it,
+             double escape, double iso, double* verts, int64_t max_verts, int32_t* tris,
+             int64_t max_tris, int64_t* n_verts, int64_t* n_tris, int64_t* n_unbracketed,
+             int nthreads) {
+  const int X = g->res[0], Y = g->res[1], Z = g->res[2];
+  const int64_t slab = (int64_t)X * Y, N = slab * Z;
+  /* 1. Active edges: every edge some cube's case places a vertex on
+   * (the union of the per-cube std::map inserts, TRIANGLE_MESH.cpp:1471-1481).
+   * Edge key = 3 * lower-endpoint linear index + axis; ascending key order
+   * equals the std::map order of (VEC3I, VEC3I) pairs (VEC3.h:181-205). */
+  unsigned char* used = (unsigned char*)calloc((size_t)N, 1); /* bit axis */
+  for (int z = 0; z < Z - 1; z++)
+    for (int y = 0; y < Y - 1; y++)
+      for (int x = 0; x < X - 1; x++) {
+        const int f = cube_flag(v, X, slab, x, y, z);
+        const unsigned short mask = QJ_MC_EDGEMASK[f];
+        for (int e = 1; e <= 12; e++)
+          if (mask & (1 << (e - 1))) {
+            const int64_t i = (int64_t)(z + EDGE_OFF[e][2]) * slab +
+                              (int64_t)(y + EDGE_OFF[e][1]) * X + (x + EDGE_OFF[e][0]);
+            used[i] |= (unsigned char)(1 << EDGE_AXIS[e]);
+          }
+      }
+  /* 2. Vertex numbering: rank in key order. */
+  int64_t* base = (int64_t*)malloc(sizeof(int64_t) * (size_t)(N + 1));
+  int64_t nv = 0;
+  for (int64_t i = 0; i < N; i++) {
+    base[i] = nv;
+    nv += (used[i] & 1) + ((used[i] >> 1) & 1) + ((used[i] >> 2) & 1);
+  }
+  base[N] = nv;
+  *n_verts = nv;
+  if (nv > max_verts) {
+    free(used);
+    free(base);
+    return -1;
+  }
+  /* 3. Edge vertices (computeEdgeInterpolations TRIANGLE_MESH.cpp:2373-2425, or
+   * computeNonlinearEdgeInterpolationsHuge TRIANGLE_MESH.cpp:2034-2123). */
+  int64_t unbr = 0;
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_num_procs();
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads) reduction(+ : unbr)
+#endif
+  for (int64_t i = 0; i < N; i++) {
+    if (!used[i]) continue;
+    const int x = (int)(i % X), y = (int)((i / X) % Y), z = (int)(i / slab);
+    int64_t k = base[i];
+    for (int a = 0; a < 3; a++) {
+      if (!(used[i] & (1 << a))) continue;
+      const int x1 = x + (a == 0), y1 = y + (a == 1), z1 = z + (a == 2);
+      double p0[3], p1[3], out[3];
+      qjo_cell_center(g, x, y, z, p0);
+      qjo_cell_center(g, x1, y1, z1, p1);
+      if (mode == 0) {
+        double off[3];
+        for (int c = 0; c < 3; c++) off[c] = p1[c] - p0[c];
+        const double d0 = v[i], d1 = v[(int64_t)z1 * slab + (int64_t)y1 * X + x1];
+        const double t = d0 / (d0 - d1);
+        for (int c = 0; c < 3; c++) out[c] = p0[c] + t * off[c];
+      } else {
+        const double f0 = qjo_nonlinear_value(m, p0, g->slice, max_it, escape, iso);
+        const double f1 = qjo_nonlinear_value(m, p1, g->slice, max_it, escape, iso);
+        int bad = (f0 * f1 >= 0.0);
+        const double *pv = p0, *nvx = p1;
+        double pval = f0, nval = f1;
+        if (f0 < 0) {
+          pv = p1; nvx = p0; pval = f1; nval = f0;
+        }
+        midpoint_search(m, g->slice, max_it, escape, iso, pv, pval, nvx, nval, 0, out, &bad);
+        unbr += bad;
+      }
+      memcpy(verts + 3 * k, out, sizeof out);
+      k++;
+    }
+  }
+  *n_unbracketed = unbr;
+  /* 4. Triangles in cube scan order (z, y, x), the case's triangles in table
+   * order, then the degenerate filter of TRIANGLE_MESH.cpp:737-756. */
+  int64_t nt = 0;
+  int overflow = 0;
+  for (int z = 0; z < Z - 1; z++)
+    for (int y = 0; y < Y - 1; y++)
+      for (int x = 0; x < X - 1; x++) {
+        const int f = cube_flag(v, X, slab, x, y, z);
+        const unsigned char* c = QJ_MC_CASES[f];
+        for (int t = 0; t < QJ_MC_MAX_TRIS && c[3 * t]; t++) {
+          int64_t id[3];
+          for (int j = 0; j < 3; j++) {
+            const int e = c[3 * t + j];
+            const int64_t i = (int64_t)(z + EDGE_OFF[e][2]) * slab +
+                              (int64_t)(y + EDGE_OFF[e][1]) * X + (x + EDGE_OFF[e][0]);
+            const int a = EDGE_AXIS[e];
+            id[j] = base[i] + ((a > 0) ? (used[i] & 1) : 0) + ((a > 1) ? ((used[i] >> 1) & 1) : 0);
+          }
+          const double* v0 = verts + 3 * id[0];
+          const double* v1 = verts + 3 * id[1];
+          const double* v2 = verts + 3 * id[2];
+          double d01[3], d02[3], d12[3];
+          for (int q = 0; q < 3; q++) {
+            d01[q] = v0[q] - v1[q];
+            d02[q] = v0[q] - v2[q];
+            d12[q] = v1[q] - v2[q];
+          }
+          const double e0 = sqrt(d01[0] * d01[0] + d01[1] * d01[1] + d01[2] * d01[2]);
+          const double e1 = sqrt(d02[0] * d02[0] + d02[1] * d02[1] + d02[2] * d02[2]);
+          const double e2 = sqrt(d12[0] * d12[0] + d12[1] * d12[1] + d12[2] * d12[2]);
+          const double eps = 1e-7;
+          if (e0 < eps || e1 < eps || e2 < eps) continue;
+          if (nt >= max_tris) {
+            overflow = 1;
+            nt++;
+            continue;
+          }
+          for (int j = 0; j < 3; j++) tris[3 * nt + j] = (int32_t)id[j];
+          nt++;
+        }
+      }
+  *n_tris = nt;
+  free(used);
+  free(base);
+  return overflow ? -1 : 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* FIELD_3D::operator()(const VEC3F&), FIELD_3D.cpp:966-1029: clamped
+ * trilinear interpolation with float weights. */
+double qjo_trilinear(const qjo_grid* g, const double* data, const double p[3]) {
+  const int X = g->res[0], Y = g->res[1], Z = g->res[2];
+  const int64_t slab = (int64_t)X * Y;
+  const double dx[3] = {g->lengths[0] / X, g->lengths[1] / Y, g->lengths[2] / Z};
+  const double inv[3] = {1.0 / dx[0], 1.0 / dx[1], 1.0 / dx[2]};
+  double pc[3], corner[3];
+  for (int c = 0; c < 3; c++) corner[c] = g->center[c] - 0.5 * g->lengths[c];
+  for (int c = 0; c < 3; c++) corner[c] += 0.5 * dx[c];
+  for (int c = 0; c < 3; c++) pc[c] = p[c] - corner[c];
+  for (int c = 0; c < 3; c++) pc[c] *= inv[c];
+  int x0 = (int)pc[0], y0 = (int)pc[1], z0 = (int)pc[2];
+  int x1 = x0 + 1, y1 = y0 + 1, z1 = z0 + 1;
+  x0 = x0 < 0 ? 0 : x0; y0 = y0 < 0 ? 0 : y0; z0 = z0 < 0 ? 0 : z0;
+  x1 = x1 < 0 ? 0 : x1; y1 = y1 < 0 ? 0 : y1; z1 = z1 < 0 ? 0 : z1;
+  x0 = x0 > X - 1 ? X - 1 : x0; y0 = y0 > Y - 1 ? Y - 1 : y0; z0 = z0 > Z - 1 ? Z - 1 : z0;
+  x1 = x1 > X - 1 ? X - 1 : x1; y1 = y1 > Y - 1 ? Y - 1 : y1; z1 = z1 > Z - 1 ? Z - 1 : z1;
+  const float s1 = (float)(pc[0] - x0), s0 = 1.0f - s1;
+  const float t1 = (float)(pc[1] - y0), t0 = 1.0f - t1;
+  const float u1 = (float)(pc[2] - z0), u0 = 1.0f - u1;
+#define AT(xx, yy, zz) data[(xx) + (int64_t)(yy) * X + (int64_t)(zz) * slab]
+  return u0 * (s0 * (t0 * AT(x0, y0, z0) + t1 * AT(x0, y1, z0)) +
+               s1 * (t0 * AT(x1, y0, z0) + t1 * AT(x1, y1, z0))) +
+         u1 * (s0 * (t0 * AT(x0, y0, z1) + t1 * AT(x0, y1, z1)) +
+               s1 * (t0 * AT(x1, y0, z1) + t1 * AT(x1, y1, z1)));
+#undef AT
+}

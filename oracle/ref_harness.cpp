@@ -1,0 +1,177 @@
+// Harness that runs the reference QUIJIBO implementation, compiled from its
+// own sources, behind a small C ABI.  TEST INFRASTRUCTURE ONLY: it is built
+// (by oracle/Makefile) only where the reference sources are present, into
+// oracle/_ref/, and is used to pin the C restatement in qj_oracle.c and to
+// generate the golden fixtures in tests/golden/.
+//
+// Everything here calls the reference's own classes; the one loop written
+// here is the escape-time loop with the escape radius as a parameter
+// (the reference hard-codes 2000), restated from OPTIMIZE_3D.cpp:1317-1362
+// around the reference's POLYNOMIAL_4D / QUATERNION / FIELD_3D calls.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <unistd.h>
+
+#include "FIELD_3D.h"
+#include "MERSENNETWISTER.h"
+#include "OPTIMIZE_3D.h"
+#include "POLYNOMIAL_4D.h"
+#include "QUATERNION.h"
+#include "TRIANGLE_MESH.h"
+
+namespace {
+
+POLYNOMIAL_4D make_poly(int n, const double* roots, const double* pows, double sigma) {
+  if (n == 0) return POLYNOMIAL_4D();
+  std::vector<QUATERNION> r;
+  std::vector<Real> p;
+  for (int i = 0; i < n; i++) {
+    r.push_back(QUATERNION(roots[4 * i], roots[4 * i + 1], roots[4 * i + 2], roots[4 * i + 3]));
+    p.push_back(pows[i]);
+  }
+  POLYNOMIAL_4D poly(r, p);
+  poly.powerScalar() = sigma;
+  return poly;
+}
+
+struct MapArgs {
+  int nt;
+  const double* troots;
+  const double* tpows;
+  double tsig;
+  int nb;
+  const double* broots;
+  const double* bpows;
+  double bsig;
+  double s;
+};
+
+int export_mesh(TRIANGLE_MESH& mesh, double* verts, int max_v, int* tris, int max_t, int* nv,
+                int* nt) {
+  const int V = (int)mesh.vertices().size();
+  const int T = (int)mesh.triangles().size();
+  *nv = V;
+  *nt = T;
+  if (V > max_v || T > max_t) return -1;
+  for (int i = 0; i < V; i++)
+    for (int c = 0; c < 3; c++) verts[3 * i + c] = (double)mesh.vertices()[i][c];
+  for (int t = 0; t < T; t++)
+    for (int j = 0; j < 3; j++) tris[3 * t + j] = mesh.vertexIndex(t, j);
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ref_sizeof_real() { return (int)sizeof(Real); }
+
+void ref_mt_rand(unsigned seed, int n, double* out) {
+  MERSENNETWISTER mt(seed);
+  for (int i = 0; i < n; i++) out[i] = mt.rand();
+}
+
+void ref_quat_pow(const double* q, double e, double* out) {
+  QUATERNION r = QUATERNION(q[0], q[1], q[2], q[3]).pow(e);
+  for (int c = 0; c < 4; c++) out[c] = (double)r[c];
+}
+
+// Escape-time field with a parameterised escape radius.
+void ref_field_escape(const MapArgs* a, const int* res, const double* center,
+                      const double* lengths, const double* rot, double slice, int max_it,
+                      double escape, double* out) {
+  POLYNOMIAL_4D top = make_poly(a->nt, a->troots, a->tpows, a->tsig);
+  POLYNOMIAL_4D bottom = make_poly(a->nb, a->broots, a->bpows, a->bsig);
+  FIELD_3D grid(res[0], res[1], res[2], VEC3F(center[0], center[1], center[2]),
+                VEC3F(lengths[0], lengths[1], lengths[2]));
+  grid.rotation() = QUATERNION(rot[0], rot[1], rot[2], rot[3]);
+  const Real s = a->s;
+#pragma omp parallel for schedule(dynamic)
+  for (int z = 0; z < res[2]; z++)
+    for (int y = 0; y < res[1]; y++)
+      for (int x = 0; x < res[0]; x++) {
+        VEC3F point = grid.cellCenter(x, y, z);
+        QUATERNION iterate(point[0], point[1], point[2], (Real)slice);
+        Real magnitude = iterate.magnitude();
+        int totalIterations = 0;
+        while (magnitude < escape && totalIterations < max_it) {
+          QUATERNION topEval = top.evaluateScaledPowerFactored(iterate);
+          if (bottom.totalRoots() > 0) {
+            QUATERNION bottomEval = bottom.evaluateScaledPowerFactored(iterate);
+            iterate = (topEval / bottomEval);
+          } else
+            iterate = topEval;
+          iterate *= s;
+          magnitude = iterate.magnitude();
+          totalIterations++;
+          if (magnitude < 10.0 * REAL_MIN) totalIterations = max_it;
+        }
+        out[(size_t)z * res[0] * res[1] + (size_t)y * res[0] + x] = (double)log(magnitude);
+      }
+}
+
+// The unmodified OPTIMIZE_3D::computeLogScaledPowerRationalMap (escape 2000).
+void ref_field_map(const MapArgs* a, const int* res, const double* center, const double* lengths,
+                   double slice, int max_it, double* out) {
+  OPTIMIZE_3D opt(res[0], res[1], res[2], VEC3F(center[0], center[1], center[2]),
+                  VEC3F(lengths[0], lengths[1], lengths[2]));
+  opt.top() = make_poly(a->nt, a->troots, a->tpows, a->tsig);
+  opt.bottom() = make_poly(a->nb, a->broots, a->bpows, a->bsig);
+  opt.maxIterations() = max_it;
+  opt.expScaling() = a->s;
+  opt.slice() = slice;
+  opt.computeLogScaledPowerRationalMap(false);
+  FIELD_3D& f = opt.fractal();
+  for (int i = 0; i < f.totalCells(); i++) out[i] = (double)f[i];
+}
+
+// Streaming nonlinear marching cubes: TRIANGLE_MESH's 11-argument
+// constructor (TRIANGLE_MESH.cpp:84-101).
+int ref_mesh_stream(const MapArgs* a, const int* res, const double* center, const double* lengths,
+                    const double* rot, double slice, int max_it, double iso, double* verts,
+                    int max_v, int* tris, int max_t, int* nv, int* nt) {
+  char path[] = "/tmp/qjref_edgecacheXXXXXX";
+  int fd = mkstemp(path);
+  if (fd < 0) return -2;
+  close(fd);
+  unlink(path);  // the constructor must not find a cache
+  int rc;
+  {
+    TRIANGLE_MESH mesh(VEC3F(center[0], center[1], center[2]),
+                       VEC3F(lengths[0], lengths[1], lengths[2]), VEC3I(res[0], res[1], res[2]),
+                       make_poly(a->nt, a->troots, a->tpows, a->tsig),
+                       make_poly(a->nb, a->broots, a->bpows, a->bsig), a->s, max_it, slice, iso,
+                       QUATERNION(rot[0], rot[1], rot[2], rot[3]), std::string(path));
+    rc = export_mesh(mesh, verts, max_v, tris, max_t, nv, nt);
+  }
+  unlink(path);
+  return rc;
+}
+
+// Nonlinear marching cubes on a stored field (TRIANGLE_MESH.cpp:62-76).
+int ref_mesh_field_nonlinear(const MapArgs* a, const int* res, const double* center,
+                             const double* lengths, const double* field, double slice, int max_it,
+                             double iso, double* verts, int max_v, int* tris, int max_t, int* nv,
+                             int* nt) {
+  FIELD_3D f(res[0], res[1], res[2], VEC3F(center[0], center[1], center[2]),
+             VEC3F(lengths[0], lengths[1], lengths[2]));
+  for (int i = 0; i < f.totalCells(); i++) f[i] = field[i];
+  TRIANGLE_MESH mesh(f, make_poly(a->nt, a->troots, a->tpows, a->tsig),
+                     make_poly(a->nb, a->broots, a->bpows, a->bsig), a->s, max_it, slice, iso);
+  return export_mesh(mesh, verts, max_v, tris, max_t, nv, nt);
+}
+
+// Linear marching cubes on a stored field (TRIANGLE_MESH.cpp:48-57).
+int ref_mesh_linear(const int* res, const double* center, const double* lengths,
+                    const double* field, double* verts, int max_v, int* tris, int max_t, int* nv,
+                    int* nt) {
+  FIELD_3D f(res[0], res[1], res[2], VEC3F(center[0], center[1], center[2]),
+             VEC3F(lengths[0], lengths[1], lengths[2]));
+  for (int i = 0; i < f.totalCells(); i++) f[i] = field[i];
+  TRIANGLE_MESH mesh(f);
+  return export_mesh(mesh, verts, max_v, tris, max_t, nv, nt);
+}
+
+}  // extern "C"
