@@ -1,0 +1,184 @@
+/*
+ * quijibo_gpu.h -- C ABI of the GB300 implementation of QUIJIBO's hot path.
+ *
+ * The reference exposes this path as C++ class methods; each entry point
+ * below names the reference interface it replaces (paths inside the QUIJIBO
+ * project).  All entry points return QJG_OK (0) or a negative QJG_ERR_* code
+ * and never exit the process; qjg_last_error() describes the last failure on
+ * a context.  Device pointers are plain CUDA device addresses; `stream` is a
+ * cudaStream_t (NULL = the legacy default stream).  A context serves one host
+ * thread at a time: its scratch buffers are shared by its calls.
+ */
+#ifndef QUIJIBO_GPU_H
+#define QUIJIBO_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QJG_OK 0
+#define QJG_ERR_ARG (-1)      /* invalid argument (sizes, handles, null pointers) */
+#define QJG_ERR_CUDA (-2)     /* a CUDA call failed */
+#define QJG_ERR_NOMEM (-3)    /* device memory could not be allocated */
+#define QJG_ERR_HANDLE (-4)   /* unknown or freed root set */
+#define QJG_ERR_CAPACITY (-5) /* an output buffer is too small; the counts say how much is needed */
+
+#define QJG_MAX_ROOTS 128 /* top + bottom roots of one root set */
+
+/* Precision forms of the field. */
+#define QJG_FP64 0        /* plain form: FP64 with the reference's QUATERNION::pow per root term */
+#define QJG_FP32 1        /* FP32 only */
+#define QJG_FP32_REFINE 2 /* FP32 bulk, FP64 re-evaluation of the band |d| < band_h * h */
+
+/* How FP64 re-evaluation raises roots to powers. */
+#define QJG_REFINE_POW 0 /* the reference's polar QUATERNION::pow (reference rounding) */
+#define QJG_REFINE_INT 1 /* repeated products when every exponent is an integer */
+
+typedef struct qjg_ctx qjg_ctx;
+typedef int32_t qjg_rootset;
+
+/* Cell-centred grid = FIELD_3D geometry (src/geometry/FIELD_3D.h:55-120):
+ * res, center, lengths (spacing lengths/res), rotation quaternion (w,x,y,z)
+ * about center, and the 4D slice coordinate of every start point. */
+typedef struct {
+  int32_t res[3];
+  double center[3];
+  double lengths[3];
+  double rot[4];
+  double slice;
+} qjg_grid;
+
+/* Escape-time iteration settings. */
+typedef struct {
+  int32_t max_it;    /* OPTIMIZE_3D::_maxIterations */
+  int32_t precision; /* QJG_FP64 / QJG_FP32 / QJG_FP32_REFINE */
+  int32_t refine_pow;/* QJG_REFINE_POW / QJG_REFINE_INT */
+  int32_t want_de;   /* also produce the distance estimate |q| log|q| / |q'| */
+  double escape;     /* escape radius (the reference uses 2000) */
+  double band_h;     /* refine band half-width in voxel spacings (2.0 = |d| < 2h) */
+  double field_tol;  /* voxels with |log|q|| < field_tol are refined too */
+} qjg_iter;
+
+typedef struct {
+  int64_t voxels;        /* voxels computed */
+  int64_t voxel_iters;   /* executed map applications (bulk pass) */
+  int64_t root_terms;    /* voxel_iters x (n_top + n_bottom) */
+  int64_t refined;       /* voxels re-evaluated in FP64 */
+  int64_t refined_iters; /* map applications of the FP64 re-evaluation */
+  int64_t nonfinite;     /* FP32 voxels that overflowed or underflowed */
+} qjg_field_stats;
+
+/* ---- context and root sets ------------------------------------------- */
+
+int qjg_create(int device, qjg_ctx** out);
+void qjg_destroy(qjg_ctx* ctx);
+const char* qjg_last_error(qjg_ctx* ctx);
+
+/* Upload a rational map and keep it resident.  Replaces building the
+ * OPTIMIZE_3D top/bottom POLYNOMIAL_4D state (src/algebra/POLYNOMIAL_4D.cpp:40-60,
+ * POLYNOMIAL_4D.h:137-150) plus _expScaling.  roots are n x (w,x,y,z);
+ * effective exponents are sigma * powers[i]; n_top >= 1; n_bot may be 0. */
+int qjg_rootset_upload(qjg_ctx* ctx, int32_t n_top, const double* top_roots,
+                       const double* top_powers, double sigma_top, int32_t n_bot,
+                       const double* bot_roots, const double* bot_powers, double sigma_bot,
+                       double scale, qjg_rootset* out);
+int qjg_rootset_free(qjg_ctx* ctx, qjg_rootset rs);
+
+/* ---- field ------------------------------------------------------------ */
+
+/* Escape-time field log|q_N| of slices [z0, z1) into device memory:
+ * d_field[(z - z0) * X * Y + y * X + x]; d_de (optional, may be NULL) gets
+ * the distance estimate.  Replaces OPTIMIZE_3D::computeLogScaledPowerRationalMap
+ * (src/solvers/OPTIMIZE_3D.cpp:1272-1370, declared OPTIMIZE_3D.h:167) and
+ * TRIANGLE_MESH::computeNonlinearSlice (src/geometry/TRIANGLE_MESH.cpp:330-381). */
+int qjg_field(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter* iter,
+              int32_t z0, int32_t z1, double* d_field, float* d_de, void* stream);
+
+/* The same with host buffers: host_field receives the full X*Y*Z field
+ * (the FIELD_3D data array), host_de (optional) the distance estimate.
+ * Inputs and outputs cross PCIe/NVLink-C2C inside the call. */
+int qjg_field_host(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter* iter,
+                   double* host_field, float* host_de, qjg_field_stats* stats);
+
+/* Counters of the last qjg_field call on ctx; synchronizes `stream`. */
+int qjg_field_stats_read(qjg_ctx* ctx, void* stream, qjg_field_stats* out);
+
+/* ---- marching cubes ---------------------------------------------------- */
+
+/* Edge-vertex placement. */
+#define QJG_EDGE_LINEAR 0 /* p0 + d0/(d0-d1) (p1-p0) from stored values */
+#define QJG_EDGE_BISECT 1 /* bisection of the map, <= 6 levels, FP64 */
+
+typedef struct {
+  int64_t n_verts;       /* vertices (written, or needed when a capacity is short) */
+  int64_t n_tris;        /* triangles after the degenerate filter (or needed before it) */
+  int64_t n_degenerate;  /* triangles dropped by the degenerate filter (edge < 1e-7) */
+  int64_t n_unbracketed; /* edges whose end values do not bracket zero (the reference exits) */
+  int64_t map_evals;     /* FP64 map evaluations of the edge bisection */
+  int64_t slabs;         /* z-slabs processed */
+  qjg_field_stats field; /* the field pass of qjg_mesh_stream */
+} qjg_mesh_stats;
+
+/* Marching cubes on a stored device field (X*Y*Z doubles).  Corners are
+ * inside when the stored value is > 0.  edge_mode QJG_EDGE_LINEAR replaces
+ * TRIANGLE_MESH(const FIELD_3D&) / computeStagedMarchingCubes
+ * (src/geometry/TRIANGLE_MESH.cpp:48-57, 989-1114); QJG_EDGE_BISECT replaces
+ * TRIANGLE_MESH(field, top, bottom, expScaling, maxIterations, slice, iso)
+ * / computeNonlinearMarchingCubes (TRIANGLE_MESH.cpp:62-76, 152-275), whose
+ * bisection evaluates the map (rs, iter: max_it, escape, refine_pow) minus iso.
+ * Outputs in device memory: vertices as 3 doubles (d_verts64) and/or 3
+ * floats (d_verts32), triangles as 3 int32 vertex indices; vertex order and
+ * triangle order are the reference's.  slab_nz cube layers per pass (<= 0: 64).
+ * Returns QJG_ERR_CAPACITY, with the needed counts in *stats, when vert_cap
+ * or tri_cap is too small.  Synchronizes `stream`. */
+int qjg_mesh_field(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter* iter,
+                   const double* d_field, int32_t edge_mode, double iso, int32_t slab_nz,
+                   double* d_verts64, float* d_verts32, int64_t vert_cap, int32_t* d_tris,
+                   int64_t tri_cap, qjg_mesh_stats* stats, void* stream);
+
+/* Streaming marching cubes: the field (iter->precision) is computed slab by
+ * slab, corners are classified by log|q| > 0, and vertices are placed by
+ * FP64 bisection of log|q| - iso.  Replaces the two-slab streaming
+ * TRIANGLE_MESH(center, lengths, res, top, bottom, expScaling, maxIterations,
+ * slice, isosurface, rotation, cacheFile) constructor /
+ * computeNonlinearMarchingCubesLowMemoryHuge (TRIANGLE_MESH.cpp:84-101,
+ * 681-768).  Outputs and capacities as qjg_mesh_field. */
+int qjg_mesh_stream(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter* iter,
+                    double iso, int32_t slab_nz, double* d_verts64, float* d_verts32,
+                    int64_t vert_cap, int32_t* d_tris, int64_t tri_cap, qjg_mesh_stats* stats,
+                    void* stream);
+
+/* ---- fitting energy and gradients ------------------------------------- */
+
+typedef struct {
+  int64_t voxels;
+  int64_t overflowed;  /* voxels whose map overflowed; the reference recomputes them
+                          in long double, here their gradient terms are left out */
+  int64_t bad_terms;   /* NaN/inf gradient terms left out (the reference's _nans/_infs) */
+} qjg_tanh_stats;
+
+/* Tanh-weighted fitting score of the map on a grid and its analytic
+ * one-application gradients, in one pass.  Replaces OPTIMIZE_3D::computeScoreAP
+ * (src/solvers/OPTIMIZE_3D.cpp:3563-3569: computeRationalMapAP + weightScore),
+ * computeExpGradientAP (:3589-3625), computeBottomGradientAP (:10012-10218),
+ * computeTopGradientAP (:8905-9106) and compute{Top,Bottom}BulkScalarGradientAP
+ * (:9250-9478, :10360-10602).  grad (host, 3 + n_bottom + n_top entries) has
+ * the layout of toothOptimizer's FormScaledFunctionGradient
+ * (projects/toothOptimizer/toothOptimizer.cpp:65-109): [d/d log s,
+ * d/d bottom exponents, d/d top exponents, d/d sigma_top, d/d sigma_bottom].
+ * The weight field (d_weights, device, FIELD_3D layout on weight_grid) is
+ * looked up trilinearly at cell centres; alpha/threshold are _tanhAlpha and
+ * _tanhThreshold (10, 0 in the reference).  max_it as _maxIterations (the
+ * gradient is exact for max_it = 1, as toothOptimizer runs it).  d_field
+ * (optional, device) receives the map's log|q|.  Synchronizes `stream`. */
+int qjg_tanh_score_grad(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, int32_t max_it,
+                        const qjg_grid* weight_grid, const double* d_weights, double alpha,
+                        double threshold, double* score, double* grad, double* d_field,
+                        qjg_tanh_stats* stats, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,36 @@
+/*
+ * quijibo_gpu_bench.h -- measurement hooks of the GB300 library.  These have
+ * no counterpart in the reference: they expose per-kernel CUDA-event timings
+ * and launch counts so that a benchmark can attribute time to kernels, and an
+ * FP32 FMA-throughput probe used as the roofline denominator of the field
+ * kernel.
+ */
+#ifndef QUIJIBO_GPU_BENCH_H
+#define QUIJIBO_GPU_BENCH_H
+
+#include <stdint.h>
+
+#include "quijibo_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Record CUDA events around each kernel a context launches (off by default). */
+int qjg_set_timing(qjg_ctx* ctx, int on);
+
+/* Milliseconds of the bulk and FP64-refine kernels of the last field call
+ * (synchronizes with it); a kernel that did not run reports 0. */
+int qjg_last_timings(qjg_ctx* ctx, float* ms_bulk, float* ms_refine);
+
+/* Kernels this context has launched since it was created. */
+int64_t qjg_launch_count(qjg_ctx* ctx);
+
+/* FP32 FMA-pipe probe: runs a kernel of independent FMA chains on every SM
+ * of `device` and returns the achieved FP32 TFLOP/s (2 flops per FMA). */
+int qjg_fma_probe(int device, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

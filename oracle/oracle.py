@@ -90,6 +90,9 @@ class Oracle:
         L.qjo_trilinear.argtypes = [C.POINTER(_Grid), _dp, _dp]
         L.qjo_trilinear.restype = C.c_double
         L.qjo_cell_center.argtypes = [C.POINTER(_Grid), C.c_int, C.c_int, C.c_int, _dp]
+        L.qjo_tanh_score_grad.argtypes = [C.POINTER(_Map), C.POINTER(_Grid), C.POINTER(_Grid), _dp,
+                                          C.c_int, C.c_double, C.c_double, _dp, _dp]
+        L.qjo_tanh_score_grad.restype = C.c_double
         self.L = L
 
     def mt_rand(self, seed, n):
@@ -147,6 +150,16 @@ class Oracle:
         return {"verts": verts[:3 * nv.value].reshape(-1, 3).copy(),
                 "tris": tris[:3 * nt.value].reshape(-1, 3).copy(), "unbracketed": nu.value}
 
+    def tanh_score_grad(self, rootset, grid, wgrid, weights, max_it, alpha=10.0, threshold=0.0):
+        """Score, gradient [log s, bottom exps, top exps, sigma_t, sigma_b], field."""
+        w = np.ascontiguousarray(weights, dtype=np.float64).reshape(-1)
+        grad = np.empty(3 + rootset.n_top + rootset.n_bottom)
+        field = np.empty(grid.n_voxels)
+        sc = self.L.qjo_tanh_score_grad(C.byref(make_map(rootset)), C.byref(make_grid(grid)),
+                                        C.byref(make_grid(wgrid)), _ptr(w), max_it, alpha,
+                                        threshold, _ptr(grad), _ptr(field))
+        return sc, grad, field.reshape(grid.res[::-1])
+
     def trilinear(self, grid, data, p):
         data = np.ascontiguousarray(data, dtype=np.float64).reshape(-1)
         p = np.ascontiguousarray(p, dtype=np.float64)
@@ -189,6 +202,9 @@ class Reference:
         L.ref_mesh_field_nonlinear.argtypes = [A, _ip, _dp, _dp, _dp, C.c_double, C.c_int,
                                                C.c_double, _dp, C.c_int, _ip, C.c_int, _ip, _ip]
         L.ref_mesh_linear.argtypes = [_ip, _dp, _dp, _dp, _dp, C.c_int, _ip, C.c_int, _ip, _ip]
+        L.ref_tanh_score_grad.argtypes = [A, _ip, _dp, _dp, C.c_double, C.c_int, _ip, _dp, _dp,
+                                          _dp, _dp, _dp]
+        L.ref_tanh_score_grad.restype = C.c_double
         self.L = L
         self.sizeof_real = L.ref_sizeof_real()
 
@@ -251,3 +267,14 @@ class Reference:
         f = np.ascontiguousarray(field, dtype=np.float64).reshape(-1)
         return self._mesh_out(self.L.ref_mesh_linear, _ptr(res, _ip), _ptr(c), _ptr(l), _ptr(f),
                               n=f.size)
+
+    def tanh_score_grad(self, rs, grid, wgrid, weights, max_it):
+        res, c, l, _ = self._g(grid)
+        wres, wc, wl, _ = self._g(wgrid)
+        w = np.ascontiguousarray(weights, dtype=np.float64).reshape(-1)
+        grad = np.empty(3 + rs.n_top + rs.n_bottom)
+        field = np.empty(grid.n_voxels)
+        sc = self.L.ref_tanh_score_grad(C.byref(_map_args(rs)), _ptr(res, _ip), _ptr(c), _ptr(l),
+                                        grid.slice, max_it, _ptr(wres, _ip), _ptr(wc), _ptr(wl),
+                                        _ptr(w), _ptr(grad), _ptr(field))
+        return sc, grad, field.reshape(grid.res[::-1])

@@ -428,3 +428,231 @@ double qjo_trilinear(const qjo_grid* g, const double* data, const double p[3]) {
                s1 * (t0 * AT(x1, y0, z1) + t1 * AT(x1, y1, z1)));
 #undef AT
 }
+
+/* ------------------------------------------------------------------ */
+/* Tanh-weighted fitting score and its analytic gradients. */
+
+/* QUATERNION::log, QUATERNION.cpp:352-365. */
+static void qlog(const double q[4], double o[4]) {
+  const double qm = qmag(q);
+  const double vm = sqrt(q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  double vn[3] = {0, 0, 0};
+  if (vm > 0)
+    for (int c = 0; c < 3; c++) vn[c] = q[1 + c] / vm;
+  const double a = acos(q[0] / qm);
+  o[0] = log(qm);
+  for (int c = 0; c < 3; c++) o[1 + c] = vn[c] * a;
+}
+
+/* QUATERNION::inverse, QUATERNION.cpp:167-172. */
+static void qinv(const double q[4], double o[4]) {
+  const double m2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+  const double inv = 1.0 / m2;
+  o[0] = q[0] * inv;
+  o[1] = -q[1] * inv;
+  o[2] = -q[2] * inv;
+  o[3] = -q[3] * inv;
+}
+
+static double qdot(const double a[4], const double b[4]) {
+  return a[0] * b[0] + a[1] * b[1] + a[2] * b[2] + a[3] * b[3];
+}
+
+/* Per-voxel state of computeRationalMapAP (OPTIMIZE_3D.cpp:1374-1488) for
+ * the gradient passes: the field value, whether the voxel overflowed, and
+ * the factors P_i of the last iteration's products (evaluated at the last
+ * iterate, as the POLYNOMIAL_CACHE forward/backward vectors are). */
+typedef struct {
+  double field;
+  int overflowed, skipped;
+  double *P; /* (nt + nb) x 4 */
+} ap_voxel;
+
+static void ap_eval(const qjo_map* m, const double p[3], double slice, int max_it,
+                    ap_voxel* v) {
+  const int nt = m->top.n, nb = m->bottom.n;
+  double q[4] = {p[0], p[1], p[2], slice};
+  double mag = qmag(q);
+  v->overflowed = 0;
+  v->skipped = 0;
+  if (mag < 1e-8) { /* "if we hit the origin, move on" */
+    v->skipped = 1;
+    v->field = 0.0;
+    return;
+  }
+  int it = 0;
+  const double escape = 20.0;
+  /* the reference reads the last iteration's caches; a voxel that never
+   * iterates has none (its gradient terms are skipped here) */
+  if (!(mag < escape && it < max_it)) v->skipped = 1;
+  while (mag < escape && it < max_it) {
+    double T[4], B[4], d[4];
+    for (int side = 0; side < 2; side++) {
+      const qjo_poly* pl = side ? &m->bottom : &m->top;
+      double* acc = side ? B : T;
+      double* Pbase = v->P + 4 * (side ? nt : 0);
+      for (int i = 0; i < pl->n; i++) {
+        for (int c = 0; c < 4; c++) d[c] = q[c] - pl->roots[4 * i + c];
+        qjo_quat_pow(d, pl->power_scalar * pl->powers[i], Pbase + 4 * i);
+        if (i == 0) {
+          memcpy(acc, Pbase, 4 * sizeof(double));
+        } else {
+          double o[4];
+          qmul(acc, Pbase + 4 * i, o);
+          memcpy(acc, o, sizeof o);
+        }
+      }
+    }
+    if (nb > 0)
+      qdiv(T, B, q);
+    else
+      memcpy(q, T, sizeof T);
+    for (int c = 0; c < 4; c++) {
+      if (isinf(T[c]) || isnan(T[c]) || (nb > 0 && (isinf(B[c]) || isnan(B[c])))) v->overflowed = 1;
+      q[c] *= m->scale;
+    }
+    mag = qmag(q);
+    if (isinf(mag) || isnan(mag)) v->overflowed = 1;
+    it++;
+  }
+  v->field = log(mag);
+}
+
+double qjo_tanh_score_grad(const qjo_map* m, const qjo_grid* g, const qjo_grid* wg,
+                           const double* weights, int max_it, double alpha, double threshold,
+                           double* grad, double* field) {
+  const int nt = m->top.n, nb = m->bottom.n;
+  const int X = g->res[0], Y = g->res[1], Z = g->res[2];
+  const int64_t N = (int64_t)X * Y * Z;
+  const int P = 3 + nt + nb;
+  double* acc = (double*)calloc((size_t)P, sizeof(double));
+  double score = 0.0;
+  ap_voxel v;
+  v.P = (double*)malloc(sizeof(double) * 4 * (size_t)(nt + nb));
+  double* S = (double*)malloc(sizeof(double) * 4 * (size_t)(nt + nb)); /* suffix products */
+  const double logs = log(m->scale);
+  /* voxel order z, y, x (weightScore's linear order; the reference's
+   * gradient passes run y, z, x -- sums differ only by rounding) */
+  for (int64_t idx = 0; idx < N; idx++) {
+    const int x = (int)(idx % X), y = (int)((idx / X) % Y), z = (int)(idx / ((int64_t)X * Y));
+    double p[3];
+    qjo_cell_center(g, x, y, z, p);
+    ap_eval(m, p, g->slice, max_it, &v);
+    if (field) field[idx] = v.field;
+    const double w = qjo_trilinear(wg, weights, p);
+    /* weightScore, OPTIMIZE_3D.cpp:4502-4517 */
+    score += (-tanh(alpha * v.field)) * w;
+    /* computeExpGradientAP, OPTIMIZE_3D.cpp:3589-3625: every cell */
+    {
+      const double St = tanh(alpha * (v.field - threshold));
+      acc[0] += -alpha * w * ((double)1.0 - St * St);
+    }
+    if (v.overflowed || v.skipped) continue;
+    /* R and F from the last iteration's products */
+    double T[4], B[4] = {1, 0, 0, 0}, R[4];
+    for (int side = 0; side < 2; side++) {
+      const int lo = side ? nt : 0, n = side ? nb : nt;
+      if (n == 0) continue;
+      double* dst = side ? B : T;
+      memcpy(dst, v.P + 4 * lo, 4 * sizeof(double));
+      for (int i = 1; i < n; i++) {
+        double o[4];
+        qmul(dst, v.P + 4 * (lo + i), o);
+        memcpy(dst, o, sizeof o);
+      }
+      /* suffix products, POLYNOMIAL_4D.cpp:1066-1072 */
+      memcpy(S + 4 * (lo + n - 1), v.P + 4 * (lo + n - 1), 4 * sizeof(double));
+      for (int i = n - 2; i >= 0; i--) qmul(v.P + 4 * (lo + i), S + 4 * (lo + i + 1), S + 4 * (lo + i));
+    }
+    qdiv(T, B, R);
+    const double Rm = qmag(R);
+    if (Rm <= 0.0 || isinf(Rm)) continue;
+    const double F = log(Rm) + logs;
+    const double th = tanh(alpha * (F - threshold));
+    const double dSdF = -alpha * w * (1 - th * th);
+    const double RR = 1.0 / qdot(R, R);
+    const double q0[4] = {p[0], p[1], p[2], g->slice};
+    /* top roots: computeTopGradientAP (OPTIMIZE_3D.cpp:8905-9006) and the
+     * bulk sigma_top term computeTopBulkScalarGradientAP (:9250-9358) */
+    double left[4] = {1, 0, 0, 0};
+    double bulk_top = 0.0, bulk_bot = 0.0;
+    for (int i = 0; i < nt; i++) {
+      /* left = forward[i-1] (advanced below), right = backward[i+1] */
+      double right[4] = {1, 0, 0, 0};
+      if (nt > 1 && i < nt - 1) memcpy(right, S + 4 * (i + 1), sizeof right);
+      double base[4], pw[4], lg[4], mid[4], t1[4], dT[4], dR[4];
+      for (int c = 0; c < 4; c++) base[c] = q0[c] - m->top.roots[4 * i + c];
+      qjo_quat_pow(base, m->top.power_scalar * m->top.powers[i], pw);
+      qlog(base, lg);
+      for (int pass = 0; pass < 2; pass++) {
+        const double k = pass == 0 ? m->top.power_scalar : m->top.powers[i];
+        double kp[4] = {pw[0] * k, pw[1] * k, pw[2] * k, pw[3] * k};
+        qmul(kp, lg, mid);
+        qmul(left, mid, t1);
+        qmul(t1, right, dT);
+        qdiv(dT, B, dR);
+        const double dFdt = RR * qdot(R, dR);
+        const double dSdt = dSdF * dFdt;
+        if (isnan(dSdt) || isinf(dSdt)) continue;
+        if (pass == 0)
+          acc[1 + nb + i] += dSdt;
+        else
+          bulk_top += dSdt;
+      }
+      /* advance the prefix: forward[i] */
+      if (i == 0)
+        memcpy(left, v.P, sizeof left);
+      else {
+        double o[4];
+        qmul(left, v.P + 4 * i, o);
+        memcpy(left, o, sizeof o);
+      }
+    }
+    /* bottom roots: computeBottomGradientAP (:10012-10116) and
+     * computeBottomBulkScalarGradientAP (:10360-10470) */
+    double lb[4] = {1, 0, 0, 0};
+    for (int j = 0; j < nb; j++) {
+      double right[4] = {1, 0, 0, 0};
+      if (nb > 1 && j < nb - 1) memcpy(right, S + 4 * (nt + j + 1), sizeof right);
+      double base[4], pw[4], lg[4], li[4], mid[4], t0[4], t1[4], dB[4], dR[4];
+      for (int c = 0; c < 4; c++) base[c] = q0[c] - m->bottom.roots[4 * j + c];
+      qjo_quat_pow(base, m->bottom.power_scalar * m->bottom.powers[j], pw);
+      qlog(base, lg);
+      qinv(lg, li);
+      const double minus1[4] = {-1, 0, 0, 0};
+      for (int pass = 0; pass < 2; pass++) {
+        if (pass == 0 && !(m->bottom.power_scalar > 0.0)) continue;
+        if (pass == 1 && m->bottom.powers[j] < 1e-8) continue;
+        const double k = 1.0 / (pass == 0 ? m->bottom.power_scalar : m->bottom.powers[j]);
+        double kp[4] = {pw[0] * k, pw[1] * k, pw[2] * k, pw[3] * k};
+        qmul(kp, li, mid);
+        qmul(minus1, lb, t0);
+        qmul(t0, mid, t1);
+        qmul(t1, right, dB);
+        qdiv(T, dB, dR);
+        const double dFdt = RR * qdot(R, dR);
+        const double dSdt = dSdF * dFdt;
+        if (isnan(dSdt) || isinf(dSdt)) continue;
+        if (pass == 0)
+          acc[1 + j] += dSdt;
+        else
+          bulk_bot += dSdt;
+      }
+      if (j == 0)
+        memcpy(lb, v.P + 4 * nt, sizeof lb);
+      else {
+        double o[4];
+        qmul(lb, v.P + 4 * (nt + j), o);
+        memcpy(lb, o, sizeof o);
+      }
+    }
+    acc[1 + nb + nt] += bulk_top;
+    acc[2 + nb + nt] += bulk_bot;
+  }
+  for (int k = 0; k < P; k++) grad[k] = acc[k];
+  free(acc);
+  free(v.P);
+  free(S);
+  return score;
+}
+

@@ -174,4 +174,36 @@ int ref_mesh_linear(const int* res, const double* center, const double* lengths,
   return export_mesh(mesh, verts, max_v, tris, max_t, nv, nt);
 }
 
+// Tanh-weighted score and its analytic gradients through the reference's
+// OPTIMIZE_3D: computeScoreAP, computeExpGradientAP, computeBottomGradientAP,
+// computeTopGradientAP and the two bulk scalar gradients, in the gradient
+// layout of toothOptimizer's FormScaledFunctionGradient
+// (projects/toothOptimizer/toothOptimizer.cpp:65-109).
+double ref_tanh_score_grad(const MapArgs* a, const int* res, const double* center,
+                           const double* lengths, double slice, int max_it, const int* wres,
+                           const double* wcenter, const double* wlengths, const double* weights,
+                           double* grad, double* field) {
+  OPTIMIZE_3D opt(res[0], res[1], res[2], VEC3F(center[0], center[1], center[2]),
+                  VEC3F(lengths[0], lengths[1], lengths[2]));
+  opt.top() = make_poly(a->nt, a->troots, a->tpows, a->tsig);
+  opt.bottom() = make_poly(a->nb, a->broots, a->bpows, a->bsig);
+  opt.maxIterations() = max_it;
+  opt.expScaling() = a->s;
+  opt.slice() = slice;
+  FIELD_3D w(wres[0], wres[1], wres[2], VEC3F(wcenter[0], wcenter[1], wcenter[2]),
+             VEC3F(wlengths[0], wlengths[1], wlengths[2]));
+  for (int i = 0; i < w.totalCells(); i++) w[i] = weights[i];
+  opt.weightField() = w;
+  const double score = (double)opt.computeScoreAP();
+  int k = 0;
+  grad[k++] = (double)opt.computeExpGradientAP();
+  for (int i = 0; i < a->nb; i++) grad[k++] = (double)opt.computeBottomGradientAP(i);
+  for (int i = 0; i < a->nt; i++) grad[k++] = (double)opt.computeTopGradientAP(i);
+  grad[k++] = (double)opt.computeTopBulkScalarGradientAP();
+  grad[k++] = (double)opt.computeBottomBulkScalarGradientAP();
+  FIELD_3D& f = opt.fractal();
+  for (int i = 0; i < f.totalCells(); i++) field[i] = (double)f[i];
+  return score;
+}
+
 }  // extern "C"

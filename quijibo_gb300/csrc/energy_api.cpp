@@ -1,0 +1,64 @@
+// C ABI of the fitting energies and their gradients.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "qj_ctx.h"
+#include "qj_energy.h"
+
+extern "C" {
+
+int qjg_tanh_score_grad(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, int32_t max_it,
+                        const qjg_grid* weight_grid, const double* d_weights, double alpha,
+                        double threshold, double* score, double* grad, double* d_field,
+                        qjg_tanh_stats* stats, void* stream) {
+  if (!ctx) return QJG_ERR_ARG;
+  const qj::MapParams* m = qj_lookup(ctx, rs);
+  if (!m) return fail(ctx, QJG_ERR_HANDLE, "unknown root set %d", rs);
+  int rc;
+  if ((rc = qj_check_grid(ctx, grid)) || (rc = qj_check_grid(ctx, weight_grid))) return rc;
+  if (max_it < 0) return fail(ctx, QJG_ERR_ARG, "max_it = %d < 0", max_it);
+  if (!d_weights || !score || !grad) return fail(ctx, QJG_ERR_ARG, "NULL weights/score/grad");
+  cudaStream_t s = (cudaStream_t)stream;
+  QJ_CUDA(ctx, cudaSetDevice(ctx->device));
+  const qj::GridParams g = qj_grid_params(grid, 0, grid->res[2]);
+  qj::WeightGrid wg;
+  wg.X = weight_grid->res[0];
+  wg.Y = weight_grid->res[1];
+  wg.Z = weight_grid->res[2];
+  for (int c = 0; c < 3; c++) {
+    // FIELD_3D.cpp:971-980: corner = center - 0.5 lengths; corner += 0.5 dxs; 1/dx
+    const double dx = weight_grid->lengths[c] / weight_grid->res[c];
+    double corner = weight_grid->center[c] - weight_grid->lengths[c] * 0.5;
+    corner += dx * 0.5;
+    wg.corner[c] = corner;
+    wg.inv[c] = 1.0 / dx;
+  }
+  const int nblocks = qj::tanh_blocks();
+  const int slots = 6 + m->nt + m->nb;
+  double* d_part = nullptr;
+  QJ_CUDA(ctx, cudaMallocAsync((void**)&d_part, sizeof(double) * ((size_t)nblocks + 1) * slots, s));
+  double* d_out = d_part + (size_t)nblocks * slots;
+  cudaError_t e = qj::launch_tanh_grad(*m, g, wg, d_weights, max_it, alpha, threshold, true,
+                                       d_field, d_part, nblocks, d_out, s);
+  std::vector<double> out(slots);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(out.data(), d_out, sizeof(double) * slots, cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(d_part, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return fail(ctx, QJG_ERR_CUDA, "tanh score: %s", cudaGetErrorString(e));
+  ctx->launches += 2;
+  const int nt = m->nt, nb = m->nb;
+  for (int k = 0; k < 3 + nt + nb; k++) grad[k] = out[k];
+  *score = out[3 + nt + nb];
+  if (stats) {
+    stats->voxels = (int64_t)grid->res[0] * grid->res[1] * grid->res[2];
+    stats->overflowed = (int64_t)out[4 + nt + nb];
+    stats->bad_terms = (int64_t)out[5 + nt + nb];
+  }
+  return QJG_OK;
+}
+
+}  // extern "C"

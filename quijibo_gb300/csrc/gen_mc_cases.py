@@ -79,7 +79,11 @@ def main(ref, out):
             ", ".join("%d omits edges %s" % (c, "/".join(map(str, es))) for c, es in omitted) or "none"),
         "#pragma once",
         "#define QJ_MC_MAX_TRIS 5",
-        "static const unsigned char QJ_MC_CASES[256][16] = {",
+        "// CUDA code defines QJ_MC_STORAGE as __constant__ storage before including",
+        "#ifndef QJ_MC_STORAGE",
+        "#define QJ_MC_STORAGE static const",
+        "#endif",
+        "QJ_MC_STORAGE unsigned char QJ_MC_CASES[256][16] = {",
     ]
     for case in range(256):
         flat = [e for tri in tab[case] for e in tri]
@@ -87,7 +91,7 @@ def main(ref, out):
         lines.append("  {" + ",".join(str(v) for v in flat) + "},  // %d" % case)
     lines.append("};")
     lines.append("// bit (e-1) set when case c places a vertex on edge e")
-    lines.append("static const unsigned short QJ_MC_EDGEMASK[256] = {")
+    lines.append("QJ_MC_STORAGE unsigned short QJ_MC_EDGEMASK[256] = {")
     masks = []
     for case in range(256):
         m = 0

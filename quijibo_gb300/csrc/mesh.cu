@@ -1,0 +1,517 @@
+// Marching cubes as a classify / scan-compact / emit pipeline over z-slabs.
+//
+// Reference: TRIANGLE_MESH's three mesher families
+//   computeNonlinearMarchingCubesLowMemoryHuge (TRIANGLE_MESH.cpp:681-768,
+//     slices from computeAllLowMemorySlicesHuge :4884-4948),
+//   computeNonlinearMarchingCubes (:152-275) and
+//   computeStagedMarchingCubes (:989-1114).
+// All three classify a cube by the signs (> 0) of its eight corner values,
+// place one vertex on every edge that some cube's case uses, number the
+// vertices in ascending (z, y, x, axis) order of the edge's lower endpoint
+// (the iteration order of the reference's std::map of (VEC3I, VEC3I) or
+// (int, int) edge keys), emit each cube's triangles in scan order, and drop
+// triangles with an edge shorter than 1e-7.  Vertices come from linear
+// interpolation of stored values (computeEdgeInterpolations :2373-2425) or
+// from the bisection of TRIANGLE_MESH::midpointSearch (:2232-2271) on the map.
+//
+// Slab window (cube layers [c0, c1) per slab; "window index" j <-> global
+// index c0 - 1 + j): flags of layers c0-1 .. c1-1, edge masks and vertex ids
+// of planes c0-1 .. c1 (plane/layer c0-1 is carried over from the previous
+// slab).  Each slab numbers the vertices of planes [c0, c1) (the last slab
+// also plane Z-1) and emits the triangles of layers [c0-1, c1-1) (the last
+// slab also layer c1-1), whose vertices all have ids by then.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#define QJ_MC_STORAGE static __constant__
+#include "mc_cases.h"
+#include "qj_device.cuh"
+#include "qj_mesh.h"
+
+namespace qj {
+
+namespace {
+
+constexpr int SCAN_T = 256;              // threads per scan block
+constexpr int SCAN_V = 8;                // items per thread
+constexpr int SCAN_B = SCAN_T * SCAN_V;  // items per scan block
+
+// Edge id (1..12) -> lower-endpoint corner offset and axis (0=x, 1=y, 2=z),
+// TRIANGLE_MESH::getVertexTriplets, TRIANGLE_MESH.cpp:1569-1665.
+__constant__ signed char c_edge_off[13][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 1}, {0, 1, 0},
+                                              {1, 0, 0}, {1, 0, 0}, {1, 0, 1}, {1, 1, 0}, {0, 1, 0},
+                                              {0, 0, 0}, {0, 0, 1}, {0, 1, 1}};
+__constant__ signed char c_edge_axis[13] = {0, 1, 2, 1, 2, 1, 2, 1, 2, 0, 0, 0, 0};
+
+__device__ __forceinline__ int ntri_of(int flag) {
+  int n = 0;
+#pragma unroll
+  for (int t = 0; t < QJ_MC_MAX_TRIS; t++) n += QJ_MC_CASES[flag][3 * t] != 0;
+  return n;
+}
+
+// Exclusive scan across a block of SCAN_T threads; returns the thread's
+// exclusive prefix and writes the block total to *total.
+__device__ __forceinline__ long long block_exclusive_scan(long long v, long long* total) {
+  __shared__ long long warp_sums[SCAN_T / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  long long inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long n = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += n;
+  }
+  if (lane == 31) warp_sums[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    long long w = lane < SCAN_T / 32 ? warp_sums[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long n = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += n;
+    }
+    if (lane < SCAN_T / 32) warp_sums[lane] = w;  // inclusive warp prefix
+  }
+  __syncthreads();
+  const long long warp_base = warp ? warp_sums[warp - 1] : 0;
+  *total = warp_sums[SCAN_T / 32 - 1];
+  __syncthreads();
+  return warp_base + inc - v;
+}
+
+// Generic pass 1: per-block sums of op.count(i) over items [0, n).
+template <class Op>
+__global__ void __launch_bounds__(SCAN_T) count_kernel(Op op, long long n, long long* bsum) {
+  const long long base = (long long)blockIdx.x * SCAN_B + (long long)threadIdx.x * SCAN_V;
+  long long c = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_V; k++)
+    if (base + k < n) c += op.count(base + k);
+  long long total;
+  block_exclusive_scan(c, &total);
+  if (threadIdx.x == 0) bsum[blockIdx.x] = total;
+}
+
+// Pass 2: exclusive scan of the nb block sums in place; bsum[nb] = total.
+__global__ void __launch_bounds__(1024) scan_bsum_kernel(long long* bsum, long long nb) {
+  __shared__ long long sh[32];
+  __shared__ long long carry_sh;
+  if (threadIdx.x == 0) carry_sh = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (long long c0 = 0; c0 < nb; c0 += 1024) {
+    const long long i = c0 + threadIdx.x;
+    const long long v = i < nb ? bsum[i] : 0;
+    long long inc = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long t = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += t;
+    }
+    if (lane == 31) sh[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+      long long w = sh[lane];
+      for (int o = 1; o < 32; o <<= 1) {
+        const long long t = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += t;
+      }
+      sh[lane] = w;
+    }
+    __syncthreads();
+    const long long carry = carry_sh;
+    const long long excl = carry + (warp ? sh[warp - 1] : 0) + inc - v;
+    if (i < nb) bsum[i] = excl;
+    __syncthreads();
+    if (threadIdx.x == 0) carry_sh = carry + sh[31];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) bsum[nb] = carry_sh;
+}
+
+// Generic pass 3: op.emit(i, k) with k = running + exclusive prefix of
+// op.count over items [0, n).
+template <class Op>
+__global__ void __launch_bounds__(SCAN_T) emit_kernel(Op op, long long n, const long long* bsum,
+                                                      long long running) {
+  const long long base = (long long)blockIdx.x * SCAN_B + (long long)threadIdx.x * SCAN_V;
+  int c[SCAN_V];
+  long long s = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_V; k++) {
+    c[k] = base + k < n ? op.count(base + k) : 0;
+    s += c[k];
+  }
+  long long total;
+  long long k0 = running + bsum[blockIdx.x] + block_exclusive_scan(s, &total);
+#pragma unroll
+  for (int k = 0; k < SCAN_V; k++) {
+    if (c[k]) op.emit(base + k, k0);
+    k0 += c[k];
+  }
+}
+
+// ------------------------------------------------------------ classify
+
+// flags[l * XY + y * X + x] for layers l of `src` planes l and l+1.
+__global__ void flags_kernel(const double* __restrict__ src, int X, int Y, long long n_layers,
+                             uint8_t* __restrict__ flags) {
+  const long long XY = (long long)X * Y;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_layers * XY;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % X);
+    const int y = (int)((i / X) % Y);
+    int f = 0;
+    if (x < X - 1 && y < Y - 1) {
+      const double* v = src + i;
+      // corner weights NNN=1 NNP=2 NPN=4 NPP=8 PNN=16 PNP=32 PPN=64 PPP=128
+      // (TRIANGLE_MESH.cpp:4929-4931; letters x, y, z)
+      f = (v[0] > 0) | ((v[XY] > 0) << 1) | ((v[X] > 0) << 2) | ((v[X + XY] > 0) << 3) |
+          ((v[1] > 0) << 4) | ((v[1 + XY] > 0) << 5) | ((v[1 + X] > 0) << 6) |
+          ((v[1 + X + XY] > 0) << 7);
+    }
+    flags[i] = (uint8_t)f;
+  }
+}
+
+// Edge masks of window planes [j0, j0 + n/XY): bit a set when the edge from
+// the voxel along axis a carries a vertex.  Flags window layer j-1 and j are
+// the cube layers below and above plane j; layers outside [lay_lo, lay_hi)
+// do not exist.
+struct MaskCount {
+  const uint8_t* flags;
+  uint8_t* masks;
+  int X, Y;
+  int j0, lay_lo, lay_hi;
+  __device__ int flag(int j, int x, int y) const {
+    if (j < lay_lo || j >= lay_hi || x < 0 || y < 0 || x > X - 2 || y > Y - 2) return 0;
+    return flags[((long long)j * Y + y) * X + x];
+  }
+  __device__ int count(long long i) const {
+    const long long XY = (long long)X * Y;
+    const int j = j0 + (int)(i / XY);
+    const int r = (int)(i % XY);
+    const int x = r % X, y = r / X;
+    // x-edge: edges 10 (cube x,y,j), 9 (x,y-1,j), 11 (x,y,j-1), 12 (x,y-1,j-1)
+    const bool ex = (QJ_MC_EDGEMASK[flag(j, x, y)] >> 9 & 1) |
+                    (QJ_MC_EDGEMASK[flag(j, x, y - 1)] >> 8 & 1) |
+                    (QJ_MC_EDGEMASK[flag(j - 1, x, y)] >> 10 & 1) |
+                    (QJ_MC_EDGEMASK[flag(j - 1, x, y - 1)] >> 11 & 1);
+    // y-edge: edges 1 (x,y,j), 5 (x-1,y,j), 3 (x,y,j-1), 7 (x-1,y,j-1)
+    const bool ey = (QJ_MC_EDGEMASK[flag(j, x, y)] >> 0 & 1) |
+                    (QJ_MC_EDGEMASK[flag(j, x - 1, y)] >> 4 & 1) |
+                    (QJ_MC_EDGEMASK[flag(j - 1, x, y)] >> 2 & 1) |
+                    (QJ_MC_EDGEMASK[flag(j - 1, x - 1, y)] >> 6 & 1);
+    // z-edge: edges 2 (x,y,j), 6 (x-1,y,j), 4 (x,y-1,j), 8 (x-1,y-1,j)
+    const bool ez = (QJ_MC_EDGEMASK[flag(j, x, y)] >> 1 & 1) |
+                    (QJ_MC_EDGEMASK[flag(j, x - 1, y)] >> 5 & 1) |
+                    (QJ_MC_EDGEMASK[flag(j, x, y - 1)] >> 3 & 1) |
+                    (QJ_MC_EDGEMASK[flag(j, x - 1, y - 1)] >> 7 & 1);
+    const int m = (int)ex | ((int)ey << 1) | ((int)ez << 2);
+    masks[(long long)j0 * XY + i] = (uint8_t)m;
+    return __popc(m);
+  }
+};
+
+// Vertex ids (global) of window planes [j0, ...) and the list of their edges
+// (window voxel index * 4 + axis) in id order.
+struct VertexEmit {
+  const uint8_t* masks;
+  int32_t* vbase;
+  uint32_t* list;
+  long long list_base;  // global id of list[0]
+  long long XY;
+  int j0;
+  __device__ int count(long long i) const { return __popc(masks[j0 * XY + i]); }
+  __device__ void emit(long long i, long long k) const {
+    const long long w = j0 * XY + i;
+    const int m = masks[w];
+    vbase[w] = (int32_t)k;
+    long long o = k - list_base;
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+      if (m >> a & 1) list[o++] = (uint32_t)(w * 4 + a);
+  }
+};
+
+struct TriCount {
+  const uint8_t* flags;
+  long long XY;
+  int j0;
+  __device__ int count(long long i) const { return ntri_of(flags[j0 * XY + i]); }
+};
+
+struct TriEmit {
+  const uint8_t* flags;
+  const uint8_t* masks;
+  const int32_t* vbase;
+  int32_t* tris;
+  long long cap;
+  int X;
+  long long XY;
+  int j0;
+  __device__ int count(long long i) const { return ntri_of(flags[j0 * XY + i]); }
+  __device__ void emit(long long i, long long k) const {
+    const long long w = j0 * XY + i;
+    const int f = flags[w];
+    const int r = (int)(i % XY);
+    const int x = r % X, y = r / X, j = j0 + (int)(i / XY);
+    for (int t = 0; t < QJ_MC_MAX_TRIS && QJ_MC_CASES[f][3 * t]; t++, k++) {
+      if (k >= cap) continue;
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const int e = QJ_MC_CASES[f][3 * t + c];
+        const long long v = ((long long)(j + c_edge_off[e][2]) * XY) +
+                            (long long)(y + c_edge_off[e][1]) * X + (x + c_edge_off[e][0]);
+        const int a = c_edge_axis[e];
+        tris[3 * k + c] = vbase[v] + __popc(masks[v] & ((1 << a) - 1));
+      }
+    }
+  }
+};
+
+// Degenerate-triangle filter of TRIANGLE_MESH.cpp:737-756 (edge < 1e-7).
+__device__ __forceinline__ double edge_len(const double* a, const double* b) {
+  using namespace q64;
+  const double d0 = sub(a[0], b[0]), d1 = sub(a[1], b[1]), d2 = sub(a[2], b[2]);
+  return __dsqrt_rn(add(add(mul(d0, d0), mul(d1, d1)), mul(d2, d2)));
+}
+
+struct DegenCount {
+  const int32_t* tris;
+  const double* v;
+  __device__ int count(long long t) const {
+    const double* a = v + 3ll * tris[3 * t];
+    const double* b = v + 3ll * tris[3 * t + 1];
+    const double* c = v + 3ll * tris[3 * t + 2];
+    const double eps = 1e-7;
+    return !(edge_len(a, b) < eps || edge_len(a, c) < eps || edge_len(b, c) < eps);
+  }
+};
+
+struct DegenEmit : DegenCount {
+  int32_t* out;
+  __device__ void emit(long long t, long long k) const {
+    out[3 * k] = tris[3 * t];
+    out[3 * k + 1] = tris[3 * t + 1];
+    out[3 * k + 2] = tris[3 * t + 2];
+  }
+};
+
+// ------------------------------------------------------------ vertices
+
+// One vertex per listed edge: linear interpolation of the stored values
+// (computeEdgeInterpolations) or the bisection of midpointSearch on the map.
+template <bool BISECT, bool POW_REF>
+__global__ void __launch_bounds__(128) vertex_kernel(const __grid_constant__ MapParams m,
+                                                     const GridParams g, const IterParams it,
+                                                     const uint32_t* __restrict__ list, long long n,
+                                                     long long id0, int c0,
+                                                     const double* __restrict__ src,
+                                                     double* __restrict__ verts, double iso,
+                                                     DevStats* st) {
+  const long long XY = (long long)g.X * g.Y;
+  unsigned long long evals = 0, unbracketed = 0;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+       k += (long long)gridDim.x * blockDim.x) {
+    const uint32_t e = list[k];
+    const int a = (int)(e & 3u);
+    const long long w = e >> 2;
+    const int z = c0 - 1 + (int)(w / XY);
+    const int r = (int)(w % XY);
+    const int x = r % g.X, y = r / g.X;
+    const int x1 = x + (a == 0), y1 = y + (a == 1), z1 = z + (a == 2);
+    double p0[3], p1[3], out[3];
+    cell_center(g, x, y, z, p0);
+    cell_center(g, x1, y1, z1, p1);
+    using namespace q64;
+    if (!BISECT) {
+      // TRIANGLE_MESH.cpp:2399-2410: p0 + (d0 / (d0 - d1)) * (p1 - p0)
+      const double d0 = src[(long long)(z - c0) * XY + r];
+      const double d1 = src[(long long)(z1 - c0) * XY + (long long)y1 * g.X + x1];
+      const double t = __ddiv_rn(d0, sub(d0, d1));
+#pragma unroll
+      for (int c = 0; c < 3; c++) out[c] = add(p0[c], mul(t, sub(p1[c], p0[c])));
+    } else {
+      int ni;
+      double dd;
+      // nonlinearValue at both ends (TRIANGLE_MESH.cpp:2060-2067)
+      const double f0 = sub(escape64<POW_REF, false>(m, it, p0, g.slice, &ni, &dd), iso);
+      const double f1 = sub(escape64<POW_REF, false>(m, it, p1, g.slice, &ni, &dd), iso);
+      evals += 2;
+      double pv[3], nv[3], pval = f0, nval = f1;
+      bool bad = mul(f0, f1) >= 0.0;
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        pv[c] = p0[c];
+        nv[c] = p1[c];
+      }
+      if (f0 < 0) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          pv[c] = p1[c];
+          nv[c] = p0[c];
+        }
+        pval = f1;
+        nval = f0;
+      }
+      // midpointSearch, TRIANGLE_MESH.cpp:2232-2271, as a loop
+      for (int rec = 0;; rec++) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) out[c] = mul(add(pv[c], nv[c]), 0.5);
+        if (mul(pval, nval) >= 0.0) {
+          bad = true;
+          break;
+        }
+        if (rec >= 6) break;
+        const double mv = sub(escape64<POW_REF, false>(m, it, out, g.slice, &ni, &dd), iso);
+        evals++;
+        if (fabs(mv) < 1e-8) break;
+        if (mv < 0) {
+#pragma unroll
+          for (int c = 0; c < 3; c++) nv[c] = out[c];
+          nval = mv;
+        } else {
+#pragma unroll
+          for (int c = 0; c < 3; c++) pv[c] = out[c];
+          pval = mv;
+        }
+      }
+      unbracketed += bad;
+    }
+    double* o = verts + 3 * (id0 + k);
+    o[0] = out[0];
+    o[1] = out[1];
+    o[2] = out[2];
+  }
+  if (BISECT) {
+    for (int o = 16; o; o >>= 1) {
+      evals += __shfl_xor_sync(0xffffffffu, evals, o);
+      unbracketed += __shfl_xor_sync(0xffffffffu, unbracketed, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      if (evals) atomicAdd(&st->aux[1], evals);
+      if (unbracketed) atomicAdd(&st->aux[2], unbracketed);
+    }
+  }
+}
+
+__global__ void to_float_kernel(const double* __restrict__ a, float* __restrict__ b, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+int sm_count() {
+  int dev = 0, n = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  return n;
+}
+
+}  // namespace
+
+long long mesh_scan_blocks(long long n) { return (n + SCAN_B - 1) / SCAN_B + 1; }
+
+cudaError_t mesh_flags(const double* src, int X, int Y, long long n_layers, uint8_t* flags,
+                       cudaStream_t s) {
+  if (n_layers <= 0) return cudaSuccess;
+  const long long n = n_layers * X * Y;
+  const int blocks = (int)std::min<long long>((n + 255) / 256, (long long)sm_count() * 16);
+  flags_kernel<<<blocks, 256, 0, s>>>(src, X, Y, n_layers, flags);
+  return cudaGetLastError();
+}
+
+cudaError_t mesh_vertex_ids(MeshWindow& w, int j0, int j1, int lay_lo, int lay_hi,
+                            long long running, long long* n_new, cudaStream_t s,
+                            const std::function<cudaError_t(long long)>& ensure_list) {
+  const long long XY = (long long)w.X * w.Y;
+  const long long n = (long long)(j1 - j0) * XY;
+  MaskCount mc{w.flags, w.masks, w.X, w.Y, j0, lay_lo, lay_hi};
+  // the emit pass needs the list buffer, which ensure_list sizes first
+  cudaError_t err = cudaSuccess;
+  const long long nb = (n + SCAN_B - 1) / SCAN_B;
+  if (n == 0) {
+    *n_new = 0;
+    return cudaSuccess;
+  }
+  count_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(mc, n, w.bsum);
+  scan_bsum_kernel<<<1, 1024, 0, s>>>(w.bsum, nb);
+  if ((err = cudaMemcpyAsync(n_new, w.bsum + nb, sizeof(long long), cudaMemcpyDeviceToHost, s)))
+    return err;
+  if ((err = cudaStreamSynchronize(s))) return err;
+  if ((err = ensure_list(*n_new))) return err;
+  VertexEmit ve{w.masks, w.vbase, w.list, running, XY, j0};
+  emit_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(ve, n, w.bsum, running);
+  return cudaGetLastError();
+}
+
+cudaError_t mesh_vertices(const MapParams& m, const GridParams& g, const IterParams& it,
+                          int edge_mode, bool pow_ref, const MeshWindow& w, long long n,
+                          long long id0, int c0, const double* src, double* verts, double iso,
+                          DevStats* st, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  const int blocks = (int)std::min<long long>((n + 127) / 128, (long long)sm_count() * 32);
+  if (edge_mode == 0)
+    vertex_kernel<false, false><<<blocks, 128, 0, s>>>(m, g, it, w.list, n, id0, c0, src, verts,
+                                                       iso, st);
+  else if (pow_ref)
+    vertex_kernel<true, true><<<blocks, 128, 0, s>>>(m, g, it, w.list, n, id0, c0, src, verts,
+                                                     iso, st);
+  else
+    vertex_kernel<true, false><<<blocks, 128, 0, s>>>(m, g, it, w.list, n, id0, c0, src, verts,
+                                                      iso, st);
+  return cudaGetLastError();
+}
+
+cudaError_t mesh_triangles(MeshWindow& w, int j0, int j1, long long running, int32_t* tris,
+                           long long cap, long long* n_new, cudaStream_t s) {
+  const long long XY = (long long)w.X * w.Y;
+  const long long n = (long long)(j1 - j0) * XY;
+  if (n <= 0) {
+    *n_new = 0;
+    return cudaSuccess;
+  }
+  const long long nb = (n + SCAN_B - 1) / SCAN_B;
+  TriCount tc{w.flags, XY, j0};
+  count_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(tc, n, w.bsum);
+  scan_bsum_kernel<<<1, 1024, 0, s>>>(w.bsum, nb);
+  cudaError_t err;
+  if ((err = cudaMemcpyAsync(n_new, w.bsum + nb, sizeof(long long), cudaMemcpyDeviceToHost, s)))
+    return err;
+  TriEmit te{w.flags, w.masks, w.vbase, tris, cap, w.X, XY, j0};
+  emit_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(te, n, w.bsum, running);
+  if ((err = cudaGetLastError())) return err;
+  return cudaStreamSynchronize(s);
+}
+
+cudaError_t mesh_filter(const int32_t* tris, long long n, const double* verts, int32_t* out,
+                        long long* bsum, long long* n_keep, cudaStream_t s) {
+  if (n == 0) {
+    *n_keep = 0;
+    return cudaSuccess;
+  }
+  const long long nb = (n + SCAN_B - 1) / SCAN_B;
+  DegenCount dc{tris, verts};
+  count_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(dc, n, bsum);
+  scan_bsum_kernel<<<1, 1024, 0, s>>>(bsum, nb);
+  DegenEmit de;
+  de.tris = tris;
+  de.v = verts;
+  de.out = out;
+  emit_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(de, n, bsum, 0);
+  cudaError_t err;
+  if ((err = cudaMemcpyAsync(n_keep, bsum + nb, sizeof(long long), cudaMemcpyDeviceToHost, s)))
+    return err;
+  return cudaStreamSynchronize(s);
+}
+
+cudaError_t mesh_to_float(const double* a, float* b, long long n, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  const int blocks = (int)std::min<long long>((n + 255) / 256, (long long)sm_count() * 16);
+  to_float_kernel<<<blocks, 256, 0, s>>>(a, b, n);
+  return cudaGetLastError();
+}
+
+}  // namespace qj

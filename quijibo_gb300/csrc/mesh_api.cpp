@@ -1,0 +1,224 @@
+// C ABI of the marching-cubes mesher: slab orchestration on the host.
+// The reference's two-slab streaming mesher keeps two FIELD_2D slices alive
+// (TRIANGLE_MESH.cpp:4884-4911); here a window of slab_nz cube layers is
+// classified, numbered and emitted per pass, with one layer/plane of flags,
+// edge masks and vertex ids carried to the next pass (see mesh.cu).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "qj_ctx.h"
+#include "qj_kernels.h"
+#include "qj_mesh.h"
+
+using qj::GridParams;
+using qj::IterParams;
+using qj::MapParams;
+
+namespace {
+
+// Grow a device buffer to hold n elements, keeping the first `keep`.
+template <class T>
+int grow_keep(qjg_ctx* ctx, T** buf, size_t* cap, size_t n, size_t keep, cudaStream_t s) {
+  if (*cap >= n && *buf) return QJG_OK;
+  size_t want = std::max(n, *cap + *cap / 2);
+  T* nb = nullptr;
+  QJ_CUDA(ctx, cudaMalloc((void**)&nb, want * sizeof(T)));
+  if (*buf && keep) QJ_CUDA(ctx, cudaMemcpyAsync(nb, *buf, keep * sizeof(T), cudaMemcpyDeviceToDevice, s));
+  QJ_CUDA(ctx, cudaStreamSynchronize(s));
+  if (*buf) cudaFree(*buf);
+  *buf = nb;
+  *cap = want;
+  return QJG_OK;
+}
+
+int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter* iter,
+              bool streaming, const double* d_field, int edge_mode, double iso, int slab_nz,
+              double* v64, float* v32, int64_t vcap, int32_t* tris, int64_t tcap,
+              qjg_mesh_stats* out, cudaStream_t s) {
+  int rc;
+  if ((rc = qj_check_grid(ctx, grid))) return rc;
+  if (edge_mode != QJG_EDGE_LINEAR && edge_mode != QJG_EDGE_BISECT)
+    return fail(ctx, QJG_ERR_ARG, "unknown edge_mode %d", edge_mode);
+  const bool bisect = edge_mode == QJG_EDGE_BISECT;
+  MapParams zero_map;
+  std::memset(&zero_map, 0, sizeof zero_map);
+  const MapParams* m = &zero_map;
+  if (bisect || streaming) {
+    m = qj_lookup(ctx, rs);
+    if (!m) return fail(ctx, QJG_ERR_HANDLE, "unknown root set %d", rs);
+    if ((rc = qj_check_iter(ctx, iter))) return rc;
+  }
+  if (!streaming && !d_field) return fail(ctx, QJG_ERR_ARG, "d_field is NULL");
+  if (!tris) return fail(ctx, QJG_ERR_ARG, "d_tris is NULL");
+  if (vcap < 0 || tcap < 0) return fail(ctx, QJG_ERR_ARG, "negative capacity");
+  qjg_mesh_stats st;
+  std::memset(&st, 0, sizeof st);
+
+  const int X = grid->res[0], Y = grid->res[1], Z = grid->res[2];
+  const long long XY = (long long)X * Y;
+  int nz = slab_nz > 0 ? slab_nz : 64;
+  // edge-list entries are window voxel index * 4 + axis in 32 bits
+  const long long nz_max = (long long)(UINT32_MAX / 4) / XY - 2;
+  if (nz_max < 1) return fail(ctx, QJG_ERR_ARG, "a %d x %d slice is too large", X, Y);
+  nz = (int)std::min<long long>(nz, nz_max);
+  nz = std::max(1, std::min(nz, std::max(Z - 1, 1)));
+  QJ_CUDA(ctx, cudaSetDevice(ctx->device));
+
+  const size_t wplanes = (size_t)(nz + 2) * XY;
+  if ((rc = ensure(ctx, &ctx->m_flags, &ctx->m_flags_cap, wplanes)) ||
+      (rc = ensure(ctx, &ctx->m_masks, &ctx->m_masks_cap, wplanes)) ||
+      (rc = ensure(ctx, &ctx->m_vbase, &ctx->m_vbase_cap, wplanes)) ||
+      (rc = ensure(ctx, &ctx->m_bsum, &ctx->m_bsum_cap, (size_t)qj::mesh_scan_blocks(wplanes))))
+    return rc;
+  if (streaming && (rc = ensure(ctx, &ctx->m_field, &ctx->m_field_cap, (size_t)(nz + 1) * XY)))
+    return rc;
+  QJ_CUDA(ctx, cudaMemsetAsync(ctx->m_flags, 0, XY, s));
+  QJ_CUDA(ctx, cudaMemsetAsync(ctx->m_masks, 0, XY, s));
+  QJ_CUDA(ctx, cudaMemsetAsync(ctx->m_vbase, 0, XY * sizeof(int32_t), s));
+  QJ_CUDA(ctx, cudaMemsetAsync(ctx->d_mstats, 0, sizeof(qj::DevStats), s));
+
+  qj::MeshWindow w;
+  w.X = X;
+  w.Y = Y;
+  w.flags = ctx->m_flags;
+  w.masks = ctx->m_masks;
+  w.vbase = ctx->m_vbase;
+  w.list = ctx->m_list;
+  w.bsum = ctx->m_bsum;
+  const GridParams g = qj_grid_params(grid, 0, Z);
+  IterParams it{};
+  if (iter) it = qj_iter_params(iter, grid);
+  const bool pow_ref = !iter || iter->refine_pow == QJG_REFINE_POW || !m->all_int;
+
+  long long nv = 0, nt = 0;
+  int prevL = 0;
+  for (int c0 = 0; c0 < Z - 1;) {
+    const int c1 = std::min(c0 + nz, Z - 1);
+    const bool last = c1 == Z - 1;
+    const int L = c1 - c0;
+    // field planes [c0, c1]
+    const double* src;
+    if (streaming) {
+      qjg_field_stats fs;
+      if (c0 == 0) {
+        if ((rc = qjg_field(ctx, rs, grid, iter, 0, c1 + 1, ctx->m_field, nullptr, s))) return rc;
+      } else {
+        QJ_CUDA(ctx, cudaMemcpyAsync(ctx->m_field, ctx->m_field + (size_t)prevL * XY,
+                                     XY * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        if ((rc = qjg_field(ctx, rs, grid, iter, c0 + 1, c1 + 1, ctx->m_field + XY, nullptr, s)))
+          return rc;
+      }
+      if ((rc = qjg_field_stats_read(ctx, s, &fs))) return rc;
+      st.field.voxels += fs.voxels;
+      st.field.voxel_iters += fs.voxel_iters;
+      st.field.root_terms += fs.root_terms;
+      st.field.refined += fs.refined;
+      st.field.refined_iters += fs.refined_iters;
+      st.field.nonfinite += fs.nonfinite;
+      src = ctx->m_field;
+    } else {
+      src = d_field + (size_t)c0 * XY;
+    }
+    // carry layer/plane c0-1 into window index 0
+    if (c0 > 0) {
+      QJ_CUDA(ctx, cudaMemcpyAsync(ctx->m_flags, ctx->m_flags + (size_t)prevL * XY, XY,
+                                   cudaMemcpyDeviceToDevice, s));
+      QJ_CUDA(ctx, cudaMemcpyAsync(ctx->m_masks, ctx->m_masks + (size_t)prevL * XY, XY,
+                                   cudaMemcpyDeviceToDevice, s));
+      QJ_CUDA(ctx, cudaMemcpyAsync(ctx->m_vbase, ctx->m_vbase + (size_t)prevL * XY,
+                                   XY * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+    }
+    // classify cube layers [c0, c1) into window layers 1..L
+    QJ_CUDA(ctx, qj::mesh_flags(src, X, Y, L, ctx->m_flags + XY, s));
+    ctx->launches++;
+    // vertex ids of planes [c0, c1) (+ Z-1 on the last slab) = window planes [1, j1)
+    const int j1 = L + 1 + (last ? 1 : 0);
+    long long n_new = 0;
+    auto ensure_list = [&](long long n) -> cudaError_t {
+      if (ensure(ctx, &ctx->m_list, &ctx->m_list_cap, (size_t)std::max<long long>(n, 1)))
+        return cudaErrorMemoryAllocation;
+      w.list = ctx->m_list;
+      return cudaSuccess;
+    };
+    QJ_CUDA(ctx, qj::mesh_vertex_ids(w, 1, j1, c0 == 0 ? 1 : 0, L + 1, nv, &n_new, s, ensure_list));
+    ctx->launches += 3;
+    if (nv + n_new > INT32_MAX)
+      return fail(ctx, QJG_ERR_CAPACITY, "more than 2^31 vertices; int32 indices cannot hold them");
+    if ((rc = grow_keep(ctx, &ctx->m_verts, &ctx->m_verts_cap, (size_t)(nv + n_new) * 3,
+                        (size_t)nv * 3, s)))
+      return rc;
+    QJ_CUDA(ctx, qj::mesh_vertices(*m, g, it, edge_mode, pow_ref, w, n_new, nv, c0, src,
+                                   ctx->m_verts, iso, ctx->d_mstats, s));
+    if (n_new) ctx->launches++;
+    nv += n_new;
+    // triangles of layers [c0-1, c1-1) (+ c1-1 on the last slab)
+    const int jt0 = c0 == 0 ? 1 : 0, jt1 = last ? L + 1 : L;
+    long long t_new = 0;
+    QJ_CUDA(ctx, qj::mesh_triangles(w, jt0, jt1, nt, tris, tcap, &t_new, s));
+    ctx->launches += 3;
+    nt += t_new;
+    prevL = L;
+    st.slabs++;
+    c0 = c1;
+  }
+
+  st.n_verts = nv;
+  st.n_tris = nt;
+  qj::DevStats ds;
+  QJ_CUDA(ctx, cudaMemcpyAsync(&ds, ctx->d_mstats, sizeof ds, cudaMemcpyDeviceToHost, s));
+  QJ_CUDA(ctx, cudaStreamSynchronize(s));
+  st.map_evals = (int64_t)ds.aux[1];
+  st.n_unbracketed = (int64_t)ds.aux[2];
+  if (nt > tcap || ((v64 || v32) && nv > vcap)) {
+    if (out) *out = st;
+    return fail(ctx, QJG_ERR_CAPACITY, "mesh needs %lld vertices / %lld triangles (capacity %lld / %lld)",
+                nv, nt, (long long)vcap, (long long)tcap);
+  }
+  // degenerate filter (needs every vertex, so it runs after the last slab)
+  if ((rc = ensure(ctx, &ctx->m_tris, &ctx->m_tris_cap, (size_t)std::max<long long>(nt * 3, 1))) ||
+      (rc = ensure(ctx, &ctx->m_bsum, &ctx->m_bsum_cap, (size_t)qj::mesh_scan_blocks(nt))))
+    return rc;
+  long long keep = 0;
+  QJ_CUDA(ctx, qj::mesh_filter(tris, nt, ctx->m_verts, ctx->m_tris, ctx->m_bsum, &keep, s));
+  if (nt) ctx->launches += 3;
+  QJ_CUDA(ctx, cudaMemcpyAsync(tris, ctx->m_tris, (size_t)keep * 3 * sizeof(int32_t),
+                               cudaMemcpyDeviceToDevice, s));
+  st.n_degenerate = nt - keep;
+  st.n_tris = keep;
+  if (v64)
+    QJ_CUDA(ctx, cudaMemcpyAsync(v64, ctx->m_verts, (size_t)nv * 3 * sizeof(double),
+                                 cudaMemcpyDeviceToDevice, s));
+  if (v32) {
+    QJ_CUDA(ctx, qj::mesh_to_float(ctx->m_verts, v32, nv * 3, s));
+    if (nv) ctx->launches++;
+  }
+  QJ_CUDA(ctx, cudaStreamSynchronize(s));
+  if (out) *out = st;
+  return QJG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qjg_mesh_field(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter* iter,
+                   const double* d_field, int32_t edge_mode, double iso, int32_t slab_nz,
+                   double* d_verts64, float* d_verts32, int64_t vert_cap, int32_t* d_tris,
+                   int64_t tri_cap, qjg_mesh_stats* stats, void* stream) {
+  if (!ctx) return QJG_ERR_ARG;
+  return mesh_core(ctx, rs, grid, iter, false, d_field, edge_mode, iso, slab_nz, d_verts64,
+                   d_verts32, vert_cap, d_tris, tri_cap, stats, (cudaStream_t)stream);
+}
+
+int qjg_mesh_stream(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter* iter,
+                    double iso, int32_t slab_nz, double* d_verts64, float* d_verts32,
+                    int64_t vert_cap, int32_t* d_tris, int64_t tri_cap, qjg_mesh_stats* stats,
+                    void* stream) {
+  if (!ctx) return QJG_ERR_ARG;
+  return mesh_core(ctx, rs, grid, iter, true, nullptr, QJG_EDGE_BISECT, iso, slab_nz, d_verts64,
+                   d_verts32, vert_cap, d_tris, tri_cap, stats, (cudaStream_t)stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,92 @@
+// Internal context of the C ABI, shared by the host translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/quijibo_gpu.h"
+#include "qj_mesh.h"
+#include "qj_params.h"
+
+struct qjg_ctx {
+  int device = 0;
+  std::string err;
+  std::vector<std::unique_ptr<qj::MapParams>> rootsets;
+  qj::DevStats* d_stats = nullptr;  // counters of the current call
+  uint32_t* d_list = nullptr;   // FP64 refine list
+  size_t list_cap = 0;
+  double* d_field = nullptr;    // staging for host-buffer calls
+  float* d_de = nullptr;
+  size_t buf_cap = 0;
+  cudaStream_t stream = nullptr;  // internal stream of host-buffer calls
+  // bookkeeping of the last field call, for qjg_field_stats_read
+  int64_t last_voxels = 0;
+  int last_roots = 0;
+  // measurement hooks
+  bool timing = false;
+  bool timed_refine = false;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  int64_t launches = 0;
+  // marching-cubes scratch
+  qj::DevStats* d_mstats = nullptr;
+  double* m_field = nullptr;    // slab field window
+  size_t m_field_cap = 0;
+  uint8_t* m_flags = nullptr;
+  size_t m_flags_cap = 0;
+  uint8_t* m_masks = nullptr;
+  size_t m_masks_cap = 0;
+  int32_t* m_vbase = nullptr;
+  size_t m_vbase_cap = 0;
+  uint32_t* m_list = nullptr;
+  size_t m_list_cap = 0;
+  long long* m_bsum = nullptr;
+  size_t m_bsum_cap = 0;
+  double* m_verts = nullptr;    // FP64 vertex store when the caller gives none
+  size_t m_verts_cap = 0;
+  int32_t* m_tris = nullptr;    // compaction target of the degenerate filter
+  size_t m_tris_cap = 0;
+};
+
+
+inline int fail(qjg_ctx* ctx, int code, const char* fmt, ...) {
+  if (ctx) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    ctx->err = buf;
+  }
+  return code;
+}
+
+#define QJ_CUDA(ctx, call)                                                                 \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? QJG_ERR_NOMEM : QJG_ERR_CUDA,     \
+                  "%s failed: %s", #call, cudaGetErrorString(e_));                         \
+  } while (0)
+
+template <class T>
+inline int ensure(qjg_ctx* ctx, T** buf, size_t* cap, size_t n) {
+  if (*cap >= n && *buf) return QJG_OK;
+  if (*buf) cudaFree(*buf);
+  *buf = nullptr;
+  *cap = 0;
+  QJ_CUDA(ctx, cudaMalloc((void**)buf, n * sizeof(T)));
+  *cap = n;
+  return QJG_OK;
+}
+
+
+// shared by the field and mesh entry points (api.cpp)
+int qj_check_grid(qjg_ctx* ctx, const qjg_grid* g);
+int qj_check_iter(qjg_ctx* ctx, const qjg_iter* it);
+qj::GridParams qj_grid_params(const qjg_grid* g, int z0, int z1);
+qj::IterParams qj_iter_params(const qjg_iter* it, const qjg_grid* g);
+qj::MapParams* qj_lookup(qjg_ctx* ctx, qjg_rootset rs);

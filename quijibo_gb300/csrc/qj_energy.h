@@ -1,0 +1,23 @@
+// Host-side launchers of the energy kernels (energy.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "qj_params.h"
+
+namespace qj {
+
+// A FIELD_3D weight grid for trilinear lookups (FIELD_3D.cpp:966-1029):
+// corner = center - lengths/2 + dx/2, inv = 1/dx.
+struct WeightGrid {
+  int X, Y, Z;
+  double corner[3];
+  double inv[3];
+};
+
+int tanh_blocks();
+cudaError_t launch_tanh_grad(const MapParams& m, const GridParams& g, const WeightGrid& wg,
+                             const double* weights, int max_it, double alpha, double thr,
+                             bool pow_ref, double* field, double* partials, int nblocks,
+                             double* out, cudaStream_t s);
+
+}  // namespace qj

@@ -1,0 +1,60 @@
+// Launch parameter blocks shared by the host library and the kernels.
+// They are passed to kernels by value, so they live in the constant bank:
+// every thread of a launch reads the same roots, which the constant cache
+// broadcasts.
+#pragma once
+#include <stdint.h>
+
+#define QJ_MAX_ROOTS 128     // top + bottom roots of one map
+#define QJ_MAX_INT_EXP 16    // largest exponent taken by the integer-power path
+
+namespace qj {
+
+// One rational map s * prod (q - t_i)^(sigma_t e_i) / prod (q - b_j)^(sigma_b f_j).
+// Roots [0, nt) are top roots, [nt, nt + nb) bottom roots.
+struct MapParams {
+  int nt, nb;
+  int all_int;                  // every effective exponent is an integer in [1, QJ_MAX_INT_EXP]
+  int pad_;
+  double scale;                 // s (OPTIMIZE_3D::_expScaling)
+  float scalef;
+  float pad2_;
+  double sigma[2];              // power scalars (top, bottom)
+  alignas(16) double r64[QJ_MAX_ROOTS][4];  // roots (w, x, y, z)
+  double e64[QJ_MAX_ROOTS];     // effective exponent sigma * e_i
+  double ep[QJ_MAX_ROOTS];      // the root's own exponent e_i (POLYNOMIAL_4D::powers())
+  alignas(16) float r32[QJ_MAX_ROOTS][4];
+  float e32[QJ_MAX_ROOTS];
+  int ie[QJ_MAX_ROOTS];         // integer exponent, or 0 when the exponent is not an integer
+};
+
+// Cell-centred grid geometry (FIELD_3D) and the z-range of one launch.
+struct GridParams {
+  int X, Y, Z;       // full grid resolution
+  int z0, z1;        // slices [z0, z1) are computed; outputs are indexed from z0
+  double center[3];
+  double half[3];    // lengths * 0.5
+  double dx[3];      // lengths / res
+  double R[3][3];    // rotation matrix of the grid quaternion
+  double slice;      // the fourth (k) coordinate of every start point
+};
+
+// Escape-time iteration settings.
+struct IterParams {
+  int max_it;
+  int want_de;
+  double escape;     // escape radius (the reference hard-codes 2000; the workloads use 2)
+  double band;       // FP32 voxels with |d| < band are re-evaluated in FP64
+  double field_tol;  // ... and so are voxels with |log|q|| < field_tol
+};
+
+// Device-side counters of one field or mesh call.
+struct DevStats {
+  unsigned long long voxel_iters;   // executed map applications
+  unsigned long long refined;       // voxels re-evaluated in FP64
+  unsigned long long nonfinite;     // FP32 voxels that overflowed or underflowed
+  unsigned long long tiles_done;    // work-queue position of the tile scheduler
+  unsigned long long aux[4];
+};
+
+}  // namespace qj

@@ -1,0 +1,257 @@
+"""ctypes bindings of the C ABI in include/quijibo_gpu.h.
+
+Loads the in-tree quijibo_gb300/_lib/libquijibo_gpu.so and raises when it is
+missing: there is no CPU path behind these calls.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from .rootsets import Grid, RootSet
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libquijibo_gpu.so")
+
+QJG_FP64, QJG_FP32, QJG_FP32_REFINE = 0, 1, 2
+QJG_REFINE_POW, QJG_REFINE_INT = 0, 1
+
+_dp = C.POINTER(C.c_double)
+_fp = C.POINTER(C.c_float)
+
+
+class QjgGrid(C.Structure):
+    _fields_ = [("res", C.c_int32 * 3), ("center", C.c_double * 3), ("lengths", C.c_double * 3),
+                ("rot", C.c_double * 4), ("slice", C.c_double)]
+
+    @classmethod
+    def of(cls, g: Grid):
+        s = cls()
+        s.res[:] = [int(v) for v in g.res]
+        s.center[:] = [float(v) for v in g.center]
+        s.lengths[:] = [float(v) for v in g.lengths]
+        s.rot[:] = [float(v) for v in g.rot]
+        s.slice = float(g.slice)
+        return s
+
+
+class QjgIter(C.Structure):
+    _fields_ = [("max_it", C.c_int32), ("precision", C.c_int32), ("refine_pow", C.c_int32),
+                ("want_de", C.c_int32), ("escape", C.c_double), ("band_h", C.c_double),
+                ("field_tol", C.c_double)]
+
+
+class QjgFieldStats(C.Structure):
+    _fields_ = [("voxels", C.c_int64), ("voxel_iters", C.c_int64), ("root_terms", C.c_int64),
+                ("refined", C.c_int64), ("refined_iters", C.c_int64), ("nonfinite", C.c_int64)]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
+QJG_EDGE_LINEAR, QJG_EDGE_BISECT = 0, 1
+
+
+class QjgMeshStats(C.Structure):
+    _fields_ = [("n_verts", C.c_int64), ("n_tris", C.c_int64), ("n_degenerate", C.c_int64),
+                ("n_unbracketed", C.c_int64), ("map_evals", C.c_int64), ("slabs", C.c_int64),
+                ("field", QjgFieldStats)]
+
+    def as_dict(self):
+        d = {k: int(getattr(self, k)) for k, _ in self._fields_ if k != "field"}
+        d["field"] = self.field.as_dict()
+        return d
+
+
+class QjgTanhStats(C.Structure):
+    _fields_ = [("voxels", C.c_int64), ("overflowed", C.c_int64), ("bad_terms", C.c_int64)]
+
+
+EXPORTS = {
+    "qjg_create": ([C.c_int, C.POINTER(C.c_void_p)], C.c_int),
+    "qjg_destroy": ([C.c_void_p], None),
+    "qjg_last_error": ([C.c_void_p], C.c_char_p),
+    "qjg_rootset_upload": ([C.c_void_p, C.c_int32, _dp, _dp, C.c_double, C.c_int32, _dp, _dp,
+                            C.c_double, C.c_double, C.POINTER(C.c_int32)], C.c_int),
+    "qjg_rootset_free": ([C.c_void_p, C.c_int32], C.c_int),
+    "qjg_field": ([C.c_void_p, C.c_int32, C.POINTER(QjgGrid), C.POINTER(QjgIter), C.c_int32,
+                   C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "qjg_field_host": ([C.c_void_p, C.c_int32, C.POINTER(QjgGrid), C.POINTER(QjgIter), _dp, _fp,
+                        C.POINTER(QjgFieldStats)], C.c_int),
+    "qjg_field_stats_read": ([C.c_void_p, C.c_void_p, C.POINTER(QjgFieldStats)], C.c_int),
+    "qjg_mesh_field": ([C.c_void_p, C.c_int32, C.POINTER(QjgGrid), C.POINTER(QjgIter), C.c_void_p,
+                        C.c_int32, C.c_double, C.c_int32, C.c_void_p, C.c_void_p, C.c_int64,
+                        C.c_void_p, C.c_int64, C.POINTER(QjgMeshStats), C.c_void_p], C.c_int),
+    "qjg_mesh_stream": ([C.c_void_p, C.c_int32, C.POINTER(QjgGrid), C.POINTER(QjgIter), C.c_double,
+                         C.c_int32, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
+                         C.POINTER(QjgMeshStats), C.c_void_p], C.c_int),
+    "qjg_tanh_score_grad": ([C.c_void_p, C.c_int32, C.POINTER(QjgGrid), C.c_int32,
+                             C.POINTER(QjgGrid), C.c_void_p, C.c_double, C.c_double, _dp, _dp,
+                             C.c_void_p, C.POINTER(QjgTanhStats), C.c_void_p], C.c_int),
+    # measurement hooks (include/quijibo_gpu_bench.h)
+    "qjg_set_timing": ([C.c_void_p, C.c_int], C.c_int),
+    "qjg_last_timings": ([C.c_void_p, _fp, _fp], C.c_int),
+    "qjg_launch_count": ([C.c_void_p], C.c_int64),
+    "qjg_fma_probe": ([C.c_int, _dp], C.c_int),
+}
+
+_lib = None
+
+
+def load():
+    """Load the library (once); raise if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("CUDA library %s is missing: run `python -m quijibo_gb300.build`"
+                               % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        for name, (args, res) in EXPORTS.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+    return _lib
+
+
+class QjgError(RuntimeError):
+    pass
+
+
+def fma_probe(device=0):
+    """Achieved FP32 TFLOP/s of an FMA-chain probe kernel on every SM."""
+    v = C.c_double()
+    rc = load().qjg_fma_probe(device, C.byref(v))
+    if rc != 0:
+        raise QjgError("qjg_fma_probe failed (%d)" % rc)
+    return v.value
+
+
+def _arr(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a.reshape(shape) if shape else a
+
+
+class Context:
+    """One device context (qjg_create); root sets stay resident on it."""
+
+    def __init__(self, device=0):
+        self.L = load()
+        h = C.c_void_p()
+        rc = self.L.qjg_create(device, C.byref(h))
+        if rc != 0:
+            raise QjgError("qjg_create(%d) failed with %d" % (device, rc))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.L.qjg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise QjgError("%s failed (%d): %s" % (what, rc, self.L.qjg_last_error(self.h).decode()))
+
+    def upload(self, rs: RootSet) -> int:
+        tr, tp = _arr(rs.top_roots, (-1, 4)), _arr(rs.top_powers)
+        br, bp = _arr(rs.bottom_roots, (-1, 4)), _arr(rs.bottom_powers)
+        out = C.c_int32()
+        p = lambda a: a.ctypes.data_as(_dp) if a.size else None
+        self._check(self.L.qjg_rootset_upload(self.h, len(tp), p(tr), p(tp), float(rs.sigma_top),
+                                              len(bp), p(br), p(bp), float(rs.sigma_bottom),
+                                              float(rs.scale), C.byref(out)), "qjg_rootset_upload")
+        return out.value
+
+    def free(self, handle):
+        self._check(self.L.qjg_rootset_free(self.h, handle), "qjg_rootset_free")
+
+    @staticmethod
+    def iter_params(max_it, escape, precision=QJG_FP64, refine_pow=QJG_REFINE_POW, want_de=False,
+                    band_h=2.0, field_tol=1e-3):
+        return QjgIter(int(max_it), int(precision), int(refine_pow), int(bool(want_de)),
+                       float(escape), float(band_h), float(field_tol))
+
+    def field(self, handle, grid: Grid, it: QjgIter, d_field, d_de=None, z0=0, z1=None,
+              stream=None):
+        """Device-pointer call: d_field / d_de are CUDA device addresses (ints)."""
+        z1 = grid.res[2] if z1 is None else z1
+        self._check(self.L.qjg_field(self.h, handle, C.byref(QjgGrid.of(grid)), C.byref(it), z0, z1,
+                                     C.c_void_p(d_field), C.c_void_p(d_de or 0),
+                                     C.c_void_p(stream or 0)), "qjg_field")
+
+    def stats(self, stream=None):
+        st = QjgFieldStats()
+        self._check(self.L.qjg_field_stats_read(self.h, C.c_void_p(stream or 0), C.byref(st)),
+                    "qjg_field_stats_read")
+        return st.as_dict()
+
+    def set_timing(self, on=True):
+        self._check(self.L.qjg_set_timing(self.h, int(on)), "qjg_set_timing")
+
+    def last_timings(self):
+        a, b = C.c_float(), C.c_float()
+        self._check(self.L.qjg_last_timings(self.h, C.byref(a), C.byref(b)), "qjg_last_timings")
+        return a.value, b.value
+
+    def launch_count(self):
+        return int(self.L.qjg_launch_count(self.h))
+
+    def field_host(self, handle, grid: Grid, it: QjgIter, de=False, out=None, de_out=None):
+        """Host-buffer call; returns (field[Z,Y,X] float64, de or None, stats)."""
+        X, Y, Z = grid.res
+        f = out if out is not None else np.empty((Z, Y, X))
+        d = (de_out if de_out is not None else np.empty((Z, Y, X), dtype=np.float32)) if de else None
+        st = QjgFieldStats()
+        self._check(self.L.qjg_field_host(self.h, handle, C.byref(QjgGrid.of(grid)), C.byref(it),
+                                          f.ctypes.data_as(_dp),
+                                          d.ctypes.data_as(_fp) if d is not None else None,
+                                          C.byref(st)), "qjg_field_host")
+        return f, d, st.as_dict()
+
+    def mesh_field(self, handle, grid: Grid, it, d_field, edge_mode, iso=0.0, slab_nz=0,
+                   d_verts64=0, d_verts32=0, vert_cap=0, d_tris=0, tri_cap=0, stream=None,
+                   check=True):
+        """Stored-field mesher on device buffers; returns (rc, stats dict)."""
+        st = QjgMeshStats()
+        rc = self.L.qjg_mesh_field(self.h, handle if handle is not None else -1,
+                                   C.byref(QjgGrid.of(grid)), C.byref(it) if it is not None else None,
+                                   C.c_void_p(d_field), int(edge_mode), float(iso), int(slab_nz),
+                                   C.c_void_p(d_verts64), C.c_void_p(d_verts32), int(vert_cap),
+                                   C.c_void_p(d_tris), int(tri_cap), C.byref(st),
+                                   C.c_void_p(stream or 0))
+        if check:
+            self._check(rc, "qjg_mesh_field")
+        return rc, st.as_dict()
+
+    def mesh_stream(self, handle, grid: Grid, it, iso=0.0, slab_nz=0, d_verts64=0, d_verts32=0,
+                    vert_cap=0, d_tris=0, tri_cap=0, stream=None, check=True):
+        """Streaming mesher (field computed per slab); returns (rc, stats dict)."""
+        st = QjgMeshStats()
+        rc = self.L.qjg_mesh_stream(self.h, handle, C.byref(QjgGrid.of(grid)), C.byref(it),
+                                    float(iso), int(slab_nz), C.c_void_p(d_verts64),
+                                    C.c_void_p(d_verts32), int(vert_cap), C.c_void_p(d_tris),
+                                    int(tri_cap), C.byref(st), C.c_void_p(stream or 0))
+        if check:
+            self._check(rc, "qjg_mesh_stream")
+        return rc, st.as_dict()
+
+    def tanh_score_grad(self, handle, grid: Grid, max_it, wgrid: Grid, d_weights, n_params,
+                        alpha=10.0, threshold=0.0, d_field=0, stream=None):
+        """(score, grad [log s, bottom exps, top exps, sigma_t, sigma_b], stats)."""
+        score = C.c_double()
+        grad = np.empty(n_params)
+        st = QjgTanhStats()
+        self._check(self.L.qjg_tanh_score_grad(self.h, handle, C.byref(QjgGrid.of(grid)),
+                                               int(max_it), C.byref(QjgGrid.of(wgrid)),
+                                               C.c_void_p(d_weights), float(alpha),
+                                               float(threshold), C.byref(score),
+                                               grad.ctypes.data_as(_dp), C.c_void_p(d_field),
+                                               C.byref(st), C.c_void_p(stream or 0)),
+                    "qjg_tanh_score_grad")
+        return score.value, grad, {k: int(getattr(st, k)) for k, _ in st._fields_}

@@ -1,0 +1,125 @@
+"""Generate the golden fixtures of the hot path from the reference itself.
+
+The reference QUIJIBO is compiled from its own sources by oracle/Makefile
+(`make -C oracle ref`) into oracle/_ref/ in two flavours: Real=double and the
+shipped default Real=long double.  This script runs it through
+oracle/ref_harness.cpp on small seeded cases and stores inputs and outputs in
+tests/golden/*.npz.  The reference sources exist only in the development
+container, so the fixtures are committed and the tests read them anywhere.
+
+    python tests/golden/gen_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle.oracle import Reference  # noqa: E402
+from quijibo_gb300.rootsets import (Grid, RootSet, draw_rootset, plain_workload,  # noqa: E402
+                                    precision_workload)
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def rs_dict(prefix, rs, g, params):
+    return {prefix + "top_roots": rs.top_roots, prefix + "top_powers": rs.top_powers,
+            prefix + "sigma_top": rs.sigma_top, prefix + "bottom_roots": rs.bottom_roots,
+            prefix + "bottom_powers": rs.bottom_powers, prefix + "sigma_bottom": rs.sigma_bottom,
+            prefix + "scale": rs.scale, prefix + "res": np.array(g.res),
+            prefix + "center": np.array(g.center), prefix + "lengths": np.array(g.lengths),
+            prefix + "rot": np.array(g.rot), prefix + "slice": g.slice,
+            prefix + "max_it": params["max_it"], prefix + "escape": params["escape"]}
+
+
+def main():
+    rd, rl = Reference("double"), Reference("ldouble")
+    assert rd.sizeof_real == 8 and rl.sizeof_real == 16
+
+    # MT19937 draws and QUATERNION::pow known answers
+    mt = {"mt_seed0": rd.mt_rand(0, 64), "mt_seed12345": rd.mt_rand(12345, 64)}
+    rng = np.random.RandomState(7)
+    qs = np.concatenate([rng.uniform(-2, 2, (40, 4)),
+                         [[1.5, 0, 0, 0], [-1.5, 0, 0, 0], [0.5, 1e-9, 0, 0], [0.0, 0.3, -0.2, 0.1]]])
+    es = np.concatenate([rng.choice([1.0, 2.0, 3.0, 0.5, 1.7, 0.25], 40), [2.0, 3.0, 1.0, 2.5]])
+    pw = np.array([rd.quat_pow(q, e) for q, e in zip(qs, es)])
+    np.savez_compressed(os.path.join(OUT, "algebra.npz"), pow_q=qs, pow_e=es, pow_out=pw, **mt)
+
+    cases = {}
+    # plain method, literal unit scale and conformal scale
+    for name, scale in (("plain_unit", "unit"), ("plain_conf", "conformal")):
+        rs, g, p = plain_workload(32, scale=scale)
+        cases[name] = (rs, g, p)
+    # precision form roots at 32^3
+    cases["prec"] = precision_workload(32)
+    # rotated, shifted grid with a non-zero slice and non-integer exponents
+    rs = draw_rootset(3, 6, 3, -1.0, 1.0, exps=(1, 2))
+    rs.top_powers = rs.top_powers * np.array([1.0, 0.5, 1.0, 1.5, 1.0, 1.0])
+    rs.sigma_top, rs.sigma_bottom = 1.1, 0.9
+    rot = np.array([0.9, 0.1, -0.2, 0.3])
+    rot = rot / np.linalg.norm(rot)
+    g = Grid((24, 20, 16), center=(0.1, -0.2, 0.05), lengths=(2.8, 2.6, 2.4), rot=tuple(rot),
+             slice=0.15)
+    from quijibo_gb300.rootsets import conformal_scale
+    rs.scale = conformal_scale(rs, g)
+    cases["general"] = (rs, g, dict(max_it=12, escape=2.0))
+
+    for name, (rs, g, p) in cases.items():
+        d = rs_dict("", rs, g, p)
+        d["field"] = rd.field_escape(rs, g, p["max_it"], p["escape"])
+        d["field_ld"] = rl.field_escape(rs, g, p["max_it"], p["escape"])
+        np.savez_compressed(os.path.join(OUT, "field_%s.npz" % name), **d)
+
+    # the unmodified OPTIMIZE_3D::computeLogScaledPowerRationalMap (escape 2000)
+    rs, g, p = precision_workload(24)
+    p = dict(max_it=10, escape=2000.0)
+    d = rs_dict("", rs, g, p)
+    d["field"] = rd.field_map(rs, g, p["max_it"])
+    np.savez_compressed(os.path.join(OUT, "field_map2000.npz"), **d)
+
+    # marching cubes: streaming nonlinear, nonlinear on a stored field, linear
+    rs, g, p = plain_workload(32, scale="conformal")
+    p = dict(max_it=20, escape=2000.0)
+    d = rs_dict("", rs, g, p)
+    ms = rd.mesh_stream(rs, g, p["max_it"])
+    d["stream_verts"], d["stream_tris"] = ms["verts"], ms["tris"]
+    f2000 = rd.field_map(rs, g, p["max_it"])
+    d["field2000"] = f2000
+    mn = rd.mesh_field_nonlinear(rs, g, f2000, p["max_it"])
+    d["nonlin_verts"], d["nonlin_tris"] = mn["verts"], mn["tris"]
+    f2 = rd.field_escape(rs, g, 20, 2.0)
+    d["field2"] = f2
+    ml = rd.mesh_linear(g, f2)
+    d["linear_verts"], d["linear_tris"] = ml["verts"], ml["tris"]
+    np.savez_compressed(os.path.join(OUT, "mesh_plain.npz"), **d)
+    rs, g, wg, w = tanh_case()
+    rd2 = Reference("double")
+    d = rs_dict("", rs, g, dict(max_it=1, escape=20.0))
+    sc, gr, f = rd2.tanh_score_grad(rs, g, wg, w, 1)
+    d.update(score=sc, grad=gr, field=f, weights=w, wres=np.array(wg.res),
+             wcenter=np.array(wg.center), wlengths=np.array(wg.lengths))
+    np.savez_compressed(os.path.join(OUT, "tanh_grad.npz"), **d)
+
+    print("stream: %d verts %d tris; nonlinear: %d/%d; linear: %d/%d" % (
+        len(ms["verts"]), len(ms["tris"]), len(mn["verts"]), len(mn["tris"]), len(ml["verts"]),
+        len(ml["tris"])))
+
+
+def tanh_case():
+    """The tanh-weighted score and gradients (maxIterations 1, as toothOptimizer
+    runs them) on a 16^3 grid with a weight field on a different grid."""
+    from quijibo_gb300.rootsets import cell_centers, conformal_scale
+    rs = draw_rootset(11, 8, 4, -1.0, 1.0, exps=(1, 2))
+    rs.sigma_top, rs.sigma_bottom = 1.05, 0.95
+    g = Grid((16, 16, 16))
+    rs.scale = conformal_scale(rs, g)
+    wg = Grid((12, 12, 12), center=(0.05, 0.0, -0.05), lengths=(3.2, 3.2, 3.2))
+    c = cell_centers(wg)
+    w = np.exp(-np.sum(c ** 2, axis=1)) * np.cos(2 * c[:, 0]) + 0.3
+    return rs, g, wg, w
+
+
+if __name__ == "__main__":
+    main()
