@@ -178,6 +178,29 @@ int qjg_tanh_score_grad(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, int3
                         double threshold, double* score, double* grad, double* d_field,
                         qjg_tanh_stats* stats, void* stream);
 
+/* Squared-error fitting energy E = sum_k (d(x_k) - t_k)^2 of the distance
+ * estimate d = |q_N| log|q_N| / |q_N'| at sample points x_k (no reference
+ * counterpart: the reference fits exponents and scales with the tanh score;
+ * this form also fits root positions).  The map's parameters live in a
+ * device vector d_params of 5 * (n_top + n_bot) + 1 doubles:
+ * [top roots (w,x,y,z) x n_top | bottom roots x n_bot | top exponents |
+ *  bottom exponents | log s] (effective exponents, sigma folded in).
+ * d_xyz: n x 3 device doubles; d_target: n device doubles; slice is the
+ * fourth coordinate; precision QJG_FP32 or QJG_FP64.  max_it <= 256.
+ * qjg_energy_forward writes E to *energy (host); qjg_energy_backward also
+ * writes dE/dparams into d_grad (device, same layout), computed by a
+ * hand-written adjoint that recomputes the iteration from checkpoints
+ * instead of storing the trajectory.  d_iters (optional, device) receives
+ * each sample's iteration count.  Both synchronize `stream`. */
+int qjg_energy_forward(qjg_ctx* ctx, const double* d_params, int32_t n_top, int32_t n_bot,
+                       int64_t n, const double* d_xyz, const double* d_target, double slice,
+                       int32_t max_it, double escape, int32_t precision, double* energy,
+                       int32_t* d_iters, void* stream);
+int qjg_energy_backward(qjg_ctx* ctx, const double* d_params, int32_t n_top, int32_t n_bot,
+                        int64_t n, const double* d_xyz, const double* d_target, double slice,
+                        int32_t max_it, double escape, int32_t precision, double* energy,
+                        double* d_grad, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

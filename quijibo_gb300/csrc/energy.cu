@@ -308,4 +308,327 @@ cudaError_t launch_tanh_grad(const MapParams& m, const GridParams& g, const Weig
   return cudaGetLastError();
 }
 
+// ===========================================================================
+// Squared-error fitting energy on the distance estimate and its adjoint.
+//
+// No reference counterpart (the reference tracks no derivative of this map
+// and fits only exponents and scales).  Per sample x_k with target t_k:
+//   q_0 = (x, y, z, slice); for n < N (escape test as the field):
+//     d_i = q_n - r_i, P_i = d_i^{e_i} (polar power), T = prod top P_i,
+//     B = prod bottom P_i, q_{n+1} = s T B^-1,
+//     g_n = sum_top e_i d_i/|d_i|^2 - sum_bot e_j d_j/|d_j|^2,
+//     L_{n+1} = L_n + log|g_n| + log|q_{n+1}|          (L = log|q'|)
+//   d = |q_N| log|q_N| exp(-L_N),  E = sum_k (d_k - t_k)^2.
+// Parameters: root positions (4 each), effective exponents, log s, laid out
+// [top roots 4nt | bottom roots 4nb | top exps nt | bottom exps nb | log s].
+// The backward pass stores no trajectory: it keeps q at every SQ_CK-th
+// iteration and recomputes each segment forward before reversing it.
+// ===========================================================================
+namespace {
+
+constexpr int SQ_T = 64;   // threads per block
+constexpr int SQ_CK = 8;   // checkpoint spacing (iterations)
+constexpr int SQ_MAXIT = 256;
+
+template <class T>
+struct V4 {
+  T w, x, y, z;
+};
+
+template <class T>
+__device__ __forceinline__ V4<T> v4mul(const V4<T>& a, const V4<T>& b) {
+  return V4<T>{a.w * b.w - a.x * b.x - a.y * b.y - a.z * b.z,
+               a.w * b.x + a.x * b.w + a.y * b.z - a.z * b.y,
+               a.w * b.y - a.x * b.z + a.y * b.w + a.z * b.x,
+               a.w * b.z + a.x * b.y - a.y * b.x + a.z * b.w};
+}
+template <class T>
+__device__ __forceinline__ V4<T> v4conj(const V4<T>& a) { return V4<T>{a.w, -a.x, -a.y, -a.z}; }
+template <class T>
+__device__ __forceinline__ T v4dot(const V4<T>& a, const V4<T>& b) {
+  return a.w * b.w + a.x * b.x + a.y * b.y + a.z * b.z;
+}
+template <class T>
+__device__ __forceinline__ V4<T> v4scale(const V4<T>& a, T k) {
+  return V4<T>{a.w * k, a.x * k, a.y * k, a.z * k};
+}
+template <class T>
+__device__ __forceinline__ V4<T> v4add(const V4<T>& a, const V4<T>& b) {
+  return V4<T>{a.w + b.w, a.x + b.x, a.y + b.y, a.z + b.z};
+}
+
+// polar power (the form of QUATERNION::pow) and its vector-Jacobian product
+template <class T>
+struct PowParts {
+  T rho, vm, theta, A, c, s;
+};
+
+template <class T>
+__device__ __forceinline__ V4<T> powv(const V4<T>& d, T e, PowParts<T>* pp) {
+  const T v2 = d.x * d.x + d.y * d.y + d.z * d.z;
+  const T rho = sqrt(v2 + d.w * d.w), vm = sqrt(v2);
+  const T theta = acos(d.w / rho);
+  const T A = exp(e * log(rho));
+  T s, c;
+  sincos(e * theta, &s, &c);
+  const T k = vm > T(0) ? A * s / vm : T(0);
+  if (pp) *pp = PowParts<T>{rho, vm, theta, A, c, s};
+  return V4<T>{A * c, k * d.x, k * d.y, k * d.z};
+}
+
+// given Pbar, accumulate dbar (returned) and ebar
+template <class T>
+__device__ __forceinline__ V4<T> powv_vjp(const V4<T>& d, T e, const PowParts<T>& p,
+                                          const V4<T>& Pb, T* ebar) {
+  const T ux = p.vm > T(0) ? d.x / p.vm : T(0), uy = p.vm > T(0) ? d.y / p.vm : T(0),
+          uz = p.vm > T(0) ? d.z / p.vm : T(0);
+  const T pu = Pb.x * ux + Pb.y * uy + Pb.z * uz;
+  const T Ab = Pb.w * p.c + pu * p.s;
+  const T phib = p.A * (pu * p.c - Pb.w * p.s);
+  const T rhob = Ab * e * p.A / p.rho;
+  const T thetab = phib * e;
+  *ebar += Ab * p.A * log(p.rho) + phib * p.theta;
+  const T r2 = p.rho * p.rho;
+  V4<T> db;
+  db.w = rhob * d.w / p.rho - thetab * p.vm / r2;
+  const T kv = rhob / p.rho;
+  const T kt = thetab * d.w / r2;
+  db.x = kv * d.x + kt * ux;
+  db.y = kv * d.y + kt * uy;
+  db.z = kv * d.z + kt * uz;
+  if (p.vm > T(0)) {
+    // u = v / |v|: (I - u u^T) ubar / |v| with ubar = A sin(phi) Pbar_v
+    const T ub = p.A * p.s;
+    const T ubx = ub * Pb.x, uby = ub * Pb.y, ubz = ub * Pb.z;
+    const T proj = ubx * ux + uby * uy + ubz * uz;
+    db.x += (ubx - proj * ux) / p.vm;
+    db.y += (uby - proj * uy) / p.vm;
+    db.z += (ubz - proj * uz) / p.vm;
+  }
+  return db;
+}
+
+template <class T>
+struct SqShared {
+  int nt, nb;
+  T s;
+};
+
+// One map application q -> Q with log|g|; fills prefix products F (per
+// side) and factors P when `keep` is set.
+template <class T>
+__device__ __forceinline__ V4<T> sq_apply(const T* __restrict__ rp, const T* __restrict__ ep,
+                                          int nt, int nb, T s, const V4<T>& q, T* lg,
+                                          V4<T>* F, V4<T>* Pf, V4<T>* Tout, V4<T>* Bout) {
+  V4<T> acc[2] = {{T(1), T(0), T(0), T(0)}, {T(1), T(0), T(0), T(0)}};
+  V4<T> g = {T(0), T(0), T(0), T(0)};
+  for (int i = 0; i < nt + nb; i++) {
+    const int side = i >= nt;
+    const V4<T> d{q.w - rp[4 * i], q.x - rp[4 * i + 1], q.y - rp[4 * i + 2], q.z - rp[4 * i + 3]};
+    const T e = ep[i];
+    const T k = (side ? -e : e) / v4dot(d, d);
+    g = v4add(g, v4scale(d, k));
+    const V4<T> P = powv<T>(d, e, nullptr);
+    acc[side] = (i == 0 || i == nt) ? P : v4mul(acc[side], P);
+    if (F) F[i] = acc[side];
+    if (Pf) Pf[i] = P;
+  }
+  V4<T> Q;
+  if (nb > 0) {
+    const V4<T> W = v4scale(v4conj(acc[1]), T(1) / v4dot(acc[1], acc[1]));
+    Q = v4scale(v4mul(acc[0], W), s);
+  } else {
+    Q = v4scale(acc[0], s);
+  }
+  *lg = T(0.5) * log(v4dot(g, g));
+  if (Tout) *Tout = acc[0];
+  if (Bout) *Bout = acc[1];
+  return Q;
+}
+
+// Forward to the end: returns d and the iteration count; fills checkpoints.
+template <class T>
+__device__ __forceinline__ T sq_forward(const T* rp, const T* ep, int nt, int nb, T s,
+                                        V4<T> q, int max_it, T esc, int* n_out, T* L_out,
+                                        V4<T>* ck, T* Lck) {
+  T L = T(0);
+  int n = 0;
+  while (sqrt(v4dot(q, q)) < esc && n < max_it) {
+    if (ck && n % SQ_CK == 0) {
+      ck[n / SQ_CK] = q;
+      Lck[n / SQ_CK] = L;
+    }
+    T lg;
+    q = sq_apply<T>(rp, ep, nt, nb, s, q, &lg, nullptr, nullptr, nullptr, nullptr);
+    L += lg + T(0.5) * log(v4dot(q, q));
+    n++;
+  }
+  const T m = sqrt(v4dot(q, q));
+  *n_out = n;
+  *L_out = L;
+  if (ck) ck[n / SQ_CK + 1] = q;  // final iterate (slot after the last checkpoint)
+  return m * log(m) * exp(-L);
+}
+
+template <class T, bool GRAD>
+__global__ void __launch_bounds__(SQ_T) sq_energy_kernel(
+    const double* __restrict__ params, int nt, int nb, const double* __restrict__ xyz,
+    const double* __restrict__ target, long long n_samples, double slice, int max_it,
+    double escape, double* __restrict__ partials, int slots, int* __restrict__ iters_out) {
+  extern __shared__ unsigned char sh_raw[];
+  const int nr = nt + nb;
+  T* rp = reinterpret_cast<T*>(sh_raw);           // 4 nr
+  T* ep = rp + 4 * nr;                            // nr
+  double* acc_sh = reinterpret_cast<double*>(sh_raw + ((sizeof(T) * 5 * nr + 15) / 16) * 16);
+  for (int k = threadIdx.x; k < 4 * nr; k += SQ_T) rp[k] = (T)params[k];
+  for (int k = threadIdx.x; k < nr; k += SQ_T) ep[k] = (T)params[4 * nr + k];
+  for (int k = threadIdx.x; k < (SQ_T / 32) * slots; k += SQ_T) acc_sh[k] = 0.0;
+  __syncthreads();
+  const T s = (T)exp(params[5 * nr]);
+  const T esc = (T)escape;
+  double* acc = acc_sh + (threadIdx.x >> 5) * slots;
+  // per-thread scratch (local memory)
+  V4<T> ck[SQ_MAXIT / SQ_CK + 2];
+  T Lck[SQ_MAXIT / SQ_CK + 2];
+  V4<T> seg[SQ_CK];
+  V4<T> Pf[QJ_MAX_ROOTS], F[QJ_MAX_ROOTS];
+  T gacc[5 * QJ_MAX_ROOTS + 1];
+  if (GRAD)
+    for (int k = 0; k <= 5 * nr; k++) gacc[k] = T(0);
+  double e_acc = 0.0;
+  const long long stride = (long long)gridDim.x * SQ_T;
+  for (long long k = (long long)blockIdx.x * SQ_T + threadIdx.x; k < n_samples; k += stride) {
+    const V4<T> q0{(T)xyz[3 * k], (T)xyz[3 * k + 1], (T)xyz[3 * k + 2], (T)slice};
+    int N;
+    T LN;
+    const T dval = sq_forward<T>(rp, ep, nt, nb, s, q0, max_it, esc, &N, &LN, GRAD ? ck : nullptr,
+                                 GRAD ? Lck : nullptr);
+    if (iters_out) iters_out[k] = N;
+    const T r = dval - (T)target[k];
+    e_acc += (double)(r * r);
+    if (!GRAD) continue;
+    // seed: dE/dd = 2 r; d = m log m exp(-L)
+    const V4<T> qN = ck[N / SQ_CK + 1];
+    const T m = sqrt(v4dot(qN, qN));
+    const T db = T(2) * r;
+    const T eL = exp(-LN);
+    V4<T> qb = v4scale(qN, db * (log(m) + T(1)) * eL / m);
+    const T Lb = -db * dval;  // constant along the chain (L_{n+1} = L_n + ...)
+    // segments in reverse
+    for (int sgi = (N - 1) / SQ_CK; sgi >= 0 && N > 0; sgi--) {
+      const int n0 = sgi * SQ_CK, n1 = min(N, n0 + SQ_CK);
+      V4<T> q = ck[sgi];
+      for (int n = n0; n < n1; n++) {
+        seg[n - n0] = q;
+        T lg;
+        q = sq_apply<T>(rp, ep, nt, nb, s, q, &lg, nullptr, nullptr, nullptr, nullptr);
+      }
+      for (int n = n1 - 1; n >= n0; n--) {
+        const V4<T> qn = seg[n - n0];
+        T lg;
+        V4<T> Tq, Bq;
+        const V4<T> Q = sq_apply<T>(rp, ep, nt, nb, s, qn, &lg, F, Pf, &Tq, &Bq);
+        // L_{n+1} = L_n + log|g| + log|Q|
+        V4<T> Qb = v4add(qb, v4scale(Q, Lb / v4dot(Q, Q)));
+        // d/d log s: <Qbar, Q>
+        gacc[5 * nr] += v4dot(Qb, Q);
+        V4<T> Tb, Bb = {T(0), T(0), T(0), T(0)};
+        if (nb > 0) {
+          const V4<T> W = v4scale(v4conj(Bq), T(1) / v4dot(Bq, Bq));
+          Tb = v4scale(v4mul(Qb, v4conj(W)), s);
+          const V4<T> Wb = v4scale(v4mul(v4conj(Tq), Qb), s);
+          Bb = v4scale(v4mul(v4mul(v4conj(W), Wb), v4conj(W)), T(-1));
+        } else {
+          Tb = v4scale(Qb, s);
+        }
+        // gradient of log|g| w.r.t. g
+        V4<T> g = {T(0), T(0), T(0), T(0)};
+        for (int i = 0; i < nr; i++) {
+          const V4<T> d{qn.w - rp[4 * i], qn.x - rp[4 * i + 1], qn.y - rp[4 * i + 2],
+                        qn.z - rp[4 * i + 3]};
+          g = v4add(g, v4scale(d, (i >= nt ? -ep[i] : ep[i]) / v4dot(d, d)));
+        }
+        const V4<T> gb = v4scale(g, Lb / v4dot(g, g));
+        V4<T> qbn = {T(0), T(0), T(0), T(0)};
+        // products: Pbar_i = conj(F_{i-1}) U, U <- U conj(P_i), from the end
+        for (int side = 1; side >= 0; side--) {
+          const int lo = side ? nt : 0, hi = side ? nr : nt;
+          if (hi == lo) continue;
+          V4<T> U = side ? Bb : Tb;
+          for (int i = hi - 1; i >= lo; i--) {
+            const V4<T> Pb = (i == lo) ? U : v4mul(v4conj(F[i - 1]), U);
+            U = v4mul(U, v4conj(Pf[i]));
+            const V4<T> d{qn.w - rp[4 * i], qn.x - rp[4 * i + 1], qn.y - rp[4 * i + 2],
+                          qn.z - rp[4 * i + 3]};
+            PowParts<T> pp;
+            powv<T>(d, ep[i], &pp);
+            T eb = T(0);
+            V4<T> dbar = powv_vjp<T>(d, ep[i], pp, Pb, &eb);
+            // g term: sgn e d/|d|^2
+            const T sgn = side ? T(-1) : T(1);
+            const T d2 = v4dot(d, d);
+            const T dg = v4dot(d, gb);
+            dbar = v4add(dbar, v4scale(v4add(v4scale(gb, T(1) / d2), v4scale(d, T(-2) * dg / (d2 * d2))),
+                                       sgn * ep[i]));
+            eb += sgn * dg / d2;
+            gacc[4 * nr + i] += eb;
+            gacc[4 * i] -= dbar.w;
+            gacc[4 * i + 1] -= dbar.x;
+            gacc[4 * i + 2] -= dbar.y;
+            gacc[4 * i + 3] -= dbar.z;
+            qbn = v4add(qbn, dbar);
+          }
+        }
+        qb = qbn;
+      }
+    }
+  }
+  // deterministic reduction: warp trees, warps in order
+  for (int k = 0; k < slots; k++) {
+    double v = (k == 0) ? e_acc : (GRAD ? (double)gacc[k - 1] : 0.0);
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) acc[k] += v;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < slots; k += SQ_T) {
+    double v = 0;
+    for (int w = 0; w < SQ_T / 32; w++) v += acc_sh[w * slots + k];
+    partials[(long long)blockIdx.x * slots + k] = v;
+  }
+}
+
+}  // namespace
+
+int sq_max_iterations() { return SQ_MAXIT; }
+
+cudaError_t launch_sq_energy(bool fp64, bool grad, const double* params, int nt, int nb,
+                             const double* xyz, const double* target, long long n, double slice,
+                             int max_it, double escape, double* partials, int nblocks,
+                             double* out, int* iters, cudaStream_t s) {
+  const int nr = nt + nb;
+  const int slots = 1 + 5 * nr + 1;
+  const size_t elem = fp64 ? sizeof(double) : sizeof(float);
+  const size_t sh = ((elem * 5 * nr + 15) / 16) * 16 + sizeof(double) * (SQ_T / 32) * slots;
+  if (fp64) {
+    if (grad)
+      sq_energy_kernel<double, true><<<nblocks, SQ_T, sh, s>>>(params, nt, nb, xyz, target, n, slice,
+                                                               max_it, escape, partials, slots, iters);
+    else
+      sq_energy_kernel<double, false><<<nblocks, SQ_T, sh, s>>>(params, nt, nb, xyz, target, n, slice,
+                                                                max_it, escape, partials, slots, iters);
+  } else {
+    if (grad)
+      sq_energy_kernel<float, true><<<nblocks, SQ_T, sh, s>>>(params, nt, nb, xyz, target, n, slice,
+                                                              max_it, escape, partials, slots, iters);
+    else
+      sq_energy_kernel<float, false><<<nblocks, SQ_T, sh, s>>>(params, nt, nb, xyz, target, n, slice,
+                                                               max_it, escape, partials, slots, iters);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  reduce_partials_kernel<<<(slots + 255) / 256, 256, 0, s>>>(partials, nblocks, slots, out);
+  return cudaGetLastError();
+}
+
 }  // namespace qj

@@ -1,6 +1,7 @@
 // C ABI of the fitting energies and their gradients.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -59,6 +60,59 @@ int qjg_tanh_score_grad(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, int3
     stats->bad_terms = (int64_t)out[5 + nt + nb];
   }
   return QJG_OK;
+}
+
+static int sq_energy(qjg_ctx* ctx, const double* d_params, int32_t nt, int32_t nb, int64_t n,
+                     const double* d_xyz, const double* d_target, double slice, int32_t max_it,
+                     double escape, int32_t precision, double* energy, double* d_grad,
+                     int32_t* d_iters, void* stream) {
+  if (!ctx) return QJG_ERR_ARG;
+  if (nt < 1 || nb < 0 || nt + nb > QJG_MAX_ROOTS)
+    return fail(ctx, QJG_ERR_ARG, "root counts top=%d bottom=%d", nt, nb);
+  if (n < 0 || !d_params || !energy || (n > 0 && (!d_xyz || !d_target)))
+    return fail(ctx, QJG_ERR_ARG, "NULL or negative energy arguments");
+  if (max_it < 0 || max_it > qj::sq_max_iterations())
+    return fail(ctx, QJG_ERR_ARG, "max_it = %d outside [0, %d]", max_it, qj::sq_max_iterations());
+  if (!(escape > 0)) return fail(ctx, QJG_ERR_ARG, "escape radius must be > 0");
+  if (precision != QJG_FP32 && precision != QJG_FP64)
+    return fail(ctx, QJG_ERR_ARG, "energy precision must be QJG_FP32 or QJG_FP64");
+  cudaStream_t s = (cudaStream_t)stream;
+  QJ_CUDA(ctx, cudaSetDevice(ctx->device));
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  const int nblocks = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * 8, (n + 63) / 64));
+  const int slots = 1 + 5 * (nt + nb) + 1;
+  double* d_part = nullptr;
+  QJ_CUDA(ctx, cudaMallocAsync((void**)&d_part, sizeof(double) * ((size_t)nblocks + 1) * slots, s));
+  double* d_out = d_part + (size_t)nblocks * slots;
+  cudaError_t e = qj::launch_sq_energy(precision == QJG_FP64, d_grad != nullptr, d_params, nt, nb,
+                                       d_xyz, d_target, n, slice, max_it, escape, d_part, nblocks,
+                                       d_out, d_iters, s);
+  if (e == cudaSuccess && d_grad)
+    e = cudaMemcpyAsync(d_grad, d_out + 1, sizeof(double) * (slots - 1), cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(energy, d_out, sizeof(double), cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(d_part, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return fail(ctx, QJG_ERR_CUDA, "energy: %s", cudaGetErrorString(e));
+  ctx->launches += 2;
+  return QJG_OK;
+}
+
+int qjg_energy_forward(qjg_ctx* ctx, const double* d_params, int32_t n_top, int32_t n_bot,
+                       int64_t n, const double* d_xyz, const double* d_target, double slice,
+                       int32_t max_it, double escape, int32_t precision, double* energy,
+                       int32_t* d_iters, void* stream) {
+  return sq_energy(ctx, d_params, n_top, n_bot, n, d_xyz, d_target, slice, max_it, escape,
+                   precision, energy, nullptr, d_iters, stream);
+}
+
+int qjg_energy_backward(qjg_ctx* ctx, const double* d_params, int32_t n_top, int32_t n_bot,
+                        int64_t n, const double* d_xyz, const double* d_target, double slice,
+                        int32_t max_it, double escape, int32_t precision, double* energy,
+                        double* d_grad, void* stream) {
+  if (!d_grad) return fail(ctx, QJG_ERR_ARG, "d_grad is NULL");
+  return sq_energy(ctx, d_params, n_top, n_bot, n, d_xyz, d_target, slice, max_it, escape,
+                   precision, energy, d_grad, nullptr, stream);
 }
 
 }  // extern "C"

@@ -20,4 +20,10 @@ cudaError_t launch_tanh_grad(const MapParams& m, const GridParams& g, const Weig
                              bool pow_ref, double* field, double* partials, int nblocks,
                              double* out, cudaStream_t s);
 
+int sq_max_iterations();
+cudaError_t launch_sq_energy(bool fp64, bool grad, const double* params, int nt, int nb,
+                             const double* xyz, const double* target, long long n, double slice,
+                             int max_it, double escape, double* partials, int nblocks,
+                             double* out, int* iters, cudaStream_t s);
+
 }  // namespace qj

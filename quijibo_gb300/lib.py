@@ -88,6 +88,12 @@ EXPORTS = {
     "qjg_tanh_score_grad": ([C.c_void_p, C.c_int32, C.POINTER(QjgGrid), C.c_int32,
                              C.POINTER(QjgGrid), C.c_void_p, C.c_double, C.c_double, _dp, _dp,
                              C.c_void_p, C.POINTER(QjgTanhStats), C.c_void_p], C.c_int),
+    "qjg_energy_forward": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p,
+                            C.c_void_p, C.c_double, C.c_int32, C.c_double, C.c_int32, _dp,
+                            C.c_void_p, C.c_void_p], C.c_int),
+    "qjg_energy_backward": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p,
+                             C.c_void_p, C.c_double, C.c_int32, C.c_double, C.c_int32, _dp,
+                             C.c_void_p, C.c_void_p], C.c_int),
     # measurement hooks (include/quijibo_gpu_bench.h)
     "qjg_set_timing": ([C.c_void_p, C.c_int], C.c_int),
     "qjg_last_timings": ([C.c_void_p, _fp, _fp], C.c_int),
@@ -255,3 +261,42 @@ class Context:
                                                C.byref(st), C.c_void_p(stream or 0)),
                     "qjg_tanh_score_grad")
         return score.value, grad, {k: int(getattr(st, k)) for k, _ in st._fields_}
+
+    def energy(self, d_params, n_top, n_bot, n, d_xyz, d_target, max_it, escape, slice_=0.0,
+               precision=QJG_FP64, d_grad=0, d_iters=0, stream=None):
+        """Squared-error energy (and, with d_grad, its gradient into d_grad)."""
+        e = C.c_double()
+        if d_grad:
+            rc = self.L.qjg_energy_backward(self.h, C.c_void_p(d_params), n_top, n_bot, int(n),
+                                            C.c_void_p(d_xyz), C.c_void_p(d_target), float(slice_),
+                                            int(max_it), float(escape), int(precision), C.byref(e),
+                                            C.c_void_p(d_grad), C.c_void_p(stream or 0))
+            self._check(rc, "qjg_energy_backward")
+        else:
+            rc = self.L.qjg_energy_forward(self.h, C.c_void_p(d_params), n_top, n_bot, int(n),
+                                           C.c_void_p(d_xyz), C.c_void_p(d_target), float(slice_),
+                                           int(max_it), float(escape), int(precision), C.byref(e),
+                                           C.c_void_p(d_iters), C.c_void_p(stream or 0))
+            self._check(rc, "qjg_energy_forward")
+        return e.value
+
+
+def params_of(rs: RootSet):
+    """The energy parameter vector [top roots | bottom roots | top exps |
+    bottom exps | log s] of a root set (effective exponents sigma * e)."""
+    return np.concatenate([np.asarray(rs.top_roots, dtype=np.float64).reshape(-1),
+                           np.asarray(rs.bottom_roots, dtype=np.float64).reshape(-1),
+                           rs.sigma_top * np.asarray(rs.top_powers, dtype=np.float64),
+                           rs.sigma_bottom * np.asarray(rs.bottom_powers, dtype=np.float64),
+                           [np.log(rs.scale)]])
+
+
+def rootset_of(params, n_top, n_bot):
+    """Inverse of params_of (sigma = 1)."""
+    p = np.asarray(params, dtype=np.float64)
+    nr = n_top + n_bot
+    r = p[:4 * nr].reshape(nr, 4)
+    e = p[4 * nr:5 * nr]
+    return RootSet(top_roots=r[:n_top].copy(), top_powers=e[:n_top].copy(),
+                   bottom_roots=r[n_top:].copy(), bottom_powers=e[n_top:].copy(),
+                   scale=float(np.exp(p[5 * nr])))
