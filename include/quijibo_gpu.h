@@ -201,6 +201,27 @@ int qjg_energy_backward(qjg_ctx* ctx, const double* d_params, int32_t n_top, int
                         int32_t max_it, double escape, int32_t precision, double* energy,
                         double* d_grad, void* stream);
 
+typedef struct {
+  int32_t steps;          /* L-BFGS iterations taken */
+  int32_t energy_evals;   /* forward evaluations (line search) */
+  int32_t gradient_evals; /* forward + adjoint evaluations */
+  double energy0;         /* energy at the start */
+  double energy;          /* energy at the end */
+} qjg_fit_stats;
+
+/* Fit the map's parameters (d_params, layout of qjg_energy_backward, updated
+ * in place on the device) to the sample targets with `steps` iterations of
+ * L-BFGS (history `history` pairs, Armijo backtracking).  The parameters,
+ * gradients and history stay on the device; only scalar energies reach the
+ * host.  Replaces the role of toothOptimizer's TAO_SOLVER::optimizeBLMVM
+ * loop (src/TOUPEE/TAO_SOLVER.h:41-43) for this energy; no bounds.
+ * energies (optional, host, steps + 1 doubles) receives the energy after
+ * each step.  Synchronizes `stream`. */
+int qjg_fit_lbfgs(qjg_ctx* ctx, double* d_params, int32_t n_top, int32_t n_bot, int64_t n,
+                  const double* d_xyz, const double* d_target, double slice, int32_t max_it,
+                  double escape, int32_t precision, int32_t steps, int32_t history,
+                  double* energies, qjg_fit_stats* stats, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -93,6 +93,9 @@ class Oracle:
         L.qjo_tanh_score_grad.argtypes = [C.POINTER(_Map), C.POINTER(_Grid), C.POINTER(_Grid), _dp,
                                           C.c_int, C.c_double, C.c_double, _dp, _dp]
         L.qjo_tanh_score_grad.restype = C.c_double
+        L.qjo_sqerr_energy.argtypes = [C.POINTER(_Map), C.c_int64, _dp, _dp, C.c_double, C.c_int,
+                                       C.c_double, C.POINTER(C.c_int32)]
+        L.qjo_sqerr_energy.restype = C.c_double
         self.L = L
 
     def mt_rand(self, seed, n):
@@ -159,6 +162,14 @@ class Oracle:
                                         C.byref(make_grid(wgrid)), _ptr(w), max_it, alpha,
                                         threshold, _ptr(grad), _ptr(field))
         return sc, grad, field.reshape(grid.res[::-1])
+
+    def sqerr_energy(self, rootset, xyz, target, max_it, escape, slice_=0.0, iters=False):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        t = np.ascontiguousarray(target, dtype=np.float64)
+        it = np.empty(len(t), dtype=np.int32) if iters else None
+        e = self.L.qjo_sqerr_energy(C.byref(make_map(rootset)), len(t), _ptr(xyz), _ptr(t), slice_,
+                                    max_it, escape, _ptr(it, C.POINTER(C.c_int32)))
+        return (e, it) if iters else e
 
     def trilinear(self, grid, data, p):
         data = np.ascontiguousarray(data, dtype=np.float64).reshape(-1)

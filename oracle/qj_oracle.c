@@ -656,3 +656,22 @@ double qjo_tanh_score_grad(const qjo_map* m, const qjo_grid* g, const qjo_grid* 
   return score;
 }
 
+/* Squared-error energy sum_k (d(x_k) - t_k)^2 of the distance estimate
+ * (no reference counterpart; d as in qjo_field's de output). */
+double qjo_sqerr_energy(const qjo_map* m, int64_t n, const double* xyz, const double* target,
+                        double slice, int max_it, double escape, int32_t* iters) {
+  double e = 0.0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : e)
+#endif
+  for (int64_t k = 0; k < n; k++) {
+    double d;
+    int32_t it;
+    escape_value(m, xyz + 3 * k, slice, max_it, escape, &d, &it);
+    if (iters) iters[k] = it;
+    const double r = d - target[k];
+    e += r * r;
+  }
+  return e;
+}
+

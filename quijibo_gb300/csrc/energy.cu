@@ -462,6 +462,7 @@ __device__ __forceinline__ T sq_forward(const T* rp, const T* ep, int nt, int nb
     q = sq_apply<T>(rp, ep, nt, nb, s, q, &lg, nullptr, nullptr, nullptr, nullptr);
     L += lg + T(0.5) * log(v4dot(q, q));
     n++;
+    if (sqrt(v4dot(q, q)) < T(1.1754943508e-37)) break;  // 10 * FLT_MIN exit of the field loop
   }
   const T m = sqrt(v4dot(q, q));
   *n_out = n;

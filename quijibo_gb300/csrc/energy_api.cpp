@@ -8,6 +8,7 @@
 
 #include "qj_ctx.h"
 #include "qj_energy.h"
+#include "qj_lbfgs.h"
 
 extern "C" {
 
@@ -113,6 +114,104 @@ int qjg_energy_backward(qjg_ctx* ctx, const double* d_params, int32_t n_top, int
   if (!d_grad) return fail(ctx, QJG_ERR_ARG, "d_grad is NULL");
   return sq_energy(ctx, d_params, n_top, n_bot, n, d_xyz, d_target, slice, max_it, escape,
                    precision, energy, d_grad, nullptr, stream);
+}
+
+int qjg_fit_lbfgs(qjg_ctx* ctx, double* d_params, int32_t nt, int32_t nb, int64_t n,
+                  const double* d_xyz, const double* d_target, double slice, int32_t max_it,
+                  double escape, int32_t precision, int32_t steps, int32_t history,
+                  double* energies, qjg_fit_stats* stats, void* stream) {
+  if (!ctx) return QJG_ERR_ARG;
+  if (!d_params || steps < 0 || history < 1 || history > 64)
+    return fail(ctx, QJG_ERR_ARG, "fit: NULL params, steps < 0 or history outside [1, 64]");
+  if (nt < 1 || nb < 0 || nt + nb > QJG_MAX_ROOTS)
+    return fail(ctx, QJG_ERR_ARG, "root counts top=%d bottom=%d", nt, nb);
+  cudaStream_t s = (cudaStream_t)stream;
+  QJ_CUDA(ctx, cudaSetDevice(ctx->device));
+  const int P = 5 * (nt + nb) + 1, m = history;
+  // x1 g0 g1 d | S Y (m x P) | rho alpha (m) | gd
+  const size_t total = (size_t)P * 4 + (size_t)2 * m * P + 2 * (size_t)m + 1;
+  double* buf = nullptr;
+  QJ_CUDA(ctx, cudaMallocAsync((void**)&buf, total * sizeof(double), s));
+  double *x = d_params, *x1 = buf, *g0 = x1 + P, *g1 = g0 + P, *d = g1 + P;
+  double *S = d + P, *Y = S + (size_t)m * P, *rho = Y + (size_t)m * P, *alpha = rho + m;
+  double* gd_dev = alpha + m;
+  qjg_fit_stats st = {};
+  int rc = QJG_OK;
+  auto energy = [&](const double* params, double* e, double* grad) {
+    return grad ? qjg_energy_backward(ctx, params, nt, nb, n, d_xyz, d_target, slice, max_it,
+                                      escape, precision, e, grad, stream)
+                : qjg_energy_forward(ctx, params, nt, nb, n, d_xyz, d_target, slice, max_it,
+                                     escape, precision, e, nullptr, stream);
+  };
+  double E = 0;
+  int k = 0, head = -1;
+  if ((rc = energy(x, &E, g0))) goto done;
+  st.gradient_evals++;
+  st.energy0 = E;
+  if (energies) energies[0] = E;
+  for (int it = 0; it < steps; it++) {
+    double gd = 0, gg = 0;
+    cudaError_t e = qj::lbfgs_direction(g0, S, Y, rho, P, m, k, head < 0 ? 0 : head, alpha, d,
+                                        gd_dev, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&gd, gd_dev, sizeof gd, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+      rc = fail(ctx, QJG_ERR_CUDA, "lbfgs: %s", cudaGetErrorString(e));
+      goto done;
+    }
+    ctx->launches++;
+    if (!(gd < 0)) {  // not a descent direction: restart from steepest descent
+      k = 0;
+      head = -1;
+      e = qj::lbfgs_direction(g0, S, Y, rho, P, m, 0, 0, alpha, d, gd_dev, s);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(&gd, gd_dev, sizeof gd, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) {
+        rc = fail(ctx, QJG_ERR_CUDA, "lbfgs: %s", cudaGetErrorString(e));
+        goto done;
+      }
+      ctx->launches++;
+    }
+    gg = -gd;  // |g|^2 when d = -g
+    double a = (k == 0) ? 1.0 / std::max(1.0, std::sqrt(std::max(gg, 0.0))) : 1.0;
+    double Et = 0;
+    bool accepted = false;
+    for (int ls = 0; ls < 30; ls++) {
+      if ((e = qj::lbfgs_axpy(x, d, a, P, x1, s)) != cudaSuccess) {
+        rc = fail(ctx, QJG_ERR_CUDA, "lbfgs: %s", cudaGetErrorString(e));
+        goto done;
+      }
+      ctx->launches++;
+      if ((rc = energy(x1, &Et, nullptr))) goto done;
+      st.energy_evals++;
+      if (std::isfinite(Et) && Et <= E + 1e-4 * a * gd) {
+        accepted = true;
+        break;
+      }
+      a *= 0.5;
+    }
+    if (!accepted) break;  // no decrease along d: converged to noise level
+    if ((rc = energy(x1, &Et, g1))) goto done;
+    st.gradient_evals++;
+    head = (head + 1) % m;
+    if ((e = qj::lbfgs_update(x, x1, g0, g1, P, head, S, Y, rho, s)) != cudaSuccess) {
+      rc = fail(ctx, QJG_ERR_CUDA, "lbfgs: %s", cudaGetErrorString(e));
+      goto done;
+    }
+    ctx->launches++;
+    k = std::min(k + 1, m);
+    cudaMemcpyAsync(x, x1, P * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(g0, g1, P * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    E = Et;
+    st.steps++;
+    if (energies) energies[st.steps] = E;
+  }
+  st.energy = E;
+done:
+  cudaFreeAsync(buf, s);
+  cudaStreamSynchronize(s);
+  if (stats) *stats = st;
+  return rc;
 }
 
 }  // extern "C"

@@ -67,6 +67,11 @@ class QjgTanhStats(C.Structure):
     _fields_ = [("voxels", C.c_int64), ("overflowed", C.c_int64), ("bad_terms", C.c_int64)]
 
 
+class QjgFitStats(C.Structure):
+    _fields_ = [("steps", C.c_int32), ("energy_evals", C.c_int32), ("gradient_evals", C.c_int32),
+                ("energy0", C.c_double), ("energy", C.c_double)]
+
+
 EXPORTS = {
     "qjg_create": ([C.c_int, C.POINTER(C.c_void_p)], C.c_int),
     "qjg_destroy": ([C.c_void_p], None),
@@ -94,6 +99,9 @@ EXPORTS = {
     "qjg_energy_backward": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p,
                              C.c_void_p, C.c_double, C.c_int32, C.c_double, C.c_int32, _dp,
                              C.c_void_p, C.c_void_p], C.c_int),
+    "qjg_fit_lbfgs": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p,
+                       C.c_void_p, C.c_double, C.c_int32, C.c_double, C.c_int32, C.c_int32,
+                       C.c_int32, _dp, C.POINTER(QjgFitStats), C.c_void_p], C.c_int),
     # measurement hooks (include/quijibo_gpu_bench.h)
     "qjg_set_timing": ([C.c_void_p, C.c_int], C.c_int),
     "qjg_last_timings": ([C.c_void_p, _fp, _fp], C.c_int),
@@ -279,6 +287,23 @@ class Context:
                                            C.c_void_p(d_iters), C.c_void_p(stream or 0))
             self._check(rc, "qjg_energy_forward")
         return e.value
+
+
+def _fit(self, d_params, n_top, n_bot, n, d_xyz, d_target, max_it, escape, steps, history=8,
+         slice_=0.0, precision=QJG_FP32, stream=None):
+    """Device L-BFGS fit; returns (energies per step, stats dict)."""
+    en = np.zeros(steps + 1)
+    st = QjgFitStats()
+    self._check(self.L.qjg_fit_lbfgs(self.h, C.c_void_p(d_params), n_top, n_bot, int(n),
+                                     C.c_void_p(d_xyz), C.c_void_p(d_target), float(slice_),
+                                     int(max_it), float(escape), int(precision), int(steps),
+                                     int(history), en.ctypes.data_as(_dp), C.byref(st),
+                                     C.c_void_p(stream or 0)), "qjg_fit_lbfgs")
+    d = {k: getattr(st, k) for k, _ in st._fields_}
+    return en[:st.steps + 1], d
+
+
+Context.fit_lbfgs = _fit
 
 
 def params_of(rs: RootSet):

@@ -1,9 +1,7 @@
 """Sample sets and target shapes of the differentiation workload.
 
-Samples: seeded Poisson-disk points in a box by phased dart throwing on a
-background grid (cell size r/sqrt(3) holds at most one point; cells whose
-indices agree mod 3 cannot conflict, so each of the 27 phases throws one dart
-into every empty cell of the phase at once).  The reference samples mesh
+Samples: seeded Poisson-disk points in a box by batched dart throwing on a
+background grid (cell size r/sqrt(3) holds at most one point).  The reference samples mesh
 surfaces with vcglib (projects/poissonDisk), which is not part of this path;
 this is a volume sampler of its own.
 
@@ -17,53 +15,55 @@ import numpy as np
 from .rootsets import draw_rootset, mt19937_rand
 
 
-def poisson_disk(n, lo=-1.0, hi=1.0, seed=0, radius=None, max_rounds=64):
-    """About n Poisson-disk points in [lo, hi]^3 (returns exactly n, shuffled)."""
+def poisson_disk(n, lo=-1.0, hi=1.0, seed=0, radius=None, batch=20000, max_batches=400):
+    """n Poisson-disk points in [lo, hi]^3: no two closer than `radius`.
+
+    Dart throwing in batches: each batch of uniform candidates is tested
+    against the accepted points through a background grid (cell size
+    r/sqrt(3), at most one point per cell, 5^3 neighbour cells), and
+    candidates of the same batch that conflict with an earlier candidate of
+    the batch are dropped (scipy's KD-tree finds those pairs)."""
+    from scipy.spatial import cKDTree
     rng = np.random.RandomState(seed)
     L = hi - lo
     if radius is None:
-        # dart throwing saturates near 0.6 of the densest packing; size r so
-        # that the box holds comfortably more than n points
         radius = (L ** 3 / (n * 1.6)) ** (1.0 / 3.0) * 0.78
     cs = radius / np.sqrt(3.0)
     G = int(np.ceil(L / cs))
-    grid = -np.ones((G, G, G), dtype=np.int64)
-    pts = np.empty((0, 3))
+    grid = -np.ones((G + 4, G + 4, G + 4), dtype=np.int64)  # 2-cell border
+    pts = np.empty((n, 3))
+    count = 0
     offs = np.array([(a, b, c) for a in range(-2, 3) for b in range(-2, 3) for c in range(-2, 3)])
-    phases = [(a, b, c) for a in range(3) for b in range(3) for c in range(3)]
-    for _ in range(max_rounds):
-        added = 0
-        for ph in phases:
-            ix = np.arange(ph[0], G, 3)
-            iy = np.arange(ph[1], G, 3)
-            iz = np.arange(ph[2], G, 3)
-            cells = np.stack(np.meshgrid(ix, iy, iz, indexing="ij"), -1).reshape(-1, 3)
-            cells = cells[grid[cells[:, 0], cells[:, 1], cells[:, 2]] < 0]
-            if len(cells) == 0:
-                continue
-            cand = lo + (cells + rng.uniform(size=cells.shape)) * cs
-            ok = np.all(cand < hi, axis=1)
-            nb = cells[:, None, :] + offs[None, :, :]
-            inside = np.all((nb >= 0) & (nb < G), axis=2)
-            nbc = np.clip(nb, 0, G - 1)
-            idx = grid[nbc[..., 0], nbc[..., 1], nbc[..., 2]]
-            idx = np.where(inside, idx, -1)
-            has = idx >= 0
-            if len(pts):
-                q = pts[np.maximum(idx, 0)]
-                d2 = np.sum((q - cand[:, None, :]) ** 2, axis=2)
-                ok &= ~np.any(has & (d2 < radius * radius), axis=1)
-            keep = np.nonzero(ok)[0]
-            base = len(pts)
-            pts = np.concatenate([pts, cand[keep]])
-            grid[cells[keep, 0], cells[keep, 1], cells[keep, 2]] = base + np.arange(len(keep))
-            added += len(keep)
-        if len(pts) >= n * 1.05 or added == 0:
-            break
-    if len(pts) < n:
-        raise RuntimeError("Poisson disk sampler saturated at %d < %d points" % (len(pts), n))
-    sel = rng.permutation(len(pts))[:n]
-    return pts[sel], radius
+    r2 = radius * radius
+    for _ in range(max_batches):
+        cand = lo + L * rng.uniform(size=(batch, 3))
+        cell = np.minimum(((cand - lo) / cs).astype(np.int64), G - 1) + 2
+        nb = cell[:, None, :] + offs[None, :, :]
+        idx = grid[nb[..., 0], nb[..., 1], nb[..., 2]]
+        has = idx >= 0
+        if count:
+            q = pts[np.maximum(idx, 0)]
+            d2 = np.sum((q - cand[:, None, :]) ** 2, axis=2)
+            ok = ~np.any(has & (d2 < r2), axis=1)
+        else:
+            ok = np.ones(batch, dtype=bool)
+        # a cell already holding a point rejects (it is within r/... of it anyway)
+        ok &= grid[cell[:, 0], cell[:, 1], cell[:, 2]] < 0
+        sel = np.nonzero(ok)[0]
+        if len(sel) > 1:
+            pairs = cKDTree(cand[sel]).query_pairs(radius, output_type="ndarray")
+            if len(pairs):
+                drop = np.zeros(len(sel), dtype=bool)
+                drop[np.maximum(pairs[:, 0], pairs[:, 1])] = True
+                sel = sel[~drop]
+        # two survivors may share a cell only if closer than r/sqrt(3)*sqrt(3) = r: excluded above
+        take = sel[:n - count]
+        pts[count:count + len(take)] = cand[take]
+        grid[cell[take, 0], cell[take, 1], cell[take, 2]] = count + np.arange(len(take))
+        count += len(take)
+        if count >= n:
+            return pts, radius
+    raise RuntimeError("Poisson disk sampler reached %d < %d points" % (count, n))
 
 
 def _rot(u):
