@@ -222,6 +222,77 @@ int qjg_fit_lbfgs(qjg_ctx* ctx, double* d_params, int32_t n_top, int32_t n_bot, 
                   double escape, int32_t precision, int32_t steps, int32_t history,
                   double* energies, qjg_fit_stats* stats, void* stream);
 
+/* ---- serving ----------------------------------------------------------- */
+
+/* A continuous-batching request server (no reference counterpart: the
+ * reference runs one driver per job).  Requests are admitted as soon as a
+ * worker slot is free and their device-memory estimate fits the HBM budget;
+ * admitted requests run concurrently on their own streams, so work submitted
+ * while others run overlaps with them.  Inputs are copied at submission;
+ * output buffers (host) must stay valid until the request completes. */
+#define QJG_REQ_FIELD 0  /* field of a map on a grid (out_field: X*Y*Z doubles, optional) */
+#define QJG_REQ_MESH 1   /* streaming field + marching cubes (out_verts / out_tris optional) */
+#define QJG_REQ_ENERGY 2 /* squared-error energy + gradient (params/xyz/target; out_grad) */
+
+#define QJG_STATUS_QUEUED 0
+#define QJG_STATUS_RUNNING 1
+#define QJG_STATUS_DONE 2
+#define QJG_STATUS_FAILED 3
+
+typedef struct qjg_server qjg_server;
+
+typedef struct {
+  int32_t kind;      /* QJG_REQ_* */
+  int32_t precision; /* field/mesh: QJG_FP64 or QJG_FP32_REFINE; energy: QJG_FP32 or QJG_FP64 */
+  int32_t n_top, n_bot;
+  const double* top_roots; /* field / mesh: the map as in qjg_rootset_upload */
+  const double* top_powers;
+  const double* bot_roots;
+  const double* bot_powers;
+  double sigma_top, sigma_bot, scale;
+  qjg_grid grid;    /* field / mesh; energy uses grid.slice only */
+  int32_t max_it;
+  double escape;
+  double iso;       /* mesh */
+  int64_t vert_cap, tri_cap; /* mesh output capacities */
+  const double* params; /* energy: parameter vector (layout of qjg_energy_backward) */
+  int64_t n_samples;
+  const double* xyz;
+  const double* target;
+  double* out_field;  /* host outputs, optional */
+  double* out_verts;
+  int32_t* out_tris;
+  double* out_grad;
+} qjg_request;
+
+typedef struct {
+  int32_t status; /* QJG_STATUS_* */
+  int32_t error;  /* QJG_OK or the failing entry point's code */
+  double latency_ms, queue_ms, run_ms;
+  double t_admit_ms, t_done_ms; /* since the server was created */
+  int64_t voxel_iters, refined;
+  int64_t n_verts, n_tris;
+  double energy;
+} qjg_result;
+
+typedef struct {
+  int64_t completed, failed;
+  double p50_ms, p99_ms, max_ms; /* submission-to-completion latency of completed requests */
+  double span_s;                 /* first submission to last completion */
+  int64_t in_use_bytes;          /* device-memory estimate of the running requests */
+  int64_t peak_in_use_bytes;
+  int32_t peak_running;          /* most requests running at once */
+} qjg_server_stats;
+
+int qjg_server_create(int device, int32_t workers, int64_t hbm_budget_bytes, qjg_server** out);
+void qjg_server_destroy(qjg_server* srv); /* drains first */
+int qjg_server_submit(qjg_server* srv, const qjg_request* req, int64_t* ticket);
+int qjg_server_poll(qjg_server* srv, int64_t ticket, qjg_result* out);
+/* waits for the ticket, returns its result and forgets it */
+int qjg_server_wait(qjg_server* srv, int64_t ticket, qjg_result* out);
+int qjg_server_drain(qjg_server* srv);
+int qjg_server_read_stats(qjg_server* srv, qjg_server_stats* out);
+
 #ifdef __cplusplus
 }
 #endif

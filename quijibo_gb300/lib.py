@@ -72,6 +72,38 @@ class QjgFitStats(C.Structure):
                 ("energy0", C.c_double), ("energy", C.c_double)]
 
 
+QJG_REQ_FIELD, QJG_REQ_MESH, QJG_REQ_ENERGY = 0, 1, 2
+QJG_STATUS_QUEUED, QJG_STATUS_RUNNING, QJG_STATUS_DONE, QJG_STATUS_FAILED = 0, 1, 2, 3
+
+
+class QjgRequest(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("precision", C.c_int32), ("n_top", C.c_int32),
+                ("n_bot", C.c_int32), ("top_roots", _dp), ("top_powers", _dp), ("bot_roots", _dp),
+                ("bot_powers", _dp), ("sigma_top", C.c_double), ("sigma_bot", C.c_double),
+                ("scale", C.c_double), ("grid", QjgGrid), ("max_it", C.c_int32),
+                ("escape", C.c_double), ("iso", C.c_double), ("vert_cap", C.c_int64),
+                ("tri_cap", C.c_int64), ("params", _dp), ("n_samples", C.c_int64), ("xyz", _dp),
+                ("target", _dp), ("out_field", _dp), ("out_verts", _dp),
+                ("out_tris", C.POINTER(C.c_int32)), ("out_grad", _dp)]
+
+
+class QjgResult(C.Structure):
+    _fields_ = [("status", C.c_int32), ("error", C.c_int32), ("latency_ms", C.c_double),
+                ("queue_ms", C.c_double), ("run_ms", C.c_double), ("t_admit_ms", C.c_double),
+                ("t_done_ms", C.c_double), ("voxel_iters", C.c_int64), ("refined", C.c_int64),
+                ("n_verts", C.c_int64), ("n_tris", C.c_int64), ("energy", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class QjgServerStats(C.Structure):
+    _fields_ = [("completed", C.c_int64), ("failed", C.c_int64), ("p50_ms", C.c_double),
+                ("p99_ms", C.c_double), ("max_ms", C.c_double), ("span_s", C.c_double),
+                ("in_use_bytes", C.c_int64), ("peak_in_use_bytes", C.c_int64),
+                ("peak_running", C.c_int32)]
+
+
 EXPORTS = {
     "qjg_create": ([C.c_int, C.POINTER(C.c_void_p)], C.c_int),
     "qjg_destroy": ([C.c_void_p], None),
@@ -102,6 +134,13 @@ EXPORTS = {
     "qjg_fit_lbfgs": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p,
                        C.c_void_p, C.c_double, C.c_int32, C.c_double, C.c_int32, C.c_int32,
                        C.c_int32, _dp, C.POINTER(QjgFitStats), C.c_void_p], C.c_int),
+    "qjg_server_create": ([C.c_int, C.c_int32, C.c_int64, C.POINTER(C.c_void_p)], C.c_int),
+    "qjg_server_destroy": ([C.c_void_p], None),
+    "qjg_server_submit": ([C.c_void_p, C.POINTER(QjgRequest), C.POINTER(C.c_int64)], C.c_int),
+    "qjg_server_poll": ([C.c_void_p, C.c_int64, C.POINTER(QjgResult)], C.c_int),
+    "qjg_server_wait": ([C.c_void_p, C.c_int64, C.POINTER(QjgResult)], C.c_int),
+    "qjg_server_drain": ([C.c_void_p], C.c_int),
+    "qjg_server_read_stats": ([C.c_void_p, C.POINTER(QjgServerStats)], C.c_int),
     # measurement hooks (include/quijibo_gpu_bench.h)
     "qjg_set_timing": ([C.c_void_p, C.c_int], C.c_int),
     "qjg_last_timings": ([C.c_void_p, _fp, _fp], C.c_int),
@@ -325,3 +364,75 @@ def rootset_of(params, n_top, n_bot):
     return RootSet(top_roots=r[:n_top].copy(), top_powers=e[:n_top].copy(),
                    bottom_roots=r[n_top:].copy(), bottom_powers=e[n_top:].copy(),
                    scale=float(np.exp(p[5 * nr])))
+
+
+class Server:
+    """Continuous-batching request server (qjg_server_*)."""
+
+    def __init__(self, device=0, workers=8, hbm_budget=64 << 30):
+        self.L = load()
+        h = C.c_void_p()
+        rc = self.L.qjg_server_create(device, workers, int(hbm_budget), C.byref(h))
+        if rc != 0:
+            raise QjgError("qjg_server_create failed (%d)" % rc)
+        self.h = h
+        self._keep = {}
+
+    def close(self):
+        if self.h:
+            self.L.qjg_server_destroy(self.h)
+            self.h = None
+
+    def submit(self, kind, rs=None, grid=None, max_it=20, escape=2.0, precision=QJG_FP32_REFINE,
+               iso=0.0, vert_cap=0, tri_cap=0, params=None, xyz=None, target=None,
+               out_field=None, out_verts=None, out_tris=None, out_grad=None):
+        r = QjgRequest()
+        r.kind, r.precision, r.max_it, r.escape, r.iso = kind, precision, max_it, escape, iso
+        keep = []
+
+        def arr(a, shape=None):
+            a = _arr(a, shape)
+            keep.append(a)
+            return a.ctypes.data_as(_dp) if a.size else None
+
+        if rs is not None:
+            r.n_top, r.n_bot = rs.n_top, rs.n_bottom
+            r.top_roots, r.top_powers = arr(rs.top_roots, (-1, 4)), arr(rs.top_powers)
+            r.bot_roots, r.bot_powers = arr(rs.bottom_roots, (-1, 4)), arr(rs.bottom_powers)
+            r.sigma_top, r.sigma_bot, r.scale = rs.sigma_top, rs.sigma_bottom, rs.scale
+        if grid is not None:
+            r.grid = QjgGrid.of(grid)
+        r.vert_cap, r.tri_cap = int(vert_cap), int(tri_cap)
+        if params is not None:
+            r.params = arr(params)
+            r.n_samples = len(target)
+            r.xyz, r.target = arr(xyz, (-1, 3)), arr(target)
+        for name, a in (("out_field", out_field), ("out_verts", out_verts), ("out_grad", out_grad)):
+            if a is not None:
+                keep.append(a)
+                setattr(r, name, a.ctypes.data_as(_dp))
+        if out_tris is not None:
+            keep.append(out_tris)
+            r.out_tris = out_tris.ctypes.data_as(C.POINTER(C.c_int32))
+        t = C.c_int64()
+        rc = self.L.qjg_server_submit(self.h, C.byref(r), C.byref(t))
+        if rc != 0:
+            raise QjgError("qjg_server_submit failed (%d)" % rc)
+        self._keep[t.value] = keep
+        return t.value
+
+    def wait(self, ticket):
+        res = QjgResult()
+        rc = self.L.qjg_server_wait(self.h, ticket, C.byref(res))
+        if rc != 0:
+            raise QjgError("qjg_server_wait failed (%d)" % rc)
+        self._keep.pop(ticket, None)
+        return res.as_dict()
+
+    def drain(self):
+        self.L.qjg_server_drain(self.h)
+
+    def stats(self):
+        st = QjgServerStats()
+        self.L.qjg_server_read_stats(self.h, C.byref(st))
+        return {k: getattr(st, k) for k, _ in st._fields_}

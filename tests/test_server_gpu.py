@@ -1,0 +1,109 @@
+"""Continuous-batching server: results are the same alone and in the mix,
+admission respects the HBM budget, and admitted work overlaps."""
+import numpy as np
+import pytest
+
+from quijibo_gb300 import lib
+from quijibo_gb300.rootsets import Grid, conformal_scale, draw_rootset
+from quijibo_gb300.samples import ShapeSDF, poisson_disk
+
+pytestmark = pytest.mark.gpu
+
+
+def mixed_requests(seed=0, n=24):
+    rng = np.random.RandomState(seed)
+    reqs = []
+    for i in range(n):
+        kind = [lib.QJG_REQ_FIELD, lib.QJG_REQ_MESH, lib.QJG_REQ_ENERGY][i % 3]
+        nt = int(rng.randint(4, 17))
+        nb = int(rng.randint(0, 6))
+        rs = draw_rootset(100 + i, nt, nb, -1.2, 1.2, exps=(1, 2))
+        res = int(rng.choice([16, 24, 32, 48]))
+        g = Grid((res, res, res))
+        rs.scale = conformal_scale(rs, g, sample_res=16)
+        max_it = int(rng.randint(5, 21))
+        if kind == lib.QJG_REQ_ENERGY:
+            xyz, _ = poisson_disk(500, seed=i)
+            reqs.append(dict(kind=kind, rs=rs, params=lib.params_of(rs), xyz=xyz,
+                             target=ShapeSDF(i)(xyz), max_it=max_it, precision=lib.QJG_FP32))
+        else:
+            reqs.append(dict(kind=kind, rs=rs, grid=g, max_it=max_it,
+                             precision=[lib.QJG_FP64, lib.QJG_FP32_REFINE][i % 2]))
+    return reqs
+
+
+def run(server, reqs):
+    tickets, outs = [], []
+    for r in reqs:
+        o = {}
+        kw = dict(r)
+        if r["kind"] == lib.QJG_REQ_FIELD:
+            o["field"] = np.empty(r["grid"].n_voxels)
+            kw["out_field"] = o["field"]
+        elif r["kind"] == lib.QJG_REQ_MESH:
+            cap = 3 * r["grid"].n_voxels
+            o["verts"] = np.empty(3 * cap)
+            o["tris"] = np.empty(3 * 2 * cap, dtype=np.int32)
+            kw.update(vert_cap=cap, tri_cap=2 * cap, out_verts=o["verts"], out_tris=o["tris"])
+        else:
+            o["grad"] = np.empty(len(r["params"]))
+            kw["out_grad"] = o["grad"]
+        kw.pop("rs") if r["kind"] == lib.QJG_REQ_ENERGY else None
+        if r["kind"] == lib.QJG_REQ_ENERGY:
+            kw["rs"] = r["rs"]
+        tickets.append(server.submit(**kw))
+        outs.append(o)
+    results = [server.wait(t) for t in tickets]
+    for o, res in zip(outs, results):
+        assert res["status"] == lib.QJG_STATUS_DONE, res
+        if "verts" in o:
+            o["verts"] = o["verts"][:3 * res["n_verts"]].copy()
+            o["tris"] = o["tris"][:3 * res["n_tris"]].copy()
+        o["energy"] = res["energy"]
+    return outs, results
+
+
+def test_results_same_alone_and_in_the_mix():
+    reqs = mixed_requests()
+    mix_srv = lib.Server(workers=6, hbm_budget=2 << 30)
+    mixed, mres = run(mix_srv, reqs)
+    st = mix_srv.stats()
+    mix_srv.close()
+    assert st["completed"] == len(reqs) and st["failed"] == 0
+    assert st["peak_running"] >= 2  # work overlapped on the device
+    alone_srv = lib.Server(workers=1, hbm_budget=2 << 30)
+    for r, m in zip(reqs, mixed):
+        a, _ = run(alone_srv, [r])
+        a = a[0]
+        for k in m:
+            if isinstance(m[k], np.ndarray):
+                np.testing.assert_array_equal(m[k], a[k], err_msg=k)
+            else:
+                assert m[k] == a[k], k
+    alone_srv.close()
+
+
+def test_budget_limits_concurrency():
+    reqs = [r for r in mixed_requests(seed=1) if r["kind"] == lib.QJG_REQ_FIELD]
+    srv = lib.Server(workers=8, hbm_budget=1)  # every request exceeds it: one at a time
+    _, res = run(srv, reqs)
+    st = srv.stats()
+    srv.close()
+    assert st["peak_running"] == 1
+    spans = sorted((r["t_admit_ms"], r["t_done_ms"]) for r in res)
+    for (a0, d0), (a1, d1) in zip(spans, spans[1:]):
+        assert a1 >= d0 - 1e-6
+
+
+def test_server_matches_direct_calls(ctx):
+    reqs = [r for r in mixed_requests(seed=2) if r["kind"] == lib.QJG_REQ_FIELD][:3]
+    srv = lib.Server(workers=3)
+    outs, _ = run(srv, reqs)
+    srv.close()
+    for r, o in zip(reqs, outs):
+        h = ctx.upload(r["rs"])
+        it = ctx.iter_params(r["max_it"], 2.0, precision=r["precision"],
+                             refine_pow=lib.QJG_REFINE_INT)
+        f, _, _ = ctx.field_host(h, r["grid"], it)
+        ctx.free(h)
+        np.testing.assert_array_equal(f.reshape(-1), o["field"])
