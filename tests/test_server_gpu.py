@@ -48,9 +48,6 @@ def run(server, reqs):
         else:
             o["grad"] = np.empty(len(r["params"]))
             kw["out_grad"] = o["grad"]
-        kw.pop("rs") if r["kind"] == lib.QJG_REQ_ENERGY else None
-        if r["kind"] == lib.QJG_REQ_ENERGY:
-            kw["rs"] = r["rs"]
         tickets.append(server.submit(**kw))
         outs.append(o)
     results = [server.wait(t) for t in tickets]
