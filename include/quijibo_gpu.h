@@ -105,6 +105,27 @@ int qjg_field_host(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg
 /* Counters of the last qjg_field call on ctx; synchronizes `stream`. */
 int qjg_field_stats_read(qjg_ctx* ctx, void* stream, qjg_field_stats* out);
 
+/* The field, for callers that cannot allocate device memory: code running
+ * while a stream is captured into a CUDA graph, plugins whose host runtime
+ * owns every device allocation, real-time loops that must not reach the
+ * allocator.  No counterpart in the reference.  The map comes as host arrays
+ * (as in qjg_rootset_upload), the output is a device buffer as in qjg_field;
+ * no context is needed and nothing is allocated: the counters and the FP64
+ * refine list live in a fixed scratch array inside the library (about
+ * 16 MiB, held on every device that loads the library until the process
+ * exits).  One call covers at most QJG_NOALLOC_MAX_VOXELS voxels (X*Y*(z1-z0));
+ * larger slab ranges return QJG_ERR_CAPACITY before anything is launched.
+ * The first call on a device looks up the scratch array's device address, so
+ * make it before any stream capture.  Every call shares the scratch array:
+ * calls whose work overlaps on the GPU (different streams or host threads)
+ * race on it and must be serialised by the caller. */
+#define QJG_NOALLOC_MAX_VOXELS (1 << 22)
+int qjg_field_noalloc(int32_t n_top, const double* top_roots, const double* top_powers,
+                      double sigma_top, int32_t n_bot, const double* bot_roots,
+                      const double* bot_powers, double sigma_bot, double scale,
+                      const qjg_grid* grid, const qjg_iter* iter, int32_t z0, int32_t z1,
+                      double* d_field, float* d_de, void* stream);
+
 /* ---- marching cubes ---------------------------------------------------- */
 
 /* Edge-vertex placement. */

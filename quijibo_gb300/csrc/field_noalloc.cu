@@ -1,0 +1,118 @@
+// Field entry point that allocates no device memory.
+//
+// Some callers of this library cannot allocate device memory on the path
+// that computes a field: code running while a stream is being captured into
+// a CUDA graph (where cudaMalloc is not allowed), plugins hosted by a runtime
+// that owns every device allocation, and real-time loops that must not hit
+// the allocator.  qjg_field_noalloc serves them.  The caller passes the map
+// (host arrays), the grid, the iteration settings and a device output
+// buffer; the only device memory the call touches besides that buffer is a
+// fixed scratch array of this file (the refine list and the counters of the
+// FP32 + FP64-refine form), which lives for as long as the library is loaded
+// on a device.  Every call shares that array, so calls whose work overlaps
+// on the GPU (different streams, or different host threads) race on it and
+// must be serialised by the caller.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
+#include "../../include/quijibo_gpu.h"
+#include "qj_ctx.h"
+#include "qj_kernels.h"
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+
+// [0, 256): the counters (qj::DevStats, padded); then one uint32 list entry
+// per voxel of the largest launch.
+constexpr size_t kStatsBytes = 256;
+constexpr size_t kScratchBytes = kStatsBytes + sizeof(uint32_t) * (size_t)QJG_NOALLOC_MAX_VOXELS;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+std::mutex g_setup_mu;
+unsigned char* g_scratch_addr[kMaxDevices] = {};
+
+// The device address of the scratch array for the current device, looked up
+// once per device (host code must not use the symbol itself as an address).
+int scratch_for_current_device(unsigned char** out) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return QJG_ERR_CUDA;
+  std::lock_guard<std::mutex> lk(g_setup_mu);
+  if (!g_scratch_addr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return QJG_ERR_CUDA;
+    g_scratch_addr[dev] = static_cast<unsigned char*>(p);
+  }
+  *out = g_scratch_addr[dev];
+  return QJG_OK;
+}
+
+}  // namespace
+
+extern "C" int qjg_field_noalloc(int32_t n_top, const double* top_roots, const double* top_powers,
+                                 double sigma_top, int32_t n_bot, const double* bot_roots,
+                                 const double* bot_powers, double sigma_bot, double scale,
+                                 const qjg_grid* grid, const qjg_iter* iter, int32_t z0, int32_t z1,
+                                 double* d_field, float* d_de, void* stream) {
+  if (n_top < 1 || n_bot < 0 || n_top + n_bot > QJG_MAX_ROOTS) return QJG_ERR_ARG;
+  if (!top_roots || !top_powers || (n_bot > 0 && (!bot_roots || !bot_powers)) || !d_field)
+    return QJG_ERR_ARG;
+  int rc;
+  if ((rc = qj_check_grid(nullptr, grid)) || (rc = qj_check_iter(nullptr, iter))) return rc;
+  if (z0 < 0 || z1 > grid->res[2] || z0 >= z1) return QJG_ERR_ARG;
+  const int64_t n = (int64_t)grid->res[0] * grid->res[1] * (z1 - z0);
+  if (n > (int64_t)QJG_NOALLOC_MAX_VOXELS) return QJG_ERR_CAPACITY;
+
+  // the map's launch parameters, built on the host stack
+  qj::MapParams m;
+  std::memset(&m, 0, sizeof m);
+  m.nt = n_top;
+  m.nb = n_bot;
+  m.scale = scale;
+  m.scalef = (float)scale;
+  m.sigma[0] = sigma_top;
+  m.sigma[1] = sigma_bot;
+  m.all_int = 1;
+  for (int i = 0; i < n_top + n_bot; i++) {
+    const bool top = i < n_top;
+    const double* r = top ? top_roots + 4 * i : bot_roots + 4 * (i - n_top);
+    const double pw = top ? top_powers[i] : bot_powers[i - n_top];
+    const double e = (top ? sigma_top : sigma_bot) * pw;
+    for (int c = 0; c < 4; c++) {
+      if (!std::isfinite(r[c])) return QJG_ERR_ARG;
+      m.r64[i][c] = r[c];
+      m.r32[i][c] = (float)r[c];
+    }
+    if (!std::isfinite(e)) return QJG_ERR_ARG;
+    m.e64[i] = e;
+    m.ep[i] = pw;
+    m.e32[i] = (float)e;
+    const bool integral = (e == std::floor(e)) && e >= 1 && e <= QJ_MAX_INT_EXP;
+    m.ie[i] = integral ? (int)e : 0;
+    if (!integral) m.all_int = 0;
+  }
+
+  unsigned char* scratch = nullptr;
+  if ((rc = scratch_for_current_device(&scratch))) return rc;
+  qj::DevStats* st = reinterpret_cast<qj::DevStats*>(scratch);
+  uint32_t* list = reinterpret_cast<uint32_t*>(scratch + kStatsBytes);
+
+  cudaStream_t s = (cudaStream_t)stream;
+  const qj::GridParams g = qj_grid_params(grid, z0, z1);
+  const qj::IterParams it = qj_iter_params(iter, grid);
+  const bool refine = iter->precision == QJG_FP32_REFINE;
+  const bool pow_ref = iter->refine_pow == QJG_REFINE_POW || !m.all_int;
+  // the counters (work-queue position, refine-list length) start at zero
+  if (cudaMemsetAsync(st, 0, sizeof(qj::DevStats), s) != cudaSuccess) return QJG_ERR_CUDA;
+  cudaError_t e;
+  if (iter->precision == QJG_FP64)
+    e = qj::launch_field64(m, g, it, pow_ref, d_field, d_de, st, s);
+  else
+    e = qj::launch_field32(m, g, it, refine, d_field, d_de, list, st, s);
+  if (e == cudaSuccess && refine) e = qj::launch_refine64(m, g, it, pow_ref, list, d_field, d_de, st, s);
+  return e == cudaSuccess ? QJG_OK : QJG_ERR_CUDA;
+}

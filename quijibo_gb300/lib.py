@@ -116,6 +116,9 @@ EXPORTS = {
     "qjg_field_host": ([C.c_void_p, C.c_int32, C.POINTER(QjgGrid), C.POINTER(QjgIter), _dp, _fp,
                         C.POINTER(QjgFieldStats)], C.c_int),
     "qjg_field_stats_read": ([C.c_void_p, C.c_void_p, C.POINTER(QjgFieldStats)], C.c_int),
+    "qjg_field_noalloc": ([C.c_int32, _dp, _dp, C.c_double, C.c_int32, _dp, _dp, C.c_double,
+                           C.c_double, C.POINTER(QjgGrid), C.POINTER(QjgIter), C.c_int32,
+                           C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "qjg_mesh_field": ([C.c_void_p, C.c_int32, C.POINTER(QjgGrid), C.POINTER(QjgIter), C.c_void_p,
                         C.c_int32, C.c_double, C.c_int32, C.c_void_p, C.c_void_p, C.c_int64,
                         C.c_void_p, C.c_int64, C.POINTER(QjgMeshStats), C.c_void_p], C.c_int),
