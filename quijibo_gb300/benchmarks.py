@@ -1,0 +1,229 @@
+"""Measurements of the mesher, the energies and the server (beside bench.py,
+which measures the headline field).  Each prints one JSON object.
+
+    python -m quijibo_gb300.benchmarks mesh   [--res 512] [--workload precision|large]
+    python -m quijibo_gb300.benchmarks energy [--samples 200000] [--steps 50]
+    python -m quijibo_gb300.benchmarks serve  [--requests 400] [--scale 0.25]
+
+All inputs are synthetic (quijibo_gb300/rootsets.py, samples.py).
+"""
+import argparse
+import json
+import statistics
+import time
+
+import numpy as np
+
+
+def _events(torch):
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def bench_mesh(args):
+    """Streaming mesher (field slab + classify/scan/emit + FP64 bisection) on
+    the precision or large workload; reports triangles/s and the time split."""
+    import torch
+
+    from . import lib
+    from .rootsets import large_workload, precision_workload
+    ctx = lib.Context(0)
+    wl = precision_workload if args.workload == "precision" else large_workload
+    rs, g, p = wl(args.res)
+    h = ctx.upload(rs)
+    it = ctx.iter_params(p["max_it"], p["escape"], precision=lib.QJG_FP32_REFINE,
+                         refine_pow=lib.QJG_REFINE_INT)
+    # capacities from a coarse pass scale with the surface (about res^2)
+    vcap = int(args.vert_cap or 12 * g.res[0] * g.res[1])
+    tcap = int(args.tri_cap or 24 * g.res[0] * g.res[1])
+    v32 = torch.empty(3 * vcap, dtype=torch.float32, device="cuda")
+    tris = torch.empty(3 * tcap, dtype=torch.int32, device="cuda")
+    kw = dict(d_verts32=v32.data_ptr(), vert_cap=vcap, d_tris=tris.data_ptr(), tri_cap=tcap,
+              slab_nz=args.slab)
+    rc, st = ctx.mesh_stream(h, g, it, check=False, **kw)  # warm-up, and sizes
+    if rc == -5:
+        raise SystemExit("raise --vert-cap/--tri-cap: needs %d / %d" % (st["n_verts"], st["n_tris"]))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _, st = ctx.mesh_stream(h, g, it, **kw)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    # the field alone over the same grid, for the split
+    f = torch.empty(g.res[0] * g.res[1] * min(g.res[2], args.slab + 1), dtype=torch.float64,
+                    device="cuda")
+    ctx.set_timing(True)
+    field_ms = 0.0
+    for z0 in range(0, g.res[2], args.slab + 1):
+        z1 = min(z0 + args.slab + 1, g.res[2])
+        ctx.field(h, g, it, f.data_ptr(), z0=z0, z1=z1)
+        b, r = ctx.last_timings()
+        field_ms += b + r
+    return {"workload": "%s %d^3" % (args.workload, args.res), "voxels": g.n_voxels,
+            "triangles": st["n_tris"], "vertices": st["n_verts"], "wall_s": wall,
+            "triangles_per_s": st["n_tris"] / wall, "gvox_s": g.n_voxels / wall / 1e9,
+            "field_only_s": field_ms / 1e3, "mesher_s": wall - field_ms / 1e3,
+            "bisection_map_evals": st["map_evals"], "unbracketed": st["n_unbracketed"],
+            "degenerate": st["n_degenerate"], "slabs": st["slabs"],
+            "refined": st["field"]["refined"]}
+
+
+def bench_energy(args):
+    """Differentiation workload: 64 top / 16 bottom roots, Poisson-disk
+    samples, 30 iterations; FP32 forward, FP32 recompute adjoint, device
+    L-BFGS."""
+    import torch
+
+    from . import lib
+    from .samples import differentiation_workload
+    ctx = lib.Context(0)
+    rs, xyz, t, p = differentiation_workload(args.samples)
+    P = torch.from_numpy(lib.params_of(rs)).cuda()
+    X = torch.from_numpy(xyz).cuda()
+    T = torch.from_numpy(t).cuda()
+    G = torch.empty_like(P)
+    n = len(t)
+    out = {"samples": n, "params": int(P.numel()), "max_it": p["max_it"]}
+    for name, prec, grad in (("forward_fp32", lib.QJG_FP32, False), ("adjoint_fp32", lib.QJG_FP32, True),
+                             ("forward_fp64", lib.QJG_FP64, False), ("adjoint_fp64", lib.QJG_FP64, True)):
+        kw = dict(precision=prec, d_grad=G.data_ptr() if grad else 0)
+        ctx.energy(P.data_ptr(), rs.n_top, rs.n_bottom, n, X.data_ptr(), T.data_ptr(), p["max_it"],
+                   p["escape"], **kw)
+        torch.cuda.synchronize()
+        reps = 3
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            e = ctx.energy(P.data_ptr(), rs.n_top, rs.n_bottom, n, X.data_ptr(), T.data_ptr(),
+                           p["max_it"], p["escape"], **kw)
+        dt = (time.perf_counter() - t0) / reps
+        out[name] = {"s": dt, "samples_per_s": n / dt, "energy": e}
+    out["gradients_per_s"] = 1.0 / out["adjoint_fp32"]["s"]
+    Pfit = P.clone()
+    t0 = time.perf_counter()
+    en, st = ctx.fit_lbfgs(Pfit.data_ptr(), rs.n_top, rs.n_bottom, n, X.data_ptr(), T.data_ptr(),
+                           p["max_it"], p["escape"], steps=args.steps, precision=lib.QJG_FP32)
+    out["lbfgs"] = dict(st, wall_s=time.perf_counter() - t0,
+                        energies=[float(v) for v in en[:: max(1, len(en) // 10)]])
+    return out
+
+
+def _stream(seed, n, scale):
+    """Poisson-arrival mix of field, field+mesh and energy+gradient requests:
+    grid sides log-uniform in [32, 512] (field) and [128, 1024] (mesh) times
+    `scale`, 10k-200k samples times `scale`, 4-64 roots, 10-60 iterations."""
+    from . import lib
+    from .rootsets import Grid, conformal_scale, draw_rootset
+    from .samples import ShapeSDF, poisson_disk
+    rng = np.random.RandomState(seed)
+    reqs = []
+    for i in range(n):
+        kind = rng.choice([lib.QJG_REQ_FIELD, lib.QJG_REQ_MESH, lib.QJG_REQ_ENERGY], p=[0.5, 0.2, 0.3])
+        nr = int(rng.randint(4, 65))
+        nb = int(rng.randint(0, nr // 3 + 1))
+        rs = draw_rootset(1000 + i, nr - nb if nr - nb >= 1 else 1, nb, -1.2, 1.2, exps=(1, 2))
+        max_it = int(rng.randint(10, 61))
+        if kind == lib.QJG_REQ_ENERGY:
+            ns = int(np.exp(rng.uniform(np.log(10_000), np.log(200_000))) * scale)
+            xyz, _ = poisson_disk(max(ns, 64), seed=i)
+            rs.scale = conformal_scale(rs, Grid((16, 16, 16), lengths=(2.0, 2.0, 2.0)), 16)
+            reqs.append(dict(kind=kind, rs=rs, params=lib.params_of(rs), xyz=xyz,
+                             target=ShapeSDF(i)(xyz), max_it=max_it, precision=lib.QJG_FP32))
+        else:
+            lo, hi = (32, 512) if kind == lib.QJG_REQ_FIELD else (128, 1024)
+            res = max(8, int(np.exp(rng.uniform(np.log(lo), np.log(hi))) * scale))
+            g = Grid((res, res, res))
+            rs.scale = conformal_scale(rs, g, 16)
+            r = dict(kind=kind, rs=rs, grid=g, max_it=max_it, precision=lib.QJG_FP32_REFINE)
+            if kind == lib.QJG_REQ_MESH:
+                r.update(vert_cap=12 * res * res + 1024, tri_cap=24 * res * res + 1024)
+            reqs.append(r)
+    return reqs
+
+
+def bench_serve(args):
+    """Serving: Poisson arrivals into the continuous-batching server vs the
+    same requests as plain FP64 launches one after another."""
+    from . import lib
+    reqs = _stream(args.seed, args.requests, args.scale)
+    # offered load: mean gap chosen so the stream arrives over --span seconds
+    rng = np.random.RandomState(args.seed + 1)
+    gaps = rng.exponential(args.span / len(reqs), size=len(reqs))
+    srv = lib.Server(workers=args.workers, hbm_budget=int(args.budget_gb * (1 << 30)))
+    # warm the workers' modules
+    srv.wait(srv.submit(**reqs[0]))
+    t0 = time.perf_counter()
+    tickets = []
+    for r, gap in zip(reqs, gaps):
+        target = time.perf_counter() + gap
+        while time.perf_counter() < target:
+            pass
+        tickets.append(srv.submit(**r))
+    results = [srv.wait(t) for t in tickets]
+    span = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    lat = np.array([r["latency_ms"] for r in results])
+    vox = sum(r["grid"].n_voxels for r in reqs if "grid" in r)
+    out = {"requests": len(reqs), "scale": args.scale, "workers": args.workers,
+           "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+           "max_ms": float(lat.max()), "throughput_req_s": len(reqs) / span,
+           "gvox_s": vox / span / 1e9, "span_s": span, "peak_running": st["peak_running"],
+           "failed": st["failed"]}
+    # baseline: a sample of the same requests, plain FP64, one at a time
+    ctx = lib.Context(0)
+    idx = list(range(0, len(reqs), max(1, len(reqs) // args.baseline_sample)))
+    base_t, serve_t = [], []
+    for i in idx:
+        r = reqs[i]
+        t1 = time.perf_counter()
+        if "grid" in r:
+            h = ctx.upload(r["rs"])
+            it = ctx.iter_params(r["max_it"], 2.0, precision=lib.QJG_FP64)
+            if r["kind"] == lib.QJG_REQ_FIELD:
+                ctx.field_host(h, r["grid"], it)
+            else:
+                import torch
+                v = torch.empty(3 * r["vert_cap"], dtype=torch.float64, device="cuda")
+                tt = torch.empty(3 * r["tri_cap"], dtype=torch.int32, device="cuda")
+                ctx.mesh_stream(h, r["grid"], it, d_verts64=v.data_ptr(), vert_cap=r["vert_cap"],
+                                d_tris=tt.data_ptr(), tri_cap=r["tri_cap"])
+            ctx.free(h)
+        else:
+            import torch
+            P = torch.from_numpy(r["params"]).cuda()
+            X = torch.from_numpy(r["xyz"]).cuda()
+            T = torch.from_numpy(r["target"]).cuda()
+            G = torch.empty_like(P)
+            ctx.energy(P.data_ptr(), r["rs"].n_top, r["rs"].n_bottom, len(r["target"]), X.data_ptr(),
+                       T.data_ptr(), r["max_it"], 2.0, precision=lib.QJG_FP64, d_grad=G.data_ptr())
+        base_t.append(time.perf_counter() - t1)
+        serve_t.append(results[i]["run_ms"] / 1e3)
+    out["baseline_fp64_serial"] = {
+        "sampled_requests": len(idx), "mean_s": statistics.mean(base_t),
+        "throughput_req_s_est": 1.0 / statistics.mean(base_t),
+        "served_run_s_same_requests": statistics.mean(serve_t)}
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("what", choices=["mesh", "energy", "serve"])
+    ap.add_argument("--res", type=int, default=512)
+    ap.add_argument("--workload", default="precision", choices=["precision", "large"])
+    ap.add_argument("--slab", type=int, default=64)
+    ap.add_argument("--vert-cap", type=int, default=0)
+    ap.add_argument("--tri-cap", type=int, default=0)
+    ap.add_argument("--samples", type=int, default=200_000)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--requests", type=int, default=400)
+    ap.add_argument("--scale", type=float, default=0.25)
+    ap.add_argument("--span", type=float, default=20.0)
+    ap.add_argument("--workers", type=int, default=8)
+    ap.add_argument("--budget-gb", type=float, default=64.0)
+    ap.add_argument("--baseline-sample", type=int, default=40)
+    ap.add_argument("--seed", type=int, default=0)
+    args = ap.parse_args()
+    fn = {"mesh": bench_mesh, "energy": bench_energy, "serve": bench_serve}[args.what]
+    print(json.dumps(fn(args)), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -175,6 +175,9 @@ int qjg_rootset_upload(qjg_ctx* ctx, int32_t n_top, const double* top_roots,
     const bool integral = (e == std::floor(e)) && e >= 1 && e <= QJ_MAX_INT_EXP;
     m->ie[i] = integral ? (int)e : 0;
     if (!integral) m->all_int = 0;
+    m->x32[i][0] = top ? (float)e : -(float)e;
+    const int ie_bits = m->ie[i];
+    std::memcpy(&m->x32[i][1], &ie_bits, sizeof ie_bits);
   }
   ctx->rootsets.push_back(std::move(m));
   *out = (qjg_rootset)(ctx->rootsets.size() - 1);

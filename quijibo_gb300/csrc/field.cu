@@ -114,34 +114,49 @@ __global__ void __launch_bounds__(128) refine64_kernel(const __grid_constant__ M
 
 // ------------------------------------------------------------------ FP32
 
+// Exponents other than 1 and 2 (kept out of line, off the hot path).
+__device__ __noinline__ q32::Q root_power_rare(q32::Q d, int ie, float e) {
+  return ie > 0 ? q32::qpow_int(d, ie) : q32::qpow(d, e);
+}
+
+// One root term (q - r_i)^(e_i) in FP32; with DE, adds (+-e_i) d/|d|^2 to g.
+// Root coordinates come as one 16-byte constant-bank load and {+-e, integer
+// exponent} as one 8-byte load.
+template <bool DE>
+__device__ __forceinline__ q32::Q root_term32(const MapParams& m, const q32::Q& q, int i,
+                                              q32::Q& g) {
+  using namespace q32;
+  const float4 root = *reinterpret_cast<const float4*>(m.r32[i]);
+  const float2 ex = *reinterpret_cast<const float2*>(m.x32[i]);
+  const Q d = {q.w - root.x, q.x - root.y, q.y - root.z, q.z - root.w};
+  if (DE) {
+    const float k = __fdividef(ex.x, norm2(d));
+    g.w = fmaf(k, d.w, g.w);
+    g.x = fmaf(k, d.x, g.x);
+    g.y = fmaf(k, d.y, g.y);
+    g.z = fmaf(k, d.z, g.z);
+  }
+  const int ie = __float_as_int(ex.y);
+  if (ie == 1) return d;
+  if (ie == 2) return qsq(d);
+  return root_power_rare(d, ie, m.e32[i]);
+}
+
+// prod_{i in [lo, hi)} (q - r_i)^(e_i), left to right; the first term starts
+// the product and the rest go two per trip.
 template <bool DE>
 __device__ __forceinline__ q32::Q product32(const MapParams& m, const q32::Q& q, int lo, int hi,
-                                            float sign, q32::Q& g) {
+                                            q32::Q& g) {
   using namespace q32;
-  Q r = {1.f, 0.f, 0.f, 0.f};
+  Q r = root_term32<DE>(m, q, lo, g);
+  int i = lo + 1;
 #pragma unroll 1
-  for (int i = lo; i < hi; i++) {
-    const float4 root = *reinterpret_cast<const float4*>(m.r32[i]);
-    const Q d = {q.w - root.x, q.x - root.y, q.y - root.z, q.z - root.w};
-    if (DE) {
-      const float k = __fdividef(sign * m.e32[i], norm2(d));
-      g.w = fmaf(k, d.w, g.w);
-      g.x = fmaf(k, d.x, g.x);
-      g.y = fmaf(k, d.y, g.y);
-      g.z = fmaf(k, d.z, g.z);
-    }
-    const int ie = m.ie[i];
-    Q t;
-    if (ie == 1)
-      t = d;
-    else if (ie == 2)
-      t = qsq(d);
-    else if (ie > 0)
-      t = qpow_int(d, ie);
-    else
-      t = qpow(d, m.e32[i]);
-    r = (i == lo) ? t : qmul(r, t);
+  for (; i + 1 < hi; i += 2) {
+    const Q t0 = root_term32<DE>(m, q, i, g);
+    const Q t1 = root_term32<DE>(m, q, i + 1, g);
+    r = qmul(qmul(r, t0), t1);
   }
+  if (i < hi) r = qmul(r, root_term32<DE>(m, q, i, g));
   return r;
 }
 
@@ -149,10 +164,10 @@ template <bool DE>
 __device__ __forceinline__ q32::Q apply32(const MapParams& m, const q32::Q& q, float* g2) {
   using namespace q32;
   Q g = {0.f, 0.f, 0.f, 0.f};
-  const Q top = product32<DE>(m, q, 0, m.nt, 1.f, g);
+  const Q top = product32<DE>(m, q, 0, m.nt, g);
   Q out;
   if (m.nb > 0) {
-    const Q bot = product32<DE>(m, q, m.nt, m.nt + m.nb, -1.f, g);
+    const Q bot = product32<DE>(m, q, m.nt, m.nt + m.nb, g);
     const float inv = __fdividef(m.scalef, norm2(bot));
     out = qmul_conj(top, bot);
     out.w *= inv;

@@ -24,6 +24,7 @@ struct MapParams {
   double e64[QJ_MAX_ROOTS];     // effective exponent sigma * e_i
   double ep[QJ_MAX_ROOTS];      // the root's own exponent e_i (POLYNOMIAL_4D::powers())
   alignas(16) float r32[QJ_MAX_ROOTS][4];
+  alignas(8) float x32[QJ_MAX_ROOTS][2];  // {+e (top) or -e (bottom), integer exponent bits}
   float e32[QJ_MAX_ROOTS];
   int ie[QJ_MAX_ROOTS];         // integer exponent, or 0 when the exponent is not an integer
 };
