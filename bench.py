@@ -265,6 +265,15 @@ def run_ours(args, world, rank, local):
         e2e = {"value": world * n / max_over_ranks(world, statistics.mean(e2e_t)) / 1e9,
                "unit": "Gvox/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 8 * n}
 
+    # serving: a Poisson-arrival stream of field / field+mesh / energy+gradient
+    # requests (sizes scaled down so the stream takes about 10 s), p50/p99
+    serving = None
+    if rank == 0 and not args.no_serve:
+        from quijibo_gb300.benchmarks import bench_serve
+        sargs = argparse.Namespace(seed=0, requests=args.serve_requests, scale=0.25, span=10.0,
+                                   workers=8, budget_gb=64.0, baseline_sample=10)
+        serving = bench_serve(sargs)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         slices = [int(v) for v in np.linspace(0, g.res[2] - 1, args.cpu_slices)]
@@ -283,13 +292,15 @@ def run_ours(args, world, rank, local):
                    "parallelism": "one grid per GPU" if world > 1 else "single GPU"},
         "fp64_plain": fp64,
         "field_stats": dict(st, bulk_ms=bulk, refine_ms=statistics.mean(refine_ms),
-                            wall_s=wall, refined_frac=st["refined"] / n),
+                            wall_s=wall, refined_frac=st["refined"] / n,
+                            lane_efficiency=st["voxel_iters"] / max(1, st["lane_iters"])),
         "roofline": {"bound": "fma", "kernel": "field32_kernel", "achieved": achieved,
                      "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                      "traffic": None,
                      "peak_source": "measured FP32 FMA-chain probe (qjg_fma_probe), same run",
                      "flops_per_launch": flops},
         "cpu_baseline": cpu,
+        "serving": serving,
         "e2e": e2e,
         "gpu_launches": launches,
         "clocks": clk,
@@ -309,6 +320,8 @@ def main():
     ap.add_argument("--ref-slices", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 plain-form comparison")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving stream")
+    ap.add_argument("--serve-requests", type=int, default=200)
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.impl == "reference":

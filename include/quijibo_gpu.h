@@ -68,6 +68,7 @@ typedef struct {
   int64_t refined;       /* voxels re-evaluated in FP64 */
   int64_t refined_iters; /* map applications of the FP64 re-evaluation */
   int64_t nonfinite;     /* FP32 voxels that overflowed or underflowed */
+  int64_t lane_iters;    /* FP32 bulk: lane slots spent (32 x the longest orbit of each warp) */
 } qjg_field_stats;
 
 /* ---- context and root sets ------------------------------------------- */
@@ -138,6 +139,7 @@ typedef struct {
   int64_t n_degenerate;  /* triangles dropped by the degenerate filter (edge < 1e-7) */
   int64_t n_unbracketed; /* edges whose end values do not bracket zero (the reference exits) */
   int64_t map_evals;     /* FP64 map evaluations of the edge bisection */
+  int64_t map_evals_fp32;/* FP32 evaluations whose sign was trusted (precision form only) */
   int64_t slabs;         /* z-slabs processed */
   qjg_field_stats field; /* the field pass of qjg_mesh_stream */
 } qjg_mesh_stats;
@@ -161,7 +163,9 @@ int qjg_mesh_field(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg
 
 /* Streaming marching cubes: the field (iter->precision) is computed slab by
  * slab, corners are classified by log|q| > 0, and vertices are placed by
- * FP64 bisection of log|q| - iso.  Replaces the two-slab streaming
+ * bisection of log|q| - iso: in FP64 for QJG_FP64; for the precision form
+ * each evaluation is tried in FP32 first and kept only when its value clears
+ * its error bound, so every bisection decision is the one FP64 makes.  Replaces the two-slab streaming
  * TRIANGLE_MESH(center, lengths, res, top, bottom, expScaling, maxIterations,
  * slice, isosurface, rotation, cacheFile) constructor /
  * computeNonlinearMarchingCubesLowMemoryHuge (TRIANGLE_MESH.cpp:84-101,
@@ -199,8 +203,11 @@ int qjg_tanh_score_grad(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, int3
                         double threshold, double* score, double* grad, double* d_field,
                         qjg_tanh_stats* stats, void* stream);
 
-/* Squared-error fitting energy E = sum_k (d(x_k) - t_k)^2 of the distance
- * estimate d = |q_N| log|q_N| / |q_N'| at sample points x_k (no reference
+/* Squared-error fitting energy E = sum_k (D tanh(d(x_k)/D) - t_k)^2 of the
+ * distance estimate d = |q_N| log|q_N| / |q_N'| at sample points x_k, with
+ * D = d_sat (d_sat <= 0: E = sum (d - t)^2; samples deep inside, where
+ * |q_N'| contracts to zero and d grows without bound, saturate at +-D and
+ * add no gradient once |d| > 20 D) (no reference
  * counterpart: the reference fits exponents and scales with the tanh score;
  * this form also fits root positions).  The map's parameters live in a
  * device vector d_params of 5 * (n_top + n_bot) + 1 doubles:
@@ -215,12 +222,12 @@ int qjg_tanh_score_grad(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, int3
  * each sample's iteration count.  Both synchronize `stream`. */
 int qjg_energy_forward(qjg_ctx* ctx, const double* d_params, int32_t n_top, int32_t n_bot,
                        int64_t n, const double* d_xyz, const double* d_target, double slice,
-                       int32_t max_it, double escape, int32_t precision, double* energy,
-                       int32_t* d_iters, void* stream);
+                       int32_t max_it, double escape, double d_sat, int32_t precision,
+                       double* energy, int32_t* d_iters, void* stream);
 int qjg_energy_backward(qjg_ctx* ctx, const double* d_params, int32_t n_top, int32_t n_bot,
                         int64_t n, const double* d_xyz, const double* d_target, double slice,
-                        int32_t max_it, double escape, int32_t precision, double* energy,
-                        double* d_grad, void* stream);
+                        int32_t max_it, double escape, double d_sat, int32_t precision,
+                        double* energy, double* d_grad, void* stream);
 
 typedef struct {
   int32_t steps;          /* L-BFGS iterations taken */
@@ -240,7 +247,7 @@ typedef struct {
  * each step.  Synchronizes `stream`. */
 int qjg_fit_lbfgs(qjg_ctx* ctx, double* d_params, int32_t n_top, int32_t n_bot, int64_t n,
                   const double* d_xyz, const double* d_target, double slice, int32_t max_it,
-                  double escape, int32_t precision, int32_t steps, int32_t history,
+                  double escape, double d_sat, int32_t precision, int32_t steps, int32_t history,
                   double* energies, qjg_fit_stats* stats, void* stream);
 
 /* ---- serving ----------------------------------------------------------- */
@@ -277,6 +284,7 @@ typedef struct {
   double iso;       /* mesh */
   int64_t vert_cap, tri_cap; /* mesh output capacities */
   const double* params; /* energy: parameter vector (layout of qjg_energy_backward) */
+  double d_sat;         /* energy: saturation distance D (as qjg_energy_backward) */
   int64_t n_samples;
   const double* xyz;
   const double* target;

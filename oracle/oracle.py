@@ -94,7 +94,7 @@ class Oracle:
                                           C.c_int, C.c_double, C.c_double, _dp, _dp]
         L.qjo_tanh_score_grad.restype = C.c_double
         L.qjo_sqerr_energy.argtypes = [C.POINTER(_Map), C.c_int64, _dp, _dp, C.c_double, C.c_int,
-                                       C.c_double, C.POINTER(C.c_int32)]
+                                       C.c_double, C.c_double, C.POINTER(C.c_int32)]
         L.qjo_sqerr_energy.restype = C.c_double
         self.L = L
 
@@ -163,12 +163,13 @@ class Oracle:
                                         threshold, _ptr(grad), _ptr(field))
         return sc, grad, field.reshape(grid.res[::-1])
 
-    def sqerr_energy(self, rootset, xyz, target, max_it, escape, slice_=0.0, iters=False):
+    def sqerr_energy(self, rootset, xyz, target, max_it, escape, slice_=0.0, iters=False,
+                     d_sat=1.0):
         xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
         t = np.ascontiguousarray(target, dtype=np.float64)
         it = np.empty(len(t), dtype=np.int32) if iters else None
         e = self.L.qjo_sqerr_energy(C.byref(make_map(rootset)), len(t), _ptr(xyz), _ptr(t), slice_,
-                                    max_it, escape, _ptr(it, C.POINTER(C.c_int32)))
+                                    max_it, escape, d_sat, _ptr(it, C.POINTER(C.c_int32)))
         return (e, it) if iters else e
 
     def trilinear(self, grid, data, p):

@@ -659,7 +659,7 @@ double qjo_tanh_score_grad(const qjo_map* m, const qjo_grid* g, const qjo_grid* 
 /* Squared-error energy sum_k (d(x_k) - t_k)^2 of the distance estimate
  * (no reference counterpart; d as in qjo_field's de output). */
 double qjo_sqerr_energy(const qjo_map* m, int64_t n, const double* xyz, const double* target,
-                        double slice, int max_it, double escape, int32_t* iters) {
+                        double slice, int max_it, double escape, double d_sat, int32_t* iters) {
   double e = 0.0;
 #ifdef _OPENMP
 #pragma omp parallel for schedule(dynamic, 64) reduction(+ : e)
@@ -669,7 +669,15 @@ double qjo_sqerr_energy(const qjo_map* m, int64_t n, const double* xyz, const do
     int32_t it;
     escape_value(m, xyz + 3 * k, slice, max_it, escape, &d, &it);
     if (iters) iters[k] = it;
-    const double r = d - target[k];
+    /* fitted value D tanh(d/D); +-D beyond |d| > 20 D (and for non-finite d) */
+    double v = d;
+    if (d_sat > 0) {
+      if (!(fabs(d) <= 20.0 * d_sat))
+        v = (d < 0 ? -1.0 : 1.0) * d_sat;
+      else
+        v = d_sat * tanh(d / d_sat);
+    }
+    const double r = v - target[k];
     e += r * r;
   }
   return e;

@@ -100,9 +100,10 @@ double qjo_tanh_score_grad(const qjo_map* m, const qjo_grid* g, const qjo_grid* 
                            const double* weights, int max_it, double alpha,
                            double threshold, double* grad, double* field);
 
-/* Squared-error energy sum_k (d(x_k) - t_k)^2 of the distance estimate d. */
+/* Squared-error energy sum_k (D tanh(d(x_k)/D) - t_k)^2 of the distance
+ * estimate d, D = d_sat (d_sat <= 0: sum (d - t)^2). */
 double qjo_sqerr_energy(const qjo_map* m, int64_t n, const double* xyz, const double* target,
-                        double slice, int max_it, double escape, int32_t* iters);
+                        double slice, int max_it, double escape, double d_sat, int32_t* iters);
 
 #ifdef __cplusplus
 }

@@ -61,9 +61,11 @@ def bench_mesh(args):
             "triangles": st["n_tris"], "vertices": st["n_verts"], "wall_s": wall,
             "triangles_per_s": st["n_tris"] / wall, "gvox_s": g.n_voxels / wall / 1e9,
             "field_only_s": field_ms / 1e3, "mesher_s": wall - field_ms / 1e3,
-            "bisection_map_evals": st["map_evals"], "unbracketed": st["n_unbracketed"],
+            "bisection_map_evals_fp64": st["map_evals"],
+            "bisection_map_evals_fp32": st["map_evals_fp32"], "unbracketed": st["n_unbracketed"],
             "degenerate": st["n_degenerate"], "slabs": st["slabs"],
-            "refined": st["field"]["refined"]}
+            "refined": st["field"]["refined"],
+            "lane_efficiency": st["field"]["voxel_iters"] / max(1, st["field"]["lane_iters"])}
 
 
 def bench_energy(args):

@@ -245,6 +245,7 @@ int qjg_field_stats_read(qjg_ctx* ctx, void* stream, qjg_field_stats* out) {
   out->refined = (int64_t)st.refined;
   out->refined_iters = (int64_t)st.aux[0];
   out->nonfinite = (int64_t)st.nonfinite;
+  out->lane_iters = (int64_t)st.aux[3];
   return QJG_OK;
 }
 
@@ -285,6 +286,7 @@ int qjg_field_host(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg
     total.refined += st.refined;
     total.refined_iters += st.refined_iters;
     total.nonfinite += st.nonfinite;
+    total.lane_iters += st.lane_iters;
   }
   if (stats) *stats = total;
   return QJG_OK;

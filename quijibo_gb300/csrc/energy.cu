@@ -312,13 +312,16 @@ cudaError_t launch_tanh_grad(const MapParams& m, const GridParams& g, const Weig
 // Squared-error fitting energy on the distance estimate and its adjoint.
 //
 // No reference counterpart (the reference tracks no derivative of this map
-// and fits only exponents and scales).  Per sample x_k with target t_k:
+// and fits only exponents and scales).  Per sample x_k with target t_k
+// (the fitted value is D tanh(d / D) with D = d_sat, so that samples deep
+// inside, whose |q'| contracts towards zero and whose d grows without bound,
+// saturate instead of dominating the sum):
 //   q_0 = (x, y, z, slice); for n < N (escape test as the field):
 //     d_i = q_n - r_i, P_i = d_i^{e_i} (polar power), T = prod top P_i,
 //     B = prod bottom P_i, q_{n+1} = s T B^-1,
 //     g_n = sum_top e_i d_i/|d_i|^2 - sum_bot e_j d_j/|d_j|^2,
 //     L_{n+1} = L_n + log|g_n| + log|q_{n+1}|          (L = log|q'|)
-//   d = |q_N| log|q_N| exp(-L_N),  E = sum_k (d_k - t_k)^2.
+//   d = |q_N| log|q_N| exp(-L_N),  E = sum_k (D tanh(d_k / D) - t_k)^2.
 // Parameters: root positions (4 each), effective exponents, log s, laid out
 // [top roots 4nt | bottom roots 4nb | top exps nt | bottom exps nb | log s].
 // The backward pass stores no trajectory: it keeps q at every SQ_CK-th
@@ -446,11 +449,12 @@ __device__ __forceinline__ V4<T> sq_apply(const T* __restrict__ rp, const T* __r
   return Q;
 }
 
-// Forward to the end: returns d and the iteration count; fills checkpoints.
+// Forward to the end: returns log|q_N|, with the iteration count, L_N and
+// log|d| through the pointers; fills checkpoints.
 template <class T>
 __device__ __forceinline__ T sq_forward(const T* rp, const T* ep, int nt, int nb, T s,
                                         V4<T> q, int max_it, T esc, int* n_out, T* L_out,
-                                        V4<T>* ck, T* Lck) {
+                                        V4<T>* ck, T* Lck, T* ld_out) {
   T L = T(0);
   int n = 0;
   while (sqrt(v4dot(q, q)) < esc && n < max_it) {
@@ -468,14 +472,47 @@ __device__ __forceinline__ T sq_forward(const T* rp, const T* ep, int nt, int nb
   *n_out = n;
   *L_out = L;
   if (ck) ck[n / SQ_CK + 1] = q;  // final iterate (slot after the last checkpoint)
-  return m * log(m) * exp(-L);
+  // log|d| first: contracting orbits drive L far below zero, and d itself
+  // out of range, long before d matters
+  const T lm = log(m);
+  *ld_out = log(fabs(lm)) + lm - L;
+  return lm;
+}
+
+// The fitted value D tanh(d / D) (d itself when D <= 0) and its derivative;
+// a sample whose |d| exceeds 20 D is saturated: value +-D, no gradient.
+template <class T>
+__device__ __forceinline__ void sq_saturate(T lm, T ld, T dsat, T* val, T* d, T* dval_dd) {
+  const T sgn = lm < T(0) ? T(-1) : T(1);
+  if (lm == T(0)) {
+    *d = T(0);
+    *val = T(0);
+    *dval_dd = T(1);
+    return;
+  }
+  if (dsat > T(0) && ld > log(T(20) * dsat)) {
+    *d = sgn * T(20) * dsat;
+    *val = sgn * dsat;
+    *dval_dd = T(0);
+    return;
+  }
+  *d = sgn * exp(ld);
+  if (dsat > T(0)) {
+    const T th = tanh(*d / dsat);
+    *val = dsat * th;
+    *dval_dd = T(1) - th * th;
+  } else {
+    *val = *d;
+    *dval_dd = T(1);
+  }
 }
 
 template <class T, bool GRAD>
 __global__ void __launch_bounds__(SQ_T) sq_energy_kernel(
     const double* __restrict__ params, int nt, int nb, const double* __restrict__ xyz,
     const double* __restrict__ target, long long n_samples, double slice, int max_it,
-    double escape, double* __restrict__ partials, int slots, int* __restrict__ iters_out) {
+    double escape, double d_sat, double* __restrict__ partials, int slots,
+    int* __restrict__ iters_out) {
   extern __shared__ unsigned char sh_raw[];
   const int nr = nt + nb;
   T* rp = reinterpret_cast<T*>(sh_raw);           // 4 nr
@@ -496,24 +533,32 @@ __global__ void __launch_bounds__(SQ_T) sq_energy_kernel(
   T gacc[5 * QJ_MAX_ROOTS + 1];
   if (GRAD)
     for (int k = 0; k <= 5 * nr; k++) gacc[k] = T(0);
-  double e_acc = 0.0;
+  double e_acc = 0.0, bad_acc = 0.0;
+  const T dsat = (T)d_sat;
   const long long stride = (long long)gridDim.x * SQ_T;
   for (long long k = (long long)blockIdx.x * SQ_T + threadIdx.x; k < n_samples; k += stride) {
     const V4<T> q0{(T)xyz[3 * k], (T)xyz[3 * k + 1], (T)xyz[3 * k + 2], (T)slice};
     int N;
-    T LN;
-    const T dval = sq_forward<T>(rp, ep, nt, nb, s, q0, max_it, esc, &N, &LN, GRAD ? ck : nullptr,
-                                 GRAD ? Lck : nullptr);
+    T LN, ld;
+    const T lm = sq_forward<T>(rp, ep, nt, nb, s, q0, max_it, esc, &N, &LN, GRAD ? ck : nullptr,
+                               GRAD ? Lck : nullptr, &ld);
     if (iters_out) iters_out[k] = N;
-    const T r = dval - (T)target[k];
+    T val, dval, dval_dd;
+    sq_saturate<T>(lm, ld, dsat, &val, &dval, &dval_dd);
+    const T r = val - (T)target[k];
     e_acc += (double)(r * r);
-    if (!GRAD) continue;
-    // seed: dE/dd = 2 r; d = m log m exp(-L)
+    if (!GRAD || dval_dd == T(0)) continue;
+    // seed: dE/dd = 2 r dval/dd; d = m log m exp(-L):
+    // dd/dm = (log m + 1) exp(-L) = d (log m + 1) / (m log m)
     const V4<T> qN = ck[N / SQ_CK + 1];
     const T m = sqrt(v4dot(qN, qN));
-    const T db = T(2) * r;
-    const T eL = exp(-LN);
-    V4<T> qb = v4scale(qN, db * (log(m) + T(1)) * eL / m);
+    const T db = T(2) * r * dval_dd;
+    const T kq = db * (lm + T(1)) * exp(ld - log(m) - log(fabs(lm)));
+    if (!isfinite(kq) || !isfinite(db * dval)) {
+      bad_acc += 1.0;
+      continue;
+    }
+    V4<T> qb = v4scale(qN, kq / m);  // d/dq_N of d: (dd/dm) q_N / m
     const T Lb = -db * dval;  // constant along the chain (L_{n+1} = L_n + ...)
     // segments in reverse
     for (int sgi = (N - 1) / SQ_CK; sgi >= 0 && N > 0; sgi--) {
@@ -586,7 +631,7 @@ __global__ void __launch_bounds__(SQ_T) sq_energy_kernel(
   }
   // deterministic reduction: warp trees, warps in order
   for (int k = 0; k < slots; k++) {
-    double v = (k == 0) ? e_acc : (GRAD ? (double)gacc[k - 1] : 0.0);
+    double v = (k == 0) ? e_acc : (k == slots - 1) ? bad_acc : (GRAD ? (double)gacc[k - 1] : 0.0);
 #pragma unroll
     for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if ((threadIdx.x & 31) == 0) acc[k] += v;
@@ -605,26 +650,26 @@ int sq_max_iterations() { return SQ_MAXIT; }
 
 cudaError_t launch_sq_energy(bool fp64, bool grad, const double* params, int nt, int nb,
                              const double* xyz, const double* target, long long n, double slice,
-                             int max_it, double escape, double* partials, int nblocks,
-                             double* out, int* iters, cudaStream_t s) {
+                             int max_it, double escape, double d_sat, double* partials,
+                             int nblocks, double* out, int* iters, cudaStream_t s) {
   const int nr = nt + nb;
-  const int slots = 1 + 5 * nr + 1;
+  const int slots = 1 + 5 * nr + 1 + 1;  // energy, gradient, skipped-sample count
   const size_t elem = fp64 ? sizeof(double) : sizeof(float);
   const size_t sh = ((elem * 5 * nr + 15) / 16) * 16 + sizeof(double) * (SQ_T / 32) * slots;
   if (fp64) {
     if (grad)
       sq_energy_kernel<double, true><<<nblocks, SQ_T, sh, s>>>(params, nt, nb, xyz, target, n, slice,
-                                                               max_it, escape, partials, slots, iters);
+                                                               max_it, escape, d_sat, partials, slots, iters);
     else
       sq_energy_kernel<double, false><<<nblocks, SQ_T, sh, s>>>(params, nt, nb, xyz, target, n, slice,
-                                                                max_it, escape, partials, slots, iters);
+                                                                max_it, escape, d_sat, partials, slots, iters);
   } else {
     if (grad)
       sq_energy_kernel<float, true><<<nblocks, SQ_T, sh, s>>>(params, nt, nb, xyz, target, n, slice,
-                                                              max_it, escape, partials, slots, iters);
+                                                              max_it, escape, d_sat, partials, slots, iters);
     else
       sq_energy_kernel<float, false><<<nblocks, SQ_T, sh, s>>>(params, nt, nb, xyz, target, n, slice,
-                                                               max_it, escape, partials, slots, iters);
+                                                               max_it, escape, d_sat, partials, slots, iters);
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;

@@ -65,8 +65,8 @@ int qjg_tanh_score_grad(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, int3
 
 static int sq_energy(qjg_ctx* ctx, const double* d_params, int32_t nt, int32_t nb, int64_t n,
                      const double* d_xyz, const double* d_target, double slice, int32_t max_it,
-                     double escape, int32_t precision, double* energy, double* d_grad,
-                     int32_t* d_iters, void* stream) {
+                     double escape, double d_sat, int32_t precision, double* energy,
+                     double* d_grad, int32_t* d_iters, void* stream) {
   if (!ctx) return QJG_ERR_ARG;
   if (nt < 1 || nb < 0 || nt + nb > QJG_MAX_ROOTS)
     return fail(ctx, QJG_ERR_ARG, "root counts top=%d bottom=%d", nt, nb);
@@ -82,15 +82,16 @@ static int sq_energy(qjg_ctx* ctx, const double* d_params, int32_t nt, int32_t n
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
   const int nblocks = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * 8, (n + 63) / 64));
-  const int slots = 1 + 5 * (nt + nb) + 1;
+  const int P = 5 * (nt + nb) + 1;
+  const int slots = 1 + P + 1;  // energy, gradient, samples left out of the gradient
   double* d_part = nullptr;
   QJ_CUDA(ctx, cudaMallocAsync((void**)&d_part, sizeof(double) * ((size_t)nblocks + 1) * slots, s));
   double* d_out = d_part + (size_t)nblocks * slots;
   cudaError_t e = qj::launch_sq_energy(precision == QJG_FP64, d_grad != nullptr, d_params, nt, nb,
-                                       d_xyz, d_target, n, slice, max_it, escape, d_part, nblocks,
-                                       d_out, d_iters, s);
+                                       d_xyz, d_target, n, slice, max_it, escape, d_sat, d_part,
+                                       nblocks, d_out, d_iters, s);
   if (e == cudaSuccess && d_grad)
-    e = cudaMemcpyAsync(d_grad, d_out + 1, sizeof(double) * (slots - 1), cudaMemcpyDeviceToDevice, s);
+    e = cudaMemcpyAsync(d_grad, d_out + 1, sizeof(double) * P, cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(energy, d_out, sizeof(double), cudaMemcpyDeviceToHost, s);
   cudaFreeAsync(d_part, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -101,24 +102,24 @@ static int sq_energy(qjg_ctx* ctx, const double* d_params, int32_t nt, int32_t n
 
 int qjg_energy_forward(qjg_ctx* ctx, const double* d_params, int32_t n_top, int32_t n_bot,
                        int64_t n, const double* d_xyz, const double* d_target, double slice,
-                       int32_t max_it, double escape, int32_t precision, double* energy,
-                       int32_t* d_iters, void* stream) {
-  return sq_energy(ctx, d_params, n_top, n_bot, n, d_xyz, d_target, slice, max_it, escape,
+                       int32_t max_it, double escape, double d_sat, int32_t precision,
+                       double* energy, int32_t* d_iters, void* stream) {
+  return sq_energy(ctx, d_params, n_top, n_bot, n, d_xyz, d_target, slice, max_it, escape, d_sat,
                    precision, energy, nullptr, d_iters, stream);
 }
 
 int qjg_energy_backward(qjg_ctx* ctx, const double* d_params, int32_t n_top, int32_t n_bot,
                         int64_t n, const double* d_xyz, const double* d_target, double slice,
-                        int32_t max_it, double escape, int32_t precision, double* energy,
-                        double* d_grad, void* stream) {
+                        int32_t max_it, double escape, double d_sat, int32_t precision,
+                        double* energy, double* d_grad, void* stream) {
   if (!d_grad) return fail(ctx, QJG_ERR_ARG, "d_grad is NULL");
-  return sq_energy(ctx, d_params, n_top, n_bot, n, d_xyz, d_target, slice, max_it, escape,
+  return sq_energy(ctx, d_params, n_top, n_bot, n, d_xyz, d_target, slice, max_it, escape, d_sat,
                    precision, energy, d_grad, nullptr, stream);
 }
 
 int qjg_fit_lbfgs(qjg_ctx* ctx, double* d_params, int32_t nt, int32_t nb, int64_t n,
                   const double* d_xyz, const double* d_target, double slice, int32_t max_it,
-                  double escape, int32_t precision, int32_t steps, int32_t history,
+                  double escape, double d_sat, int32_t precision, int32_t steps, int32_t history,
                   double* energies, qjg_fit_stats* stats, void* stream) {
   if (!ctx) return QJG_ERR_ARG;
   if (!d_params || steps < 0 || history < 1 || history > 64)
@@ -139,9 +140,9 @@ int qjg_fit_lbfgs(qjg_ctx* ctx, double* d_params, int32_t nt, int32_t nb, int64_
   int rc = QJG_OK;
   auto energy = [&](const double* params, double* e, double* grad) {
     return grad ? qjg_energy_backward(ctx, params, nt, nb, n, d_xyz, d_target, slice, max_it,
-                                      escape, precision, e, grad, stream)
+                                      escape, d_sat, precision, e, grad, stream)
                 : qjg_energy_forward(ctx, params, nt, nb, n, d_xyz, d_target, slice, max_it,
-                                     escape, precision, e, nullptr, stream);
+                                     escape, d_sat, precision, e, nullptr, stream);
   };
   double E = 0;
   int k = 0, head = -1;

@@ -114,77 +114,6 @@ __global__ void __launch_bounds__(128) refine64_kernel(const __grid_constant__ M
 
 // ------------------------------------------------------------------ FP32
 
-// Exponents other than 1 and 2 (kept out of line, off the hot path).
-__device__ __noinline__ q32::Q root_power_rare(q32::Q d, int ie, float e) {
-  return ie > 0 ? q32::qpow_int(d, ie) : q32::qpow(d, e);
-}
-
-// One root term (q - r_i)^(e_i) in FP32; with DE, adds (+-e_i) d/|d|^2 to g.
-// Root coordinates come as one 16-byte constant-bank load and {+-e, integer
-// exponent} as one 8-byte load.
-template <bool DE>
-__device__ __forceinline__ q32::Q root_term32(const MapParams& m, const q32::Q& q, int i,
-                                              q32::Q& g) {
-  using namespace q32;
-  const float4 root = *reinterpret_cast<const float4*>(m.r32[i]);
-  const float2 ex = *reinterpret_cast<const float2*>(m.x32[i]);
-  const Q d = {q.w - root.x, q.x - root.y, q.y - root.z, q.z - root.w};
-  if (DE) {
-    const float k = __fdividef(ex.x, norm2(d));
-    g.w = fmaf(k, d.w, g.w);
-    g.x = fmaf(k, d.x, g.x);
-    g.y = fmaf(k, d.y, g.y);
-    g.z = fmaf(k, d.z, g.z);
-  }
-  const int ie = __float_as_int(ex.y);
-  if (ie == 1) return d;
-  if (ie == 2) return qsq(d);
-  return root_power_rare(d, ie, m.e32[i]);
-}
-
-// prod_{i in [lo, hi)} (q - r_i)^(e_i), left to right; the first term starts
-// the product and the rest go two per trip.
-template <bool DE>
-__device__ __forceinline__ q32::Q product32(const MapParams& m, const q32::Q& q, int lo, int hi,
-                                            q32::Q& g) {
-  using namespace q32;
-  Q r = root_term32<DE>(m, q, lo, g);
-  int i = lo + 1;
-#pragma unroll 1
-  for (; i + 1 < hi; i += 2) {
-    const Q t0 = root_term32<DE>(m, q, i, g);
-    const Q t1 = root_term32<DE>(m, q, i + 1, g);
-    r = qmul(qmul(r, t0), t1);
-  }
-  if (i < hi) r = qmul(r, root_term32<DE>(m, q, i, g));
-  return r;
-}
-
-template <bool DE>
-__device__ __forceinline__ q32::Q apply32(const MapParams& m, const q32::Q& q, float* g2) {
-  using namespace q32;
-  Q g = {0.f, 0.f, 0.f, 0.f};
-  const Q top = product32<DE>(m, q, 0, m.nt, g);
-  Q out;
-  if (m.nb > 0) {
-    const Q bot = product32<DE>(m, q, m.nt, m.nt + m.nb, g);
-    const float inv = __fdividef(m.scalef, norm2(bot));
-    out = qmul_conj(top, bot);
-    out.w *= inv;
-    out.x *= inv;
-    out.y *= inv;
-    out.z *= inv;
-  } else {
-    out = top;
-    out.w *= m.scalef;
-    out.x *= m.scalef;
-    out.y *= m.scalef;
-    out.z *= m.scalef;
-  }
-  if (DE) *g2 = norm2(g);
-  return out;
-}
-
 template <bool DE>
 __global__ void __launch_bounds__(128) field32_kernel(const __grid_constant__ MapParams m,
                                                       const GridParams g, const IterParams it, double* __restrict__ field,
@@ -196,7 +125,7 @@ __global__ void __launch_bounds__(128) field32_kernel(const __grid_constant__ Ma
   const float esc2 = (float)(it.escape * it.escape);
   const float l2band = log2f((float)it.band), ftol = (float)it.field_tol;
   const float esc_tol = 2e-3f;  // relative, on |q|^2
-  unsigned long long iters_acc = 0, nonfinite_acc = 0;
+  unsigned long long iters_acc = 0, nonfinite_acc = 0, lane_iters_acc = 0;
   for (;;) {
     const long long t = next_tile(&st->tiles_done);
     if (t >= tm.total) break;
@@ -207,6 +136,7 @@ __global__ void __launch_bounds__(128) field32_kernel(const __grid_constant__ Ma
     const bool valid = (x < g.X && y < g.Y);
     bool need = false;
     long long i = 0;
+    int n_exec = 0;
     if (valid) {
       double p[3];
       cell_center(g, x, y, g.z0 + zl, p);
@@ -230,6 +160,7 @@ __global__ void __launch_bounds__(128) field32_kernel(const __grid_constant__ Ma
         }
       }
       iters_acc += n;
+      n_exec = n;
       const float f = 0.5f * logf(m2);
       // d = |q| log|q| / |q'| kept as log2|d|: contracting orbits drive |q'|
       // below the FP32 range long before d itself matters
@@ -252,6 +183,9 @@ __global__ void __launch_bounds__(128) field32_kernel(const __grid_constant__ Ma
         if (DE && de) de[i] = d;
       }
     }
+    // lane slots the warp spent: 32 x its longest orbit
+    const unsigned wmax = __reduce_max_sync(0xffffffffu, (unsigned)n_exec);
+    if (lane == 0) lane_iters_acc += 32ull * wmax;
     // warp-aggregated append to the refine list
     const unsigned mask = __ballot_sync(0xffffffffu, need);
     if (mask) {
@@ -263,6 +197,7 @@ __global__ void __launch_bounds__(128) field32_kernel(const __grid_constant__ Ma
   }
   warp_add(&st->voxel_iters, iters_acc);
   warp_add(&st->nonfinite, nonfinite_acc);
+  warp_add(&st->aux[3], lane_iters_acc);
 }
 
 // ------------------------------------------------------------- launchers

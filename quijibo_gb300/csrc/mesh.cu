@@ -303,7 +303,30 @@ struct DegenEmit : DegenCount {
 
 // One vertex per listed edge: linear interpolation of the stored values
 // (computeEdgeInterpolations) or the bisection of midpointSearch on the map.
-template <bool BISECT, bool POW_REF>
+// A bisection value log|q_N| - iso.  With HYBRID the FP32 orbit is tried
+// first and trusted when its value clears its error bound and the 1e-8 stop
+// test by a margin: then the FP64 value has the same sign and also fails the
+// stop test, so every decision of the search is the one FP64 would make.
+template <bool POW_REF, bool HYBRID>
+__device__ __forceinline__ double bisect_value(const MapParams& m, const GridParams& g,
+                                               const IterParams& it, const double p[3], double iso,
+                                               unsigned long long* e32, unsigned long long* e64) {
+  if (HYBRID) {
+    float err;
+    const float f = escape32(m, it, p, g.slice, &err);
+    const float v = f - (float)iso;
+    if (fabsf(v) > 1.01f * err + 1e-8f + 1e-6f * fabsf((float)iso)) {
+      (*e32)++;
+      return (double)v;
+    }
+  }
+  (*e64)++;
+  int ni;
+  double dd;
+  return q64::sub(escape64<POW_REF, false>(m, it, p, g.slice, &ni, &dd), iso);
+}
+
+template <bool BISECT, bool POW_REF, bool HYBRID>
 __global__ void __launch_bounds__(128) vertex_kernel(const __grid_constant__ MapParams m,
                                                      const GridParams g, const IterParams it,
                                                      const uint32_t* __restrict__ list, long long n,
@@ -312,7 +335,7 @@ __global__ void __launch_bounds__(128) vertex_kernel(const __grid_constant__ Map
                                                      double* __restrict__ verts, double iso,
                                                      DevStats* st) {
   const long long XY = (long long)g.X * g.Y;
-  unsigned long long evals = 0, unbracketed = 0;
+  unsigned long long evals = 0, evals32 = 0, unbracketed = 0;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
        k += (long long)gridDim.x * blockDim.x) {
     const uint32_t e = list[k];
@@ -334,12 +357,9 @@ __global__ void __launch_bounds__(128) vertex_kernel(const __grid_constant__ Map
 #pragma unroll
       for (int c = 0; c < 3; c++) out[c] = add(p0[c], mul(t, sub(p1[c], p0[c])));
     } else {
-      int ni;
-      double dd;
       // nonlinearValue at both ends (TRIANGLE_MESH.cpp:2060-2067)
-      const double f0 = sub(escape64<POW_REF, false>(m, it, p0, g.slice, &ni, &dd), iso);
-      const double f1 = sub(escape64<POW_REF, false>(m, it, p1, g.slice, &ni, &dd), iso);
-      evals += 2;
+      const double f0 = bisect_value<POW_REF, HYBRID>(m, g, it, p0, iso, &evals32, &evals);
+      const double f1 = bisect_value<POW_REF, HYBRID>(m, g, it, p1, iso, &evals32, &evals);
       double pv[3], nv[3], pval = f0, nval = f1;
       bool bad = mul(f0, f1) >= 0.0;
 #pragma unroll
@@ -365,8 +385,7 @@ __global__ void __launch_bounds__(128) vertex_kernel(const __grid_constant__ Map
           break;
         }
         if (rec >= 6) break;
-        const double mv = sub(escape64<POW_REF, false>(m, it, out, g.slice, &ni, &dd), iso);
-        evals++;
+        const double mv = bisect_value<POW_REF, HYBRID>(m, g, it, out, iso, &evals32, &evals);
         if (fabs(mv) < 1e-8) break;
         if (mv < 0) {
 #pragma unroll
@@ -388,11 +407,13 @@ __global__ void __launch_bounds__(128) vertex_kernel(const __grid_constant__ Map
   if (BISECT) {
     for (int o = 16; o; o >>= 1) {
       evals += __shfl_xor_sync(0xffffffffu, evals, o);
+      evals32 += __shfl_xor_sync(0xffffffffu, evals32, o);
       unbracketed += __shfl_xor_sync(0xffffffffu, unbracketed, o);
     }
     if ((threadIdx.x & 31) == 0) {
       if (evals) atomicAdd(&st->aux[1], evals);
       if (unbracketed) atomicAdd(&st->aux[2], unbracketed);
+      if (evals32) atomicAdd(&st->aux[3], evals32);
     }
   }
 }
@@ -448,20 +469,20 @@ cudaError_t mesh_vertex_ids(MeshWindow& w, int j0, int j1, int lay_lo, int lay_h
 }
 
 cudaError_t mesh_vertices(const MapParams& m, const GridParams& g, const IterParams& it,
-                          int edge_mode, bool pow_ref, const MeshWindow& w, long long n,
-                          long long id0, int c0, const double* src, double* verts, double iso,
-                          DevStats* st, cudaStream_t s) {
+                          int edge_mode, bool pow_ref, bool hybrid, const MeshWindow& w,
+                          long long n, long long id0, int c0, const double* src, double* verts,
+                          double iso, DevStats* st, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   const int blocks = (int)std::min<long long>((n + 127) / 128, (long long)sm_count() * 32);
+#define QJ_VK(B, P, H) \
+  vertex_kernel<B, P, H><<<blocks, 128, 0, s>>>(m, g, it, w.list, n, id0, c0, src, verts, iso, st)
   if (edge_mode == 0)
-    vertex_kernel<false, false><<<blocks, 128, 0, s>>>(m, g, it, w.list, n, id0, c0, src, verts,
-                                                       iso, st);
+    QJ_VK(false, false, false);
   else if (pow_ref)
-    vertex_kernel<true, true><<<blocks, 128, 0, s>>>(m, g, it, w.list, n, id0, c0, src, verts,
-                                                     iso, st);
+    hybrid ? QJ_VK(true, true, true) : QJ_VK(true, true, false);
   else
-    vertex_kernel<true, false><<<blocks, 128, 0, s>>>(m, g, it, w.list, n, id0, c0, src, verts,
-                                                      iso, st);
+    hybrid ? QJ_VK(true, false, true) : QJ_VK(true, false, false);
+#undef QJ_VK
   return cudaGetLastError();
 }
 

@@ -117,6 +117,7 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
       st.field.refined += fs.refined;
       st.field.refined_iters += fs.refined_iters;
       st.field.nonfinite += fs.nonfinite;
+      st.field.lane_iters += fs.lane_iters;
       src = ctx->m_field;
     } else {
       src = d_field + (size_t)c0 * XY;
@@ -149,7 +150,9 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
     if ((rc = grow_keep(ctx, &ctx->m_verts, &ctx->m_verts_cap, (size_t)(nv + n_new) * 3,
                         (size_t)nv * 3, s)))
       return rc;
-    QJ_CUDA(ctx, qj::mesh_vertices(*m, g, it, edge_mode, pow_ref, w, n_new, nv, c0, src,
+    // FP32-first bisection unless the plain FP64 form is asked for
+    const bool hybrid = iter && iter->precision != QJG_FP64;
+    QJ_CUDA(ctx, qj::mesh_vertices(*m, g, it, edge_mode, pow_ref, hybrid, w, n_new, nv, c0, src,
                                    ctx->m_verts, iso, ctx->d_mstats, s));
     if (n_new) ctx->launches++;
     nv += n_new;
@@ -171,6 +174,7 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
   QJ_CUDA(ctx, cudaStreamSynchronize(s));
   st.map_evals = (int64_t)ds.aux[1];
   st.n_unbracketed = (int64_t)ds.aux[2];
+  st.map_evals_fp32 = (int64_t)ds.aux[3];
   if (nt > tcap || ((v64 || v32) && nv > vcap)) {
     if (out) *out = st;
     return fail(ctx, QJG_ERR_CAPACITY, "mesh needs %lld vertices / %lld triangles (capacity %lld / %lld)",

@@ -262,4 +262,110 @@ __device__ __forceinline__ double escape64(const MapParams& m, const IterParams&
   return f;
 }
 
+// ------------------------------------------------------- FP32 map
+
+// Exponents other than 1 and 2 (kept out of line, off the hot path).
+static __device__ __noinline__ q32::Q root_power_rare(q32::Q d, int ie, float e) {
+  return ie > 0 ? q32::qpow_int(d, ie) : q32::qpow(d, e);
+}
+
+// One root term (q - r_i)^(e_i) in FP32; with DE, adds (+-e_i) d/|d|^2 to g.
+// Root coordinates come as one 16-byte constant-bank load and {+-e, integer
+// exponent} as one 8-byte load.
+template <bool DE>
+__device__ __forceinline__ q32::Q root_term32(const MapParams& m, const q32::Q& q, int i,
+                                              q32::Q& g) {
+  using namespace q32;
+  const float4 root = *reinterpret_cast<const float4*>(m.r32[i]);
+  const float2 ex = *reinterpret_cast<const float2*>(m.x32[i]);
+  const Q d = {q.w - root.x, q.x - root.y, q.y - root.z, q.z - root.w};
+  if (DE) {
+    const float k = __fdividef(ex.x, norm2(d));
+    g.w = fmaf(k, d.w, g.w);
+    g.x = fmaf(k, d.x, g.x);
+    g.y = fmaf(k, d.y, g.y);
+    g.z = fmaf(k, d.z, g.z);
+  }
+  const int ie = __float_as_int(ex.y);
+  if (ie == 1) return d;
+  if (ie == 2) return qsq(d);
+  return root_power_rare(d, ie, m.e32[i]);
+}
+
+// prod_{i in [lo, hi)} (q - r_i)^(e_i), left to right; the first term starts
+// the product and the rest go two per trip.
+template <bool DE>
+__device__ __forceinline__ q32::Q product32(const MapParams& m, const q32::Q& q, int lo, int hi,
+                                            q32::Q& g) {
+  using namespace q32;
+  Q r = root_term32<DE>(m, q, lo, g);
+  int i = lo + 1;
+#pragma unroll 1
+  for (; i + 1 < hi; i += 2) {
+    const Q t0 = root_term32<DE>(m, q, i, g);
+    const Q t1 = root_term32<DE>(m, q, i + 1, g);
+    r = qmul(qmul(r, t0), t1);
+  }
+  if (i < hi) r = qmul(r, root_term32<DE>(m, q, i, g));
+  return r;
+}
+
+template <bool DE>
+__device__ __forceinline__ q32::Q apply32(const MapParams& m, const q32::Q& q, float* g2) {
+  using namespace q32;
+  Q g = {0.f, 0.f, 0.f, 0.f};
+  const Q top = product32<DE>(m, q, 0, m.nt, g);
+  Q out;
+  if (m.nb > 0) {
+    const Q bot = product32<DE>(m, q, m.nt, m.nt + m.nb, g);
+    const float inv = __fdividef(m.scalef, norm2(bot));
+    out = qmul_conj(top, bot);
+    out.w *= inv;
+    out.x *= inv;
+    out.y *= inv;
+    out.z *= inv;
+  } else {
+    out = top;
+    out.w *= m.scalef;
+    out.x *= m.scalef;
+    out.y *= m.scalef;
+    out.z *= m.scalef;
+  }
+  if (DE) *g2 = norm2(g);
+  return out;
+}
+
+// The FP32 escape loop at an arbitrary point with the distance estimate:
+// returns log|q_N| and, through *err, a conservative bound on its FP32
+// error: 64 * 2^-24 * (|q_0| + 1) * |q_N'| / |q_N|, the first-order growth
+// of a relative perturbation of the start point through the orbit (64 covers
+// the rounding of every root term and iteration).  *err is infinite when
+// FP32 cannot follow the orbit (|q| below 1e-18, overflow).
+__device__ __forceinline__ float escape32(const MapParams& m, const IterParams& it,
+                                          const double p[3], double slice, float* err) {
+  using namespace q32;
+  Q q = {(float)p[0], (float)p[1], (float)p[2], (float)slice};
+  const float q0 = sqrtf(norm2(q));
+  const float esc2 = (float)(it.escape * it.escape);
+  float m2 = norm2(q), l2d = 0.f;
+  int n = 0;
+  bool bad = false;
+  while (m2 < esc2 && n < it.max_it) {
+    float gg = 0.f;
+    q = apply32<true>(m, q, &gg);
+    m2 = norm2(q);
+    l2d += 0.5f * (__log2f(gg) + __log2f(m2));
+    n++;
+    if (m2 < 1e-36f) {
+      bad = true;
+      break;
+    }
+  }
+  const float f = 0.5f * logf(m2);
+  const float e = 64.f * 5.9604645e-8f * (q0 + 1.f) * exp2f(l2d - 0.5f * __log2f(m2));
+  *err = (bad || !isfinite(f) || isnan(e)) ? __int_as_float(0x7f800000) : e;
+  return f;
+}
+
 }  // namespace qj
+

@@ -23,7 +23,7 @@ cudaError_t launch_tanh_grad(const MapParams& m, const GridParams& g, const Weig
 int sq_max_iterations();
 cudaError_t launch_sq_energy(bool fp64, bool grad, const double* params, int nt, int nb,
                              const double* xyz, const double* target, long long n, double slice,
-                             int max_it, double escape, double* partials, int nblocks,
-                             double* out, int* iters, cudaStream_t s);
+                             int max_it, double escape, double d_sat, double* partials,
+                             int nblocks, double* out, int* iters, cudaStream_t s);
 
 }  // namespace qj

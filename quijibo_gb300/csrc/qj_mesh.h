@@ -28,9 +28,9 @@ cudaError_t mesh_vertex_ids(MeshWindow& w, int j0, int j1, int lay_lo, int lay_h
                             long long running, long long* n_new, cudaStream_t s,
                             const std::function<cudaError_t(long long)>& ensure_list);
 cudaError_t mesh_vertices(const MapParams& m, const GridParams& g, const IterParams& it,
-                          int edge_mode, bool pow_ref, const MeshWindow& w, long long n,
-                          long long id0, int c0, const double* src, double* verts, double iso,
-                          DevStats* st, cudaStream_t s);
+                          int edge_mode, bool pow_ref, bool hybrid, const MeshWindow& w,
+                          long long n, long long id0, int c0, const double* src, double* verts,
+                          double iso, DevStats* st, cudaStream_t s);
 cudaError_t mesh_triangles(MeshWindow& w, int j0, int j1, long long running, int32_t* tris,
                            long long cap, long long* n_new, cudaStream_t s);
 cudaError_t mesh_filter(const int32_t* tris, long long n, const double* verts, int32_t* out,

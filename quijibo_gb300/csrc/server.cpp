@@ -160,8 +160,8 @@ void run_job(qjg_ctx* ctx, cudaStream_t s, Job& j) {
     double e = 0;
     if (rc == QJG_OK)
       rc = qjg_energy_backward(ctx, d_p, r.n_top, r.n_bot, r.n_samples, d_x, d_t, r.grid.slice,
-                               r.max_it, r.escape, r.precision == QJG_FP64 ? QJG_FP64 : QJG_FP32,
-                               &e, d_g, s);
+                               r.max_it, r.escape, r.d_sat,
+                               r.precision == QJG_FP64 ? QJG_FP64 : QJG_FP32, &e, d_g, s);
     out.energy = e;
     if (rc == QJG_OK && r.out_grad &&
         cudaMemcpyAsync(r.out_grad, d_g, P * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess)

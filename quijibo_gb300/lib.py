@@ -43,7 +43,8 @@ class QjgIter(C.Structure):
 
 class QjgFieldStats(C.Structure):
     _fields_ = [("voxels", C.c_int64), ("voxel_iters", C.c_int64), ("root_terms", C.c_int64),
-                ("refined", C.c_int64), ("refined_iters", C.c_int64), ("nonfinite", C.c_int64)]
+                ("refined", C.c_int64), ("refined_iters", C.c_int64), ("nonfinite", C.c_int64),
+                ("lane_iters", C.c_int64)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}
@@ -54,7 +55,8 @@ QJG_EDGE_LINEAR, QJG_EDGE_BISECT = 0, 1
 
 class QjgMeshStats(C.Structure):
     _fields_ = [("n_verts", C.c_int64), ("n_tris", C.c_int64), ("n_degenerate", C.c_int64),
-                ("n_unbracketed", C.c_int64), ("map_evals", C.c_int64), ("slabs", C.c_int64),
+                ("n_unbracketed", C.c_int64), ("map_evals", C.c_int64),
+                ("map_evals_fp32", C.c_int64), ("slabs", C.c_int64),
                 ("field", QjgFieldStats)]
 
     def as_dict(self):
@@ -82,7 +84,8 @@ class QjgRequest(C.Structure):
                 ("bot_powers", _dp), ("sigma_top", C.c_double), ("sigma_bot", C.c_double),
                 ("scale", C.c_double), ("grid", QjgGrid), ("max_it", C.c_int32),
                 ("escape", C.c_double), ("iso", C.c_double), ("vert_cap", C.c_int64),
-                ("tri_cap", C.c_int64), ("params", _dp), ("n_samples", C.c_int64), ("xyz", _dp),
+                ("tri_cap", C.c_int64), ("params", _dp), ("d_sat", C.c_double),
+                ("n_samples", C.c_int64), ("xyz", _dp),
                 ("target", _dp), ("out_field", _dp), ("out_verts", _dp),
                 ("out_tris", C.POINTER(C.c_int32)), ("out_grad", _dp)]
 
@@ -129,14 +132,14 @@ EXPORTS = {
                              C.POINTER(QjgGrid), C.c_void_p, C.c_double, C.c_double, _dp, _dp,
                              C.c_void_p, C.POINTER(QjgTanhStats), C.c_void_p], C.c_int),
     "qjg_energy_forward": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p,
-                            C.c_void_p, C.c_double, C.c_int32, C.c_double, C.c_int32, _dp,
-                            C.c_void_p, C.c_void_p], C.c_int),
+                            C.c_void_p, C.c_double, C.c_int32, C.c_double, C.c_double, C.c_int32,
+                            _dp, C.c_void_p, C.c_void_p], C.c_int),
     "qjg_energy_backward": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p,
-                             C.c_void_p, C.c_double, C.c_int32, C.c_double, C.c_int32, _dp,
-                             C.c_void_p, C.c_void_p], C.c_int),
+                             C.c_void_p, C.c_double, C.c_int32, C.c_double, C.c_double, C.c_int32,
+                             _dp, C.c_void_p, C.c_void_p], C.c_int),
     "qjg_fit_lbfgs": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p,
-                       C.c_void_p, C.c_double, C.c_int32, C.c_double, C.c_int32, C.c_int32,
-                       C.c_int32, _dp, C.POINTER(QjgFitStats), C.c_void_p], C.c_int),
+                       C.c_void_p, C.c_double, C.c_int32, C.c_double, C.c_double, C.c_int32,
+                       C.c_int32, C.c_int32, _dp, C.POINTER(QjgFitStats), C.c_void_p], C.c_int),
     "qjg_server_create": ([C.c_int, C.c_int32, C.c_int64, C.POINTER(C.c_void_p)], C.c_int),
     "qjg_server_destroy": ([C.c_void_p], None),
     "qjg_server_submit": ([C.c_void_p, C.POINTER(QjgRequest), C.POINTER(C.c_int64)], C.c_int),
@@ -313,32 +316,35 @@ class Context:
         return score.value, grad, {k: int(getattr(st, k)) for k, _ in st._fields_}
 
     def energy(self, d_params, n_top, n_bot, n, d_xyz, d_target, max_it, escape, slice_=0.0,
-               precision=QJG_FP64, d_grad=0, d_iters=0, stream=None):
+               precision=QJG_FP64, d_grad=0, d_iters=0, d_sat=1.0, stream=None):
         """Squared-error energy (and, with d_grad, its gradient into d_grad)."""
         e = C.c_double()
         if d_grad:
             rc = self.L.qjg_energy_backward(self.h, C.c_void_p(d_params), n_top, n_bot, int(n),
                                             C.c_void_p(d_xyz), C.c_void_p(d_target), float(slice_),
-                                            int(max_it), float(escape), int(precision), C.byref(e),
-                                            C.c_void_p(d_grad), C.c_void_p(stream or 0))
+                                            int(max_it), float(escape), float(d_sat),
+                                            int(precision), C.byref(e), C.c_void_p(d_grad),
+                                            C.c_void_p(stream or 0))
             self._check(rc, "qjg_energy_backward")
         else:
             rc = self.L.qjg_energy_forward(self.h, C.c_void_p(d_params), n_top, n_bot, int(n),
                                            C.c_void_p(d_xyz), C.c_void_p(d_target), float(slice_),
-                                           int(max_it), float(escape), int(precision), C.byref(e),
-                                           C.c_void_p(d_iters), C.c_void_p(stream or 0))
+                                           int(max_it), float(escape), float(d_sat),
+                                           int(precision), C.byref(e), C.c_void_p(d_iters),
+                                           C.c_void_p(stream or 0))
             self._check(rc, "qjg_energy_forward")
         return e.value
 
 
 def _fit(self, d_params, n_top, n_bot, n, d_xyz, d_target, max_it, escape, steps, history=8,
-         slice_=0.0, precision=QJG_FP32, stream=None):
+         slice_=0.0, precision=QJG_FP32, d_sat=1.0, stream=None):
     """Device L-BFGS fit; returns (energies per step, stats dict)."""
     en = np.zeros(steps + 1)
     st = QjgFitStats()
     self._check(self.L.qjg_fit_lbfgs(self.h, C.c_void_p(d_params), n_top, n_bot, int(n),
                                      C.c_void_p(d_xyz), C.c_void_p(d_target), float(slice_),
-                                     int(max_it), float(escape), int(precision), int(steps),
+                                     int(max_it), float(escape), float(d_sat), int(precision),
+                                     int(steps),
                                      int(history), en.ctypes.data_as(_dp), C.byref(st),
                                      C.c_void_p(stream or 0)), "qjg_fit_lbfgs")
     d = {k: getattr(st, k) for k, _ in st._fields_}
@@ -388,9 +394,10 @@ class Server:
 
     def submit(self, kind, rs=None, grid=None, max_it=20, escape=2.0, precision=QJG_FP32_REFINE,
                iso=0.0, vert_cap=0, tri_cap=0, params=None, xyz=None, target=None,
-               out_field=None, out_verts=None, out_tris=None, out_grad=None):
+               out_field=None, out_verts=None, out_tris=None, out_grad=None, d_sat=1.0):
         r = QjgRequest()
         r.kind, r.precision, r.max_it, r.escape, r.iso = kind, precision, max_it, escape, iso
+        r.d_sat = d_sat
         keep = []
 
         def arr(a, shape=None):
