@@ -26,6 +26,12 @@ int qjg_last_timings(qjg_ctx* ctx, float* ms_bulk, float* ms_refine);
 /* Kernels this context has launched since it was created. */
 int64_t qjg_launch_count(qjg_ctx* ctx);
 
+/* Process-wide choice of the FP32 bulk field kernel, for A/B timing and the
+ * bit-equality test of the two forms: 1 (the default) two voxels per lane on
+ * the packed f32x2 instructions, 0 one voxel per lane.  Both give the same
+ * bits.  Set it while no field call is in flight. */
+int qjg_set_field32_pairs(int on);
+
 /* FP32 FMA-pipe probe: runs a kernel of independent FMA chains on every SM
  * of `device` and returns the achieved FP32 TFLOP/s (2 flops per FMA). */
 int qjg_fma_probe(int device, double* tflops);

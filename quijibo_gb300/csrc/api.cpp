@@ -95,6 +95,44 @@ MapParams* qj_lookup(qjg_ctx* ctx, qjg_rootset rs) {
   return ctx->rootsets[rs].get();
 }
 
+int qj_fill_map(MapParams* m, int n_top, const double* top_roots, const double* top_powers,
+                double sigma_top, int n_bot, const double* bot_roots, const double* bot_powers,
+                double sigma_bot, double scale) {
+  std::memset(m, 0, sizeof(MapParams));
+  m->nt = n_top;
+  m->nb = n_bot;
+  m->scale = scale;
+  m->scalef = (float)scale;
+  m->sigma[0] = sigma_top;
+  m->sigma[1] = sigma_bot;
+  m->all_int = 1;
+  for (int i = 0; i < n_top + n_bot; i++) {
+    const bool top = i < n_top;
+    const double* r = top ? top_roots + 4 * i : bot_roots + 4 * (i - n_top);
+    const double pw = top ? top_powers[i] : bot_powers[i - n_top];
+    // _powerScalar * _rootPowers[x], POLYNOMIAL_4D.cpp:914, 919
+    const double e = (top ? sigma_top : sigma_bot) * pw;
+    if (!std::isfinite(e)) return i;
+    for (int c = 0; c < 4; c++) {
+      if (!std::isfinite(r[c])) return i;
+      m->r64[i][c] = r[c];
+      m->r32[i][c] = (float)r[c];
+      m->rn2[i][c] = make_float2(-m->r32[i][c], -m->r32[i][c]);
+    }
+    m->e64[i] = e;
+    m->ep[i] = pw;
+    m->e32[i] = (float)e;
+    const bool integral = (e == std::floor(e)) && e >= 1 && e <= QJ_MAX_INT_EXP;
+    m->ie[i] = integral ? (int)e : 0;
+    if (!integral) m->all_int = 0;
+    m->x32[i][0] = top ? (float)e : -(float)e;
+    m->ex2[i] = make_float2(m->x32[i][0], m->x32[i][0]);
+    const int ie_bits = m->ie[i];
+    std::memcpy(&m->x32[i][1], &ie_bits, sizeof ie_bits);
+  }
+  return -1;
+}
+
 extern "C" {
 
 int qjg_create(int device, qjg_ctx** out) {
@@ -119,6 +157,9 @@ void qjg_destroy(qjg_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   cudaFree(ctx->d_stats);
   cudaFree(ctx->d_list);
+  cudaFree(ctx->d_sorted);
+  cudaFree(ctx->d_keys);
+  cudaFree(ctx->d_hist);
   cudaFree(ctx->d_field);
   cudaFree(ctx->d_de);
   cudaFree(ctx->d_mstats);
@@ -149,36 +190,9 @@ int qjg_rootset_upload(qjg_ctx* ctx, int32_t n_top, const double* top_roots,
   if (!top_roots || !top_powers || (n_bot > 0 && (!bot_roots || !bot_powers)))
     return fail(ctx, QJG_ERR_ARG, "root or power array is NULL");
   std::unique_ptr<MapParams> m(new MapParams());
-  std::memset(m.get(), 0, sizeof(MapParams));
-  m->nt = n_top;
-  m->nb = n_bot;
-  m->scale = scale;
-  m->scalef = (float)scale;
-  m->sigma[0] = sigma_top;
-  m->sigma[1] = sigma_bot;
-  m->all_int = 1;
-  for (int i = 0; i < n_top + n_bot; i++) {
-    const bool top = i < n_top;
-    const double* r = top ? top_roots + 4 * i : bot_roots + 4 * (i - n_top);
-    const double pw = top ? top_powers[i] : bot_powers[i - n_top];
-    // _powerScalar * _rootPowers[x], POLYNOMIAL_4D.cpp:914, 919
-    const double e = (top ? sigma_top : sigma_bot) * pw;
-    for (int c = 0; c < 4; c++) {
-      if (!std::isfinite(r[c])) return fail(ctx, QJG_ERR_ARG, "root %d is not finite", i);
-      m->r64[i][c] = r[c];
-      m->r32[i][c] = (float)r[c];
-    }
-    if (!std::isfinite(e)) return fail(ctx, QJG_ERR_ARG, "exponent %d is not finite", i);
-    m->e64[i] = e;
-    m->ep[i] = pw;
-    m->e32[i] = (float)e;
-    const bool integral = (e == std::floor(e)) && e >= 1 && e <= QJ_MAX_INT_EXP;
-    m->ie[i] = integral ? (int)e : 0;
-    if (!integral) m->all_int = 0;
-    m->x32[i][0] = top ? (float)e : -(float)e;
-    const int ie_bits = m->ie[i];
-    std::memcpy(&m->x32[i][1], &ie_bits, sizeof ie_bits);
-  }
+  const int bad = qj_fill_map(m.get(), n_top, top_roots, top_powers, sigma_top, n_bot, bot_roots,
+                              bot_powers, sigma_bot, scale);
+  if (bad >= 0) return fail(ctx, QJG_ERR_ARG, "root %d or its exponent is not finite", bad);
   ctx->rootsets.push_back(std::move(m));
   *out = (qjg_rootset)(ctx->rootsets.size() - 1);
   return QJG_OK;
@@ -211,20 +225,25 @@ int qjg_field(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
   const GridParams g = qj_grid_params(grid, z0, z1);
   IterParams it = qj_iter_params(iter, grid);
   const bool pow_ref = iter->refine_pow == QJG_REFINE_POW || !m->all_int;
-  if (refine && (rc = ensure(ctx, &ctx->d_list, &ctx->list_cap, (size_t)n))) return rc;
+  if (refine && ((rc = ensure(ctx, &ctx->d_list, &ctx->list_cap, (size_t)n)) ||
+                 (rc = ensure(ctx, &ctx->d_sorted, &ctx->sorted_cap, (size_t)n)) ||
+                 (rc = ensure(ctx, &ctx->d_keys, &ctx->keys_cap, (size_t)n)) ||
+                 (rc = ensure(ctx, &ctx->d_hist, &ctx->hist_cap, (size_t)qj::REFINE_KEYS))))
+    return rc;
   QJ_CUDA(ctx, cudaMemsetAsync(ctx->d_stats, 0, sizeof(DevStats), s));
   if (ctx->timing) QJ_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
   if (iter->precision == QJG_FP64) {
     QJ_CUDA(ctx, qj::launch_field64(*m, g, it, pow_ref, d_field, d_de, ctx->d_stats, s));
   } else {
-    QJ_CUDA(ctx, qj::launch_field32(*m, g, it, refine, d_field, d_de, ctx->d_list, ctx->d_stats, s));
+    QJ_CUDA(ctx, qj::launch_field32(*m, g, it, refine, d_field, d_de, ctx->d_list, ctx->d_keys,
+                                    ctx->d_stats, s));
   }
   ctx->launches++;
   if (ctx->timing) QJ_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
   if (refine) {
-    QJ_CUDA(ctx, qj::launch_refine64(*m, g, it, pow_ref, ctx->d_list, d_field, d_de,
-                                     ctx->d_stats, s));
-    ctx->launches++;
+    QJ_CUDA(ctx, qj::launch_refine64(*m, g, it, pow_ref, ctx->d_list, ctx->d_keys,
+                                     ctx->d_sorted, ctx->d_hist, d_field, d_de, ctx->d_stats, s));
+    ctx->launches += 4;  // histogram, offsets, scatter, refine
   }
   if (ctx->timing) QJ_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
   ctx->timed_refine = refine;
@@ -312,5 +331,10 @@ int qjg_last_timings(qjg_ctx* ctx, float* ms_bulk, float* ms_refine) {
 }
 
 int64_t qjg_launch_count(qjg_ctx* ctx) { return ctx ? ctx->launches : -1; }
+
+int qjg_set_field32_pairs(int on) {
+  qj::set_field32_pairs(on);
+  return QJG_OK;
+}
 
 }  // extern "C"

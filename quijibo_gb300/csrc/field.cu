@@ -29,9 +29,9 @@ struct TileMap {
   long long per_slice, total;
 };
 
-__device__ __forceinline__ TileMap tile_map(const GridParams& g) {
+__device__ __forceinline__ TileMap tile_map(const GridParams& g, int tile_x = TILE_X) {
   TileMap t;
-  t.tx_n = (g.X + TILE_X - 1) / TILE_X;
+  t.tx_n = (g.X + tile_x - 1) / tile_x;
   t.ty_n = (g.Y + TILE_Y - 1) / TILE_Y;
   t.per_slice = (long long)t.tx_n * t.ty_n;
   t.total = t.per_slice * (g.z1 - g.z0);
@@ -114,17 +114,90 @@ __global__ void __launch_bounds__(128) refine64_kernel(const __grid_constant__ M
 
 // ------------------------------------------------------------------ FP32
 
+// Sort key of a refine-list entry: the FP32 orbit length, which predicts the
+// FP64 one.
+__device__ __forceinline__ uint8_t refine_key(int n) { return (uint8_t)min(n, 255); }
+
+// Escape state of one voxel's FP32 orbit.
+struct Orbit32 {
+  float m2;           // |q_n|^2
+  float l2d;          // log2 |q_n'|
+  int n;
+  bool live, bad;     // still iterating; FP32 lost the orbit (|q| below 1e-18)
+  bool near;          // an iterate before the last lay within FP32 error of the escape radius
+  float err;          // first-order relative FP32 error of q_n (with DE)
+};
+
+__device__ __forceinline__ Orbit32 orbit_start(bool valid, float m2, float esc2, int max_it) {
+  return Orbit32{m2, 0.f, 0, valid && m2 < esc2 && max_it > 0, false, false, q32::EPS32};
+}
+
+// One map application's bookkeeping, the loop test of the reference escape
+// loop (OPTIMIZE_3D.cpp:1317-1362) included.
+template <bool DE>
+__device__ __forceinline__ void orbit_step(Orbit32& o, float m2, float gg, float esc2,
+                                           int max_it) {
+  if (!o.live) return;
+  if (DE) {
+    o.near = o.near || q32::near_radius(o.m2, esc2, o.err);
+    o.err = q32::propagate_err(o.err, gg, o.m2);
+    o.l2d += 0.5f * (__log2f(gg) + __log2f(m2));
+  }
+  o.m2 = m2;
+  o.n++;
+  // |q| below 1e-18: |q|^2 nears the bottom of the FP32 range, where FP32
+  // cannot follow the reference's 10*FLT_MIN exit; hand to FP64
+  if (m2 < 1e-36f) {
+    o.bad = true;
+    o.live = false;
+  } else {
+    o.live = m2 < esc2 && o.n < max_it;
+  }
+}
+
+// Field value, distance estimate and the refine decision of a finished
+// orbit; writes the voxel unless it goes to the FP64 refine list.
+template <bool DE>
+__device__ __forceinline__ bool orbit_finish(const Orbit32& o, const IterParams& it, float esc2,
+                                             float l2band, int refine, long long i,
+                                             double* __restrict__ field, float* __restrict__ de,
+                                             unsigned long long& nonfinite_acc) {
+  const float f = 0.5f * logf(o.m2);
+  // d = |q| log|q| / |q'| kept as log2|d|: contracting orbits drive |q'|
+  // below the FP32 range long before d itself matters
+  float l2abs_d = 0.f, d = 0.f;
+  if (DE) {
+    l2abs_d = __log2f(fabsf(f)) + 0.5f * __log2f(o.m2) - o.l2d;
+    d = copysignf(exp2f(l2abs_d), f);
+  }
+  const bool bad = o.bad || !isfinite(f) || (DE && isnan(l2abs_d));
+  nonfinite_acc += bad;
+  // the escape test is a discontinuity: where an iterate lies within FP32
+  // error of the escape radius, FP64 may stop the orbit at a different
+  // iterate.  The last iterate of an orbit cut by max_it is the same
+  // iterate on either side of the radius.
+  const bool near_escape =
+      DE && (o.near || (o.m2 >= esc2 && o.n < it.max_it && q32::near_radius(o.m2, esc2, o.err)));
+  const bool need = refine && (bad || near_escape || l2abs_d < l2band ||
+                               fabsf(f) < (float)it.field_tol);
+  if (!need) {
+    field[i] = (double)f;
+    if (DE && de) de[i] = d;
+  }
+  return need;
+}
+
+// One voxel per lane: the form the mesher's bisection shares (escape32).
 template <bool DE>
 __global__ void __launch_bounds__(128) field32_kernel(const __grid_constant__ MapParams m,
                                                       const GridParams g, const IterParams it, double* __restrict__ field,
                                                       float* __restrict__ de, uint32_t* refine_list,
-                                                      int refine, DevStats* st) {
+                                                      uint8_t* refine_keys, int refine, DevStats* st) {
   using namespace q32;
   const TileMap tm = tile_map(g);
   const int lane = threadIdx.x & 31;
   const float esc2 = (float)(it.escape * it.escape);
-  const float l2band = log2f((float)it.band), ftol = (float)it.field_tol;
-  const float esc_tol = 2e-3f;  // relative, on |q|^2
+  const float l2band = log2f((float)it.band);
   unsigned long long iters_acc = 0, nonfinite_acc = 0, lane_iters_acc = 0;
   for (;;) {
     const long long t = next_tile(&st->tiles_done);
@@ -134,57 +207,21 @@ __global__ void __launch_bounds__(128) field32_kernel(const __grid_constant__ Ma
     const int x = (int)(r % tm.tx_n) * TILE_X + (lane & 7);
     const int y = (int)(r / tm.tx_n) * TILE_Y + (lane >> 3);
     const bool valid = (x < g.X && y < g.Y);
-    bool need = false;
-    long long i = 0;
-    int n_exec = 0;
-    if (valid) {
-      double p[3];
-      cell_center(g, x, y, g.z0 + zl, p);
-      Q q = {(float)p[0], (float)p[1], (float)p[2], (float)g.slice};
-      float m2 = norm2(q), m2_prev = m2;
-      float l2d = 0.f;  // log2 |q_n'|
-      int n = 0;
-      bool bad = false;
-      while (m2 < esc2 && n < it.max_it) {
-        float gg = 0.f;
-        q = apply32<DE>(m, q, &gg);
-        m2_prev = m2;
-        m2 = norm2(q);
-        if (DE) l2d += 0.5f * (__log2f(gg) + __log2f(m2));
-        n++;
-        // |q| below 1e-18: |q|^2 nears the bottom of the FP32 range, where
-        // FP32 cannot follow the reference's 10*FLT_MIN exit; hand to FP64
-        if (m2 < 1e-36f) {
-          bad = true;
-          break;
-        }
-      }
-      iters_acc += n;
-      n_exec = n;
-      const float f = 0.5f * logf(m2);
-      // d = |q| log|q| / |q'| kept as log2|d|: contracting orbits drive |q'|
-      // below the FP32 range long before d itself matters
-      float l2abs_d = 0.f, d = 0.f;
-      if (DE) {
-        l2abs_d = __log2f(fabsf(f)) + 0.5f * __log2f(m2) - l2d;
-        d = copysignf(exp2f(l2abs_d), f);
-      }
-      bad = bad || !isfinite(f) || (DE && isnan(l2abs_d));
-      nonfinite_acc += bad;
-      // the escape test is a discontinuity: an orbit whose escaping iterate
-      // (or the one before it) lies within FP32 error of the escape radius
-      // may escape one iteration earlier or later in FP64
-      const bool near_escape = n > 0 && m2 >= esc2 &&
-                               (fabsf(m2 - esc2) < esc_tol * esc2 || fabsf(m2_prev - esc2) < esc_tol * esc2);
-      need = refine && (bad || near_escape || l2abs_d < l2band || fabsf(f) < ftol);
-      i = ((long long)zl * g.Y + y) * g.X + x;
-      if (!need) {
-        field[i] = (double)f;
-        if (DE && de) de[i] = d;
-      }
+    double p[3];
+    cell_center(g, x, y, g.z0 + zl, p);
+    Q q = {(float)p[0], (float)p[1], (float)p[2], (float)g.slice};
+    Orbit32 o = orbit_start(valid, norm2(q), esc2, it.max_it);
+    while (o.live) {
+      float gg = 0.f;
+      q = apply32<DE>(m, q, &gg);
+      orbit_step<DE>(o, norm2(q), gg, esc2, it.max_it);
     }
+    iters_acc += o.n;
+    const long long i = ((long long)zl * g.Y + y) * g.X + x;
+    const bool need =
+        valid && orbit_finish<DE>(o, it, esc2, l2band, refine, i, field, de, nonfinite_acc);
     // lane slots the warp spent: 32 x its longest orbit
-    const unsigned wmax = __reduce_max_sync(0xffffffffu, (unsigned)n_exec);
+    const unsigned wmax = __reduce_max_sync(0xffffffffu, (unsigned)o.n);
     if (lane == 0) lane_iters_acc += 32ull * wmax;
     // warp-aggregated append to the refine list
     const unsigned mask = __ballot_sync(0xffffffffu, need);
@@ -192,7 +229,89 @@ __global__ void __launch_bounds__(128) field32_kernel(const __grid_constant__ Ma
       unsigned long long base = 0;
       if (lane == 0) base = atomicAdd(&st->refined, (unsigned long long)__popc(mask));
       base = __shfl_sync(0xffffffffu, base, 0);
-      if (need) refine_list[base + __popc(mask & ((1u << lane) - 1u))] = (uint32_t)i;
+      if (need) {
+        const unsigned long long slot = base + __popc(mask & ((1u << lane) - 1u));
+        refine_list[slot] = (uint32_t)i;
+        if (refine_keys) refine_keys[slot] = refine_key(o.n);
+      }
+    }
+  }
+  warp_add(&st->voxel_iters, iters_acc);
+  warp_add(&st->nonfinite, nonfinite_acc);
+  warp_add(&st->aux[3], lane_iters_acc);
+}
+
+// Two voxels per lane, (x, y) and (x + 1, y), on the packed f32x2 pipe
+// forms: one issue slot does the arithmetic of both orbits, and each orbit
+// rounds exactly as in field32_kernel.  Warp tile 16 x 4.  A lane runs until
+// both of its orbits stop; the one that stopped first keeps iterating
+// unobserved (its state is frozen in its Orbit32).
+static constexpr int TILE2_X = 16;
+
+template <bool DE>
+__global__ void __launch_bounds__(128) field32x2_kernel(const __grid_constant__ MapParams m,
+                                                        const GridParams g, const IterParams it,
+                                                        double* __restrict__ field,
+                                                        float* __restrict__ de,
+                                                        uint32_t* refine_list,
+                                                        uint8_t* refine_keys, int refine,
+                                                        DevStats* st) {
+  using namespace q32x2;
+  const TileMap tm = tile_map(g, TILE2_X);
+  const int lane = threadIdx.x & 31;
+  const float esc2 = (float)(it.escape * it.escape);
+  const float l2band = log2f((float)it.band);
+  unsigned long long iters_acc = 0, nonfinite_acc = 0, lane_iters_acc = 0;
+  for (;;) {
+    const long long t = next_tile(&st->tiles_done);
+    if (t >= tm.total) break;
+    const int zl = (int)(t / tm.per_slice);
+    const long long r = t - (long long)zl * tm.per_slice;
+    const int x = (int)(r % tm.tx_n) * TILE2_X + 2 * (lane & 7);
+    const int y = (int)(r / tm.tx_n) * TILE_Y + (lane >> 3);
+    const bool va = (x < g.X && y < g.Y), vb = (x + 1 < g.X && y < g.Y);
+    double pa[3], pb[3];
+    cell_center(g, x, y, g.z0 + zl, pa);
+    cell_center(g, x + 1, y, g.z0 + zl, pb);
+    Q2 q = {make_float2((float)pa[0], (float)pb[0]), make_float2((float)pa[1], (float)pb[1]),
+            make_float2((float)pa[2], (float)pb[2]), pair((float)g.slice)};
+    const float2 m20 = norm2(q);
+    Orbit32 a = orbit_start(va, m20.x, esc2, it.max_it);
+    Orbit32 b = orbit_start(vb, m20.y, esc2, it.max_it);
+    while (a.live || b.live) {
+      float2 gg = pair(0.f);
+      q = apply32x2<DE>(m, q, &gg);
+      const float2 m2 = norm2(q);
+      orbit_step<DE>(a, m2.x, gg.x, esc2, it.max_it);
+      orbit_step<DE>(b, m2.y, gg.y, esc2, it.max_it);
+    }
+    iters_acc += a.n + b.n;
+    const long long i = ((long long)zl * g.Y + y) * g.X + x;
+    const bool need_a =
+        va && orbit_finish<DE>(a, it, esc2, l2band, refine, i, field, de, nonfinite_acc);
+    const bool need_b =
+        vb && orbit_finish<DE>(b, it, esc2, l2band, refine, i + 1, field, de, nonfinite_acc);
+    // voxel slots the warp spent: 64 x its longest orbit
+    const unsigned wmax = __reduce_max_sync(0xffffffffu, (unsigned)max(a.n, b.n));
+    if (lane == 0) lane_iters_acc += 64ull * wmax;
+    // warp-aggregated append to the refine list, A voxels first
+    const unsigned ma = __ballot_sync(0xffffffffu, need_a);
+    const unsigned mb = __ballot_sync(0xffffffffu, need_b);
+    if (ma | mb) {
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(&st->refined, (unsigned long long)(__popc(ma) + __popc(mb)));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      const unsigned below = (1u << lane) - 1u;
+      if (need_a) {
+        const unsigned long long slot = base + __popc(ma & below);
+        refine_list[slot] = (uint32_t)i;
+        if (refine_keys) refine_keys[slot] = refine_key(a.n);
+      }
+      if (need_b) {
+        const unsigned long long slot = base + __popc(ma) + __popc(mb & below);
+        refine_list[slot] = (uint32_t)(i + 1);
+        if (refine_keys) refine_keys[slot] = refine_key(b.n);
+      }
     }
   }
   warp_add(&st->voxel_iters, iters_acc);
@@ -234,22 +353,117 @@ cudaError_t launch_field64(const MapParams& m, const GridParams& g, const IterPa
   return cudaGetLastError();
 }
 
+// 1: field32x2_kernel (the default), 0: field32_kernel
+static int g_field32_pairs = 1;
+
+void set_field32_pairs(int on) { g_field32_pairs = on ? 1 : 0; }
+
 cudaError_t launch_field32(const MapParams& m, const GridParams& g, const IterParams& it,
-                           bool refine, double* field, float* de, uint32_t* list, DevStats* st,
-                           cudaStream_t s) {
+                           bool refine, double* field, float* de, uint32_t* list, uint8_t* keys,
+                           DevStats* st, cudaStream_t s) {
   const bool want = it.want_de || refine;
+  const int r = refine ? 1 : 0;
+  if (g_field32_pairs) {
+    const void* fn =
+        want ? (const void*)field32x2_kernel<true> : (const void*)field32x2_kernel<false>;
+    const int blocks = grid_blocks(fn, 128);
+    if (want)
+      field32x2_kernel<true><<<blocks, 128, 0, s>>>(m, g, it, field, de, list, keys, r, st);
+    else
+      field32x2_kernel<false><<<blocks, 128, 0, s>>>(m, g, it, field, de, list, keys, 0, st);
+    return cudaGetLastError();
+  }
   const void* fn = want ? (const void*)field32_kernel<true> : (const void*)field32_kernel<false>;
   const int blocks = grid_blocks(fn, 128);
   if (want)
-    field32_kernel<true><<<blocks, 128, 0, s>>>(m, g, it, field, de, list, refine ? 1 : 0, st);
+    field32_kernel<true><<<blocks, 128, 0, s>>>(m, g, it, field, de, list, keys, r, st);
   else
-    field32_kernel<false><<<blocks, 128, 0, s>>>(m, g, it, field, de, list, 0, st);
+    field32_kernel<false><<<blocks, 128, 0, s>>>(m, g, it, field, de, list, keys, 0, st);
   return cudaGetLastError();
 }
 
+// ------------------------------------------------------ refine-list order
+// A refine warp runs until its longest orbit ends, and the list comes out of
+// the FP32 pass in tile order, where 1-iteration and 40-iteration orbits
+// share warps.  A counting sort by the FP32 orbit length (longest first)
+// gives each refine warp orbits of one length.
+
+__global__ void __launch_bounds__(256) refine_hist_kernel(const uint8_t* __restrict__ keys,
+                                                          const DevStats* counts,
+                                                          unsigned* __restrict__ hist) {
+  __shared__ unsigned sh[REFINE_KEYS];
+  for (int k = threadIdx.x; k < REFINE_KEYS; k += blockDim.x) sh[k] = 0;
+  __syncthreads();
+  const unsigned long long n = counts->refined;
+  for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < n;
+       k += (unsigned long long)gridDim.x * blockDim.x)
+    atomicAdd(&sh[keys[k]], 1u);
+  __syncthreads();
+  for (int k = threadIdx.x; k < REFINE_KEYS; k += blockDim.x)
+    if (sh[k]) atomicAdd(&hist[k], sh[k]);
+}
+
+// Counts -> first output slot of each key, largest key first (one block of
+// REFINE_KEYS threads; Hillis-Steele scan in shared memory).
+__global__ void __launch_bounds__(REFINE_KEYS) refine_offsets_kernel(unsigned* hist) {
+  __shared__ unsigned sh[REFINE_KEYS];
+  const int t = threadIdx.x;
+  const int key = REFINE_KEYS - 1 - t;
+  const unsigned c = hist[key];
+  sh[t] = c;
+  __syncthreads();
+  for (int o = 1; o < REFINE_KEYS; o <<= 1) {
+    const unsigned v = t >= o ? sh[t - o] : 0u;
+    __syncthreads();
+    sh[t] += v;
+    __syncthreads();
+  }
+  hist[key] = sh[t] - c;
+}
+
+// Scatter into key order; lanes with equal keys share one cursor update.
+__global__ void __launch_bounds__(256) refine_scatter_kernel(const uint32_t* __restrict__ list,
+                                                             const uint8_t* __restrict__ keys,
+                                                             const DevStats* counts,
+                                                             unsigned* __restrict__ cursor,
+                                                             uint32_t* __restrict__ out) {
+  const unsigned long long n = counts->refined;
+  const int lane = threadIdx.x & 31;
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  for (unsigned long long base = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) & ~31ull;
+       base < n; base += stride) {
+    const unsigned long long k = base + lane;
+    const bool v = k < n;
+    const int key = v ? (int)keys[k] : REFINE_KEYS;  // idle lanes group apart
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    const int leader = __ffs(peers) - 1;
+    unsigned pos = 0;
+    if (v && lane == leader) pos = atomicAdd(&cursor[key], (unsigned)__popc(peers));
+    pos = __shfl_sync(0xffffffffu, pos, leader);
+    if (v) out[pos + __popc(peers & ((1u << lane) - 1u))] = list[k];
+  }
+}
+
+static int sm_count() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms;
+}
+
 cudaError_t launch_refine64(const MapParams& m, const GridParams& g, const IterParams& it,
-                            bool pow_ref, const uint32_t* list, double* field, float* de,
+                            bool pow_ref, const uint32_t* list, const uint8_t* keys,
+                            uint32_t* sorted, unsigned* hist, double* field, float* de,
                             DevStats* st, cudaStream_t s) {
+  if (keys) {
+    cudaError_t e = cudaMemsetAsync(hist, 0, REFINE_KEYS * sizeof(unsigned), s);
+    if (e != cudaSuccess) return e;
+    const int blocks = 2 * sm_count();
+    refine_hist_kernel<<<blocks, 256, 0, s>>>(keys, st, hist);
+    refine_offsets_kernel<<<1, REFINE_KEYS, 0, s>>>(hist);
+    refine_scatter_kernel<<<blocks, 256, 0, s>>>(list, keys, st, hist, sorted);
+    list = sorted;
+  }
   const void* fn = pow_ref ? (const void*)refine64_kernel<true> : (const void*)refine64_kernel<false>;
   const int blocks = grid_blocks(fn, 128);
   if (pow_ref)

@@ -69,35 +69,9 @@ extern "C" int qjg_field_noalloc(int32_t n_top, const double* top_roots, const d
 
   // the map's launch parameters, built on the host stack
   qj::MapParams m;
-  std::memset(&m, 0, sizeof m);
-  m.nt = n_top;
-  m.nb = n_bot;
-  m.scale = scale;
-  m.scalef = (float)scale;
-  m.sigma[0] = sigma_top;
-  m.sigma[1] = sigma_bot;
-  m.all_int = 1;
-  for (int i = 0; i < n_top + n_bot; i++) {
-    const bool top = i < n_top;
-    const double* r = top ? top_roots + 4 * i : bot_roots + 4 * (i - n_top);
-    const double pw = top ? top_powers[i] : bot_powers[i - n_top];
-    const double e = (top ? sigma_top : sigma_bot) * pw;
-    for (int c = 0; c < 4; c++) {
-      if (!std::isfinite(r[c])) return QJG_ERR_ARG;
-      m.r64[i][c] = r[c];
-      m.r32[i][c] = (float)r[c];
-    }
-    if (!std::isfinite(e)) return QJG_ERR_ARG;
-    m.e64[i] = e;
-    m.ep[i] = pw;
-    m.e32[i] = (float)e;
-    const bool integral = (e == std::floor(e)) && e >= 1 && e <= QJ_MAX_INT_EXP;
-    m.ie[i] = integral ? (int)e : 0;
-    if (!integral) m.all_int = 0;
-    m.x32[i][0] = top ? (float)e : -(float)e;
-    const int ie_bits = m.ie[i];
-    std::memcpy(&m.x32[i][1], &ie_bits, sizeof ie_bits);
-  }
+  if (qj_fill_map(&m, n_top, top_roots, top_powers, sigma_top, n_bot, bot_roots, bot_powers,
+                  sigma_bot, scale) >= 0)
+    return QJG_ERR_ARG;
 
   unsigned char* scratch = nullptr;
   if ((rc = scratch_for_current_device(&scratch))) return rc;
@@ -115,7 +89,9 @@ extern "C" int qjg_field_noalloc(int32_t n_top, const double* top_roots, const d
   if (iter->precision == QJG_FP64)
     e = qj::launch_field64(m, g, it, pow_ref, d_field, d_de, st, s);
   else
-    e = qj::launch_field32(m, g, it, refine, d_field, d_de, list, st, s);
-  if (e == cudaSuccess && refine) e = qj::launch_refine64(m, g, it, pow_ref, list, d_field, d_de, st, s);
+    e = qj::launch_field32(m, g, it, refine, d_field, d_de, list, nullptr, st, s);
+  if (e == cudaSuccess && refine)
+    e = qj::launch_refine64(m, g, it, pow_ref, list, nullptr, nullptr, nullptr, d_field, d_de, st,
+                            s);
   return e == cudaSuccess ? QJG_OK : QJG_ERR_CUDA;
 }

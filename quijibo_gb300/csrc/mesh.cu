@@ -307,6 +307,16 @@ struct DegenEmit : DegenCount {
 // first and trusted when its value clears its error bound and the 1e-8 stop
 // test by a margin: then the FP64 value has the same sign and also fails the
 // stop test, so every decision of the search is the one FP64 would make.
+template <bool POW_REF>
+__device__ __forceinline__ double value64(const MapParams& m, const GridParams& g,
+                                          const IterParams& it, const double p[3], double iso,
+                                          unsigned long long* e64) {
+  (*e64)++;
+  int ni;
+  double dd;
+  return q64::sub(escape64<POW_REF, false>(m, it, p, g.slice, &ni, &dd), iso);
+}
+
 template <bool POW_REF, bool HYBRID>
 __device__ __forceinline__ double bisect_value(const MapParams& m, const GridParams& g,
                                                const IterParams& it, const double p[3], double iso,
@@ -320,10 +330,7 @@ __device__ __forceinline__ double bisect_value(const MapParams& m, const GridPar
       return (double)v;
     }
   }
-  (*e64)++;
-  int ni;
-  double dd;
-  return q64::sub(escape64<POW_REF, false>(m, it, p, g.slice, &ni, &dd), iso);
+  return value64<POW_REF>(m, g, it, p, iso, e64);
 }
 
 template <bool BISECT, bool POW_REF, bool HYBRID>
@@ -358,8 +365,13 @@ __global__ void __launch_bounds__(128) vertex_kernel(const __grid_constant__ Map
       for (int c = 0; c < 3; c++) out[c] = add(p0[c], mul(t, sub(p1[c], p0[c])));
     } else {
       // nonlinearValue at both ends (TRIANGLE_MESH.cpp:2060-2067)
-      const double f0 = bisect_value<POW_REF, HYBRID>(m, g, it, p0, iso, &evals32, &evals);
-      const double f1 = bisect_value<POW_REF, HYBRID>(m, g, it, p1, iso, &evals32, &evals);
+      double f0 = bisect_value<POW_REF, HYBRID>(m, g, it, p0, iso, &evals32, &evals);
+      double f1 = bisect_value<POW_REF, HYBRID>(m, g, it, p1, iso, &evals32, &evals);
+      if (HYBRID && mul(f0, f1) >= 0.0) {
+        // the end values decide the whole search: confirm a failed bracket in FP64
+        f0 = value64<POW_REF>(m, g, it, p0, iso, &evals);
+        f1 = value64<POW_REF>(m, g, it, p1, iso, &evals);
+      }
       double pv[3], nv[3], pval = f0, nval = f1;
       bool bad = mul(f0, f1) >= 0.0;
 #pragma unroll

@@ -19,6 +19,12 @@ struct qjg_ctx {
   qj::DevStats* d_stats = nullptr;  // counters of the current call
   uint32_t* d_list = nullptr;   // FP64 refine list
   size_t list_cap = 0;
+  uint32_t* d_sorted = nullptr; // the refine list in orbit-length order
+  size_t sorted_cap = 0;
+  uint8_t* d_keys = nullptr;    // FP32 orbit length of each refine entry
+  size_t keys_cap = 0;
+  unsigned* d_hist = nullptr;   // counting-sort counters
+  size_t hist_cap = 0;
   double* d_field = nullptr;    // staging for host-buffer calls
   float* d_de = nullptr;
   size_t buf_cap = 0;
@@ -85,6 +91,12 @@ inline int ensure(qjg_ctx* ctx, T** buf, size_t* cap, size_t n) {
 
 
 // shared by the field and mesh entry points (api.cpp)
+// Fills the launch parameters of the map s * prod (q - t_i)^(sigma_t e_i) /
+// prod (q - b_j)^(sigma_b f_j).  Returns -1 when every value is finite, else
+// the index of the first root (coordinate or exponent) that is not.
+int qj_fill_map(qj::MapParams* m, int n_top, const double* top_roots, const double* top_powers,
+                double sigma_top, int n_bot, const double* bot_roots, const double* bot_powers,
+                double sigma_bot, double scale);
 int qj_check_grid(qjg_ctx* ctx, const qjg_grid* g);
 int qj_check_iter(qjg_ctx* ctx, const qjg_iter* it);
 qj::GridParams qj_grid_params(const qjg_grid* g, int z0, int z1);

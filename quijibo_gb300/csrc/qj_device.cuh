@@ -125,6 +125,34 @@ __device__ __forceinline__ float norm2(const Q& q) {
   return fmaf(q.z, q.z, fmaf(q.y, q.y, fmaf(q.x, q.x, q.w * q.w)));
 }
 
+// FP32 error tracking along an orbit.  err is a first-order estimate of the
+// relative error of q_n: each map application scales the incoming relative
+// error by |grad log|R|| * |q| (the log-derivative the distance estimate
+// tracks) and adds ERR_STEP of fresh rounding (24-root maps round about
+// 100 times per application; ERR_STEP = 64 ulp covers them in RMS).
+constexpr float EPS32 = 5.9604645e-8f;  // 2^-24
+constexpr float ERR_STEP = 64.f * EPS32;
+
+__device__ __forceinline__ float propagate_err(float err, float gg, float m2_in) {
+  float amp;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(amp) : "f"(gg * m2_in));
+  return fmaf(err, amp, ERR_STEP);
+}
+
+// |q|^2 = m2 is within its FP32 error of the escape radius squared
+__device__ __forceinline__ bool near_radius(float m2, float esc2, float err) {
+  return fabsf(m2 - esc2) < 2.f * err * esc2;
+}
+
+// 1/x by the MUFU reciprocal (PTX rcp.approx.ftz.f32): about 1 ulp, subnormal
+// x taken as 0 (result inf).  Both FP32 paths use it so their values agree bit
+// for bit.
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 // Integer power 1..QJ_MAX_INT_EXP by square-and-multiply (powers of one
 // quaternion commute, so any order is exact algebra).
 __device__ __forceinline__ Q qpow_int(const Q& d, int n) {
@@ -160,6 +188,64 @@ __device__ __forceinline__ Q qpow(const Q& q, float e) {
 }
 
 }  // namespace q32
+
+// ------------------------------------------------------- FP32, two voxels
+// The q32 arithmetic on (voxel A, voxel B) pairs: every operation is the
+// packed f32x2 form of the q32 one (fma.rn.f32x2 and friends, one issue slot
+// for two lanes of work), in the same order, so each half of a result is
+// bit-identical to the scalar q32 value of its voxel.
+namespace q32x2 {
+
+struct Q2 {
+  float2 w, x, y, z;
+};
+
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 pair(float a) { return make_float2(a, a); }
+
+__device__ __forceinline__ Q2 qmul(const Q2& a, const Q2& b) {
+  Q2 o;
+  o.w = fma2(neg2(a.z), b.z, fma2(neg2(a.y), b.y, fma2(neg2(a.x), b.x, mul2(a.w, b.w))));
+  o.x = fma2(neg2(a.z), b.y, fma2(a.y, b.z, fma2(a.x, b.w, mul2(a.w, b.x))));
+  o.y = fma2(a.z, b.x, fma2(a.y, b.w, fma2(neg2(a.x), b.z, mul2(a.w, b.y))));
+  o.z = fma2(a.z, b.w, fma2(neg2(a.y), b.x, fma2(a.x, b.y, mul2(a.w, b.z))));
+  return o;
+}
+
+__device__ __forceinline__ Q2 qmul_conj(const Q2& a, const Q2& b) {
+  Q2 o;
+  o.w = fma2(a.z, b.z, fma2(a.y, b.y, fma2(a.x, b.x, mul2(a.w, b.w))));
+  o.x = fma2(a.z, b.y, fma2(neg2(a.y), b.z, fma2(a.x, b.w, mul2(neg2(a.w), b.x))));
+  o.y = fma2(neg2(a.z), b.x, fma2(a.y, b.w, fma2(a.x, b.z, mul2(neg2(a.w), b.y))));
+  o.z = fma2(a.z, b.w, fma2(a.y, b.x, fma2(neg2(a.x), b.y, mul2(neg2(a.w), b.z))));
+  return o;
+}
+
+__device__ __forceinline__ Q2 qsq(const Q2& a) {
+  Q2 o;
+  const float2 w2 = add2(a.w, a.w);
+  o.w = fma2(neg2(a.z), a.z, fma2(neg2(a.y), a.y, fma2(neg2(a.x), a.x, mul2(a.w, a.w))));
+  o.x = mul2(w2, a.x);
+  o.y = mul2(w2, a.y);
+  o.z = mul2(w2, a.z);
+  return o;
+}
+
+__device__ __forceinline__ float2 norm2(const Q2& q) {
+  return fma2(q.z, q.z, fma2(q.y, q.y, fma2(q.x, q.x, mul2(q.w, q.w))));
+}
+
+__device__ __forceinline__ q32::Q lo(const Q2& a) { return q32::Q{a.w.x, a.x.x, a.y.x, a.z.x}; }
+__device__ __forceinline__ q32::Q hi(const Q2& a) { return q32::Q{a.w.y, a.x.y, a.y.y, a.z.y}; }
+__device__ __forceinline__ Q2 join(const q32::Q& a, const q32::Q& b) {
+  return Q2{make_float2(a.w, b.w), make_float2(a.x, b.x), make_float2(a.y, b.y),
+            make_float2(a.z, b.z)};
+}
+
+}  // namespace q32x2
 
 // ----------------------------------------------------------------- geometry
 
@@ -280,7 +366,7 @@ __device__ __forceinline__ q32::Q root_term32(const MapParams& m, const q32::Q& 
   const float2 ex = *reinterpret_cast<const float2*>(m.x32[i]);
   const Q d = {q.w - root.x, q.x - root.y, q.y - root.z, q.z - root.w};
   if (DE) {
-    const float k = __fdividef(ex.x, norm2(d));
+    const float k = ex.x * rcp_approx(norm2(d));
     g.w = fmaf(k, d.w, g.w);
     g.x = fmaf(k, d.x, g.x);
     g.y = fmaf(k, d.y, g.y);
@@ -318,7 +404,7 @@ __device__ __forceinline__ q32::Q apply32(const MapParams& m, const q32::Q& q, f
   Q out;
   if (m.nb > 0) {
     const Q bot = product32<DE>(m, q, m.nt, m.nt + m.nb, g);
-    const float inv = __fdividef(m.scalef, norm2(bot));
+    const float inv = m.scalef * rcp_approx(norm2(bot));
     out = qmul_conj(top, bot);
     out.w *= inv;
     out.x *= inv;
@@ -335,35 +421,104 @@ __device__ __forceinline__ q32::Q apply32(const MapParams& m, const q32::Q& q, f
   return out;
 }
 
-// The FP32 escape loop at an arbitrary point with the distance estimate:
-// returns log|q_N| and, through *err, a conservative bound on its FP32
-// error: 64 * 2^-24 * (|q_0| + 1) * |q_N'| / |q_N|, the first-order growth
-// of a relative perturbation of the start point through the orbit (64 covers
-// the rounding of every root term and iteration).  *err is infinite when
-// FP32 cannot follow the orbit (|q| below 1e-18, overflow).
+// root_term32 / product32 / apply32 on a voxel pair.
+template <bool DE>
+__device__ __forceinline__ q32x2::Q2 root_term32x2(const MapParams& m, const q32x2::Q2& q, int i,
+                                                   q32x2::Q2& g) {
+  using namespace q32x2;
+  const float4 rwx = *reinterpret_cast<const float4*>(&m.rn2[i][0]);
+  const float4 ryz = *reinterpret_cast<const float4*>(&m.rn2[i][2]);
+  const Q2 d = {add2(q.w, make_float2(rwx.x, rwx.y)), add2(q.x, make_float2(rwx.z, rwx.w)),
+                add2(q.y, make_float2(ryz.x, ryz.y)), add2(q.z, make_float2(ryz.z, ryz.w))};
+  if (DE) {
+    const float2 n = norm2(d);
+    const float2 k = mul2(m.ex2[i], make_float2(q32::rcp_approx(n.x), q32::rcp_approx(n.y)));
+    g.w = fma2(k, d.w, g.w);
+    g.x = fma2(k, d.x, g.x);
+    g.y = fma2(k, d.y, g.y);
+    g.z = fma2(k, d.z, g.z);
+  }
+  const int ie = m.ie[i];
+  if (ie == 1) return d;
+  if (ie == 2) return qsq(d);
+  return join(root_power_rare(lo(d), ie, m.e32[i]), root_power_rare(hi(d), ie, m.e32[i]));
+}
+
+template <bool DE>
+__device__ __forceinline__ q32x2::Q2 product32x2(const MapParams& m, const q32x2::Q2& q, int lo,
+                                                 int hi, q32x2::Q2& g) {
+  using namespace q32x2;
+  Q2 r = root_term32x2<DE>(m, q, lo, g);
+  int i = lo + 1;
+#pragma unroll 1
+  for (; i + 1 < hi; i += 2) {
+    const Q2 t0 = root_term32x2<DE>(m, q, i, g);
+    const Q2 t1 = root_term32x2<DE>(m, q, i + 1, g);
+    r = qmul(qmul(r, t0), t1);
+  }
+  if (i < hi) r = qmul(r, root_term32x2<DE>(m, q, i, g));
+  return r;
+}
+
+template <bool DE>
+__device__ __forceinline__ q32x2::Q2 apply32x2(const MapParams& m, const q32x2::Q2& q,
+                                               float2* g2) {
+  using namespace q32x2;
+  Q2 g = {pair(0.f), pair(0.f), pair(0.f), pair(0.f)};
+  const Q2 top = product32x2<DE>(m, q, 0, m.nt, g);
+  Q2 out;
+  if (m.nb > 0) {
+    const Q2 bot = product32x2<DE>(m, q, m.nt, m.nt + m.nb, g);
+    const float2 n = norm2(bot);
+    const float2 inv =
+        mul2(pair(m.scalef), make_float2(q32::rcp_approx(n.x), q32::rcp_approx(n.y)));
+    out = qmul_conj(top, bot);
+    out.w = mul2(out.w, inv);
+    out.x = mul2(out.x, inv);
+    out.y = mul2(out.y, inv);
+    out.z = mul2(out.z, inv);
+  } else {
+    const float2 s = pair(m.scalef);
+    out.w = mul2(top.w, s);
+    out.x = mul2(top.x, s);
+    out.y = mul2(top.y, s);
+    out.z = mul2(top.z, s);
+  }
+  if (DE) *g2 = norm2(g);
+  return out;
+}
+
+// The FP32 escape loop at an arbitrary point: returns log|q_N| and, through
+// *err, the first-order estimate of its FP32 error (the relative error of
+// q_N carried by q32::propagate_err).  *err is infinite when FP32 cannot
+// follow the orbit (|q| below 1e-18, overflow) or an iterate lies within its
+// error of the escape radius.
 __device__ __forceinline__ float escape32(const MapParams& m, const IterParams& it,
                                           const double p[3], double slice, float* err) {
   using namespace q32;
   Q q = {(float)p[0], (float)p[1], (float)p[2], (float)slice};
-  const float q0 = sqrtf(norm2(q));
   const float esc2 = (float)(it.escape * it.escape);
-  float m2 = norm2(q), l2d = 0.f;
+  float m2 = norm2(q), e = q32::EPS32;
   int n = 0;
-  bool bad = false;
+  bool bad = false, near = false;
   while (m2 < esc2 && n < it.max_it) {
     float gg = 0.f;
     q = apply32<true>(m, q, &gg);
+    near = near || q32::near_radius(m2, esc2, e);
+    e = q32::propagate_err(e, gg, m2);
     m2 = norm2(q);
-    l2d += 0.5f * (__log2f(gg) + __log2f(m2));
     n++;
     if (m2 < 1e-36f) {
       bad = true;
       break;
     }
   }
+  // an iterate within FP32 error of the escape radius may stop the FP64
+  // orbit at another iterate: no bound holds across that step (the last
+  // iterate of an orbit cut by max_it is the same iterate either way)
+  bad = bad || near || (m2 >= esc2 && n < it.max_it && q32::near_radius(m2, esc2, e));
   const float f = 0.5f * logf(m2);
-  const float e = 64.f * 5.9604645e-8f * (q0 + 1.f) * exp2f(l2d - 0.5f * __log2f(m2));
-  *err = (bad || !isfinite(f) || isnan(e)) ? __int_as_float(0x7f800000) : e;
+  *err = (bad || !isfinite(f) || !(e < 1.f)) ? __int_as_float(0x7f800000) : e;
   return f;
 }
 

@@ -10,11 +10,21 @@ namespace qj {
 // field.cu
 cudaError_t launch_field64(const MapParams& m, const GridParams& g, const IterParams& it,
                            bool pow_ref, double* field, float* de, DevStats* st, cudaStream_t s);
+// FP32 bulk pass; with refine, appends the voxels to re-evaluate to `list`
+// and, when `keys` is not null, each one's FP32 orbit length to `keys`.
 cudaError_t launch_field32(const MapParams& m, const GridParams& g, const IterParams& it,
-                           bool refine, double* field, float* de, uint32_t* list, DevStats* st,
-                           cudaStream_t s);
+                           bool refine, double* field, float* de, uint32_t* list, uint8_t* keys,
+                           DevStats* st, cudaStream_t s);
+// process-wide choice of the FP32 bulk kernel: 1 two voxels per lane
+// (field32x2_kernel, the default), 0 one voxel per lane (field32_kernel)
+void set_field32_pairs(int on);
+// FP64 re-evaluation of the listed voxels.  With `keys`, the list is first
+// counting-sorted by key into `sorted` (capacity of the list; `hist` holds
+// REFINE_KEYS counters) so that each warp gets orbits of one length.
+constexpr int REFINE_KEYS = 256;
 cudaError_t launch_refine64(const MapParams& m, const GridParams& g, const IterParams& it,
-                            bool pow_ref, const uint32_t* list, double* field, float* de,
+                            bool pow_ref, const uint32_t* list, const uint8_t* keys,
+                            uint32_t* sorted, unsigned* hist, double* field, float* de,
                             DevStats* st, cudaStream_t s);
 
 }  // namespace qj

@@ -3,6 +3,7 @@
 // every thread of a launch reads the same roots, which the constant cache
 // broadcasts.
 #pragma once
+#include <cuda_runtime.h>
 #include <stdint.h>
 
 #define QJ_MAX_ROOTS 128     // top + bottom roots of one map
@@ -27,6 +28,9 @@ struct MapParams {
   alignas(8) float x32[QJ_MAX_ROOTS][2];  // {+e (top) or -e (bottom), integer exponent bits}
   float e32[QJ_MAX_ROOTS];
   int ie[QJ_MAX_ROOTS];         // integer exponent, or 0 when the exponent is not an integer
+  // the two-voxel FP32 path: every value doubled into a (voxel A, voxel B) pair
+  alignas(16) float2 rn2[QJ_MAX_ROOTS][4];  // (-t_c, -t_c) for c = w, x, y, z
+  alignas(8) float2 ex2[QJ_MAX_ROOTS];      // (x32[i][0], x32[i][0])
 };
 
 // Cell-centred grid geometry (FIELD_3D) and the z-range of one launch.

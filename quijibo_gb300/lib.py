@@ -152,6 +152,7 @@ EXPORTS = {
     "qjg_last_timings": ([C.c_void_p, _fp, _fp], C.c_int),
     "qjg_launch_count": ([C.c_void_p], C.c_int64),
     "qjg_fma_probe": ([C.c_int, _dp], C.c_int),
+    "qjg_set_field32_pairs": ([C.c_int], C.c_int),
 }
 
 _lib = None
@@ -175,6 +176,11 @@ def load():
 
 class QjgError(RuntimeError):
     pass
+
+
+def set_field32_pairs(on):
+    """Process-wide FP32 bulk kernel form: True two voxels per lane (default)."""
+    load().qjg_set_field32_pairs(int(bool(on)))
 
 
 def fma_probe(device=0):

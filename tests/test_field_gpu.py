@@ -136,3 +136,41 @@ def test_tiny_and_ragged_grids(ctx, oracle):
         f, _, _ = run(ctx, rs, g, p)
         o = oracle.field(rs, g, p["max_it"], p["escape"])["field"]
         assert np.quantile(rel_err(f, o), 0.99) <= 1e-12
+
+
+def _field32_both_forms(ctx, rs, g, p, precision):
+    out = []
+    try:
+        for pairs in (True, False):
+            lib.set_field32_pairs(pairs)
+            out.append(run(ctx, rs, g, p, precision=precision, want_de=True,
+                           refine_pow=lib.QJG_REFINE_INT))
+    finally:
+        lib.set_field32_pairs(True)
+    return out
+
+
+@pytest.mark.parametrize("case", ["prec64", "ragged", "general", "top_only"])
+@pytest.mark.parametrize("precision", [lib.QJG_FP32, lib.QJG_FP32_REFINE])
+def test_fp32_voxel_pairs_equal_single_voxel_form(ctx, case, precision):
+    """The two-voxel f32x2 kernel rounds every operation as the one-voxel
+    kernel does: same field and distance bits, same counters."""
+    from quijibo_gb300.rootsets import Grid, draw_rootset
+    if case == "prec64":
+        rs, g, p = precision_workload(64)
+    elif case == "ragged":
+        rs, _, p = precision_workload(32)
+        g = Grid((33, 7, 5))
+    elif case == "general":
+        rs, _, p, _ = load_case("field_general")
+        g = Grid((31, 20, 6), center=(0.1, -0.2, 0.05), lengths=(2.8, 2.6, 2.4), slice=0.15)
+    else:
+        rs = draw_rootset(5, 5, 0, -1.0, 1.0, exps=(1, 2, 3))
+        g = Grid((40, 40, 8))
+        p = dict(max_it=10, escape=2.0)
+    (fa, da, sa), (fb, db, sb) = _field32_both_forms(ctx, rs, g, p, precision)
+    assert np.array_equal(fa.view(np.uint64), fb.view(np.uint64))
+    assert np.array_equal(da.view(np.uint32), db.view(np.uint32))
+    for k in ("voxel_iters", "refined", "refined_iters", "nonfinite"):
+        assert sa[k] == sb[k], k
+    assert sa["voxel_iters"] > 0

@@ -109,8 +109,9 @@ def test_mesh_matches_oracle_64(ctx, oracle, wl):
     ctx.free(h)
 
 
-def test_fp32_refine_stream_topology_matches_fp64(ctx):
-    rs, g, p = precision_workload(64)
+@pytest.mark.parametrize("res", [64, 160])
+def test_fp32_refine_stream_topology_matches_fp64(ctx, res):
+    rs, g, p = precision_workload(res)
     h = ctx.upload(rs)
     res = []
     for prec in (lib.QJG_FP64, lib.QJG_FP32_REFINE):
@@ -123,7 +124,11 @@ def test_fp32_refine_stream_topology_matches_fp64(ctx):
     (b64, _, bt), sb = res[1]
     np.testing.assert_array_equal(at, bt)
     assert sb["field"]["refined"] > 0
-    _bisect_close(b64, a64, g.spacing)
+    # the FP32-first bisection takes every decision the FP64 one takes, so the
+    # vertices are the same doubles
+    assert sb["map_evals_fp32"] > sb["map_evals"] and sa["map_evals_fp32"] == 0
+    assert sa["n_unbracketed"] == 0 and sb["n_unbracketed"] == 0
+    np.testing.assert_array_equal(b64, a64)
     ctx.free(h)
 
 
