@@ -31,7 +31,12 @@ METRIC = "Julia field Gvox/s (FP32+refine vs FP64, same sign map); p50/p99 req l
 RES = 512
 WORKLOAD = ("precision form: 16 top / 8 bottom roots U[-1.2,1.2]^4 (seed 0), exponents {1,2}, "
             "s = u * conformal scale (u in [0.5,2]), 40 iterations, escape 2, %d^3 grid over "
-            "[-1.5,1.5]^3, slice 0; FP32 bulk + FP64 re-evaluation of |d| < 2h")
+            "[-1.5,1.5]^3, slice 0; FP32 bulk, double-float-head re-run of voxels whose tracked "
+            "FP32 error exceeds rel_tol, FP64 re-evaluation of |d| < 2h")
+# DRAM bytes of one field32x2_kernel launch on the 512^3 workload (ncu,
+# dram__bytes_read.sum + dram__bytes_write.sum, one pass at full size): the
+# FMA-bound kernel moves ~7.7 B per voxel, the FP64 field it writes
+TRAFFIC_PER_VOXEL = (19.15e6 + 1.01e9) / 512 ** 3
 
 
 def field_flops(rs, voxel_iters, de=True):
@@ -194,7 +199,7 @@ def run_ours(args, world, rank, local):
     field = torch.empty(n, dtype=torch.float64, device="cuda")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > L2 (129 MB)
     it = ctx.iter_params(p["max_it"], p["escape"], precision=lib.QJG_FP32_REFINE,
-                         refine_pow=lib.QJG_REFINE_INT, band_h=2.0)
+                         refine_pow=lib.QJG_REFINE_INT, band_h=2.0, rel_tol=args.rel_tol)
     ctx.set_timing(True)
 
     for _ in range(args.warmup):
@@ -296,15 +301,17 @@ def run_ours(args, world, rank, local):
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
         "config": {"workload": WORKLOAD % args.res, "res": args.res, "voxels": n,
+                   "rel_tol": args.rel_tol,
                    "l2": "L2 flushed (256 MiB write) between timed steps; output 1 GiB > L2",
                    "parallelism": "one grid per GPU" if world > 1 else "single GPU"},
         "fp64_plain": fp64,
         "field_stats": dict(st, bulk_ms=bulk, refine_ms=statistics.mean(refine_ms),
                             wall_s=wall, refined_frac=st["refined"] / n,
                             lane_efficiency=st["voxel_iters"] / max(1, st["lane_iters"])),
-        "roofline": {"bound": "fma", "kernel": "field32_kernel", "achieved": achieved,
+        "roofline": {"bound": "fma", "kernel": "field32x2_kernel", "achieved": achieved,
                      "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                     "traffic": None,
+                     "traffic": TRAFFIC_PER_VOXEL * n,
+                     "traffic_source": "ncu dram bytes of one 512^3 launch, per voxel x voxels",
                      "peak_source": "measured FP32 FMA-chain probe (qjg_fma_probe), same run",
                      "flops_per_launch": flops},
         "cpu_baseline": cpu,
@@ -324,6 +331,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--res", type=int, default=RES)
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--rel-tol", type=float, default=1e-6,
+                    help="target relative field error of the precision form (0: band rule only)")
     ap.add_argument("--cpu-slices", type=int, default=12)
     ap.add_argument("--ref-slices", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")

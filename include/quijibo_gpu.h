@@ -59,6 +59,9 @@ typedef struct {
   double escape;     /* escape radius (the reference uses 2000) */
   double band_h;     /* refine band half-width in voxel spacings (2.0 = |d| < 2h) */
   double field_tol;  /* voxels with |log|q|| < field_tol are refined too */
+  double rel_tol;    /* QJG_FP32_REFINE: target relative field error (e.g. 1e-6); voxels whose
+                        tracked FP32 error exceeds it are re-run with a double-float head and,
+                        if still above it, in FP64.  0 = the band rule alone. */
 } qjg_iter;
 
 typedef struct {
@@ -69,6 +72,8 @@ typedef struct {
   int64_t refined_iters; /* map applications of the FP64 re-evaluation */
   int64_t nonfinite;     /* FP32 voxels that overflowed or underflowed */
   int64_t lane_iters;    /* FP32 bulk: lane slots spent (32 x the longest orbit of each warp) */
+  int64_t rerun;         /* voxels re-run with a double-float head (rel_tol) */
+  int64_t rerun_iters;   /* map applications of those re-runs */
 } qjg_field_stats;
 
 /* ---- context and root sets ------------------------------------------- */

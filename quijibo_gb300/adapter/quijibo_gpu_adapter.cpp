@@ -113,7 +113,7 @@ qjg_grid grid_of(const VEC3I& res, const VEC3F& center, const VEC3F& lengths,
 }
 
 qjg_iter iter_of(int max_it, double escape, int prec) {
-  qjg_iter it;
+  qjg_iter it = {};
   it.max_it = max_it;
   it.precision = prec;
   it.refine_pow = QJG_REFINE_POW;
@@ -121,6 +121,7 @@ qjg_iter iter_of(int max_it, double escape, int prec) {
   it.escape = escape;
   it.band_h = 2.0;
   it.field_tol = 1e-3;
+  it.rel_tol = prec == QJG_FP32_REFINE ? 1e-6 : 0.0;
   return it;
 }
 

@@ -87,6 +87,12 @@ IterParams qj_iter_params(const qjg_iter* it, const qjg_grid* g) {
   for (int c = 1; c < 3; c++) h = std::fmin(h, g->lengths[c] / g->res[c]);
   p.band = it->band_h * h;
   p.field_tol = it->field_tol;
+  // the tracked error overestimates the actual FP32 error: at most about a
+  // third of it on the precision and large workloads, so est_tol = 3 rel_tol
+  // leaves no voxel above rel_tol unselected there
+  p.est_tol = it->rel_tol > 0 ? 3.0 * it->rel_tol : 0.0;
+  p.ff_head = 2;
+  p.pad_ = 0;
   return p;
 }
 
@@ -103,6 +109,8 @@ int qj_fill_map(MapParams* m, int n_top, const double* top_roots, const double* 
   m->nb = n_bot;
   m->scale = scale;
   m->scalef = (float)scale;
+  m->scale_ff[0] = m->scalef;
+  m->scale_ff[1] = (float)(scale - (double)m->scalef);
   m->sigma[0] = sigma_top;
   m->sigma[1] = sigma_bot;
   m->all_int = 1;
@@ -118,6 +126,8 @@ int qj_fill_map(MapParams* m, int n_top, const double* top_roots, const double* 
       m->r64[i][c] = r[c];
       m->r32[i][c] = (float)r[c];
       m->rn2[i][c] = make_float2(-m->r32[i][c], -m->r32[i][c]);
+      m->rff[i][c][0] = m->r32[i][c];
+      m->rff[i][c][1] = (float)(r[c] - (double)m->r32[i][c]);
     }
     m->e64[i] = e;
     m->ep[i] = pw;
@@ -160,6 +170,7 @@ void qjg_destroy(qjg_ctx* ctx) {
   cudaFree(ctx->d_sorted);
   cudaFree(ctx->d_keys);
   cudaFree(ctx->d_hist);
+  cudaFree(ctx->d_ff);
   cudaFree(ctx->d_field);
   cudaFree(ctx->d_de);
   cudaFree(ctx->d_mstats);
@@ -230,16 +241,23 @@ int qjg_field(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
                  (rc = ensure(ctx, &ctx->d_keys, &ctx->keys_cap, (size_t)n)) ||
                  (rc = ensure(ctx, &ctx->d_hist, &ctx->hist_cap, (size_t)qj::REFINE_KEYS))))
     return rc;
+  const bool rerun = refine && it.est_tol > 0.0 && m->all_int;
+  if (rerun && (rc = ensure(ctx, &ctx->d_ff, &ctx->ff_cap, (size_t)n))) return rc;
   QJ_CUDA(ctx, cudaMemsetAsync(ctx->d_stats, 0, sizeof(DevStats), s));
   if (ctx->timing) QJ_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
   if (iter->precision == QJG_FP64) {
     QJ_CUDA(ctx, qj::launch_field64(*m, g, it, pow_ref, d_field, d_de, ctx->d_stats, s));
   } else {
     QJ_CUDA(ctx, qj::launch_field32(*m, g, it, refine, d_field, d_de, ctx->d_list, ctx->d_keys,
-                                    ctx->d_stats, s));
+                                    rerun ? ctx->d_ff : nullptr, ctx->d_stats, s));
   }
   ctx->launches++;
   if (ctx->timing) QJ_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
+  if (rerun) {
+    QJ_CUDA(ctx, qj::launch_rerun_ff(*m, g, it, ctx->d_ff, d_field, d_de, ctx->d_list, ctx->d_keys,
+                                     ctx->d_stats, s));
+    ctx->launches++;
+  }
   if (refine) {
     QJ_CUDA(ctx, qj::launch_refine64(*m, g, it, pow_ref, ctx->d_list, ctx->d_keys,
                                      ctx->d_sorted, ctx->d_hist, d_field, d_de, ctx->d_stats, s));
@@ -265,6 +283,8 @@ int qjg_field_stats_read(qjg_ctx* ctx, void* stream, qjg_field_stats* out) {
   out->refined_iters = (int64_t)st.aux[0];
   out->nonfinite = (int64_t)st.nonfinite;
   out->lane_iters = (int64_t)st.aux[3];
+  out->rerun = (int64_t)st.rerun;
+  out->rerun_iters = (int64_t)st.rerun_iters;
   return QJG_OK;
 }
 
@@ -306,6 +326,8 @@ int qjg_field_host(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg
     total.refined_iters += st.refined_iters;
     total.nonfinite += st.nonfinite;
     total.lane_iters += st.lane_iters;
+    total.rerun += st.rerun;
+    total.rerun_iters += st.rerun_iters;
   }
   if (stats) *stats = total;
   return QJG_OK;

@@ -18,6 +18,7 @@
 #include <stdint.h>
 
 #include "qj_device.cuh"
+#include "qj_ff.cuh"
 #include "qj_kernels.h"
 
 namespace qj {
@@ -155,13 +156,17 @@ __device__ __forceinline__ void orbit_step(Orbit32& o, float m2, float gg, float
   }
 }
 
+// Where a finished orbit goes.
+enum Route : int { WRITTEN = 0, TO_FP64 = 1, TO_FF = 2 };
+
 // Field value, distance estimate and the refine decision of a finished
-// orbit; writes the voxel unless it goes to the FP64 refine list.
+// orbit; writes the voxel when it stays (WRITTEN).  allow_ff: the voxel may
+// go to the double-float re-run (not for re-runs themselves).
 template <bool DE>
-__device__ __forceinline__ bool orbit_finish(const Orbit32& o, const IterParams& it, float esc2,
-                                             float l2band, int refine, long long i,
-                                             double* __restrict__ field, float* __restrict__ de,
-                                             unsigned long long& nonfinite_acc) {
+__device__ __forceinline__ int orbit_finish(const Orbit32& o, const IterParams& it, float esc2,
+                                            float l2band, int refine, bool allow_ff, long long i,
+                                            double* __restrict__ field, float* __restrict__ de,
+                                            unsigned long long& nonfinite_acc) {
   const float f = 0.5f * logf(o.m2);
   // d = |q| log|q| / |q'| kept as log2|d|: contracting orbits drive |q'|
   // below the FP32 range long before d itself matters
@@ -172,32 +177,71 @@ __device__ __forceinline__ bool orbit_finish(const Orbit32& o, const IterParams&
   }
   const bool bad = o.bad || !isfinite(f) || (DE && isnan(l2abs_d));
   nonfinite_acc += bad;
-  // the escape test is a discontinuity: where an iterate lies within FP32
-  // error of the escape radius, FP64 may stop the orbit at a different
-  // iterate.  The last iterate of an orbit cut by max_it is the same
-  // iterate on either side of the radius.
-  const bool near_escape =
-      DE && (o.near || (o.m2 >= esc2 && o.n < it.max_it && q32::near_radius(o.m2, esc2, o.err)));
-  const bool need = refine && (bad || near_escape || l2abs_d < l2band ||
-                               fabsf(f) < (float)it.field_tol);
-  if (!need) {
+  int route = WRITTEN;
+  if (refine) {
+    // the escape test is a discontinuity: where an iterate lies within FP32
+    // error of the escape radius, FP64 may stop the orbit at a different
+    // iterate.  The last iterate of an orbit cut by max_it is the same
+    // iterate on either side of the radius.
+    const bool near_escape =
+        DE && (o.near || (o.m2 >= esc2 && o.n < it.max_it && q32::near_radius(o.m2, esc2, o.err)));
+    if (bad || near_escape || l2abs_d < l2band || fabsf(f) < (float)it.field_tol)
+      route = TO_FP64;
+    else if (it.est_tol > 0.0 && !(o.err <= (float)it.est_tol * fabsf(f)))
+      route = (allow_ff && it.ff_head > 0) ? TO_FF : TO_FP64;
+  }
+  if (route == WRITTEN) {
     field[i] = (double)f;
     if (DE && de) de[i] = d;
   }
-  return need;
+  return route;
 }
+
+// Warp-aggregated append of up to two entries per lane (lane order, the a
+// entries first) to a list whose length counter is *count.
+__device__ __forceinline__ void warp_append(bool a, uint32_t ia, int na, bool b, uint32_t ib,
+                                            int nb, unsigned long long* count, uint32_t* list,
+                                            uint8_t* keys) {
+  const int lane = threadIdx.x & 31;
+  const unsigned ma = __ballot_sync(0xffffffffu, a);
+  const unsigned mb = __ballot_sync(0xffffffffu, b);
+  if (!(ma | mb)) return;
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(count, (unsigned long long)(__popc(ma) + __popc(mb)));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  const unsigned below = (1u << lane) - 1u;
+  if (a) {
+    const unsigned long long slot = base + __popc(ma & below);
+    list[slot] = ia;
+    if (keys) keys[slot] = refine_key(na);
+  }
+  if (b) {
+    const unsigned long long slot = base + __popc(ma) + __popc(mb & below);
+    list[slot] = ib;
+    if (keys) keys[slot] = refine_key(nb);
+  }
+}
+
+// Lists a bulk pass fills (device pointers; keys and ff may be null).
+struct RefineLists {
+  uint32_t* list;  // voxels for the FP64 re-evaluation (length in DevStats::refined)
+  uint8_t* keys;   // their FP32 orbit lengths, the sort key of the FP64 pass
+  uint32_t* ff;    // voxels for the double-float re-run (length in DevStats::rerun)
+};
 
 // One voxel per lane: the form the mesher's bisection shares (escape32).
 template <bool DE>
 __global__ void __launch_bounds__(128) field32_kernel(const __grid_constant__ MapParams m,
-                                                      const GridParams g, const IterParams it, double* __restrict__ field,
-                                                      float* __restrict__ de, uint32_t* refine_list,
-                                                      uint8_t* refine_keys, int refine, DevStats* st) {
+                                                      const GridParams g, const IterParams it,
+                                                      double* __restrict__ field,
+                                                      float* __restrict__ de, RefineLists rl,
+                                                      int refine, DevStats* st) {
   using namespace q32;
   const TileMap tm = tile_map(g);
   const int lane = threadIdx.x & 31;
   const float esc2 = (float)(it.escape * it.escape);
   const float l2band = log2f((float)it.band);
+  const bool allow_ff = rl.ff != nullptr;
   unsigned long long iters_acc = 0, nonfinite_acc = 0, lane_iters_acc = 0;
   for (;;) {
     const long long t = next_tile(&st->tiles_done);
@@ -218,23 +262,14 @@ __global__ void __launch_bounds__(128) field32_kernel(const __grid_constant__ Ma
     }
     iters_acc += o.n;
     const long long i = ((long long)zl * g.Y + y) * g.X + x;
-    const bool need =
-        valid && orbit_finish<DE>(o, it, esc2, l2band, refine, i, field, de, nonfinite_acc);
+    const int route = valid ? orbit_finish<DE>(o, it, esc2, l2band, refine, allow_ff, i, field,
+                                               de, nonfinite_acc)
+                            : WRITTEN;
     // lane slots the warp spent: 32 x its longest orbit
     const unsigned wmax = __reduce_max_sync(0xffffffffu, (unsigned)o.n);
     if (lane == 0) lane_iters_acc += 32ull * wmax;
-    // warp-aggregated append to the refine list
-    const unsigned mask = __ballot_sync(0xffffffffu, need);
-    if (mask) {
-      unsigned long long base = 0;
-      if (lane == 0) base = atomicAdd(&st->refined, (unsigned long long)__popc(mask));
-      base = __shfl_sync(0xffffffffu, base, 0);
-      if (need) {
-        const unsigned long long slot = base + __popc(mask & ((1u << lane) - 1u));
-        refine_list[slot] = (uint32_t)i;
-        if (refine_keys) refine_keys[slot] = refine_key(o.n);
-      }
-    }
+    warp_append(route == TO_FP64, (uint32_t)i, o.n, false, 0, 0, &st->refined, rl.list, rl.keys);
+    warp_append(route == TO_FF, (uint32_t)i, 0, false, 0, 0, &st->rerun, rl.ff, nullptr);
   }
   warp_add(&st->voxel_iters, iters_acc);
   warp_add(&st->nonfinite, nonfinite_acc);
@@ -252,15 +287,14 @@ template <bool DE>
 __global__ void __launch_bounds__(128) field32x2_kernel(const __grid_constant__ MapParams m,
                                                         const GridParams g, const IterParams it,
                                                         double* __restrict__ field,
-                                                        float* __restrict__ de,
-                                                        uint32_t* refine_list,
-                                                        uint8_t* refine_keys, int refine,
-                                                        DevStats* st) {
+                                                        float* __restrict__ de, RefineLists rl,
+                                                        int refine, DevStats* st) {
   using namespace q32x2;
   const TileMap tm = tile_map(g, TILE2_X);
   const int lane = threadIdx.x & 31;
   const float esc2 = (float)(it.escape * it.escape);
   const float l2band = log2f((float)it.band);
+  const bool allow_ff = rl.ff != nullptr;
   unsigned long long iters_acc = 0, nonfinite_acc = 0, lane_iters_acc = 0;
   for (;;) {
     const long long t = next_tile(&st->tiles_done);
@@ -287,36 +321,80 @@ __global__ void __launch_bounds__(128) field32x2_kernel(const __grid_constant__ 
     }
     iters_acc += a.n + b.n;
     const long long i = ((long long)zl * g.Y + y) * g.X + x;
-    const bool need_a =
-        va && orbit_finish<DE>(a, it, esc2, l2band, refine, i, field, de, nonfinite_acc);
-    const bool need_b =
-        vb && orbit_finish<DE>(b, it, esc2, l2band, refine, i + 1, field, de, nonfinite_acc);
+    const int ra = va ? orbit_finish<DE>(a, it, esc2, l2band, refine, allow_ff, i, field, de,
+                                         nonfinite_acc)
+                      : WRITTEN;
+    const int rb = vb ? orbit_finish<DE>(b, it, esc2, l2band, refine, allow_ff, i + 1, field, de,
+                                         nonfinite_acc)
+                      : WRITTEN;
     // voxel slots the warp spent: 64 x its longest orbit
     const unsigned wmax = __reduce_max_sync(0xffffffffu, (unsigned)max(a.n, b.n));
     if (lane == 0) lane_iters_acc += 64ull * wmax;
-    // warp-aggregated append to the refine list, A voxels first
-    const unsigned ma = __ballot_sync(0xffffffffu, need_a);
-    const unsigned mb = __ballot_sync(0xffffffffu, need_b);
-    if (ma | mb) {
-      unsigned long long base = 0;
-      if (lane == 0) base = atomicAdd(&st->refined, (unsigned long long)(__popc(ma) + __popc(mb)));
-      base = __shfl_sync(0xffffffffu, base, 0);
-      const unsigned below = (1u << lane) - 1u;
-      if (need_a) {
-        const unsigned long long slot = base + __popc(ma & below);
-        refine_list[slot] = (uint32_t)i;
-        if (refine_keys) refine_keys[slot] = refine_key(a.n);
-      }
-      if (need_b) {
-        const unsigned long long slot = base + __popc(ma) + __popc(mb & below);
-        refine_list[slot] = (uint32_t)(i + 1);
-        if (refine_keys) refine_keys[slot] = refine_key(b.n);
-      }
-    }
+    warp_append(ra == TO_FP64, (uint32_t)i, a.n, rb == TO_FP64, (uint32_t)(i + 1), b.n,
+                &st->refined, rl.list, rl.keys);
+    warp_append(ra == TO_FF, (uint32_t)i, 0, rb == TO_FF, (uint32_t)(i + 1), 0, &st->rerun,
+                rl.ff, nullptr);
   }
   warp_add(&st->voxel_iters, iters_acc);
   warp_add(&st->nonfinite, nonfinite_acc);
   warp_add(&st->aux[3], lane_iters_acc);
+}
+
+// The double-float re-run of the listed voxels: it.ff_head map applications
+// in double-float, then FP32 to the end, one voxel per lane.  The tracked
+// error restarts at the rounding of the head's result to FP32, so voxels
+// whose error came from the first iterations now pass; the others (and the
+// band, escape-radius and overflow cases) go to the FP64 list.
+__global__ void __launch_bounds__(128) rerun_ff_kernel(const __grid_constant__ MapParams m,
+                                                       const GridParams g, const IterParams it,
+                                                       const uint32_t* __restrict__ ff_list,
+                                                       double* __restrict__ field,
+                                                       float* __restrict__ de, uint32_t* list,
+                                                       uint8_t* keys, DevStats* st) {
+  const unsigned long long n_list = st->rerun;
+  const float esc2 = (float)(it.escape * it.escape);
+  const float l2band = log2f((float)it.band);
+  const int lane = threadIdx.x & 31;
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  unsigned long long iters_acc = 0, nonfinite_acc = 0;
+  // warp-uniform trips: the append below is a warp collective
+  for (unsigned long long base = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) & ~31ull;
+       base < n_list; base += stride) {
+    const unsigned long long k = base + lane;
+    const bool valid = k < n_list;
+    uint32_t i = 0;
+    int route = WRITTEN;
+    Orbit32 o = orbit_start(false, 0.f, esc2, it.max_it);
+    if (valid) {
+      i = ff_list[k];
+      const int x = (int)(i % (uint32_t)g.X);
+      const int y = (int)((i / (uint32_t)g.X) % (uint32_t)g.Y);
+      const int zl = (int)(i / ((uint32_t)g.X * (uint32_t)g.Y));
+      double p[3];
+      cell_center(g, x, y, g.z0 + zl, p);
+      qff::Q q = {qff::from_double(p[0]), qff::from_double(p[1]), qff::from_double(p[2]),
+                  qff::from_double(g.slice)};
+      o = orbit_start(true, qff::norm2(q).hi, esc2, it.max_it);
+      for (int h = 0; h < it.ff_head && o.live; h++) {
+        float gg = 0.f;
+        q = apply_ff<true>(m, q, &gg);
+        o.err = q32::EPS32;  // double-float iterates: only their FP32 rounding counts
+        orbit_step<true>(o, qff::norm2(q).hi, gg, esc2, it.max_it);
+      }
+      o.err = q32::EPS32;
+      q32::Q qf = qff::hi(q);
+      while (o.live) {
+        float gg = 0.f;
+        qf = apply32<true>(m, qf, &gg);
+        orbit_step<true>(o, q32::norm2(qf), gg, esc2, it.max_it);
+      }
+      iters_acc += o.n;
+      route = orbit_finish<true>(o, it, esc2, l2band, 1, false, i, field, de, nonfinite_acc);
+    }
+    warp_append(route == TO_FP64, i, o.n, false, 0, 0, &st->refined, list, keys);
+  }
+  warp_add(&st->rerun_iters, iters_acc);
+  warp_add(&st->nonfinite, nonfinite_acc);
 }
 
 // ------------------------------------------------------------- launchers
@@ -360,25 +438,35 @@ void set_field32_pairs(int on) { g_field32_pairs = on ? 1 : 0; }
 
 cudaError_t launch_field32(const MapParams& m, const GridParams& g, const IterParams& it,
                            bool refine, double* field, float* de, uint32_t* list, uint8_t* keys,
-                           DevStats* st, cudaStream_t s) {
+                           uint32_t* ff_list, DevStats* st, cudaStream_t s) {
   const bool want = it.want_de || refine;
   const int r = refine ? 1 : 0;
+  // the double-float head needs integer exponents and an error target
+  const RefineLists rl = {list, keys, (refine && m.all_int && it.est_tol > 0.0) ? ff_list : nullptr};
   if (g_field32_pairs) {
     const void* fn =
         want ? (const void*)field32x2_kernel<true> : (const void*)field32x2_kernel<false>;
     const int blocks = grid_blocks(fn, 128);
     if (want)
-      field32x2_kernel<true><<<blocks, 128, 0, s>>>(m, g, it, field, de, list, keys, r, st);
+      field32x2_kernel<true><<<blocks, 128, 0, s>>>(m, g, it, field, de, rl, r, st);
     else
-      field32x2_kernel<false><<<blocks, 128, 0, s>>>(m, g, it, field, de, list, keys, 0, st);
+      field32x2_kernel<false><<<blocks, 128, 0, s>>>(m, g, it, field, de, rl, 0, st);
     return cudaGetLastError();
   }
   const void* fn = want ? (const void*)field32_kernel<true> : (const void*)field32_kernel<false>;
   const int blocks = grid_blocks(fn, 128);
   if (want)
-    field32_kernel<true><<<blocks, 128, 0, s>>>(m, g, it, field, de, list, keys, r, st);
+    field32_kernel<true><<<blocks, 128, 0, s>>>(m, g, it, field, de, rl, r, st);
   else
-    field32_kernel<false><<<blocks, 128, 0, s>>>(m, g, it, field, de, list, keys, 0, st);
+    field32_kernel<false><<<blocks, 128, 0, s>>>(m, g, it, field, de, rl, 0, st);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rerun_ff(const MapParams& m, const GridParams& g, const IterParams& it,
+                            const uint32_t* ff_list, double* field, float* de, uint32_t* list,
+                            uint8_t* keys, DevStats* st, cudaStream_t s) {
+  const int blocks = grid_blocks((const void*)rerun_ff_kernel, 128);
+  rerun_ff_kernel<<<blocks, 128, 0, s>>>(m, g, it, ff_list, field, de, list, keys, st);
   return cudaGetLastError();
 }
 

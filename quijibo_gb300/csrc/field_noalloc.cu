@@ -89,7 +89,7 @@ extern "C" int qjg_field_noalloc(int32_t n_top, const double* top_roots, const d
   if (iter->precision == QJG_FP64)
     e = qj::launch_field64(m, g, it, pow_ref, d_field, d_de, st, s);
   else
-    e = qj::launch_field32(m, g, it, refine, d_field, d_de, list, nullptr, st, s);
+    e = qj::launch_field32(m, g, it, refine, d_field, d_de, list, nullptr, nullptr, st, s);
   if (e == cudaSuccess && refine)
     e = qj::launch_refine64(m, g, it, pow_ref, list, nullptr, nullptr, nullptr, d_field, d_de, st,
                             s);

@@ -118,6 +118,8 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
       st.field.refined_iters += fs.refined_iters;
       st.field.nonfinite += fs.nonfinite;
       st.field.lane_iters += fs.lane_iters;
+      st.field.rerun += fs.rerun;
+      st.field.rerun_iters += fs.rerun_iters;
       src = ctx->m_field;
     } else {
       src = d_field + (size_t)c0 * XY;

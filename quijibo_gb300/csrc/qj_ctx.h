@@ -25,6 +25,8 @@ struct qjg_ctx {
   size_t keys_cap = 0;
   unsigned* d_hist = nullptr;   // counting-sort counters
   size_t hist_cap = 0;
+  uint32_t* d_ff = nullptr;     // double-float re-run list
+  size_t ff_cap = 0;
   double* d_field = nullptr;    // staging for host-buffer calls
   float* d_de = nullptr;
   size_t buf_cap = 0;

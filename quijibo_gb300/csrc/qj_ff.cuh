@@ -1,0 +1,209 @@
+// Double-float ("float-float") arithmetic: a value is an unevaluated sum
+// hi + lo of two FP32 numbers with |lo| <= ulp(hi)/2, about 44 significant
+// bits.  Built from the error-free transformations of Knuth (TwoSum) and
+// Dekker (FastTwoSum, and TwoProduct through a fused multiply-add), as in
+// the double-double literature (Hida, Li & Bailey 2001), here on FP32 words.
+// On sm_103a the FP64 pipe runs at 1/64 of the FP32 rate, so a double-float
+// Hamilton product (~170 FP32 operations) costs about a sixth of an FP64 one.
+//
+// Used for the first iterations of voxels whose FP32 orbit is too
+// ill-conditioned for the requested relative error: rounding errors of the
+// early iterations are amplified the most, so a double-float head followed by
+// FP32 removes most of the error at a fraction of the FP64 cost.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "qj_device.cuh"
+
+namespace qj {
+namespace qff {
+
+struct F {
+  float hi, lo;
+};
+
+// s + e = a + b exactly (Knuth TwoSum, 6 operations, no ordering needed)
+__device__ __forceinline__ F two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return F{s, e};
+}
+
+// s + e = a + b exactly when |a| >= |b| (Dekker FastTwoSum)
+__device__ __forceinline__ F fast_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return F{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+// p + e = a * b exactly (the FMA gives the low part)
+__device__ __forceinline__ F two_prod(float a, float b) {
+  const float p = __fmul_rn(a, b);
+  return F{p, __fmaf_rn(a, b, -p)};
+}
+
+__device__ __forceinline__ F from_double(double v) {
+  const float hi = __double2float_rn(v);
+  return F{hi, __double2float_rn(v - (double)hi)};
+}
+
+__device__ __forceinline__ F neg(F a) { return F{-a.hi, -a.lo}; }
+
+__device__ __forceinline__ F add(F a, F b) {
+  const F s = two_sum(a.hi, b.hi);
+  return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+
+__device__ __forceinline__ F mul(F a, F b) {
+  const F p = two_prod(a.hi, b.hi);
+  return fast_two_sum(p.hi, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, p.lo)));
+}
+
+__device__ __forceinline__ F mul(F a, float b) {
+  const F p = two_prod(a.hi, b);
+  return fast_two_sum(p.hi, __fmaf_rn(a.lo, b, p.lo));
+}
+
+// a0*b0 + a1*b1 + a2*b2 + a3*b3: four exact products, the high parts summed
+// with TwoSum, every low part and rounding error gathered in one FP32 sum
+__device__ __forceinline__ F dot4(F a0, F b0, F a1, F b1, F a2, F b2, F a3, F b3) {
+  const F p0 = two_prod(a0.hi, b0.hi), p1 = two_prod(a1.hi, b1.hi);
+  const F p2 = two_prod(a2.hi, b2.hi), p3 = two_prod(a3.hi, b3.hi);
+  float e = __fmaf_rn(a0.hi, b0.lo, __fmaf_rn(a0.lo, b0.hi, p0.lo));
+  e = __fadd_rn(e, __fmaf_rn(a1.hi, b1.lo, __fmaf_rn(a1.lo, b1.hi, p1.lo)));
+  e = __fadd_rn(e, __fmaf_rn(a2.hi, b2.lo, __fmaf_rn(a2.lo, b2.hi, p2.lo)));
+  e = __fadd_rn(e, __fmaf_rn(a3.hi, b3.lo, __fmaf_rn(a3.lo, b3.hi, p3.lo)));
+  F s = two_sum(p0.hi, p1.hi);
+  e = __fadd_rn(e, s.lo);
+  s = two_sum(s.hi, p2.hi);
+  e = __fadd_rn(e, s.lo);
+  s = two_sum(s.hi, p3.hi);
+  e = __fadd_rn(e, s.lo);
+  return fast_two_sum(s.hi, e);
+}
+
+struct Q {
+  F w, x, y, z;
+};
+
+__device__ __forceinline__ Q qmul(const Q& a, const Q& b) {
+  Q o;
+  o.w = dot4(a.w, b.w, a.x, neg(b.x), a.y, neg(b.y), a.z, neg(b.z));
+  o.x = dot4(a.w, b.x, a.x, b.w, a.y, b.z, a.z, neg(b.y));
+  o.y = dot4(a.w, b.y, a.x, neg(b.z), a.y, b.w, a.z, b.x);
+  o.z = dot4(a.w, b.z, a.x, b.y, a.y, neg(b.x), a.z, b.w);
+  return o;
+}
+
+// a * conj(b)
+__device__ __forceinline__ Q qmul_conj(const Q& a, const Q& b) {
+  Q o;
+  o.w = dot4(a.w, b.w, a.x, b.x, a.y, b.y, a.z, b.z);
+  o.x = dot4(a.w, neg(b.x), a.x, b.w, a.y, neg(b.z), a.z, b.y);
+  o.y = dot4(a.w, neg(b.y), a.x, b.z, a.y, b.w, a.z, neg(b.x));
+  o.z = dot4(a.w, neg(b.z), a.x, neg(b.y), a.y, b.x, a.z, b.w);
+  return o;
+}
+
+__device__ __forceinline__ Q qsq(const Q& a) {
+  Q o;
+  o.w = dot4(a.w, a.w, a.x, neg(a.x), a.y, neg(a.y), a.z, neg(a.z));
+  const F w2 = F{2.f * a.w.hi, 2.f * a.w.lo};  // exact
+  o.x = mul(w2, a.x);
+  o.y = mul(w2, a.y);
+  o.z = mul(w2, a.z);
+  return o;
+}
+
+__device__ __forceinline__ F norm2(const Q& q) {
+  return dot4(q.w, q.w, q.x, q.x, q.y, q.y, q.z, q.z);
+}
+
+__device__ __forceinline__ q32::Q hi(const Q& q) { return q32::Q{q.w.hi, q.x.hi, q.y.hi, q.z.hi}; }
+
+// 1 / a: the FP32 reciprocal refined by one Newton step in double-float
+__device__ __forceinline__ F recip(F a) {
+  const float r = q32::rcp_approx(a.hi);
+  // r + r * (1 - a * r)
+  const F ar = mul(a, r);
+  const F resid = add(F{1.f, 0.f}, neg(ar));
+  return add(F{r, 0.f}, mul(resid, r));
+}
+
+// Integer power 1..QJ_MAX_INT_EXP by square-and-multiply.
+__device__ __forceinline__ Q qpow_int(const Q& d, int n) {
+  if (n == 1) return d;
+  if (n == 2) return qsq(d);
+  Q r = d, b = d;
+  bool first = true;
+  while (n) {
+    if (n & 1) {
+      r = first ? b : qmul(r, b);
+      first = false;
+    }
+    n >>= 1;
+    if (n) b = qsq(b);
+  }
+  return r;
+}
+
+}  // namespace qff
+
+// One root term (q - r_i)^(e_i) in double-float (integer exponents only);
+// with DE, adds (+-e_i) d/|d|^2 to g from the high parts, as the FP32 form.
+template <bool DE>
+__device__ __forceinline__ qff::Q root_term_ff(const MapParams& m, const qff::Q& q, int i,
+                                               q32::Q& g) {
+  using namespace qff;
+  const Q d = {add(q.w, neg(F{m.rff[i][0][0], m.rff[i][0][1]})),
+               add(q.x, neg(F{m.rff[i][1][0], m.rff[i][1][1]})),
+               add(q.y, neg(F{m.rff[i][2][0], m.rff[i][2][1]})),
+               add(q.z, neg(F{m.rff[i][3][0], m.rff[i][3][1]}))};
+  if (DE) {
+    const q32::Q dh = hi(d);
+    const float k = m.x32[i][0] * q32::rcp_approx(q32::norm2(dh));
+    g.w = fmaf(k, dh.w, g.w);
+    g.x = fmaf(k, dh.x, g.x);
+    g.y = fmaf(k, dh.y, g.y);
+    g.z = fmaf(k, dh.z, g.z);
+  }
+  return qpow_int(d, m.ie[i]);
+}
+
+template <bool DE>
+__device__ __forceinline__ qff::Q product_ff(const MapParams& m, const qff::Q& q, int lo, int hi,
+                                             q32::Q& g) {
+  qff::Q r = root_term_ff<DE>(m, q, lo, g);
+#pragma unroll 1
+  for (int i = lo + 1; i < hi; i++) r = qff::qmul(r, root_term_ff<DE>(m, q, i, g));
+  return r;
+}
+
+// One map application in double-float; *g2 = |grad log|R||^2 in FP32.
+// Requires m.all_int (integer effective exponents).
+template <bool DE>
+__device__ __forceinline__ qff::Q apply_ff(const MapParams& m, const qff::Q& q, float* g2) {
+  using namespace qff;
+  q32::Q g = {0.f, 0.f, 0.f, 0.f};
+  const Q top = product_ff<DE>(m, q, 0, m.nt, g);
+  Q out;
+  if (m.nb > 0) {
+    const Q bot = product_ff<DE>(m, q, m.nt, m.nt + m.nb, g);
+    const F inv = mul(recip(norm2(bot)), F{m.scale_ff[0], m.scale_ff[1]});
+    out = qmul_conj(top, bot);
+    out.w = mul(out.w, inv);
+    out.x = mul(out.x, inv);
+    out.y = mul(out.y, inv);
+    out.z = mul(out.z, inv);
+  } else {
+    const F s = {m.scale_ff[0], m.scale_ff[1]};
+    out.w = mul(top.w, s);
+    out.x = mul(top.x, s);
+    out.y = mul(top.y, s);
+    out.z = mul(top.z, s);
+  }
+  if (DE) *g2 = q32::norm2(g);
+  return out;
+}
+
+}  // namespace qj

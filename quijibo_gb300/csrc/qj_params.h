@@ -31,6 +31,9 @@ struct MapParams {
   // the two-voxel FP32 path: every value doubled into a (voxel A, voxel B) pair
   alignas(16) float2 rn2[QJ_MAX_ROOTS][4];  // (-t_c, -t_c) for c = w, x, y, z
   alignas(8) float2 ex2[QJ_MAX_ROOTS];      // (x32[i][0], x32[i][0])
+  // the double-float head: each root coordinate and the scale as hi + lo
+  alignas(8) float rff[QJ_MAX_ROOTS][4][2];
+  float scale_ff[2];
 };
 
 // Cell-centred grid geometry (FIELD_3D) and the z-range of one launch.
@@ -51,6 +54,12 @@ struct IterParams {
   double escape;     // escape radius (the reference hard-codes 2000; the workloads use 2)
   double band;       // FP32 voxels with |d| < band are re-evaluated in FP64
   double field_tol;  // ... and so are voxels with |log|q|| < field_tol
+  // voxels whose tracked FP32 error exceeds est_tol * |log|q|| are re-run:
+  // with ff_head double-float iterations first (integer exponents), or in
+  // FP64 when ff_head is 0.  est_tol 0 = off.
+  double est_tol;
+  int ff_head;
+  int pad_;
 };
 
 // Device-side counters of one field or mesh call.
@@ -60,6 +69,8 @@ struct DevStats {
   unsigned long long nonfinite;     // FP32 voxels that overflowed or underflowed
   unsigned long long tiles_done;    // work-queue position of the tile scheduler
   unsigned long long aux[4];
+  unsigned long long rerun;         // length of the double-float re-run list
+  unsigned long long rerun_iters;   // map applications of the re-runs
 };
 
 }  // namespace qj

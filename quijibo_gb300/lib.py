@@ -38,13 +38,13 @@ class QjgGrid(C.Structure):
 class QjgIter(C.Structure):
     _fields_ = [("max_it", C.c_int32), ("precision", C.c_int32), ("refine_pow", C.c_int32),
                 ("want_de", C.c_int32), ("escape", C.c_double), ("band_h", C.c_double),
-                ("field_tol", C.c_double)]
+                ("field_tol", C.c_double), ("rel_tol", C.c_double)]
 
 
 class QjgFieldStats(C.Structure):
     _fields_ = [("voxels", C.c_int64), ("voxel_iters", C.c_int64), ("root_terms", C.c_int64),
                 ("refined", C.c_int64), ("refined_iters", C.c_int64), ("nonfinite", C.c_int64),
-                ("lane_iters", C.c_int64)]
+                ("lane_iters", C.c_int64), ("rerun", C.c_int64), ("rerun_iters", C.c_int64)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}
@@ -238,9 +238,9 @@ class Context:
 
     @staticmethod
     def iter_params(max_it, escape, precision=QJG_FP64, refine_pow=QJG_REFINE_POW, want_de=False,
-                    band_h=2.0, field_tol=1e-3):
+                    band_h=2.0, field_tol=1e-3, rel_tol=0.0):
         return QjgIter(int(max_it), int(precision), int(refine_pow), int(bool(want_de)),
-                       float(escape), float(band_h), float(field_tol))
+                       float(escape), float(band_h), float(field_tol), float(rel_tol))
 
     def field(self, handle, grid: Grid, it: QjgIter, d_field, d_de=None, z0=0, z1=None,
               stream=None):

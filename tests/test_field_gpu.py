@@ -174,3 +174,23 @@ def test_fp32_voxel_pairs_equal_single_voxel_form(ctx, case, precision):
     for k in ("voxel_iters", "refined", "refined_iters", "nonfinite"):
         assert sa[k] == sb[k], k
     assert sa["voxel_iters"] > 0
+
+
+@pytest.mark.parametrize("wl,res", [("precision", 128), ("large", 64)])
+def test_fp32_refine_rel_tol_bounds_field_error(ctx, wl, res):
+    """With rel_tol = 1e-6 every voxel is within 1e-6 relative of the FP64
+    field (the FP64 form is pinned to the oracle and the reference by the
+    tests above) and the sign map is identical; without it the band rule
+    alone leaves voxels above 1e-6."""
+    from quijibo_gb300.rootsets import large_workload
+    rs, g, p = (precision_workload if wl == "precision" else large_workload)(res)
+    f64, _, _ = run(ctx, rs, g, p, precision=lib.QJG_FP64, refine_pow=lib.QJG_REFINE_INT)
+    band, _, sb = run(ctx, rs, g, p, precision=lib.QJG_FP32_REFINE, want_de=True,
+                      refine_pow=lib.QJG_REFINE_INT)
+    tight, _, st = run(ctx, rs, g, p, precision=lib.QJG_FP32_REFINE, want_de=True,
+                       refine_pow=lib.QJG_REFINE_INT, rel_tol=1e-6)
+    assert np.array_equal(tight > 0, f64 > 0)
+    assert rel_err(band, f64).max() > 1e-6
+    assert rel_err(tight, f64).max() <= 1e-6
+    assert st["rerun"] > 0 and st["rerun_iters"] > 0
+    assert st["refined"] >= sb["refined"]
