@@ -27,6 +27,8 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+from quijibo_gb300.roofline import field_flops  # noqa: E402
+
 METRIC = "Julia field Gvox/s (FP32+refine vs FP64, same sign map); p50/p99 req latency"
 RES = 512
 WORKLOAD = ("precision form: 16 top / 8 bottom roots U[-1.2,1.2]^4 (seed 0), exponents {1,2}, "
@@ -37,25 +39,6 @@ WORKLOAD = ("precision form: 16 top / 8 bottom roots U[-1.2,1.2]^4 (seed 0), exp
 # dram__bytes_read.sum + dram__bytes_write.sum, one pass at full size): the
 # FMA-bound kernel moves ~7.7 B per voxel, the FP64 field it writes
 TRAFFIC_PER_VOXEL = (19.15e6 + 1.01e9) / 512 ** 3
-
-
-def field_flops(rs, voxel_iters, de=True):
-    """Algorithmic FP32 flops of `voxel_iters` map applications (FMA = 2).
-
-    Per root term: 4 (q - r) + 11 per squaring (exponent 2) + 28 per
-    accumulating Hamilton product (the first root of each product has none)
-    + 16 for the distance-estimate gradient term (|d|^2 7, divide 1, 4 FMA 8).
-    Per application: T * conj(B) 28, |B|^2 7, s/|B|^2 1, scaling 4, |q|^2 7,
-    and with the estimate |g|^2 7 + two logs and their sum 3 (10)."""
-    per = 0
-    for pw, n in ((rs.top_powers, rs.n_top), (rs.bottom_powers, rs.n_bottom)):
-        if n == 0:
-            continue
-        per += 4 * n + 28 * (n - 1) + sum(11 * (int(e) - 1) for e in pw)
-        if de:
-            per += 16 * n
-    per += (28 + 7 + 1 if rs.n_bottom else 0) + 4 + 7 + (10 if de else 0)
-    return per * voxel_iters
 
 
 class ClockSampler:

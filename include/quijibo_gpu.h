@@ -147,6 +147,12 @@ typedef struct {
   int64_t map_evals_fp32;/* FP32 evaluations whose sign was trusted (precision form only) */
   int64_t slabs;         /* z-slabs processed */
   qjg_field_stats field; /* the field pass of qjg_mesh_stream */
+  /* with qjg_set_timing on (else 0): device milliseconds of each phase, summed over slabs */
+  double ms_field;       /* slab fields (qjg_mesh_stream) */
+  double ms_classify;    /* cube flags, edge masks, vertex ids */
+  double ms_vertices;    /* vertex placement (interpolation or bisection) */
+  double ms_triangles;   /* triangle emission */
+  double ms_filter;      /* degenerate-triangle filter and output conversion */
 } qjg_mesh_stats;
 
 /* Marching cubes on a stored device field (X*Y*Z doubles).  Corners are

@@ -4,6 +4,7 @@ which measures the headline field).  Each prints one JSON object.
     python -m quijibo_gb300.benchmarks mesh   [--res 512] [--workload precision|large]
     python -m quijibo_gb300.benchmarks energy [--samples 200000] [--steps 50]
     python -m quijibo_gb300.benchmarks serve  [--requests 400] [--scale 0.25]
+    python -m quijibo_gb300.benchmarks large  [--res 2200] [--slab 64] [--check-slices 4]
 
 All inputs are synthetic (quijibo_gb300/rootsets.py, samples.py).
 """
@@ -28,6 +29,7 @@ def bench_mesh(args):
     from .rootsets import large_workload, precision_workload
     ctx = lib.Context(0)
     wl = precision_workload if args.workload == "precision" else large_workload
+    args.res = args.res or 512
     rs, g, p = wl(args.res)
     h = ctx.upload(rs)
     it = ctx.iter_params(p["max_it"], p["escape"], precision=lib.QJG_FP32_REFINE,
@@ -205,10 +207,131 @@ def bench_serve(args):
     return out
 
 
+def bench_large(args):
+    """The large-grid configuration: 48 top / 24 bottom roots, 60 iterations,
+    a res^3 grid (2200 by default) in 64-slice z-slabs.  (1) The precision
+    field (FP32 bulk, double-float re-run at rel_tol, FP64 band) streamed
+    through the mesher to FP32 vertices and int32 triangles, with the device
+    time of each mesher phase; (2) the field alone over the same slabs, for
+    the FMA-pipe roofline of the bulk kernel; (3) evenly spaced z-slices in
+    both the precision form and the plain FP64 form: sign map, error, and
+    the FP64 form's speed."""
+    import torch
+
+    from . import lib
+    from .rootsets import large_workload
+    from .roofline import field_flops
+    ctx = lib.Context(0)
+    args.res = args.res or 2200
+    rs, g, p = large_workload(args.res)
+    h = ctx.upload(rs)
+    n = g.n_voxels
+    XY = g.res[0] * g.res[1]
+    it = ctx.iter_params(p["max_it"], p["escape"], precision=lib.QJG_FP32_REFINE,
+                         refine_pow=lib.QJG_REFINE_INT, rel_tol=args.rel_tol)
+    out = {"workload": "large %d^3: 48 top / 24 bottom roots U[-1.2,1.2]^4 (seed 0), exponents "
+                       "{1,2}, s = u * conformal scale, 60 iterations, escape 2" % args.res,
+           "voxels": n, "slab": args.slab, "rel_tol": args.rel_tol}
+    # warm the modules on a small grid
+    from .rootsets import Grid
+    small = Grid((64, 64, 64))
+    ws = torch.empty(64 ** 3, dtype=torch.float64, device="cuda")
+    ctx.field(h, small, it, ws.data_ptr())
+    torch.cuda.synchronize()
+    del ws
+
+    # (1) streamed field + mesh
+    if not args.no_mesh:
+        vcap = int(args.vert_cap or 40 * XY)
+        tcap = int(args.tri_cap or 80 * XY)
+        v32 = torch.empty(3 * vcap, dtype=torch.float32, device="cuda")
+        tris = torch.empty(3 * tcap, dtype=torch.int32, device="cuda")
+        ctx.set_timing(True)
+        t0 = time.perf_counter()
+        rc, st = ctx.mesh_stream(h, g, it, check=False, d_verts32=v32.data_ptr(), vert_cap=vcap,
+                                 d_tris=tris.data_ptr(), tri_cap=tcap, slab_nz=args.slab)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        if rc == -5:
+            raise SystemExit("raise --vert-cap/--tri-cap: needs %d / %d" % (st["n_verts"], st["n_tris"]))
+        V, T = st["n_verts"], st["n_tris"] + st["n_degenerate"]
+        # algorithmic HBM bytes of classify + id + triangle phases: the FP64
+        # field read once, flags / masks / id bases written and read, edge
+        # list entries, triangles
+        cls_bytes = n * (8 + 1 + 1 + 4) + 4 * V
+        tri_bytes = n * 1 + 12 * T
+        mesh_ms = st["ms_classify"] + st["ms_triangles"]
+        out["mesh"] = {"triangles": st["n_tris"], "vertices": V, "degenerate": st["n_degenerate"],
+                       "unbracketed": st["n_unbracketed"], "wall_s": wall,
+                       "triangles_per_s": st["n_tris"] / wall,
+                       "ms_field": st["ms_field"], "ms_classify": st["ms_classify"],
+                       "ms_vertices": st["ms_vertices"], "ms_triangles": st["ms_triangles"],
+                       "ms_filter": st["ms_filter"],
+                       "classify_emit_gb_s": (cls_bytes + tri_bytes) / (mesh_ms * 1e-3) / 1e9,
+                       "bisection_map_evals_fp64": st["map_evals"],
+                       "bisection_map_evals_fp32": st["map_evals_fp32"], "slabs": st["slabs"],
+                       "field": st["field"]}
+        del v32, tris
+        torch.cuda.empty_cache()
+
+    # (2) the field alone, slab by slab
+    ctx.set_timing(True)
+    buf = torch.empty(args.slab * XY, dtype=torch.float64, device="cuda")
+    bulk = rest = 0.0
+    tot = {}
+    for z0 in range(0, g.res[2], args.slab):
+        z1 = min(z0 + args.slab, g.res[2])
+        ctx.field(h, g, it, buf.data_ptr(), z0=z0, z1=z1)
+        b, r = ctx.last_timings()
+        bulk, rest = bulk + b, rest + r
+        for k, v in ctx.stats().items():
+            tot[k] = tot.get(k, 0) + v
+    del buf
+    flops = field_flops(rs, tot["voxel_iters"])
+    peak = lib.fma_probe(0)
+    out["field"] = {"gvox_s": n / ((bulk + rest) * 1e-3) / 1e9, "bulk_ms": bulk, "rest_ms": rest,
+                    "roofline": {"achieved_tflops": flops / (bulk * 1e-3) / 1e12,
+                                 "peak_tflops": peak, "frac": flops / (bulk * 1e-3) / 1e12 / peak},
+                    "stats": tot, "lane_efficiency": tot["voxel_iters"] / max(1, tot["lane_iters"])}
+
+    # (3) sampled slices against the plain FP64 form
+    it64 = ctx.iter_params(p["max_it"], p["escape"], precision=lib.QJG_FP64)
+    zs = [int(v) for v in np.linspace(0, g.res[2] - 1, args.check_slices)]
+    a = torch.empty(XY, dtype=torch.float64, device="cuda")
+    b64 = torch.empty(XY, dtype=torch.float64, device="cuda")
+    ms64 = ms32 = 0.0
+    sign = 0
+    mx = 0.0
+    ss = 0.0
+    for z in zs:
+        e0, e1 = _events(torch)
+        e0.record()
+        ctx.field(h, g, it64, b64.data_ptr(), z0=z, z1=z + 1)
+        e1.record()
+        e1.synchronize()
+        ms64 += e0.elapsed_time(e1)
+        e0.record()
+        ctx.field(h, g, it, a.data_ptr(), z0=z, z1=z + 1)
+        e1.record()
+        e1.synchronize()
+        ms32 += e0.elapsed_time(e1)
+        sign += int(((a > 0) != (b64 > 0)).sum().item())
+        rel = (a - b64).abs() / b64.abs().clamp_min(1e-300)
+        mx = max(mx, float(rel.max().item()))
+        ss += float(rel.pow(2).sum().item())
+    nv = len(zs) * XY
+    fp64_gvox = nv / (ms64 * 1e-3) / 1e9
+    out["fp64_check"] = {"slices": zs, "voxels": nv, "sign_map_disagreements": sign,
+                         "max_rel_err": mx, "rms_rel_err": (ss / nv) ** 0.5,
+                         "fp64_gvox_s": fp64_gvox, "fp64_full_grid_s_est": n / fp64_gvox / 1e9,
+                         "speedup_field_vs_fp64": out["field"]["gvox_s"] / fp64_gvox}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["mesh", "energy", "serve"])
-    ap.add_argument("--res", type=int, default=512)
+    ap.add_argument("what", choices=["mesh", "energy", "serve", "large"])
+    ap.add_argument("--res", type=int, default=0, help="grid edge (mesh: 512, large: 2200)")
     ap.add_argument("--workload", default="precision", choices=["precision", "large"])
     ap.add_argument("--slab", type=int, default=64)
     ap.add_argument("--vert-cap", type=int, default=0)
@@ -222,8 +345,12 @@ def main():
     ap.add_argument("--budget-gb", type=float, default=64.0)
     ap.add_argument("--baseline-sample", type=int, default=40)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--rel-tol", type=float, default=1e-6)
+    ap.add_argument("--check-slices", type=int, default=4)
+    ap.add_argument("--no-mesh", action="store_true")
     args = ap.parse_args()
-    fn = {"mesh": bench_mesh, "energy": bench_energy, "serve": bench_serve}[args.what]
+    fn = {"mesh": bench_mesh, "energy": bench_energy, "serve": bench_serve,
+          "large": bench_large}[args.what]
     print(json.dumps(fn(args)), flush=True)
 
 

@@ -185,6 +185,8 @@ void qjg_destroy(qjg_ctx* ctx) {
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   for (cudaEvent_t e : ctx->ev)
     if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : ctx->mev)
+    if (e) cudaEventDestroy(e);
   delete ctx;
 }
 
@@ -337,6 +339,8 @@ int qjg_set_timing(qjg_ctx* ctx, int on) {
   if (!ctx) return QJG_ERR_ARG;
   QJ_CUDA(ctx, cudaSetDevice(ctx->device));
   for (cudaEvent_t& e : ctx->ev)
+    if (!e) QJ_CUDA(ctx, cudaEventCreate(&e));
+  for (cudaEvent_t& e : ctx->mev)
     if (!e) QJ_CUDA(ctx, cudaEventCreate(&e));
   ctx->timing = on != 0;
   return QJG_OK;

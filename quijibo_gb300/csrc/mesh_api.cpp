@@ -94,12 +94,26 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
 
   long long nv = 0, nt = 0;
   int prevL = 0;
+  // phase timing (qjg_set_timing): events mev[0..4] bracket the phases of a slab
+  const bool timed = ctx->timing;
+  auto mark = [&](int k) -> cudaError_t {
+    return timed ? cudaEventRecord(ctx->mev[k], s) : cudaSuccess;
+  };
+  auto span = [&](int a, int b, double* acc) -> cudaError_t {
+    if (!timed) return cudaSuccess;
+    float ms = 0.f;
+    cudaError_t e = cudaEventSynchronize(ctx->mev[b]);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ctx->mev[a], ctx->mev[b]);
+    *acc += ms;
+    return e;
+  };
   for (int c0 = 0; c0 < Z - 1;) {
     const int c1 = std::min(c0 + nz, Z - 1);
     const bool last = c1 == Z - 1;
     const int L = c1 - c0;
     // field planes [c0, c1]
     const double* src;
+    QJ_CUDA(ctx, mark(0));
     if (streaming) {
       qjg_field_stats fs;
       if (c0 == 0) {
@@ -134,6 +148,7 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
                                    XY * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
     }
     // classify cube layers [c0, c1) into window layers 1..L
+    QJ_CUDA(ctx, mark(1));
     QJ_CUDA(ctx, qj::mesh_flags(src, X, Y, L, ctx->m_flags + XY, s));
     ctx->launches++;
     // vertex ids of planes [c0, c1) (+ Z-1 on the last slab) = window planes [1, j1)
@@ -152,17 +167,24 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
     if ((rc = grow_keep(ctx, &ctx->m_verts, &ctx->m_verts_cap, (size_t)(nv + n_new) * 3,
                         (size_t)nv * 3, s)))
       return rc;
+    QJ_CUDA(ctx, mark(2));
     // FP32-first bisection unless the plain FP64 form is asked for
     const bool hybrid = iter && iter->precision != QJG_FP64;
     QJ_CUDA(ctx, qj::mesh_vertices(*m, g, it, edge_mode, pow_ref, hybrid, w, n_new, nv, c0, src,
                                    ctx->m_verts, iso, ctx->d_mstats, s));
     if (n_new) ctx->launches++;
     nv += n_new;
+    QJ_CUDA(ctx, mark(3));
     // triangles of layers [c0-1, c1-1) (+ c1-1 on the last slab)
     const int jt0 = c0 == 0 ? 1 : 0, jt1 = last ? L + 1 : L;
     long long t_new = 0;
     QJ_CUDA(ctx, qj::mesh_triangles(w, jt0, jt1, nt, tris, tcap, &t_new, s));
     ctx->launches += 3;
+    QJ_CUDA(ctx, mark(4));
+    QJ_CUDA(ctx, span(0, 1, &st.ms_field));
+    QJ_CUDA(ctx, span(1, 2, &st.ms_classify));
+    QJ_CUDA(ctx, span(2, 3, &st.ms_vertices));
+    QJ_CUDA(ctx, span(3, 4, &st.ms_triangles));
     nt += t_new;
     prevL = L;
     st.slabs++;
@@ -187,6 +209,7 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
       (rc = ensure(ctx, &ctx->m_bsum, &ctx->m_bsum_cap, (size_t)qj::mesh_scan_blocks(nt))))
     return rc;
   long long keep = 0;
+  QJ_CUDA(ctx, mark(0));
   QJ_CUDA(ctx, qj::mesh_filter(tris, nt, ctx->m_verts, ctx->m_tris, ctx->m_bsum, &keep, s));
   if (nt) ctx->launches += 3;
   QJ_CUDA(ctx, cudaMemcpyAsync(tris, ctx->m_tris, (size_t)keep * 3 * sizeof(int32_t),
@@ -200,7 +223,9 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
     QJ_CUDA(ctx, qj::mesh_to_float(ctx->m_verts, v32, nv * 3, s));
     if (nv) ctx->launches++;
   }
+  QJ_CUDA(ctx, mark(1));
   QJ_CUDA(ctx, cudaStreamSynchronize(s));
+  QJ_CUDA(ctx, span(0, 1, &st.ms_filter));
   if (out) *out = st;
   return QJG_OK;
 }

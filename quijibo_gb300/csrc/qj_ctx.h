@@ -38,6 +38,7 @@ struct qjg_ctx {
   bool timing = false;
   bool timed_refine = false;
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t mev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // mesher phases
   int64_t launches = 0;
   // marching-cubes scratch
   qj::DevStats* d_mstats = nullptr;

@@ -378,8 +378,10 @@ __device__ __forceinline__ q32::Q root_term32(const MapParams& m, const q32::Q& 
   return root_power_rare(d, ie, m.e32[i]);
 }
 
-// prod_{i in [lo, hi)} (q - r_i)^(e_i), left to right; the first term starts
-// the product and the rest go two per trip.
+// prod_{i in [lo, hi)} (q - r_i)^(e_i) in left-to-right order; the first
+// term starts the product and the rest go two per trip as r * (t0 * t1):
+// the same algebra as (r * t0) * t1, with t0 * t1 off the serial chain
+// through r, which halves the dependent-latency path of the loop.
 template <bool DE>
 __device__ __forceinline__ q32::Q product32(const MapParams& m, const q32::Q& q, int lo, int hi,
                                             q32::Q& g) {
@@ -390,7 +392,7 @@ __device__ __forceinline__ q32::Q product32(const MapParams& m, const q32::Q& q,
   for (; i + 1 < hi; i += 2) {
     const Q t0 = root_term32<DE>(m, q, i, g);
     const Q t1 = root_term32<DE>(m, q, i + 1, g);
-    r = qmul(qmul(r, t0), t1);
+    r = qmul(r, qmul(t0, t1));
   }
   if (i < hi) r = qmul(r, root_term32<DE>(m, q, i, g));
   return r;
@@ -454,7 +456,7 @@ __device__ __forceinline__ q32x2::Q2 product32x2(const MapParams& m, const q32x2
   for (; i + 1 < hi; i += 2) {
     const Q2 t0 = root_term32x2<DE>(m, q, i, g);
     const Q2 t1 = root_term32x2<DE>(m, q, i + 1, g);
-    r = qmul(qmul(r, t0), t1);
+    r = qmul(r, qmul(t0, t1));
   }
   if (i < hi) r = qmul(r, root_term32x2<DE>(m, q, i, g));
   return r;

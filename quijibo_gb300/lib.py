@@ -57,10 +57,14 @@ class QjgMeshStats(C.Structure):
     _fields_ = [("n_verts", C.c_int64), ("n_tris", C.c_int64), ("n_degenerate", C.c_int64),
                 ("n_unbracketed", C.c_int64), ("map_evals", C.c_int64),
                 ("map_evals_fp32", C.c_int64), ("slabs", C.c_int64),
-                ("field", QjgFieldStats)]
+                ("field", QjgFieldStats), ("ms_field", C.c_double), ("ms_classify", C.c_double),
+                ("ms_vertices", C.c_double), ("ms_triangles", C.c_double),
+                ("ms_filter", C.c_double)]
 
     def as_dict(self):
-        d = {k: int(getattr(self, k)) for k, _ in self._fields_ if k != "field"}
+        d = {k: int(getattr(self, k)) for k, t in self._fields_
+             if k != "field" and t is C.c_int64}
+        d.update({k: float(getattr(self, k)) for k, t in self._fields_ if t is C.c_double})
         d["field"] = self.field.as_dict()
         return d
 

@@ -152,3 +152,22 @@ def test_degenerate_grids_give_empty_meshes(ctx):
         _, st = ctx.mesh_stream(h, g, it, **out.kw())
         assert st["n_verts"] == 0 and st["n_tris"] == 0
     ctx.free(h)
+
+
+def test_phase_timing_of_the_streaming_mesher(ctx):
+    rs, g, p = precision_workload(48)
+    h = ctx.upload(rs)
+    it = ctx.iter_params(p["max_it"], p["escape"], precision=lib.QJG_FP32_REFINE,
+                         refine_pow=lib.QJG_REFINE_INT)
+    out = Out(g.n_voxels)
+    _, off = ctx.mesh_stream(h, g, it, slab_nz=16, **out.kw())
+    assert off["ms_field"] == 0 and off["ms_classify"] == 0
+    ctx.set_timing(True)
+    try:
+        _, st = ctx.mesh_stream(h, g, it, slab_nz=16, **out.kw())
+    finally:
+        ctx.set_timing(False)
+    assert st["n_tris"] == off["n_tris"] > 0
+    for k in ("ms_field", "ms_classify", "ms_vertices", "ms_triangles", "ms_filter"):
+        assert st[k] > 0, k
+    ctx.free(h)
