@@ -54,7 +54,8 @@ struct IterParams {
   double escape;     // escape radius (the reference hard-codes 2000; the workloads use 2)
   double band;       // FP32 voxels with |d| < band are re-evaluated in FP64
   double field_tol;  // ... and so are voxels with |log|q|| < field_tol
-  // voxels whose tracked FP32 error exceeds est_tol * |log|q|| are re-run:
+  // voxels whose tracked FP32 error exceeds est_tol * |log|q|| (est_tol is the
+  // caller's rel_tol) are re-run:
   // with ff_head double-float iterations first (integer exponents), or in
   // FP64 when ff_head is 0.  est_tol 0 = off.
   double est_tol;
