@@ -182,6 +182,9 @@ void qjg_destroy(qjg_ctx* ctx) {
   cudaFree(ctx->m_bsum);
   cudaFree(ctx->m_verts);
   cudaFree(ctx->m_tris);
+  cudaFree(ctx->m_estate);
+  cudaFree(ctx->m_epark);
+  cudaFree(ctx->m_ecount);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   for (cudaEvent_t e : ctx->ev)
     if (e) cudaEventDestroy(e);

@@ -430,6 +430,263 @@ __global__ void __launch_bounds__(128) vertex_kernel(const __grid_constant__ Map
   }
 }
 
+// ------------------------------------------------- vertices, FP32 first
+
+// The FP32-first bisection with its FP64 evaluations taken out of line.  In
+// vertex_kernel<BISECT, *, HYBRID> a warp whose lane needs one FP64 map
+// evaluation waits for it at 1/64 of the FP32 rate while its other lanes
+// idle.  Here each edge carries its bisection state; an edge that needs an
+// FP64 value parks on a list, one kernel evaluates every parked point (a
+// warp of FP64 work), and the edges resume.  The decisions, and so the
+// vertices, are those of vertex_kernel.
+
+struct EdgeState {
+  double a[3], b[3];  // stages 0-3: the edge's ends p0, p1; stage 4: positive, negative end
+  double va, vb;      // their values
+  double pending;     // FP64 value of the point the edge waits for
+  int stage;          // 0 f(p0), 1 f(p1), 2 FP64 f(p0), 3 FP64 f(p1), 4 bisection
+  int rec;            // bisection level
+  int flags;          // EDGE_* bits
+  int pad;
+};
+
+enum : int { EDGE_PENDING = 1, EDGE_A64 = 2, EDGE_B64 = 4 };
+
+__device__ __forceinline__ void edge_point(const EdgeState& e, double p[3]) {
+  using namespace q64;
+#pragma unroll
+  for (int c = 0; c < 3; c++)
+    p[c] = e.stage == 0 || e.stage == 2 ? e.a[c]
+           : e.stage == 1 || e.stage == 3 ? e.b[c]
+                                          : mul(add(e.a[c], e.b[c]), 0.5);
+}
+
+// Runs the edge until it is done (returns false; the vertex is written and
+// *bad set) or needs an FP64 value (returns true).
+template <bool POW_REF>
+__device__ bool edge_advance(const MapParams& m, const GridParams& g, const IterParams& it,
+                             EdgeState& e, double iso, double* vert, bool* bad,
+                             unsigned long long* e32) {
+  using namespace q64;
+  for (;;) {
+    double p[3];
+    edge_point(e, p);
+    if (e.stage == 4) {
+      // midpointSearch, TRIANGLE_MESH.cpp:2232-2271
+      if (mul(e.va, e.vb) >= 0.0 || e.rec >= 6) {
+        *bad = mul(e.va, e.vb) >= 0.0;
+        vert[0] = p[0];
+        vert[1] = p[1];
+        vert[2] = p[2];
+        return false;
+      }
+    }
+    double v;
+    bool from64 = false;
+    if (e.flags & EDGE_PENDING) {
+      v = e.pending;
+      e.flags &= ~EDGE_PENDING;
+      from64 = true;
+    } else if (e.stage == 2 || e.stage == 3) {
+      return true;
+    } else {
+      float err;
+      const float f = escape32(m, it, p, g.slice, &err);
+      const float vf = f - (float)iso;
+      if (!(fabsf(vf) > 1.01f * err + 1e-8f + 1e-6f * fabsf((float)iso))) return true;
+      (*e32)++;
+      v = (double)vf;
+    }
+    bool orient = false;
+    switch (e.stage) {
+      case 0:
+        e.va = v;
+        if (from64) e.flags |= EDGE_A64;
+        e.stage = 1;
+        break;
+      case 1:
+        e.vb = v;
+        if (from64) e.flags |= EDGE_B64;
+        if (mul(e.va, e.vb) >= 0.0) {
+          // a failed bracket decides the whole edge: confirm it in FP64
+          if (!(e.flags & EDGE_A64)) e.stage = 2;
+          else if (!(e.flags & EDGE_B64)) e.stage = 3;
+          else orient = true;
+        } else {
+          orient = true;
+        }
+        break;
+      case 2:
+        e.va = v;
+        e.flags |= EDGE_A64;
+        if (e.flags & EDGE_B64) orient = true;
+        else e.stage = 3;
+        break;
+      case 3:
+        e.vb = v;
+        e.flags |= EDGE_B64;
+        orient = true;
+        break;
+      default:
+        if (fabs(v) < 1e-8) {
+          vert[0] = p[0];
+          vert[1] = p[1];
+          vert[2] = p[2];
+          *bad = false;
+          return false;
+        }
+        if (v < 0) {
+          e.b[0] = p[0];
+          e.b[1] = p[1];
+          e.b[2] = p[2];
+          e.vb = v;
+        } else {
+          e.a[0] = p[0];
+          e.a[1] = p[1];
+          e.a[2] = p[2];
+          e.va = v;
+        }
+        e.rec++;
+    }
+    if (orient) {
+      // positive end first (TRIANGLE_MESH.cpp:2060-2080)
+      if (e.va < 0) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          const double t = e.a[c];
+          e.a[c] = e.b[c];
+          e.b[c] = t;
+        }
+        const double t = e.va;
+        e.va = e.vb;
+        e.vb = t;
+      }
+      e.stage = 4;
+      e.rec = 0;
+    }
+  }
+}
+
+__device__ __forceinline__ void warp_push(bool want, uint32_t k, unsigned long long* count,
+                                          uint32_t* list) {
+  const unsigned mask = __ballot_sync(0xffffffffu, want);
+  if (!mask) return;
+  const int lane = threadIdx.x & 31;
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(count, (unsigned long long)__popc(mask));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (want) list[base + __popc(mask & ((1u << lane) - 1u))] = k;
+}
+
+__device__ __forceinline__ void edge_counts(unsigned long long e32, unsigned long long e64,
+                                            unsigned long long bad, DevStats* st) {
+  for (int o = 16; o; o >>= 1) {
+    e32 += __shfl_xor_sync(0xffffffffu, e32, o);
+    e64 += __shfl_xor_sync(0xffffffffu, e64, o);
+    bad += __shfl_xor_sync(0xffffffffu, bad, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (e64) atomicAdd(&st->aux[1], e64);
+    if (bad) atomicAdd(&st->aux[2], bad);
+    if (e32) atomicAdd(&st->aux[3], e32);
+  }
+}
+
+// Starts every edge of the slab; edges that need FP64 go to `park`.
+template <bool POW_REF>
+__global__ void __launch_bounds__(128) edge_start_kernel(const __grid_constant__ MapParams m,
+                                                         const GridParams g, const IterParams it,
+                                                         const uint32_t* __restrict__ list,
+                                                         long long n, long long id0, int c0,
+                                                         EdgeState* __restrict__ es,
+                                                         double* __restrict__ verts, double iso,
+                                                         uint32_t* park,
+                                                         unsigned long long* n_park,
+                                                         DevStats* st) {
+  const long long XY = (long long)g.X * g.Y;
+  unsigned long long e32 = 0, nbad = 0;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long base = (blockIdx.x * (long long)blockDim.x + threadIdx.x) & ~31ll; base < n;
+       base += stride) {
+    const long long k = base + (threadIdx.x & 31);
+    bool wait = false;
+    if (k < n) {
+      const uint32_t e = list[k];
+      const int a = (int)(e & 3u);
+      const long long w = e >> 2;
+      const int z = c0 - 1 + (int)(w / XY);
+      const int r = (int)(w % XY);
+      const int x = r % g.X, y = r / g.X;
+      EdgeState s;
+      cell_center(g, x, y, z, s.a);
+      cell_center(g, x + (a == 0), y + (a == 1), z + (a == 2), s.b);
+      s.va = s.vb = s.pending = 0.0;
+      s.stage = s.rec = s.flags = s.pad = 0;
+      bool bad = false;
+      wait = edge_advance<POW_REF>(m, g, it, s, iso, verts + 3 * (id0 + k), &bad, &e32);
+      nbad += bad;
+      if (wait) es[k] = s;
+    }
+    warp_push(wait, (uint32_t)k, n_park, park);
+  }
+  edge_counts(e32, 0, nbad, st);
+}
+
+// The FP64 value of every parked edge's point.
+template <bool POW_REF>
+__global__ void __launch_bounds__(128) edge_fp64_kernel(const __grid_constant__ MapParams m,
+                                                        const GridParams g, const IterParams it,
+                                                        const uint32_t* __restrict__ park,
+                                                        const unsigned long long* n_park,
+                                                        EdgeState* __restrict__ es, double iso,
+                                                        DevStats* st) {
+  const unsigned long long n = *n_park;
+  unsigned long long e64 = 0;
+  for (unsigned long long j = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; j < n;
+       j += (unsigned long long)gridDim.x * blockDim.x) {
+    EdgeState& e = es[park[j]];
+    double p[3];
+    edge_point(e, p);
+    e.pending = value64<POW_REF>(m, g, it, p, iso, &e64);
+    e.flags |= EDGE_PENDING;
+  }
+  for (int o = 16; o; o >>= 1) e64 += __shfl_xor_sync(0xffffffffu, e64, o);
+  if ((threadIdx.x & 31) == 0 && e64) atomicAdd(&st->aux[1], e64);
+}
+
+// Resumes the parked edges; those that need FP64 again go to `next`.
+template <bool POW_REF>
+__global__ void __launch_bounds__(128) edge_resume_kernel(const __grid_constant__ MapParams m,
+                                                          const GridParams g, const IterParams it,
+                                                          const uint32_t* __restrict__ park,
+                                                          const unsigned long long* n_park,
+                                                          long long id0,
+                                                          EdgeState* __restrict__ es,
+                                                          double* __restrict__ verts, double iso,
+                                                          uint32_t* next,
+                                                          unsigned long long* n_next,
+                                                          DevStats* st) {
+  const unsigned long long n = *n_park;
+  unsigned long long e32 = 0, nbad = 0;
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  for (unsigned long long base = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) & ~31ull;
+       base < n; base += stride) {
+    const unsigned long long j = base + (threadIdx.x & 31);
+    bool wait = false;
+    uint32_t k = 0;
+    if (j < n) {
+      k = park[j];
+      EdgeState s = es[k];
+      bool bad = false;
+      wait = edge_advance<POW_REF>(m, g, it, s, iso, verts + 3 * (id0 + k), &bad, &e32);
+      nbad += bad;
+      if (wait) es[k] = s;
+    }
+    warp_push(wait, k, n_next, next);
+  }
+  edge_counts(e32, 0, nbad, st);
+}
+
 __global__ void to_float_kernel(const double* __restrict__ a, float* __restrict__ b, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
@@ -444,6 +701,8 @@ int sm_count() {
 }
 
 }  // namespace
+
+size_t mesh_edge_state_bytes() { return sizeof(EdgeState); }
 
 long long mesh_scan_blocks(long long n) { return (n + SCAN_B - 1) / SCAN_B + 1; }
 
@@ -480,11 +739,47 @@ cudaError_t mesh_vertex_ids(MeshWindow& w, int j0, int j1, int lay_lo, int lay_h
   return cudaGetLastError();
 }
 
+template <bool POW_REF>
+static cudaError_t parked_vertices(const MapParams& m, const GridParams& g, const IterParams& it,
+                                   const MeshWindow& w, long long n, long long id0, int c0,
+                                   double* verts, double iso, DevStats* st,
+                                   const EdgeScratch& sc, cudaStream_t s) {
+  const int blocks = (int)std::min<long long>((n + 127) / 128, (long long)sm_count() * 32);
+  EdgeState* es = static_cast<EdgeState*>(sc.state);
+  cudaError_t err = cudaMemsetAsync(sc.count, 0, 2 * sizeof(unsigned long long), s);
+  if (err) return err;
+  edge_start_kernel<POW_REF><<<blocks, 128, 0, s>>>(m, g, it, w.list, n, id0, c0, es, verts, iso,
+                                                    sc.list[0], sc.count, st);
+  // each round gives every parked edge one FP64 value; an edge asks for at
+  // most 2 at its ends (one each, or a re-check of a failed bracket) and 6
+  // in the bisection
+  for (int round = 0, cur = 0;; round++, cur ^= 1) {
+    unsigned long long parked = 0;
+    if ((err = cudaMemcpyAsync(&parked, sc.count + cur, sizeof parked, cudaMemcpyDeviceToHost, s)))
+      return err;
+    if ((err = cudaStreamSynchronize(s))) return err;
+    if (parked == 0) return cudaGetLastError();
+    if (round == 8) return cudaErrorInvalidValue;  // cannot happen: see the count above
+    const int pb = (int)std::min<long long>(((long long)parked + 127) / 128,
+                                            (long long)sm_count() * 32);
+    edge_fp64_kernel<POW_REF><<<pb, 128, 0, s>>>(m, g, it, sc.list[cur], sc.count + cur, es, iso,
+                                                 st);
+    if ((err = cudaMemsetAsync(sc.count + (cur ^ 1), 0, sizeof(unsigned long long), s)))
+      return err;
+    edge_resume_kernel<POW_REF><<<pb, 128, 0, s>>>(m, g, it, sc.list[cur], sc.count + cur, id0,
+                                                   es, verts, iso, sc.list[cur ^ 1],
+                                                   sc.count + (cur ^ 1), st);
+  }
+}
+
 cudaError_t mesh_vertices(const MapParams& m, const GridParams& g, const IterParams& it,
                           int edge_mode, bool pow_ref, bool hybrid, const MeshWindow& w,
                           long long n, long long id0, int c0, const double* src, double* verts,
-                          double iso, DevStats* st, cudaStream_t s) {
+                          double iso, DevStats* st, const EdgeScratch* scratch, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
+  if (edge_mode != 0 && hybrid && scratch)
+    return pow_ref ? parked_vertices<true>(m, g, it, w, n, id0, c0, verts, iso, st, *scratch, s)
+                   : parked_vertices<false>(m, g, it, w, n, id0, c0, verts, iso, st, *scratch, s);
   const int blocks = (int)std::min<long long>((n + 127) / 128, (long long)sm_count() * 32);
 #define QJ_VK(B, P, H) \
   vertex_kernel<B, P, H><<<blocks, 128, 0, s>>>(m, g, it, w.list, n, id0, c0, src, verts, iso, st)

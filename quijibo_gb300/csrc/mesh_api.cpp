@@ -170,8 +170,21 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
     QJ_CUDA(ctx, mark(2));
     // FP32-first bisection unless the plain FP64 form is asked for
     const bool hybrid = iter && iter->precision != QJG_FP64;
+    qj::EdgeScratch esc{};
+    const bool parked = hybrid && bisect && n_new > 0;
+    if (parked) {
+      if ((rc = ensure(ctx, &ctx->m_estate, &ctx->m_estate_cap,
+                       (size_t)n_new * qj::mesh_edge_state_bytes())) ||
+          (rc = ensure(ctx, &ctx->m_epark, &ctx->m_epark_cap, (size_t)n_new * 2)) ||
+          (rc = ensure(ctx, &ctx->m_ecount, &ctx->m_ecount_cap, (size_t)2)))
+        return rc;
+      esc.state = ctx->m_estate;
+      esc.list[0] = ctx->m_epark;
+      esc.list[1] = ctx->m_epark + n_new;
+      esc.count = ctx->m_ecount;
+    }
     QJ_CUDA(ctx, qj::mesh_vertices(*m, g, it, edge_mode, pow_ref, hybrid, w, n_new, nv, c0, src,
-                                   ctx->m_verts, iso, ctx->d_mstats, s));
+                                   ctx->m_verts, iso, ctx->d_mstats, parked ? &esc : nullptr, s));
     if (n_new) ctx->launches++;
     nv += n_new;
     QJ_CUDA(ctx, mark(3));

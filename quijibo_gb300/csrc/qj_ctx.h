@@ -58,6 +58,12 @@ struct qjg_ctx {
   size_t m_verts_cap = 0;
   int32_t* m_tris = nullptr;    // compaction target of the degenerate filter
   size_t m_tris_cap = 0;
+  uint8_t* m_estate = nullptr;  // bisection state per edge (FP32-first mesher)
+  size_t m_estate_cap = 0;
+  uint32_t* m_epark = nullptr;  // two parking lists of edges waiting for FP64
+  size_t m_epark_cap = 0;
+  unsigned long long* m_ecount = nullptr;
+  size_t m_ecount_cap = 0;
 };
 
 
