@@ -333,6 +333,30 @@ int qjg_server_wait(qjg_server* srv, int64_t ticket, qjg_result* out);
 int qjg_server_drain(qjg_server* srv);
 int qjg_server_read_stats(qjg_server* srv, qjg_server_stats* out);
 
+/* ---- file formats ------------------------------------------------------ */
+
+/* FIELD_3D's binary stream: int xRes, yRes, zRes; double center[3], lengths[3];
+ * double data[X*Y*Z] (x fastest).  Replaces FIELD_3D::write(string) / write(FILE*)
+ * (src/geometry/FIELD_3D.cpp:280-300, 4371-4393).  `field` is host or device memory. */
+int qjg_field3d_write(const char* path, const int32_t res[3], const double center[3],
+                      const double lengths[3], const double* field);
+/* The header of such a file, and its data into `field` (host or device, at
+ * least X*Y*Z doubles, else QJG_ERR_CAPACITY).  Replace FIELD_3D::read(FILE*)
+ * (FIELD_3D.cpp:4398-4450). */
+int qjg_field3d_read_header(const char* path, int32_t res[3], double center[3],
+                            double lengths[3]);
+int qjg_field3d_read(const char* path, double* field, int64_t capacity);
+/* TRIANGLE_MESH's raw stream (int V, int T, V x 3 doubles, T x 3 ints), the
+ * format TRIANGLE_MESH::read(FILE*) loads.  Replaces TRIANGLE_MESH::write(FILE*)
+ * (src/geometry/TRIANGLE_MESH.cpp:4502-4522).  Buffers host or device. */
+int qjg_mesh_write_raw(const char* path, const double* verts, int64_t n_verts,
+                       const int32_t* tris, int64_t n_tris);
+/* OBJ text as TRIANGLE_MESH::writeOBJ prints it ("v %.16f %.16f %.16f", then
+ * "f %i %i %i" 1-based; TRIANGLE_MESH.cpp:2762-2800), from FP64 or FP32
+ * vertices (exactly one of verts64 / verts32), host or device buffers. */
+int qjg_mesh_write_obj(const char* path, const double* verts64, const float* verts32,
+                       int64_t n_verts, const int32_t* tris, int64_t n_tris);
+
 #ifdef __cplusplus
 }
 #endif

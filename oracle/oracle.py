@@ -217,6 +217,9 @@ class Reference:
         L.ref_tanh_score_grad.argtypes = [A, _ip, _dp, _dp, C.c_double, C.c_int, _ip, _dp, _dp,
                                           _dp, _dp, _dp]
         L.ref_tanh_score_grad.restype = C.c_double
+        L.ref_field_write.argtypes = [C.c_char_p, _ip, _dp, _dp, _dp]
+        L.ref_mesh_write.argtypes = [_dp, C.c_int, _ip, C.c_int, C.c_char_p, C.c_char_p]
+        L.ref_mesh_write.restype = C.c_int
         self.L = L
         self.sizeof_real = L.ref_sizeof_real()
 
@@ -225,6 +228,21 @@ class Reference:
         res = np.array(grid.res, dtype=np.int32)
         return (res, np.array(grid.center, dtype=np.float64),
                 np.array(grid.lengths, dtype=np.float64), np.array(grid.rot, dtype=np.float64))
+
+    def field_write(self, path, res, center, lengths, data):
+        """FIELD_3D::write(string) of `data` (x fastest)."""
+        self.L.ref_field_write(str(path).encode(), _ptr(np.asarray(res, dtype=np.int32), _ip),
+                               _ptr(np.asarray(center, dtype=np.float64)),
+                               _ptr(np.asarray(lengths, dtype=np.float64)),
+                               _ptr(np.ascontiguousarray(data, dtype=np.float64).ravel()))
+
+    def mesh_write(self, verts, tris, obj_path, raw_path):
+        """TRIANGLE_MESH::read of the raw stream, then writeOBJ and write(FILE*)."""
+        v = np.ascontiguousarray(verts, dtype=np.float64).ravel()
+        t = np.ascontiguousarray(tris, dtype=np.int32).ravel()
+        rc = self.L.ref_mesh_write(_ptr(v), len(v) // 3, _ptr(t, _ip), len(t) // 3,
+                                   str(obj_path).encode(), str(raw_path).encode())
+        assert rc == 0, rc
 
     def mt_rand(self, seed, n):
         out = np.empty(n)

@@ -13,6 +13,7 @@
 #include <cstring>
 #include <string>
 #include <unistd.h>
+#include <vector>
 
 #include "FIELD_3D.h"
 #include "MERSENNETWISTER.h"
@@ -204,6 +205,38 @@ double ref_tanh_score_grad(const MapArgs* a, const int* res, const double* cente
   FIELD_3D& f = opt.fractal();
   for (int i = 0; i < f.totalCells(); i++) field[i] = (double)f[i];
   return score;
+}
+
+// FIELD_3D::write(string) of a field (FIELD_3D.cpp:280-300, 4371-4393).
+void ref_field_write(const char* path, const int* res, const double* center,
+                     const double* lengths, const double* data) {
+  FIELD_3D f(res[0], res[1], res[2], VEC3F(center[0], center[1], center[2]),
+             VEC3F(lengths[0], lengths[1], lengths[2]));
+  for (int i = 0; i < f.totalCells(); i++) f[i] = data[i];
+  f.write(std::string(path));
+}
+
+// A TRIANGLE_MESH loaded through its own raw reader (TRIANGLE_MESH::read,
+// TRIANGLE_MESH.cpp:4527-4553), then written by writeOBJ (:2762-2800) and by
+// write(FILE*) (:4502-4522).
+int ref_mesh_write(const double* verts, int nv, const int* tris, int nt, const char* obj_path,
+                   const char* raw_path) {
+  std::vector<char> buf(8 + (size_t)nv * 24 + (size_t)nt * 12);
+  std::memcpy(buf.data(), &nv, 4);
+  std::memcpy(buf.data() + 4, &nt, 4);
+  std::memcpy(buf.data() + 8, verts, (size_t)nv * 24);
+  std::memcpy(buf.data() + 8 + (size_t)nv * 24, tris, (size_t)nt * 12);
+  FILE* in = fmemopen(buf.data(), buf.size(), "rb");
+  if (!in) return -1;
+  TRIANGLE_MESH mesh;
+  mesh.read(in);
+  std::fclose(in);
+  mesh.writeOBJ(std::string(obj_path));
+  FILE* out = std::fopen(raw_path, "wb");
+  if (!out) return -2;
+  mesh.write(out);
+  std::fclose(out);
+  return 0;
 }
 
 }  // extern "C"

@@ -144,6 +144,12 @@ EXPORTS = {
     "qjg_fit_lbfgs": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p,
                        C.c_void_p, C.c_double, C.c_int32, C.c_double, C.c_double, C.c_int32,
                        C.c_int32, C.c_int32, _dp, C.POINTER(QjgFitStats), C.c_void_p], C.c_int),
+    "qjg_field3d_write": ([C.c_char_p, C.POINTER(C.c_int32), _dp, _dp, C.c_void_p], C.c_int),
+    "qjg_field3d_read_header": ([C.c_char_p, C.POINTER(C.c_int32), _dp, _dp], C.c_int),
+    "qjg_field3d_read": ([C.c_char_p, C.c_void_p, C.c_int64], C.c_int),
+    "qjg_mesh_write_raw": ([C.c_char_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64], C.c_int),
+    "qjg_mesh_write_obj": ([C.c_char_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64],
+                           C.c_int),
     "qjg_server_create": ([C.c_int, C.c_int32, C.c_int64, C.POINTER(C.c_void_p)], C.c_int),
     "qjg_server_destroy": ([C.c_void_p], None),
     "qjg_server_submit": ([C.c_void_p, C.POINTER(QjgRequest), C.POINTER(C.c_int64)], C.c_int),
@@ -180,6 +186,77 @@ def load():
 
 class QjgError(RuntimeError):
     pass
+
+
+def _addr(a):
+    """Address of a host numpy array or of a device buffer given as an int."""
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    return a.ctypes.data
+
+
+def _io_check(rc, what):
+    if rc != 0:
+        raise QjgError("%s failed (%d)" % (what, rc))
+
+
+def field3d_write(path, grid_res, center, lengths, field):
+    """FIELD_3D binary file from a host array (Z, Y, X) or a device address."""
+    res = (C.c_int32 * 3)(*[int(v) for v in grid_res])
+    c = np.ascontiguousarray(center, dtype=np.float64)
+    ln = np.ascontiguousarray(lengths, dtype=np.float64)
+    if not isinstance(field, int):
+        field = np.ascontiguousarray(field, dtype=np.float64)
+    _io_check(load().qjg_field3d_write(str(path).encode(), res, c.ctypes.data_as(_dp),
+                                       ln.ctypes.data_as(_dp), C.c_void_p(_addr(field))),
+              "qjg_field3d_write")
+
+
+def field3d_read(path):
+    """(res (X, Y, Z), center, lengths, field[Z, Y, X]) of a FIELD_3D file."""
+    res = (C.c_int32 * 3)()
+    c = np.empty(3)
+    ln = np.empty(3)
+    L = load()
+    _io_check(L.qjg_field3d_read_header(str(path).encode(), res, c.ctypes.data_as(_dp),
+                                        ln.ctypes.data_as(_dp)), "qjg_field3d_read_header")
+    X, Y, Z = res[0], res[1], res[2]
+    f = np.empty((Z, Y, X))
+    _io_check(L.qjg_field3d_read(str(path).encode(), C.c_void_p(f.ctypes.data), f.size),
+              "qjg_field3d_read")
+    return (X, Y, Z), c, ln, f
+
+
+def mesh_write_raw(path, verts, tris, n_verts=None, n_tris=None):
+    """TRIANGLE_MESH raw stream from FP64 vertices and int32 triangles (host
+    arrays, or device addresses with explicit counts)."""
+    if not isinstance(verts, int):
+        verts = np.ascontiguousarray(verts, dtype=np.float64)
+        n_verts = len(verts.reshape(-1, 3))
+    if not isinstance(tris, int):
+        tris = np.ascontiguousarray(tris, dtype=np.int32)
+        n_tris = len(tris.reshape(-1, 3))
+    _io_check(load().qjg_mesh_write_raw(str(path).encode(), C.c_void_p(_addr(verts)), n_verts,
+                                        C.c_void_p(_addr(tris)), n_tris), "qjg_mesh_write_raw")
+
+
+def mesh_write_obj(path, verts, tris, n_verts=None, n_tris=None, fp32=None):
+    """OBJ as TRIANGLE_MESH::writeOBJ prints it.  Host arrays (float64 or
+    float32 vertices) or device addresses (fp32 says which) with counts."""
+    if not isinstance(verts, int):
+        fp32 = verts.dtype == np.float32
+        verts = np.ascontiguousarray(verts)
+        n_verts = len(verts.reshape(-1, 3))
+    if not isinstance(tris, int):
+        tris = np.ascontiguousarray(tris, dtype=np.int32)
+        n_tris = len(tris.reshape(-1, 3))
+    v64 = None if fp32 else _addr(verts)
+    v32 = _addr(verts) if fp32 else None
+    _io_check(load().qjg_mesh_write_obj(str(path).encode(), C.c_void_p(v64), C.c_void_p(v32),
+                                        n_verts, C.c_void_p(_addr(tris)), n_tris),
+              "qjg_mesh_write_obj")
 
 
 def set_field32_pairs(on):

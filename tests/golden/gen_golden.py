@@ -102,9 +102,33 @@ def main():
              wcenter=np.array(wg.center), wlengths=np.array(wg.lengths))
     np.savez_compressed(os.path.join(OUT, "tanh_grad.npz"), **d)
 
+    io_case(rd)
+
     print("stream: %d verts %d tris; nonlinear: %d/%d; linear: %d/%d" % (
         len(ms["verts"]), len(ms["tris"]), len(mn["verts"]), len(mn["tris"]), len(ml["verts"]),
         len(ml["tris"])))
+
+
+def io_inputs():
+    """A small field and mesh with values that exercise the number formats:
+    signed zeros, tiny and large magnitudes, values that round at the 16th
+    decimal."""
+    field = np.array([0.0, -0.0, 1.0, -1.0, 1e-300, -2.5e-17, 3.141592653589793, 1e10,
+                      -123456.7890123456, 0.1, 2.0 / 3.0, 7.0]).reshape(2, 2, 3)
+    res, center, lengths = (3, 2, 2), (0.25, -0.5, 1.0), (3.0, 2.0, 2.5)
+    verts = np.array([[0.0, -0.0, 1.0], [1e-17, -1e-17, 0.5], [0.1, 0.2, 0.3],
+                      [-1.2345678901234567, 98765.4321, 1.0 / 3.0], [2.5, -2.5, 1e-5],
+                      [0.9999999999999999, -0.30000000000000004, 4.440892098500626e-16]])
+    tris = np.array([[0, 1, 2], [2, 3, 4], [4, 5, 0], [1, 3, 5]], dtype=np.int32)
+    return field, res, center, lengths, verts, tris
+
+
+def io_case(rd):
+    """FIELD_3D::write, TRIANGLE_MESH::writeOBJ and TRIANGLE_MESH::write output
+    bytes of io_inputs()."""
+    field, res, center, lengths, verts, tris = io_inputs()
+    rd.field_write(os.path.join(OUT, "io_field.field3d"), res, center, lengths, field)
+    rd.mesh_write(verts, tris, os.path.join(OUT, "io_mesh.obj"), os.path.join(OUT, "io_mesh.raw"))
 
 
 def tanh_case():
