@@ -267,8 +267,12 @@ int qjg_fit_lbfgs(qjg_ctx* ctx, double* d_params, int32_t n_top, int32_t n_bot, 
  * reference runs one driver per job).  Requests are admitted as soon as a
  * worker slot is free and their device-memory estimate fits the HBM budget;
  * admitted requests run concurrently on their own streams, so work submitted
- * while others run overlaps with them.  Inputs are copied at submission;
- * output buffers (host) must stay valid until the request completes. */
+ * while others run overlaps with them.  Field requests in the precision form
+ * with integer exponents and at most 2^26 voxels are served by a batch
+ * worker instead: every such request waiting when it becomes free (up to 64
+ * and the batch arena) runs in one multi-request pass, replayed from a
+ * captured CUDA graph.  Inputs are copied at submission; output buffers
+ * (host) must stay valid until the request completes. */
 #define QJG_REQ_FIELD 0  /* field of a map on a grid (out_field: X*Y*Z doubles, optional) */
 #define QJG_REQ_MESH 1   /* streaming field + marching cubes (out_verts / out_tris optional) */
 #define QJG_REQ_ENERGY 2 /* squared-error energy + gradient (params/xyz/target; out_grad) */
@@ -303,6 +307,7 @@ typedef struct {
   double* out_verts;
   int32_t* out_tris;
   double* out_grad;
+  double rel_tol;     /* field / mesh in QJG_FP32_REFINE: as qjg_iter.rel_tol (0: band rule) */
 } qjg_request;
 
 typedef struct {
@@ -322,6 +327,10 @@ typedef struct {
   int64_t in_use_bytes;          /* device-memory estimate of the running requests */
   int64_t peak_in_use_bytes;
   int32_t peak_running;          /* most requests running at once */
+  int32_t pad_;
+  int64_t batched;               /* field requests served inside multi-request batches */
+  int64_t batches;               /* batch passes (one CUDA-graph replay each) */
+  int64_t max_batch;             /* most requests in one batch */
 } qjg_server_stats;
 
 int qjg_server_create(int device, int32_t workers, int64_t hbm_budget_bytes, qjg_server** out);

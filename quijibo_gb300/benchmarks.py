@@ -167,10 +167,27 @@ def bench_serve(args):
     lat = np.array([r["latency_ms"] for r in results])
     vox = sum(r["grid"].n_voxels for r in reqs if "grid" in r)
     out = {"requests": len(reqs), "scale": args.scale, "workers": args.workers,
+           "offered_req_s": len(reqs) / args.span,
            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
            "max_ms": float(lat.max()), "throughput_req_s": len(reqs) / span,
            "gvox_s": vox / span / 1e9, "span_s": span, "peak_running": st["peak_running"],
-           "failed": st["failed"]}
+           "failed": st["failed"], "batched": st["batched"], "batches": st["batches"],
+           "max_batch": st["max_batch"]}
+    # capacity: the same requests submitted at once
+    srv = lib.Server(workers=args.workers, hbm_budget=int(args.budget_gb * (1 << 30)))
+    srv.wait(srv.submit(**reqs[0]))
+    t0 = time.perf_counter()
+    tickets = [srv.submit(**r) for r in reqs]
+    results_b = [srv.wait(t) for t in tickets]
+    span_b = time.perf_counter() - t0
+    st_b = srv.stats()
+    srv.close()
+    lat_b = np.array([r["latency_ms"] for r in results_b])
+    out["burst"] = {"throughput_req_s": len(reqs) / span_b, "gvox_s": vox / span_b / 1e9,
+                    "span_s": span_b, "p50_ms": float(np.percentile(lat_b, 50)),
+                    "p99_ms": float(np.percentile(lat_b, 99)), "peak_running": st_b["peak_running"],
+                    "batched": st_b["batched"], "batches": st_b["batches"],
+                    "max_batch": st_b["max_batch"], "failed": st_b["failed"]}
     # baseline: a sample of the same requests, plain FP64, one at a time
     ctx = lib.Context(0)
     idx = list(range(0, len(reqs), max(1, len(reqs) // args.baseline_sample)))

@@ -222,13 +222,6 @@ __device__ __forceinline__ void warp_append(bool a, uint32_t ia, int na, bool b,
   }
 }
 
-// Lists a bulk pass fills (device pointers; keys and ff may be null).
-struct RefineLists {
-  uint32_t* list;  // voxels for the FP64 re-evaluation (length in DevStats::refined)
-  uint8_t* keys;   // their FP32 orbit lengths, the sort key of the FP64 pass
-  uint32_t* ff;    // voxels for the double-float re-run (length in DevStats::rerun)
-};
-
 // One voxel per lane: the form the mesher's bisection shares (escape32).
 template <bool DE>
 __global__ void __launch_bounds__(128) field32_kernel(const __grid_constant__ MapParams m,
@@ -283,61 +276,81 @@ __global__ void __launch_bounds__(128) field32_kernel(const __grid_constant__ Ma
 // unobserved (its state is frozen in its Orbit32).
 static constexpr int TILE2_X = 16;
 
+// Per-warp tallies of a bulk pass.
+struct BulkAcc {
+  unsigned long long iters = 0, nonfinite = 0, lane_iters = 0;
+};
+
+// One 16 x 4 tile (tile index t of the launch's z-range) of the two-voxel
+// bulk pass; list entries are `tag | local voxel index`.  Returns the
+// executed map applications of the warp's voxels (summed over the warp).
+template <bool DE>
+__device__ __forceinline__ unsigned long long tile2(const MapParams& m, const GridParams& g,
+                                                    const IterParams& it, long long t,
+                                                    double* __restrict__ field,
+                                                    float* __restrict__ de, const RefineLists& rl,
+                                                    int refine, bool allow_ff, uint32_t tag,
+                                                    DevStats* st, BulkAcc& acc) {
+  using namespace q32x2;
+  const TileMap tm = tile_map(g, TILE2_X);
+  const int lane = threadIdx.x & 31;
+  const float esc2 = (float)(it.escape * it.escape);
+  const float l2band = log2f((float)it.band);
+  const int zl = (int)(t / tm.per_slice);
+  const long long r = t - (long long)zl * tm.per_slice;
+  const int x = (int)(r % tm.tx_n) * TILE2_X + 2 * (lane & 7);
+  const int y = (int)(r / tm.tx_n) * TILE_Y + (lane >> 3);
+  const bool va = (x < g.X && y < g.Y), vb = (x + 1 < g.X && y < g.Y);
+  double pa[3], pb[3];
+  cell_center(g, x, y, g.z0 + zl, pa);
+  cell_center(g, x + 1, y, g.z0 + zl, pb);
+  Q2 q = {make_float2((float)pa[0], (float)pb[0]), make_float2((float)pa[1], (float)pb[1]),
+          make_float2((float)pa[2], (float)pb[2]), pair((float)g.slice)};
+  const float2 m20 = norm2(q);
+  Orbit32 a = orbit_start(va, m20.x, esc2, it.max_it);
+  Orbit32 b = orbit_start(vb, m20.y, esc2, it.max_it);
+  while (a.live || b.live) {
+    float2 gg = pair(0.f);
+    q = apply32x2<DE>(m, q, &gg);
+    const float2 m2 = norm2(q);
+    orbit_step<DE>(a, m2.x, gg.x, esc2, it.max_it);
+    orbit_step<DE>(b, m2.y, gg.y, esc2, it.max_it);
+  }
+  acc.iters += a.n + b.n;
+  const long long i = ((long long)zl * g.Y + y) * g.X + x;
+  const int ra = va ? orbit_finish<DE>(a, it, esc2, l2band, refine, allow_ff, i, field, de,
+                                       acc.nonfinite)
+                    : WRITTEN;
+  const int rb = vb ? orbit_finish<DE>(b, it, esc2, l2band, refine, allow_ff, i + 1, field, de,
+                                       acc.nonfinite)
+                    : WRITTEN;
+  // voxel slots the warp spent: 64 x its longest orbit
+  const unsigned wmax = __reduce_max_sync(0xffffffffu, (unsigned)max(a.n, b.n));
+  if (lane == 0) acc.lane_iters += 64ull * wmax;
+  warp_append(ra == TO_FP64, tag | (uint32_t)i, a.n, rb == TO_FP64, tag | (uint32_t)(i + 1), b.n,
+              &st->refined, rl.list, rl.keys);
+  warp_append(ra == TO_FF, tag | (uint32_t)i, 0, rb == TO_FF, tag | (uint32_t)(i + 1), 0,
+              &st->rerun, rl.ff, nullptr);
+  return __reduce_add_sync(0xffffffffu, (unsigned)(a.n + b.n));
+}
+
 template <bool DE>
 __global__ void __launch_bounds__(128) field32x2_kernel(const __grid_constant__ MapParams m,
                                                         const GridParams g, const IterParams it,
                                                         double* __restrict__ field,
                                                         float* __restrict__ de, RefineLists rl,
                                                         int refine, DevStats* st) {
-  using namespace q32x2;
   const TileMap tm = tile_map(g, TILE2_X);
-  const int lane = threadIdx.x & 31;
-  const float esc2 = (float)(it.escape * it.escape);
-  const float l2band = log2f((float)it.band);
   const bool allow_ff = rl.ff != nullptr;
-  unsigned long long iters_acc = 0, nonfinite_acc = 0, lane_iters_acc = 0;
+  BulkAcc acc;
   for (;;) {
     const long long t = next_tile(&st->tiles_done);
     if (t >= tm.total) break;
-    const int zl = (int)(t / tm.per_slice);
-    const long long r = t - (long long)zl * tm.per_slice;
-    const int x = (int)(r % tm.tx_n) * TILE2_X + 2 * (lane & 7);
-    const int y = (int)(r / tm.tx_n) * TILE_Y + (lane >> 3);
-    const bool va = (x < g.X && y < g.Y), vb = (x + 1 < g.X && y < g.Y);
-    double pa[3], pb[3];
-    cell_center(g, x, y, g.z0 + zl, pa);
-    cell_center(g, x + 1, y, g.z0 + zl, pb);
-    Q2 q = {make_float2((float)pa[0], (float)pb[0]), make_float2((float)pa[1], (float)pb[1]),
-            make_float2((float)pa[2], (float)pb[2]), pair((float)g.slice)};
-    const float2 m20 = norm2(q);
-    Orbit32 a = orbit_start(va, m20.x, esc2, it.max_it);
-    Orbit32 b = orbit_start(vb, m20.y, esc2, it.max_it);
-    while (a.live || b.live) {
-      float2 gg = pair(0.f);
-      q = apply32x2<DE>(m, q, &gg);
-      const float2 m2 = norm2(q);
-      orbit_step<DE>(a, m2.x, gg.x, esc2, it.max_it);
-      orbit_step<DE>(b, m2.y, gg.y, esc2, it.max_it);
-    }
-    iters_acc += a.n + b.n;
-    const long long i = ((long long)zl * g.Y + y) * g.X + x;
-    const int ra = va ? orbit_finish<DE>(a, it, esc2, l2band, refine, allow_ff, i, field, de,
-                                         nonfinite_acc)
-                      : WRITTEN;
-    const int rb = vb ? orbit_finish<DE>(b, it, esc2, l2band, refine, allow_ff, i + 1, field, de,
-                                         nonfinite_acc)
-                      : WRITTEN;
-    // voxel slots the warp spent: 64 x its longest orbit
-    const unsigned wmax = __reduce_max_sync(0xffffffffu, (unsigned)max(a.n, b.n));
-    if (lane == 0) lane_iters_acc += 64ull * wmax;
-    warp_append(ra == TO_FP64, (uint32_t)i, a.n, rb == TO_FP64, (uint32_t)(i + 1), b.n,
-                &st->refined, rl.list, rl.keys);
-    warp_append(ra == TO_FF, (uint32_t)i, 0, rb == TO_FF, (uint32_t)(i + 1), 0, &st->rerun,
-                rl.ff, nullptr);
+    tile2<DE>(m, g, it, t, field, de, rl, refine, allow_ff, 0u, st, acc);
   }
-  warp_add(&st->voxel_iters, iters_acc);
-  warp_add(&st->nonfinite, nonfinite_acc);
-  warp_add(&st->aux[3], lane_iters_acc);
+  warp_add(&st->voxel_iters, acc.iters);
+  warp_add(&st->nonfinite, acc.nonfinite);
+  warp_add(&st->aux[3], acc.lane_iters);
 }
 
 // The double-float re-run of the listed voxels: it.ff_head map applications
@@ -345,6 +358,38 @@ __global__ void __launch_bounds__(128) field32x2_kernel(const __grid_constant__ 
 // error restarts at the rounding of the head's result to FP32, so voxels
 // whose error came from the first iterations now pass; the others (and the
 // band, escape-radius and overflow cases) go to the FP64 list.
+// One re-run voxel (local index i); returns its route (WRITTEN or TO_FP64)
+// and leaves its orbit in *o.
+__device__ __forceinline__ int rerun_voxel(const MapParams& m, const GridParams& g,
+                                           const IterParams& it, uint32_t i,
+                                           double* __restrict__ field, float* __restrict__ de,
+                                           Orbit32* o, unsigned long long& nonfinite_acc) {
+  const float esc2 = (float)(it.escape * it.escape);
+  const int x = (int)(i % (uint32_t)g.X);
+  const int y = (int)((i / (uint32_t)g.X) % (uint32_t)g.Y);
+  const int zl = (int)(i / ((uint32_t)g.X * (uint32_t)g.Y));
+  double p[3];
+  cell_center(g, x, y, g.z0 + zl, p);
+  qff::Q q = {qff::from_double(p[0]), qff::from_double(p[1]), qff::from_double(p[2]),
+              qff::from_double(g.slice)};
+  *o = orbit_start(true, qff::norm2(q).hi, esc2, it.max_it);
+  for (int h = 0; h < it.ff_head && o->live; h++) {
+    float gg = 0.f;
+    q = apply_ff<true>(m, q, &gg);
+    o->err = q32::EPS32;  // double-float iterates: only their FP32 rounding counts
+    orbit_step<true>(*o, qff::norm2(q).hi, gg, esc2, it.max_it);
+  }
+  o->err = q32::EPS32;
+  q32::Q qf = qff::hi(q);
+  while (o->live) {
+    float gg = 0.f;
+    qf = apply32<true>(m, qf, &gg);
+    orbit_step<true>(*o, q32::norm2(qf), gg, esc2, it.max_it);
+  }
+  return orbit_finish<true>(*o, it, esc2, log2f((float)it.band), 1, false, i, field, de,
+                            nonfinite_acc);
+}
+
 __global__ void __launch_bounds__(128) rerun_ff_kernel(const __grid_constant__ MapParams m,
                                                        const GridParams g, const IterParams it,
                                                        const uint32_t* __restrict__ ff_list,
@@ -352,8 +397,6 @@ __global__ void __launch_bounds__(128) rerun_ff_kernel(const __grid_constant__ M
                                                        float* __restrict__ de, uint32_t* list,
                                                        uint8_t* keys, DevStats* st) {
   const unsigned long long n_list = st->rerun;
-  const float esc2 = (float)(it.escape * it.escape);
-  const float l2band = log2f((float)it.band);
   const int lane = threadIdx.x & 31;
   const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
   unsigned long long iters_acc = 0, nonfinite_acc = 0;
@@ -361,40 +404,124 @@ __global__ void __launch_bounds__(128) rerun_ff_kernel(const __grid_constant__ M
   for (unsigned long long base = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) & ~31ull;
        base < n_list; base += stride) {
     const unsigned long long k = base + lane;
-    const bool valid = k < n_list;
     uint32_t i = 0;
     int route = WRITTEN;
-    Orbit32 o = orbit_start(false, 0.f, esc2, it.max_it);
-    if (valid) {
+    Orbit32 o = orbit_start(false, 0.f, 0.f, 0);
+    if (k < n_list) {
       i = ff_list[k];
-      const int x = (int)(i % (uint32_t)g.X);
-      const int y = (int)((i / (uint32_t)g.X) % (uint32_t)g.Y);
-      const int zl = (int)(i / ((uint32_t)g.X * (uint32_t)g.Y));
-      double p[3];
-      cell_center(g, x, y, g.z0 + zl, p);
-      qff::Q q = {qff::from_double(p[0]), qff::from_double(p[1]), qff::from_double(p[2]),
-                  qff::from_double(g.slice)};
-      o = orbit_start(true, qff::norm2(q).hi, esc2, it.max_it);
-      for (int h = 0; h < it.ff_head && o.live; h++) {
-        float gg = 0.f;
-        q = apply_ff<true>(m, q, &gg);
-        o.err = q32::EPS32;  // double-float iterates: only their FP32 rounding counts
-        orbit_step<true>(o, qff::norm2(q).hi, gg, esc2, it.max_it);
-      }
-      o.err = q32::EPS32;
-      q32::Q qf = qff::hi(q);
-      while (o.live) {
-        float gg = 0.f;
-        qf = apply32<true>(m, qf, &gg);
-        orbit_step<true>(o, q32::norm2(qf), gg, esc2, it.max_it);
-      }
+      route = rerun_voxel(m, g, it, i, field, de, &o, nonfinite_acc);
       iters_acc += o.n;
-      route = orbit_finish<true>(o, it, esc2, l2band, 1, false, i, field, de, nonfinite_acc);
     }
     warp_append(route == TO_FP64, i, o.n, false, 0, 0, &st->refined, list, keys);
   }
   warp_add(&st->rerun_iters, iters_acc);
   warp_add(&st->nonfinite, nonfinite_acc);
+}
+
+// ------------------------------------------------------------- batches
+// Several field requests (different grids and maps) in one pass: the tiles
+// of all items form one work queue, list entries carry the item in their top
+// bits (BATCH_SHIFT), and each kernel reads the item's map and grid from the
+// batch table in global memory.  Per voxel, the arithmetic is that of the
+// single-request kernels, so each item's field has the same bits as its own
+// qjg_field call.
+
+// the item owning tile t (largest k with tile0[k] <= t)
+__device__ __forceinline__ int batch_item(const long long* tile0, int n, long long t) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tile0[mid] <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <bool DE>
+__global__ void __launch_bounds__(128) field32x2_batch_kernel(const BatchTable* __restrict__ tab,
+                                                              const MapParams* __restrict__ maps,
+                                                              RefineLists rl,
+                                                              BatchCounts* __restrict__ counts,
+                                                              DevStats* st) {
+  __shared__ long long tile0[BATCH_MAX];
+  const int n = tab->n;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) tile0[k] = tab->items[k].tile0;
+  __syncthreads();
+  const long long total = tab->total_tiles;
+  BulkAcc acc;
+  for (;;) {
+    const long long t = next_tile(&st->tiles_done);
+    if (t >= total) break;
+    const int k = batch_item(tile0, n, t);
+    const BatchItem& b = tab->items[k];
+    const MapParams& m = maps[k];
+    const bool allow_ff = rl.ff != nullptr && b.refine && m.all_int && b.it.est_tol > 0.0;
+    const unsigned long long it_sum =
+        tile2<DE>(m, b.g, b.it, t - tile0[k], b.field, b.de, rl, b.refine, allow_ff,
+                  (uint32_t)k << BATCH_SHIFT, st, acc);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&counts[k].voxel_iters, it_sum);
+  }
+  warp_add(&st->voxel_iters, acc.iters);
+  warp_add(&st->nonfinite, acc.nonfinite);
+  warp_add(&st->aux[3], acc.lane_iters);
+}
+
+__global__ void __launch_bounds__(128) rerun_ff_batch_kernel(const BatchTable* __restrict__ tab,
+                                                             const MapParams* __restrict__ maps,
+                                                             const uint32_t* __restrict__ ff_list,
+                                                             uint32_t* list, uint8_t* keys,
+                                                             DevStats* st) {
+  const unsigned long long n_list = st->rerun;
+  const int lane = threadIdx.x & 31;
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  unsigned long long iters_acc = 0, nonfinite_acc = 0;
+  for (unsigned long long base = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) & ~31ull;
+       base < n_list; base += stride) {
+    const unsigned long long j = base + lane;
+    uint32_t e = 0;
+    int route = WRITTEN;
+    Orbit32 o = orbit_start(false, 0.f, 0.f, 0);
+    if (j < n_list) {
+      e = ff_list[j];
+      const int k = (int)(e >> BATCH_SHIFT);
+      const BatchItem& b = tab->items[k];
+      route = rerun_voxel(maps[k], b.g, b.it, e & BATCH_MASK, b.field, b.de, &o, nonfinite_acc);
+      iters_acc += o.n;
+    }
+    warp_append(route == TO_FP64, e, o.n, false, 0, 0, &st->refined, list, keys);
+  }
+  warp_add(&st->rerun_iters, iters_acc);
+  warp_add(&st->nonfinite, nonfinite_acc);
+}
+
+// FP64 re-evaluation of batch entries (integer exponents by products: the
+// batch admits only maps whose effective exponents are integers).
+__global__ void __launch_bounds__(128) refine64_batch_kernel(const BatchTable* __restrict__ tab,
+                                                             const MapParams* __restrict__ maps,
+                                                             const uint32_t* list,
+                                                             DevStats* st) {
+  const unsigned long long n_list = st->refined;
+  unsigned long long iters_acc = 0;
+  for (unsigned long long j = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; j < n_list;
+       j += (unsigned long long)gridDim.x * blockDim.x) {
+    const uint32_t e = list[j];
+    const int k = (int)(e >> BATCH_SHIFT);
+    const uint32_t i = e & BATCH_MASK;
+    const BatchItem& b = tab->items[k];
+    const GridParams& g = b.g;
+    const int x = (int)(i % (uint32_t)g.X);
+    const int y = (int)((i / (uint32_t)g.X) % (uint32_t)g.Y);
+    const int zl = (int)(i / ((uint32_t)g.X * (uint32_t)g.Y));
+    double p[3];
+    cell_center(g, x, y, g.z0 + zl, p);
+    int n;
+    double d = 0.0;
+    const double f = escape64<false, true>(maps[k], b.it, p, g.slice, &n, &d);
+    b.field[i] = f;
+    if (b.de) b.de[i] = (float)d;
+    iters_acc += n;
+  }
+  warp_add(&st->aux[0], iters_acc);
 }
 
 // ------------------------------------------------------------- launchers
@@ -558,6 +685,34 @@ cudaError_t launch_refine64(const MapParams& m, const GridParams& g, const IterP
     refine64_kernel<true><<<blocks, 128, 0, s>>>(m, g, it, list, st, field, de, st);
   else
     refine64_kernel<false><<<blocks, 128, 0, s>>>(m, g, it, list, st, field, de, st);
+  return cudaGetLastError();
+}
+
+BatchShapes batch_shapes() {
+  BatchShapes sh;
+  sh.bulk = grid_blocks((const void*)field32x2_batch_kernel<true>, 128);
+  sh.rerun = grid_blocks((const void*)rerun_ff_batch_kernel, 128);
+  sh.sort = 2 * sm_count();
+  sh.refine = grid_blocks((const void*)refine64_batch_kernel, 128);
+  return sh;
+}
+
+long long batch_item_tiles(int X, int Y, int Z) {
+  return (long long)((X + TILE2_X - 1) / TILE2_X) * ((Y + TILE_Y - 1) / TILE_Y) * Z;
+}
+
+cudaError_t launch_field_batch(const BatchBuffers& b, const BatchShapes& sh, cudaStream_t s) {
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(b.st, 0, sizeof(DevStats), s))) return e;
+  if ((e = cudaMemsetAsync(b.counts, 0, BATCH_MAX * sizeof(BatchCounts), s))) return e;
+  field32x2_batch_kernel<true><<<sh.bulk, 128, 0, s>>>(b.tab, b.maps, b.rl, b.counts, b.st);
+  rerun_ff_batch_kernel<<<sh.rerun, 128, 0, s>>>(b.tab, b.maps, b.rl.ff, b.rl.list, b.rl.keys,
+                                                 b.st);
+  if ((e = cudaMemsetAsync(b.hist, 0, REFINE_KEYS * sizeof(unsigned), s))) return e;
+  refine_hist_kernel<<<sh.sort, 256, 0, s>>>(b.rl.keys, b.st, b.hist);
+  refine_offsets_kernel<<<1, REFINE_KEYS, 0, s>>>(b.hist);
+  refine_scatter_kernel<<<sh.sort, 256, 0, s>>>(b.rl.list, b.rl.keys, b.st, b.hist, b.sorted);
+  refine64_batch_kernel<<<sh.refine, 128, 0, s>>>(b.tab, b.maps, b.sorted, b.st);
   return cudaGetLastError();
 }
 

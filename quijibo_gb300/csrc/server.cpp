@@ -8,8 +8,12 @@
 // around a large one without starving it for long).  Each worker owns a
 // context (private scratch) and a stream, so admitted requests run
 // concurrently on the device; a request admitted while others run overlaps
-// with them.  Results are copied to caller buffers; latencies are measured
-// from submission to completion on the host clock.
+// with them.  Small field requests in the precision form go to a batch
+// worker: all that wait when it frees up run as one multi-request pass (one
+// tile queue over every item, field.cu's batch kernels), replayed from a
+// CUDA graph captured on the first batch, with the batch table rewritten in
+// place each time.  Results are copied to caller buffers; latencies are
+// measured from submission to completion on the host clock.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -26,6 +30,7 @@
 
 #include "../../include/quijibo_gpu.h"
 #include "qj_ctx.h"
+#include "qj_kernels.h"
 
 namespace {
 
@@ -37,8 +42,77 @@ struct Job {
   // owned copies of the inputs
   std::vector<double> top_roots, top_powers, bot_roots, bot_powers, xyz, target, params;
   int64_t est_bytes = 0;
+  int64_t voxels = 0;
+  bool batchable = false;
   Clock::time_point t_submit, t_admit, t_done;
   qjg_result res;
+};
+
+// Device and pinned host buffers of the batch worker, and its graph.
+struct FieldBatcher {
+  int64_t cap = 0;  // voxels per batch (sum over items)
+  cudaStream_t s = nullptr;
+  qj::BatchTable* d_tab = nullptr;
+  qj::MapParams* d_maps = nullptr;
+  double* d_arena = nullptr;
+  uint32_t *d_list = nullptr, *d_sorted = nullptr, *d_ff = nullptr;
+  uint8_t* d_keys = nullptr;
+  unsigned* d_hist = nullptr;
+  qj::BatchCounts* d_counts = nullptr;
+  qj::DevStats* d_st = nullptr;
+  qj::BatchTable* h_tab = nullptr;
+  qj::MapParams* h_maps = nullptr;
+  qj::BatchCounts* h_counts = nullptr;
+  qj::BatchShapes sh{};
+  cudaGraphExec_t exec = nullptr;
+  bool ok = false;
+
+  int init(int64_t voxels) {
+    cap = voxels;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return QJG_ERR_CUDA;
+    const size_t n = (size_t)cap;
+    if (cudaMalloc((void**)&d_tab, sizeof(qj::BatchTable)) ||
+        cudaMalloc((void**)&d_maps, qj::BATCH_MAX * sizeof(qj::MapParams)) ||
+        cudaMalloc((void**)&d_arena, n * sizeof(double)) ||
+        cudaMalloc((void**)&d_list, n * sizeof(uint32_t)) ||
+        cudaMalloc((void**)&d_sorted, n * sizeof(uint32_t)) ||
+        cudaMalloc((void**)&d_ff, n * sizeof(uint32_t)) || cudaMalloc((void**)&d_keys, n) ||
+        cudaMalloc((void**)&d_hist, qj::REFINE_KEYS * sizeof(unsigned)) ||
+        cudaMalloc((void**)&d_counts, qj::BATCH_MAX * sizeof(qj::BatchCounts)) ||
+        cudaMalloc((void**)&d_st, sizeof(qj::DevStats)) ||
+        cudaMallocHost((void**)&h_tab, sizeof(qj::BatchTable)) ||
+        cudaMallocHost((void**)&h_maps, qj::BATCH_MAX * sizeof(qj::MapParams)) ||
+        cudaMallocHost((void**)&h_counts, qj::BATCH_MAX * sizeof(qj::BatchCounts)))
+      return QJG_ERR_NOMEM;
+    sh = qj::batch_shapes();
+    ok = true;
+    return QJG_OK;
+  }
+
+  ~FieldBatcher() {
+    if (exec) cudaGraphExecDestroy(exec);
+    for (void* p : {(void*)d_tab, (void*)d_maps, (void*)d_arena, (void*)d_list, (void*)d_sorted,
+                    (void*)d_ff, (void*)d_keys, (void*)d_hist, (void*)d_counts, (void*)d_st})
+      if (p) cudaFree(p);
+    for (void* p : {(void*)h_tab, (void*)h_maps, (void*)h_counts})
+      if (p) cudaFreeHost(p);
+    if (s) cudaStreamDestroy(s);
+  }
+
+  qj::BatchBuffers buffers() const {
+    qj::BatchBuffers b;
+    b.tab = d_tab;
+    b.maps = d_maps;
+    b.rl = {d_list, d_keys, d_ff};
+    b.sorted = d_sorted;
+    b.hist = d_hist;
+    b.counts = d_counts;
+    b.st = d_st;
+    return b;
+  }
+
+  // One pass over `jobs` (each batchable; their voxels sum to <= cap).
+  int run(std::vector<std::shared_ptr<Job>>& jobs);
 };
 
 int64_t estimate_bytes(const qjg_request& r) {
@@ -81,6 +155,14 @@ struct qjg_server {
   Clock::time_point t_first, t_last;
   bool any = false;
 
+  // batch worker
+  std::unique_ptr<FieldBatcher> batcher;
+  int64_t batch_cap = 0;  // 0: no batch worker
+  bool batch_idle = false;
+  std::vector<std::shared_ptr<Job>> batch_q;
+  std::condition_variable batch_cv;
+  int64_t batched = 0, batches = 0, max_batch = 0;
+
   explicit qjg_server(int workers) : idle(workers, 0), worker_q(workers), worker_cv(workers) {}
 };
 
@@ -104,6 +186,7 @@ void run_job(qjg_ctx* ctx, cudaStream_t s, Job& j) {
   it.escape = r.escape;
   it.band_h = 2.0;
   it.field_tol = 1e-3;
+  it.rel_tol = r.precision == QJG_FP32_REFINE ? r.rel_tol : 0.0;
   if (rc == QJG_OK && r.kind == QJG_REQ_FIELD) {
     const int64_t vox = (int64_t)r.grid.res[0] * r.grid.res[1] * r.grid.res[2];
     double* d_field = nullptr;
@@ -174,6 +257,26 @@ void run_job(qjg_ctx* ctx, cudaStream_t s, Job& j) {
   out.error = rc;
 }
 
+// Completion bookkeeping of one job (srv->mu held).
+void finish_job(qjg_server* srv, Job& j, Clock::time_point now) {
+  j.t_done = now;
+  j.res.status = j.res.error == QJG_OK ? QJG_STATUS_DONE : QJG_STATUS_FAILED;
+  j.res.latency_ms = std::chrono::duration<double, std::milli>(j.t_done - j.t_submit).count();
+  j.res.queue_ms = std::chrono::duration<double, std::milli>(j.t_admit - j.t_submit).count();
+  j.res.run_ms = std::chrono::duration<double, std::milli>(j.t_done - j.t_admit).count();
+  srv->in_use -= j.est_bytes;
+  srv->running--;
+  j.res.t_admit_ms = std::chrono::duration<double, std::milli>(j.t_admit - srv->t_created).count();
+  j.res.t_done_ms = std::chrono::duration<double, std::milli>(j.t_done - srv->t_created).count();
+  if (j.res.error == QJG_OK) {
+    srv->completed++;
+    srv->latencies_ms.push_back(j.res.latency_ms);
+  } else {
+    srv->failed++;
+  }
+  srv->t_last = j.t_done;
+}
+
 void worker_main(qjg_server* srv, int w) {
   qjg_ctx* ctx = nullptr;
   cudaSetDevice(srv->device);
@@ -199,22 +302,7 @@ void worker_main(qjg_server* srv, int w) {
       run_job(ctx, s, *j);
     {
       std::lock_guard<std::mutex> lk(srv->mu);
-      j->t_done = Clock::now();
-      j->res.status = j->res.error == QJG_OK ? QJG_STATUS_DONE : QJG_STATUS_FAILED;
-      j->res.latency_ms = std::chrono::duration<double, std::milli>(j->t_done - j->t_submit).count();
-      j->res.queue_ms = std::chrono::duration<double, std::milli>(j->t_admit - j->t_submit).count();
-      j->res.run_ms = std::chrono::duration<double, std::milli>(j->t_done - j->t_admit).count();
-      srv->in_use -= j->est_bytes;
-      srv->running--;
-      j->res.t_admit_ms = std::chrono::duration<double, std::milli>(j->t_admit - srv->t_created).count();
-      j->res.t_done_ms = std::chrono::duration<double, std::milli>(j->t_done - srv->t_created).count();
-      if (j->res.error == QJG_OK) {
-        srv->completed++;
-        srv->latencies_ms.push_back(j->res.latency_ms);
-      } else {
-        srv->failed++;
-      }
-      srv->t_last = j->t_done;
+      finish_job(srv, *j, Clock::now());
       srv->cv_done.notify_all();
       srv->cv_dispatch.notify_one();
     }
@@ -223,13 +311,136 @@ void worker_main(qjg_server* srv, int w) {
   if (ctx) qjg_destroy(ctx);
 }
 
+int FieldBatcher::run(std::vector<std::shared_ptr<Job>>& jobs) {
+  const int n = (int)jobs.size();
+  int64_t off = 0, tiles = 0;
+  h_tab->n = n;
+  for (int k = 0; k < n; k++) {
+    const qjg_request& r = jobs[k]->req;
+    const Job& j = *jobs[k];
+    if (qj_fill_map(&h_maps[k], r.n_top, j.top_roots.data(), j.top_powers.data(), r.sigma_top,
+                    r.n_bot, j.bot_roots.empty() ? nullptr : j.bot_roots.data(),
+                    j.bot_powers.empty() ? nullptr : j.bot_powers.data(), r.sigma_bot,
+                    r.scale) >= 0)
+      return QJG_ERR_ARG;
+    qjg_iter it = {};
+    it.max_it = r.max_it;
+    it.precision = r.precision;
+    it.refine_pow = QJG_REFINE_INT;
+    it.want_de = 1;
+    it.escape = r.escape;
+    it.band_h = 2.0;
+    it.field_tol = 1e-3;
+    it.rel_tol = r.precision == QJG_FP32_REFINE ? r.rel_tol : 0.0;
+    qj::BatchItem& b = h_tab->items[k];
+    b.g = qj_grid_params(&r.grid, 0, r.grid.res[2]);
+    b.it = qj_iter_params(&it, &r.grid);
+    b.field = d_arena + off;
+    b.de = nullptr;
+    b.tile0 = tiles;
+    b.refine = r.precision == QJG_FP32_REFINE ? 1 : 0;
+    b.pad_ = 0;
+    off += j.voxels;
+    tiles += qj::batch_item_tiles(r.grid.res[0], r.grid.res[1], r.grid.res[2]);
+  }
+  h_tab->total_tiles = tiles;
+  if (cudaMemcpyAsync(d_maps, h_maps, (size_t)n * sizeof(qj::MapParams), cudaMemcpyHostToDevice,
+                      s) ||
+      cudaMemcpyAsync(d_tab, h_tab, sizeof(qj::BatchTable), cudaMemcpyHostToDevice, s))
+    return QJG_ERR_CUDA;
+  if (!exec) {
+    // the pass reads the table from d_tab and every count from the device,
+    // so one capture serves every batch
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) return QJG_ERR_CUDA;
+    const cudaError_t le = qj::launch_field_batch(buffers(), sh, s);
+    const cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    if (le || ce || !graph) return QJG_ERR_CUDA;
+    const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie) {
+      exec = nullptr;
+      return QJG_ERR_CUDA;
+    }
+  }
+  if (cudaGraphLaunch(exec, s)) return QJG_ERR_CUDA;
+  if (cudaMemcpyAsync(h_counts, d_counts, (size_t)n * sizeof(qj::BatchCounts),
+                      cudaMemcpyDeviceToHost, s))
+    return QJG_ERR_CUDA;
+  off = 0;
+  for (int k = 0; k < n; k++) {
+    Job& j = *jobs[k];
+    if (j.req.out_field &&
+        cudaMemcpyAsync(j.req.out_field, d_arena + off, (size_t)j.voxels * sizeof(double),
+                        cudaMemcpyDeviceToHost, s))
+      return QJG_ERR_CUDA;
+    off += j.voxels;
+  }
+  if (cudaStreamSynchronize(s)) return QJG_ERR_CUDA;
+  for (int k = 0; k < n; k++) jobs[k]->res.voxel_iters = (int64_t)h_counts[k].voxel_iters;
+  return QJG_OK;
+}
+
+void batch_main(qjg_server* srv) {
+  cudaSetDevice(srv->device);
+  for (;;) {
+    std::vector<std::shared_ptr<Job>> jobs;
+    {
+      std::unique_lock<std::mutex> lk(srv->mu);
+      srv->batch_idle = true;
+      srv->cv_dispatch.notify_one();
+      srv->batch_cv.wait(lk, [&] { return srv->stop || !srv->batch_q.empty(); });
+      srv->batch_idle = false;
+      if (srv->batch_q.empty()) break;  // stopping
+      jobs.swap(srv->batch_q);
+      for (auto& j : jobs) j->res.status = QJG_STATUS_RUNNING;
+    }
+    const int rc = srv->batcher->run(jobs);
+    {
+      std::lock_guard<std::mutex> lk(srv->mu);
+      const Clock::time_point now = Clock::now();
+      srv->batches++;
+      srv->batched += (int64_t)jobs.size();
+      srv->max_batch = std::max<int64_t>(srv->max_batch, (int64_t)jobs.size());
+      for (auto& j : jobs) {
+        j->res.error = rc;
+        finish_job(srv, *j, now);
+      }
+      srv->cv_done.notify_all();
+      srv->cv_dispatch.notify_one();
+    }
+  }
+}
+
 void dispatcher_main(qjg_server* srv) {
   std::unique_lock<std::mutex> lk(srv->mu);
   const int nw = (int)srv->worker_q.size();
   for (;;) {
+    bool admitted = false;
+    // the batch worker takes every batchable request waiting when it is free
+    if (srv->batcher && srv->batch_idle && srv->batch_q.empty()) {
+      int64_t vox = 0;
+      for (size_t i = 0; i < srv->waiting.size() && (int)srv->batch_q.size() < qj::BATCH_MAX;) {
+        auto job = srv->waiting[i];
+        if (!job->batchable || vox + job->voxels > srv->batch_cap) {
+          i++;
+          continue;
+        }
+        srv->waiting.erase(srv->waiting.begin() + (long)i);
+        vox += job->voxels;
+        job->t_admit = Clock::now();
+        srv->batch_q.push_back(job);
+        srv->running++;
+      }
+      if (!srv->batch_q.empty()) {
+        srv->peak_running = std::max(srv->peak_running, srv->running);
+        srv->batch_idle = false;
+        srv->batch_cv.notify_one();
+        admitted = true;
+      }
+    }
     // admit while a worker is idle and the head (or a request within the
     // lookahead window) fits the budget
-    bool admitted = false;
     int w = -1;
     for (int k = 0; k < nw; k++)
       if (srv->idle[k] && srv->worker_q[k].empty()) {
@@ -237,12 +448,14 @@ void dispatcher_main(qjg_server* srv) {
         break;
       }
     if (w >= 0 && !srv->waiting.empty()) {
-      const int look = std::min<int>(srv->lookahead, (int)srv->waiting.size());
-      for (int i = 0; i < look; i++) {
+      int seen = 0;
+      for (size_t i = 0; i < srv->waiting.size() && seen < srv->lookahead; i++) {
         auto job = srv->waiting[i];
+        if (job->batchable && srv->batcher) continue;  // the batch worker's
+        seen++;
         // a request larger than the whole budget runs alone
         if (srv->in_use + job->est_bytes <= srv->budget || srv->in_use == 0) {
-          srv->waiting.erase(srv->waiting.begin() + i);
+          srv->waiting.erase(srv->waiting.begin() + (long)i);
           srv->in_use += job->est_bytes;
           srv->peak_in_use = std::max(srv->peak_in_use, srv->in_use);
           srv->running++;
@@ -272,7 +485,23 @@ int qjg_server_create(int device, int32_t workers, int64_t hbm_budget_bytes, qjg
   qjg_server* srv = new qjg_server(workers);
   srv->device = device;
   srv->budget = hbm_budget_bytes;
+  // the batch worker's arena (FP64 outputs, lists; ~21 B per voxel) is set
+  // aside from the budget when the budget holds at least four times it
+  const int64_t cap = 1ll << 25;
+  const int64_t arena = cap * 21 + (int64_t)qj::BATCH_MAX * (int64_t)sizeof(qj::MapParams);
+  if (hbm_budget_bytes >= 4 * arena) {
+    cudaSetDevice(device);
+    std::unique_ptr<FieldBatcher> fb(new FieldBatcher());
+    if (fb->init(cap) == QJG_OK) {
+      srv->batcher = std::move(fb);
+      srv->batch_cap = cap;
+      srv->budget -= arena;
+    } else {
+      cudaGetLastError();
+    }
+  }
   for (int w = 0; w < workers; w++) srv->threads.emplace_back(worker_main, srv, w);
+  if (srv->batcher) srv->threads.emplace_back(batch_main, srv);
   srv->threads.emplace_back(dispatcher_main, srv);
   *out = srv;
   return QJG_OK;
@@ -303,6 +532,21 @@ int qjg_server_submit(qjg_server* srv, const qjg_request* req, int64_t* ticket) 
     }
   }
   j->est_bytes = estimate_bytes(*req);
+  j->voxels = (int64_t)req->grid.res[0] * req->grid.res[1] * req->grid.res[2];
+  if (req->kind == QJG_REQ_FIELD && req->precision != QJG_FP64 && req->grid.res[0] > 0 &&
+      req->grid.res[1] > 0 && req->grid.res[2] > 0 && j->voxels <= srv->batch_cap &&
+      j->voxels <= qj::BATCH_ITEM_VOXELS && req->max_it >= 0 && req->escape > 0) {
+    // batch items take integer effective exponents (the double-float head and
+    // the FP64 pass by products)
+    bool ints = true;
+    for (int i = 0; i < nt + nb && ints; i++) {
+      const double e = (i < nt ? req->sigma_top * req->top_powers[i]
+                               : req->sigma_bot * req->bot_powers[i - nt]);
+      ints = e == std::floor(e) && e >= 1 && e <= QJ_MAX_INT_EXP;
+    }
+    j->batchable = ints;
+    if (ints) j->est_bytes = 0;  // inside the batch arena
+  }
   std::memset(&j->res, 0, sizeof j->res);
   j->res.status = QJG_STATUS_QUEUED;
   {
@@ -351,6 +595,7 @@ int qjg_server_drain(qjg_server* srv) {
     if (!srv->waiting.empty()) return false;
     for (auto& q : srv->worker_q)
       if (!q.empty()) return false;
+    if (!srv->batch_q.empty()) return false;
     for (auto& kv : srv->jobs)
       if (kv.second->res.status == QJG_STATUS_QUEUED || kv.second->res.status == QJG_STATUS_RUNNING)
         return false;
@@ -378,6 +623,10 @@ int qjg_server_read_stats(qjg_server* srv, qjg_server_stats* out) {
   out->in_use_bytes = srv->in_use;
   out->peak_in_use_bytes = srv->peak_in_use;
   out->peak_running = srv->peak_running;
+  out->pad_ = 0;
+  out->batched = srv->batched;
+  out->batches = srv->batches;
+  out->max_batch = srv->max_batch;
   return QJG_OK;
 }
 
@@ -389,8 +638,10 @@ void qjg_server_destroy(qjg_server* srv) {
     srv->stop = true;
   }
   srv->cv_dispatch.notify_all();
+  srv->batch_cv.notify_all();
   for (auto& cv : srv->worker_cv) cv.notify_all();
   for (auto& t : srv->threads) t.join();
+  srv->batcher.reset();
   delete srv;
 }
 

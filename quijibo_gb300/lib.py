@@ -91,7 +91,7 @@ class QjgRequest(C.Structure):
                 ("tri_cap", C.c_int64), ("params", _dp), ("d_sat", C.c_double),
                 ("n_samples", C.c_int64), ("xyz", _dp),
                 ("target", _dp), ("out_field", _dp), ("out_verts", _dp),
-                ("out_tris", C.POINTER(C.c_int32)), ("out_grad", _dp)]
+                ("out_tris", C.POINTER(C.c_int32)), ("out_grad", _dp), ("rel_tol", C.c_double)]
 
 
 class QjgResult(C.Structure):
@@ -108,7 +108,8 @@ class QjgServerStats(C.Structure):
     _fields_ = [("completed", C.c_int64), ("failed", C.c_int64), ("p50_ms", C.c_double),
                 ("p99_ms", C.c_double), ("max_ms", C.c_double), ("span_s", C.c_double),
                 ("in_use_bytes", C.c_int64), ("peak_in_use_bytes", C.c_int64),
-                ("peak_running", C.c_int32)]
+                ("peak_running", C.c_int32), ("pad_", C.c_int32), ("batched", C.c_int64),
+                ("batches", C.c_int64), ("max_batch", C.c_int64)]
 
 
 EXPORTS = {
@@ -481,10 +482,11 @@ class Server:
 
     def submit(self, kind, rs=None, grid=None, max_it=20, escape=2.0, precision=QJG_FP32_REFINE,
                iso=0.0, vert_cap=0, tri_cap=0, params=None, xyz=None, target=None,
-               out_field=None, out_verts=None, out_tris=None, out_grad=None, d_sat=1.0):
+               out_field=None, out_verts=None, out_tris=None, out_grad=None, d_sat=1.0,
+               rel_tol=0.0):
         r = QjgRequest()
         r.kind, r.precision, r.max_it, r.escape, r.iso = kind, precision, max_it, escape, iso
-        r.d_sat = d_sat
+        r.d_sat, r.rel_tol = d_sat, rel_tol
         keep = []
 
         def arr(a, shape=None):

@@ -104,3 +104,39 @@ def test_server_matches_direct_calls(ctx):
         f, _, _ = ctx.field_host(h, r["grid"], it)
         ctx.free(h)
         np.testing.assert_array_equal(f.reshape(-1), o["field"])
+
+
+def test_batched_field_requests_equal_direct_calls(ctx):
+    """Small precision-form field requests submitted together are served in
+    multi-request batch passes (a replayed CUDA graph); each field has the
+    bits of its own qjg_field call.  FP64 and non-integer-exponent requests
+    take the per-request workers."""
+    rng = np.random.RandomState(5)
+    reqs = []
+    for i in range(40):
+        nt, nb = int(rng.randint(3, 20)), int(rng.randint(0, 8))
+        rs = draw_rootset(300 + i, nt, nb, -1.2, 1.2, exps=(1, 2))
+        res = (int(rng.choice([8, 17, 24, 33])), int(rng.choice([9, 16, 31])),
+               int(rng.choice([5, 12, 20])))
+        g = Grid(res)
+        rs.scale = conformal_scale(rs, g, sample_res=16)
+        prec = lib.QJG_FP64 if i % 10 == 9 else lib.QJG_FP32_REFINE
+        if i % 10 == 4:
+            rs.top_powers = rs.top_powers * 1.5  # non-integer effective exponents
+        reqs.append(dict(kind=lib.QJG_REQ_FIELD, rs=rs, grid=g, max_it=int(rng.randint(5, 31)),
+                         precision=prec, rel_tol=[0.0, 1e-6][i % 2]))
+    srv = lib.Server(workers=4)
+    outs, res = run(srv, reqs)
+    st = srv.stats()
+    srv.close()
+    n_batchable = sum(1 for i in range(40) if i % 10 not in (4, 9))
+    assert st["batched"] == n_batchable and st["failed"] == 0
+    assert st["max_batch"] > 1 and st["batches"] < n_batchable
+    for r, o, rr in zip(reqs, outs, res):
+        h = ctx.upload(r["rs"])
+        it = ctx.iter_params(r["max_it"], 2.0, precision=r["precision"],
+                             refine_pow=lib.QJG_REFINE_INT, rel_tol=r["rel_tol"])
+        f, _, fs = ctx.field_host(h, r["grid"], it)
+        ctx.free(h)
+        np.testing.assert_array_equal(f.reshape(-1), o["field"])
+        assert rr["voxel_iters"] == fs["voxel_iters"]
