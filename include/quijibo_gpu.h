@@ -342,6 +342,27 @@ int qjg_server_wait(qjg_server* srv, int64_t ticket, qjg_result* out);
 int qjg_server_drain(qjg_server* srv);
 int qjg_server_read_stats(qjg_server* srv, qjg_server_stats* out);
 
+/* ---- optimizer set-up passes ------------------------------------------ */
+
+/* The weight field of a signed distance field (X*Y*Z doubles, device):
+ * 1 / (breadth-first layer from the sign-change shells), negated inside and
+ * quartered outside; with `normalized`, scaled to sum |w| = 1 and 0.5 per
+ * side.  Replaces FIELD_3D::invertedDistance / invertedDistanceNormalized
+ * (src/geometry/FIELD_3D.cpp:5241-5352).  QJG_ERR_ARG when the field has no
+ * sign change that reaches every cell (the reference loops forever). */
+int qjg_inverted_distance(qjg_ctx* ctx, const int32_t res[3], const double* d_dist,
+                          int32_t normalized, double* d_out, void* stream);
+/* The conformal-radius scan: the one-application field log|T/B| of `rs` with
+ * the roots' own exponents (no power scalar), s = 1, escape 20 on `grid`;
+ * scores sum -tanh(alpha (F - x)) W over four passes of ~100 thresholds x,
+ * W = the inverted distance of d_dist (on dist_grid) at the cell centres.
+ * Returns the lowest score, its threshold and exp(-threshold), the scale the
+ * optimizer starts from.  Replaces OPTIMIZE_3D::estimateConformalRadius
+ * (src/solvers/OPTIMIZE_3D.cpp:4693-4772; alpha is _tanhAlpha = 10). */
+int qjg_conformal_radius(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid,
+                         const qjg_grid* dist_grid, const double* d_dist, double alpha,
+                         double* min_score, double* threshold, double* exp_scaling, void* stream);
+
 /* ---- file formats ------------------------------------------------------ */
 
 /* FIELD_3D's binary stream: int xRes, yRes, zRes; double center[3], lengths[3];

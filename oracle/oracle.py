@@ -217,6 +217,9 @@ class Reference:
         L.ref_tanh_score_grad.argtypes = [A, _ip, _dp, _dp, C.c_double, C.c_int, _ip, _dp, _dp,
                                           _dp, _dp, _dp]
         L.ref_tanh_score_grad.restype = C.c_double
+        L.ref_inverted_distance.argtypes = [_ip, _dp, _dp, _dp, C.c_int, _dp]
+        L.ref_conformal_radius.argtypes = [A, _ip, _dp, _dp, C.c_double, _ip, _dp, _dp, _dp, _dp]
+        L.ref_conformal_radius.restype = C.c_double
         L.ref_field_write.argtypes = [C.c_char_p, _ip, _dp, _dp, _dp]
         L.ref_mesh_write.argtypes = [_dp, C.c_int, _ip, C.c_int, C.c_char_p, C.c_char_p]
         L.ref_mesh_write.restype = C.c_int
@@ -228,6 +231,26 @@ class Reference:
         res = np.array(grid.res, dtype=np.int32)
         return (res, np.array(grid.center, dtype=np.float64),
                 np.array(grid.lengths, dtype=np.float64), np.array(grid.rot, dtype=np.float64))
+
+    def inverted_distance(self, grid, dist, normalized=False):
+        """FIELD_3D::invertedDistance[Normalized] of `dist` (x fastest)."""
+        res, c, ln, _ = self._g(grid)
+        out = np.empty(int(np.prod(grid.res)))
+        self.L.ref_inverted_distance(_ptr(res, _ip), _ptr(c), _ptr(ln),
+                                     _ptr(np.ascontiguousarray(dist, dtype=np.float64).ravel()),
+                                     int(bool(normalized)), _ptr(out))
+        return out
+
+    def conformal_radius(self, rs, grid, dgrid, dist):
+        """OPTIMIZE_3D::estimateConformalRadius: (lowest score, exp scaling)."""
+        res, c, ln, _ = self._g(grid)
+        dres, dc, dln, _ = self._g(dgrid)
+        es = C.c_double()
+        sc = self.L.ref_conformal_radius(C.byref(_map_args(rs)), _ptr(res, _ip), _ptr(c), _ptr(ln),
+                                         float(grid.slice), _ptr(dres, _ip), _ptr(dc), _ptr(dln),
+                                         _ptr(np.ascontiguousarray(dist, dtype=np.float64).ravel()),
+                                         C.byref(es))
+        return sc, es.value
 
     def field_write(self, path, res, center, lengths, data):
         """FIELD_3D::write(string) of `data` (x fastest)."""
@@ -308,3 +331,94 @@ class Reference:
                                         grid.slice, max_it, _ptr(wres, _ip), _ptr(wc), _ptr(wl),
                                         _ptr(w), _ptr(grad), _ptr(field))
         return sc, grad, field.reshape(grid.res[::-1])
+
+
+# ---------------------------------------------------------------------------
+# The optimizer's set-up passes, restated with numpy (test infrastructure).
+
+def inverted_distance(dist, normalized=False):
+    """FIELD_3D::invertedDistance[Normalized] (FIELD_3D.cpp:5241-5352) of a
+    (Z, Y, X) signed distance field: the 26-neighbour sign-change shells get
+    1, every other cell the 6-neighbour breadth-first layer of the
+    reference's sweep loop, then 1/v, negated inside, quartered outside."""
+    d = np.asarray(dist, dtype=np.float64)
+    Z, Y, X = d.shape
+    n = d.size
+    pad = np.pad(d, 1)
+    flip = np.zeros(d.shape, dtype=bool)
+    for k in (-1, 0, 1):
+        for j in (-1, 0, 1):
+            for i in (-1, 0, 1):
+                if i == j == k == 0:
+                    continue
+                nb = pad[1 + k:1 + k + Z, 1 + j:1 + j + Y, 1 + i:1 + i + X]
+                flip |= nb * d < 0
+    final = flip.astype(np.float64)
+    while True:
+        zero = final <= 1e-5
+        if not zero.any():
+            break
+        p = np.pad(final, 1)
+        nbs = np.stack([p[1:-1, 1:-1, :-2], p[1:-1, 1:-1, 2:], p[1:-1, :-2, 1:-1],
+                        p[1:-1, 2:, 1:-1], p[:-2, 1:-1, 1:-1], p[2:, 1:-1, 1:-1]])
+        smallest = np.where(nbs > 1e-5, nbs, n + 1.0).min(axis=0)
+        upd = zero & (smallest < n)
+        if not upd.any():
+            raise ValueError("no sign change reaches every cell")
+        final = np.where(upd, smallest + 1.0, final)
+    final = 1.0 / final
+    final = np.where(d < 0, -final, final * 0.25)
+    if normalized:
+        final = final * (1.0 / np.abs(final).sum())
+        inside = final[d < 0].sum()
+        outside = final[d >= 0].sum()
+        final = final * np.where(d < 0, 0.5 / abs(inside), 0.5 / abs(outside))
+    return final
+
+
+def cell_centers_ref(grid):
+    """FIELD_3D::cellCenter of every cell of an unrotated grid, in the
+    reference's operation order (FIELD_3D.cpp:818-841), x fastest."""
+    axes = []
+    for c in range(3):
+        dx = grid.lengths[c] / grid.res[c]
+        i = np.arange(grid.res[c], dtype=np.float64)
+        f = grid.center[c] - grid.lengths[c] * 0.5
+        f = f + i * dx
+        f = f + dx * 0.5
+        f = f - grid.center[c]
+        axes.append(f + grid.center[c])
+    z, y, x = np.meshgrid(axes[2], axes[1], axes[0], indexing="ij")
+    return np.stack([x, y, z], axis=-1).reshape(-1, 3)
+
+
+def conformal_radius(oracle, rs, grid, dgrid, dist, alpha=10.0):
+    """OPTIMIZE_3D::estimateConformalRadius (OPTIMIZE_3D.cpp:4693-4772):
+    returns (lowest score, threshold, exp(-threshold))."""
+    import copy
+    r1 = copy.deepcopy(rs)
+    r1.sigma_top = r1.sigma_bottom = 1.0
+    r1.scale = 1.0
+    f = oracle.field(r1, grid, 1, 20.0)["field"].ravel().copy()
+    inf = np.isinf(f)
+    if inf.any():
+        f[inf] = f[~inf].sum() / (~inf).sum()
+    w_field = inverted_distance(np.asarray(dist).reshape(dgrid.res[::-1]))
+    pts = cell_centers_ref(grid)
+    w = np.array([oracle.trilinear(dgrid, w_field, p) for p in pts])
+    lo, hi = f.min(), f.max()
+    min_t, found = lo, np.finfo(np.float32).max
+    for _ in range(4):
+        inc = (hi - lo) / 100
+        xs = []
+        x = lo
+        while x < hi:
+            xs.append(x)
+            x += inc
+        found = np.finfo(np.float32).max
+        for x in xs:
+            s = np.sum(-np.tanh(alpha * (f - x)) * w)
+            if s < found:
+                found, min_t = s, x
+        lo, hi = min_t - 5 * inc, min_t + 5 * inc
+    return found, min_t, np.exp(-min_t)

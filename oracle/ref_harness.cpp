@@ -207,6 +207,38 @@ double ref_tanh_score_grad(const MapArgs* a, const int* res, const double* cente
   return score;
 }
 
+// FIELD_3D::invertedDistance / invertedDistanceNormalized (FIELD_3D.cpp:5241-5352).
+void ref_inverted_distance(const int* res, const double* center, const double* lengths,
+                           const double* dist, int normalized, double* out) {
+  FIELD_3D d(res[0], res[1], res[2], VEC3F(center[0], center[1], center[2]),
+             VEC3F(lengths[0], lengths[1], lengths[2]));
+  for (int i = 0; i < d.totalCells(); i++) d[i] = dist[i];
+  FIELD_3D w = normalized ? d.invertedDistanceNormalized() : d.invertedDistance();
+  for (int i = 0; i < w.totalCells(); i++) out[i] = (double)w[i];
+}
+
+// OPTIMIZE_3D::estimateConformalRadius (OPTIMIZE_3D.cpp:4693-4772): returns
+// the lowest score; *exp_scaling = the _expScaling it leaves behind.
+double ref_conformal_radius(const MapArgs* a, const int* res, const double* center,
+                            const double* lengths, double slice, const int* dres,
+                            const double* dcenter, const double* dlengths, const double* dist,
+                            double* exp_scaling) {
+  OPTIMIZE_3D opt(res[0], res[1], res[2], VEC3F(center[0], center[1], center[2]),
+                  VEC3F(lengths[0], lengths[1], lengths[2]));
+  opt.top() = make_poly(a->nt, a->troots, a->tpows, a->tsig);
+  opt.bottom() = make_poly(a->nb, a->broots, a->bpows, a->bsig);
+  opt.expScaling() = a->s;
+  opt.maxIterations() = 7;
+  opt.slice() = slice;
+  FIELD_3D d(dres[0], dres[1], dres[2], VEC3F(dcenter[0], dcenter[1], dcenter[2]),
+             VEC3F(dlengths[0], dlengths[1], dlengths[2]));
+  for (int i = 0; i < d.totalCells(); i++) d[i] = dist[i];
+  opt.distanceField() = d;
+  const double score = (double)opt.estimateConformalRadius();
+  *exp_scaling = (double)opt.expScaling();
+  return score;
+}
+
 // FIELD_3D::write(string) of a field (FIELD_3D.cpp:280-300, 4371-4393).
 void ref_field_write(const char* path, const int* res, const double* center,
                      const double* lengths, const double* data) {

@@ -10,6 +10,22 @@
 #include "qj_energy.h"
 #include "qj_lbfgs.h"
 
+qj::WeightGrid qj_weight_grid(const qjg_grid* g) {
+  qj::WeightGrid wg;
+  wg.X = g->res[0];
+  wg.Y = g->res[1];
+  wg.Z = g->res[2];
+  for (int c = 0; c < 3; c++) {
+    // FIELD_3D.cpp:971-980: corner = center - 0.5 lengths; corner += 0.5 dxs; 1/dx
+    const double dx = g->lengths[c] / g->res[c];
+    double corner = g->center[c] - g->lengths[c] * 0.5;
+    corner += dx * 0.5;
+    wg.corner[c] = corner;
+    wg.inv[c] = 1.0 / dx;
+  }
+  return wg;
+}
+
 extern "C" {
 
 int qjg_tanh_score_grad(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, int32_t max_it,
@@ -26,18 +42,7 @@ int qjg_tanh_score_grad(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, int3
   cudaStream_t s = (cudaStream_t)stream;
   QJ_CUDA(ctx, cudaSetDevice(ctx->device));
   const qj::GridParams g = qj_grid_params(grid, 0, grid->res[2]);
-  qj::WeightGrid wg;
-  wg.X = weight_grid->res[0];
-  wg.Y = weight_grid->res[1];
-  wg.Z = weight_grid->res[2];
-  for (int c = 0; c < 3; c++) {
-    // FIELD_3D.cpp:971-980: corner = center - 0.5 lengths; corner += 0.5 dxs; 1/dx
-    const double dx = weight_grid->lengths[c] / weight_grid->res[c];
-    double corner = weight_grid->center[c] - weight_grid->lengths[c] * 0.5;
-    corner += dx * 0.5;
-    wg.corner[c] = corner;
-    wg.inv[c] = 1.0 / dx;
-  }
+  const qj::WeightGrid wg = qj_weight_grid(weight_grid);
   const int nblocks = qj::tanh_blocks();
   const int slots = 6 + m->nt + m->nb;
   double* d_part = nullptr;

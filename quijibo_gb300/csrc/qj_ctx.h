@@ -111,3 +111,5 @@ int qj_check_iter(qjg_ctx* ctx, const qjg_iter* it);
 qj::GridParams qj_grid_params(const qjg_grid* g, int z0, int z1);
 qj::IterParams qj_iter_params(const qjg_iter* it, const qjg_grid* g);
 qj::MapParams* qj_lookup(qjg_ctx* ctx, qjg_rootset rs);
+// trilinear-lookup geometry of a FIELD_3D on grid g (energy_api.cpp)
+qj::WeightGrid qj_weight_grid(const qjg_grid* g);

@@ -270,6 +270,33 @@ __device__ __forceinline__ void cell_center(const GridParams& g, int x, int y, i
   }
 }
 
+// FIELD_3D::operator()(const VEC3F&), FIELD_3D.cpp:966-1029.
+__device__ __forceinline__ double trilinear(const WeightGrid& wg, const double* __restrict__ data,
+                            const double p[3]) {
+  using namespace q64;
+  double pc[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) pc[c] = mul(sub(p[c], wg.corner[c]), wg.inv[c]);
+  int x0 = (int)pc[0], y0 = (int)pc[1], z0 = (int)pc[2];
+  int x1 = x0 + 1, y1 = y0 + 1, z1 = z0 + 1;
+  x0 = x0 < 0 ? 0 : x0; y0 = y0 < 0 ? 0 : y0; z0 = z0 < 0 ? 0 : z0;
+  x1 = x1 < 0 ? 0 : x1; y1 = y1 < 0 ? 0 : y1; z1 = z1 < 0 ? 0 : z1;
+  x0 = x0 > wg.X - 1 ? wg.X - 1 : x0; y0 = y0 > wg.Y - 1 ? wg.Y - 1 : y0;
+  z0 = z0 > wg.Z - 1 ? wg.Z - 1 : z0;
+  x1 = x1 > wg.X - 1 ? wg.X - 1 : x1; y1 = y1 > wg.Y - 1 ? wg.Y - 1 : y1;
+  z1 = z1 > wg.Z - 1 ? wg.Z - 1 : z1;
+  const float s1 = __double2float_rn(sub(pc[0], (double)x0)), s0 = __fsub_rn(1.0f, s1);
+  const float t1 = __double2float_rn(sub(pc[1], (double)y0)), t0 = __fsub_rn(1.0f, t1);
+  const float u1 = __double2float_rn(sub(pc[2], (double)z0)), u0 = __fsub_rn(1.0f, u1);
+  const long long XY = (long long)wg.X * wg.Y;
+  auto at = [&](int x, int y, int z) { return data[x + (long long)y * wg.X + z * XY]; };
+  const double a = add(mul((double)s0, add(mul((double)t0, at(x0, y0, z0)), mul((double)t1, at(x0, y1, z0)))),
+                       mul((double)s1, add(mul((double)t0, at(x1, y0, z0)), mul((double)t1, at(x1, y1, z0)))));
+  const double b = add(mul((double)s0, add(mul((double)t0, at(x0, y0, z1)), mul((double)t1, at(x0, y1, z1)))),
+                       mul((double)s1, add(mul((double)t0, at(x1, y0, z1)), mul((double)t1, at(x1, y1, z1)))));
+  return add(mul((double)u0, a), mul((double)u1, b));
+}
+
 // ------------------------------------------------------- FP64 escape loop
 
 // prod_{i in [lo, hi)} (q - r_i)^(e_i), left to right, as

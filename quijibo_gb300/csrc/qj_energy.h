@@ -8,11 +8,6 @@ namespace qj {
 
 // A FIELD_3D weight grid for trilinear lookups (FIELD_3D.cpp:966-1029):
 // corner = center - lengths/2 + dx/2, inv = 1/dx.
-struct WeightGrid {
-  int X, Y, Z;
-  double corner[3];
-  double inv[3];
-};
 
 int tanh_blocks();
 cudaError_t launch_tanh_grad(const MapParams& m, const GridParams& g, const WeightGrid& wg,

@@ -47,6 +47,14 @@ struct GridParams {
   double slice;      // the fourth (k) coordinate of every start point
 };
 
+// A FIELD_3D sampled by trilinear lookup: first cell centre and 1/dx
+// (FIELD_3D.cpp:971-980).
+struct WeightGrid {
+  int X, Y, Z;
+  double corner[3];
+  double inv[3];
+};
+
 // Escape-time iteration settings.
 struct IterParams {
   int max_it;

@@ -145,6 +145,10 @@ EXPORTS = {
     "qjg_fit_lbfgs": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p,
                        C.c_void_p, C.c_double, C.c_int32, C.c_double, C.c_double, C.c_int32,
                        C.c_int32, C.c_int32, _dp, C.POINTER(QjgFitStats), C.c_void_p], C.c_int),
+    "qjg_inverted_distance": ([C.c_void_p, C.POINTER(C.c_int32), C.c_void_p, C.c_int32,
+                               C.c_void_p, C.c_void_p], C.c_int),
+    "qjg_conformal_radius": ([C.c_void_p, C.c_int32, C.POINTER(QjgGrid), C.POINTER(QjgGrid),
+                              C.c_void_p, C.c_double, _dp, _dp, _dp, C.c_void_p], C.c_int),
     "qjg_field3d_write": ([C.c_char_p, C.POINTER(C.c_int32), _dp, _dp, C.c_void_p], C.c_int),
     "qjg_field3d_read_header": ([C.c_char_p, C.POINTER(C.c_int32), _dp, _dp], C.c_int),
     "qjg_field3d_read": ([C.c_char_p, C.c_void_p, C.c_int64], C.c_int),
@@ -337,6 +341,23 @@ class Context:
         self._check(self.L.qjg_field_stats_read(self.h, C.c_void_p(stream or 0), C.byref(st)),
                     "qjg_field_stats_read")
         return st.as_dict()
+
+    def inverted_distance(self, res, d_dist, normalized, d_out, stream=None):
+        """FIELD_3D::invertedDistance[Normalized] on device buffers."""
+        r = (C.c_int32 * 3)(*[int(v) for v in res])
+        self._check(self.L.qjg_inverted_distance(self.h, r, C.c_void_p(d_dist), int(normalized),
+                                                 C.c_void_p(d_out), C.c_void_p(stream or 0)),
+                    "qjg_inverted_distance")
+
+    def conformal_radius(self, handle, grid: Grid, dist_grid: Grid, d_dist, alpha=10.0,
+                         stream=None):
+        """estimateConformalRadius: (lowest score, threshold, exp(-threshold))."""
+        sc, th, es = C.c_double(), C.c_double(), C.c_double()
+        self._check(self.L.qjg_conformal_radius(self.h, handle, C.byref(QjgGrid.of(grid)),
+                                                C.byref(QjgGrid.of(dist_grid)), C.c_void_p(d_dist),
+                                                float(alpha), C.byref(sc), C.byref(th), C.byref(es),
+                                                C.c_void_p(stream or 0)), "qjg_conformal_radius")
+        return sc.value, th.value, es.value
 
     def set_timing(self, on=True):
         self._check(self.L.qjg_set_timing(self.h, int(on)), "qjg_set_timing")

@@ -103,6 +103,7 @@ def main():
     np.savez_compressed(os.path.join(OUT, "tanh_grad.npz"), **d)
 
     io_case(rd)
+    conformal_case(rd)
 
     print("stream: %d verts %d tris; nonlinear: %d/%d; linear: %d/%d" % (
         len(ms["verts"]), len(ms["tris"]), len(mn["verts"]), len(mn["tris"]), len(ml["verts"]),
@@ -129,6 +130,34 @@ def io_case(rd):
     field, res, center, lengths, verts, tris = io_inputs()
     rd.field_write(os.path.join(OUT, "io_field.field3d"), res, center, lengths, field)
     rd.mesh_write(verts, tris, os.path.join(OUT, "io_mesh.obj"), os.path.join(OUT, "io_mesh.raw"))
+
+
+def conformal_inputs():
+    """Map, fractal grid and a signed distance field (union of two
+    ellipsoids, negative inside) on a different grid, for the weight field
+    and the conformal-radius scan."""
+    from quijibo_gb300.rootsets import cell_centers
+    rs = draw_rootset(21, 6, 3, -1.0, 1.0, exps=(1, 2))
+    rs.sigma_top, rs.sigma_bottom, rs.scale = 1.1, 0.9, 0.37  # the scan ignores all three
+    g = Grid((20, 20, 20), slice=0.05)
+    dg = Grid((18, 16, 14), center=(0.05, -0.02, 0.0), lengths=(3.2, 3.0, 2.8))
+    c = cell_centers(dg)
+    e1 = np.sqrt(((c - [0.3, 0.0, 0.1]) ** 2 / np.array([0.6, 0.45, 0.5]) ** 2).sum(1)) - 1.0
+    e2 = np.sqrt(((c - [-0.4, 0.2, -0.1]) ** 2 / np.array([0.35, 0.5, 0.4]) ** 2).sum(1)) - 1.0
+    dist = np.minimum(e1 * 0.45, e2 * 0.35)
+    return rs, g, dg, dist
+
+
+def conformal_case(rd):
+    """FIELD_3D::invertedDistance[Normalized] and estimateConformalRadius."""
+    rs, g, dg, dist = conformal_inputs()
+    d = rs_dict("", rs, g, dict(max_it=1, escape=20.0))
+    d.update(dres=np.array(dg.res), dcenter=np.array(dg.center), dlengths=np.array(dg.lengths),
+             dist=dist, inv=rd.inverted_distance(dg, dist, False),
+             inv_norm=rd.inverted_distance(dg, dist, True))
+    score, es = rd.conformal_radius(rs, g, dg, dist)
+    d.update(score=score, exp_scaling=es)
+    np.savez_compressed(os.path.join(OUT, "conformal.npz"), **d)
 
 
 def tanh_case():
