@@ -33,6 +33,8 @@ extern "C" {
 #define QJG_FP32_REFINE 2 /* FP32 bulk, FP64 re-evaluation of the band |d| < band_h * h */
 
 /* How FP64 re-evaluation raises roots to powers. */
+#define QJG_FORM_QUOTIENT 0
+#define QJG_FORM_LAGRANGE 1
 #define QJG_REFINE_POW 0 /* the reference's polar QUATERNION::pow (reference rounding) */
 #define QJG_REFINE_INT 1 /* repeated products when every exponent is an integer */
 
@@ -62,6 +64,10 @@ typedef struct {
   double rel_tol;    /* QJG_FP32_REFINE: target relative field error (e.g. 1e-6); voxels whose
                         tracked FP32 error exceeds it are re-run with a double-float head and,
                         if still above it, in FP64.  0 = the band rule alone. */
+  int32_t form;      /* QJG_FORM_QUOTIENT: T(q) / B(q) (computeLogScaledPowerRationalMap);
+                        QJG_FORM_LAGRANGE: RATIONAL_4D::evaluateLagrange order, top and bottom
+                        factors interleaved (RATIONAL_4D.cpp:27-73; QJG_FP64 only) */
+  int32_t pad_;
 } qjg_iter;
 
 typedef struct {

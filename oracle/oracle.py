@@ -35,7 +35,7 @@ class _Poly(C.Structure):
 
 
 class _Map(C.Structure):
-    _fields_ = [("top", _Poly), ("bottom", _Poly), ("scale", C.c_double)]
+    _fields_ = [("top", _Poly), ("bottom", _Poly), ("scale", C.c_double), ("lagrange", C.c_int)]
 
 
 class _Grid(C.Structure):
@@ -55,7 +55,7 @@ def make_map(rootset):
 
     m = _Map(poly(rootset.top_roots, rootset.top_powers, rootset.sigma_top),
              poly(rootset.bottom_roots, rootset.bottom_powers, rootset.sigma_bottom),
-             float(rootset.scale))
+             float(rootset.scale), int(bool(getattr(rootset, "lagrange", False))))
     m._keep = keep
     return m
 
@@ -217,6 +217,10 @@ class Reference:
         L.ref_tanh_score_grad.argtypes = [A, _ip, _dp, _dp, C.c_double, C.c_int, _ip, _dp, _dp,
                                           _dp, _dp, _dp]
         L.ref_tanh_score_grad.restype = C.c_double
+        L.ref_field_lagrange.argtypes = [A, _ip, _dp, _dp, _dp, C.c_double, C.c_int, C.c_double,
+                                         _dp]
+        L.ref_mesh_lagrange.argtypes = [A, _ip, _dp, _dp, _dp, C.c_double, C.c_int, C.c_double,
+                                        _dp, C.c_int, _ip, C.c_int, _ip, _ip]
         L.ref_inverted_distance.argtypes = [_ip, _dp, _dp, _dp, C.c_int, _dp]
         L.ref_conformal_radius.argtypes = [A, _ip, _dp, _dp, C.c_double, _ip, _dp, _dp, _dp, _dp]
         L.ref_conformal_radius.restype = C.c_double
@@ -231,6 +235,20 @@ class Reference:
         res = np.array(grid.res, dtype=np.int32)
         return (res, np.array(grid.center, dtype=np.float64),
                 np.array(grid.lengths, dtype=np.float64), np.array(grid.rot, dtype=np.float64))
+
+    def field_lagrange(self, rs, grid, max_it, escape):
+        """The Lagrange-order escape loop (computeLagrangeNonlinearSlice)."""
+        res, c, ln, r = self._g(grid)
+        out = np.empty(int(np.prod(grid.res)))
+        self.L.ref_field_lagrange(C.byref(_map_args(rs)), _ptr(res, _ip), _ptr(c), _ptr(ln),
+                                  _ptr(r), float(grid.slice), int(max_it), float(escape), _ptr(out))
+        return out
+
+    def mesh_lagrange(self, rs, grid, max_it, iso=0.0):
+        res, c, ln, r = self._g(grid)
+        return self._mesh_out(self.L.ref_mesh_lagrange, C.byref(_map_args(rs)), _ptr(res, _ip),
+                              _ptr(c), _ptr(ln), _ptr(r), float(grid.slice), int(max_it),
+                              float(iso), n=int(np.prod(grid.res)))
 
     def inverted_distance(self, grid, dist, normalized=False):
         """FIELD_3D::invertedDistance[Normalized] of `dist` (x fastest)."""

@@ -106,9 +106,52 @@ void qjo_eval_factored(const qjo_poly* p, const double q[4], double out[4]) {
   memcpy(out, r, sizeof r);
 }
 
+/* POLYNOMIAL_4D::evaluateRoot, POLYNOMIAL_4D.cpp:928-940. */
+static void root_term(const qjo_poly* p, int i, const double q[4], double out[4]) {
+  double d[4];
+  for (int c = 0; c < 4; c++) d[c] = q[c] - p->roots[4 * i + c];
+  qjo_quat_pow(d, p->power_scalar * p->powers[i], out);
+}
+
+/* RATIONAL_4D::evaluateLagrange, RATIONAL_4D.cpp:27-73: top and bottom
+ * factors interleaved (times top_k, then divided by bottom_k), the leftovers
+ * of the longer side after; without bottom roots the plain factored top. */
+static void lagrange_apply(const qjo_map* m, const double q[4], double out[4]) {
+  const int nt = m->top.n, nb = m->bottom.n;
+  double r[4] = {1, 0, 0, 0}, t[4], o[4];
+  const int same = nt > nb ? nb : nt;
+  for (int k = 0; k < same; k++) {
+    root_term(&m->top, k, q, t);
+    qmul(r, t, o);
+    root_term(&m->bottom, k, q, t);
+    qdiv(o, t, r);
+  }
+  if (nt > nb) {
+    for (int k = same; k < nt; k++) {
+      root_term(&m->top, k, q, t);
+      qmul(r, t, o);
+      memcpy(r, o, sizeof r);
+    }
+  } else {
+    for (int k = same; k < nb; k++) {
+      root_term(&m->bottom, k, q, t);
+      qdiv(r, t, o);
+      memcpy(r, o, sizeof r);
+    }
+  }
+  memcpy(out, r, sizeof r);
+}
+
 /* One map application as in the escape loop of
- * OPTIMIZE_3D::computeLogScaledPowerRationalMap (OPTIMIZE_3D.cpp:1331-1350). */
+ * OPTIMIZE_3D::computeLogScaledPowerRationalMap (OPTIMIZE_3D.cpp:1331-1350),
+ * or in the Lagrange order (TRIANGLE_MESH::computeLagrangeNonlinearSlice,
+ * TRIANGLE_MESH.cpp:281-322). */
 void qjo_map_apply(const qjo_map* m, const double q[4], double out[4]) {
+  if (m->lagrange && m->bottom.n > 0) {
+    lagrange_apply(m, q, out);
+    for (int c = 0; c < 4; c++) out[c] *= m->scale;
+    return;
+  }
   double t[4];
   qjo_eval_factored(&m->top, q, t);
   if (m->bottom.n > 0) {
@@ -225,8 +268,38 @@ int64_t qjo_field(const qjo_map* m, const qjo_grid* g, int max_it, double escape
   return terms;
 }
 
+/* TRIANGLE_MESH::lagrangeNonlinearValue, TRIANGLE_MESH.cpp:1684-1747: an
+ * overflowing iterate reverts to the previous one and stops; an infinite
+ * value returns FLT_MAX.  (The reference leaves the "previous" magnitude
+ * unset when the first application overflows; here it is |q_0|.) */
+static double lagrange_value(const qjo_map* m, const double p[3], double slice, int max_it,
+                             double escape, double iso) {
+  double q[4] = {p[0], p[1], p[2], slice}, prev[4];
+  double mag = qmag(q), prev_mag = mag;
+  memcpy(prev, q, sizeof q);
+  int it = 0;
+  while (mag < escape && it < max_it) {
+    double nq[4];
+    qjo_map_apply(m, q, nq);
+    memcpy(q, nq, sizeof q);
+    mag = qmag(q);
+    if (isinf(mag)) {
+      memcpy(q, prev, sizeof q);
+      mag = prev_mag;
+      break;
+    }
+    memcpy(prev, q, sizeof q);
+    prev_mag = mag;
+    it++;
+    if (mag < 10.0 * QJO_REAL_MIN) it = max_it;
+  }
+  const double f = log(mag) - iso;
+  return isinf(f) ? 3.40282346638528859812e+38 : f;
+}
+
 double qjo_nonlinear_value(const qjo_map* m, const double p[3], double slice, int max_it,
                            double escape, double iso) {
+  if (m->lagrange) return lagrange_value(m, p, slice, max_it, escape, iso);
   return escape_value(m, p, slice, max_it, escape, NULL, NULL) - iso;
 }
 

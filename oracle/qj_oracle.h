@@ -36,6 +36,7 @@ typedef struct {
   qjo_poly top;
   qjo_poly bottom;
   double scale; /* OPTIMIZE_3D::_expScaling */
+  int lagrange; /* 1: RATIONAL_4D::evaluateLagrange order (and lagrangeNonlinearValue) */
 } qjo_map;
 
 /* A cell-centred grid (FIELD_3D geometry).  rot is a quaternion (w,x,y,z)

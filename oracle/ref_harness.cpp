@@ -20,6 +20,7 @@
 #include "OPTIMIZE_3D.h"
 #include "POLYNOMIAL_4D.h"
 #include "QUATERNION.h"
+#include "RATIONAL_4D.h"
 #include "TRIANGLE_MESH.h"
 
 namespace {
@@ -205,6 +206,53 @@ double ref_tanh_score_grad(const MapArgs* a, const int* res, const double* cente
   FIELD_3D& f = opt.fractal();
   for (int i = 0; i < f.totalCells(); i++) field[i] = (double)f[i];
   return score;
+}
+
+// The escape loop of TRIANGLE_MESH::computeLagrangeNonlinearSlice
+// (TRIANGLE_MESH.cpp:281-322) over a whole grid, escape as a parameter:
+// RATIONAL_4D::evaluateLagrange, then the scale.
+void ref_field_lagrange(const MapArgs* a, const int* res, const double* center,
+                        const double* lengths, const double* rot, double slice, int max_it,
+                        double escape, double* out) {
+  POLYNOMIAL_4D top = make_poly(a->nt, a->troots, a->tpows, a->tsig);
+  POLYNOMIAL_4D bottom = make_poly(a->nb, a->broots, a->bpows, a->bsig);
+  FIELD_3D grid(res[0], res[1], res[2], VEC3F(center[0], center[1], center[2]),
+                VEC3F(lengths[0], lengths[1], lengths[2]));
+  grid.rotation() = QUATERNION(rot[0], rot[1], rot[2], rot[3]);
+  const Real s = a->s;
+#pragma omp parallel for schedule(dynamic)
+  for (int z = 0; z < res[2]; z++) {
+    RATIONAL_4D rational(top, bottom);
+    for (int y = 0; y < res[1]; y++)
+      for (int x = 0; x < res[0]; x++) {
+        VEC3F point = grid.cellCenter(x, y, z);
+        QUATERNION iterate(point[0], point[1], point[2], (Real)slice);
+        Real magnitude = iterate.magnitude();
+        int totalIterations = 0;
+        while (magnitude < escape && totalIterations < max_it) {
+          iterate = rational.evaluateLagrange(iterate);
+          iterate *= s;
+          magnitude = iterate.magnitude();
+          totalIterations++;
+          if (magnitude < 10.0 * REAL_MIN) totalIterations = max_it;
+        }
+        out[(size_t)z * res[0] * res[1] + (size_t)y * res[0] + x] = (double)log(magnitude);
+      }
+  }
+}
+
+// The Lagrange streaming mesher: TRIANGLE_MESH's 10-argument constructor
+// (TRIANGLE_MESH.cpp:106-123, computeLagrangeNonlinearMarchingCubesLowMemoryHuge).
+int ref_mesh_lagrange(const MapArgs* a, const int* res, const double* center,
+                      const double* lengths, const double* rot, double slice, int max_it,
+                      double iso, double* verts, int max_v, int* tris, int max_t, int* nv,
+                      int* nt) {
+  TRIANGLE_MESH mesh(VEC3F(center[0], center[1], center[2]),
+                     VEC3F(lengths[0], lengths[1], lengths[2]), VEC3I(res[0], res[1], res[2]),
+                     make_poly(a->nt, a->troots, a->tpows, a->tsig),
+                     make_poly(a->nb, a->broots, a->bpows, a->bsig), a->s, max_it, slice, iso,
+                     QUATERNION(rot[0], rot[1], rot[2], rot[3]));
+  return export_mesh(mesh, verts, max_v, tris, max_t, nv, nt);
 }
 
 // FIELD_3D::invertedDistance / invertedDistanceNormalized (FIELD_3D.cpp:5241-5352).

@@ -50,6 +50,9 @@
 #define QJA_MESH_STREAM                                                                      \
   "_ZN13TRIANGLE_MESHC1ERK5" QJA_V "S3_RKS0_IiERK13POLYNOMIAL_4DS9_" QJA_R "i" QJA_R QJA_R \
   "RK10QUATERNIONRKNSt7__cxx1112basic_stringIcSt11char_traitsIcESaIcEEE"
+#define QJA_MESH_LAGRANGE \
+  "_ZN13TRIANGLE_MESHC1ERK5" QJA_V "S3_RKS0_IiERK13POLYNOMIAL_4DS9_" QJA_R "i" QJA_R QJA_R \
+  "RK10QUATERNION"
 #define QJA_SCORE "_ZN11OPTIMIZE_3D14computeScoreAPEv"
 #define QJA_EXPG "_ZN11OPTIMIZE_3D20computeExpGradientAPEv"
 #define QJA_TOPG "_ZN11OPTIMIZE_3D20computeTopGradientAPEi"
@@ -257,6 +260,28 @@ void qja_mesh_stream(TRIANGLE_MESH* self, const VEC3F& center, const VEC3F& leng
   const qjg_rootset h = upload(top, bottom, expScaling);
   const qjg_grid g = grid_of(res, center, lengths, rotation, slice);
   const qjg_iter it = iter_of(maxIterations, 2000.0, precision());
+  run_mesher(self, (int64_t)res[0] * res[1] * 8, [&](MeshOut& o, qjg_mesh_stats* st) {
+    return qjg_mesh_stream(gpu(), h, &g, &it, (double)isosurface, 0, o.v, nullptr, o.vcap, o.t,
+                           o.tcap, st, nullptr);
+  });
+  qjg_rootset_free(gpu(), h);
+}
+
+// TRIANGLE_MESH(center, lengths, res, top, bottom, expScaling, maxIterations,
+// slice, isosurface, rotation): the Lagrange streaming mesher
+// (TRIANGLE_MESH.cpp:106-123), always in the FP64 form.
+void qja_mesh_lagrange(TRIANGLE_MESH* self, const VEC3F& center, const VEC3F& lengths,
+                       const VEC3I& res, const POLYNOMIAL_4D& top, const POLYNOMIAL_4D& bottom,
+                       Real expScaling, int maxIterations, Real slice, Real isosurface,
+                       const QUATERNION& rotation) __asm__("__wrap_" QJA_MESH_LAGRANGE);
+void qja_mesh_lagrange(TRIANGLE_MESH* self, const VEC3F& center, const VEC3F& lengths,
+                       const VEC3I& res, const POLYNOMIAL_4D& top, const POLYNOMIAL_4D& bottom,
+                       Real expScaling, int maxIterations, Real slice, Real isosurface,
+                       const QUATERNION& rotation) {
+  const qjg_rootset h = upload(top, bottom, expScaling);
+  const qjg_grid g = grid_of(res, center, lengths, rotation, slice);
+  qjg_iter it = iter_of(maxIterations, 2000.0, QJG_FP64);
+  it.form = QJG_FORM_LAGRANGE;
   run_mesher(self, (int64_t)res[0] * res[1] * 8, [&](MeshOut& o, qjg_mesh_stats* st) {
     return qjg_mesh_stream(gpu(), h, &g, &it, (double)isosurface, 0, o.v, nullptr, o.vcap, o.t,
                            o.tcap, st, nullptr);

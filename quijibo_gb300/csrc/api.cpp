@@ -75,6 +75,10 @@ int qj_check_iter(qjg_ctx* ctx, const qjg_iter* it) {
     return fail(ctx, QJG_ERR_ARG, "unknown precision %d", it->precision);
   if (it->refine_pow != QJG_REFINE_POW && it->refine_pow != QJG_REFINE_INT)
     return fail(ctx, QJG_ERR_ARG, "unknown refine_pow %d", it->refine_pow);
+  if (it->form != QJG_FORM_QUOTIENT && it->form != QJG_FORM_LAGRANGE)
+    return fail(ctx, QJG_ERR_ARG, "unknown form %d", it->form);
+  if (it->form == QJG_FORM_LAGRANGE && it->precision != QJG_FP64)
+    return fail(ctx, QJG_ERR_ARG, "the Lagrange form is computed in the plain FP64 form only");
   return QJG_OK;
 }
 
@@ -92,7 +96,7 @@ IterParams qj_iter_params(const qjg_iter* it, const qjg_grid* g) {
   // (5x or more for 99.9% of voxels on the precision and large workloads)
   p.est_tol = it->rel_tol > 0 ? it->rel_tol : 0.0;
   p.ff_head = 2;
-  p.pad_ = 0;
+  p.lagrange = it->form == QJG_FORM_LAGRANGE ? 1 : 0;
   return p;
 }
 

@@ -312,6 +312,7 @@ __device__ __forceinline__ double value64(const MapParams& m, const GridParams& 
                                           const IterParams& it, const double p[3], double iso,
                                           unsigned long long* e64) {
   (*e64)++;
+  if (it.lagrange) return lagrange_value64<POW_REF>(m, it, p, g.slice, iso);
   int ni;
   double dd;
   return q64::sub(escape64<POW_REF, false>(m, it, p, g.slice, &ni, &dd), iso);

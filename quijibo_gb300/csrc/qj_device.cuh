@@ -302,6 +302,28 @@ __device__ __forceinline__ double trilinear(const WeightGrid& wg, const double* 
 // prod_{i in [lo, hi)} (q - r_i)^(e_i), left to right, as
 // POLYNOMIAL_4D::evaluateScaledPowerFactored (POLYNOMIAL_4D.cpp:912-923);
 // with DE, adds sign * sum e_i (q - r_i) / |q - r_i|^2 to g.
+// One root term (q - r_i)^(e_i) (POLYNOMIAL_4D::evaluateRoot,
+// POLYNOMIAL_4D.cpp:928-940); with DE, adds sign * e_i d/|d|^2 to g.
+template <bool POW_REF, bool DE>
+__device__ __forceinline__ q64::Q term64(const MapParams& m, const q64::Q& q, int i, double sign,
+                                         q64::Q& g) {
+  using namespace q64;
+  Q d;
+  d.w = sub(q.w, m.r64[i][0]);
+  d.x = sub(q.x, m.r64[i][1]);
+  d.y = sub(q.y, m.r64[i][2]);
+  d.z = sub(q.z, m.r64[i][3]);
+  if (DE) {
+    // no reference counterpart: gradient of log|R| for the distance estimate
+    const double k = sign * m.e64[i] / norm2(d);
+    g.w += k * d.w;
+    g.x += k * d.x;
+    g.y += k * d.y;
+    g.z += k * d.z;
+  }
+  return POW_REF ? qpow(d, m.e64[i]) : qpow_int(d, m.ie[i]);
+}
+
 template <bool POW_REF, bool DE>
 __device__ __forceinline__ q64::Q product64(const MapParams& m, const q64::Q& q, int lo, int hi,
                                             double sign, q64::Q& g) {
@@ -309,36 +331,51 @@ __device__ __forceinline__ q64::Q product64(const MapParams& m, const q64::Q& q,
   Q r = {1.0, 0.0, 0.0, 0.0};
 #pragma unroll 1
   for (int i = lo; i < hi; i++) {
-    Q d;
-    d.w = sub(q.w, m.r64[i][0]);
-    d.x = sub(q.x, m.r64[i][1]);
-    d.y = sub(q.y, m.r64[i][2]);
-    d.z = sub(q.z, m.r64[i][3]);
-    if (DE) {
-      // no reference counterpart: gradient of log|R| for the distance estimate
-      const double k = sign * m.e64[i] / norm2(d);
-      g.w += k * d.w;
-      g.x += k * d.x;
-      g.y += k * d.y;
-      g.z += k * d.z;
-    }
-    const Q t = POW_REF ? qpow(d, m.e64[i]) : qpow_int(d, m.ie[i]);
+    const Q t = term64<POW_REF, DE>(m, q, i, sign, g);
     r = (i == lo) ? t : qmul(r, t);
   }
   return r;
 }
 
+// RATIONAL_4D::evaluateLagrange (RATIONAL_4D.cpp:27-73): from 1, times top
+// term k then divided by bottom term k for the common k, then the longer
+// side's leftovers; without bottom roots the plain factored top.
+template <bool POW_REF, bool DE>
+__device__ __forceinline__ q64::Q lagrange64(const MapParams& m, const q64::Q& q, q64::Q& g) {
+  using namespace q64;
+  if (m.nb == 0) return product64<POW_REF, DE>(m, q, 0, m.nt, 1.0, g);
+  Q r = {1.0, 0.0, 0.0, 0.0};
+  const int same = m.nt < m.nb ? m.nt : m.nb;
+#pragma unroll 1
+  for (int k = 0; k < same; k++) {
+    r = qmul(r, term64<POW_REF, DE>(m, q, k, 1.0, g));
+    r = qdiv(r, term64<POW_REF, DE>(m, q, m.nt + k, -1.0, g));
+  }
+#pragma unroll 1
+  for (int k = same; k < m.nt; k++) r = qmul(r, term64<POW_REF, DE>(m, q, k, 1.0, g));
+#pragma unroll 1
+  for (int k = same; k < m.nb; k++) r = qdiv(r, term64<POW_REF, DE>(m, q, m.nt + k, -1.0, g));
+  return r;
+}
+
 // One application of the map in reference order (OPTIMIZE_3D.cpp:1331-1350),
 // plus |grad log|R|| for the distance estimate when DE is set.
+// With `lagrange`, the map in the Lagrange order (TRIANGLE_MESH.cpp:281-322).
 template <bool POW_REF, bool DE>
-__device__ __forceinline__ q64::Q apply64(const MapParams& m, const q64::Q& q, double* gnorm) {
+__device__ __forceinline__ q64::Q apply64(const MapParams& m, const q64::Q& q, double* gnorm,
+                                          bool lagrange = false) {
   using namespace q64;
   Q g = {0.0, 0.0, 0.0, 0.0};
-  const Q top = product64<POW_REF, DE>(m, q, 0, m.nt, 1.0, g);
-  Q out = top;
-  if (m.nb > 0) {
-    const Q bot = product64<POW_REF, DE>(m, q, m.nt, m.nt + m.nb, -1.0, g);
-    out = qdiv(top, bot);
+  Q out;
+  if (lagrange) {
+    out = lagrange64<POW_REF, DE>(m, q, g);
+  } else {
+    const Q top = product64<POW_REF, DE>(m, q, 0, m.nt, 1.0, g);
+    out = top;
+    if (m.nb > 0) {
+      const Q bot = product64<POW_REF, DE>(m, q, m.nt, m.nt + m.nb, -1.0, g);
+      out = qdiv(top, bot);
+    }
   }
   out.w = mul(out.w, m.scale);
   out.x = mul(out.x, m.scale);
@@ -362,7 +399,7 @@ __device__ __forceinline__ double escape64(const MapParams& m, const IterParams&
   const double tiny = 10.0 * 0x1p-126;  // 10 * FLT_MIN (SETTINGS.h:60)
   while (mg < it.escape && n < it.max_it) {
     double gn = 0.0;
-    q = apply64<POW_REF, DE>(m, q, &gn);
+    q = apply64<POW_REF, DE>(m, q, &gn, it.lagrange != 0);
     mg = mag(q);
     if (DE) dn = (dn * gn) * mg;
     n++;
@@ -373,6 +410,38 @@ __device__ __forceinline__ double escape64(const MapParams& m, const IterParams&
   *iters = executed;
   if (DE) *de = mg * f / dn;
   return f;
+}
+
+// TRIANGLE_MESH::lagrangeNonlinearValue (TRIANGLE_MESH.cpp:1684-1747): the
+// Lagrange escape loop minus iso, where an overflowing iterate reverts to
+// the previous one and stops, and an infinite value becomes FLT_MAX.  (The
+// reference leaves the previous magnitude unset when the first application
+// overflows; here it is |q_0|.)
+template <bool POW_REF>
+__device__ __forceinline__ double lagrange_value64(const MapParams& m, const IterParams& it,
+                                                   const double p[3], double slice, double iso) {
+  using namespace q64;
+  Q q = {p[0], p[1], p[2], slice};
+  double mg = mag(q), prev_mg = mg;
+  Q prev = q;
+  int n = 0;
+  const double tiny = 10.0 * 0x1p-126;
+  while (mg < it.escape && n < it.max_it) {
+    double gn;
+    q = apply64<POW_REF, false>(m, q, &gn, true);
+    mg = mag(q);
+    if (isinf(mg)) {
+      q = prev;
+      mg = prev_mg;
+      break;
+    }
+    prev = q;
+    prev_mg = mg;
+    n++;
+    if (mg < tiny) n = it.max_it;
+  }
+  const double f = sub(log(mg), iso);
+  return isinf(f) ? 3.40282346638528859812e+38 : f;
 }
 
 // ------------------------------------------------------- FP32 map

@@ -68,7 +68,7 @@ struct IterParams {
   // FP64 when ff_head is 0.  est_tol 0 = off.
   double est_tol;
   int ff_head;
-  int pad_;
+  int lagrange;      // the map in RATIONAL_4D::evaluateLagrange order (FP64 form)
 };
 
 // Device-side counters of one field or mesh call.

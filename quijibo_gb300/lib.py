@@ -38,7 +38,8 @@ class QjgGrid(C.Structure):
 class QjgIter(C.Structure):
     _fields_ = [("max_it", C.c_int32), ("precision", C.c_int32), ("refine_pow", C.c_int32),
                 ("want_de", C.c_int32), ("escape", C.c_double), ("band_h", C.c_double),
-                ("field_tol", C.c_double), ("rel_tol", C.c_double)]
+                ("field_tol", C.c_double), ("rel_tol", C.c_double), ("form", C.c_int32),
+                ("pad_", C.c_int32)]
 
 
 class QjgFieldStats(C.Structure):
@@ -324,9 +325,10 @@ class Context:
 
     @staticmethod
     def iter_params(max_it, escape, precision=QJG_FP64, refine_pow=QJG_REFINE_POW, want_de=False,
-                    band_h=2.0, field_tol=1e-3, rel_tol=0.0):
+                    band_h=2.0, field_tol=1e-3, rel_tol=0.0, lagrange=False):
         return QjgIter(int(max_it), int(precision), int(refine_pow), int(bool(want_de)),
-                       float(escape), float(band_h), float(field_tol), float(rel_tol))
+                       float(escape), float(band_h), float(field_tol), float(rel_tol),
+                       int(bool(lagrange)), 0)
 
     def field(self, handle, grid: Grid, it: QjgIter, d_field, d_de=None, z0=0, z1=None,
               stream=None):

@@ -104,6 +104,7 @@ def main():
 
     io_case(rd)
     conformal_case(rd)
+    lagrange_case(rd)
 
     print("stream: %d verts %d tris; nonlinear: %d/%d; linear: %d/%d" % (
         len(ms["verts"]), len(ms["tris"]), len(mn["verts"]), len(mn["tris"]), len(ml["verts"]),
@@ -130,6 +131,29 @@ def io_case(rd):
     field, res, center, lengths, verts, tris = io_inputs()
     rd.field_write(os.path.join(OUT, "io_field.field3d"), res, center, lengths, field)
     rd.mesh_write(verts, tris, os.path.join(OUT, "io_mesh.obj"), os.path.join(OUT, "io_mesh.raw"))
+
+
+def lagrange_case(rd):
+    """RATIONAL_4D::evaluateLagrange fields (more top than bottom roots, and
+    more bottom than top) and the Lagrange streaming mesher."""
+    from quijibo_gb300.rootsets import conformal_scale
+    d = {}
+    for tag, (nt, nb, seed) in (("a", (6, 3, 31)), ("b", (3, 5, 32))):
+        rs = draw_rootset(seed, nt, nb, -1.0, 1.0, exps=(1, 2))
+        rs.sigma_top, rs.sigma_bottom = 1.0, 1.0
+        g = Grid((24, 22, 20), slice=0.1)
+        rs.scale = conformal_scale(rs, g)
+        d.update(rs_dict(tag + "_", rs, g, dict(max_it=10, escape=2000.0)))
+        d[tag + "_field"] = rd.field_lagrange(rs, g, 10, 2000.0)
+        d[tag + "_field2"] = rd.field_lagrange(rs, g, 10, 2.0)
+    # the mesher on case a
+    rs = draw_rootset(31, 6, 3, -1.0, 1.0, exps=(1, 2))
+    g = Grid((24, 22, 20), slice=0.1)
+    rs.scale = conformal_scale(rs, g)
+    m = rd.mesh_lagrange(rs, g, 10)
+    d["a_mesh_verts"], d["a_mesh_tris"] = m["verts"], m["tris"]
+    np.savez_compressed(os.path.join(OUT, "lagrange.npz"), **d)
+    return len(m["tris"])
 
 
 def conformal_inputs():

@@ -18,7 +18,7 @@ def test_reference_drivers_link_through_adapter():
     build.build()
     adir = os.path.join(ROOT, "quijibo_gb300", "adapter")
     subprocess.run(["make", "-s", "-j8", "-C", adir, "REF=" + REF], check=True)
-    for exe in ("bunnyMarchingCubes3D_gpu", "toothOptimizer_gpu"):
+    for exe in ("bunnyMarchingCubes3D_gpu", "toothOptimizer_gpu", "lagrangeBunny3D_gpu"):
         path = os.path.join(adir, "_build", exe)
         assert os.path.exists(path)
         syms = subprocess.run(["nm", path], capture_output=True, text=True, check=True).stdout
@@ -26,3 +26,8 @@ def test_reference_drivers_link_through_adapter():
     tooth = subprocess.run(["nm", os.path.join(adir, "_build", "toothOptimizer_gpu")],
                            capture_output=True, text=True, check=True).stdout
     assert "__wrap__ZN11OPTIMIZE_3D14computeScoreAPEv" in tooth
+    lag = subprocess.run(["nm", os.path.join(adir, "_build", "lagrangeBunny3D_gpu")],
+                         capture_output=True, text=True, check=True).stdout
+    # the 10-argument (Lagrange) streaming mesher constructor
+    assert ("__wrap__ZN13TRIANGLE_MESHC1ERK5TVEC3IeES3_RKS0_IiERK13POLYNOMIAL_4DS9_eieeRK10QUATERNION\n"
+            in lag)
