@@ -393,6 +393,29 @@ int qjg_mesh_write_raw(const char* path, const double* verts, int64_t n_verts,
 int qjg_mesh_write_obj(const char* path, const double* verts64, const float* verts32,
                        int64_t n_verts, const int32_t* tris, int64_t n_tris);
 
+/* The optimizer state file (.o3d): OPTIMIZE_3D::write / read
+ * (src/solvers/OPTIMIZE_3D.cpp:3253-3360).  Roots are n x (w,x,y,z); the
+ * fields are the fractal, distance and curvature FIELD_3D streams, in that
+ * order.  The writer stores empty coefficient lists (the power-factored
+ * path never reads them; OPTIMIZE_3D::read accepts them). */
+typedef struct {
+  int32_t res[3];
+  double center[3], lengths[3];
+  int32_t n_top, n_bot;
+  double sigma_top, sigma_bot; /* the polynomials' power scalars */
+  double exp_scaling;
+  int32_t history;             /* length of the (unwritten) optimizer history */
+  int32_t field_res[3][3];
+  double field_center[3][3], field_lengths[3][3];
+} qjg_o3d_info;
+int qjg_o3d_read_info(const char* path, qjg_o3d_info* info);
+/* Host buffers sized from the info; any may be NULL to skip it. */
+int qjg_o3d_read(const char* path, double* top_roots, double* top_powers, double* bot_roots,
+                 double* bot_powers, double* fractal, double* distance, double* curvature);
+int qjg_o3d_write(const char* path, const qjg_o3d_info* info, const double* top_roots,
+                  const double* top_powers, const double* bot_roots, const double* bot_powers,
+                  const double* fractal, const double* distance, const double* curvature);
+
 #ifdef __cplusplus
 }
 #endif

@@ -221,6 +221,8 @@ class Reference:
                                          _dp]
         L.ref_mesh_lagrange.argtypes = [A, _ip, _dp, _dp, _dp, C.c_double, C.c_int, C.c_double,
                                         _dp, C.c_int, _ip, C.c_int, _ip, _ip]
+        L.ref_o3d_write.argtypes = [C.c_char_p, A, _ip, _dp, _dp, _dp, _ip, _dp, _dp, _dp, _dp]
+        L.ref_o3d_read.argtypes = [C.c_char_p, _ip, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
         L.ref_inverted_distance.argtypes = [_ip, _dp, _dp, _dp, C.c_int, _dp]
         L.ref_conformal_radius.argtypes = [A, _ip, _dp, _dp, C.c_double, _ip, _dp, _dp, _dp, _dp]
         L.ref_conformal_radius.restype = C.c_double
@@ -249,6 +251,31 @@ class Reference:
         return self._mesh_out(self.L.ref_mesh_lagrange, C.byref(_map_args(rs)), _ptr(res, _ip),
                               _ptr(c), _ptr(ln), _ptr(r), float(grid.slice), int(max_it),
                               float(iso), n=int(np.prod(grid.res)))
+
+    def o3d_write(self, path, rs, grid, fractal, dgrid, dist, curv):
+        """OPTIMIZE_3D::write of a state (the fractal on grid, the distance and
+        curvature fields on dgrid)."""
+        res, c, ln, _ = self._g(grid)
+        dres, dc, dln, _ = self._g(dgrid)
+        f = lambda a: _ptr(np.ascontiguousarray(a, dtype=np.float64).ravel())  # noqa: E731
+        self.L.ref_o3d_write(str(path).encode(), C.byref(_map_args(rs)), _ptr(res, _ip), _ptr(c),
+                             _ptr(ln), f(fractal), _ptr(dres, _ip), _ptr(dc), _ptr(dln), f(dist),
+                             f(curv))
+
+    def o3d_read(self, path, max_roots=256, max_cells=1 << 20):
+        """OPTIMIZE_3D::read: what the reference takes from a state file."""
+        counts = np.zeros(2, dtype=np.int32)
+        tr, br = np.empty(4 * max_roots), np.empty(4 * max_roots)
+        tp, bp = np.empty(max_roots), np.empty(max_roots)
+        sc = np.empty(3)
+        fr, di = np.empty(max_cells), np.empty(max_cells)
+        self.L.ref_o3d_read(str(path).encode(), _ptr(counts, _ip), _ptr(tr), _ptr(tp), _ptr(br),
+                            _ptr(bp), _ptr(sc), _ptr(fr), _ptr(di))
+        nt, nb = int(counts[0]), int(counts[1])
+        return {"top_roots": tr[:4 * nt].reshape(-1, 4), "top_powers": tp[:nt],
+                "bottom_roots": br[:4 * nb].reshape(-1, 4), "bottom_powers": bp[:nb],
+                "sigma_top": sc[0], "sigma_bottom": sc[1], "scale": sc[2], "fractal": fr,
+                "dist": di}
 
     def inverted_distance(self, grid, dist, normalized=False):
         """FIELD_3D::invertedDistance[Normalized] of `dist` (x fastest)."""

@@ -287,6 +287,57 @@ double ref_conformal_radius(const MapArgs* a, const int* res, const double* cent
   return score;
 }
 
+// OPTIMIZE_3D::write (OPTIMIZE_3D.cpp:3253-3297) of a state: the map, the
+// fractal on (res, center, lengths), distance and curvature on (dres, ...).
+void ref_o3d_write(const char* path, const MapArgs* a, const int* res, const double* center,
+                   const double* lengths, const double* fractal, const int* dres,
+                   const double* dcenter, const double* dlengths, const double* dist,
+                   const double* curv) {
+  OPTIMIZE_3D opt(res[0], res[1], res[2], VEC3F(center[0], center[1], center[2]),
+                  VEC3F(lengths[0], lengths[1], lengths[2]));
+  opt.top() = make_poly(a->nt, a->troots, a->tpows, a->tsig);
+  opt.bottom() = make_poly(a->nb, a->broots, a->bpows, a->bsig);
+  opt.expScaling() = a->s;
+  for (int i = 0; i < opt.fractal().totalCells(); i++) opt.fractal()[i] = fractal[i];
+  FIELD_3D d(dres[0], dres[1], dres[2], VEC3F(dcenter[0], dcenter[1], dcenter[2]),
+             VEC3F(dlengths[0], dlengths[1], dlengths[2]));
+  FIELD_3D c = d;
+  for (int i = 0; i < d.totalCells(); i++) {
+    d[i] = dist[i];
+    c[i] = curv[i];
+  }
+  opt.distanceField() = d;
+  opt.curvatureField() = c;
+  opt.write(std::string(path));
+}
+
+// OPTIMIZE_3D::read (OPTIMIZE_3D.cpp:3302-3360) of a state: counts,
+// roots (w,x,y,z), powers, power scalars, expScaling; the fractal and the
+// distance field data.
+void ref_o3d_read(const char* path, int* counts, double* troots, double* tpows, double* broots,
+                  double* bpows, double* scalars, double* fractal, double* dist) {
+  OPTIMIZE_3D opt;
+  opt.read(std::string(path));
+  const POLYNOMIAL_4D& t = opt.top();
+  const POLYNOMIAL_4D& b = opt.bottom();
+  counts[0] = t.totalRoots();
+  counts[1] = b.totalRoots();
+  for (int i = 0; i < t.totalRoots(); i++) {
+    for (int c = 0; c < 4; c++) troots[4 * i + c] = (double)t.roots()[i][c];
+    tpows[i] = (double)t.powers()[i];
+  }
+  for (int i = 0; i < b.totalRoots(); i++) {
+    for (int c = 0; c < 4; c++) broots[4 * i + c] = (double)b.roots()[i][c];
+    bpows[i] = (double)b.powers()[i];
+  }
+  scalars[0] = (double)t.powerScalar();
+  scalars[1] = (double)b.powerScalar();
+  scalars[2] = (double)opt.expScaling();
+  for (int i = 0; i < opt.fractal().totalCells(); i++) fractal[i] = (double)opt.fractal()[i];
+  for (int i = 0; i < opt.distanceField().totalCells(); i++)
+    dist[i] = (double)opt.distanceField()[i];
+}
+
 // FIELD_3D::write(string) of a field (FIELD_3D.cpp:280-300, 4371-4393).
 void ref_field_write(const char* path, const int* res, const double* center,
                      const double* lengths, const double* data) {

@@ -214,3 +214,141 @@ int qjg_mesh_write_obj(const char* path, const double* verts64, const float* ver
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- .o3d
+// OPTIMIZE_3D::write / read (src/solvers/OPTIMIZE_3D.cpp:3253-3360): int
+// xRes, yRes, zRes; VEC3 center, lengths; top and bottom POLYNOMIAL_4D
+// (POLYNOMIAL_4D.cpp:650-727: int totalRoots; coefficient, derivative and
+// second-derivative quaternion lists, each an int count then 4 doubles w x y
+// z per entry; the roots likewise; an int count then totalRoots doubles of
+// powers; the power scalar); double expScaling; int history count; then the
+// fractal, distance and curvature FIELD_3D streams.
+
+namespace {
+
+constexpr int32_t kMaxRoots = 1 << 20;
+constexpr int32_t kMaxList = 1 << 28;
+
+struct Reader {
+  FILE* f;
+  bool ok = true;
+  template <class T>
+  T get() {
+    T v{};
+    if (ok && std::fread(&v, sizeof v, 1, f) != 1) ok = false;
+    return v;
+  }
+  void get_n(double* dst, int64_t n) {
+    if (!ok || n <= 0) return;
+    if (dst) {
+      if (std::fread(dst, sizeof(double), (size_t)n, f) != (size_t)n) ok = false;
+    } else if (std::fseek(f, (long)(n * (int64_t)sizeof(double)), SEEK_CUR) != 0) {
+      ok = false;
+    }
+  }
+};
+
+// One polynomial; roots (n x 4) and powers (n) are copied when not null.
+bool read_poly(Reader& r, int32_t* n, double* sigma, double* roots, double* powers) {
+  const int32_t total = r.get<int32_t>();
+  if (!r.ok || total < 0 || total > kMaxRoots) return false;
+  for (int list = 0; list < 3; list++) {  // coefficients, derivatives, second derivatives
+    const int32_t c = r.get<int32_t>();
+    if (!r.ok || c < 0 || c > kMaxList) return false;
+    r.get_n(nullptr, 4ll * c);
+  }
+  const int32_t nr = r.get<int32_t>();
+  if (!r.ok || nr < 0 || nr > kMaxRoots) return false;
+  r.get_n(nr == total ? roots : nullptr, 4ll * nr);
+  if (nr != total && roots) return false;
+  r.get<int32_t>();  // the powers' count; the reader takes totalRoots of them
+  r.get_n(powers, total);
+  const double ps = r.get<double>();
+  if (n) *n = total;
+  if (sigma) *sigma = ps;
+  return r.ok;
+}
+
+bool read_field_header(Reader& r, int32_t res[3], double c[3], double l[3]) {
+  for (int k = 0; k < 3; k++) res[k] = r.get<int32_t>();
+  for (int k = 0; k < 3; k++) c[k] = r.get<double>();
+  for (int k = 0; k < 3; k++) l[k] = r.get<double>();
+  return r.ok;
+}
+
+int64_t cells(const int32_t res[3]) {
+  return (res[0] > 0 && res[1] > 0 && res[2] > 0) ? (int64_t)res[0] * res[1] * res[2] : 0;
+}
+
+int read_o3d(const char* path, qjg_o3d_info* info, double* top_roots, double* top_powers,
+             double* bot_roots, double* bot_powers, double* fields[3]) {
+  if (!path || !info) return QJG_ERR_ARG;
+  File in(path, "rb");
+  if (!in.f) return QJG_ERR_ARG;
+  Reader r{in.f};
+  for (int k = 0; k < 3; k++) info->res[k] = r.get<int32_t>();
+  for (int k = 0; k < 3; k++) info->center[k] = r.get<double>();
+  for (int k = 0; k < 3; k++) info->lengths[k] = r.get<double>();
+  if (!r.ok) return QJG_ERR_ARG;
+  if (!read_poly(r, &info->n_top, &info->sigma_top, top_roots, top_powers) ||
+      !read_poly(r, &info->n_bot, &info->sigma_bot, bot_roots, bot_powers))
+    return QJG_ERR_ARG;
+  info->exp_scaling = r.get<double>();
+  info->history = r.get<int32_t>();
+  for (int k = 0; k < 3; k++) {
+    if (!read_field_header(r, info->field_res[k], info->field_center[k], info->field_lengths[k]))
+      return QJG_ERR_ARG;
+    r.get_n(fields ? fields[k] : nullptr, cells(info->field_res[k]));
+  }
+  return r.ok ? QJG_OK : QJG_ERR_ARG;
+}
+
+bool write_poly(File& out, int32_t n, const double* roots, const double* powers, double sigma) {
+  const int32_t zero = 0;
+  bool ok = out.put(&n, 4);
+  for (int list = 0; list < 3; list++) ok = ok && out.put(&zero, 4);
+  ok = ok && out.put(&n, 4) && (n == 0 || out.put(roots, (size_t)n * 32));
+  ok = ok && out.put(&n, 4) && (n == 0 || out.put(powers, (size_t)n * 8));
+  return ok && out.put(&sigma, 8);
+}
+
+}  // namespace
+
+extern "C" {
+
+int qjg_o3d_read_info(const char* path, qjg_o3d_info* info) {
+  return read_o3d(path, info, nullptr, nullptr, nullptr, nullptr, nullptr);
+}
+
+int qjg_o3d_read(const char* path, double* top_roots, double* top_powers, double* bot_roots,
+                 double* bot_powers, double* fractal, double* distance, double* curvature) {
+  qjg_o3d_info info;
+  double* fields[3] = {fractal, distance, curvature};
+  return read_o3d(path, &info, top_roots, top_powers, bot_roots, bot_powers, fields);
+}
+
+int qjg_o3d_write(const char* path, const qjg_o3d_info* info, const double* top_roots,
+                  const double* top_powers, const double* bot_roots, const double* bot_powers,
+                  const double* fractal, const double* distance, const double* curvature) {
+  if (!path || !info || info->n_top < 0 || info->n_bot < 0 ||
+      (info->n_top && (!top_roots || !top_powers)) || (info->n_bot && (!bot_roots || !bot_powers)))
+    return QJG_ERR_ARG;
+  const double* fields[3] = {fractal, distance, curvature};
+  for (int k = 0; k < 3; k++)
+    if (cells(info->field_res[k]) > 0 && !fields[k]) return QJG_ERR_ARG;
+  File out(path, "wb");
+  if (!out.f) return QJG_ERR_ARG;
+  bool ok = out.put(info->res, 12) && out.put(info->center, 24) && out.put(info->lengths, 24);
+  ok = ok && write_poly(out, info->n_top, top_roots, top_powers, info->sigma_top);
+  ok = ok && write_poly(out, info->n_bot, bot_roots, bot_powers, info->sigma_bot);
+  ok = ok && out.put(&info->exp_scaling, 8) && out.put(&info->history, 4);
+  for (int k = 0; k < 3 && ok; k++) {
+    ok = out.put(info->field_res[k], 12) && out.put(info->field_center[k], 24) &&
+         out.put(info->field_lengths[k], 24);
+    const int64_t n = cells(info->field_res[k]);
+    if (ok && n > 0) ok = out.put(fields[k], (size_t)n * 8);
+  }
+  return ok ? QJG_OK : QJG_ERR_ARG;
+}
+
+}  // extern "C"

@@ -51,6 +51,14 @@ class QjgFieldStats(C.Structure):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}
 
 
+class QjgO3dInfo(C.Structure):
+    _fields_ = [("res", C.c_int32 * 3), ("center", C.c_double * 3), ("lengths", C.c_double * 3),
+                ("n_top", C.c_int32), ("n_bot", C.c_int32), ("sigma_top", C.c_double),
+                ("sigma_bot", C.c_double), ("exp_scaling", C.c_double), ("history", C.c_int32),
+                ("field_res", (C.c_int32 * 3) * 3), ("field_center", (C.c_double * 3) * 3),
+                ("field_lengths", (C.c_double * 3) * 3)]
+
+
 QJG_EDGE_LINEAR, QJG_EDGE_BISECT = 0, 1
 
 
@@ -156,6 +164,9 @@ EXPORTS = {
     "qjg_mesh_write_raw": ([C.c_char_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64], C.c_int),
     "qjg_mesh_write_obj": ([C.c_char_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64],
                            C.c_int),
+    "qjg_o3d_read_info": ([C.c_char_p, C.POINTER(QjgO3dInfo)], C.c_int),
+    "qjg_o3d_read": ([C.c_char_p] + [C.c_void_p] * 7, C.c_int),
+    "qjg_o3d_write": ([C.c_char_p, C.POINTER(QjgO3dInfo)] + [C.c_void_p] * 7, C.c_int),
     "qjg_server_create": ([C.c_int, C.c_int32, C.c_int64, C.POINTER(C.c_void_p)], C.c_int),
     "qjg_server_destroy": ([C.c_void_p], None),
     "qjg_server_submit": ([C.c_void_p, C.POINTER(QjgRequest), C.POINTER(C.c_int64)], C.c_int),
@@ -263,6 +274,67 @@ def mesh_write_obj(path, verts, tris, n_verts=None, n_tris=None, fp32=None):
     _io_check(load().qjg_mesh_write_obj(str(path).encode(), C.c_void_p(v64), C.c_void_p(v32),
                                         n_verts, C.c_void_p(_addr(tris)), n_tris),
               "qjg_mesh_write_obj")
+
+
+FIELD_NAMES = ("fractal", "distance", "curvature")
+
+
+def o3d_read(path):
+    """An optimizer state file: dict with the RootSet fields, the grid
+    (res, center, lengths), exp scaling, history count and the three fields
+    as (res, center, lengths, data[Z, Y, X])."""
+    L = load()
+    info = QjgO3dInfo()
+    _io_check(L.qjg_o3d_read_info(str(path).encode(), C.byref(info)), "qjg_o3d_read_info")
+    nt, nb = info.n_top, info.n_bot
+    tr, tp = np.empty((nt, 4)), np.empty(nt)
+    br, bp = np.empty((nb, 4)), np.empty(nb)
+    fields = []
+    for k in range(3):
+        res = tuple(info.field_res[k])
+        n = int(np.prod(res)) if min(res) > 0 else 0
+        fields.append((res, tuple(info.field_center[k]), tuple(info.field_lengths[k]),
+                       np.empty(res[::-1] if n else 0)))
+    p = lambda a: C.c_void_p(a.ctypes.data if a.size else 0)  # noqa: E731
+    _io_check(L.qjg_o3d_read(str(path).encode(), p(tr), p(tp), p(br), p(bp),
+                             *[p(f[3]) for f in fields]), "qjg_o3d_read")
+    return {"top_roots": tr, "top_powers": tp, "sigma_top": info.sigma_top,
+            "bottom_roots": br, "bottom_powers": bp, "sigma_bottom": info.sigma_bot,
+            "scale": info.exp_scaling, "res": tuple(info.res), "center": tuple(info.center),
+            "lengths": tuple(info.lengths), "history": info.history,
+            **{name: f for name, f in zip(FIELD_NAMES, fields)}}
+
+
+def o3d_write(path, rs, grid_res, center, lengths, fields, history=0):
+    """Write a state file; `fields` maps fractal / distance / curvature to
+    (res, center, lengths, data) (missing ones are written empty)."""
+    info = QjgO3dInfo()
+    info.res[:] = [int(v) for v in grid_res]
+    info.center[:] = list(center)
+    info.lengths[:] = list(lengths)
+    info.n_top, info.n_bot = rs.n_top, rs.n_bottom
+    info.sigma_top, info.sigma_bot, info.exp_scaling = rs.sigma_top, rs.sigma_bottom, rs.scale
+    info.history = history
+    keep = []
+
+    def arr(a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        keep.append(a)
+        return C.c_void_p(a.ctypes.data if a.size else 0)
+
+    data = []
+    for k, name in enumerate(FIELD_NAMES):
+        if name in fields:
+            res, c, ln, d = fields[name]
+            info.field_res[k][:] = [int(v) for v in res]
+            info.field_center[k][:] = list(c)
+            info.field_lengths[k][:] = list(ln)
+            data.append(arr(d))
+        else:
+            data.append(C.c_void_p(0))
+    _io_check(load().qjg_o3d_write(str(path).encode(), C.byref(info), arr(rs.top_roots),
+                                   arr(rs.top_powers), arr(rs.bottom_roots), arr(rs.bottom_powers),
+                                   *data), "qjg_o3d_write")
 
 
 def set_field32_pairs(on):

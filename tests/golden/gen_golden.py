@@ -105,6 +105,7 @@ def main():
     io_case(rd)
     conformal_case(rd)
     lagrange_case(rd)
+    o3d_case(rd)
 
     print("stream: %d verts %d tris; nonlinear: %d/%d; linear: %d/%d" % (
         len(ms["verts"]), len(ms["tris"]), len(mn["verts"]), len(mn["tris"]), len(ml["verts"]),
@@ -154,6 +155,26 @@ def lagrange_case(rd):
     d["a_mesh_verts"], d["a_mesh_tris"] = m["verts"], m["tris"]
     np.savez_compressed(os.path.join(OUT, "lagrange.npz"), **d)
     return len(m["tris"])
+
+
+def o3d_inputs():
+    """A small optimizer state: map, fractal, distance (with a sign change)
+    and curvature fields."""
+    rs = draw_rootset(41, 4, 2, -1.0, 1.0, exps=(1, 2))
+    rs.sigma_top, rs.sigma_bottom, rs.scale = 1.25, 0.75, 0.625
+    g = Grid((6, 5, 4), center=(0.1, -0.2, 0.3), lengths=(3.0, 2.5, 2.0))
+    dg = Grid((5, 4, 3), center=(0.0, 0.05, -0.05), lengths=(2.5, 2.0, 1.5))
+    rng = np.random.RandomState(41)
+    fractal = rng.standard_normal(g.n_voxels)
+    dist = np.linspace(-1.0, 1.0, dg.n_voxels) + 0.013
+    curv = rng.uniform(-2, 2, dg.n_voxels)
+    return rs, g, fractal, dg, dist, curv
+
+
+def o3d_case(rd):
+    """OPTIMIZE_3D::write of o3d_inputs()."""
+    rs, g, fractal, dg, dist, curv = o3d_inputs()
+    rd.o3d_write(os.path.join(OUT, "io_state.o3d"), rs, g, fractal, dg, dist, curv)
 
 
 def conformal_inputs():

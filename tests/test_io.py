@@ -1,6 +1,6 @@
 """File formats against the bytes the reference's own writers produce
 (tests/golden/io_*, made by gen_golden.py through FIELD_3D::write,
-TRIANGLE_MESH::writeOBJ and TRIANGLE_MESH::write)."""
+TRIANGLE_MESH::writeOBJ, TRIANGLE_MESH::write and OPTIMIZE_3D::write)."""
 import os
 import sys
 
@@ -123,3 +123,52 @@ def test_writers_take_device_buffers(tmp_path):
                               back.numel()) == 0
     torch.cuda.synchronize()
     assert torch.equal(back.view(torch.int64), fd.view(torch.int64))
+
+
+def test_o3d_reader_takes_the_reference_state_file():
+    from gen_golden import o3d_inputs
+    rs, g, fractal, dg, dist, curv = o3d_inputs()
+    st = lib.o3d_read(os.path.join(GOLDEN, "io_state.o3d"))
+    np.testing.assert_array_equal(st["top_roots"], rs.top_roots)
+    np.testing.assert_array_equal(st["top_powers"], rs.top_powers)
+    np.testing.assert_array_equal(st["bottom_roots"], rs.bottom_roots)
+    np.testing.assert_array_equal(st["bottom_powers"], rs.bottom_powers)
+    assert (st["sigma_top"], st["sigma_bottom"], st["scale"]) == (1.25, 0.75, 0.625)
+    assert st["res"] == g.res and st["center"] == g.center and st["lengths"] == g.lengths
+    for name, grid, data in (("fractal", g, fractal), ("distance", dg, dist),
+                             ("curvature", dg, curv)):
+        res, c, ln, f = st[name]
+        assert res == grid.res and c == grid.center and ln == grid.lengths
+        np.testing.assert_array_equal(f.ravel(), data)
+
+
+def test_o3d_writer_round_trips(tmp_path):
+    from gen_golden import o3d_inputs
+    rs, g, fractal, dg, dist, curv = o3d_inputs()
+    out = tmp_path / "s.o3d"
+    lib.o3d_write(out, rs, g.res, g.center, g.lengths,
+                  {"fractal": (g.res, g.center, g.lengths, fractal),
+                   "distance": (dg.res, dg.center, dg.lengths, dist),
+                   "curvature": (dg.res, dg.center, dg.lengths, curv)})
+    st = lib.o3d_read(out)
+    np.testing.assert_array_equal(st["top_roots"], rs.top_roots)
+    np.testing.assert_array_equal(st["distance"][3].ravel(), dist)
+    # the reference's own reader takes it too (where the reference is built)
+    from oracle.oracle import REF_SO, Reference
+    if not os.path.exists(REF_SO["double"]):
+        pytest.skip("reference not built here")
+    ref = Reference("double").o3d_read(out)
+    np.testing.assert_array_equal(ref["top_roots"], rs.top_roots)
+    np.testing.assert_array_equal(ref["bottom_powers"], rs.bottom_powers)
+    assert (ref["sigma_top"], ref["sigma_bottom"], ref["scale"]) == (1.25, 0.75, 0.625)
+    # (OPTIMIZE_3D::read rebuilds its fractal from the score fields, so only
+    # the distance field survives as stored)
+    np.testing.assert_array_equal(ref["dist"][:dg.n_voxels], dist)
+
+
+def test_o3d_reader_rejects_truncated_files(tmp_path):
+    data = open(os.path.join(GOLDEN, "io_state.o3d"), "rb").read()
+    out = tmp_path / "cut.o3d"
+    out.write_bytes(data[:len(data) // 2])
+    with pytest.raises(lib.QjgError):
+        lib.o3d_read(out)
