@@ -558,15 +558,37 @@ __device__ __forceinline__ q32x2::Q2 product32x2(const MapParams& m, const q32x2
   return r;
 }
 
-template <bool DE>
+// product32x2 over a compile-time count N of roots from index LO: the same
+// association, fully unrolled, so every root's constants sit at a fixed
+// offset of the parameter bank.
+template <bool DE, int LO, int N>
+__device__ __forceinline__ q32x2::Q2 product32x2_fixed(const MapParams& m, const q32x2::Q2& q,
+                                                       q32x2::Q2& g) {
+  using namespace q32x2;
+  Q2 r = root_term32x2<DE>(m, q, LO, g);
+#pragma unroll
+  for (int k = 1; k + 1 < N; k += 2) {
+    const Q2 t0 = root_term32x2<DE>(m, q, LO + k, g);
+    const Q2 t1 = root_term32x2<DE>(m, q, LO + k + 1, g);
+    r = qmul(r, qmul(t0, t1));
+  }
+  if (N % 2 == 0) r = qmul(r, root_term32x2<DE>(m, q, LO + N - 1, g));
+  return r;
+}
+
+// NT, NB > 0: the root counts are compile-time constants (they must equal
+// m.nt and m.nb); 0: read from m.
+template <bool DE, int NT = 0, int NB = 0>
 __device__ __forceinline__ q32x2::Q2 apply32x2(const MapParams& m, const q32x2::Q2& q,
                                                float2* g2) {
   using namespace q32x2;
   Q2 g = {pair(0.f), pair(0.f), pair(0.f), pair(0.f)};
-  const Q2 top = product32x2<DE>(m, q, 0, m.nt, g);
+  const Q2 top = NT > 0 ? product32x2_fixed<DE, 0, (NT > 0 ? NT : 1)>(m, q, g)
+                        : product32x2<DE>(m, q, 0, m.nt, g);
   Q2 out;
-  if (m.nb > 0) {
-    const Q2 bot = product32x2<DE>(m, q, m.nt, m.nt + m.nb, g);
+  if (NT > 0 ? NB > 0 : m.nb > 0) {
+    const Q2 bot = NT > 0 ? product32x2_fixed<DE, (NT > 0 ? NT : 0), (NB > 0 ? NB : 1)>(m, q, g)
+                          : product32x2<DE>(m, q, m.nt, m.nt + m.nb, g);
     const float2 n = norm2(bot);
     const float2 inv =
         mul2(pair(m.scalef), make_float2(q32::rcp_approx(n.x), q32::rcp_approx(n.y)));
