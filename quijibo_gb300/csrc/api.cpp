@@ -175,6 +175,10 @@ void qjg_destroy(qjg_ctx* ctx) {
   cudaFree(ctx->d_keys);
   cudaFree(ctx->d_hist);
   cudaFree(ctx->d_ff);
+  if (ctx->h_stats) cudaFreeHost(ctx->h_stats);
+  for (cudaEvent_t e : ctx->chunk_ev)
+    if (e) cudaEventDestroy(e);
+  if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
   cudaFree(ctx->d_field);
   cudaFree(ctx->d_de);
   cudaFree(ctx->d_mstats);
@@ -304,39 +308,66 @@ int qjg_field_host(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg
   if ((rc = qj_check_grid(ctx, grid)) || (rc = qj_check_iter(ctx, iter))) return rc;
   if (!host_field) return fail(ctx, QJG_ERR_ARG, "host_field is NULL");
   const int64_t slab = (int64_t)grid->res[0] * grid->res[1];
-  // slices per chunk: at most 2^31 voxels and 1 GiB of field per chunk
-  int64_t chunk = std::max<int64_t>(1, std::min<int64_t>((int64_t)1 << 31, (int64_t)1 << 27) / slab);
-  chunk = std::min<int64_t>(chunk, grid->res[2]);
+  // chunks of slices, computed on ctx->stream into two alternating device
+  // buffers while the previous chunk copies out on ctx->copy_stream: about
+  // eight chunks of at least 2^22 voxels, at most 2^27 voxels each
+  const int64_t Z = grid->res[2];
+  int64_t chunk = std::max<int64_t>((Z + 7) / 8, ((int64_t)1 << 22) / slab);
+  chunk = std::max<int64_t>(1, std::min<int64_t>(chunk, ((int64_t)1 << 27) / slab));
+  chunk = std::min<int64_t>(chunk, Z);
+  const int64_t n_chunks = (Z + chunk - 1) / chunk;
   QJ_CUDA(ctx, cudaSetDevice(ctx->device));
-  if ((rc = ensure(ctx, &ctx->d_field, &ctx->buf_cap, (size_t)(chunk * slab)))) return rc;
-  if (host_de) {
-    cudaFree(ctx->d_de);
-    ctx->d_de = nullptr;
-    QJ_CUDA(ctx, cudaMalloc((void**)&ctx->d_de, (size_t)(chunk * slab) * sizeof(float)));
+  if ((rc = ensure(ctx, &ctx->d_field, &ctx->buf_cap, (size_t)(2 * chunk * slab)))) return rc;
+  if (host_de && (rc = ensure(ctx, &ctx->d_de, &ctx->de_cap, (size_t)(2 * chunk * slab))))
+    return rc;
+  if (!ctx->copy_stream)
+    QJ_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+  for (cudaEvent_t& e : ctx->chunk_ev)
+    if (!e) QJ_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  if (ctx->h_stats_cap < (size_t)n_chunks) {
+    if (ctx->h_stats) cudaFreeHost(ctx->h_stats);
+    ctx->h_stats = nullptr;
+    ctx->h_stats_cap = 0;
+    QJ_CUDA(ctx, cudaMallocHost((void**)&ctx->h_stats, (size_t)n_chunks * sizeof(DevStats)));
+    ctx->h_stats_cap = (size_t)n_chunks;
   }
-  qjg_field_stats total = {};
-  for (int64_t z0 = 0; z0 < grid->res[2]; z0 += chunk) {
-    const int64_t z1 = std::min<int64_t>(z0 + chunk, grid->res[2]);
-    if ((rc = qjg_field(ctx, rs, grid, iter, (int32_t)z0, (int32_t)z1, ctx->d_field,
-                        host_de ? ctx->d_de : nullptr, ctx->stream)))
-      return rc;
+  cudaStream_t cs = ctx->stream, xs = ctx->copy_stream;
+  for (int64_t k = 0; k < n_chunks; k++) {
+    const int64_t z0 = k * chunk, z1 = std::min<int64_t>(z0 + chunk, Z);
+    const int b = (int)(k & 1);
+    double* df = ctx->d_field + (size_t)b * chunk * slab;
+    float* dd = host_de ? ctx->d_de + (size_t)b * chunk * slab : nullptr;
+    // the buffer's previous chunk must have left the device
+    if (k >= 2) QJ_CUDA(ctx, cudaStreamWaitEvent(cs, ctx->chunk_ev[2 + b], 0));
+    if ((rc = qjg_field(ctx, rs, grid, iter, (int32_t)z0, (int32_t)z1, df, dd, cs))) return rc;
+    QJ_CUDA(ctx, cudaMemcpyAsync(ctx->h_stats + k, ctx->d_stats, sizeof(DevStats),
+                                 cudaMemcpyDeviceToHost, cs));
+    QJ_CUDA(ctx, cudaEventRecord(ctx->chunk_ev[b], cs));
+    QJ_CUDA(ctx, cudaStreamWaitEvent(xs, ctx->chunk_ev[b], 0));
     const size_t nb = (size_t)((z1 - z0) * slab);
-    QJ_CUDA(ctx, cudaMemcpyAsync(host_field + z0 * slab, ctx->d_field, nb * sizeof(double),
-                                 cudaMemcpyDeviceToHost, ctx->stream));
+    QJ_CUDA(ctx, cudaMemcpyAsync(host_field + z0 * slab, df, nb * sizeof(double),
+                                 cudaMemcpyDeviceToHost, xs));
     if (host_de)
-      QJ_CUDA(ctx, cudaMemcpyAsync(host_de + z0 * slab, ctx->d_de, nb * sizeof(float),
-                                   cudaMemcpyDeviceToHost, ctx->stream));
-    qjg_field_stats st;
-    if ((rc = qjg_field_stats_read(ctx, ctx->stream, &st))) return rc;
-    total.voxels += st.voxels;
-    total.voxel_iters += st.voxel_iters;
-    total.root_terms += st.root_terms;
-    total.refined += st.refined;
-    total.refined_iters += st.refined_iters;
-    total.nonfinite += st.nonfinite;
-    total.lane_iters += st.lane_iters;
-    total.rerun += st.rerun;
-    total.rerun_iters += st.rerun_iters;
+      QJ_CUDA(ctx, cudaMemcpyAsync(host_de + z0 * slab, dd, nb * sizeof(float),
+                                   cudaMemcpyDeviceToHost, xs));
+    QJ_CUDA(ctx, cudaEventRecord(ctx->chunk_ev[2 + b], xs));
+  }
+  QJ_CUDA(ctx, cudaStreamSynchronize(cs));
+  QJ_CUDA(ctx, cudaStreamSynchronize(xs));
+  qjg_field_stats total = {};
+  const int roots = ctx->last_roots;
+  for (int64_t k = 0; k < n_chunks; k++) {
+    const DevStats& st = ctx->h_stats[k];
+    const int64_t z0 = k * chunk, z1 = std::min<int64_t>(z0 + chunk, Z);
+    total.voxels += (z1 - z0) * slab;
+    total.voxel_iters += (int64_t)st.voxel_iters;
+    total.root_terms += (int64_t)st.voxel_iters * roots;
+    total.refined += (int64_t)st.refined;
+    total.refined_iters += (int64_t)st.aux[0];
+    total.nonfinite += (int64_t)st.nonfinite;
+    total.lane_iters += (int64_t)st.aux[3];
+    total.rerun += (int64_t)st.rerun;
+    total.rerun_iters += (int64_t)st.rerun_iters;
   }
   if (stats) *stats = total;
   return QJG_OK;

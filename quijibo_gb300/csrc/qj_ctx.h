@@ -27,9 +27,14 @@ struct qjg_ctx {
   size_t hist_cap = 0;
   uint32_t* d_ff = nullptr;     // double-float re-run list
   size_t ff_cap = 0;
-  double* d_field = nullptr;    // staging for host-buffer calls
+  double* d_field = nullptr;    // staging for host-buffer calls: two chunk buffers
   float* d_de = nullptr;
   size_t buf_cap = 0;
+  size_t de_cap = 0;
+  cudaStream_t copy_stream = nullptr;  // host-buffer calls: copies beside the compute stream
+  cudaEvent_t chunk_ev[4] = {nullptr, nullptr, nullptr, nullptr};  // computed / copied, per buffer
+  qj::DevStats* h_stats = nullptr;     // pinned per-chunk counters
+  size_t h_stats_cap = 0;
   cudaStream_t stream = nullptr;  // internal stream of host-buffer calls
   // bookkeeping of the last field call, for qjg_field_stats_read
   int64_t last_voxels = 0;
