@@ -38,7 +38,24 @@ void rotation_matrix(const double q[4], double R[3][3]) {
   R[2][2] = 1 - 2 * x * x - 2 * y * y;
 }
 
+// The device address of a page-locked (cudaHostAlloc / cudaHostRegister)
+// host buffer, or null for other memory.
+void* mapped_host(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 }  // namespace
+
+// scratch target for stats nobody asked for
+static qjg_field_stats& total_sink(qjg_ctx*) {
+  static thread_local qjg_field_stats sink;
+  return sink;
+}
 
 int qj_check_grid(qjg_ctx* ctx, const qjg_grid* g) {
   if (!g) return fail(ctx, QJG_ERR_ARG, "grid is NULL");
@@ -317,6 +334,17 @@ int qjg_field_host(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg
   chunk = std::min<int64_t>(chunk, Z);
   const int64_t n_chunks = (Z + chunk - 1) / chunk;
   QJ_CUDA(ctx, cudaSetDevice(ctx->device));
+  // page-locked host buffers are mapped into the device's address space: the
+  // kernels then write the field straight into them (over NVLink-C2C on a
+  // Grace host) and nothing is staged or copied
+  void* df_mapped = mapped_host(host_field);
+  void* dd_mapped = host_de ? mapped_host(host_de) : nullptr;
+  if (df_mapped && (!host_de || dd_mapped) && slab * Z <= (int64_t)UINT32_MAX) {
+    if ((rc = qjg_field(ctx, rs, grid, iter, 0, (int32_t)Z, (double*)df_mapped, (float*)dd_mapped,
+                        ctx->stream)))
+      return rc;
+    return qjg_field_stats_read(ctx, ctx->stream, stats ? stats : &total_sink(ctx));
+  }
   if ((rc = ensure(ctx, &ctx->d_field, &ctx->buf_cap, (size_t)(2 * chunk * slab)))) return rc;
   if (host_de && (rc = ensure(ctx, &ctx->d_de, &ctx->de_cap, (size_t)(2 * chunk * slab))))
     return rc;

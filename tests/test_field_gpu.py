@@ -194,3 +194,23 @@ def test_fp32_refine_rel_tol_bounds_field_error(ctx, wl, res):
     assert rel_err(tight, f64).max() <= 1e-6
     assert st["rerun"] > 0 and st["rerun_iters"] > 0
     assert st["refined"] >= sb["refined"]
+
+
+def test_host_entry_point_pinned_and_pageable_buffers_agree(ctx):
+    """Page-locked output buffers are written in place by the kernels,
+    pageable ones through the chunked copy pipeline: same bits."""
+    torch = pytest.importorskip("torch")
+    rs, g, p = precision_workload(72)
+    h = ctx.upload(rs)
+    it = ctx.iter_params(p["max_it"], p["escape"], precision=lib.QJG_FP32_REFINE,
+                         refine_pow=lib.QJG_REFINE_INT, want_de=True, rel_tol=1e-6)
+    a, da, sa = ctx.field_host(h, g, it, de=True)
+    pinned = torch.empty(g.n_voxels, dtype=torch.float64, pin_memory=True)
+    pinned_de = torch.empty(g.n_voxels, dtype=torch.float32, pin_memory=True)
+    b, db, sb = ctx.field_host(h, g, it, de=True, out=pinned.numpy().reshape(g.res[::-1]),
+                               de_out=pinned_de.numpy().reshape(g.res[::-1]))
+    ctx.free(h)
+    assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+    assert np.array_equal(da.view(np.uint32), db.view(np.uint32))
+    for k in ("voxels", "voxel_iters", "refined", "rerun"):
+        assert sa[k] == sb[k], k
