@@ -626,9 +626,9 @@ __global__ void __launch_bounds__(128) edge_start_kernel(const __grid_constant__
       bool bad = false;
       wait = edge_advance<POW_REF>(m, g, it, s, iso, verts + 3 * (id0 + k), &bad, &e32);
       nbad += bad;
-      if (wait) es[k] = s;
+      if (wait) es[id0 + k] = s;
     }
-    warp_push(wait, (uint32_t)k, n_park, park);
+    warp_push(wait, (uint32_t)(id0 + k), n_park, park);
   }
   edge_counts(e32, 0, nbad, st);
 }
@@ -661,7 +661,6 @@ __global__ void __launch_bounds__(128) edge_resume_kernel(const __grid_constant_
                                                           const GridParams g, const IterParams it,
                                                           const uint32_t* __restrict__ park,
                                                           const unsigned long long* n_park,
-                                                          long long id0,
                                                           EdgeState* __restrict__ es,
                                                           double* __restrict__ verts, double iso,
                                                           uint32_t* next,
@@ -679,7 +678,7 @@ __global__ void __launch_bounds__(128) edge_resume_kernel(const __grid_constant_
       k = park[j];
       EdgeState s = es[k];
       bool bad = false;
-      wait = edge_advance<POW_REF>(m, g, it, s, iso, verts + 3 * (id0 + k), &bad, &e32);
+      wait = edge_advance<POW_REF>(m, g, it, s, iso, verts + 3 * (long long)k, &bad, &e32);
       nbad += bad;
       if (wait) es[k] = s;
     }
@@ -741,16 +740,23 @@ cudaError_t mesh_vertex_ids(MeshWindow& w, int j0, int j1, int lay_lo, int lay_h
 }
 
 template <bool POW_REF>
-static cudaError_t parked_vertices(const MapParams& m, const GridParams& g, const IterParams& it,
-                                   const MeshWindow& w, long long n, long long id0, int c0,
-                                   double* verts, double iso, DevStats* st,
-                                   const EdgeScratch& sc, cudaStream_t s) {
+static cudaError_t parked_start(const MapParams& m, const GridParams& g, const IterParams& it,
+                                const MeshWindow& w, long long n, long long id0, int c0,
+                                double* verts, double iso, DevStats* st, const EdgeScratch& sc,
+                                cudaStream_t s) {
   const int blocks = (int)std::min<long long>((n + 127) / 128, (long long)sm_count() * 32);
-  EdgeState* es = static_cast<EdgeState*>(sc.state);
-  cudaError_t err = cudaMemsetAsync(sc.count, 0, 2 * sizeof(unsigned long long), s);
-  if (err) return err;
-  edge_start_kernel<POW_REF><<<blocks, 128, 0, s>>>(m, g, it, w.list, n, id0, c0, es, verts, iso,
+  edge_start_kernel<POW_REF><<<blocks, 128, 0, s>>>(m, g, it, w.list, n, id0, c0,
+                                                    static_cast<EdgeState*>(sc.state), verts, iso,
                                                     sc.list[0], sc.count, st);
+  return cudaGetLastError();
+}
+
+template <bool POW_REF>
+static cudaError_t parked_finish(const MapParams& m, const GridParams& g, const IterParams& it,
+                                 double* verts, double iso, DevStats* st, const EdgeScratch& sc,
+                                 cudaStream_t s) {
+  EdgeState* es = static_cast<EdgeState*>(sc.state);
+  cudaError_t err;
   // each round gives every parked edge one FP64 value; an edge asks for at
   // most 2 at its ends (one each, or a re-check of a failed bracket) and 6
   // in the bisection
@@ -767,10 +773,17 @@ static cudaError_t parked_vertices(const MapParams& m, const GridParams& g, cons
                                                  st);
     if ((err = cudaMemsetAsync(sc.count + (cur ^ 1), 0, sizeof(unsigned long long), s)))
       return err;
-    edge_resume_kernel<POW_REF><<<pb, 128, 0, s>>>(m, g, it, sc.list[cur], sc.count + cur, id0,
-                                                   es, verts, iso, sc.list[cur ^ 1],
+    edge_resume_kernel<POW_REF><<<pb, 128, 0, s>>>(m, g, it, sc.list[cur], sc.count + cur, es,
+                                                   verts, iso, sc.list[cur ^ 1],
                                                    sc.count + (cur ^ 1), st);
   }
+}
+
+cudaError_t mesh_parked_finish(const MapParams& m, const GridParams& g, const IterParams& it,
+                               bool pow_ref, double* verts, double iso, DevStats* st,
+                               const EdgeScratch& sc, cudaStream_t s) {
+  return pow_ref ? parked_finish<true>(m, g, it, verts, iso, st, sc, s)
+                 : parked_finish<false>(m, g, it, verts, iso, st, sc, s);
 }
 
 cudaError_t mesh_vertices(const MapParams& m, const GridParams& g, const IterParams& it,
@@ -779,8 +792,8 @@ cudaError_t mesh_vertices(const MapParams& m, const GridParams& g, const IterPar
                           double iso, DevStats* st, const EdgeScratch* scratch, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   if (edge_mode != 0 && hybrid && scratch)
-    return pow_ref ? parked_vertices<true>(m, g, it, w, n, id0, c0, verts, iso, st, *scratch, s)
-                   : parked_vertices<false>(m, g, it, w, n, id0, c0, verts, iso, st, *scratch, s);
+    return pow_ref ? parked_start<true>(m, g, it, w, n, id0, c0, verts, iso, st, *scratch, s)
+                   : parked_start<false>(m, g, it, w, n, id0, c0, verts, iso, st, *scratch, s);
   const int blocks = (int)std::min<long long>((n + 127) / 128, (long long)sm_count() * 32);
 #define QJ_VK(B, P, H) \
   vertex_kernel<B, P, H><<<blocks, 128, 0, s>>>(m, g, it, w.list, n, id0, c0, src, verts, iso, st)

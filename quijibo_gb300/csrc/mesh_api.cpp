@@ -78,6 +78,8 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
   QJ_CUDA(ctx, cudaMemsetAsync(ctx->m_masks, 0, XY, s));
   QJ_CUDA(ctx, cudaMemsetAsync(ctx->m_vbase, 0, XY * sizeof(int32_t), s));
   QJ_CUDA(ctx, cudaMemsetAsync(ctx->d_mstats, 0, sizeof(qj::DevStats), s));
+  if ((rc = ensure(ctx, &ctx->m_ecount, &ctx->m_ecount_cap, (size_t)2))) return rc;
+  QJ_CUDA(ctx, cudaMemsetAsync(ctx->m_ecount, 0, 2 * sizeof(unsigned long long), s));
 
   qj::MeshWindow w;
   w.X = X;
@@ -173,14 +175,15 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
     qj::EdgeScratch esc{};
     const bool parked = hybrid && bisect && n_new > 0;
     if (parked) {
-      if ((rc = ensure(ctx, &ctx->m_estate, &ctx->m_estate_cap,
-                       (size_t)n_new * qj::mesh_edge_state_bytes())) ||
-          (rc = ensure(ctx, &ctx->m_epark, &ctx->m_epark_cap, (size_t)n_new * 2)) ||
-          (rc = ensure(ctx, &ctx->m_ecount, &ctx->m_ecount_cap, (size_t)2)))
+      // edge states by global vertex id; parked ids accumulate over slabs
+      const size_t eb = qj::mesh_edge_state_bytes();
+      if ((rc = grow_keep(ctx, &ctx->m_estate, &ctx->m_estate_cap, (size_t)(nv + n_new) * eb,
+                          (size_t)nv * eb, s)) ||
+          (rc = grow_keep(ctx, &ctx->m_epark, &ctx->m_epark_cap, (size_t)(nv + n_new),
+                          (size_t)nv, s)))
         return rc;
       esc.state = ctx->m_estate;
       esc.list[0] = ctx->m_epark;
-      esc.list[1] = ctx->m_epark + n_new;
       esc.count = ctx->m_ecount;
     }
     QJ_CUDA(ctx, qj::mesh_vertices(*m, g, it, edge_mode, pow_ref, hybrid, w, n_new, nv, c0, src,
@@ -204,6 +207,22 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
     c0 = c1;
   }
 
+  // the parked edges of every slab, resolved together
+  const bool any_parked = iter && iter->precision != QJG_FP64 && bisect && nv > 0;
+  if (any_parked) {
+    QJ_CUDA(ctx, mark(0));
+    if ((rc = grow_keep(ctx, &ctx->m_epark, &ctx->m_epark_cap, (size_t)(2 * nv), (size_t)nv, s)))
+      return rc;
+    qj::EdgeScratch esc{};
+    esc.state = ctx->m_estate;
+    esc.list[0] = ctx->m_epark;
+    esc.list[1] = ctx->m_epark + nv;
+    esc.count = ctx->m_ecount;
+    QJ_CUDA(ctx, qj::mesh_parked_finish(*m, g, it, pow_ref, ctx->m_verts, iso, ctx->d_mstats, esc,
+                                        s));
+    QJ_CUDA(ctx, mark(1));
+    QJ_CUDA(ctx, span(0, 1, &st.ms_vertices));
+  }
   st.n_verts = nv;
   st.n_tris = nt;
   qj::DevStats ds;

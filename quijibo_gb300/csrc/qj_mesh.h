@@ -28,20 +28,27 @@ cudaError_t mesh_vertex_ids(MeshWindow& w, int j0, int j1, int lay_lo, int lay_h
                             long long running, long long* n_new, cudaStream_t s,
                             const std::function<cudaError_t(long long)>& ensure_list);
 // Scratch of the FP32-first bisection with parked FP64 evaluations: one
-// edge state per vertex of the slab (mesh_edge_state_bytes() each), two
-// parking lists of as many uint32 entries, two counters.
+// edge state per vertex of the mesh (mesh_edge_state_bytes() each, indexed
+// by global vertex id), two parking lists of global vertex ids (list 0
+// collects every slab's parked edges), two counters (zeroed once per mesh).
 struct EdgeScratch {
   void* state;
   uint32_t* list[2];
   unsigned long long* count;
 };
 size_t mesh_edge_state_bytes();
-// Vertex placement.  With hybrid bisection and a scratch, FP64 evaluations
-// are parked and batched (several launches and host reads of the list sizes).
+// Vertex placement.  With hybrid bisection and a scratch, the edges that
+// need FP64 values are parked and their vertices written by
+// mesh_parked_finish after the last slab.
 cudaError_t mesh_vertices(const MapParams& m, const GridParams& g, const IterParams& it,
                           int edge_mode, bool pow_ref, bool hybrid, const MeshWindow& w,
                           long long n, long long id0, int c0, const double* src, double* verts,
                           double iso, DevStats* st, const EdgeScratch* scratch, cudaStream_t s);
+// Resolves every parked edge: rounds of one batched FP64 evaluation per
+// parked edge and a resumption (host reads of the list sizes in between).
+cudaError_t mesh_parked_finish(const MapParams& m, const GridParams& g, const IterParams& it,
+                               bool pow_ref, double* verts, double iso, DevStats* st,
+                               const EdgeScratch& sc, cudaStream_t s);
 cudaError_t mesh_triangles(MeshWindow& w, int j0, int j1, long long running, int32_t* tris,
                            long long cap, long long* n_new, cudaStream_t s);
 cudaError_t mesh_filter(const int32_t* tris, long long n, const double* verts, int32_t* out,
