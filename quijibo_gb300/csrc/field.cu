@@ -334,8 +334,11 @@ __device__ __forceinline__ unsigned long long tile2(const MapParams& m, const Gr
   return __reduce_add_sync(0xffffffffu, (unsigned)(a.n + b.n));
 }
 
+// The unrolled forms (NT > 0) ask for 4 resident blocks per SM: ptxas then
+// keeps them at ~110 registers without spills, 3.7% faster at 16 / 8 roots
+// (the looped form is unchanged by it).
 template <bool DE, int NT = 0, int NB = 0>
-__global__ void __launch_bounds__(128) field32x2_kernel(const __grid_constant__ MapParams m,
+__global__ void __launch_bounds__(128, NT > 0 ? 4 : 0) field32x2_kernel(const __grid_constant__ MapParams m,
                                                         const GridParams g, const IterParams it,
                                                         double* __restrict__ field,
                                                         float* __restrict__ de, RefineLists rl,
