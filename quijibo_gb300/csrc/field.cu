@@ -574,9 +574,10 @@ cudaError_t launch_field32(const MapParams& m, const GridParams& g, const IterPa
   // the double-float head needs integer exponents and an error target
   const RefineLists rl = {list, keys, (refine && m.all_int && it.est_tol > 0.0) ? ff_list : nullptr};
   if (g_field32_pairs) {
-    // small root counts compiled in (the precision form's 16 / 8 and the
-    // plain form's 8 / 0): fully unrolled, 5% faster at 16 / 8.  Large maps
-    // keep the loop: unrolled 48 / 24 ran 38% slower (instruction fetch).
+    // root counts of the benchmark maps compiled in: the precision form's
+    // 16 / 8 and the plain form's 8 / 0 fully unrolled (5% faster at 16 / 8),
+    // the large form's 48 / 24 two pairs per trip (8% faster; fully unrolled
+    // it ran 38% slower, instruction fetch); other maps read their counts
 #define QJ_F32X2(NT, NB)                                                                   \
   do {                                                                                     \
     const void* fn = want ? (const void*)field32x2_kernel<true, NT, NB>                   \
@@ -591,6 +592,8 @@ cudaError_t launch_field32(const MapParams& m, const GridParams& g, const IterPa
       QJ_F32X2(16, 8);
     else if (m.nt == 8 && m.nb == 0)
       QJ_F32X2(8, 0);
+    else if (m.nt == 48 && m.nb == 24)
+      QJ_F32X2(48, 24);
     else
       QJ_F32X2(0, 0);
 #undef QJ_F32X2

@@ -559,18 +559,29 @@ __device__ __forceinline__ q32x2::Q2 product32x2(const MapParams& m, const q32x2
 }
 
 // product32x2 over a compile-time count N of roots from index LO: the same
-// association, fully unrolled, so every root's constants sit at a fixed
-// offset of the parameter bank.
+// association, unrolled (fully up to 24 roots), so every root's constants sit
+// at a fixed offset of the parameter bank.
 template <bool DE, int LO, int N>
 __device__ __forceinline__ q32x2::Q2 product32x2_fixed(const MapParams& m, const q32x2::Q2& q,
                                                        q32x2::Q2& g) {
   using namespace q32x2;
   Q2 r = root_term32x2<DE>(m, q, LO, g);
+  if (N <= 24) {
 #pragma unroll
-  for (int k = 1; k + 1 < N; k += 2) {
-    const Q2 t0 = root_term32x2<DE>(m, q, LO + k, g);
-    const Q2 t1 = root_term32x2<DE>(m, q, LO + k + 1, g);
-    r = qmul(r, qmul(t0, t1));
+    for (int k = 1; k + 1 < N; k += 2) {
+      const Q2 t0 = root_term32x2<DE>(m, q, LO + k, g);
+      const Q2 t1 = root_term32x2<DE>(m, q, LO + k + 1, g);
+      r = qmul(r, qmul(t0, t1));
+    }
+  } else {
+    // long maps: two pairs per trip (fully unrolled 48 / 24 roots overflow
+    // the instruction cache; 2 per trip measured best of 1 to 8)
+#pragma unroll 2
+    for (int k = 1; k + 1 < N; k += 2) {
+      const Q2 t0 = root_term32x2<DE>(m, q, LO + k, g);
+      const Q2 t1 = root_term32x2<DE>(m, q, LO + k + 1, g);
+      r = qmul(r, qmul(t0, t1));
+    }
   }
   if (N % 2 == 0) r = qmul(r, root_term32x2<DE>(m, q, LO + N - 1, g));
   return r;
