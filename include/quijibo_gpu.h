@@ -369,6 +369,101 @@ int qjg_conformal_radius(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid,
                          const qjg_grid* dist_grid, const double* d_dist, double alpha,
                          double* min_score, double* threshold, double* exp_scaling, void* stream);
 
+/* ---- optimizer ---------------------------------------------------------- */
+
+/* Objective of qjg_blmvm: *f = f(x) and g = its gradient (n entries).  A
+ * non-zero return stops the solver, which returns that value. */
+typedef int (*qjg_objective_fn)(void* user, int32_t n, const double* x, double* f, double* g);
+/* Called after every iteration; a non-zero return ends the run
+ * (reason QJG_BLMVM_CONVERGED_USER). */
+typedef int (*qjg_monitor_fn)(void* user, int32_t iter, double f, double gnorm, const double* x);
+
+/* Solver settings; qjg_blmvm_defaults gives TAO_SOLVER's defaults with the
+ * tolerances toothOptimizer sets (src/TOUPEE/TAO_SOLVER.cpp:40-63,
+ * projects/toothOptimizer/toothOptimizer.cpp:150-160). */
+typedef struct {
+  int32_t max_it;       /* iterations (2000) */
+  int32_t ls_max_funcs; /* trial points per line search (30) */
+  double fatol;         /* stop when |g|^2 <= fatol (1e-8) */
+  double frtol;         /* ... |g|^2 / |f| <= frtol (1e-8) */
+  double gatol;         /* ... |g| <= gatol (1e-8) */
+  double grtol;         /* ... |g / f| <= grtol (1e-8) */
+  double gttol;         /* ... |g| / |g_0| <= gttol (0) */
+} qjg_blmvm_settings;
+
+/* Why the solver stopped: TAO's SOLVER_STATE codes (TAO_SOLVER.h:62-81). */
+#define QJG_BLMVM_CONVERGED_FATOL 1
+#define QJG_BLMVM_CONVERGED_FRTOL 2
+#define QJG_BLMVM_CONVERGED_GATOL 3
+#define QJG_BLMVM_CONVERGED_GRTOL 4
+#define QJG_BLMVM_CONVERGED_GTTOL 5
+#define QJG_BLMVM_CONVERGED_MINF 7
+#define QJG_BLMVM_CONVERGED_USER 8
+#define QJG_BLMVM_DIVERGED_MAXITS (-2)
+#define QJG_BLMVM_DIVERGED_NAN (-4)
+#define QJG_BLMVM_DIVERGED_LS_FAILURE (-6)
+
+typedef struct {
+  int32_t reason;      /* QJG_BLMVM_* */
+  int32_t iterations;
+  int32_t evaluations; /* objective calls */
+  int32_t grad_steps;  /* quasi-Newton directions that were not descent (scaled gradient used) */
+  int32_t resets;      /* failed line searches retried along the scaled gradient */
+  int32_t pad_;
+  double f;            /* objective at the returned x */
+  double gnorm;        /* norm of the bound-projected gradient there */
+} qjg_blmvm_stats;
+
+void qjg_blmvm_defaults(qjg_blmvm_settings* out);
+
+/* Minimise fg over lower <= x <= upper from x (the result is written back):
+ * BLMVM with the Moré-Thuente line search, as QUIJIBO's TAO port runs it.
+ * Replaces TAO_SOLVER::optimizeBLMVM (src/TOUPEE/TAO_SOLVER.h:41-43,
+ * TAO_SOLVER.cpp:72-341).  Host only: the objective may launch GPU work.
+ * settings NULL = qjg_blmvm_defaults.  Returns QJG_OK, QJG_ERR_ARG, or the
+ * objective's non-zero status. */
+int qjg_blmvm(int32_t n, double* x, const double* lower, const double* upper, qjg_objective_fn fg,
+              void* fg_user, qjg_monitor_fn monitor, void* monitor_user,
+              const qjg_blmvm_settings* settings, qjg_blmvm_stats* stats);
+
+/* The optimizer's map: OPTIMIZE_3D's top/bottom POLYNOMIAL_4D and
+ * _expScaling.  The roots stay fixed; fits update the exponents, the power
+ * scalars and the scale in place. */
+typedef struct {
+  int32_t n_top;
+  int32_t n_bot;
+  const double* top_roots; /* n_top x (w,x,y,z) */
+  const double* bot_roots; /* n_bot x (w,x,y,z) */
+  double* top_powers;      /* n_top */
+  double* bot_powers;      /* n_bot */
+  double sigma_top;        /* powerScalar() */
+  double sigma_bot;
+  double scale;            /* expScaling() */
+} qjg_map_state;
+
+#define QJG_FIT_SCALED_ONLY 0 /* variables [log s, sigma_top, sigma_bot] */
+#define QJG_FIT_SCALED 1      /* [log s, bottom exponents, top exponents, sigma_top, sigma_bot] */
+
+/* One BLMVM solve of the tanh score of qjg_tanh_score_grad on `grid`
+ * (max_it map applications, weights on weight_grid): every objective
+ * evaluation is one GPU pass over the grid.  Bounds as the reference's: log s
+ * free, every other variable >= 0.  Replaces callConstrainedScaledOnlyTao /
+ * callConstrainedScaledTao with FormScaledOnlyFunctionGradient /
+ * FormScaledFunctionGradient (projects/toothOptimizer/toothOptimizer.cpp:
+ * 65-229).  The monitor (optional) sees the solver's variables after each
+ * iteration; d_field (optional, device) receives the field of the last
+ * evaluation, as OPTIMIZE_3D::_fractal holds it.  settings NULL = defaults. */
+int qjg_tanh_fit(qjg_ctx* ctx, int32_t mode, qjg_map_state* state, const qjg_grid* grid,
+                 int32_t max_it, const qjg_grid* weight_grid, const double* d_weights, double alpha,
+                 double threshold, const qjg_blmvm_settings* settings, qjg_monitor_fn monitor,
+                 void* monitor_user, double* d_field, qjg_blmvm_stats* stats, void* stream);
+
+/* sum |w| over the cell centres of grid, the weights looked up trilinearly:
+ * OPTIMIZE_3D::computeMaximumScaledPowerRationalScore
+ * (src/solvers/OPTIMIZE_3D.cpp:4484-4497). */
+int qjg_tanh_max_score(qjg_ctx* ctx, const qjg_grid* grid, const qjg_grid* weight_grid,
+                       const double* d_weights, double* out, void* stream);
+
 /* ---- file formats ------------------------------------------------------ */
 
 /* FIELD_3D's binary stream: int xRes, yRes, zRes; double center[3], lengths[3];

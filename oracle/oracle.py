@@ -6,9 +6,11 @@ itself, compiled from its own sources into oracle/_ref/ (only where those
 sources are present); it pins the restatement and generates golden fixtures.
 Only tests, the smoke check and the benchmark's CPU-baseline leg use this.
 """
+import contextlib
 import ctypes as C
 import os
 import subprocess
+import sys
 
 import numpy as np
 
@@ -178,6 +180,26 @@ class Oracle:
         return self.L.qjo_trilinear(C.byref(make_grid(grid)), _ptr(data), _ptr(p))
 
 
+_REF_OBJECTIVE = C.CFUNCTYPE(None, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                             C.POINTER(C.c_double))
+
+
+@contextlib.contextmanager
+def _quiet():
+    """Silence the reference's progress printing on stdout."""
+    sys.stdout.flush()
+    saved = os.dup(1)
+    null = os.open(os.devnull, os.O_WRONLY)
+    try:
+        os.dup2(null, 1)
+        yield
+    finally:
+        C.CDLL(None).fflush(None)
+        os.dup2(saved, 1)
+        os.close(null)
+        os.close(saved)
+
+
 class _MapArgs(C.Structure):
     _fields_ = [("nt", C.c_int), ("troots", _dp), ("tpows", _dp), ("tsig", C.c_double),
                 ("nb", C.c_int), ("broots", _dp), ("bpows", _dp), ("bsig", C.c_double),
@@ -226,6 +248,10 @@ class Reference:
         L.ref_inverted_distance.argtypes = [_ip, _dp, _dp, _dp, C.c_int, _dp]
         L.ref_conformal_radius.argtypes = [A, _ip, _dp, _dp, C.c_double, _ip, _dp, _dp, _dp, _dp]
         L.ref_conformal_radius.restype = C.c_double
+        L.ref_blmvm.argtypes = [C.c_int, _dp, _dp, _dp, _REF_OBJECTIVE]
+        L.ref_tanh_fit.argtypes = [C.c_int, A, _ip, _dp, _dp, C.c_double, C.c_int, _ip, _dp, _dp,
+                                   _dp, _dp, _dp, C.c_int]
+        L.ref_tanh_fit.restype = C.c_int
         L.ref_field_write.argtypes = [C.c_char_p, _ip, _dp, _dp, _dp]
         L.ref_mesh_write.argtypes = [_dp, C.c_int, _ip, C.c_int, C.c_char_p, C.c_char_p]
         L.ref_mesh_write.restype = C.c_int
@@ -296,6 +322,41 @@ class Reference:
                                          _ptr(np.ascontiguousarray(dist, dtype=np.float64).ravel()),
                                          C.byref(es))
         return sc, es.value
+
+    def blmvm(self, fun, x0, lower, upper):
+        """TAO_SOLVER::optimizeBLMVM of fun(x) -> (f, grad); returns the
+        solution and every evaluation as (f, x)."""
+        hist = []
+
+        def cb(n, xp, fp, gp):
+            x = np.ctypeslib.as_array(xp, (n,)).copy()
+            f, g = fun(x)
+            hist.append((f, x))
+            fp[0] = f
+            np.ctypeslib.as_array(gp, (n,))[:] = g
+        fn = _REF_OBJECTIVE(cb)
+        x = np.array(x0, dtype=np.float64)
+        lo = np.ascontiguousarray(lower, dtype=np.float64)
+        hi = np.ascontiguousarray(upper, dtype=np.float64)
+        with _quiet():
+            self.L.ref_blmvm(len(x), _ptr(x), _ptr(lo), _ptr(hi), fn)
+        return x, hist
+
+    def tanh_fit(self, mode, rs, grid, wgrid, weights, max_it=1, hist_cap=1 << 22):
+        """toothOptimizer's scaled-only (0) or scaled (1) BLMVM solve: final
+        [bottom powers, top powers, sigma_t, sigma_b, expScaling] and the
+        evaluations as rows {f, state...}."""
+        res, c, l, _ = self._g(grid)
+        wres, wc, wl, _ = self._g(wgrid)
+        w = np.ascontiguousarray(weights, dtype=np.float64).reshape(-1)
+        out = np.empty(rs.n_top + rs.n_bottom + 3)
+        hist = np.empty(hist_cap)
+        with _quiet():
+            ne = self.L.ref_tanh_fit(int(mode), C.byref(_map_args(rs)), _ptr(res, _ip), _ptr(c),
+                                     _ptr(l), grid.slice, int(max_it), _ptr(wres, _ip), _ptr(wc),
+                                     _ptr(wl), _ptr(w), _ptr(out), _ptr(hist), hist_cap)
+        n = 3 if mode == 0 else 3 + rs.n_top + rs.n_bottom
+        return out, hist[:ne * (n + 1)].reshape(ne, n + 1)
 
     def field_write(self, path, res, center, lengths, data):
         """FIELD_3D::write(string) of `data` (x fastest)."""

@@ -21,6 +21,7 @@
 #include "POLYNOMIAL_4D.h"
 #include "QUATERNION.h"
 #include "RATIONAL_4D.h"
+#include "TAO_SOLVER.h"
 #include "TRIANGLE_MESH.h"
 
 namespace {
@@ -64,9 +65,157 @@ int export_mesh(TRIANGLE_MESH& mesh, double* verts, int max_v, int* tris, int ma
   return 0;
 }
 
+// ---- the BLMVM callbacks -------------------------------------------------
+// TAO_SOLVER takes a plain function pointer with no user data, so the
+// objective of the current solve is held here.
+typedef void (*ref_objective)(int n, const double* x, double* f, double* g);
+ref_objective g_objective = nullptr;
+
+void objective_trampoline(const VECTOR& x, Real& f, VECTOR& g) {
+  const int n = (int)x.size();
+  std::vector<double> xx(n), gg(n);
+  for (int i = 0; i < n; i++) xx[i] = (double)x[i];
+  double ff = 0;
+  g_objective(n, xx.data(), &ff, gg.data());
+  f = ff;
+  g.resize(n);
+  for (int i = 0; i < n; i++) g[i] = gg[i];
+}
+
+// toothOptimizer's two objectives over a global OPTIMIZE_3D, restated from
+// FormScaledFunctionGradient / FormScaledOnlyFunctionGradient
+// (projects/toothOptimizer/toothOptimizer.cpp:65-130); every evaluation's
+// value and state are appended to the history.
+OPTIMIZE_3D* g_opt = nullptr;
+std::vector<double>* g_hist = nullptr;
+
+void record(const VECTOR& state, Real f) {
+  g_hist->push_back((double)f);
+  for (int i = 0; i < state.size(); i++) g_hist->push_back((double)state[i]);
+}
+
+void scaled_fg(const VECTOR& state, Real& function, VECTOR& gradient) {
+  OPTIMIZE_3D& o = *g_opt;
+  const int nt = o.top().totalRoots(), nb = o.bottom().totalRoots();
+  const int k = 1 + nt + nb;
+  o.expScaling() = exp(state[0]);
+  int xi = 1;
+  for (int i = 0; i < nb; i++, xi++) o.bottom().powersMutable()[i] = state[xi];
+  for (int i = 0; i < nt; i++, xi++) o.top().powersMutable()[i] = state[xi];
+  o.top().powerScalar() = state[k];
+  o.bottom().powerScalar() = state[k + 1];
+  function = o.computeScoreAP();
+  gradient.resize(k + 2);
+  gradient[0] = o.computeExpGradientAP();
+  for (int i = 0; i < nb; i++) gradient[i + 1] = o.computeBottomGradientAP(i);
+  for (int i = 0; i < nt; i++) gradient[i + 1 + nb] = o.computeTopGradientAP(i);
+  gradient[k] = o.computeTopBulkScalarGradientAP();
+  gradient[k + 1] = o.computeBottomBulkScalarGradientAP();
+  record(state, function);
+}
+
+void scaled_only_fg(const VECTOR& state, Real& function, VECTOR& gradient) {
+  OPTIMIZE_3D& o = *g_opt;
+  o.expScaling() = exp(state[0]);
+  o.top().powerScalar() = state[1];
+  o.bottom().powerScalar() = state[2];
+  function = o.computeScoreAP();
+  gradient.resize(3);
+  gradient[0] = o.computeExpGradientAP();
+  gradient[1] = o.computeTopBulkScalarGradientAP();
+  gradient[2] = o.computeBottomBulkScalarGradientAP();
+  record(state, function);
+}
+
 }  // namespace
 
 extern "C" {
+
+// TAO_SOLVER::optimizeBLMVM (src/TOUPEE/TAO_SOLVER.cpp:72-341) with the
+// tolerances toothOptimizer sets, on an objective given as a C callback.
+void ref_blmvm(int n, double* x, const double* lower, const double* upper, ref_objective fg) {
+  g_objective = fg;
+  VECTOR sol(n), lo(n), hi(n);
+  for (int i = 0; i < n; i++) {
+    sol[i] = x[i];
+    lo[i] = lower[i];
+    hi[i] = upper[i];
+  }
+  TAO_SOLVER tao;
+  tao.SetTolerances(1e-8, 1e-8, 1e-8, 1e-8, 0);
+  tao.optimizeBLMVM(sol, hi, lo, objective_trampoline);
+  for (int i = 0; i < n; i++) x[i] = (double)sol[i];
+  g_objective = nullptr;
+}
+
+// callConstrainedScaledOnlyTao (mode 0) or callConstrainedScaledTao (mode 1)
+// of toothOptimizer (toothOptimizer.cpp:136-229) on the map `a`, grid and
+// weight field, with maxIterations max_it.  out gets the final bottom powers,
+// top powers, sigma_top, sigma_bottom and expScaling; hist (capacity
+// hist_cap doubles) every evaluation as {f, state...}.  Returns the number
+// of evaluations.
+int ref_tanh_fit(int mode, const MapArgs* a, const int* res, const double* center,
+                 const double* lengths, double slice, int max_it, const int* wres,
+                 const double* wcenter, const double* wlengths, const double* weights,
+                 double* out, double* hist, int hist_cap) {
+  OPTIMIZE_3D opt(res[0], res[1], res[2], VEC3F(center[0], center[1], center[2]),
+                  VEC3F(lengths[0], lengths[1], lengths[2]));
+  opt.top() = make_poly(a->nt, a->troots, a->tpows, a->tsig);
+  opt.bottom() = make_poly(a->nb, a->broots, a->bpows, a->bsig);
+  opt.maxIterations() = max_it;
+  opt.expScaling() = a->s;
+  opt.slice() = slice;
+  FIELD_3D w(wres[0], wres[1], wres[2], VEC3F(wcenter[0], wcenter[1], wcenter[2]),
+             VEC3F(wlengths[0], wlengths[1], wlengths[2]));
+  for (int i = 0; i < w.totalCells(); i++) w[i] = weights[i];
+  opt.weightField() = w;
+  std::vector<double> hv;
+  g_opt = &opt;
+  g_hist = &hv;
+  const int nt = a->nt, nb = a->nb;
+  const int n = mode == 0 ? 3 : 3 + nt + nb;
+  VECTOR sol(n);
+  sol[0] = log(opt.expScaling());
+  if (mode == 0) {
+    sol[1] = opt.top().powerScalar();
+    sol[2] = opt.bottom().powerScalar();
+  } else {
+    int xi = 1;
+    for (int i = 0; i < nb; i++, xi++) sol[xi] = opt.bottom().powersMutable()[i];
+    for (int i = 0; i < nt; i++, xi++) sol[xi] = opt.top().powersMutable()[i];
+    sol[n - 2] = opt.top().powerScalar();
+    sol[n - 1] = opt.bottom().powerScalar();
+  }
+  VECTOR hi = VECTOR::Constant(n, FLT_MAX);
+  VECTOR lo = VECTOR::Zero(n);
+  lo[0] = -FLT_MAX;
+  TAO_SOLVER tao;
+  tao.SetTolerances(1e-8, 1e-8, 1e-8, 1e-8, 0);
+  tao.optimizeBLMVM(sol, hi, lo, mode == 0 ? scaled_only_fg : scaled_fg);
+  // the caller's copy-back
+  opt.expScaling() = exp(sol[0]);
+  if (mode == 0) {
+    opt.top().powerScalar() = sol[1];
+    opt.bottom().powerScalar() = sol[2];
+  } else {
+    int xi = 1;
+    for (int i = 0; i < nb; i++, xi++) opt.bottom().powersMutable()[i] = sol[xi];
+    for (int i = 0; i < nt; i++, xi++) opt.top().powersMutable()[i] = sol[xi];
+    opt.top().powerScalar() = sol[n - 2];
+    opt.bottom().powerScalar() = sol[n - 1];
+  }
+  int k = 0;
+  for (int i = 0; i < nb; i++) out[k++] = (double)opt.bottom().powersMutable()[i];
+  for (int i = 0; i < nt; i++) out[k++] = (double)opt.top().powersMutable()[i];
+  out[k++] = (double)opt.top().powerScalar();
+  out[k++] = (double)opt.bottom().powerScalar();
+  out[k++] = (double)opt.expScaling();
+  const int evals = (int)(hv.size() / (n + 1));
+  for (size_t i = 0; i < hv.size() && (int)i < hist_cap; i++) hist[i] = hv[i];
+  g_opt = nullptr;
+  g_hist = nullptr;
+  return evals;
+}
 
 int ref_sizeof_real() { return (int)sizeof(Real); }
 

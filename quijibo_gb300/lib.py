@@ -121,6 +121,32 @@ class QjgServerStats(C.Structure):
                 ("batches", C.c_int64), ("max_batch", C.c_int64)]
 
 
+class QjgBlmvmSettings(C.Structure):
+    _fields_ = [("max_it", C.c_int32), ("ls_max_funcs", C.c_int32), ("fatol", C.c_double),
+                ("frtol", C.c_double), ("gatol", C.c_double), ("grtol", C.c_double),
+                ("gttol", C.c_double)]
+
+
+class QjgBlmvmStats(C.Structure):
+    _fields_ = [("reason", C.c_int32), ("iterations", C.c_int32), ("evaluations", C.c_int32),
+                ("grad_steps", C.c_int32), ("resets", C.c_int32), ("pad_", C.c_int32),
+                ("f", C.c_double), ("gnorm", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad_"}
+
+
+class QjgMapState(C.Structure):
+    _fields_ = [("n_top", C.c_int32), ("n_bot", C.c_int32), ("top_roots", _dp),
+                ("bot_roots", _dp), ("top_powers", _dp), ("bot_powers", _dp),
+                ("sigma_top", C.c_double), ("sigma_bot", C.c_double), ("scale", C.c_double)]
+
+
+QJG_FIT_SCALED_ONLY = 0
+QJG_FIT_SCALED = 1
+OBJECTIVE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int32, _dp, _dp, _dp)
+MONITOR_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int32, C.c_double, C.c_double, _dp)
+
 EXPORTS = {
     "qjg_create": ([C.c_int, C.POINTER(C.c_void_p)], C.c_int),
     "qjg_destroy": ([C.c_void_p], None),
@@ -158,6 +184,15 @@ EXPORTS = {
                                C.c_void_p, C.c_void_p], C.c_int),
     "qjg_conformal_radius": ([C.c_void_p, C.c_int32, C.POINTER(QjgGrid), C.POINTER(QjgGrid),
                               C.c_void_p, C.c_double, _dp, _dp, _dp, C.c_void_p], C.c_int),
+    "qjg_blmvm_defaults": ([C.POINTER(QjgBlmvmSettings)], None),
+    "qjg_blmvm": ([C.c_int32, _dp, _dp, _dp, OBJECTIVE_FN, C.c_void_p, MONITOR_FN, C.c_void_p,
+                   C.POINTER(QjgBlmvmSettings), C.POINTER(QjgBlmvmStats)], C.c_int),
+    "qjg_tanh_fit": ([C.c_void_p, C.c_int32, C.POINTER(QjgMapState), C.POINTER(QjgGrid),
+                      C.c_int32, C.POINTER(QjgGrid), C.c_void_p, C.c_double, C.c_double,
+                      C.POINTER(QjgBlmvmSettings), MONITOR_FN, C.c_void_p, C.c_void_p,
+                      C.POINTER(QjgBlmvmStats), C.c_void_p], C.c_int),
+    "qjg_tanh_max_score": ([C.c_void_p, C.POINTER(QjgGrid), C.POINTER(QjgGrid), C.c_void_p, _dp,
+                            C.c_void_p], C.c_int),
     "qjg_field3d_write": ([C.c_char_p, C.POINTER(C.c_int32), _dp, _dp, C.c_void_p], C.c_int),
     "qjg_field3d_read_header": ([C.c_char_p, C.POINTER(C.c_int32), _dp, _dp], C.c_int),
     "qjg_field3d_read": ([C.c_char_p, C.c_void_p, C.c_int64], C.c_int),
@@ -351,6 +386,62 @@ def fma_probe(device=0):
     return v.value
 
 
+def blmvm_settings(**kw):
+    """The solver defaults (TAO's, with toothOptimizer's tolerances), with
+    any field overridden by keyword."""
+    st = QjgBlmvmSettings()
+    load().qjg_blmvm_defaults(C.byref(st))
+    for k, v in kw.items():
+        setattr(st, k, v)
+    return st
+
+
+def _monitor_fn(monitor):
+    if monitor is None:
+        return MONITOR_FN(), None
+
+    def cb(user, it, f, gnorm, x):
+        try:
+            return int(bool(monitor(it, f, gnorm, x)))
+        except Exception:
+            return 1
+    fn = MONITOR_FN(cb)
+    return fn, fn
+
+
+def blmvm(fun, x0, lower, upper, settings=None, monitor=None):
+    """Minimise fun(x) -> (f, grad) over lower <= x <= upper with the
+    library's BLMVM (qjg_blmvm).  Returns (x, stats dict).  monitor(iter, f,
+    gnorm, x_ptr) returning True ends the run."""
+    x = np.array(x0, dtype=np.float64)
+    lo = np.ascontiguousarray(lower, dtype=np.float64)
+    hi = np.ascontiguousarray(upper, dtype=np.float64)
+    n = len(x)
+    err = []
+
+    def cb(user, nn, xp, fp, gp):
+        try:
+            f, g = fun(np.ctypeslib.as_array(xp, (nn,)).copy())
+            fp[0] = f
+            gp_arr = np.ctypeslib.as_array(gp, (nn,))
+            gp_arr[:] = g
+            return 0
+        except Exception as e:  # reported after the solver returns
+            err.append(e)
+            return 99
+    fn = OBJECTIVE_FN(cb)
+    mfn, _keep = _monitor_fn(monitor)
+    st = QjgBlmvmStats()
+    rc = load().qjg_blmvm(n, x.ctypes.data_as(_dp), lo.ctypes.data_as(_dp), hi.ctypes.data_as(_dp),
+                          fn, None, mfn, None, C.byref(settings) if settings else None,
+                          C.byref(st))
+    if err:
+        raise err[0]
+    if rc != 0:
+        raise QjgError("qjg_blmvm failed (%d)" % rc)
+    return x, st.as_dict()
+
+
 def _arr(a, shape=None):
     a = np.ascontiguousarray(a, dtype=np.float64)
     return a.reshape(shape) if shape else a
@@ -497,6 +588,37 @@ class Context:
                                                C.byref(st), C.c_void_p(stream or 0)),
                     "qjg_tanh_score_grad")
         return score.value, grad, {k: int(getattr(st, k)) for k, _ in st._fields_}
+
+    def tanh_fit(self, mode, rs: RootSet, grid: Grid, max_it, wgrid: Grid, d_weights,
+                 alpha=10.0, threshold=0.0, settings=None, monitor=None, d_field=0, stream=None):
+        """One BLMVM solve of toothOptimizer (QJG_FIT_SCALED_ONLY or
+        QJG_FIT_SCALED); rs's exponents, power scalars and scale are updated
+        in place.  Returns the solver stats."""
+        tr, br = _arr(rs.top_roots, (-1, 4)), _arr(rs.bottom_roots, (-1, 4))
+        tp, bp = _arr(rs.top_powers).copy(), _arr(rs.bottom_powers).copy()
+        p = lambda a: a.ctypes.data_as(_dp) if a.size else None
+        ms = QjgMapState(len(tp), len(bp), p(tr), p(br), p(tp), p(bp), float(rs.sigma_top),
+                         float(rs.sigma_bottom), float(rs.scale))
+        mfn, _keep = _monitor_fn(monitor)
+        st = QjgBlmvmStats()
+        self._check(self.L.qjg_tanh_fit(self.h, int(mode), C.byref(ms), C.byref(QjgGrid.of(grid)),
+                                        int(max_it), C.byref(QjgGrid.of(wgrid)),
+                                        C.c_void_p(d_weights), float(alpha), float(threshold),
+                                        C.byref(settings) if settings else None, mfn, None,
+                                        C.c_void_p(d_field), C.byref(st), C.c_void_p(stream or 0)),
+                    "qjg_tanh_fit")
+        rs.top_powers, rs.bottom_powers = tp, bp
+        rs.sigma_top, rs.sigma_bottom, rs.scale = ms.sigma_top, ms.sigma_bot, ms.scale
+        return st.as_dict()
+
+    def tanh_max_score(self, grid: Grid, wgrid: Grid, d_weights, stream=None):
+        """sum |w| at the cell centres (computeMaximumScaledPowerRationalScore)."""
+        out = C.c_double()
+        self._check(self.L.qjg_tanh_max_score(self.h, C.byref(QjgGrid.of(grid)),
+                                              C.byref(QjgGrid.of(wgrid)), C.c_void_p(d_weights),
+                                              C.byref(out), C.c_void_p(stream or 0)),
+                    "qjg_tanh_max_score")
+        return out.value
 
     def energy(self, d_params, n_top, n_bot, n, d_xyz, d_target, max_it, escape, slice_=0.0,
                precision=QJG_FP64, d_grad=0, d_iters=0, d_sat=1.0, stream=None):

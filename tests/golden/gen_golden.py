@@ -103,6 +103,8 @@ def main():
     np.savez_compressed(os.path.join(OUT, "tanh_grad.npz"), **d)
 
     io_case(rd)
+    blmvm_case(rd)
+    tanh_fit_case(rd)
     conformal_case(rd)
     lagrange_case(rd)
     o3d_case(rd)
@@ -203,6 +205,54 @@ def conformal_case(rd):
     score, es = rd.conformal_radius(rs, g, dg, dist)
     d.update(score=score, exp_scaling=es)
     np.savez_compressed(os.path.join(OUT, "conformal.npz"), **d)
+
+
+def blmvm_case(rd):
+    """TAO_SOLVER::optimizeBLMVM on the objectives of blmvm_problems.py:
+    every evaluated point and value, and the solution."""
+    from blmvm_problems import problems
+    d = {}
+    for name, (fun, x0, lo, hi) in problems().items():
+        x, hist = rd.blmvm(lambda v: fun(list(v)), x0, lo, hi)
+        d[name + "_x"] = x
+        d[name + "_f"] = np.array([h[0] for h in hist])
+        d[name + "_pts"] = np.array([h[1] for h in hist])
+    np.savez_compressed(os.path.join(OUT, "blmvm.npz"), **d)
+
+
+def tanh_fit_inputs():
+    """Two toothOptimizer fits: (a) the tanh_case map, grid and weights;
+    (b) the conformal_case map at 25^3 from its conformal scale, weights the
+    normalized inverted distance x 100."""
+    import copy
+    rs_a, g_a, wg_a, w_a = tanh_case()
+    rs_b, _, dg, dist = conformal_inputs()
+    rs_b = copy.deepcopy(rs_b)
+    rs_b.sigma_top = rs_b.sigma_bottom = 1.0
+    return [("a", rs_a, g_a, wg_a, w_a), ("b", rs_b, Grid((25, 25, 25), slice=0.05), dg, dist)]
+
+
+def tanh_fit_case(rd):
+    """callConstrainedScaledOnlyTao then callConstrainedScaledTao from its
+    result, as optimizeSpecificResolution runs them
+    (toothOptimizer.cpp:410-415)."""
+    d = {}
+    for tag, rs, g, wg, w in tanh_fit_inputs():
+        if tag == "b":
+            w = rd.inverted_distance(wg, w, True) * 100.0
+            _, rs.scale = rd.conformal_radius(rs, Grid((20, 20, 20), slice=0.05), wg,
+                                              tanh_fit_inputs()[1][4])
+        d.update(rs_dict(tag + "_", rs, g, dict(max_it=1, escape=20.0)))
+        d.update({tag + "_weights": w, tag + "_wres": np.array(wg.res),
+                  tag + "_wcenter": np.array(wg.center), tag + "_wlengths": np.array(wg.lengths)})
+        for mode in (0, 1):
+            out, hist = rd.tanh_fit(mode, rs, g, wg, w, 1)
+            d["%s_out%d" % (tag, mode)] = out
+            d["%s_hist%d" % (tag, mode)] = hist
+            nb, nt = rs.n_bottom, rs.n_top
+            rs.bottom_powers, rs.top_powers = out[:nb].copy(), out[nb:nb + nt].copy()
+            rs.sigma_top, rs.sigma_bottom, rs.scale = out[-3], out[-2], out[-1]
+    np.savez_compressed(os.path.join(OUT, "tanh_fit.npz"), **d)
 
 
 def tanh_case():
