@@ -464,6 +464,70 @@ int qjg_tanh_fit(qjg_ctx* ctx, int32_t mode, qjg_map_state* state, const qjg_gri
 int qjg_tanh_max_score(qjg_ctx* ctx, const qjg_grid* grid, const qjg_grid* weight_grid,
                        const double* d_weights, double* out, void* stream);
 
+/* buildReweightedInsideField's arithmetic (projects/toothOptimizer/
+ * toothOptimizer.cpp:302-381) on device fields of n cells: md = the target's
+ * signed distance, fd = the fitted shape's, w = the weights.  Target-inside
+ * cells (md < 0) the shape misses (fd > 0) share 0.25 of the weight, those it
+ * covers (fd < 0) another 0.25, each region scaled uniformly; every other
+ * cell gets 0.5 / (number of cells with md > 0).  *poor_sum / *well_sum (may
+ * be NULL) get the two regions' weight sums before scaling. */
+int qjg_reweight_inside(qjg_ctx* ctx, int64_t n, const double* d_md, const double* d_fd,
+                        const double* d_w, double* d_out, double* poor_sum, double* well_sum,
+                        void* stream);
+
+/* Signed distance (negative inside), on `grid`, of a closed triangle mesh
+ * given in host buffers: what toothOptimizer obtains from its external sdfGen
+ * program (toothOptimizer.cpp:285-300).  Returns 0 on success. */
+typedef int (*qjg_sdf_fn)(void* user, const double* verts, int64_t n_verts, const int32_t* tris,
+                          int64_t n_tris, const qjg_grid* grid, double* out);
+
+/* toothOptimizer's run (projects/toothOptimizer/toothOptimizer.cpp:462-530):
+ * read the state file, take the weights from the normalized inverted distance
+ * of its distance field, move a unit-cube problem to the fractal's frame
+ * (translate all but the first root by -1/2, scale by fractal_radius, when
+ * the field is smaller than 0.95 fractal_radius), multiply every exponent but
+ * the first of each polynomial by amp, set both power scalars to 1, then
+ * optimizeSpecificResolution (:385-457) per level: the conformal-radius scan
+ * (first level only), the scaled-only solve, the scaled solve, the reweighted
+ * solve (when `sdf` is given: the level's field, infinities clamped to the
+ * mean and borders set as computeFractal does, meshed by linear marching
+ * cubes and handed to sdf), the unweighted solve, and <output_prefix>_res_<res>.o3d.
+ * Every solve is qjg_tanh_fit on the level's grid at maxIterations 1. */
+typedef struct {
+  const char* input_path;      /* the .o3d state to start from */
+  const char* checkpoint_path; /* state written every 10th solver iteration of the run (the
+                                  monitor's output.o3d, toothOptimizer.cpp:48-61); NULL: none */
+  const char* output_prefix;   /* NULL: no per-level state files */
+  double fractal_radius;       /* "fractal radius" (4) */
+  double amp;                  /* "initial bulk scalar amplitude" (-1) */
+  int32_t n_levels;            /* entries of levels[] (the reference: 3) */
+  int32_t levels[8];           /* grid resolution per level (25, 50, 97) */
+  int32_t pad_;
+  qjg_sdf_fn sdf;              /* NULL: the reweighted solve is skipped */
+  void* sdf_user;
+  const qjg_blmvm_settings* settings; /* NULL: qjg_blmvm_defaults */
+} qjg_tooth_config;
+
+typedef struct {
+  int32_t res;
+  int32_t reweighted;       /* 1 when the reweighted solve ran */
+  int64_t mesh_tris;        /* triangles handed to sdf */
+  double conformal_score;   /* the scan's lowest score (first level; else 0) */
+  double initial_score;     /* the tanh score at the level's start */
+  double max_score;         /* computeMaximumScaledPowerRationalScore, original weights */
+  double final_score;       /* the tanh score after the last solve */
+  double poor_sum, well_sum;/* buildReweightedInsideField's region sums */
+  qjg_blmvm_stats solve[4]; /* scaled-only, scaled, reweighted, unweighted */
+  double ms;                /* wall time of the level */
+  int32_t checkpoints;      /* state files written by the monitor during the level */
+  int32_t pad_;
+} qjg_tooth_level;
+
+/* Runs cfg->n_levels levels; levels_out gets one entry per level.  Each
+ * level's map (roots in the fractal frame) is in its state file. */
+int qjg_tooth_optimize(qjg_ctx* ctx, const qjg_tooth_config* cfg, qjg_tooth_level* levels_out,
+                       void* stream);
+
 /* ---- file formats ------------------------------------------------------ */
 
 /* FIELD_3D's binary stream: int xRes, yRes, zRes; double center[3], lengths[3];

@@ -252,6 +252,8 @@ class Reference:
         L.ref_tanh_fit.argtypes = [C.c_int, A, _ip, _dp, _dp, C.c_double, C.c_int, _ip, _dp, _dp,
                                    _dp, _dp, _dp, C.c_int]
         L.ref_tanh_fit.restype = C.c_int
+        L.ref_tooth_run.argtypes = [C.c_char_p, C.c_double, C.c_double, C.c_int, _ip, _dp, _ip,
+                                    _dp]
         L.ref_field_write.argtypes = [C.c_char_p, _ip, _dp, _dp, _dp]
         L.ref_mesh_write.argtypes = [_dp, C.c_int, _ip, C.c_int, C.c_char_p, C.c_char_p]
         L.ref_mesh_write.restype = C.c_int
@@ -357,6 +359,19 @@ class Reference:
                                      _ptr(wl), _ptr(w), _ptr(out), _ptr(hist), hist_cap)
         n = 3 if mode == 0 else 3 + rs.n_top + rs.n_bottom
         return out, hist[:ne * (n + 1)].reshape(ne, n + 1)
+
+    def tooth_run(self, path, n_top, n_bot, levels, radius=4.0, amp=-1.0):
+        """toothOptimizer's main without the reweighted solve: per level
+        [bottom powers, top powers, sigma_t, sigma_b, scale], evaluations of
+        its three solves, and the final roots (top then bottom)."""
+        lv = np.asarray(levels, dtype=np.int32)
+        out = np.empty((len(lv), n_top + n_bot + 3))
+        ev = np.empty((len(lv), 3), dtype=np.int32)
+        roots = np.empty((n_top + n_bot, 4))
+        with _quiet():
+            self.L.ref_tooth_run(str(path).encode(), float(radius), float(amp), len(lv),
+                                 _ptr(lv, _ip), _ptr(out), _ptr(ev, _ip), _ptr(roots))
+        return out, ev, roots
 
     def field_write(self, path, res, center, lengths, data):
         """FIELD_3D::write(string) of `data` (x fastest)."""
@@ -528,3 +543,20 @@ def conformal_radius(oracle, rs, grid, dgrid, dist, alpha=10.0):
                 found, min_t = s, x
         lo, hi = min_t - 5 * inc, min_t + 5 * inc
     return found, min_t, np.exp(-min_t)
+
+
+def reweight_inside(md, fd, w):
+    """buildReweightedInsideField's arithmetic (projects/toothOptimizer/
+    toothOptimizer.cpp:302-381): (reweighted field, poor sum, well sum)."""
+    md, fd, w = (np.asarray(a, dtype=np.float64).ravel() for a in (md, fd, w))
+    inside = md < 0
+    poor = inside & (fd > 0)
+    well = inside & (fd < 0)
+    poor_sum, well_sum = float(np.sum(w[poor])), float(np.sum(w[well]))
+    total_worth, outside_worth, poor_fraction = 0.5, 0.5, 0.5
+    outside = ((outside_worth * total_worth) / (1.0 - outside_worth)) / np.count_nonzero(md > 0)
+    out = w.copy()
+    out[poor] *= total_worth * poor_fraction / abs(poor_sum)
+    out[well] *= total_worth * (1.0 - poor_fraction) / abs(well_sum)
+    out[~inside] = outside
+    return out, poor_sum, well_sum

@@ -148,6 +148,92 @@ void ref_blmvm(int n, double* x, const double* lower, const double* upper, ref_o
   g_objective = nullptr;
 }
 
+// toothOptimizer's main (projects/toothOptimizer/toothOptimizer.cpp:462-530)
+// and optimizeSpecificResolution (:385-457) around the reference's classes,
+// for the levels given and without the reweighted solve (it needs the
+// external sdfGen): read, frame change, amp, then per level the conformal
+// scan (first level), scaled-only, scaled and unweighted scaled solves.
+// out gets per level [bottom powers, top powers, sigma_t, sigma_b, scale],
+// evals per level the evaluations of the three solves; roots_out the final
+// roots (top then bottom, 4 each).
+void ref_tooth_run(const char* path, double radius, double amp, int nlev, const int* levels,
+                   double* out, int* evals, double* roots_out) {
+  OPTIMIZE_3D opt;
+  opt.read(std::string(path));
+  if (opt.lengths()[0] < 0.95 * radius) {
+    opt.translateEverythingExceptFirst(VEC3F(-0.5, -0.5, -0.5));
+    opt.scaleEverything(radius);
+  }
+  POLYNOMIAL_4D& top = opt.top();
+  POLYNOMIAL_4D& bottom = opt.bottom();
+  for (int x = 1; x < top.totalRoots(); x++) top.powersMutable()[x] *= amp;
+  for (int x = 1; x < bottom.totalRoots(); x++) bottom.powersMutable()[x] *= amp;
+  top.powerScalar() = 1;
+  bottom.powerScalar() = 1;
+  const int nt = top.totalRoots(), nb = bottom.totalRoots();
+  std::vector<double> hv;
+  g_opt = &opt;
+  g_hist = &hv;
+  for (int l = 0; l < nlev; l++) {
+    const int res = levels[l];
+    VEC3F center = opt.fractal().center();
+    VEC3F lengths = opt.fractal().lengths();
+    opt.fractal() = FIELD_3D(res, res, res, center, lengths);
+    opt.auxiliary() = FIELD_3D(res, res, res, center, lengths);
+    opt.maxIterations() = 1;
+    if (l == 0) opt.estimateConformalRadius();
+    for (int mode = 0; mode < 3; mode++) {
+      const int n = mode == 0 ? 3 : 3 + nt + nb;
+      VECTOR sol(n);
+      sol[0] = log(opt.expScaling());
+      if (mode == 0) {
+        sol[1] = opt.top().powerScalar();
+        sol[2] = opt.bottom().powerScalar();
+      } else {
+        int xi = 1;
+        for (int i = 0; i < nb; i++, xi++) sol[xi] = opt.bottom().powersMutable()[i];
+        for (int i = 0; i < nt; i++, xi++) sol[xi] = opt.top().powersMutable()[i];
+        sol[n - 2] = opt.top().powerScalar();
+        sol[n - 1] = opt.bottom().powerScalar();
+      }
+      VECTOR hi = VECTOR::Constant(n, FLT_MAX);
+      VECTOR lo = VECTOR::Zero(n);
+      lo[0] = -FLT_MAX;
+      hv.clear();
+      TAO_SOLVER tao;
+      tao.SetTolerances(1e-8, 1e-8, 1e-8, 1e-8, 0);
+      tao.maxScore() = opt.computeMaximumScaledPowerRationalScore();
+      tao.optimizeBLMVM(sol, hi, lo, mode == 0 ? scaled_only_fg : scaled_fg);
+      evals[3 * l + mode] = (int)(hv.size() / (n + 1));
+      opt.expScaling() = exp(sol[0]);
+      if (mode == 0) {
+        opt.top().powerScalar() = sol[1];
+        opt.bottom().powerScalar() = sol[2];
+      } else {
+        int xi = 1;
+        for (int i = 0; i < nb; i++, xi++) opt.bottom().powersMutable()[i] = sol[xi];
+        for (int i = 0; i < nt; i++, xi++) opt.top().powersMutable()[i] = sol[xi];
+        opt.top().powerScalar() = sol[n - 2];
+        opt.bottom().powerScalar() = sol[n - 1];
+      }
+    }
+    double* o = out + (size_t)l * (nt + nb + 3);
+    int k = 0;
+    for (int i = 0; i < nb; i++) o[k++] = (double)opt.bottom().powersMutable()[i];
+    for (int i = 0; i < nt; i++) o[k++] = (double)opt.top().powersMutable()[i];
+    o[k++] = (double)opt.top().powerScalar();
+    o[k++] = (double)opt.bottom().powerScalar();
+    o[k++] = (double)opt.expScaling();
+  }
+  int k = 0;
+  for (int i = 0; i < nt; i++)
+    for (int c = 0; c < 4; c++) roots_out[k++] = (double)opt.top().roots()[i][c];
+  for (int i = 0; i < nb; i++)
+    for (int c = 0; c < 4; c++) roots_out[k++] = (double)opt.bottom().roots()[i][c];
+  g_opt = nullptr;
+  g_hist = nullptr;
+}
+
 // callConstrainedScaledOnlyTao (mode 0) or callConstrainedScaledTao (mode 1)
 // of toothOptimizer (toothOptimizer.cpp:136-229) on the map `a`, grid and
 // weight field, with maxIterations max_it.  out gets the final bottom powers,

@@ -220,6 +220,61 @@ __global__ void __launch_bounds__(CT) scan_kernel(const double* __restrict__ f,
   }
 }
 
+// buildReweightedInsideField's region sums (toothOptimizer.cpp:318-340):
+// per block {w over target-inside cells the fractal misses (fd > 0), w over
+// target-inside cells it covers (fd < 0), count of target-outside cells}.
+__global__ void __launch_bounds__(CT) region_sums_kernel(const double* __restrict__ md,
+                                                         const double* __restrict__ fd,
+                                                         const double* __restrict__ w, long long n,
+                                                         double* __restrict__ part) {
+  __shared__ double sh[CT / 32];
+  double poor = 0.0, well = 0.0, outside = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    if (md[i] < 0) {
+      if (fd[i] > 0) poor += w[i];
+      if (fd[i] < 0) well += w[i];
+    }
+    if (md[i] > 0) outside += 1.0;
+  }
+  poor = block_sum(poor, sh);
+  well = block_sum(well, sh);
+  outside = block_sum(outside, sh);
+  if (threadIdx.x == 0) {
+    part[3 * blockIdx.x] = poor;
+    part[3 * blockIdx.x + 1] = well;
+    part[3 * blockIdx.x + 2] = outside;
+  }
+}
+
+// The reweighted field (toothOptimizer.cpp:368-381): inside cells scaled by
+// their region's factor, every other cell the flat outside value.
+__global__ void reweight_kernel(const double* __restrict__ md, const double* __restrict__ fd,
+                                const double* __restrict__ w, long long n, double k_poor,
+                                double k_well, double outside, double* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    double v = w[i];
+    if (md[i] < 0) {
+      if (fd[i] > 0) v = __dmul_rn(v, k_poor);
+      if (fd[i] < 0) v = __dmul_rn(v, k_well);
+    } else {
+      v = outside;
+    }
+    out[i] = v;
+  }
+}
+
+// FIELD_3D::setBorders (FIELD_3D.cpp:5357-5379): every boundary cell = value.
+__global__ void borders_kernel(double* __restrict__ f, int X, int Y, int Z, double value) {
+  const long long n = (long long)X * Y * Z;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % X), y = (int)((i / X) % Y), z = (int)(i / ((long long)X * Y));
+    if (x == 0 || y == 0 || z == 0 || x == X - 1 || y == Y - 1 || z == Z - 1) f[i] = value;
+  }
+}
+
 // Block partials summed in block order (Neumaier compensation).
 __global__ void reduce_cols_kernel(const double* __restrict__ part, int nblk, int ncol,
                                    double* __restrict__ out) {
@@ -268,6 +323,26 @@ cudaError_t launch_side_sums(const double* dist, const double* w, long long n, d
   const int nb = blocks_for(n);
   sums_kernel<<<nb, CT, 0, s>>>(dist, w, n, scale, part);
   reduce_cols_kernel<<<1, 32, 0, s>>>(part, nb, 3, out3);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_region_sums(const double* md, const double* fd, const double* w, long long n,
+                               double* part, double* out3, cudaStream_t s) {
+  const int nb = blocks_for(n);
+  region_sums_kernel<<<nb, CT, 0, s>>>(md, fd, w, n, part);
+  reduce_cols_kernel<<<1, 32, 0, s>>>(part, nb, 3, out3);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_reweight(const double* md, const double* fd, const double* w, long long n,
+                            double k_poor, double k_well, double outside, double* out,
+                            cudaStream_t s) {
+  reweight_kernel<<<blocks_for(n), CT, 0, s>>>(md, fd, w, n, k_poor, k_well, outside, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_borders(double* f, int X, int Y, int Z, double value, cudaStream_t s) {
+  borders_kernel<<<blocks_for((long long)X * Y * Z), CT, 0, s>>>(f, X, Y, Z, value);
   return cudaGetLastError();
 }
 

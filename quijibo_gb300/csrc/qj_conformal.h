@@ -15,6 +15,16 @@ cudaError_t launch_invert(const double* dist, double* w, long long n, cudaStream
 // part holds 3 * conformal_blocks(n) doubles
 cudaError_t launch_side_sums(const double* dist, const double* w, long long n, double scale,
                              double* part, double* out3, cudaStream_t s);
+// out3 = {sum w where md < 0 and fd > 0, sum w where md < 0 and fd < 0,
+// count of md > 0}; part holds 3 * conformal_blocks(n) doubles
+cudaError_t launch_region_sums(const double* md, const double* fd, const double* w, long long n,
+                               double* part, double* out3, cudaStream_t s);
+// out = w * k_poor (md < 0, fd > 0), w * k_well (md < 0, fd < 0), w (md < 0,
+// fd = 0), `outside` (md >= 0)
+cudaError_t launch_reweight(const double* md, const double* fd, const double* w, long long n,
+                            double k_poor, double k_well, double outside, double* out,
+                            cudaStream_t s);
+cudaError_t launch_borders(double* f, int X, int Y, int Z, double value, cudaStream_t s);
 cudaError_t launch_scale_sides(const double* dist, double* w, long long n, double scale,
                                double k_in, double k_out, cudaStream_t s);
 // part: 4 doubles per block {sum of non-infinite values, their count, min, max}

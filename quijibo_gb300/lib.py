@@ -146,6 +146,30 @@ QJG_FIT_SCALED_ONLY = 0
 QJG_FIT_SCALED = 1
 OBJECTIVE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int32, _dp, _dp, _dp)
 MONITOR_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int32, C.c_double, C.c_double, _dp)
+SDF_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, _dp, C.c_int64, C.POINTER(C.c_int32), C.c_int64,
+                     C.POINTER(QjgGrid), _dp)
+
+
+class QjgToothConfig(C.Structure):
+    _fields_ = [("input_path", C.c_char_p), ("checkpoint_path", C.c_char_p),
+                ("output_prefix", C.c_char_p), ("fractal_radius", C.c_double),
+                ("amp", C.c_double), ("n_levels", C.c_int32), ("levels", C.c_int32 * 8),
+                ("pad_", C.c_int32), ("sdf", SDF_FN), ("sdf_user", C.c_void_p),
+                ("settings", C.POINTER(QjgBlmvmSettings))]
+
+
+class QjgToothLevel(C.Structure):
+    _fields_ = [("res", C.c_int32), ("reweighted", C.c_int32), ("mesh_tris", C.c_int64),
+                ("conformal_score", C.c_double), ("initial_score", C.c_double),
+                ("max_score", C.c_double), ("final_score", C.c_double), ("poor_sum", C.c_double),
+                ("well_sum", C.c_double), ("solve", QjgBlmvmStats * 4), ("ms", C.c_double),
+                ("checkpoints", C.c_int32), ("pad_", C.c_int32)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("solve", "pad_")}
+        d["solve"] = [self.solve[i].as_dict() for i in range(4)]
+        return d
+
 
 EXPORTS = {
     "qjg_create": ([C.c_int, C.POINTER(C.c_void_p)], C.c_int),
@@ -192,6 +216,10 @@ EXPORTS = {
                       C.POINTER(QjgBlmvmSettings), MONITOR_FN, C.c_void_p, C.c_void_p,
                       C.POINTER(QjgBlmvmStats), C.c_void_p], C.c_int),
     "qjg_tanh_max_score": ([C.c_void_p, C.POINTER(QjgGrid), C.POINTER(QjgGrid), C.c_void_p, _dp,
+                            C.c_void_p], C.c_int),
+    "qjg_reweight_inside": ([C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                             C.c_void_p, _dp, _dp, C.c_void_p], C.c_int),
+    "qjg_tooth_optimize": ([C.c_void_p, C.POINTER(QjgToothConfig), C.POINTER(QjgToothLevel),
                             C.c_void_p], C.c_int),
     "qjg_field3d_write": ([C.c_char_p, C.POINTER(C.c_int32), _dp, _dp, C.c_void_p], C.c_int),
     "qjg_field3d_read_header": ([C.c_char_p, C.POINTER(C.c_int32), _dp, _dp], C.c_int),
@@ -619,6 +647,55 @@ class Context:
                                               C.byref(out), C.c_void_p(stream or 0)),
                     "qjg_tanh_max_score")
         return out.value
+
+    def reweight_inside(self, n, d_md, d_fd, d_w, d_out, stream=None):
+        """buildReweightedInsideField's arithmetic; returns (poor_sum, well_sum)."""
+        poor, well = C.c_double(), C.c_double()
+        self._check(self.L.qjg_reweight_inside(self.h, int(n), C.c_void_p(d_md), C.c_void_p(d_fd),
+                                               C.c_void_p(d_w), C.c_void_p(d_out),
+                                               C.byref(poor), C.byref(well),
+                                               C.c_void_p(stream or 0)), "qjg_reweight_inside")
+        return poor.value, well.value
+
+    def tooth_optimize(self, input_path, levels=(25, 50, 97), fractal_radius=4.0, amp=-1.0,
+                       output_prefix=None, checkpoint_path=None, sdf=None, settings=None,
+                       stream=None):
+        """toothOptimizer's run (qjg_tooth_optimize); per-level stats.
+        sdf(verts (V,3), tris (T,3), grid) -> signed distance on grid
+        (x fastest) enables the reweighted solve."""
+        cfg = QjgToothConfig()
+        enc = lambda p: str(p).encode() if p is not None else None  # noqa: E731
+        cfg.input_path = enc(input_path)
+        cfg.checkpoint_path = enc(checkpoint_path)
+        cfg.output_prefix = enc(output_prefix)
+        cfg.fractal_radius = float(fractal_radius)
+        cfg.amp = float(amp)
+        cfg.n_levels = len(levels)
+        for i, r in enumerate(levels):
+            cfg.levels[i] = int(r)
+        err = []
+        if sdf is not None:
+            def cb(user, vp, nv, tp, nt, gp, out):
+                try:
+                    v = np.ctypeslib.as_array(vp, (int(nv), 3)).copy() if nv else np.zeros((0, 3))
+                    t = (np.ctypeslib.as_array(tp, (int(nt), 3)).copy() if nt
+                         else np.zeros((0, 3), dtype=np.int32))
+                    gr = gp.contents
+                    n = gr.res[0] * gr.res[1] * gr.res[2]
+                    np.ctypeslib.as_array(out, (n,))[:] = np.asarray(sdf(v, t, gr)).ravel()
+                    return 0
+                except Exception as e:
+                    err.append(e)
+                    return 1
+            cfg.sdf = SDF_FN(cb)
+        if settings is not None:
+            cfg.settings = C.pointer(settings)
+        out = (QjgToothLevel * len(levels))()
+        rc = self.L.qjg_tooth_optimize(self.h, C.byref(cfg), out, C.c_void_p(stream or 0))
+        if err:
+            raise err[0]
+        self._check(rc, "qjg_tooth_optimize")
+        return [out[i].as_dict() for i in range(len(levels))]
 
     def energy(self, d_params, n_top, n_bot, n, d_xyz, d_target, max_it, escape, slice_=0.0,
                precision=QJG_FP64, d_grad=0, d_iters=0, d_sat=1.0, stream=None):

@@ -105,6 +105,7 @@ def main():
     io_case(rd)
     blmvm_case(rd)
     tanh_fit_case(rd)
+    tooth_case(rd)
     conformal_case(rd)
     lagrange_case(rd)
     o3d_case(rd)
@@ -253,6 +254,51 @@ def tanh_fit_case(rd):
             rs.bottom_powers, rs.top_powers = out[:nb].copy(), out[nb:nb + nt].copy()
             rs.sigma_top, rs.sigma_bottom, rs.scale = out[-3], out[-2], out[-1]
     np.savez_compressed(os.path.join(OUT, "tanh_fit.npz"), **d)
+
+
+TOOTH_LEVELS = (12, 16, 20)
+TOOTH_CASES = {"a": (2, 1.0, 0.3), "b": (1, 0.8, 0.2)}  # seed, amp, root spread
+
+
+def tooth_inputs(seed, spread):
+    """A toothOptimizer problem in the unit-cube frame of its input files:
+    the signed distance of an ellipsoid (negative inside) on a 14 x 16 x 18
+    grid over [0, 1]^3; 5 top roots (the first at the origin, the rest within
+    `spread` of the centre) and 3 bottom roots (the first near the origin),
+    exponents 1 or 2."""
+    from quijibo_gb300.rootsets import cell_centers
+    rng = np.random.RandomState(seed)
+    nt, nb = 5, 3
+    top = np.zeros((nt, 4))
+    top[1:, :3] = 0.5 + rng.uniform(-spread, spread, (nt - 1, 3))
+    top[1:, 3] = rng.uniform(-0.05, 0.05, nt - 1)
+    bot = np.zeros((nb, 4))
+    bot[:, :3] = 0.5 + rng.uniform(-1.5 * spread, 1.5 * spread, (nb, 3))
+    bot[0, :3] = 0.03
+    rs = RootSet(top_roots=top, top_powers=rng.choice([1.0, 2.0], nt), bottom_roots=bot,
+                 bottom_powers=rng.choice([1.0, 2.0], nb), sigma_top=1.0, sigma_bottom=1.0,
+                 scale=1.0)
+    dg = Grid((14, 16, 18), center=(0.5, 0.5, 0.5), lengths=(1.0, 1.0, 1.0))
+    c = cell_centers(dg) - 0.5
+    r = np.sqrt(((c / np.array([0.3, 0.24, 0.2])) ** 2).sum(1))
+    dist = (r - 1.0) * 0.22
+    g = Grid((4, 4, 4), center=(0.5, 0.5, 0.5), lengths=(1.0, 1.0, 1.0))
+    return rs, g, np.zeros(g.n_voxels), dg, dist, dist.copy()
+
+
+def tooth_case(rd):
+    """toothOptimizer's run (without the sdfGen-dependent reweighted solve)
+    on tooth_input_<case>.o3d, written by the reference's OPTIMIZE_3D::write,
+    at levels TOOTH_LEVELS with fractal radius 4."""
+    d = {"levels": np.array(TOOTH_LEVELS), "radius": 4.0}
+    for tag, (seed, amp, spread) in TOOTH_CASES.items():
+        rs, g, fractal, dg, dist, curv = tooth_inputs(seed, spread)
+        path = os.path.join(OUT, "tooth_input_%s.o3d" % tag)
+        rd.o3d_write(path, rs, g, fractal, dg, dist, curv)
+        out, ev, roots = rd.tooth_run(path, rs.n_top, rs.n_bottom, TOOTH_LEVELS, 4.0, amp)
+        d.update({tag + "_out": out, tag + "_evals": ev, tag + "_roots": roots, tag + "_amp": amp,
+                  tag + "_n_top": rs.n_top, tag + "_n_bot": rs.n_bottom})
+    np.savez_compressed(os.path.join(OUT, "tooth.npz"), **d)
 
 
 def tanh_case():
