@@ -362,10 +362,11 @@ class Reference:
 
     def tooth_run(self, path, n_top, n_bot, levels, radius=4.0, amp=-1.0):
         """toothOptimizer's main without the reweighted solve: per level
-        [bottom powers, top powers, sigma_t, sigma_b, scale], evaluations of
-        its three solves, and the final roots (top then bottom)."""
+        [bottom powers, top powers, sigma_t, sigma_b, scale, final score],
+        evaluations of its three solves, and the final roots (top then
+        bottom)."""
         lv = np.asarray(levels, dtype=np.int32)
-        out = np.empty((len(lv), n_top + n_bot + 3))
+        out = np.empty((len(lv), n_top + n_bot + 4))
         ev = np.empty((len(lv), 3), dtype=np.int32)
         roots = np.empty((n_top + n_bot, 4))
         with _quiet():

@@ -153,7 +153,8 @@ void ref_blmvm(int n, double* x, const double* lower, const double* upper, ref_o
 // for the levels given and without the reweighted solve (it needs the
 // external sdfGen): read, frame change, amp, then per level the conformal
 // scan (first level), scaled-only, scaled and unweighted scaled solves.
-// out gets per level [bottom powers, top powers, sigma_t, sigma_b, scale],
+// out gets per level [bottom powers, top powers, sigma_t, sigma_b, scale,
+// score at the level's end (computeScoreAP)],
 // evals per level the evaluations of the three solves; roots_out the final
 // roots (top then bottom, 4 each).
 void ref_tooth_run(const char* path, double radius, double amp, int nlev, const int* levels,
@@ -217,13 +218,14 @@ void ref_tooth_run(const char* path, double radius, double amp, int nlev, const 
         opt.bottom().powerScalar() = sol[n - 1];
       }
     }
-    double* o = out + (size_t)l * (nt + nb + 3);
+    double* o = out + (size_t)l * (nt + nb + 4);
     int k = 0;
     for (int i = 0; i < nb; i++) o[k++] = (double)opt.bottom().powersMutable()[i];
     for (int i = 0; i < nt; i++) o[k++] = (double)opt.top().powersMutable()[i];
     o[k++] = (double)opt.top().powerScalar();
     o[k++] = (double)opt.bottom().powerScalar();
     o[k++] = (double)opt.expScaling();
+    o[k++] = (double)opt.computeScoreAP();
   }
   int k = 0;
   for (int i = 0; i < nt; i++)

@@ -257,7 +257,10 @@ def tanh_fit_case(rd):
 
 
 TOOTH_LEVELS = (12, 16, 20)
-TOOTH_CASES = {"a": (2, 1.0, 0.3), "b": (1, 0.8, 0.2)}  # seed, amp, root spread
+# seed, amp, root spread: of 48 such problems these two are the ones whose
+# reference run keeps its evaluation counts when the input roots move by
+# 1e-12 (the rest amplify such a change to O(1) differences)
+TOOTH_CASES = {"a": (9, 0.8, 0.2), "b": (1, 1.0, 0.2)}
 
 
 def tooth_inputs(seed, spread):

@@ -22,6 +22,15 @@ def level_state(path):
                            [st["sigma_top"], st["sigma_bottom"], st["scale"]]]), st
 
 
+# The reference's run amplifies rounding: moving its input roots by 1e-12
+# (relative) moves its end states by up to 1.7e-6 / 9.5e-5 in the exponents
+# and power scalars, 1.2e-3 / 2.1e-2 in the scale, and 8.5e-12 / 1.3e-8 in the
+# level's final score (cases a / b), with the same evaluation counts.  The GPU
+# score and gradients differ from the reference's by ~1e-12, so the end states
+# are compared at ten times those spreads.
+RTOL = {"a": (1.7e-5, 1.2e-2, 1e-10), "b": (1e-3, 0.2, 1.3e-7)}
+
+
 @pytest.mark.parametrize("tag", ["a", "b"])
 def test_run_matches_reference(ctx, tag, tmp_path):
     levels = tuple(int(v) for v in GOLD["levels"])
@@ -29,12 +38,15 @@ def test_run_matches_reference(ctx, tag, tmp_path):
                              float(GOLD["radius"]), float(GOLD[tag + "_amp"]),
                              output_prefix=str(tmp_path / "run"))
     ref, ev = GOLD[tag + "_out"], GOLD[tag + "_evals"]
+    r_par, r_scale, r_score = RTOL[tag]
     for l, res in enumerate(levels):
         L = out[l]
         assert L["res"] == res and L["reweighted"] == 0
         assert [L["solve"][k]["evaluations"] for k in (0, 1, 3)] == ev[l].tolist()
         state, st = level_state(str(tmp_path / ("run_res_%d.o3d" % res)))
-        np.testing.assert_allclose(state, ref[l], rtol=1e-7, atol=1e-12)
+        np.testing.assert_allclose(state[:-1], ref[l][:-2], rtol=r_par, atol=1e-12)
+        assert abs(state[-1] - ref[l][-2]) <= r_scale * abs(ref[l][-2])
+        assert abs(L["final_score"] - ref[l][-1]) <= r_score * abs(ref[l][-1])
         assert st["fractal"][0] == (res, res, res)
     # the frame change moves the roots exactly as the reference does
     roots = np.concatenate([st["top_roots"].reshape(-1, 4), st["bottom_roots"].reshape(-1, 4)])
