@@ -139,6 +139,8 @@ int qjg_conformal_radius(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid,
   double* scores = sc.get<double>(4096);
   if (!f || !wf || !wl || !part || !thr || !scores)
     return fail(ctx, QJG_ERR_NOMEM, "no memory for the conformal scan");
+  // the field kernel takes its tiles from the context's counter block
+  QJ_CUDA(ctx, cudaMemsetAsync(ctx->d_stats, 0, sizeof(qj::DevStats), s));
   QJ_CUDA(ctx, qj::launch_field64(m, qj_grid_params(grid, 0, grid->res[2]),
                                   qj_iter_params(&it, grid), true, f, nullptr, ctx->d_stats, s));
   // clampInfsToMean (FIELD_3D.cpp:5182-5203), then the field's range

@@ -4,7 +4,9 @@
 // one-application gradients in one pass per voxel, FP64 in reference
 // operation order:
 //   score  = sum -tanh(alpha F) w                 weightScore, OPTIMIZE_3D.cpp:4502-4517
-//   F      = the adaptive-precision map           computeRationalMapAP, :1374-1488
+//   F      = the adaptive-precision map           computeRationalMapAP, :1374-1567
+//            (voxels whose FP64 map overflows: recomputed in extended range,
+//            field, score and gradients, where the reference uses long double)
 //   g[0]   = d/d log s                            computeExpGradientAP, :3589-3625
 //   g[1+j] = d/d bottom exponent j                computeBottomGradientAP, :10012-10116
 //   g[1+nb+i] = d/d top exponent i                computeTopGradientAP, :8905-9006
@@ -67,6 +69,128 @@ __device__ __forceinline__ void warp_accum(double* acc, int slot, double v) {
   if ((threadIdx.x & 31) == 0) acc[slot] += v;
 }
 
+// ---- extended range -------------------------------------------------------
+// Voxels whose FP64 map overflows are recomputed by the reference in long
+// double (computeRationalMapAP's second pass, OPTIMIZE_3D.cpp:1490-1567, and
+// the "overflow pass" of every gradient, e.g. :9007-9106).  Here a quaternion
+// is a mantissa m (largest component in [0.5, 1)) times 2^e: the same
+// formulas, with the range of the exponent instead of more mantissa bits.
+struct QX {
+  Q m;
+  int e;
+};
+
+constexpr double LN2 = 0.6931471805599453;
+
+__device__ __forceinline__ QX xnorm(const Q& m, int e) {
+  const double a = fmax(fmax(fabs(m.w), fabs(m.x)), fmax(fabs(m.y), fabs(m.z)));
+  if (!(a > 0.0) || isinf(a)) return QX{m, e};
+  int k;
+  frexp(a, &k);
+  return QX{Q{ldexp(m.w, -k), ldexp(m.x, -k), ldexp(m.y, -k), ldexp(m.z, -k)}, e + k};
+}
+
+__device__ __forceinline__ QX xof(const Q& q) { return xnorm(q, 0); }
+
+__device__ __forceinline__ QX xmul(const QX& a, const QX& b) {
+  return xnorm(qmul(a.m, b.m), a.e + b.e);
+}
+
+// l * (conj(r) / |r|^2), as operator/(q,q)
+__device__ __forceinline__ QX xdiv(const QX& l, const QX& r) {
+  const double inv = __ddiv_rn(1.0, norm2(r.m));
+  const QX ri = xnorm(Q{mul(r.m.w, inv), mul(-r.m.x, inv), mul(-r.m.y, inv), mul(-r.m.z, inv)},
+                      -r.e);
+  return xmul(l, ri);
+}
+
+// times a finite scalar of any size
+__device__ __forceinline__ QX xscale(const QX& a, double k) {
+  int ke = 0;
+  const double km = frexp(k, &ke);
+  return xnorm(qscale(a.m, km), a.e + ke);
+}
+
+__device__ __forceinline__ double xlogmag(const QX& a) {
+  return add(log(mag(a.m)), mul((double)a.e, LN2));
+}
+
+// (a . b) / (a . a), both scaled
+__device__ __forceinline__ double xdot_ratio(const QX& a, const QX& b) {
+  return ldexp(__ddiv_rn(qdot(a.m, b.m), qdot(a.m, a.m)), b.e - a.e);
+}
+
+// QUATERNION::pow (QUATERNION.cpp:375-393) with |q|^e = 2^k 2^f
+__device__ __forceinline__ QX xpow(const Q& q, double e) {
+  const double partial = add(add(mul(q.x, q.x), mul(q.y, q.y)), mul(q.z, q.z));
+  const double qm = __dsqrt_rn(add(partial, mul(q.w, q.w)));
+  if (!(qm > 0.0)) {
+    const double nan = __longlong_as_double(0x7ff8000000000000ll);
+    return QX{Q{nan, nan, nan, nan}, 0};
+  }
+  const double vm = __dsqrt_rn(partial);
+  const double vminv = (vm > 0.0) ? __ddiv_rn(1.0, vm) : 0.0;
+  const double scale = mul(mul(e, acos(__ddiv_rn(q.w, qm))), vminv);
+  const double mm = mul(scale, vm);
+  const double minv = (mm > 0.0) ? __ddiv_rn(1.0, mm) : 0.0;
+  const double l2 = mul(e, log2(qm));
+  const double k = floor(l2);
+  const double em = exp2(sub(l2, k));
+  double s, c;
+  sincos(mm, &s, &c);
+  const double scale2 = mul(mul(mul(scale, em), minv), s);
+  return xnorm(Q{mul(em, c), mul(scale2, q.x), mul(scale2, q.y), mul(scale2, q.z)}, (int)k);
+}
+
+__device__ __forceinline__ QX xpow_int(const Q& d, int n) {
+  const QX b = xof(d);
+  QX r = b;
+  for (int k = 1; k < n; k++) r = xmul(r, b);
+  return r;
+}
+
+// The map iterated in extended range from q0 (an FP64 overflow detected):
+// returns log|q_N| (0 where it is still not a number, as the reference's
+// stillNans); the last application's factors go to (Pf, Pe) and its top and
+// bottom products to *T, *B.
+template <bool POW_REF>
+__device__ __noinline__ double ext_map(const MapParams& m, const Q q0, int max_it, Q* Pf, int* Pe,
+                                       QX* Tout, QX* Bout) {
+  const int nt = m.nt, nb = m.nb;
+  Q q = q0;
+  double mg = mag(q0), logm = log(mg);
+  QX T = {Q{1, 0, 0, 0}, 0}, B = T;
+  int it = 0;
+  while (mg < 20.0 && it < max_it) {
+#pragma unroll 1
+    for (int side = 0; side < 2; side++) {
+      const int lo = side ? nt : 0, hi = side ? nt + nb : nt;
+      QX acc = {Q{1, 0, 0, 0}, 0};
+#pragma unroll 1
+      for (int i = lo; i < hi; i++) {
+        const Q d{sub(q.w, m.r64[i][0]), sub(q.x, m.r64[i][1]), sub(q.y, m.r64[i][2]),
+                  sub(q.z, m.r64[i][3])};
+        const QX f = POW_REF ? xpow(d, m.e64[i]) : xpow_int(d, m.ie[i]);
+        Pf[i] = f.m;
+        Pe[i] = f.e;
+        acc = (i == lo) ? f : xmul(acc, f);
+      }
+      if (side == 0)
+        T = acc;
+      else if (nb > 0)
+        B = acc;
+    }
+    const QX R = xscale(nb > 0 ? xdiv(T, B) : T, m.scale);
+    logm = xlogmag(R);
+    mg = exp(logm);
+    if (mg < 20.0) q = Q{ldexp(R.m.w, R.e), ldexp(R.m.x, R.e), ldexp(R.m.y, R.e), ldexp(R.m.z, R.e)};
+    it++;
+  }
+  *Tout = T;
+  *Bout = B;
+  return isnan(logm) ? 0.0 : logm;
+}
+
 template <bool POW_REF>
 __global__ void __launch_bounds__(EN_T) tanh_grad_kernel(const __grid_constant__ MapParams m,
                                                          const GridParams g, const WeightGrid wg,
@@ -81,6 +205,7 @@ __global__ void __launch_bounds__(EN_T) tanh_grad_kernel(const __grid_constant__
   __syncthreads();
   Q Pf[QJ_MAX_ROOTS];  // last iteration's factors (local memory)
   Q Sf[QJ_MAX_ROOTS];  // their suffix products
+  int Pe[QJ_MAX_ROOTS], Se[QJ_MAX_ROOTS];  // their exponents on the extended path
   const int nt = m.nt, nb = m.nb;
   const long long N = (long long)g.X * g.Y * g.Z;
   const double logs = log(m.scale);
@@ -92,9 +217,10 @@ __global__ void __launch_bounds__(EN_T) tanh_grad_kernel(const __grid_constant__
     const long long idx = rd * stride + (long long)blockIdx.x * EN_T + threadIdx.x;
     const bool live = idx < N;
     double c_exp = 0, c_score = 0, c_over = 0, c_bad = 0, c_bulk_t = 0, c_bulk_b = 0;
-    bool grad_ok = false;
+    bool grad_ok = false, grad_x = false;
     double dSdF = 0, RR = 0;
     Q R = {0, 0, 0, 0}, T = {1, 0, 0, 0}, B = {1, 0, 0, 0}, q0 = {0, 0, 0, 0};
+    QX Tx = {Q{1, 0, 0, 0}, 0}, Bx = Tx, Rx = Tx;
     if (live) {
       const int x = (int)(idx % g.X), y = (int)((idx / g.X) % g.Y);
       const int z = (int)(idx / ((long long)g.X * g.Y));
@@ -126,14 +252,18 @@ __global__ void __launch_bounds__(EN_T) tanh_grad_kernel(const __grid_constant__
               B = acc_q;
           }
           q = nb > 0 ? qdiv(T, B) : T;
+          // what raises FE_OVERFLOW in the reference: a non-finite factor
+          // product, |B|^2 beyond range inside the division, or the quotient
           over = over || !isfinite(T.w) || !isfinite(T.x) || !isfinite(T.y) || !isfinite(T.z) ||
-                 (nb > 0 && (!isfinite(B.w) || !isfinite(B.x) || !isfinite(B.y) || !isfinite(B.z)));
+                 (nb > 0 && (!isfinite(B.w) || !isfinite(B.x) || !isfinite(B.y) ||
+                             !isfinite(B.z) || isinf(norm2(B)))) ||
+                 !isfinite(q.w) || !isfinite(q.x) || !isfinite(q.y) || !isfinite(q.z);
           q = qscale(q, m.scale);
           mg = mag(q);
           if (isinf(mg) || isnan(mg)) over = true;
           it++;
         }
-        fval = log(mg);
+        fval = over ? ext_map<POW_REF>(m, q0, max_it, Pf, Pe, &Tx, &Bx) : log(mg);
       }
       if (field) field[idx] = fval;
       const double w = trilinear(wg, weights, p);
@@ -162,6 +292,28 @@ __global__ void __launch_bounds__(EN_T) tanh_grad_kernel(const __grid_constant__
             for (int i = hi - 2; i >= lo; i--) Sf[i] = qmul(Pf[i], Sf[i + 1]);
           }
         }
+      } else if (iterated) {
+        // the gradients' overflow pass, on the extended factors
+        Rx = xdiv(Tx, Bx);
+        if (qdot(Rx.m, Rx.m) > 0.0 && isfinite(Rx.m.w)) {
+          const double F = add(xlogmag(Rx), logs);
+          const double th = tanh(mul(alpha, sub(F, thr)));
+          dSdF = mul(mul(-alpha, w), sub(1.0, mul(th, th)));
+          grad_x = true;
+#pragma unroll 1
+          for (int side = 0; side < 2; side++) {
+            const int lo = side ? nt : 0, hi = side ? nt + nb : nt;
+            if (hi == lo) continue;
+            Sf[hi - 1] = Pf[hi - 1];
+            Se[hi - 1] = Pe[hi - 1];
+#pragma unroll 1
+            for (int i = hi - 2; i >= lo; i--) {
+              const QX sx = xmul(QX{Pf[i], Pe[i]}, QX{Sf[i + 1], Se[i + 1]});
+              Sf[i] = sx.m;
+              Se[i] = sx.e;
+            }
+          }
+        }
       }
     }
     warp_accum(acc, 0, c_exp);
@@ -169,6 +321,7 @@ __global__ void __launch_bounds__(EN_T) tanh_grad_kernel(const __grid_constant__
     warp_accum(acc, s_over, c_over);
     // top roots: left = forward[i-1], right = backward[i+1]
     Q left = {1, 0, 0, 0};
+    QX lx = {Q{1, 0, 0, 0}, 0};
 #pragma unroll 1
     for (int i = 0; i < nt; i++) {
       double c_i = 0;
@@ -193,11 +346,30 @@ __global__ void __launch_bounds__(EN_T) tanh_grad_kernel(const __grid_constant__
             c_bulk_t += dSdt;
         }
         left = (i == 0) ? Pf[0] : qmul(left, Pf[i]);
+      } else if (grad_x) {
+        const QX right = (nt > 1 && i < nt - 1) ? QX{Sf[i + 1], Se[i + 1]} : QX{Q{1, 0, 0, 0}, 0};
+        const Q base{sub(q0.w, m.r64[i][0]), sub(q0.x, m.r64[i][1]), sub(q0.y, m.r64[i][2]),
+                     sub(q0.z, m.r64[i][3])};
+        const QX pw = xpow(base, m.e64[i]);
+        const QX lg = xof(qlog(base));
+#pragma unroll 1
+        for (int pass = 0; pass < 2; pass++) {
+          const double k = pass == 0 ? m.sigma[0] : m.ep[i];
+          const QX dT = xmul(xmul(lx, xmul(xscale(pw, k), lg)), right);
+          // the overflow passes add every term, not-a-number included
+          const double dSdt = mul(dSdF, xdot_ratio(Rx, xdiv(dT, Bx)));
+          if (pass == 0)
+            c_i = dSdt;
+          else
+            c_bulk_t += dSdt;
+        }
+        lx = (i == 0) ? QX{Pf[0], Pe[0]} : xmul(lx, QX{Pf[i], Pe[i]});
       }
       warp_accum(acc, 1 + nb + i, c_i);
     }
     // bottom roots: the reference's formula, R' = T / (-left * middle * right)
     Q lb = {1, 0, 0, 0};
+    QX lbx = {Q{1, 0, 0, 0}, 0};
 #pragma unroll 1
     for (int j = 0; j < nb; j++) {
       double c_j = 0;
@@ -225,6 +397,28 @@ __global__ void __launch_bounds__(EN_T) tanh_grad_kernel(const __grid_constant__
             c_bulk_b += dSdt;
         }
         lb = (j == 0) ? Pf[nt] : qmul(lb, Pf[nt + j]);
+      } else if (grad_x) {
+        const QX right = (nb > 1 && j < nb - 1) ? QX{Sf[nt + j + 1], Se[nt + j + 1]}
+                                                : QX{Q{1, 0, 0, 0}, 0};
+        const Q base{sub(q0.w, m.r64[nt + j][0]), sub(q0.x, m.r64[nt + j][1]),
+                     sub(q0.y, m.r64[nt + j][2]), sub(q0.z, m.r64[nt + j][3])};
+        const QX pw = xpow(base, m.e64[nt + j]);
+        const QX li = xof(qinv(qlog(base)));
+        const QX minus1 = {Q{-0.5, 0, 0, 0}, 1};
+        // (the overflow pass of computeBottomGradientAP has no power-scalar
+        // guard: with sigma_b = 0 its terms are not numbers, :10130-10216)
+#pragma unroll 1
+        for (int pass = 0; pass < 2; pass++) {
+          if (pass == 1 && m.ep[nt + j] < 1e-8) continue;
+          const double k = __ddiv_rn(1.0, pass == 0 ? m.sigma[1] : m.ep[nt + j]);
+          const QX dB = xmul(xmul(xmul(minus1, lbx), xmul(xscale(pw, k), li)), right);
+          const double dSdt = mul(dSdF, xdot_ratio(Rx, xdiv(Tx, dB)));
+          if (pass == 0)
+            c_j = dSdt;
+          else
+            c_bulk_b += dSdt;
+        }
+        lbx = (j == 0) ? QX{Pf[nt], Pe[nt]} : xmul(lbx, QX{Pf[nt + j], Pe[nt + j]});
       }
       warp_accum(acc, 1 + j, c_j);
     }

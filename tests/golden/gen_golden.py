@@ -106,6 +106,7 @@ def main():
     blmvm_case(rd)
     tanh_fit_case(rd)
     tooth_case(rd)
+    tanh_overflow_case(rd)
     conformal_case(rd)
     lagrange_case(rd)
     o3d_case(rd)
@@ -302,6 +303,37 @@ def tooth_case(rd):
         d.update({tag + "_out": out, tag + "_evals": ev, tag + "_roots": roots, tag + "_amp": amp,
                   tag + "_n_top": rs.n_top, tag + "_n_bot": rs.n_bottom})
     np.savez_compressed(os.path.join(OUT, "tooth.npz"), **d)
+
+
+def tanh_overflow_case(rd):
+    """The tanh score and gradients where the FP64 map overflows, so the
+    reference recomputes voxels in long double: the tooth_inputs("a") map in
+    the fractal frame on a 12^3 grid with (a) the large power scalar and small
+    scale a BLMVM line search tries (sigma_t 162.73, sigma_b 0, s e^-35.86),
+    (b) both polynomials beyond range (sigma_t = sigma_b = 140, s = 1)."""
+    seed, amp, spread = TOOTH_CASES["a"]
+    rs, _, _, dg, dist, _ = tooth_inputs(seed, spread)
+    w = rd.inverted_distance(dg, dist, True)
+    R = 4.0
+    tr, br = rs.top_roots.copy(), rs.bottom_roots.copy()
+    tr[1:, :3] += -0.5
+    br[1:, :3] += -0.5
+    rs.top_roots, rs.bottom_roots = tr * R, br * R
+    rs.top_powers[1:] *= amp
+    rs.bottom_powers[1:] *= amp
+    c = (np.array(dg.center) - 0.5) * R
+    wg = Grid(dg.res, tuple(c), tuple(np.array(dg.lengths) * R))
+    g = Grid((12, 12, 12), tuple(c), wg.lengths)
+    d = rs_dict("", rs, g, dict(max_it=1, escape=20.0))
+    d.update(weights=w, wres=np.array(wg.res), wcenter=np.array(wg.center),
+             wlengths=np.array(wg.lengths))
+    for tag, (st, sb, sc) in (("a", (162.72999184, 0.0, np.exp(-35.86015467))),
+                              ("b", (140.0, 140.0, 1.0))):
+        rs.sigma_top, rs.sigma_bottom, rs.scale = st, sb, sc
+        score, grad, field = rd.tanh_score_grad(rs, g, wg, w, 1)
+        d.update({tag + "_sigmas": np.array([st, sb, sc]), tag + "_score": score,
+                  tag + "_grad": grad, tag + "_field": field})
+    np.savez_compressed(os.path.join(OUT, "tanh_overflow.npz"), **d)
 
 
 def tanh_case():

@@ -53,10 +53,15 @@ def test_gpu_conformal_radius_matches_reference(ctx):
     rs, g, dg, d = case()
     h = ctx.upload(rs)
     dist = torch.from_numpy(d["dist"].copy()).cuda()
-    score, thr, es = ctx.conformal_radius(h, g, dg, dist.data_ptr())
+    # twice on one context, after another field pass: the scan's field must
+    # not inherit the work counters of earlier launches
+    for _ in range(2):
+        score, thr, es = ctx.conformal_radius(h, g, dg, dist.data_ptr())
+        assert es == pytest.approx(float(d["exp_scaling"]), rel=1e-14)
+        assert score == pytest.approx(float(d["score"]), rel=1e-11)
+        f = torch.empty(g.n_voxels, dtype=torch.float64, device="cuda")
+        ctx.field(h, g, ctx.iter_params(3, 2.0), f.data_ptr())
     ctx.free(h)
-    assert es == pytest.approx(float(d["exp_scaling"]), rel=1e-14)
-    assert score == pytest.approx(float(d["score"]), rel=1e-11)
 
 
 @pytest.mark.gpu

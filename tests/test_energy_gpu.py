@@ -83,3 +83,33 @@ def test_tanh_gradient_matches_finite_differences_fp64(ctx):
             dn.top_powers = rs.top_powers.copy(); dn.top_powers[i] -= eps
         fd = (score(up) - score(dn)) / (2 * eps)
         assert abs(fd - gr[k]) <= 1e-5 * max(abs(gr[k]), 1e-3 * np.abs(gr).max()), (checks[k], fd, gr[k])
+
+
+@pytest.mark.parametrize("tag", ["a", "b"])
+def test_tanh_overflow_pass_matches_reference(ctx, tag):
+    """Voxels whose FP64 map overflows: the reference recomputes them in long
+    double (field, score and every gradient's overflow pass); here in
+    extended range.  (a) the large power scalar and tiny scale a line search
+    of toothOptimizer tries, sigma_b = 0, where the reference's bottom
+    gradients are not numbers; (b) both polynomials beyond range."""
+    rs, g, p, d = load_case("tanh_overflow")
+    rs.sigma_top, rs.sigma_bottom, rs.scale = (float(v) for v in d[tag + "_sigmas"])
+    wg = _wgrid(d)
+    h = ctx.upload(rs)
+    w = torch.from_numpy(d["weights"]).cuda()
+    f = torch.empty(g.n_voxels, dtype=torch.float64, device="cuda")
+    n = 3 + rs.n_top + rs.n_bottom
+    sc, gr, st = ctx.tanh_score_grad(h, g, 1, wg, w.data_ptr(), n, d_field=f.data_ptr())
+    ctx.free(h)
+    assert st["overflowed"] > 0
+    ff, rf = f.cpu().numpy().ravel(), d[tag + "_field"].ravel()
+    fin = np.isfinite(rf)
+    assert np.array_equal(fin, np.isfinite(ff)) and np.array_equal(ff[~fin], rf[~fin])
+    # extended range carries ~1e-13 absolute error in log|q| of the
+    # recomputed voxels (an exponent of ~1000 in FP64), the rest is FP64-exact
+    assert np.max(np.abs(ff[fin] - rf[fin])) <= 1e-11 * max(1.0, np.abs(rf[fin]).max())
+    assert abs(sc - d[tag + "_score"]) <= 1e-11 * abs(d[tag + "_score"])
+    rg = d[tag + "_grad"]
+    assert np.array_equal(np.isnan(gr), np.isnan(rg))
+    ok = ~np.isnan(rg)
+    np.testing.assert_allclose(gr[ok], rg[ok], rtol=1e-8, atol=1e-12 * max(1e-30, np.abs(rg[ok]).max()))
