@@ -251,10 +251,26 @@ __global__ void __launch_bounds__(EN_T) tanh_grad_kernel(const __grid_constant__
             else if (nb > 0)
               B = acc_q;
           }
+          // the suffix products evaluateScaledPowerFactored caches in the same
+          // evaluation (POLYNOMIAL_4D.cpp:1066-1072); an overflow there flags
+          // the voxel like one in the forward product (a non-finite
+          // intermediate leaves the full suffix product non-finite)
+          bool suffix_ok = true;
+#pragma unroll 1
+          for (int side = 0; side < 2; side++) {
+            const int lo = side ? nt : 0, hi = side ? nt + nb : nt;
+            if (hi == lo) continue;
+            Sf[hi - 1] = Pf[hi - 1];
+#pragma unroll 1
+            for (int i = hi - 2; i >= lo; i--) Sf[i] = qmul(Pf[i], Sf[i + 1]);
+            suffix_ok = suffix_ok && isfinite(Sf[lo].w) && isfinite(Sf[lo].x) &&
+                        isfinite(Sf[lo].y) && isfinite(Sf[lo].z);
+          }
           q = nb > 0 ? qdiv(T, B) : T;
           // what raises FE_OVERFLOW in the reference: a non-finite factor
           // product, |B|^2 beyond range inside the division, or the quotient
-          over = over || !isfinite(T.w) || !isfinite(T.x) || !isfinite(T.y) || !isfinite(T.z) ||
+          over = over || !suffix_ok || !isfinite(T.w) || !isfinite(T.x) || !isfinite(T.y) ||
+                 !isfinite(T.z) ||
                  (nb > 0 && (!isfinite(B.w) || !isfinite(B.x) || !isfinite(B.y) ||
                              !isfinite(B.z) || isinf(norm2(B)))) ||
                  !isfinite(q.w) || !isfinite(q.x) || !isfinite(q.y) || !isfinite(q.z);
@@ -281,16 +297,7 @@ __global__ void __launch_bounds__(EN_T) tanh_grad_kernel(const __grid_constant__
           const double th = tanh(mul(alpha, sub(F, thr)));
           dSdF = mul(mul(-alpha, w), sub(1.0, mul(th, th)));
           RR = __ddiv_rn(1.0, qdot(R, R));
-          grad_ok = true;
-          // suffix products (POLYNOMIAL_4D.cpp:1066-1072), per side
-#pragma unroll 1
-          for (int side = 0; side < 2; side++) {
-            const int lo = side ? nt : 0, hi = side ? nt + nb : nt;
-            if (hi == lo) continue;
-            Sf[hi - 1] = Pf[hi - 1];
-#pragma unroll 1
-            for (int i = hi - 2; i >= lo; i--) Sf[i] = qmul(Pf[i], Sf[i + 1]);
-          }
+          grad_ok = true;  // Sf holds the last application's suffix products
         }
       } else if (iterated) {
         // the gradients' overflow pass, on the extended factors
