@@ -210,6 +210,7 @@ __global__ void __launch_bounds__(EN_T) tanh_grad_kernel(const __grid_constant__
   const long long N = (long long)g.X * g.Y * g.Z;
   const double logs = log(m.scale);
   const int s_score = 3 + nt + nb, s_over = s_score + 1, s_bad = s_score + 2;
+  const int s_bulkb_x = s_score + 3;
   // every lane of a warp walks the same number of rounds so shuffles stay full
   const long long stride = (long long)gridDim.x * EN_T;
   const long long rounds = (N + stride - 1) / stride;
@@ -217,6 +218,7 @@ __global__ void __launch_bounds__(EN_T) tanh_grad_kernel(const __grid_constant__
     const long long idx = rd * stride + (long long)blockIdx.x * EN_T + threadIdx.x;
     const bool live = idx < N;
     double c_exp = 0, c_score = 0, c_over = 0, c_bad = 0, c_bulk_t = 0, c_bulk_b = 0;
+    double c_bulk_bx = 0;  // sigma_b terms of the extended path, summed apart
     bool grad_ok = false, grad_x = false;
     double dSdF = 0, RR = 0;
     Q R = {0, 0, 0, 0}, T = {1, 0, 0, 0}, B = {1, 0, 0, 0}, q0 = {0, 0, 0, 0};
@@ -423,7 +425,7 @@ __global__ void __launch_bounds__(EN_T) tanh_grad_kernel(const __grid_constant__
           if (pass == 0)
             c_j = dSdt;
           else
-            c_bulk_b += dSdt;
+            c_bulk_bx += dSdt;
         }
         lbx = (j == 0) ? QX{Pf[nt], Pe[nt]} : xmul(lbx, QX{Pf[nt + j], Pe[nt + j]});
       }
@@ -432,6 +434,7 @@ __global__ void __launch_bounds__(EN_T) tanh_grad_kernel(const __grid_constant__
     warp_accum(acc, 1 + nb + nt, c_bulk_t);
     warp_accum(acc, 2 + nb + nt, c_bulk_b);
     warp_accum(acc, s_bad, c_bad);
+    warp_accum(acc, s_bulkb_x, c_bulk_bx);
   }
   __syncthreads();
   for (int k = threadIdx.x; k < slots; k += EN_T) {
@@ -456,7 +459,18 @@ __global__ void reduce_partials_kernel(const double* __restrict__ partials, int 
   }
 }
 
+// computeBottomBulkScalarGradientAP starts its overflow pass from zeroed
+// per-slice sums (OPTIMIZE_3D.cpp:10466-10471) where
+// computeTopBulkScalarGradientAP keeps them: once any voxel overflowed or gave
+// a non-finite term, the sigma_b gradient is the overflow pass's sum alone.
+__global__ void bottom_bulk_fix_kernel(double* __restrict__ out, int nt, int nb) {
+  const int s_score = 3 + nt + nb;
+  if (out[s_score + 1] + out[s_score + 2] > 0.0) out[2 + nb + nt] = out[s_score + 3];
+}
+
 }  // namespace
+
+int tanh_slots(int nt, int nb) { return 7 + nt + nb; }
 
 int tanh_blocks() {
   int dev = 0, sms = 0;
@@ -469,7 +483,7 @@ cudaError_t launch_tanh_grad(const MapParams& m, const GridParams& g, const Weig
                              const double* weights, int max_it, double alpha, double thr,
                              bool pow_ref, double* field, double* partials, int nblocks,
                              double* out, cudaStream_t s) {
-  const int slots = 6 + m.nt + m.nb;
+  const int slots = tanh_slots(m.nt, m.nb);
   const size_t sh = sizeof(double) * (EN_T / 32) * slots;
   if (pow_ref)
     tanh_grad_kernel<true><<<nblocks, EN_T, sh, s>>>(m, g, wg, weights, max_it, alpha, thr, field,
@@ -480,6 +494,7 @@ cudaError_t launch_tanh_grad(const MapParams& m, const GridParams& g, const Weig
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   reduce_partials_kernel<<<1, 256, 0, s>>>(partials, nblocks, slots, out);
+  bottom_bulk_fix_kernel<<<1, 1, 0, s>>>(out, m.nt, m.nb);
   return cudaGetLastError();
 }
 

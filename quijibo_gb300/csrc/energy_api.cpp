@@ -44,7 +44,7 @@ int qjg_tanh_score_grad(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, int3
   const qj::GridParams g = qj_grid_params(grid, 0, grid->res[2]);
   const qj::WeightGrid wg = qj_weight_grid(weight_grid);
   const int nblocks = qj::tanh_blocks();
-  const int slots = 6 + m->nt + m->nb;
+  const int slots = qj::tanh_slots(m->nt, m->nb);
   double* d_part = nullptr;
   QJ_CUDA(ctx, cudaMallocAsync((void**)&d_part, sizeof(double) * ((size_t)nblocks + 1) * slots, s));
   double* d_out = d_part + (size_t)nblocks * slots;
@@ -56,7 +56,7 @@ int qjg_tanh_score_grad(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, int3
   cudaFreeAsync(d_part, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return fail(ctx, QJG_ERR_CUDA, "tanh score: %s", cudaGetErrorString(e));
-  ctx->launches += 2;
+  ctx->launches += 3;
   const int nt = m->nt, nb = m->nb;
   for (int k = 0; k < 3 + nt + nb; k++) grad[k] = out[k];
   *score = out[3 + nt + nb];

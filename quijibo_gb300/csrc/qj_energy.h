@@ -10,6 +10,9 @@ namespace qj {
 // corner = center - lengths/2 + dx/2, inv = 1/dx.
 
 int tanh_blocks();
+// out[] of launch_tanh_grad: [d log s, d bottom exps, d top exps, d sigma_t,
+// d sigma_b, score, overflowed voxels, non-finite terms left out, scratch]
+int tanh_slots(int nt, int nb);
 cudaError_t launch_tanh_grad(const MapParams& m, const GridParams& g, const WeightGrid& wg,
                              const double* weights, int max_it, double alpha, double thr,
                              bool pow_ref, double* field, double* partials, int nblocks,

@@ -100,7 +100,7 @@ int qjg_tanh_fit(qjg_ctx* ctx, int32_t mode, qjg_map_state* state, const qjg_gri
   const qj::GridParams g = qj_grid_params(grid, 0, grid->res[2]);
   const qj::WeightGrid wg = qj_weight_grid(weight_grid);
   const int nblocks = qj::tanh_blocks();
-  const int slots = 6 + nt + nb;
+  const int slots = qj::tanh_slots(nt, nb);
   double* d_part = nullptr;
   QJ_CUDA(ctx, cudaMallocAsync((void**)&d_part, sizeof(double) * ((size_t)nblocks + 1) * slots, s));
   double* d_out = d_part + (size_t)nblocks * slots;
@@ -139,7 +139,7 @@ int qjg_tanh_fit(qjg_ctx* ctx, int32_t mode, qjg_map_state* state, const qjg_gri
       fail(ctx, QJG_ERR_CUDA, "tanh fit: %s", cudaGetErrorString(e));
       return QJG_ERR_CUDA;
     }
-    ctx->launches += 2;
+    ctx->launches += 3;
     *f = h_out[3 + nt + nb];
     lay.grad(h_out, gv);
     return 0;
