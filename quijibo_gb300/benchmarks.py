@@ -345,9 +345,92 @@ def bench_large(args):
     return out
 
 
+def tooth_problem(path, n_top=12, n_bot=6, dres=64, seed=3):
+    """A toothOptimizer input in the unit-cube frame of its state files: the
+    signed distance of an ellipsoid (negative inside) on a dres^3 grid over
+    [0, 1]^3, the first top root at the origin, the others around the shape,
+    exponents 1 or 2; written as an .o3d state file."""
+    import numpy as np
+
+    from . import lib
+    from .rootsets import Grid, RootSet, cell_centers
+    rng = np.random.RandomState(seed)
+    top = np.zeros((n_top, 4))
+    top[1:, :3] = 0.5 + rng.uniform(-0.2, 0.2, (n_top - 1, 3))
+    top[1:, 3] = rng.uniform(-0.05, 0.05, n_top - 1)
+    bot = np.zeros((n_bot, 4))
+    bot[:, :3] = 0.5 + rng.uniform(-0.3, 0.3, (n_bot, 3))
+    bot[0, :3] = 0.03
+    rs = RootSet(top_roots=top, top_powers=rng.choice([1.0, 2.0], n_top), bottom_roots=bot,
+                 bottom_powers=rng.choice([1.0, 2.0], n_bot), scale=1.0)
+    dg = Grid((dres,) * 3, center=(0.5, 0.5, 0.5), lengths=(1.0, 1.0, 1.0))
+    c = cell_centers(dg) - 0.5
+    dist = (np.sqrt(((c / np.array([0.3, 0.24, 0.2])) ** 2).sum(1)) - 1.0) * 0.22
+    lib.o3d_write(path, rs, (4, 4, 4), (0.5, 0.5, 0.5), (1.0, 1.0, 1.0),
+                  {"fractal": ((4, 4, 4), (0.5,) * 3, (1.0,) * 3, np.zeros(64)),
+                   "distance": (dg.res, dg.center, dg.lengths, dist),
+                   "curvature": (dg.res, dg.center, dg.lengths, dist)})
+    return rs
+
+
+def bench_tooth(args):
+    """toothOptimizer's run (qjg_tooth_optimize) at levels 25, 50, 97 on a
+    synthetic 12 top / 6 bottom root problem with a 64^3 target distance
+    field (the reweighted solve needs an external signed-distance program and
+    is left out): evaluations, time per level and per evaluation, against
+    the C restatement's score-and-gradient evaluation on one host core."""
+    import os
+    import tempfile
+
+    import numpy as np
+
+    from . import lib
+    from .rootsets import Grid
+    levels = (25, 50, 97)
+    ctx = lib.Context(0)
+    tmp = tempfile.mkdtemp()
+    path = os.path.join(tmp, "tooth_bench.o3d")
+    tooth_problem(path)
+    ctx.tooth_optimize(path, (12,), 4.0, 0.8)  # warm-up (module load, allocator)
+    t0 = time.perf_counter()
+    out = ctx.tooth_optimize(path, levels, 4.0, 0.8, output_prefix=os.path.join(tmp, "run"))
+    wall = time.perf_counter() - t0
+    res = {"workload": "toothOptimizer run, levels 25/50/97, 12 top / 6 bottom roots, 64^3 "
+                       "target, fractal radius 4, amp 0.8, no reweighted solve",
+           "wall_s": wall, "levels": []}
+    # CPU: the oracle's one-pass score and gradients at each level's end state
+    from oracle.oracle import Oracle, build
+    build()
+    o = Oracle()
+    cpu_total = 0.0
+    for L in out:
+        ev = sum(sv["evaluations"] for sv in L["solve"])
+        st = lib.o3d_read(os.path.join(tmp, "run_res_%d.o3d" % L["res"]))
+        rs = lib.RootSet(top_roots=st["top_roots"], top_powers=st["top_powers"],
+                         sigma_top=st["sigma_top"], bottom_roots=st["bottom_roots"],
+                         bottom_powers=st["bottom_powers"], sigma_bottom=st["sigma_bottom"],
+                         scale=st["scale"])
+        dres, dc, dl, dd = st["distance"]
+        g = Grid((L["res"],) * 3, dc, dl)
+        wg = Grid(dres, dc, dl)
+        w = np.abs(dd).ravel() + 0.01  # any weights: the cost does not depend on them
+        t1 = time.perf_counter()
+        o.tanh_score_grad(rs, g, wg, w, 1)
+        cpu_eval = time.perf_counter() - t1
+        cpu_total += cpu_eval * ev
+        res["levels"].append({"res": L["res"], "evaluations": ev, "ms": L["ms"],
+                              "gpu_ms_per_eval": L["ms"] / max(1, ev),
+                              "cpu_ms_per_eval_1core": cpu_eval * 1e3,
+                              "final_score": L["final_score"],
+                              "solves": [sv["reason"] for sv in L["solve"]]})
+    res["cpu_projected_s_1core"] = cpu_total
+    res["speedup_vs_cpu_port"] = cpu_total / wall
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["mesh", "energy", "serve", "large"])
+    ap.add_argument("what", choices=["mesh", "energy", "serve", "large", "tooth"])
     ap.add_argument("--res", type=int, default=0, help="grid edge (mesh: 512, large: 2200)")
     ap.add_argument("--workload", default="precision", choices=["precision", "large"])
     ap.add_argument("--slab", type=int, default=64)
@@ -367,7 +450,7 @@ def main():
     ap.add_argument("--no-mesh", action="store_true")
     args = ap.parse_args()
     fn = {"mesh": bench_mesh, "energy": bench_energy, "serve": bench_serve,
-          "large": bench_large}[args.what]
+          "large": bench_large, "tooth": bench_tooth}[args.what]
     print(json.dumps(fn(args)), flush=True)
 
 
