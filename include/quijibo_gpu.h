@@ -199,6 +199,8 @@ typedef struct {
   int64_t overflowed;  /* voxels whose map overflowed; the reference recomputes them
                           in long double, here their gradient terms are left out */
   int64_t bad_terms;   /* NaN/inf gradient terms left out (the reference's _nans/_infs) */
+  int64_t band_voxels; /* voxels whose per-parameter terms were computed; the others' are exact
+                          zeros (saturated tanh or zero weight) */
 } qjg_tanh_stats;
 
 /* Tanh-weighted fitting score of the map on a grid and its analytic

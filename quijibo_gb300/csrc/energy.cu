@@ -191,98 +191,344 @@ __device__ __noinline__ double ext_map(const MapParams& m, const Q q0, int max_i
   return isnan(logm) ? 0.0 : logm;
 }
 
+// Exponent of a finite positive double (its bits), -1023 for zero and
+// denormals, 1024 for infinities and not-a-number.
+__device__ __forceinline__ int ilog2_bits(double v) {
+  return (int)((__double_as_longlong(v) >> 52) & 0x7ff) - 1023;
+}
+
+// One voxel's map (computeRationalMapAP's first pass, OPTIMIZE_3D.cpp:1408-1488):
+// the last application's factors Pf and the suffix products Sf the reference
+// caches with them, T and B, the overflow flag as FE_OVERFLOW would raise it.
+// With BOUNDS, also what decides whether a voxel's gradient terms can be
+// skipped as exact zeros: the spread of the factors' magnitudes and whether
+// every q0 - root is of moderate size and away from 1.
+struct Voxel {
+  Q q0, T, B;
+  double mg;
+  int its;
+  bool over, iterated;
+  int spread;      // sum over factors of |log2 |factor|^2|
+  bool bases_ok;
+};
+
+template <bool POW_REF, bool BOUNDS>
+__device__ __forceinline__ void eval_voxel(const MapParams& m, const Q& q0, int max_it, Q* Pf,
+                                           Q* Sf, Voxel& v) {
+  const int nt = m.nt, nb = m.nb;
+  v.q0 = q0;
+  v.T = Q{1, 0, 0, 0};
+  v.B = Q{1, 0, 0, 0};
+  v.its = 0;
+  v.over = false;
+  v.iterated = false;
+  v.spread = 0;
+  v.bases_ok = true;
+  Q q = q0;
+  double mg = mag(q);
+  if (!(mg < 1e-8)) {  // "if we hit the origin, move on"
+    while (mg < 20.0 && v.its < max_it) {  // computeRationalMapAP's escape radius 20
+      v.iterated = true;
+      if (BOUNDS) {
+        v.spread = 0;
+        v.bases_ok = true;
+      }
+#pragma unroll 1
+      for (int side = 0; side < 2; side++) {
+        const int lo = side ? nt : 0, hi = side ? nt + nb : nt;
+        Q acc_q = {1, 0, 0, 0};
+#pragma unroll 1
+        for (int i = lo; i < hi; i++) {
+          const Q d{sub(q.w, m.r64[i][0]), sub(q.x, m.r64[i][1]), sub(q.y, m.r64[i][2]),
+                    sub(q.z, m.r64[i][3])};
+          Pf[i] = POW_REF ? qpow(d, m.e64[i]) : qpow_int(d, m.ie[i]);
+          acc_q = (i == lo) ? Pf[i] : qmul(acc_q, Pf[i]);
+          if (BOUNDS) {
+            v.spread += abs(ilog2_bits(norm2(Pf[i])));
+            const double b2 = norm2(d);
+            const Q d1{sub(d.w, 1.0), d.x, d.y, d.z};
+            v.bases_ok = v.bases_ok && b2 > 1e-40 && b2 < 1e40 && norm2(d1) > 1e-20;
+          }
+        }
+        if (side == 0)
+          v.T = acc_q;
+        else if (nb > 0)
+          v.B = acc_q;
+      }
+      // the suffix products evaluateScaledPowerFactored caches in the same
+      // evaluation (POLYNOMIAL_4D.cpp:1066-1072); an overflow there flags
+      // the voxel like one in the forward product (a non-finite
+      // intermediate leaves the full suffix product non-finite)
+      bool suffix_ok = true;
+#pragma unroll 1
+      for (int side = 0; side < 2; side++) {
+        const int lo = side ? nt : 0, hi = side ? nt + nb : nt;
+        if (hi == lo) continue;
+        Sf[hi - 1] = Pf[hi - 1];
+#pragma unroll 1
+        for (int i = hi - 2; i >= lo; i--) Sf[i] = qmul(Pf[i], Sf[i + 1]);
+        suffix_ok = suffix_ok && isfinite(Sf[lo].w) && isfinite(Sf[lo].x) &&
+                    isfinite(Sf[lo].y) && isfinite(Sf[lo].z);
+      }
+      const Q& T = v.T;
+      const Q& B = v.B;
+      q = nb > 0 ? qdiv(T, B) : T;
+      // what raises FE_OVERFLOW in the reference: a non-finite factor
+      // product, |B|^2 beyond range inside the division, or the quotient
+      v.over = v.over || !suffix_ok || !isfinite(T.w) || !isfinite(T.x) || !isfinite(T.y) ||
+               !isfinite(T.z) ||
+               (nb > 0 && (!isfinite(B.w) || !isfinite(B.x) || !isfinite(B.y) ||
+                           !isfinite(B.z) || isinf(norm2(B)))) ||
+               !isfinite(q.w) || !isfinite(q.x) || !isfinite(q.y) || !isfinite(q.z);
+      q = qscale(q, m.scale);
+      mg = mag(q);
+      if (isinf(mg) || isnan(mg)) v.over = true;
+      v.its++;
+    }
+  }
+  v.mg = mg;
+}
+
+// R = T / B and dS/dF of a voxel whose map did not overflow; false when R is
+// zero or infinite (the reference skips such voxels in every gradient).
+__device__ __forceinline__ bool grad_setup(const Voxel& v, double logs, double alpha, double thr,
+                                           double w, Q& R, double& dSdF, double& RR) {
+  R = qdiv(v.T, v.B);
+  const double Rm = mag(R);
+  if (Rm <= 0.0 || isinf(Rm)) return false;
+  const double F = add(log(Rm), logs);
+  const double th = tanh(mul(alpha, sub(F, thr)));
+  dSdF = mul(mul(-alpha, w), sub(1.0, mul(th, th)));
+  RR = __ddiv_rn(1.0, qdot(R, R));
+  return true;
+}
+
+// The per-parameter gradient terms of one voxel (FP64 path) and their warp
+// sums; every lane of the warp calls it (inactive lanes with ok = false).
 template <bool POW_REF>
-__global__ void __launch_bounds__(EN_T) tanh_grad_kernel(const __grid_constant__ MapParams m,
+__device__ __forceinline__ void grad_terms(const MapParams& m, const Voxel& v, bool ok,
+                                           const Q& R, double dSdF, double RR, const Q* Pf,
+                                           const Q* Sf, double* acc, int s_bad) {
+  const int nt = m.nt, nb = m.nb;
+  const Q& q0 = v.q0;
+  const Q& T = v.T;
+  const Q& B = v.B;
+  // one application from q0: the map's factor is the gradient's power, bit for bit
+  const bool reuse = POW_REF && v.its == 1;
+  double c_bulk_t = 0, c_bulk_b = 0, c_bad = 0;
+  // top roots: left = forward[i-1], right = backward[i+1]
+  Q left = {1, 0, 0, 0};
+#pragma unroll 1
+  for (int i = 0; i < nt; i++) {
+    double c_i = 0;
+    if (ok) {
+      const Q right = (nt > 1 && i < nt - 1) ? Sf[i + 1] : Q{1, 0, 0, 0};
+      const Q base{sub(q0.w, m.r64[i][0]), sub(q0.x, m.r64[i][1]), sub(q0.y, m.r64[i][2]),
+                   sub(q0.z, m.r64[i][3])};
+      const Q pw = reuse ? Pf[i] : qpow(base, m.e64[i]);
+      const Q lg = qlog(base);
+#pragma unroll 1
+      for (int pass = 0; pass < 2; pass++) {
+        const double k = pass == 0 ? m.sigma[0] : m.ep[i];
+        const Q dT = qmul(qmul(left, qmul(qscale(pw, k), lg)), right);
+        const double dSdt = mul(dSdF, mul(RR, qdot(R, qdiv(dT, B))));
+        if (isnan(dSdt) || isinf(dSdt)) {
+          c_bad += 1;
+          continue;
+        }
+        if (pass == 0)
+          c_i = dSdt;
+        else
+          c_bulk_t += dSdt;
+      }
+      left = (i == 0) ? Pf[0] : qmul(left, Pf[i]);
+    }
+    warp_accum(acc, 1 + nb + i, c_i);
+  }
+  // bottom roots: the reference's formula, R' = T / (-left * middle * right)
+  Q lb = {1, 0, 0, 0};
+#pragma unroll 1
+  for (int j = 0; j < nb; j++) {
+    double c_j = 0;
+    if (ok) {
+      const Q right = (nb > 1 && j < nb - 1) ? Sf[nt + j + 1] : Q{1, 0, 0, 0};
+      const Q base{sub(q0.w, m.r64[nt + j][0]), sub(q0.x, m.r64[nt + j][1]),
+                   sub(q0.y, m.r64[nt + j][2]), sub(q0.z, m.r64[nt + j][3])};
+      const Q pw = reuse ? Pf[nt + j] : qpow(base, m.e64[nt + j]);
+      const Q li = qinv(qlog(base));
+      const Q minus1 = {-1, 0, 0, 0};
+#pragma unroll 1
+      for (int pass = 0; pass < 2; pass++) {
+        if (pass == 0 && !(m.sigma[1] > 0.0)) continue;
+        if (pass == 1 && m.ep[nt + j] < 1e-8) continue;
+        const double k = __ddiv_rn(1.0, pass == 0 ? m.sigma[1] : m.ep[nt + j]);
+        const Q dB = qmul(qmul(qmul(minus1, lb), qmul(qscale(pw, k), li)), right);
+        const double dSdt = mul(dSdF, mul(RR, qdot(R, qdiv(T, dB))));
+        if (isnan(dSdt) || isinf(dSdt)) {
+          c_bad += 1;
+          continue;
+        }
+        if (pass == 0)
+          c_j = dSdt;
+        else
+          c_bulk_b += dSdt;
+      }
+      lb = (j == 0) ? Pf[nt] : qmul(lb, Pf[nt + j]);
+    }
+    warp_accum(acc, 1 + j, c_j);
+  }
+  warp_accum(acc, 1 + nb + nt, c_bulk_t);
+  warp_accum(acc, 2 + nb + nt, c_bulk_b);
+  warp_accum(acc, s_bad, c_bad);
+}
+
+// The same terms on the extended factors of an overflowed voxel (the
+// gradients' overflow passes: every term added, not-a-number included; the
+// sigma_b terms summed apart).
+__device__ __noinline__ void grad_terms_ext(const MapParams& m, const Q q0, bool ok, const QX Rx,
+                                            const QX Tx, const QX Bx, double dSdF, const Q* Pf,
+                                            const int* Pe, const Q* Sf, const int* Se,
+                                            double* acc, int s_bulkb_x) {
+  const int nt = m.nt, nb = m.nb;
+  double c_bulk_t = 0, c_bulk_bx = 0;
+  QX lx = {Q{1, 0, 0, 0}, 0};
+#pragma unroll 1
+  for (int i = 0; i < nt; i++) {
+    double c_i = 0;
+    if (ok) {
+      const QX right = (nt > 1 && i < nt - 1) ? QX{Sf[i + 1], Se[i + 1]} : QX{Q{1, 0, 0, 0}, 0};
+      const Q base{sub(q0.w, m.r64[i][0]), sub(q0.x, m.r64[i][1]), sub(q0.y, m.r64[i][2]),
+                   sub(q0.z, m.r64[i][3])};
+      const QX pw = xpow(base, m.e64[i]);
+      const QX lg = xof(qlog(base));
+#pragma unroll 1
+      for (int pass = 0; pass < 2; pass++) {
+        const double k = pass == 0 ? m.sigma[0] : m.ep[i];
+        const QX dT = xmul(xmul(lx, xmul(xscale(pw, k), lg)), right);
+        const double dSdt = mul(dSdF, xdot_ratio(Rx, xdiv(dT, Bx)));
+        if (pass == 0)
+          c_i = dSdt;
+        else
+          c_bulk_t += dSdt;
+      }
+      lx = (i == 0) ? QX{Pf[0], Pe[0]} : xmul(lx, QX{Pf[i], Pe[i]});
+    }
+    warp_accum(acc, 1 + nb + i, c_i);
+  }
+  QX lbx = {Q{1, 0, 0, 0}, 0};
+#pragma unroll 1
+  for (int j = 0; j < nb; j++) {
+    double c_j = 0;
+    if (ok) {
+      const QX right = (nb > 1 && j < nb - 1) ? QX{Sf[nt + j + 1], Se[nt + j + 1]}
+                                              : QX{Q{1, 0, 0, 0}, 0};
+      const Q base{sub(q0.w, m.r64[nt + j][0]), sub(q0.x, m.r64[nt + j][1]),
+                   sub(q0.y, m.r64[nt + j][2]), sub(q0.z, m.r64[nt + j][3])};
+      const QX pw = xpow(base, m.e64[nt + j]);
+      const QX li = xof(qinv(qlog(base)));
+      const QX minus1 = {Q{-0.5, 0, 0, 0}, 1};
+      // (the overflow pass of computeBottomGradientAP has no power-scalar
+      // guard: with sigma_b = 0 its terms are not numbers, :10130-10216)
+#pragma unroll 1
+      for (int pass = 0; pass < 2; pass++) {
+        if (pass == 1 && m.ep[nt + j] < 1e-8) continue;
+        const double k = __ddiv_rn(1.0, pass == 0 ? m.sigma[1] : m.ep[nt + j]);
+        const QX dB = xmul(xmul(xmul(minus1, lbx), xmul(xscale(pw, k), li)), right);
+        const double dSdt = mul(dSdF, xdot_ratio(Rx, xdiv(Tx, dB)));
+        if (pass == 0)
+          c_j = dSdt;
+        else
+          c_bulk_bx += dSdt;
+      }
+      lbx = (j == 0) ? QX{Pf[nt], Pe[nt]} : xmul(lbx, QX{Pf[nt + j], Pe[nt + j]});
+    }
+    warp_accum(acc, 1 + j, c_j);
+  }
+  warp_accum(acc, 1 + nb + nt, c_bulk_t);
+  warp_accum(acc, s_bulkb_x, c_bulk_bx);
+}
+
+// Block b takes a contiguous range of voxels, EN_T at a time.  Every voxel's
+// map, field, score and d/d log s term are computed in the first step; the
+// voxels whose other gradient terms are not all exact zeros (saturated tanh
+// or zero weight, with every intermediate provably in range) are queued in
+// shared memory in voxel order and their terms computed EN_T at a time, so
+// the expensive per-parameter loop runs in full warps.
+template <bool POW_REF>
+__global__ void __launch_bounds__(EN_T, 4) tanh_grad_kernel(const __grid_constant__ MapParams m,
                                                          const GridParams g, const WeightGrid wg,
                                                          const double* __restrict__ weights,
                                                          int max_it, double alpha, double thr,
                                                          double* __restrict__ field,
                                                          double* __restrict__ partials, int slots) {
   extern __shared__ double acc_sh[];  // [EN_T / 32][slots]
-  const int warp = threadIdx.x >> 5;
+  __shared__ long long queue[2 * EN_T];
+  __shared__ int queued, wcount[EN_T / 32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double* acc = acc_sh + warp * slots;
   for (int k = threadIdx.x; k < (EN_T / 32) * slots; k += EN_T) acc_sh[k] = 0.0;
+  if (threadIdx.x == 0) queued = 0;
   __syncthreads();
-  Q Pf[QJ_MAX_ROOTS];  // last iteration's factors (local memory)
+  Q Pf[QJ_MAX_ROOTS];  // last application's factors (local memory)
   Q Sf[QJ_MAX_ROOTS];  // their suffix products
   int Pe[QJ_MAX_ROOTS], Se[QJ_MAX_ROOTS];  // their exponents on the extended path
   const int nt = m.nt, nb = m.nb;
   const long long N = (long long)g.X * g.Y * g.Z;
   const double logs = log(m.scale);
   const int s_score = 3 + nt + nb, s_over = s_score + 1, s_bad = s_score + 2;
-  const int s_bulkb_x = s_score + 3;
-  // every lane of a warp walks the same number of rounds so shuffles stay full
-  const long long stride = (long long)gridDim.x * EN_T;
-  const long long rounds = (N + stride - 1) / stride;
-  for (long long rd = 0; rd < rounds; rd++) {
-    const long long idx = rd * stride + (long long)blockIdx.x * EN_T + threadIdx.x;
-    const bool live = idx < N;
-    double c_exp = 0, c_score = 0, c_over = 0, c_bad = 0, c_bulk_t = 0, c_bulk_b = 0;
-    double c_bulk_bx = 0;  // sigma_b terms of the extended path, summed apart
-    bool grad_ok = false, grad_x = false;
+  const int s_bulkb_x = s_score + 3, s_band = s_score + 4;
+  // every k a gradient term scales by (sigma_t, e_i; 1/sigma_b, 1/e_j) within
+  // [1e-10, 1e10] (or zero where a term is identically zero)
+  bool k_ok = (m.sigma[0] == 0.0 || (fabs(m.sigma[0]) >= 1e-10 && fabs(m.sigma[0]) <= 1e10)) &&
+              (!(m.sigma[1] > 0.0) || (m.sigma[1] >= 1e-10 && m.sigma[1] <= 1e10));
+  for (int i = 0; i < nt + nb; i++) {
+    const double e = fabs(m.ep[i]);
+    k_ok = k_ok && (e == 0.0 || (e >= 1e-10 && e <= 1e10));
+  }
+  const long long per = (N + gridDim.x - 1) / gridDim.x;
+  const long long lo_b = (long long)blockIdx.x * per;
+  const long long hi_b = lo_b + per < N ? lo_b + per : N;
+  auto cell = [&](long long idx, double* p) {
+    const int x = (int)(idx % g.X), y = (int)((idx / g.X) % g.Y);
+    const int z = (int)(idx / ((long long)g.X * g.Y));
+    cell_center(g, x, y, z, p);
+  };
+  // the queued voxels' terms: each thread re-evaluates one voxel's map
+  auto drain = [&](int count) {
+    const bool ok = threadIdx.x < count;
+    Voxel v;
+    Q R = {0, 0, 0, 0};
     double dSdF = 0, RR = 0;
-    Q R = {0, 0, 0, 0}, T = {1, 0, 0, 0}, B = {1, 0, 0, 0}, q0 = {0, 0, 0, 0};
-    QX Tx = {Q{1, 0, 0, 0}, 0}, Bx = Tx, Rx = Tx;
-    if (live) {
-      const int x = (int)(idx % g.X), y = (int)((idx / g.X) % g.Y);
-      const int z = (int)(idx / ((long long)g.X * g.Y));
+    bool good = false;
+    if (ok) {
       double p[3];
-      cell_center(g, x, y, z, p);
+      cell(queue[threadIdx.x], p);
+      eval_voxel<POW_REF, false>(m, Q{p[0], p[1], p[2], g.slice}, max_it, Pf, Sf, v);
+      good = grad_setup(v, logs, alpha, thr, trilinear(wg, weights, p), R, dSdF, RR);
+    } else {
+      v.its = 0;
+    }
+    grad_terms<POW_REF>(m, v, good, R, dSdF, RR, Pf, Sf, acc, s_bad);
+  };
+  for (long long base = lo_b; base < hi_b; base += EN_T) {
+    const long long idx = base + threadIdx.x;
+    const bool live = idx < hi_b;
+    double c_exp = 0, c_score = 0, c_over = 0, c_band = 0;
+    bool want = false, ext = false;
+    Voxel v;
+    v.over = false;
+    double dSdF = 0;
+    QX Tx = {Q{1, 0, 0, 0}, 0}, Bx = Tx, Rx = Tx;
+    Q q0 = {0, 0, 0, 0};
+    if (live) {
+      double p[3];
+      cell(idx, p);
       q0 = Q{p[0], p[1], p[2], g.slice};
-      Q q = q0;
-      double mg = mag(q);
-      bool over = false, iterated = false;
+      eval_voxel<POW_REF, true>(m, q0, max_it, Pf, Sf, v);
       double fval = 0.0;
-      if (!(mg < 1e-8)) {  // "if we hit the origin, move on"
-        int it = 0;
-        while (mg < 20.0 && it < max_it) {  // computeRationalMapAP's escape radius 20
-          iterated = true;
-#pragma unroll 1
-          for (int side = 0; side < 2; side++) {
-            const int lo = side ? nt : 0, hi = side ? nt + nb : nt;
-            Q acc_q = {1, 0, 0, 0};
-#pragma unroll 1
-            for (int i = lo; i < hi; i++) {
-              Q d{sub(q.w, m.r64[i][0]), sub(q.x, m.r64[i][1]), sub(q.y, m.r64[i][2]),
-                  sub(q.z, m.r64[i][3])};
-              Pf[i] = POW_REF ? qpow(d, m.e64[i]) : qpow_int(d, m.ie[i]);
-              acc_q = (i == lo) ? Pf[i] : qmul(acc_q, Pf[i]);
-            }
-            if (side == 0)
-              T = acc_q;
-            else if (nb > 0)
-              B = acc_q;
-          }
-          // the suffix products evaluateScaledPowerFactored caches in the same
-          // evaluation (POLYNOMIAL_4D.cpp:1066-1072); an overflow there flags
-          // the voxel like one in the forward product (a non-finite
-          // intermediate leaves the full suffix product non-finite)
-          bool suffix_ok = true;
-#pragma unroll 1
-          for (int side = 0; side < 2; side++) {
-            const int lo = side ? nt : 0, hi = side ? nt + nb : nt;
-            if (hi == lo) continue;
-            Sf[hi - 1] = Pf[hi - 1];
-#pragma unroll 1
-            for (int i = hi - 2; i >= lo; i--) Sf[i] = qmul(Pf[i], Sf[i + 1]);
-            suffix_ok = suffix_ok && isfinite(Sf[lo].w) && isfinite(Sf[lo].x) &&
-                        isfinite(Sf[lo].y) && isfinite(Sf[lo].z);
-          }
-          q = nb > 0 ? qdiv(T, B) : T;
-          // what raises FE_OVERFLOW in the reference: a non-finite factor
-          // product, |B|^2 beyond range inside the division, or the quotient
-          over = over || !suffix_ok || !isfinite(T.w) || !isfinite(T.x) || !isfinite(T.y) ||
-                 !isfinite(T.z) ||
-                 (nb > 0 && (!isfinite(B.w) || !isfinite(B.x) || !isfinite(B.y) ||
-                             !isfinite(B.z) || isinf(norm2(B)))) ||
-                 !isfinite(q.w) || !isfinite(q.x) || !isfinite(q.y) || !isfinite(q.z);
-          q = qscale(q, m.scale);
-          mg = mag(q);
-          if (isinf(mg) || isnan(mg)) over = true;
-          it++;
-        }
-        fval = over ? ext_map<POW_REF>(m, q0, max_it, Pf, Pe, &Tx, &Bx) : log(mg);
-      }
+      if (v.iterated || v.mg >= 1e-8) fval = log(v.mg);
+      if (!(mag(q0) < 1e-8) && v.over)
+        fval = ext_map<POW_REF>(m, q0, max_it, Pf, Pe, &Tx, &Bx);
       if (field) field[idx] = fval;
       const double w = trilinear(wg, weights, p);
       c_score = mul(-tanh(mul(alpha, fval)), w);
@@ -290,25 +536,27 @@ __global__ void __launch_bounds__(EN_T) tanh_grad_kernel(const __grid_constant__
         const double S = tanh(mul(alpha, sub(fval, thr)));
         c_exp = mul(mul(-alpha, w), sub(1.0, mul(S, S)));
       }
-      c_over = over ? 1.0 : 0.0;
-      if (iterated && !over) {
-        R = qdiv(T, B);
-        const double Rm = mag(R);
-        if (!(Rm <= 0.0 || isinf(Rm))) {
-          const double F = add(log(Rm), logs);
-          const double th = tanh(mul(alpha, sub(F, thr)));
-          dSdF = mul(mul(-alpha, w), sub(1.0, mul(th, th)));
-          RR = __ddiv_rn(1.0, qdot(R, R));
-          grad_ok = true;  // Sf holds the last application's suffix products
+      c_over = v.over ? 1.0 : 0.0;
+      if (v.iterated && !v.over) {
+        Q R;
+        double RR;
+        if (grad_setup(v, logs, alpha, thr, w, R, dSdF, RR)) {
+          // dSdF = 0 makes every term dSdF * y an exact zero; y stays finite
+          // when the factors' magnitudes spread over at most 2^300, every
+          // q0 - root is moderate and away from 1 and every k is moderate
+          const double r2 = qdot(R, R), b2 = norm2(v.B);
+          const bool zero_terms = dSdF == 0.0 && k_ok && v.bases_ok && v.spread <= 300 &&
+                                  r2 > 1e-260 && r2 < 1e260 && b2 > 1e-130 && b2 < 1e130;
+          want = !zero_terms;
         }
-      } else if (iterated) {
+      } else if (v.iterated) {
         // the gradients' overflow pass, on the extended factors
         Rx = xdiv(Tx, Bx);
         if (qdot(Rx.m, Rx.m) > 0.0 && isfinite(Rx.m.w)) {
           const double F = add(xlogmag(Rx), logs);
           const double th = tanh(mul(alpha, sub(F, thr)));
           dSdF = mul(mul(-alpha, w), sub(1.0, mul(th, th)));
-          grad_x = true;
+          ext = true;
 #pragma unroll 1
           for (int side = 0; side < 2; side++) {
             const int lo = side ? nt : 0, hi = side ? nt + nb : nt;
@@ -324,118 +572,39 @@ __global__ void __launch_bounds__(EN_T) tanh_grad_kernel(const __grid_constant__
           }
         }
       }
+      c_band = want ? 1.0 : 0.0;
     }
     warp_accum(acc, 0, c_exp);
     warp_accum(acc, s_score, c_score);
     warp_accum(acc, s_over, c_over);
-    // top roots: left = forward[i-1], right = backward[i+1]
-    Q left = {1, 0, 0, 0};
-    QX lx = {Q{1, 0, 0, 0}, 0};
-#pragma unroll 1
-    for (int i = 0; i < nt; i++) {
-      double c_i = 0;
-      if (grad_ok) {
-        const Q right = (nt > 1 && i < nt - 1) ? Sf[i + 1] : Q{1, 0, 0, 0};
-        const Q base{sub(q0.w, m.r64[i][0]), sub(q0.x, m.r64[i][1]), sub(q0.y, m.r64[i][2]),
-                     sub(q0.z, m.r64[i][3])};
-        const Q pw = qpow(base, m.e64[i]);
-        const Q lg = qlog(base);
-#pragma unroll 1
-        for (int pass = 0; pass < 2; pass++) {
-          const double k = pass == 0 ? m.sigma[0] : m.ep[i];
-          const Q dT = qmul(qmul(left, qmul(qscale(pw, k), lg)), right);
-          const double dSdt = mul(dSdF, mul(RR, qdot(R, qdiv(dT, B))));
-          if (isnan(dSdt) || isinf(dSdt)) {
-            c_bad += 1;
-            continue;
-          }
-          if (pass == 0)
-            c_i = dSdt;
-          else
-            c_bulk_t += dSdt;
-        }
-        left = (i == 0) ? Pf[0] : qmul(left, Pf[i]);
-      } else if (grad_x) {
-        const QX right = (nt > 1 && i < nt - 1) ? QX{Sf[i + 1], Se[i + 1]} : QX{Q{1, 0, 0, 0}, 0};
-        const Q base{sub(q0.w, m.r64[i][0]), sub(q0.x, m.r64[i][1]), sub(q0.y, m.r64[i][2]),
-                     sub(q0.z, m.r64[i][3])};
-        const QX pw = xpow(base, m.e64[i]);
-        const QX lg = xof(qlog(base));
-#pragma unroll 1
-        for (int pass = 0; pass < 2; pass++) {
-          const double k = pass == 0 ? m.sigma[0] : m.ep[i];
-          const QX dT = xmul(xmul(lx, xmul(xscale(pw, k), lg)), right);
-          // the overflow passes add every term, not-a-number included
-          const double dSdt = mul(dSdF, xdot_ratio(Rx, xdiv(dT, Bx)));
-          if (pass == 0)
-            c_i = dSdt;
-          else
-            c_bulk_t += dSdt;
-        }
-        lx = (i == 0) ? QX{Pf[0], Pe[0]} : xmul(lx, QX{Pf[i], Pe[i]});
-      }
-      warp_accum(acc, 1 + nb + i, c_i);
+    warp_accum(acc, s_band, c_band);
+    if (__any_sync(0xffffffffu, ext))
+      grad_terms_ext(m, q0, ext, Rx, Tx, Bx, dSdF, Pf, Pe, Sf, Se, acc, s_bulkb_x);
+    // append the voxels that need their terms, in voxel order
+    const unsigned bal = __ballot_sync(0xffffffffu, want);
+    if (lane == 0) wcount[warp] = __popc(bal);
+    __syncthreads();
+    int off = queued;
+    for (int k = 0; k < warp; k++) off += wcount[k];
+    if (want) queue[off + __popc(bal & ((1u << lane) - 1u))] = idx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int tot = 0;
+      for (int k = 0; k < EN_T / 32; k++) tot += wcount[k];
+      queued += tot;
     }
-    // bottom roots: the reference's formula, R' = T / (-left * middle * right)
-    Q lb = {1, 0, 0, 0};
-    QX lbx = {Q{1, 0, 0, 0}, 0};
-#pragma unroll 1
-    for (int j = 0; j < nb; j++) {
-      double c_j = 0;
-      if (grad_ok) {
-        const Q right = (nb > 1 && j < nb - 1) ? Sf[nt + j + 1] : Q{1, 0, 0, 0};
-        const Q base{sub(q0.w, m.r64[nt + j][0]), sub(q0.x, m.r64[nt + j][1]),
-                     sub(q0.y, m.r64[nt + j][2]), sub(q0.z, m.r64[nt + j][3])};
-        const Q pw = qpow(base, m.e64[nt + j]);
-        const Q li = qinv(qlog(base));
-        const Q minus1 = {-1, 0, 0, 0};
-#pragma unroll 1
-        for (int pass = 0; pass < 2; pass++) {
-          if (pass == 0 && !(m.sigma[1] > 0.0)) continue;
-          if (pass == 1 && m.ep[nt + j] < 1e-8) continue;
-          const double k = __ddiv_rn(1.0, pass == 0 ? m.sigma[1] : m.ep[nt + j]);
-          const Q dB = qmul(qmul(qmul(minus1, lb), qmul(qscale(pw, k), li)), right);
-          const double dSdt = mul(dSdF, mul(RR, qdot(R, qdiv(T, dB))));
-          if (isnan(dSdt) || isinf(dSdt)) {
-            c_bad += 1;
-            continue;
-          }
-          if (pass == 0)
-            c_j = dSdt;
-          else
-            c_bulk_b += dSdt;
-        }
-        lb = (j == 0) ? Pf[nt] : qmul(lb, Pf[nt + j]);
-      } else if (grad_x) {
-        const QX right = (nb > 1 && j < nb - 1) ? QX{Sf[nt + j + 1], Se[nt + j + 1]}
-                                                : QX{Q{1, 0, 0, 0}, 0};
-        const Q base{sub(q0.w, m.r64[nt + j][0]), sub(q0.x, m.r64[nt + j][1]),
-                     sub(q0.y, m.r64[nt + j][2]), sub(q0.z, m.r64[nt + j][3])};
-        const QX pw = xpow(base, m.e64[nt + j]);
-        const QX li = xof(qinv(qlog(base)));
-        const QX minus1 = {Q{-0.5, 0, 0, 0}, 1};
-        // (the overflow pass of computeBottomGradientAP has no power-scalar
-        // guard: with sigma_b = 0 its terms are not numbers, :10130-10216)
-#pragma unroll 1
-        for (int pass = 0; pass < 2; pass++) {
-          if (pass == 1 && m.ep[nt + j] < 1e-8) continue;
-          const double k = __ddiv_rn(1.0, pass == 0 ? m.sigma[1] : m.ep[nt + j]);
-          const QX dB = xmul(xmul(xmul(minus1, lbx), xmul(xscale(pw, k), li)), right);
-          const double dSdt = mul(dSdF, xdot_ratio(Rx, xdiv(Tx, dB)));
-          if (pass == 0)
-            c_j = dSdt;
-          else
-            c_bulk_bx += dSdt;
-        }
-        lbx = (j == 0) ? QX{Pf[nt], Pe[nt]} : xmul(lbx, QX{Pf[nt + j], Pe[nt + j]});
-      }
-      warp_accum(acc, 1 + j, c_j);
+    __syncthreads();
+    if (queued >= EN_T) {
+      drain(EN_T);
+      __syncthreads();
+      const int rest = queued - EN_T;
+      if (threadIdx.x < rest) queue[threadIdx.x] = queue[EN_T + threadIdx.x];
+      __syncthreads();
+      if (threadIdx.x == 0) queued = rest;
+      __syncthreads();
     }
-    warp_accum(acc, 1 + nb + nt, c_bulk_t);
-    warp_accum(acc, 2 + nb + nt, c_bulk_b);
-    warp_accum(acc, s_bad, c_bad);
-    warp_accum(acc, s_bulkb_x, c_bulk_bx);
   }
+  if (queued > 0) drain(queued);
   __syncthreads();
   for (int k = threadIdx.x; k < slots; k += EN_T) {
     double s = 0;
@@ -470,7 +639,7 @@ __global__ void bottom_bulk_fix_kernel(double* __restrict__ out, int nt, int nb)
 
 }  // namespace
 
-int tanh_slots(int nt, int nb) { return 7 + nt + nb; }
+int tanh_slots(int nt, int nb) { return 8 + nt + nb; }
 
 int tanh_blocks() {
   int dev = 0, sms = 0;

@@ -64,6 +64,7 @@ int qjg_tanh_score_grad(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, int3
     stats->voxels = (int64_t)grid->res[0] * grid->res[1] * grid->res[2];
     stats->overflowed = (int64_t)out[4 + nt + nb];
     stats->bad_terms = (int64_t)out[5 + nt + nb];
+    stats->band_voxels = (int64_t)out[7 + nt + nb];
   }
   return QJG_OK;
 }

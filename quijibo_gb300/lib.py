@@ -79,7 +79,8 @@ class QjgMeshStats(C.Structure):
 
 
 class QjgTanhStats(C.Structure):
-    _fields_ = [("voxels", C.c_int64), ("overflowed", C.c_int64), ("bad_terms", C.c_int64)]
+    _fields_ = [("voxels", C.c_int64), ("overflowed", C.c_int64), ("bad_terms", C.c_int64),
+                ("band_voxels", C.c_int64)]
 
 
 class QjgFitStats(C.Structure):
