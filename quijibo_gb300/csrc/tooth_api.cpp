@@ -120,6 +120,8 @@ int qjg_tanh_fit(qjg_ctx* ctx, int32_t mode, qjg_map_state* state, const qjg_gri
   lay.to_vars(*state, x.data());
 
   int cuda_failed = 0;
+  qj::MapParams m_last;  // the last evaluation's map, whose field d_field gets
+  bool evaluated = false;
   qj::blmvm::Objective obj = [&](const double* xv, double* f, double* gv) -> int {
     lay.from_vars(xv, cur, tp.data(), bp.data());
     if (qj_fill_map(&m, nt, cur.top_roots, tp.data(), cur.sigma_top, nb, cur.bot_roots, bp.data(),
@@ -129,8 +131,12 @@ int qjg_tanh_fit(qjg_ctx* ctx, int32_t mode, qjg_map_state* state, const qjg_gri
       for (int i = 0; i < n; i++) gv[i] = NAN;
       return 0;
     }
+    // no field during the solve (the score kernel then classifies saturated
+    // voxels in FP32); d_field is filled once at the end
     cudaError_t e = qj::launch_tanh_grad(m, g, wg, d_weights, max_it, alpha, threshold, true,
-                                         d_field, d_part, nblocks, d_out, s);
+                                         nullptr, d_part, nblocks, d_out, s);
+    m_last = m;
+    evaluated = true;
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(h_out, d_out, sizeof(double) * slots, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -151,6 +157,17 @@ int qjg_tanh_fit(qjg_ctx* ctx, int32_t mode, qjg_map_state* state, const qjg_gri
     };
   qj::blmvm::Stats bs;
   rc = qj::blmvm::minimize(n, x.data(), lo.data(), hi.data(), obj, mon, st, bs);
+  if (!rc && d_field && evaluated) {
+    // OPTIMIZE_3D::_fractal: the field of the last evaluation
+    cudaError_t e = qj::launch_tanh_grad(m_last, g, wg, d_weights, max_it, alpha, threshold, true,
+                                         d_field, d_part, nblocks, d_out, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+      cuda_failed = 1;
+      rc = fail(ctx, QJG_ERR_CUDA, "tanh fit field: %s", cudaGetErrorString(e));
+    }
+    ctx->launches += 3;
+  }
   cudaFreeAsync(d_part, s);
   cudaStreamSynchronize(s);
   cudaFreeHost(h_out);
@@ -239,6 +256,8 @@ struct ToothRun {
   int level_checkpoints = 0;
   int cur_res = 0;
   int fit_mode = 0;
+  qjg_grid cur_grid;               // the running fit's grid and weights
+  const double* cur_w = nullptr;
 
   qjg_map_state state() {
     qjg_map_state m;
@@ -318,7 +337,14 @@ int tooth_monitor(void* user, int32_t, double, double, const double* x) {
   r.tpow = tp;
   r.bpow = bp;
   r.take(m);
-  const int rc = r.write_state(r.cfg->checkpoint_path, r.cur_res);
+  // the fractal of the iterate, as the reference's last evaluation left it
+  std::vector<double> g(3 + tp.size() + bp.size());
+  double sc = 0;
+  int rc = r.with_rootset([&](qjg_rootset rs) {
+    return qjg_tanh_score_grad(r.ctx, rs, &r.cur_grid, 1, &r.dgrid, r.cur_w, 10.0, 0.0, &sc,
+                               g.data(), r.d_field.p, nullptr, r.s);
+  });
+  if (!rc) rc = r.write_state(r.cfg->checkpoint_path, r.cur_res);
   r.tpow = keep_t;
   r.bpow = keep_b;
   r.sig_t = ks[0];
@@ -543,6 +569,8 @@ int qjg_tooth_optimize(qjg_ctx* ctx, const qjg_tooth_config* cfg, qjg_tooth_leve
     };
     auto fit = [&](int mode, const double* d_weights, qjg_blmvm_stats* st) {
       r.fit_mode = mode;
+      r.cur_grid = fg;
+      r.cur_w = d_weights;
       qjg_map_state m = r.state();
       const int frc = qjg_tanh_fit(ctx, mode, &m, &fg, 1, &r.dgrid, d_weights, 10.0, 0.0,
                                    cfg->settings, tooth_monitor, &r, r.d_field.p, st, r.s);
