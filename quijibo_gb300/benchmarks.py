@@ -425,6 +425,32 @@ def bench_tooth(args):
                               "solves": [sv["reason"] for sv in L["solve"]]})
     res["cpu_projected_s_1core"] = cpu_total
     res["speedup_vs_cpu_port"] = cpu_total / wall
+    # one evaluation at the last level's end state, timed alone, without and
+    # with the field written
+    import torch
+    L = out[-1]
+    st = lib.o3d_read(os.path.join(tmp, "run_res_%d.o3d" % L["res"]))
+    rs = lib.RootSet(top_roots=st["top_roots"], top_powers=st["top_powers"],
+                     sigma_top=st["sigma_top"], bottom_roots=st["bottom_roots"],
+                     bottom_powers=st["bottom_powers"], sigma_bottom=st["sigma_bottom"],
+                     scale=st["scale"])
+    dres, dc, dl, dd = st["distance"]
+    g = Grid((L["res"],) * 3, dc, dl)
+    wg = Grid(dres, dc, dl)
+    dist = torch.from_numpy(np.ascontiguousarray(dd.ravel())).cuda()
+    w = torch.empty_like(dist)
+    ctx.inverted_distance(dres, dist.data_ptr(), True, w.data_ptr())
+    f = torch.empty(g.n_voxels, dtype=torch.float64, device="cuda")
+    h = ctx.upload(rs)
+    npar = 3 + rs.n_top + rs.n_bottom
+    for tag, fp in (("no_field", 0), ("with_field", f.data_ptr())):
+        ctx.tanh_score_grad(h, g, 1, wg, w.data_ptr(), npar, d_field=fp)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        for _ in range(5):
+            _, _, sst = ctx.tanh_score_grad(h, g, 1, wg, w.data_ptr(), npar, d_field=fp)
+        res["eval_%s" % tag] = {"ms": (time.perf_counter() - t1) / 5 * 1e3, **sst}
+    ctx.free(h)
     return res
 
 

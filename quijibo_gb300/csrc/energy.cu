@@ -448,68 +448,13 @@ __device__ __noinline__ void grad_terms_ext(const MapParams& m, const Q q0, bool
   warp_accum(acc, s_bulkb_x, c_bulk_bx);
 }
 
-// One application of the map (max_it = 1) has |q1| = s |T| / |B| with
-// |T| = prod |q0 - t_i|^(sigma_t e_i) (the quaternion norm is multiplicative),
-// so log2 of every product the FP64 path forms is a sum of
-// sigma e log2|q0 - root|.  In FP32 with a bound on its error this decides,
-// without a quaternion power, that a voxel's FP64 evaluation neither
-// overflows nor underflows, that its tanh is saturated (|alpha F| >= 25, where
-// FP64 tanh is exactly +-1) and that its gradient terms are exact zeros; its
-// score term is then -sign(F) w and its d/d log s term a zero, the bits the
-// FP64 path produces.  Returns 0 (not decided), +1 or -1 (the sign of F).
-__device__ __forceinline__ int saturated_sign(const MapParams& m, const Q& q0, double alpha,
-                                              double thr) {
-  const int nt = m.nt, nb = m.nb;
-  float sum[2] = {0.f, 0.f}, mass = 0.f, spread = 0.f, emass = 0.f;
-  float pmax = 0.f;  // largest |log2| of a prefix or suffix product
-#pragma unroll 1
-  for (int side = 0; side < 2; side++) {
-    const int lo = side ? nt : 0, hi = side ? nt + nb : nt;
-    float run = 0.f;
-#pragma unroll 1
-    for (int i = lo; i < hi; i++) {
-      const Q d{sub(q0.w, m.r64[i][0]), sub(q0.x, m.r64[i][1]), sub(q0.y, m.r64[i][2]),
-                sub(q0.z, m.r64[i][3])};
-      const double b2 = norm2(d);
-      const Q d1{sub(d.w, 1.0), d.x, d.y, d.z};
-      // bases moderate (and normal in FP32) and away from 1 (the gradient's
-      // log and its inverse)
-      if (!(b2 > 1e-30 && b2 < 1e30) || !(norm2(d1) > 1e-20)) return 0;
-      const float lf = (float)m.e64[i] * 0.5f * __log2f((float)b2);  // log2 |factor|
-      run += lf;
-      mass += fabsf(lf);
-      emass += fabsf((float)m.e64[i]);
-      spread += 2.f * fabsf(lf);
-      pmax = fmaxf(pmax, fabsf(run));
-    }
-    sum[side] = run;
-    // suffix products: total minus a prefix, bounded by |total| + max |prefix|
-    pmax = fmaxf(pmax, fabsf(run) + pmax);
-  }
-  const float ls = __log2f((float)m.scale);
-  const float l2R = sum[0] - sum[1];
-  const float F = (l2R + ls) * 0.6931472f;
-  // FP32 error: conversions and products ~6e-8 relative per term, the
-  // running sums n * 6e-8 of their partial sums (<= 4e-6 of the term mass for
-  // n <= 128), the log2 approximation ~2e-7 absolute times each exponent
-  const float err = 4e-6f * (mass + fabsf(ls) + 1.f) + 3e-7f * (emass + 1.f) + 1e-6f * fabsf(F);
-  const float a = (float)fabs(alpha);
-  const float Fm = fabsf(F) - err, Fmt = fabsf(F - (float)thr) - err;
-  if (!(a * Fm >= 25.f && a * Fmt >= 25.f)) return 0;
-  // every product within 2^+-450 (no FP64 overflow or underflow, |B|^2 and
-  // |q1|^2 in range), |R| and |B| within the gradient path's bounds
-  if (!(pmax + err < 450.f && fabsf(l2R) + err < 400.f && fabsf(sum[1]) + err < 200.f &&
-        spread + err < 250.f && fabsf(l2R + ls) + err < 450.f))
-    return 0;
-  return F > 0.f ? 1 : -1;
-}
-
 // Block b takes a contiguous range of voxels, EN_T at a time.  Every voxel's
-// map, field, score and d/d log s term are computed in the first step; the
-// voxels whose other gradient terms are not all exact zeros (saturated tanh
-// or zero weight, with every intermediate provably in range) are queued in
-// shared memory in voxel order and their terms computed EN_T at a time, so
-// the expensive per-parameter loop runs in full warps.
+// map, field, score and d/d log s term are computed in the first step.  The
+// per-parameter terms are skipped where they are exact zeros (saturated tanh
+// or zero weight, with every intermediate provably in range); a warp with at
+// least 16 voxels needing them computes them at once from the factors it
+// holds, sparser ones queue their voxels in shared memory, in voxel order,
+// to be re-evaluated and computed EN_T at a time in full warps.
 template <bool POW_REF>
 __global__ void __launch_bounds__(EN_T, 4) tanh_grad_kernel(const __grid_constant__ MapParams m,
                                                          const GridParams g, const WeightGrid wg,
@@ -541,8 +486,6 @@ __global__ void __launch_bounds__(EN_T, 4) tanh_grad_kernel(const __grid_constan
     const double e = fabs(m.ep[i]);
     k_ok = k_ok && (e == 0.0 || (e >= 1e-10 && e <= 1e10));
   }
-  // the FP32 classification (one application, no field to write)
-  const bool fast = max_it == 1 && field == nullptr && k_ok;
   const long long per = (N + gridDim.x - 1) / gridDim.x;
   const long long lo_b = (long long)blockIdx.x * per;
   const long long hi_b = lo_b + per < N ? lo_b + per : N;
@@ -575,24 +518,14 @@ __global__ void __launch_bounds__(EN_T, 4) tanh_grad_kernel(const __grid_constan
     bool want = false, ext = false;
     Voxel v;
     v.over = false;
+    v.iterated = false;
+    v.its = 0;
     double dSdF = 0;
     QX Tx = {Q{1, 0, 0, 0}, 0}, Bx = Tx, Rx = Tx;
     Q q0 = {0, 0, 0, 0};
-    int sat = 0;
-    if (live && fast) {
-      double p[3];
-      cell(idx, p);
-      q0 = Q{p[0], p[1], p[2], g.slice};
-      const double mq = mag(q0);
-      if (mq >= 1e-8 && mq < 20.0) sat = saturated_sign(m, q0, alpha, thr);
-      if (sat) {
-        const double w = trilinear(wg, weights, p);
-        const double S = sat > 0 ? 1.0 : -1.0;  // tanh of a saturated argument
-        c_score = mul(-S, w);
-        c_exp = mul(mul(-alpha, w), sub(1.0, mul(S, S)));
-      }
-    }
-    if (live && !sat) {
+    Q Rg = {0, 0, 0, 0};
+    double RRg = 0;
+    if (live) {
       double p[3];
       cell(idx, p);
       q0 = Q{p[0], p[1], p[2], g.slice};
@@ -610,8 +543,8 @@ __global__ void __launch_bounds__(EN_T, 4) tanh_grad_kernel(const __grid_constan
       }
       c_over = v.over ? 1.0 : 0.0;
       if (v.iterated && !v.over) {
-        Q R;
-        double RR;
+        Q& R = Rg;
+        double& RR = RRg;
         if (grad_setup(v, logs, alpha, thr, w, R, dSdF, RR)) {
           // dSdF = 0 makes every term dSdF * y an exact zero; y stays finite
           // when the factors' magnitudes spread over at most 2^300, every
@@ -652,8 +585,15 @@ __global__ void __launch_bounds__(EN_T, 4) tanh_grad_kernel(const __grid_constan
     warp_accum(acc, s_band, c_band);
     if (__any_sync(0xffffffffu, ext))
       grad_terms_ext(m, q0, ext, Rx, Tx, Bx, dSdF, Pf, Pe, Sf, Se, acc, s_bulkb_x);
-    // append the voxels that need their terms, in voxel order
-    const unsigned bal = __ballot_sync(0xffffffffu, want);
+    // a warp with many voxels needing their terms computes them now, from
+    // the factors it holds; the others append theirs to the queue, in voxel
+    // order, to be computed in full warps
+    unsigned bal = __ballot_sync(0xffffffffu, want);
+    if (__popc(bal) >= 16) {
+      grad_terms<POW_REF>(m, v, want, Rg, dSdF, RRg, Pf, Sf, acc, s_bad);
+      bal = 0;
+      want = false;
+    }
     if (lane == 0) wcount[warp] = __popc(bal);
     __syncthreads();
     int off = queued;

@@ -11,7 +11,8 @@ namespace qj {
 
 int tanh_blocks();
 // out[] of launch_tanh_grad: [d log s, d bottom exps, d top exps, d sigma_t,
-// d sigma_b, score, overflowed voxels, non-finite terms left out, scratch]
+// d sigma_b, score, overflowed voxels, non-finite terms left out, scratch,
+// voxels with per-parameter terms]
 int tanh_slots(int nt, int nb);
 cudaError_t launch_tanh_grad(const MapParams& m, const GridParams& g, const WeightGrid& wg,
                              const double* weights, int max_it, double alpha, double thr,

@@ -131,8 +131,7 @@ int qjg_tanh_fit(qjg_ctx* ctx, int32_t mode, qjg_map_state* state, const qjg_gri
       for (int i = 0; i < n; i++) gv[i] = NAN;
       return 0;
     }
-    // no field during the solve (the score kernel then classifies saturated
-    // voxels in FP32); d_field is filled once at the end
+    // no field during the solve; d_field is filled once at the end
     cudaError_t e = qj::launch_tanh_grad(m, g, wg, d_weights, max_it, alpha, threshold, true,
                                          nullptr, d_part, nblocks, d_out, s);
     m_last = m;

@@ -113,39 +113,3 @@ def test_tanh_overflow_pass_matches_reference(ctx, tag):
     assert np.array_equal(np.isnan(gr), np.isnan(rg))
     ok = ~np.isnan(rg)
     np.testing.assert_allclose(gr[ok], rg[ok], rtol=1e-8, atol=1e-12 * max(1e-30, np.abs(rg[ok]).max()))
-
-
-@pytest.mark.parametrize("case_name", ["tanh_grad", "tanh_overflow_a", "tanh_overflow_b", "drawn"])
-def test_tanh_fast_classification_is_exact(ctx, case_name):
-    """Without a field to write, the kernel classifies saturated voxels from
-    FP32 log-magnitudes instead of evaluating the map in FP64; score and
-    gradients must keep every bit of the full FP64 pass (which a field
-    request forces)."""
-    if case_name == "drawn":
-        rs = draw_rootset(5, 10, 5, -1.2, 1.2, exps=(1, 2))
-        rs.sigma_top, rs.sigma_bottom = 1.3, 0.8
-        g = Grid((40, 36, 32))
-        rs.scale = conformal_scale(rs, g)
-        wg = Grid((20, 20, 20), lengths=(3.2, 3.2, 3.2))
-        c = cell_centers(wg)
-        wts = np.exp(-np.sum(c ** 2, axis=1)) * np.cos(2 * c[:, 0]) + 0.3
-    else:
-        name = "tanh_overflow" if case_name.startswith("tanh_overflow") else "tanh_grad"
-        rs, g, p, d = load_case(name)
-        if name == "tanh_overflow":
-            rs.sigma_top, rs.sigma_bottom, rs.scale = (float(v) for v in d[case_name[-1] + "_sigmas"])
-        wg, wts = _wgrid(d), d["weights"]
-    h = ctx.upload(rs)
-    w = torch.from_numpy(np.ascontiguousarray(wts, dtype=np.float64)).cuda()
-    f = torch.empty(g.n_voxels, dtype=torch.float64, device="cuda")
-    n = 3 + rs.n_top + rs.n_bottom
-    s_fast, g_fast, st_fast = ctx.tanh_score_grad(h, g, 1, wg, w.data_ptr(), n)
-    s_full, g_full, st_full = ctx.tanh_score_grad(h, g, 1, wg, w.data_ptr(), n,
-                                                  d_field=f.data_ptr())
-    ctx.free(h)
-    assert np.array_equal(np.float64(s_fast).view(np.uint64), np.float64(s_full).view(np.uint64))
-    assert np.array_equal(np.isnan(g_fast), np.isnan(g_full))
-    ok = ~np.isnan(g_full)
-    assert np.array_equal(g_fast[ok], g_full[ok])
-    assert st_fast["overflowed"] == st_full["overflowed"]
-    assert st_fast["bad_terms"] == st_full["bad_terms"]
