@@ -454,9 +454,56 @@ def bench_tooth(args):
     return res
 
 
+def bench_tanh(args):
+    """toothOptimizer's objective alone: one pass of the tanh score and its
+    21 gradients (FP64, reference rounding) on the synthetic tooth problem of
+    `bench_tooth` moved to the fractal frame, sigma 1 and the conformal
+    scale, on a res^3 grid (97 by default); `--steps` timed passes."""
+    import os
+    import tempfile
+
+    import numpy as np
+    import torch
+
+    from . import lib
+    from .rootsets import Grid
+    res = args.res or 97
+    ctx = lib.Context(0)
+    path = os.path.join(tempfile.mkdtemp(), "tanh_bench.o3d")
+    tooth_problem(path)
+    st = lib.o3d_read(path)
+    R = 4.0
+    tr, br = st["top_roots"].copy(), st["bottom_roots"].copy()
+    tr[1:, :3] += -0.5
+    br[1:, :3] += -0.5
+    rs = lib.RootSet(top_roots=tr * R, top_powers=st["top_powers"], bottom_roots=br * R,
+                     bottom_powers=st["bottom_powers"], scale=1.0)
+    dres, dc, dl, dd = st["distance"]
+    c = tuple((np.array(dc) - 0.5) * R)
+    wg = Grid(dres, c, tuple(np.array(dl) * R))
+    g = Grid((res,) * 3, c, wg.lengths)
+    dist = torch.from_numpy(np.ascontiguousarray(dd.ravel()) * R).cuda()
+    w = torch.empty_like(dist)
+    ctx.inverted_distance(dres, dist.data_ptr(), True, w.data_ptr())
+    h = ctx.upload(rs)
+    _, _, rs.scale = ctx.conformal_radius(h, g, wg, dist.data_ptr())
+    ctx.free(h)
+    h = ctx.upload(rs)
+    npar = 3 + rs.n_top + rs.n_bottom
+    ctx.tanh_score_grad(h, g, 1, wg, w.data_ptr(), npar)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        score, _, sst = ctx.tanh_score_grad(h, g, 1, wg, w.data_ptr(), npar)
+    ms = (time.perf_counter() - t0) / args.steps * 1e3
+    ctx.free(h)
+    return {"workload": "tanh score + %d gradients, 12 top / 6 bottom roots, %d^3" % (npar, res),
+            "ms_per_eval": ms, "voxels_per_s": g.n_voxels / ms * 1e3, "score": score, **sst}
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["mesh", "energy", "serve", "large", "tooth"])
+    ap.add_argument("what", choices=["mesh", "energy", "serve", "large", "tooth", "tanh"])
     ap.add_argument("--res", type=int, default=0, help="grid edge (mesh: 512, large: 2200)")
     ap.add_argument("--workload", default="precision", choices=["precision", "large"])
     ap.add_argument("--slab", type=int, default=64)
@@ -476,7 +523,7 @@ def main():
     ap.add_argument("--no-mesh", action="store_true")
     args = ap.parse_args()
     fn = {"mesh": bench_mesh, "energy": bench_energy, "serve": bench_serve,
-          "large": bench_large, "tooth": bench_tooth}[args.what]
+          "large": bench_large, "tooth": bench_tooth, "tanh": bench_tanh}[args.what]
     print(json.dumps(fn(args)), flush=True)
 
 
