@@ -95,8 +95,14 @@ __global__ void __launch_bounds__(128) refine64_kernel(const __grid_constant__ M
                                                        float* __restrict__ de, DevStats* st) {
   const unsigned long long n_list = counts->refined;
   unsigned long long iters_acc = 0;
-  for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < n_list;
-       k += (unsigned long long)gridDim.x * blockDim.x) {
+  // the list is sorted by FP32 orbit length: warps take 32-entry chunks
+  // (similar orbits, coherent warps) dealt round-robin over the blocks, so
+  // every SM gets short and long orbits alike
+  const unsigned long long slot = (threadIdx.x >> 5) * (unsigned long long)gridDim.x + blockIdx.x;
+  const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x >> 5);
+  for (unsigned long long c = slot; c * 32 < n_list; c += warps) {
+    const unsigned long long k = c * 32 + (threadIdx.x & 31);
+    if (k >= n_list) continue;
     const uint32_t i = list[k];
     const int x = (int)(i % (uint32_t)g.X);
     const int y = (int)((i / (uint32_t)g.X) % (uint32_t)g.Y);
@@ -505,8 +511,12 @@ __global__ void __launch_bounds__(128) refine64_batch_kernel(const BatchTable* _
                                                              DevStats* st) {
   const unsigned long long n_list = st->refined;
   unsigned long long iters_acc = 0;
-  for (unsigned long long j = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; j < n_list;
-       j += (unsigned long long)gridDim.x * blockDim.x) {
+  // sorted list: 32-entry chunks dealt round-robin over the blocks (as refine64_kernel)
+  const unsigned long long slot = (threadIdx.x >> 5) * (unsigned long long)gridDim.x + blockIdx.x;
+  const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x >> 5);
+  for (unsigned long long c = slot; c * 32 < n_list; c += warps) {
+    const unsigned long long j = c * 32 + (threadIdx.x & 31);
+    if (j >= n_list) continue;
     const uint32_t e = list[j];
     const int k = (int)(e >> BATCH_SHIFT);
     const uint32_t i = e & BATCH_MASK;
