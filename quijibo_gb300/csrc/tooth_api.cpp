@@ -330,11 +330,12 @@ int tooth_monitor(void* user, int32_t, double, double, const double* x) {
   qjg_map_state m = r.state();
   std::vector<double> tp(r.tpow), bp(r.bpow);
   lay.from_vars(x, m, tp.data(), bp.data());
-  // write the iterate's map, then restore the run's own copy
+  // write the iterate's map, then restore the run's own copy (element-wise:
+  // the running fit holds pointers into these arrays)
   std::vector<double> keep_t(r.tpow), keep_b(r.bpow);
   const double ks[3] = {r.sig_t, r.sig_b, r.scale};
-  r.tpow = tp;
-  r.bpow = bp;
+  std::copy(tp.begin(), tp.end(), r.tpow.begin());
+  std::copy(bp.begin(), bp.end(), r.bpow.begin());
   r.take(m);
   // the fractal of the iterate, as the reference's last evaluation left it
   std::vector<double> g(3 + tp.size() + bp.size());
@@ -344,8 +345,8 @@ int tooth_monitor(void* user, int32_t, double, double, const double* x) {
                                g.data(), r.d_field.p, nullptr, r.s);
   });
   if (!rc) rc = r.write_state(r.cfg->checkpoint_path, r.cur_res);
-  r.tpow = keep_t;
-  r.bpow = keep_b;
+  std::copy(keep_t.begin(), keep_t.end(), r.tpow.begin());
+  std::copy(keep_b.begin(), keep_b.end(), r.bpow.begin());
   r.sig_t = ks[0];
   r.sig_b = ks[1];
   r.scale = ks[2];
