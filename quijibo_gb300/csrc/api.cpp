@@ -81,6 +81,20 @@ GridParams qj_grid_params(const qjg_grid* g, int z0, int z1) {
   }
   rotation_matrix(g->rot, p.R);
   p.slice = g->slice;
+  // cell centre = center + R (center - half + (idx + 0.5) dx - center)
+  auto split = [](double v, float out[2]) {
+    out[0] = (float)v;
+    out[1] = (float)(v - (double)out[0]);
+  };
+  for (int c = 0; c < 3; c++) {
+    double a = p.center[c];
+    for (int k = 0; k < 3; k++) {
+      a += p.R[c][k] * (-p.half[k] + 0.5 * p.dx[k]);
+      split(p.R[c][k] * p.dx[k], p.ffb[c][k]);
+    }
+    split(a, p.ffa[c]);
+  }
+  split(p.slice, p.ffslice);
   return p;
 }
 
@@ -114,6 +128,8 @@ IterParams qj_iter_params(const qjg_iter* it, const qjg_grid* g) {
   p.est_tol = it->rel_tol > 0 ? it->rel_tol : 0.0;
   p.ff_head = 2;
   p.lagrange = it->form == QJG_FORM_LAGRANGE ? 1 : 0;
+  p.field_tolf = (float)p.field_tol;
+  p.est_tolf = (float)p.est_tol;
   return p;
 }
 

@@ -191,9 +191,9 @@ __device__ __forceinline__ int orbit_finish(const Orbit32& o, const IterParams& 
     // iterate on either side of the radius.
     const bool near_escape =
         DE && (o.near || (o.m2 >= esc2 && o.n < it.max_it && q32::near_radius(o.m2, esc2, o.err)));
-    if (bad || near_escape || l2abs_d < l2band || fabsf(f) < (float)it.field_tol)
+    if (bad || near_escape || l2abs_d < l2band || fabsf(f) < it.field_tolf)
       route = TO_FP64;
-    else if (it.est_tol > 0.0 && !(o.err <= (float)it.est_tol * fabsf(f)))
+    else if (it.est_tolf > 0.f && !(o.err <= it.est_tolf * fabsf(f)))
       route = (allow_ff && it.ff_head > 0) ? TO_FF : TO_FP64;
   }
   if (route == WRITTEN) {
@@ -370,17 +370,14 @@ __global__ void __launch_bounds__(128, NT > 0 ? 4 : 0) field32x2_kernel(const __
 // One re-run voxel (local index i); returns its route (WRITTEN or TO_FP64)
 // and leaves its orbit in *o.
 __device__ __forceinline__ int rerun_voxel(const MapParams& m, const GridParams& g,
-                                           const IterParams& it, uint32_t i,
-                                           double* __restrict__ field, float* __restrict__ de,
-                                           Orbit32* o, unsigned long long& nonfinite_acc) {
-  const float esc2 = (float)(it.escape * it.escape);
+                                           const IterParams& it, float esc2, float l2band,
+                                           uint32_t i, double* __restrict__ field,
+                                           float* __restrict__ de, Orbit32* o,
+                                           unsigned long long& nonfinite_acc) {
   const int x = (int)(i % (uint32_t)g.X);
   const int y = (int)((i / (uint32_t)g.X) % (uint32_t)g.Y);
   const int zl = (int)(i / ((uint32_t)g.X * (uint32_t)g.Y));
-  double p[3];
-  cell_center(g, x, y, g.z0 + zl, p);
-  qff::Q q = {qff::from_double(p[0]), qff::from_double(p[1]), qff::from_double(p[2]),
-              qff::from_double(g.slice)};
+  qff::Q q = qff::cell_center_ff(g, x, y, g.z0 + zl);
   *o = orbit_start(true, qff::norm2(q).hi, esc2, it.max_it);
   for (int h = 0; h < it.ff_head && o->live; h++) {
     float gg = 0.f;
@@ -395,8 +392,7 @@ __device__ __forceinline__ int rerun_voxel(const MapParams& m, const GridParams&
     qf = apply32<true>(m, qf, &gg);
     orbit_step<true>(*o, q32::norm2(qf), gg, esc2, it.max_it);
   }
-  return orbit_finish<true>(*o, it, esc2, log2f((float)it.band), 1, false, i, field, de,
-                            nonfinite_acc);
+  return orbit_finish<true>(*o, it, esc2, l2band, 1, false, i, field, de, nonfinite_acc);
 }
 
 __global__ void __launch_bounds__(128) rerun_ff_kernel(const __grid_constant__ MapParams m,
@@ -409,6 +405,7 @@ __global__ void __launch_bounds__(128) rerun_ff_kernel(const __grid_constant__ M
   const int lane = threadIdx.x & 31;
   const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
   unsigned long long iters_acc = 0, nonfinite_acc = 0;
+  const float esc2 = (float)(it.escape * it.escape), l2band = log2f((float)it.band);
   // warp-uniform trips: the append below is a warp collective
   for (unsigned long long base = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) & ~31ull;
        base < n_list; base += stride) {
@@ -418,7 +415,7 @@ __global__ void __launch_bounds__(128) rerun_ff_kernel(const __grid_constant__ M
     Orbit32 o = orbit_start(false, 0.f, 0.f, 0);
     if (k < n_list) {
       i = ff_list[k];
-      route = rerun_voxel(m, g, it, i, field, de, &o, nonfinite_acc);
+      route = rerun_voxel(m, g, it, esc2, l2band, i, field, de, &o, nonfinite_acc);
       iters_acc += o.n;
     }
     warp_append(route == TO_FP64, i, o.n, false, 0, 0, &st->refined, list, keys);
@@ -494,7 +491,9 @@ __global__ void __launch_bounds__(128) rerun_ff_batch_kernel(const BatchTable* _
       e = ff_list[j];
       const int k = (int)(e >> BATCH_SHIFT);
       const BatchItem& b = tab->items[k];
-      route = rerun_voxel(maps[k], b.g, b.it, e & BATCH_MASK, b.field, b.de, &o, nonfinite_acc);
+      route = rerun_voxel(maps[k], b.g, b.it, (float)(b.it.escape * b.it.escape),
+                          log2f((float)b.it.band), e & BATCH_MASK, b.field, b.de, &o,
+                          nonfinite_acc);
       iters_acc += o.n;
     }
     warp_append(route == TO_FP64, e, o.n, false, 0, 0, &st->refined, list, keys);

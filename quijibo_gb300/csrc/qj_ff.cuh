@@ -147,6 +147,22 @@ __device__ __forceinline__ Q qpow_int(const Q& d, int n) {
   return r;
 }
 
+// The cell centre (x, y, z) of g as double-float, from the affine
+// coefficients of GridParams: within ~2^-44 of the exact centre, like a
+// double rounded to a pair, without FP64 instructions.
+__device__ __forceinline__ Q cell_center_ff(const GridParams& g, int x, int y, int z) {
+  const float idx[3] = {(float)x, (float)y, (float)z};  // exact (< 2^24)
+  F p[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    F s = {g.ffa[c][0], g.ffa[c][1]};
+#pragma unroll
+    for (int k = 0; k < 3; k++) s = add(s, mul(F{g.ffb[c][k][0], g.ffb[c][k][1]}, idx[k]));
+    p[c] = s;
+  }
+  return Q{p[0], p[1], p[2], F{g.ffslice[0], g.ffslice[1]}};
+}
+
 }  // namespace qff
 
 // One root term (q - r_i)^(e_i) in double-float (integer exponents only);

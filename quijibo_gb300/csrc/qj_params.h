@@ -45,6 +45,12 @@ struct GridParams {
   double dx[3];      // lengths / res
   double R[3][3];    // rotation matrix of the grid quaternion
   double slice;      // the fourth (k) coordinate of every start point
+  // the cell centre as an affine map of (x, y, z), p_c = a_c + sum_k b_ck idx_k,
+  // as double-float pairs (hi, lo): the double-float re-run starts from it
+  // without FP64 arithmetic
+  float ffa[3][2];
+  float ffb[3][3][2];
+  float ffslice[2];
 };
 
 // A FIELD_3D sampled by trilinear lookup: first cell centre and 1/dx
@@ -69,6 +75,8 @@ struct IterParams {
   double est_tol;
   int ff_head;
   int lagrange;      // the map in RATIONAL_4D::evaluateLagrange order (FP64 form)
+  float field_tolf;  // field_tol and est_tol as FP32 (the FP32 kernels' tests)
+  float est_tolf;
 };
 
 // Device-side counters of one field or mesh call.
