@@ -250,9 +250,7 @@ __global__ void __launch_bounds__(128) field32_kernel(const __grid_constant__ Ma
     const int x = (int)(r % tm.tx_n) * TILE_X + (lane & 7);
     const int y = (int)(r / tm.tx_n) * TILE_Y + (lane >> 3);
     const bool valid = (x < g.X && y < g.Y);
-    double p[3];
-    cell_center(g, x, y, g.z0 + zl, p);
-    Q q = {(float)p[0], (float)p[1], (float)p[2], (float)g.slice};
+    Q q = qff::cell_center_f32(g, x, y, g.z0 + zl);
     Orbit32 o = orbit_start(valid, norm2(q), esc2, it.max_it);
     while (o.live) {
       float gg = 0.f;
@@ -296,22 +294,20 @@ __device__ __forceinline__ unsigned long long tile2(const MapParams& m, const Gr
                                                     double* __restrict__ field,
                                                     float* __restrict__ de, const RefineLists& rl,
                                                     int refine, bool allow_ff, uint32_t tag,
-                                                    DevStats* st, BulkAcc& acc) {
+                                                    DevStats* st, BulkAcc& acc, float esc2,
+                                                    float l2band) {
   using namespace q32x2;
   const TileMap tm = tile_map(g, TILE2_X);
   const int lane = threadIdx.x & 31;
-  const float esc2 = (float)(it.escape * it.escape);
-  const float l2band = log2f((float)it.band);
   const int zl = (int)(t / tm.per_slice);
   const long long r = t - (long long)zl * tm.per_slice;
   const int x = (int)(r % tm.tx_n) * TILE2_X + 2 * (lane & 7);
   const int y = (int)(r / tm.tx_n) * TILE_Y + (lane >> 3);
   const bool va = (x < g.X && y < g.Y), vb = (x + 1 < g.X && y < g.Y);
-  double pa[3], pb[3];
-  cell_center(g, x, y, g.z0 + zl, pa);
-  cell_center(g, x + 1, y, g.z0 + zl, pb);
-  Q2 q = {make_float2((float)pa[0], (float)pb[0]), make_float2((float)pa[1], (float)pb[1]),
-          make_float2((float)pa[2], (float)pb[2]), pair((float)g.slice)};
+  // start points from the double-float cell centre: no FP64 at the tile start
+  const q32::Q pa = qff::cell_center_f32(g, x, y, g.z0 + zl);
+  const q32::Q pb = qff::cell_center_f32(g, x + 1, y, g.z0 + zl);
+  Q2 q = join(pa, pb);
   const float2 m20 = norm2(q);
   Orbit32 a = orbit_start(va, m20.x, esc2, it.max_it);
   Orbit32 b = orbit_start(vb, m20.y, esc2, it.max_it);
@@ -351,11 +347,12 @@ __global__ void __launch_bounds__(128, NT > 0 ? 4 : 0) field32x2_kernel(const __
                                                         int refine, DevStats* st) {
   const TileMap tm = tile_map(g, TILE2_X);
   const bool allow_ff = rl.ff != nullptr;
+  const float esc2 = (float)(it.escape * it.escape), l2band = log2f((float)it.band);
   BulkAcc acc;
   for (;;) {
     const long long t = next_tile(&st->tiles_done);
     if (t >= tm.total) break;
-    tile2<DE, NT, NB>(m, g, it, t, field, de, rl, refine, allow_ff, 0u, st, acc);
+    tile2<DE, NT, NB>(m, g, it, t, field, de, rl, refine, allow_ff, 0u, st, acc, esc2, l2band);
   }
   warp_add(&st->voxel_iters, acc.iters);
   warp_add(&st->nonfinite, acc.nonfinite);
@@ -464,7 +461,8 @@ __global__ void __launch_bounds__(128) field32x2_batch_kernel(const BatchTable* 
     const bool allow_ff = rl.ff != nullptr && b.refine && m.all_int && b.it.est_tol > 0.0;
     const unsigned long long it_sum =
         tile2<DE>(m, b.g, b.it, t - tile0[k], b.field, b.de, rl, b.refine, allow_ff,
-                  (uint32_t)k << BATCH_SHIFT, st, acc);
+                  (uint32_t)k << BATCH_SHIFT, st, acc, (float)(b.it.escape * b.it.escape),
+                  log2f((float)b.it.band));
     if ((threadIdx.x & 31) == 0) atomicAdd(&counts[k].voxel_iters, it_sum);
   }
   warp_add(&st->voxel_iters, acc.iters);

@@ -163,6 +163,13 @@ __device__ __forceinline__ Q cell_center_ff(const GridParams& g, int x, int y, i
   return Q{p[0], p[1], p[2], F{g.ffslice[0], g.ffslice[1]}};
 }
 
+// The FP32 start point of the bulk kernels: the cell centre rounded to FP32
+// from its double-float value (the FP32 rounding of the exact centre, as a
+// double centre rounded to FP32 gives but for ties within 2^-44)
+__device__ __forceinline__ q32::Q cell_center_f32(const GridParams& g, int x, int y, int z) {
+  return hi(cell_center_ff(g, x, y, z));
+}
+
 }  // namespace qff
 
 // One root term (q - r_i)^(e_i) in double-float (integer exponents only);
