@@ -452,9 +452,10 @@ __device__ __noinline__ void grad_terms_ext(const MapParams& m, const Q q0, bool
 // map, field, score and d/d log s term are computed in the first step.  The
 // per-parameter terms are skipped where they are exact zeros (saturated tanh
 // or zero weight, with every intermediate provably in range); a warp with at
-// least 16 voxels needing them computes them at once from the factors it
-// holds, sparser ones queue their voxels in shared memory, in voxel order,
-// to be re-evaluated and computed EN_T at a time in full warps.
+// least 24 voxels needing them computes them at once from the factors it
+// holds (16.2 / 15.0 / 14.5 ms per pass at 8 / 16 / 24 on the 97^3
+// objective benchmark), sparser ones queue their voxels in shared memory, in
+// voxel order, to be re-evaluated and computed EN_T at a time in full warps.
 template <bool POW_REF>
 __global__ void __launch_bounds__(EN_T, 4) tanh_grad_kernel(const __grid_constant__ MapParams m,
                                                          const GridParams g, const WeightGrid wg,
@@ -589,7 +590,7 @@ __global__ void __launch_bounds__(EN_T, 4) tanh_grad_kernel(const __grid_constan
     // the factors it holds; the others append theirs to the queue, in voxel
     // order, to be computed in full warps
     unsigned bal = __ballot_sync(0xffffffffu, want);
-    if (__popc(bal) >= 16) {
+    if (__popc(bal) >= 24) {
       grad_terms<POW_REF>(m, v, want, Rg, dSdF, RRg, Pf, Sf, acc, s_bad);
       bal = 0;
       want = false;
