@@ -392,6 +392,50 @@ __device__ __forceinline__ int rerun_voxel(const MapParams& m, const GridParams&
   return orbit_finish<true>(*o, it, esc2, l2band, 1, false, i, field, de, nonfinite_acc);
 }
 
+// rerun_voxel for two listed voxels on one lane (b may be absent), on packed
+// f32x2 operands: each voxel gets the bits of rerun_voxel.
+__device__ __forceinline__ void rerun_pair(const MapParams& m, const GridParams& g,
+                                           const IterParams& it, float esc2, float l2band,
+                                           uint32_t ia, bool vb, uint32_t ib,
+                                           double* __restrict__ field, float* __restrict__ de,
+                                           Orbit32* oa, Orbit32* ob, int* ra, int* rb,
+                                           unsigned long long& nonfinite_acc) {
+  auto centre = [&](uint32_t i) {
+    const int x = (int)(i % (uint32_t)g.X);
+    const int y = (int)((i / (uint32_t)g.X) % (uint32_t)g.Y);
+    const int zl = (int)(i / ((uint32_t)g.X * (uint32_t)g.Y));
+    return qff::cell_center_ff(g, x, y, g.z0 + zl);
+  };
+  const qff::Q qa = centre(ia);
+  qff2::Q q = qff2::join(qa, vb ? centre(ib) : qa);
+  qff2::F2 n2 = qff2::norm2(q);
+  *oa = orbit_start(true, n2.hi.x, esc2, it.max_it);
+  *ob = orbit_start(vb, n2.hi.y, esc2, it.max_it);
+  for (int h = 0; h < it.ff_head && (oa->live || ob->live); h++) {
+    float2 gg = q32x2::pair(0.f);
+    q = apply_ff2<true>(m, q, &gg);
+    oa->err = q32::EPS32;  // double-float iterates: only their FP32 rounding counts
+    ob->err = q32::EPS32;
+    n2 = qff2::norm2(q);
+    orbit_step<true>(*oa, n2.hi.x, gg.x, esc2, it.max_it);
+    orbit_step<true>(*ob, n2.hi.y, gg.y, esc2, it.max_it);
+  }
+  oa->err = q32::EPS32;
+  ob->err = q32::EPS32;
+  q32x2::Q2 qf = qff2::hi(q);
+  while (oa->live || ob->live) {
+    float2 gg = q32x2::pair(0.f);
+    qf = apply32x2<true>(m, qf, &gg);
+    const float2 m2 = q32x2::norm2(qf);
+    orbit_step<true>(*oa, m2.x, gg.x, esc2, it.max_it);
+    orbit_step<true>(*ob, m2.y, gg.y, esc2, it.max_it);
+  }
+  *ra = orbit_finish<true>(*oa, it, esc2, l2band, 1, false, ia, field, de, nonfinite_acc);
+  *rb = vb ? orbit_finish<true>(*ob, it, esc2, l2band, 1, false, ib, field, de, nonfinite_acc)
+           : WRITTEN;
+}
+
+// Two consecutive list entries per lane.
 __global__ void __launch_bounds__(128) rerun_ff_kernel(const __grid_constant__ MapParams m,
                                                        const GridParams g, const IterParams it,
                                                        const uint32_t* __restrict__ ff_list,
@@ -400,22 +444,26 @@ __global__ void __launch_bounds__(128) rerun_ff_kernel(const __grid_constant__ M
                                                        uint8_t* keys, DevStats* st) {
   const unsigned long long n_list = st->rerun;
   const int lane = threadIdx.x & 31;
-  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x * 2;
   unsigned long long iters_acc = 0, nonfinite_acc = 0;
   const float esc2 = (float)(it.escape * it.escape), l2band = log2f((float)it.band);
   // warp-uniform trips: the append below is a warp collective
-  for (unsigned long long base = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) & ~31ull;
+  for (unsigned long long base =
+           ((blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) & ~31ull) * 2;
        base < n_list; base += stride) {
-    const unsigned long long k = base + lane;
-    uint32_t i = 0;
-    int route = WRITTEN;
-    Orbit32 o = orbit_start(false, 0.f, 0.f, 0);
+    const unsigned long long k = base + 2 * lane;
+    uint32_t ia = 0, ib = 0;
+    int ra = WRITTEN, rb = WRITTEN;
+    Orbit32 oa = orbit_start(false, 0.f, 0.f, 0), ob = oa;
     if (k < n_list) {
-      i = ff_list[k];
-      route = rerun_voxel(m, g, it, esc2, l2band, i, field, de, &o, nonfinite_acc);
-      iters_acc += o.n;
+      ia = ff_list[k];
+      const bool vb = k + 1 < n_list;
+      if (vb) ib = ff_list[k + 1];
+      rerun_pair(m, g, it, esc2, l2band, ia, vb, ib, field, de, &oa, &ob, &ra, &rb,
+                 nonfinite_acc);
+      iters_acc += oa.n + ob.n;
     }
-    warp_append(route == TO_FP64, i, o.n, false, 0, 0, &st->refined, list, keys);
+    warp_append(ra == TO_FP64, ia, oa.n, rb == TO_FP64, ib, ob.n, &st->refined, list, keys);
   }
   warp_add(&st->rerun_iters, iters_acc);
   warp_add(&st->nonfinite, nonfinite_acc);

@@ -229,4 +229,205 @@ __device__ __forceinline__ qff::Q apply_ff(const MapParams& m, const qff::Q& q, 
   return out;
 }
 
+// ---- two voxels per lane -------------------------------------------------
+// The same double-float arithmetic on packed f32x2 operands (voxel a in .x,
+// voxel b in .y).  Every packed operation rounds each half as its scalar
+// form does, so each voxel gets the bits of the one-voxel code.
+namespace qff2 {
+
+using q32x2::add2;
+using q32x2::fma2;
+using q32x2::mul2;
+using q32x2::neg2;
+using q32x2::pair;
+
+struct F2 {
+  float2 hi, lo;
+};
+
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return add2(a, neg2(b)); }
+
+__device__ __forceinline__ F2 two_sum(float2 a, float2 b) {
+  const float2 s = add2(a, b);
+  const float2 bb = sub2(s, a);
+  const float2 e = add2(sub2(a, sub2(s, bb)), sub2(b, bb));
+  return F2{s, e};
+}
+
+__device__ __forceinline__ F2 fast_two_sum(float2 a, float2 b) {
+  const float2 s = add2(a, b);
+  return F2{s, sub2(b, sub2(s, a))};
+}
+
+__device__ __forceinline__ F2 two_prod(float2 a, float2 b) {
+  const float2 p = mul2(a, b);
+  return F2{p, fma2(a, b, neg2(p))};
+}
+
+__device__ __forceinline__ F2 neg(F2 a) { return F2{neg2(a.hi), neg2(a.lo)}; }
+
+__device__ __forceinline__ F2 add(F2 a, F2 b) {
+  const F2 s = two_sum(a.hi, b.hi);
+  return fast_two_sum(s.hi, add2(s.lo, add2(a.lo, b.lo)));
+}
+
+__device__ __forceinline__ F2 mul(F2 a, F2 b) {
+  const F2 p = two_prod(a.hi, b.hi);
+  return fast_two_sum(p.hi, fma2(a.hi, b.lo, fma2(a.lo, b.hi, p.lo)));
+}
+
+__device__ __forceinline__ F2 mul(F2 a, float2 b) {
+  const F2 p = two_prod(a.hi, b);
+  return fast_two_sum(p.hi, fma2(a.lo, b, p.lo));
+}
+
+__device__ __forceinline__ F2 dot4(F2 a0, F2 b0, F2 a1, F2 b1, F2 a2, F2 b2, F2 a3, F2 b3) {
+  const F2 p0 = two_prod(a0.hi, b0.hi), p1 = two_prod(a1.hi, b1.hi);
+  const F2 p2 = two_prod(a2.hi, b2.hi), p3 = two_prod(a3.hi, b3.hi);
+  float2 e = fma2(a0.hi, b0.lo, fma2(a0.lo, b0.hi, p0.lo));
+  e = add2(e, fma2(a1.hi, b1.lo, fma2(a1.lo, b1.hi, p1.lo)));
+  e = add2(e, fma2(a2.hi, b2.lo, fma2(a2.lo, b2.hi, p2.lo)));
+  e = add2(e, fma2(a3.hi, b3.lo, fma2(a3.lo, b3.hi, p3.lo)));
+  F2 t = two_sum(p0.hi, p1.hi);
+  e = add2(e, t.lo);
+  t = two_sum(t.hi, p2.hi);
+  e = add2(e, t.lo);
+  t = two_sum(t.hi, p3.hi);
+  e = add2(e, t.lo);
+  return fast_two_sum(t.hi, e);
+}
+
+struct Q {
+  F2 w, x, y, z;
+};
+
+__device__ __forceinline__ Q qmul(const Q& a, const Q& b) {
+  Q o;
+  o.w = dot4(a.w, b.w, a.x, neg(b.x), a.y, neg(b.y), a.z, neg(b.z));
+  o.x = dot4(a.w, b.x, a.x, b.w, a.y, b.z, a.z, neg(b.y));
+  o.y = dot4(a.w, b.y, a.x, neg(b.z), a.y, b.w, a.z, b.x);
+  o.z = dot4(a.w, b.z, a.x, b.y, a.y, neg(b.x), a.z, b.w);
+  return o;
+}
+
+__device__ __forceinline__ Q qmul_conj(const Q& a, const Q& b) {
+  Q o;
+  o.w = dot4(a.w, b.w, a.x, b.x, a.y, b.y, a.z, b.z);
+  o.x = dot4(a.w, neg(b.x), a.x, b.w, a.y, neg(b.z), a.z, b.y);
+  o.y = dot4(a.w, neg(b.y), a.x, b.z, a.y, b.w, a.z, neg(b.x));
+  o.z = dot4(a.w, neg(b.z), a.x, neg(b.y), a.y, b.x, a.z, b.w);
+  return o;
+}
+
+__device__ __forceinline__ Q qsq(const Q& a) {
+  Q o;
+  o.w = dot4(a.w, a.w, a.x, neg(a.x), a.y, neg(a.y), a.z, neg(a.z));
+  const F2 w2 = F2{mul2(pair(2.f), a.w.hi), mul2(pair(2.f), a.w.lo)};  // exact
+  o.x = mul(w2, a.x);
+  o.y = mul(w2, a.y);
+  o.z = mul(w2, a.z);
+  return o;
+}
+
+__device__ __forceinline__ F2 norm2(const Q& q) {
+  return dot4(q.w, q.w, q.x, q.x, q.y, q.y, q.z, q.z);
+}
+
+__device__ __forceinline__ q32x2::Q2 hi(const Q& q) {
+  return q32x2::Q2{q.w.hi, q.x.hi, q.y.hi, q.z.hi};
+}
+
+__device__ __forceinline__ float2 rcp2(float2 x) {
+  return make_float2(q32::rcp_approx(x.x), q32::rcp_approx(x.y));
+}
+
+__device__ __forceinline__ F2 recip(F2 a) {
+  const float2 r = rcp2(a.hi);
+  const F2 ar = mul(a, r);
+  const F2 resid = add(F2{pair(1.f), pair(0.f)}, neg(ar));
+  return add(F2{r, pair(0.f)}, mul(resid, r));
+}
+
+__device__ __forceinline__ Q qpow_int(const Q& d, int n) {
+  if (n == 1) return d;
+  if (n == 2) return qsq(d);
+  Q r = d, b = d;
+  bool first = true;
+  while (n) {
+    if (n & 1) {
+      r = first ? b : qmul(r, b);
+      first = false;
+    }
+    n >>= 1;
+    if (n) b = qsq(b);
+  }
+  return r;
+}
+
+__device__ __forceinline__ F2 join(const qff::F& a, const qff::F& b) {
+  return F2{make_float2(a.hi, b.hi), make_float2(a.lo, b.lo)};
+}
+
+__device__ __forceinline__ Q join(const qff::Q& a, const qff::Q& b) {
+  return Q{join(a.w, b.w), join(a.x, b.x), join(a.y, b.y), join(a.z, b.z)};
+}
+
+}  // namespace qff2
+
+// root_term_ff for two voxels
+template <bool DE>
+__device__ __forceinline__ qff2::Q root_term_ff2(const MapParams& m, const qff2::Q& q, int i,
+                                                 q32x2::Q2& g) {
+  using namespace qff2;
+  auto rootc = [&](int c) {
+    return F2{pair(m.rff[i][c][0]), pair(m.rff[i][c][1])};
+  };
+  const Q d = {add(q.w, neg(rootc(0))), add(q.x, neg(rootc(1))), add(q.y, neg(rootc(2))),
+               add(q.z, neg(rootc(3)))};
+  if (DE) {
+    const q32x2::Q2 dh = hi(d);
+    const float2 k = mul2(pair(m.x32[i][0]), rcp2(q32x2::norm2(dh)));
+    g.w = fma2(k, dh.w, g.w);
+    g.x = fma2(k, dh.x, g.x);
+    g.y = fma2(k, dh.y, g.y);
+    g.z = fma2(k, dh.z, g.z);
+  }
+  return qpow_int(d, m.ie[i]);
+}
+
+template <bool DE>
+__device__ __forceinline__ qff2::Q product_ff2(const MapParams& m, const qff2::Q& q, int lo,
+                                               int hi, q32x2::Q2& g) {
+  qff2::Q r = root_term_ff2<DE>(m, q, lo, g);
+#pragma unroll 1
+  for (int i = lo + 1; i < hi; i++) r = qff2::qmul(r, root_term_ff2<DE>(m, q, i, g));
+  return r;
+}
+
+// apply_ff for two voxels; *g2 = each one's |grad log|R||^2 in FP32
+template <bool DE>
+__device__ __forceinline__ qff2::Q apply_ff2(const MapParams& m, const qff2::Q& q, float2* g2) {
+  using namespace qff2;
+  q32x2::Q2 g = {pair(0.f), pair(0.f), pair(0.f), pair(0.f)};
+  const Q top = product_ff2<DE>(m, q, 0, m.nt, g);
+  const F2 s = {pair(m.scale_ff[0]), pair(m.scale_ff[1])};
+  Q out;
+  if (m.nb > 0) {
+    const Q bot = product_ff2<DE>(m, q, m.nt, m.nt + m.nb, g);
+    const F2 inv = mul(recip(norm2(bot)), s);
+    out = qmul_conj(top, bot);
+    out.w = mul(out.w, inv);
+    out.x = mul(out.x, inv);
+    out.y = mul(out.y, inv);
+    out.z = mul(out.z, inv);
+  } else {
+    out.w = mul(top.w, s);
+    out.x = mul(top.x, s);
+    out.y = mul(top.y, s);
+    out.z = mul(top.z, s);
+  }
+  if (DE) *g2 = q32x2::norm2(g);
+  return out;
+}
+
 }  // namespace qj
