@@ -315,6 +315,12 @@ __device__ __forceinline__ void grad_terms(const MapParams& m, const Voxel& v, b
   const Q& B = v.B;
   // one application from q0: the map's factor is the gradient's power, bit for bit
   const bool reuse = POW_REF && v.its == 1;
+  // x / B = x * (conj(B) / |B|^2) (operator/): B's factor once, not per term
+  Q Bi = {0, 0, 0, 0};
+  if (ok) {
+    const double inv = __ddiv_rn(1.0, norm2(B));
+    Bi = Q{mul(B.w, inv), mul(-B.x, inv), mul(-B.y, inv), mul(-B.z, inv)};
+  }
   double c_bulk_t = 0, c_bulk_b = 0, c_bad = 0;
   // top roots: left = forward[i-1], right = backward[i+1]
   Q left = {1, 0, 0, 0};
@@ -331,7 +337,7 @@ __device__ __forceinline__ void grad_terms(const MapParams& m, const Voxel& v, b
       for (int pass = 0; pass < 2; pass++) {
         const double k = pass == 0 ? m.sigma[0] : m.ep[i];
         const Q dT = qmul(qmul(left, qmul(qscale(pw, k), lg)), right);
-        const double dSdt = mul(dSdF, mul(RR, qdot(R, qdiv(dT, B))));
+        const double dSdt = mul(dSdF, mul(RR, qdot(R, qmul(dT, Bi))));
         if (isnan(dSdt) || isinf(dSdt)) {
           c_bad += 1;
           continue;
