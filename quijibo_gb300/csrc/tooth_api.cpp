@@ -309,6 +309,8 @@ struct ToothRun {
       o.field_res[1][c] = o.field_res[2][c] = dgrid.res[c];
       o.field_center[1][c] = o.field_center[2][c] = dgrid.center[c];
       o.field_lengths[1][c] = o.field_lengths[2][c] = dgrid.lengths[c];
+      // setScoreFields made the optimizer's resolution and box the distance field's
+      o.res[c] = dgrid.res[c];
       o.center[c] = dgrid.center[c];
       o.lengths[c] = dgrid.lengths[c];
     }

@@ -48,6 +48,9 @@ def test_run_matches_reference(ctx, tag, tmp_path):
         assert abs(state[-1] - ref[l][-2]) <= r_scale * abs(ref[l][-2])
         assert abs(L["final_score"] - ref[l][-1]) <= r_score * abs(ref[l][-1])
         assert st["fractal"][0] == (res, res, res)
+        # OPTIMIZE_3D::write's header: the resolution and box setScoreFields took
+        # from the distance field
+        assert st["res"] == st["distance"][0] and st["center"] == st["distance"][1]
     # the frame change moves the roots exactly as the reference does
     roots = np.concatenate([st["top_roots"].reshape(-1, 4), st["bottom_roots"].reshape(-1, 4)])
     assert np.array_equal(roots, GOLD[tag + "_roots"])
