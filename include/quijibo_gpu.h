@@ -151,6 +151,8 @@ typedef struct {
   int64_t n_unbracketed; /* edges whose end values do not bracket zero (the reference exits) */
   int64_t map_evals;     /* FP64 map evaluations of the edge bisection */
   int64_t map_evals_fp32;/* FP32 evaluations whose sign was trusted (precision form only) */
+  int64_t map_evals_ff;  /* double-float evaluations that decided a point FP32 could not
+                            (precision form, integer exponents) */
   int64_t slabs;         /* z-slabs processed */
   qjg_field_stats field; /* the field pass of qjg_mesh_stream */
   /* with qjg_set_timing on (else 0): device milliseconds of each phase, summed over slabs */

@@ -64,7 +64,8 @@ def bench_mesh(args):
             "triangles_per_s": st["n_tris"] / wall, "gvox_s": g.n_voxels / wall / 1e9,
             "field_only_s": field_ms / 1e3, "mesher_s": wall - field_ms / 1e3,
             "bisection_map_evals_fp64": st["map_evals"],
-            "bisection_map_evals_fp32": st["map_evals_fp32"], "unbracketed": st["n_unbracketed"],
+            "bisection_map_evals_fp32": st["map_evals_fp32"],
+            "bisection_map_evals_ff": st["map_evals_ff"], "unbracketed": st["n_unbracketed"],
             "degenerate": st["n_degenerate"], "slabs": st["slabs"],
             "refined": st["field"]["refined"],
             "lane_efficiency": st["field"]["voxel_iters"] / max(1, st["field"]["lane_iters"])}
@@ -286,7 +287,8 @@ def bench_large(args):
                        "ms_filter": st["ms_filter"],
                        "classify_emit_gb_s": (cls_bytes + tri_bytes) / (mesh_ms * 1e-3) / 1e9,
                        "bisection_map_evals_fp64": st["map_evals"],
-                       "bisection_map_evals_fp32": st["map_evals_fp32"], "slabs": st["slabs"],
+                       "bisection_map_evals_fp32": st["map_evals_fp32"],
+                       "bisection_map_evals_ff": st["map_evals_ff"], "slabs": st["slabs"],
                        "field": st["field"]}
         del v32, tris
         torch.cuda.empty_cache()

@@ -28,6 +28,7 @@
 #define QJ_MC_STORAGE static __constant__
 #include "mc_cases.h"
 #include "qj_device.cuh"
+#include "qj_ff.cuh"
 #include "qj_mesh.h"
 
 namespace qj {
@@ -633,6 +634,55 @@ __global__ void __launch_bounds__(128) edge_start_kernel(const __grid_constant__
   edge_counts(e32, 0, nbad, st);
 }
 
+// Every parked edge's point in double-float first (integer exponents): where
+// its tracked error bound decides what FP64 would (the sign, and in the
+// bisection whether |value| < 1e-8), that value stands in for FP64's; the
+// other edges, and the failed-bracket re-checks, go on to FP64 (`list64`).
+__global__ void __launch_bounds__(128) edge_ff_kernel(const __grid_constant__ MapParams m,
+                                                      const GridParams g, const IterParams it,
+                                                      const uint32_t* __restrict__ park,
+                                                      const unsigned long long* n_park,
+                                                      EdgeState* __restrict__ es, double iso,
+                                                      uint32_t* list64,
+                                                      unsigned long long* n_list64,
+                                                      DevStats* st) {
+  const unsigned long long n = *n_park;
+  unsigned long long eff = 0;
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  for (unsigned long long base = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) & ~31ull;
+       base < n; base += stride) {
+    const unsigned long long j = base + (threadIdx.x & 31);
+    bool need64 = false;
+    uint32_t k = 0;
+    if (j < n) {
+      k = park[j];
+      EdgeState& e = es[k];
+      need64 = true;
+      if (m.all_int && e.stage != 2 && e.stage != 3) {
+        double p[3];
+        edge_point(e, p);
+        float err;
+        const double f = escape_ff(m, it, p, g.slice, &err);
+        const double v = f - iso;
+        // FP64 rounding of f - iso and of the reference's own |q| on top
+        const double eb = 1.01 * (double)err + 1e-15 * (fabs(f) + fabs(iso));
+        bool decided = isfinite(eb) && fabs(v) > eb;  // the sign
+        if (e.stage == 4)  // and the bisection's stop test
+          decided = isfinite(eb) && (fabs(v) > eb + 1e-8 || fabs(v) + eb < 1e-8);
+        if (decided) {
+          e.pending = v;
+          e.flags |= EDGE_PENDING;
+          need64 = false;
+          eff++;
+        }
+      }
+    }
+    warp_push(need64, k, n_list64, list64);
+  }
+  for (int o = 16; o; o >>= 1) eff += __shfl_xor_sync(0xffffffffu, eff, o);
+  if ((threadIdx.x & 31) == 0 && eff) atomicAdd(&st->ff_evals, eff);
+}
+
 // The FP64 value of every parked edge's point.
 template <bool POW_REF>
 __global__ void __launch_bounds__(128) edge_fp64_kernel(const __grid_constant__ MapParams m,
@@ -757,9 +807,9 @@ static cudaError_t parked_finish(const MapParams& m, const GridParams& g, const 
                                  cudaStream_t s) {
   EdgeState* es = static_cast<EdgeState*>(sc.state);
   cudaError_t err;
-  // each round gives every parked edge one FP64 value; an edge asks for at
-  // most 2 at its ends (one each, or a re-check of a failed bracket) and 6
-  // in the bisection
+  // each round gives every parked edge one value (double-float where its
+  // bound decides, else FP64); an edge asks for at most 2 at its ends (one
+  // each, or a re-check of a failed bracket) and 6 in the bisection
   for (int round = 0, cur = 0;; round++, cur ^= 1) {
     unsigned long long parked = 0;
     if ((err = cudaMemcpyAsync(&parked, sc.count + cur, sizeof parked, cudaMemcpyDeviceToHost, s)))
@@ -769,7 +819,11 @@ static cudaError_t parked_finish(const MapParams& m, const GridParams& g, const 
     if (round == 8) return cudaErrorInvalidValue;  // cannot happen: see the count above
     const int pb = (int)std::min<long long>(((long long)parked + 127) / 128,
                                             (long long)sm_count() * 32);
-    edge_fp64_kernel<POW_REF><<<pb, 128, 0, s>>>(m, g, it, sc.list[cur], sc.count + cur, es, iso,
+    // double-float first; what it cannot decide, in FP64
+    if ((err = cudaMemsetAsync(sc.count + 2, 0, sizeof(unsigned long long), s))) return err;
+    edge_ff_kernel<<<pb, 128, 0, s>>>(m, g, it, sc.list[cur], sc.count + cur, es, iso,
+                                      sc.list[2], sc.count + 2, st);
+    edge_fp64_kernel<POW_REF><<<pb, 128, 0, s>>>(m, g, it, sc.list[2], sc.count + 2, es, iso,
                                                  st);
     if ((err = cudaMemsetAsync(sc.count + (cur ^ 1), 0, sizeof(unsigned long long), s)))
       return err;

@@ -78,8 +78,8 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
   QJ_CUDA(ctx, cudaMemsetAsync(ctx->m_masks, 0, XY, s));
   QJ_CUDA(ctx, cudaMemsetAsync(ctx->m_vbase, 0, XY * sizeof(int32_t), s));
   QJ_CUDA(ctx, cudaMemsetAsync(ctx->d_mstats, 0, sizeof(qj::DevStats), s));
-  if ((rc = ensure(ctx, &ctx->m_ecount, &ctx->m_ecount_cap, (size_t)2))) return rc;
-  QJ_CUDA(ctx, cudaMemsetAsync(ctx->m_ecount, 0, 2 * sizeof(unsigned long long), s));
+  if ((rc = ensure(ctx, &ctx->m_ecount, &ctx->m_ecount_cap, (size_t)3))) return rc;
+  QJ_CUDA(ctx, cudaMemsetAsync(ctx->m_ecount, 0, 3 * sizeof(unsigned long long), s));
 
   qj::MeshWindow w;
   w.X = X;
@@ -211,12 +211,13 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
   const bool any_parked = iter && iter->precision != QJG_FP64 && bisect && nv > 0;
   if (any_parked) {
     QJ_CUDA(ctx, mark(0));
-    if ((rc = grow_keep(ctx, &ctx->m_epark, &ctx->m_epark_cap, (size_t)(2 * nv), (size_t)nv, s)))
+    if ((rc = grow_keep(ctx, &ctx->m_epark, &ctx->m_epark_cap, (size_t)(3 * nv), (size_t)nv, s)))
       return rc;
     qj::EdgeScratch esc{};
     esc.state = ctx->m_estate;
     esc.list[0] = ctx->m_epark;
     esc.list[1] = ctx->m_epark + nv;
+    esc.list[2] = ctx->m_epark + 2 * nv;
     esc.count = ctx->m_ecount;
     QJ_CUDA(ctx, qj::mesh_parked_finish(*m, g, it, pow_ref, ctx->m_verts, iso, ctx->d_mstats, esc,
                                         s));
@@ -231,6 +232,7 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
   st.map_evals = (int64_t)ds.aux[1];
   st.n_unbracketed = (int64_t)ds.aux[2];
   st.map_evals_fp32 = (int64_t)ds.aux[3];
+  st.map_evals_ff = (int64_t)ds.ff_evals;
   if (nt > tcap || ((v64 || v32) && nv > vcap)) {
     if (out) *out = st;
     return fail(ctx, QJG_ERR_CAPACITY, "mesh needs %lld vertices / %lld triangles (capacity %lld / %lld)",

@@ -139,6 +139,14 @@ __device__ __forceinline__ float propagate_err(float err, float gg, float m2_in)
   return fmaf(err, amp, ERR_STEP);
 }
 
+// the same with another per-application step (the double-float model)
+__device__ __forceinline__ float propagate_err_step(float err, float gg, float m2_in,
+                                                    float step) {
+  float amp;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(amp) : "f"(gg * m2_in));
+  return fmaf(err, amp, step);
+}
+
 // |q|^2 = m2 is within its FP32 error of the escape radius squared
 __device__ __forceinline__ bool near_radius(float m2, float esc2, float err) {
   return fabsf(m2 - esc2) < 2.f * err * esc2;

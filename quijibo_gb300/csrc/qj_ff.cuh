@@ -172,6 +172,12 @@ __device__ __forceinline__ q32::Q cell_center_f32(const GridParams& g, int x, in
 
 }  // namespace qff
 
+// Relative rounding of double-float arithmetic (sloppy add: ~2^-44 under
+// cancellation) and its per-application step, scaled as the FP32 model's
+// (q32::ERR_STEP = 64 ulp).
+constexpr float EPS_FF = 5.684342e-14f;  // 2^-44
+constexpr float ERR_STEP_FF = 64.f * EPS_FF;
+
 // One root term (q - r_i)^(e_i) in double-float (integer exponents only);
 // with DE, adds (+-e_i) d/|d|^2 to g from the high parts, as the FP32 form.
 template <bool DE>
@@ -227,6 +233,49 @@ __device__ __forceinline__ qff::Q apply_ff(const MapParams& m, const qff::Q& q, 
   }
   if (DE) *g2 = q32::norm2(g);
   return out;
+}
+
+// The escape loop in double-float at an arbitrary point (integer exponents):
+// returns log|q_N| and, through *err, a first-order bound on its absolute
+// error, propagated as the FP32 model's (relative error of q_n scaled by
+// |grad log|R|| |q_n| and ERR_STEP_FF added per application).  *err is
+// infinite where no bound holds: an iterate within its error of the escape
+// radius (FP64 may stop at another iterate), |q| near the bottom of the FP32
+// exponent range the pairs live in, or a non-finite value.
+__device__ __forceinline__ double escape_ff(const MapParams& m, const IterParams& it,
+                                            const double p[3], double slice, float* err) {
+  using namespace qff;
+  Q q = {from_double(p[0]), from_double(p[1]), from_double(p[2]), from_double(slice)};
+  const double esc2 = it.escape * it.escape;
+  auto m2_of = [](const Q& v) {
+    const F n = norm2(v);
+    return (double)n.hi + (double)n.lo;
+  };
+  double m2 = m2_of(q);
+  float e = EPS_FF;
+  int n = 0;
+  bool bad = false, near = false;
+  // the escape test compares |q|^2 with esc^2 in FP64 here and |q| with esc
+  // in the reference: a relative margin of 1e-14 covers the difference
+  auto near_esc = [&](double v) {
+    return fabs(v - esc2) < 2.0 * fmax((double)e, 1e-14) * esc2;
+  };
+  while (m2 < esc2 && n < it.max_it) {
+    float gg = 0.f;
+    q = apply_ff<true>(m, q, &gg);
+    near = near || near_esc(m2);
+    e = q32::propagate_err_step(e, gg, (float)m2, ERR_STEP_FF);
+    m2 = m2_of(q);
+    n++;
+    if (m2 < 1e-28) {
+      bad = true;
+      break;
+    }
+  }
+  bad = bad || near || (m2 >= esc2 && n < it.max_it && near_esc(m2));
+  const double f = 0.5 * log(m2);
+  *err = (bad || !isfinite(f) || !(e < 1e-3f)) ? __int_as_float(0x7f800000) : e;
+  return f;
 }
 
 // ---- two voxels per lane -------------------------------------------------

@@ -33,8 +33,8 @@ cudaError_t mesh_vertex_ids(MeshWindow& w, int j0, int j1, int lay_lo, int lay_h
 // collects every slab's parked edges), two counters (zeroed once per mesh).
 struct EdgeScratch {
   void* state;
-  uint32_t* list[2];
-  unsigned long long* count;
+  uint32_t* list[3];  // two parking lists (rounds alternate) and the FP64 sub-list
+  unsigned long long* count;  // their three lengths
 };
 size_t mesh_edge_state_bytes();
 // Vertex placement.  With hybrid bisection and a scratch, the edges that

@@ -88,6 +88,7 @@ struct DevStats {
   unsigned long long aux[4];
   unsigned long long rerun;         // length of the double-float re-run list
   unsigned long long rerun_iters;   // map applications of the re-runs
+  unsigned long long ff_evals;      // mesher: double-float evaluations that decided a point
 };
 
 }  // namespace qj

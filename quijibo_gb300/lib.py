@@ -65,7 +65,7 @@ QJG_EDGE_LINEAR, QJG_EDGE_BISECT = 0, 1
 class QjgMeshStats(C.Structure):
     _fields_ = [("n_verts", C.c_int64), ("n_tris", C.c_int64), ("n_degenerate", C.c_int64),
                 ("n_unbracketed", C.c_int64), ("map_evals", C.c_int64),
-                ("map_evals_fp32", C.c_int64), ("slabs", C.c_int64),
+                ("map_evals_fp32", C.c_int64), ("map_evals_ff", C.c_int64), ("slabs", C.c_int64),
                 ("field", QjgFieldStats), ("ms_field", C.c_double), ("ms_classify", C.c_double),
                 ("ms_vertices", C.c_double), ("ms_triangles", C.c_double),
                 ("ms_filter", C.c_double)]

@@ -124,9 +124,11 @@ def test_fp32_refine_stream_topology_matches_fp64(ctx, res):
     (b64, _, bt), sb = res[1]
     np.testing.assert_array_equal(at, bt)
     assert sb["field"]["refined"] > 0
-    # the FP32-first bisection takes every decision the FP64 one takes, so the
-    # vertices are the same doubles
+    # the FP32-first bisection (with its double-float tier for points FP32
+    # cannot decide) takes every decision the FP64 one takes, so the vertices
+    # are the same doubles
     assert sb["map_evals_fp32"] > sb["map_evals"] and sa["map_evals_fp32"] == 0
+    assert sb["map_evals_ff"] > sb["map_evals"] and sa["map_evals_ff"] == 0
     assert sa["n_unbracketed"] == 0 and sb["n_unbracketed"] == 0
     np.testing.assert_array_equal(b64, a64)
     ctx.free(h)
