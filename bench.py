@@ -290,6 +290,7 @@ def run_ours(args, world, rank, local):
         "fp64_plain": fp64,
         "field_stats": dict(st, bulk_ms=bulk, refine_ms=statistics.mean(refine_ms),
                             wall_s=wall, refined_frac=st["refined"] / n,
+                            gvoxel_iterations_s=world * st["voxel_iters"] / (ms * 1e-3) / 1e9,
                             lane_efficiency=st["voxel_iters"] / max(1, st["lane_iters"])),
         "roofline": {"bound": "fma", "kernel": "field32x2_kernel", "achieved": achieved,
                      "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,

@@ -309,6 +309,7 @@ def bench_large(args):
     flops = field_flops(rs, tot["voxel_iters"])
     peak = lib.fma_probe(0)
     out["field"] = {"gvox_s": n / ((bulk + rest) * 1e-3) / 1e9, "bulk_ms": bulk, "rest_ms": rest,
+                    "gvoxel_iterations_s": tot["voxel_iters"] / ((bulk + rest) * 1e-3) / 1e9,
                     "roofline": {"achieved_tflops": flops / (bulk * 1e-3) / 1e12,
                                  "peak_tflops": peak, "frac": flops / (bulk * 1e-3) / 1e12 / peak},
                     "stats": tot, "lane_efficiency": tot["voxel_iters"] / max(1, tot["lane_iters"])}

@@ -21,6 +21,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "qj_device.cuh"
 #include "qj_energy.h"
@@ -702,13 +703,18 @@ cudaError_t launch_tanh_grad(const MapParams& m, const GridParams& g, const Weig
 //   d = |q_N| log|q_N| exp(-L_N),  E = sum_k (D tanh(d_k / D) - t_k)^2.
 // Parameters: root positions (4 each), effective exponents, log s, laid out
 // [top roots 4nt | bottom roots 4nb | top exps nt | bottom exps nb | log s].
-// The backward pass stores no trajectory: it keeps q at every SQ_CK-th
-// iteration and recomputes each segment forward before reversing it.
+// The forward pass keeps q at every SQ_CK-th iteration of the samples whose
+// gradient is wanted; the backward pass stores no trajectory: it recomputes
+// each segment forward from its checkpoint before reversing it.
 // ===========================================================================
 namespace {
 
-constexpr int SQ_T = 64;   // threads per block
-constexpr int SQ_CK = 8;   // checkpoint spacing (iterations)
+constexpr int SQ_T = 64;    // threads per block of the backward pass
+constexpr int SQ_BWD_PER_SM = 8;  // backward blocks per SM
+constexpr int SQF_T = 128;  // threads per block of the forward pass
+constexpr int SQC_T = 256;  // threads per chunk block
+constexpr int SQ_CH = 2048; // samples per chunk (sums and sort)
+constexpr int SQ_CK = 8;    // checkpoint spacing (iterations)
 constexpr int SQ_MAXIT = 256;
 
 template <class T>
@@ -746,6 +752,22 @@ struct PowParts {
 
 template <class T>
 __device__ __forceinline__ V4<T> powv(const V4<T>& d, T e, PowParts<T>* pp) {
+  if constexpr (std::is_same<T, float>::value) {
+    // FP32: the same polar form through base-2 logarithm and exponential,
+    // the angle as atan2(|v|, w) and its multiple in half-turns (sincospif),
+    // and 1/|v| as one reciprocal square root
+    const float v2 = d.x * d.x + d.y * d.y + d.z * d.z;
+    const float r2 = v2 + d.w * d.w;
+    const float rv = v2 > 0.f ? rsqrtf(v2) : 0.f;
+    const float vm = v2 * rv;
+    const float theta = atan2f(vm, d.w);
+    const float A = exp2f(0.5f * e * log2f(r2));
+    float s, c;
+    sincospif(e * theta * 0.318309886183790672f, &s, &c);
+    const float k = A * s * rv;
+    if (pp) *pp = PowParts<T>{sqrtf(r2), vm, theta, A, c, s};
+    return V4<T>{A * c, k * d.x, k * d.y, k * d.z};
+  }
   const T v2 = d.x * d.x + d.y * d.y + d.z * d.z;
   const T rho = sqrt(v2 + d.w * d.w), vm = sqrt(v2);
   const T theta = acos(d.w / rho);
@@ -789,30 +811,31 @@ __device__ __forceinline__ V4<T> powv_vjp(const V4<T>& d, T e, const PowParts<T>
   return db;
 }
 
-template <class T>
-struct SqShared {
-  int nt, nb;
-  T s;
-};
-
 // One map application q -> Q with log|g|; fills prefix products F (per
 // side) and factors P when `keep` is set.
 template <class T>
 __device__ __forceinline__ V4<T> sq_apply(const T* __restrict__ rp, const T* __restrict__ ep,
                                           int nt, int nb, T s, const V4<T>& q, T* lg,
                                           V4<T>* F, V4<T>* Pf, V4<T>* Tout, V4<T>* Bout) {
+  // acc[0]: top product, acc[1]: bottom product (two loops, so that the
+  // running products stay in registers)
   V4<T> acc[2] = {{T(1), T(0), T(0), T(0)}, {T(1), T(0), T(0), T(0)}};
   V4<T> g = {T(0), T(0), T(0), T(0)};
-  for (int i = 0; i < nt + nb; i++) {
-    const int side = i >= nt;
-    const V4<T> d{q.w - rp[4 * i], q.x - rp[4 * i + 1], q.y - rp[4 * i + 2], q.z - rp[4 * i + 3]};
-    const T e = ep[i];
-    const T k = (side ? -e : e) / v4dot(d, d);
-    g = v4add(g, v4scale(d, k));
-    const V4<T> P = powv<T>(d, e, nullptr);
-    acc[side] = (i == 0 || i == nt) ? P : v4mul(acc[side], P);
-    if (F) F[i] = acc[side];
-    if (Pf) Pf[i] = P;
+#pragma unroll
+  for (int side = 0; side < 2; side++) {
+    const int lo = side ? nt : 0, hi = side ? nt + nb : nt;
+    V4<T> a = acc[side];
+    for (int i = lo; i < hi; i++) {
+      const V4<T> d{q.w - rp[4 * i], q.x - rp[4 * i + 1], q.y - rp[4 * i + 2], q.z - rp[4 * i + 3]};
+      const T e = ep[i];
+      const T k = (side ? -e : e) / v4dot(d, d);
+      g = v4add(g, v4scale(d, k));
+      const V4<T> P = powv<T>(d, e, nullptr);
+      a = i == lo ? P : v4mul(a, P);
+      if (F) F[i] = a;
+      if (Pf) Pf[i] = P;
+    }
+    acc[side] = a;
   }
   V4<T> Q;
   if (nb > 0) {
@@ -825,36 +848,6 @@ __device__ __forceinline__ V4<T> sq_apply(const T* __restrict__ rp, const T* __r
   if (Tout) *Tout = acc[0];
   if (Bout) *Bout = acc[1];
   return Q;
-}
-
-// Forward to the end: returns log|q_N|, with the iteration count, L_N and
-// log|d| through the pointers; fills checkpoints.
-template <class T>
-__device__ __forceinline__ T sq_forward(const T* rp, const T* ep, int nt, int nb, T s,
-                                        V4<T> q, int max_it, T esc, int* n_out, T* L_out,
-                                        V4<T>* ck, T* Lck, T* ld_out) {
-  T L = T(0);
-  int n = 0;
-  while (sqrt(v4dot(q, q)) < esc && n < max_it) {
-    if (ck && n % SQ_CK == 0) {
-      ck[n / SQ_CK] = q;
-      Lck[n / SQ_CK] = L;
-    }
-    T lg;
-    q = sq_apply<T>(rp, ep, nt, nb, s, q, &lg, nullptr, nullptr, nullptr, nullptr);
-    L += lg + T(0.5) * log(v4dot(q, q));
-    n++;
-    if (sqrt(v4dot(q, q)) < T(1.1754943508e-37)) break;  // 10 * FLT_MIN exit of the field loop
-  }
-  const T m = sqrt(v4dot(q, q));
-  *n_out = n;
-  *L_out = L;
-  if (ck) ck[n / SQ_CK + 1] = q;  // final iterate (slot after the last checkpoint)
-  // log|d| first: contracting orbits drive L far below zero, and d itself
-  // out of range, long before d matters
-  const T lm = log(m);
-  *ld_out = log(fabs(lm)) + lm - L;
-  return lm;
 }
 
 // The fitted value D tanh(d / D) (d itself when D <= 0) and its derivative;
@@ -885,12 +878,223 @@ __device__ __forceinline__ void sq_saturate(T lm, T ld, T dsat, T* val, T* d, T*
   }
 }
 
+// Per-sample results of the forward pass.  keys[k]: the orbit length N of a
+// sample whose gradient the backward pass computes (N >= 1), -1 for a sample
+// that adds nothing to the gradient (saturated, or N = 0), -2 for a sample
+// left out because its seed is not finite (counted).
+template <class T>
+struct SqFwdOut {
+  double* contrib;  // (D tanh(d/D) - t)^2 per sample
+  int* keys;
+  int* iters;       // orbit lengths (optional)
+  V4<T>* seed_q;    // dE/dq_N per sample (gradient pass)
+  T* seed_L;        // dE/dL (constant along the orbit)
+  V4<T>* ck;        // q_n at n = 0, SQ_CK, 2 SQ_CK, ...: ck[(n / SQ_CK) * n_samples + k]
+};
+
+// Forward pass with lane refill: every lane iterates its own sample and takes
+// the next unclaimed one (a warp-aggregated atomic on *claim) as soon as its
+// orbit ends, so a warp's lanes stay busy however the orbit lengths differ.
+// The per-sample results go to SqFwdOut; the sums are formed afterwards in
+// sample order, so they do not depend on which lane took which sample.
 template <class T, bool GRAD>
-__global__ void __launch_bounds__(SQ_T) sq_energy_kernel(
+__global__ void __launch_bounds__(SQF_T) sq_fwd_kernel(
     const double* __restrict__ params, int nt, int nb, const double* __restrict__ xyz,
     const double* __restrict__ target, long long n_samples, double slice, int max_it,
-    double escape, double d_sat, double* __restrict__ partials, int slots,
-    int* __restrict__ iters_out) {
+    double escape, double d_sat, unsigned long long* __restrict__ claim, SqFwdOut<T> o) {
+  extern __shared__ unsigned char sh_raw[];
+  const int nr = nt + nb;
+  T* rp = reinterpret_cast<T*>(sh_raw);  // 4 nr
+  T* ep = rp + 4 * nr;                   // nr
+  for (int k = threadIdx.x; k < 4 * nr; k += SQF_T) rp[k] = (T)params[k];
+  for (int k = threadIdx.x; k < nr; k += SQF_T) ep[k] = (T)params[4 * nr + k];
+  __syncthreads();
+  const T s = (T)exp(params[5 * nr]);
+  const T esc = (T)escape, dsat = (T)d_sat;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+
+  // the sample's value, residual and (gradient pass) seed
+  auto finish = [&](long long k, const V4<T>& q, T L, int n) {
+    const T m = sqrt(v4dot(q, q));
+    // log|d| first: contracting orbits drive L far below zero, and d itself
+    // out of range, long before d matters
+    const T lm = log(m);
+    const T ld = log(fabs(lm)) + lm - L;
+    if (o.iters) o.iters[k] = n;
+    T val, dval, dval_dd;
+    sq_saturate<T>(lm, ld, dsat, &val, &dval, &dval_dd);
+    const T r = val - (T)target[k];
+    o.contrib[k] = (double)(r * r);
+    if (!GRAD) return;
+    int key = -1;
+    if (dval_dd != T(0)) {
+      // seed: dE/dd = 2 r dval/dd; d = m log m exp(-L):
+      // dd/dm = (log m + 1) exp(-L) = d (log m + 1) / (m log m)
+      const T db = T(2) * r * dval_dd;
+      const T kq = db * (lm + T(1)) * exp(ld - log(m) - log(fabs(lm)));
+      if (!isfinite(kq) || !isfinite(db * dval)) {
+        key = -2;
+      } else if (n > 0) {
+        o.seed_q[k] = v4scale(q, kq / m);  // d/dq_N of d: (dd/dm) q_N / m
+        o.seed_L[k] = -db * dval;
+        key = n;
+      }
+    }
+    o.keys[k] = key;
+  };
+
+  long long k = 0;
+  bool live = false, done = false;
+  V4<T> q{T(0), T(0), T(0), T(0)};
+  T L = T(0);
+  int n = 0;
+  for (;;) {
+    // lanes without a sample claim one; a claimed sample whose orbit does
+    // not start (|q_0| >= escape or max_it = 0) ends at once and claims again
+    unsigned want = __ballot_sync(0xffffffffu, !live && !done);
+    while (want) {
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(claim, (unsigned long long)__popc(want));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (!live && !done) {
+        k = (long long)(base + __popc(want & lt));
+        if (k >= n_samples) {
+          done = true;
+        } else {
+          q = V4<T>{(T)xyz[3 * k], (T)xyz[3 * k + 1], (T)xyz[3 * k + 2], (T)slice};
+          L = T(0);
+          n = 0;
+          if (sqrt(v4dot(q, q)) < esc && n < max_it)
+            live = true;
+          else
+            finish(k, q, L, n);
+        }
+      }
+      want = __ballot_sync(0xffffffffu, !live && !done);
+    }
+    if (!__any_sync(0xffffffffu, live)) break;
+    if (live) {
+      if (GRAD && n % SQ_CK == 0) o.ck[(long long)(n / SQ_CK) * n_samples + k] = q;
+      T lg;
+      q = sq_apply<T>(rp, ep, nt, nb, s, q, &lg, nullptr, nullptr, nullptr, nullptr);
+      L += lg + T(0.5) * log(v4dot(q, q));
+      n++;
+      // 10 * FLT_MIN exit of the field loop
+      const T m = sqrt(v4dot(q, q));
+      if (!(m < esc && n < max_it) || m < T(1.1754943508e-37)) {
+        finish(k, q, L, n);
+        live = false;
+      }
+    }
+  }
+}
+
+// Per chunk of SQ_CH samples: the energy and the left-out count summed in a
+// fixed tree (one partial row per chunk, after the backward pass's rows), and
+// (gradient pass) the histogram of orbit lengths for the sort, bucket
+// max_it - N so that long orbits come first: hist[bucket * nchunks + chunk].
+__global__ void __launch_bounds__(SQC_T) sq_chunk_kernel(const double* __restrict__ contrib,
+                                                         const int* __restrict__ keys,
+                                                         long long n, int max_it, int nchunks,
+                                                         int* __restrict__ hist,
+                                                         double* __restrict__ partials, int slots,
+                                                         int row0) {
+  __shared__ double red_e[SQC_T], red_b[SQC_T];
+  __shared__ int h[SQ_MAXIT + 1];
+  const int c = blockIdx.x, t = threadIdx.x;
+  for (int b = t; b <= max_it; b += SQC_T) h[b] = 0;
+  __syncthreads();
+  double e = 0.0, bad = 0.0;
+  for (int i = t; i < SQ_CH; i += SQC_T) {
+    const long long k = (long long)c * SQ_CH + i;
+    if (k >= n) break;
+    e += contrib[k];
+    if (keys) {
+      const int key = keys[k];
+      if (key == -2) bad += 1.0;
+      else if (key > 0) atomicAdd(&h[max_it - key], 1);
+    }
+  }
+  red_e[t] = e;
+  red_b[t] = bad;
+  __syncthreads();
+  for (int w = SQC_T / 2; w; w >>= 1) {
+    if (t < w) {
+      red_e[t] += red_e[t + w];
+      red_b[t] += red_b[t + w];
+    }
+    __syncthreads();
+  }
+  double* row = partials + (long long)(row0 + c) * slots;
+  for (int j = t; j < slots; j += SQC_T) row[j] = j == 0 ? red_e[0] : j == slots - 1 ? red_b[0] : 0.0;
+  if (keys)
+    for (int b = t; b <= max_it; b += SQC_T) hist[(long long)b * nchunks + c] = h[b];
+}
+
+// Exclusive scan of the histogram in place (one block); *total = entries.
+__global__ void __launch_bounds__(1024) sq_scan_kernel(int* __restrict__ hist, long long m,
+                                                       int* __restrict__ total) {
+  __shared__ int sums[1024];
+  const int t = threadIdx.x;
+  const long long per = (m + 1023) / 1024, lo = min(m, t * per), hi = min(m, lo + per);
+  int own = 0;
+  for (long long i = lo; i < hi; i++) own += hist[i];
+  sums[t] = own;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    const int v = t >= off ? sums[t - off] : 0;
+    __syncthreads();
+    sums[t] += v;
+    __syncthreads();
+  }
+  int run = sums[t] - own;
+  for (long long i = lo; i < hi; i++) {
+    const int v = hist[i];
+    hist[i] = run;
+    run += v;
+  }
+  if (t == 1023) *total = sums[1023];
+}
+
+// Stable scatter of the gradient samples into perm, longest orbits first:
+// one warp per chunk walks its samples in order; lanes with the same bucket
+// take consecutive slots in lane order (__match_any_sync).
+__global__ void __launch_bounds__(32) sq_scatter_kernel(const int* __restrict__ keys, long long n,
+                                                        int max_it, int nchunks,
+                                                        const int* __restrict__ hist,
+                                                        unsigned* __restrict__ perm) {
+  __shared__ int off[SQ_MAXIT + 1];
+  const int c = blockIdx.x, lane = threadIdx.x;
+  for (int b = lane; b <= max_it; b += 32) off[b] = hist[(long long)b * nchunks + c];
+  __syncwarp();
+  const unsigned lt = (1u << lane) - 1u;
+  for (int i0 = 0; i0 < SQ_CH; i0 += 32) {
+    const long long k = (long long)c * SQ_CH + i0 + lane;
+    const int key = k < n ? keys[k] : -1;
+    const int b = key > 0 ? max_it - key : -1;
+    const unsigned grp = __match_any_sync(0xffffffffu, b);
+    const int rank = __popc(grp & lt);
+    if (b >= 0) perm[off[b] + rank] = (unsigned)k;
+    __syncwarp();
+    if (b >= 0 && rank == 0) off[b] += __popc(grp);
+    __syncwarp();
+  }
+}
+
+// Backward pass over the sorted gradient samples: warp w takes groups of 32
+// consecutive entries w, w + W, ... (equal orbit lengths within a group, so
+// no lane waits on another's longer orbit).  It stores no trajectory: from
+// each checkpoint it recomputes the segment forward before reversing it.
+// Each thread's sums run over a fixed set of samples, so the gradient is the
+// same on every run.
+template <class T>
+__global__ void __launch_bounds__(SQ_T) sq_bwd_kernel(
+    const double* __restrict__ params, int nt, int nb, long long n_samples,
+    const unsigned* __restrict__ perm, const int* __restrict__ total,
+    const int* __restrict__ keys, const V4<T>* __restrict__ seed_q,
+    const T* __restrict__ seed_L, const V4<T>* __restrict__ ck, double* __restrict__ partials,
+    int slots) {
   extern __shared__ unsigned char sh_raw[];
   const int nr = nt + nb;
   T* rp = reinterpret_cast<T*>(sh_raw);           // 4 nr
@@ -901,47 +1105,27 @@ __global__ void __launch_bounds__(SQ_T) sq_energy_kernel(
   for (int k = threadIdx.x; k < (SQ_T / 32) * slots; k += SQ_T) acc_sh[k] = 0.0;
   __syncthreads();
   const T s = (T)exp(params[5 * nr]);
-  const T esc = (T)escape;
   double* acc = acc_sh + (threadIdx.x >> 5) * slots;
   // per-thread scratch (local memory)
-  V4<T> ck[SQ_MAXIT / SQ_CK + 2];
-  T Lck[SQ_MAXIT / SQ_CK + 2];
   V4<T> seg[SQ_CK];
-  V4<T> Pf[QJ_MAX_ROOTS], F[QJ_MAX_ROOTS];
+  V4<T> F[QJ_MAX_ROOTS];
   T gacc[5 * QJ_MAX_ROOTS + 1];
-  if (GRAD)
-    for (int k = 0; k <= 5 * nr; k++) gacc[k] = T(0);
-  double e_acc = 0.0, bad_acc = 0.0;
-  const T dsat = (T)d_sat;
-  const long long stride = (long long)gridDim.x * SQ_T;
-  for (long long k = (long long)blockIdx.x * SQ_T + threadIdx.x; k < n_samples; k += stride) {
-    const V4<T> q0{(T)xyz[3 * k], (T)xyz[3 * k + 1], (T)xyz[3 * k + 2], (T)slice};
-    int N;
-    T LN, ld;
-    const T lm = sq_forward<T>(rp, ep, nt, nb, s, q0, max_it, esc, &N, &LN, GRAD ? ck : nullptr,
-                               GRAD ? Lck : nullptr, &ld);
-    if (iters_out) iters_out[k] = N;
-    T val, dval, dval_dd;
-    sq_saturate<T>(lm, ld, dsat, &val, &dval, &dval_dd);
-    const T r = val - (T)target[k];
-    e_acc += (double)(r * r);
-    if (!GRAD || dval_dd == T(0)) continue;
-    // seed: dE/dd = 2 r dval/dd; d = m log m exp(-L):
-    // dd/dm = (log m + 1) exp(-L) = d (log m + 1) / (m log m)
-    const V4<T> qN = ck[N / SQ_CK + 1];
-    const T m = sqrt(v4dot(qN, qN));
-    const T db = T(2) * r * dval_dd;
-    const T kq = db * (lm + T(1)) * exp(ld - log(m) - log(fabs(lm)));
-    if (!isfinite(kq) || !isfinite(db * dval)) {
-      bad_acc += 1.0;
-      continue;
-    }
-    V4<T> qb = v4scale(qN, kq / m);  // d/dq_N of d: (dd/dm) q_N / m
-    const T Lb = -db * dval;  // constant along the chain (L_{n+1} = L_n + ...)
+  for (int k = 0; k <= 5 * nr; k++) gacc[k] = T(0);
+  const int count = *total;
+  const int lane = threadIdx.x & 31;
+  const long long W = ((long long)gridDim.x * SQ_T) >> 5;
+  for (long long grp = ((long long)blockIdx.x * SQ_T + threadIdx.x) >> 5; grp * 32 < count;
+       grp += W) {
+    const long long j = grp * 32 + lane;
+    if (j >= count) continue;
+    const long long k = perm[j];
+    const int N = keys[k];
+    V4<T> qb = seed_q[k];
+    const T Lb = seed_L[k];
     // segments in reverse
-    for (int sgi = (N - 1) / SQ_CK; sgi >= 0 && N > 0; sgi--) {
+    for (int sgi = (N - 1) / SQ_CK; sgi >= 0; sgi--) {
       const int n0 = sgi * SQ_CK, n1 = min(N, n0 + SQ_CK);
-      V4<T> q = ck[sgi];
+      V4<T> q = ck[(long long)sgi * n_samples + k];
       for (int n = n0; n < n1; n++) {
         seg[n - n0] = q;
         T lg;
@@ -951,17 +1135,17 @@ __global__ void __launch_bounds__(SQ_T) sq_energy_kernel(
         const V4<T> qn = seg[n - n0];
         T lg;
         V4<T> Tq, Bq;
-        const V4<T> Q = sq_apply<T>(rp, ep, nt, nb, s, qn, &lg, F, Pf, &Tq, &Bq);
+        const V4<T> Q = sq_apply<T>(rp, ep, nt, nb, s, qn, &lg, F, nullptr, &Tq, &Bq);
         // L_{n+1} = L_n + log|g| + log|Q|
         V4<T> Qb = v4add(qb, v4scale(Q, Lb / v4dot(Q, Q)));
         // d/d log s: <Qbar, Q>
         gacc[5 * nr] += v4dot(Qb, Q);
         V4<T> Tb, Bb = {T(0), T(0), T(0), T(0)};
         if (nb > 0) {
-          const V4<T> W = v4scale(v4conj(Bq), T(1) / v4dot(Bq, Bq));
-          Tb = v4scale(v4mul(Qb, v4conj(W)), s);
+          const V4<T> W4 = v4scale(v4conj(Bq), T(1) / v4dot(Bq, Bq));
+          Tb = v4scale(v4mul(Qb, v4conj(W4)), s);
           const V4<T> Wb = v4scale(v4mul(v4conj(Tq), Qb), s);
-          Bb = v4scale(v4mul(v4mul(v4conj(W), Wb), v4conj(W)), T(-1));
+          Bb = v4scale(v4mul(v4mul(v4conj(W4), Wb), v4conj(W4)), T(-1));
         } else {
           Tb = v4scale(Qb, s);
         }
@@ -980,12 +1164,12 @@ __global__ void __launch_bounds__(SQ_T) sq_energy_kernel(
           if (hi == lo) continue;
           V4<T> U = side ? Bb : Tb;
           for (int i = hi - 1; i >= lo; i--) {
-            const V4<T> Pb = (i == lo) ? U : v4mul(v4conj(F[i - 1]), U);
-            U = v4mul(U, v4conj(Pf[i]));
             const V4<T> d{qn.w - rp[4 * i], qn.x - rp[4 * i + 1], qn.y - rp[4 * i + 2],
                           qn.z - rp[4 * i + 3]};
             PowParts<T> pp;
-            powv<T>(d, ep[i], &pp);
+            const V4<T> P = powv<T>(d, ep[i], &pp);
+            const V4<T> Pb = (i == lo) ? U : v4mul(v4conj(F[i - 1]), U);
+            U = v4mul(U, v4conj(P));
             T eb = T(0);
             V4<T> dbar = powv_vjp<T>(d, ep[i], pp, Pb, &eb);
             // g term: sgn e d/|d|^2
@@ -1007,9 +1191,10 @@ __global__ void __launch_bounds__(SQ_T) sq_energy_kernel(
       }
     }
   }
-  // deterministic reduction: warp trees, warps in order
+  // deterministic reduction: warp trees, warps in order (the energy and the
+  // left-out count are in the chunk rows)
   for (int k = 0; k < slots; k++) {
-    double v = (k == 0) ? e_acc : (k == slots - 1) ? bad_acc : (GRAD ? (double)gacc[k - 1] : 0.0);
+    double v = (k == 0 || k == slots - 1) ? 0.0 : (double)gacc[k - 1];
 #pragma unroll
     for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if ((threadIdx.x & 31) == 0) acc[k] += v;
@@ -1022,37 +1207,153 @@ __global__ void __launch_bounds__(SQ_T) sq_energy_kernel(
   }
 }
 
+// Compensated sum of partials[b][k] over rows b, one warp per slot k: each
+// lane a Neumaier sum over rows lane, lane + 32, ..., then the 32 (sum,
+// compensation) pairs in a fixed tree, so the result is the same on every run.
+__global__ void __launch_bounds__(256) sq_reduce_kernel(const double* __restrict__ partials,
+                                                        int rows, int slots,
+                                                        double* __restrict__ out) {
+  const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (k >= slots) return;
+  double sum = 0, c = 0;
+  for (int b = lane; b < rows; b += 32) {
+    const double v = partials[(long long)b * slots + k];
+    const double t = sum + v;
+    c += (fabs(sum) >= fabs(v)) ? (sum - t) + v : (v - t) + sum;
+    sum = t;
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    const double s2 = __shfl_down_sync(0xffffffffu, sum, o);
+    const double c2 = __shfl_down_sync(0xffffffffu, c, o);
+    const double t = sum + s2;
+    c += c2 + ((fabs(sum) >= fabs(s2)) ? (sum - t) + s2 : (s2 - t) + sum);
+    sum = t;
+  }
+  if (lane == 0) out[k] = sum + c;
+}
+
+// Byte layout of the energy scratch (each piece 256-byte aligned).
+struct SqLayout {
+  size_t claim, total, contrib, keys, perm, hist, seed_q, seed_L, ck, partials, out, bytes;
+  int nchunks, nbwd, nck, slots;
+};
+
+SqLayout sq_layout(bool fp64, bool grad, long long n, int max_it, int nt, int nb, int sms) {
+  SqLayout L{};
+  const size_t el = fp64 ? sizeof(double) : sizeof(float);
+  L.slots = 1 + 5 * (nt + nb) + 1 + 1;  // energy, gradient, left-out samples
+  L.nchunks = (int)std::max<long long>(1, (n + SQ_CH - 1) / SQ_CH);
+  L.nbwd = grad ? sms * SQ_BWD_PER_SM : 0;
+  L.nck = max_it > 0 ? (max_it - 1) / SQ_CK + 1 : 0;
+  size_t at = 0;
+  auto take = [&](size_t b) {
+    const size_t o = at;
+    at += (b + 255) / 256 * 256;
+    return o;
+  };
+  const size_t nn = (size_t)std::max<long long>(n, 0);
+  L.claim = take(sizeof(unsigned long long));
+  L.total = take(sizeof(int));
+  L.contrib = take(sizeof(double) * nn);
+  L.keys = take(sizeof(int) * nn);
+  if (grad) {
+    L.perm = take(sizeof(unsigned) * nn);
+    L.hist = take(sizeof(int) * (size_t)(max_it + 1) * L.nchunks);
+    L.seed_q = take(4 * el * nn);
+    L.seed_L = take(el * nn);
+    L.ck = take(4 * el * nn * L.nck);
+  }
+  L.partials = take(sizeof(double) * (size_t)(L.nbwd + L.nchunks) * L.slots);
+  L.out = take(sizeof(double) * L.slots);
+  L.bytes = at;
+  return L;
+}
+
+int sm_count() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms;
+}
+
+template <class T>
+cudaError_t sq_launch(bool grad, const double* params, int nt, int nb, const double* xyz,
+                      const double* target, long long n, double slice, int max_it, double escape,
+                      double d_sat, unsigned char* scr, const SqLayout& L, int* iters, int sms,
+                      cudaStream_t s, int* launches) {
+  const int nr = nt + nb;
+  unsigned long long* claim = reinterpret_cast<unsigned long long*>(scr + L.claim);
+  int* total = reinterpret_cast<int*>(scr + L.total);
+  double* partials = reinterpret_cast<double*>(scr + L.partials);
+  SqFwdOut<T> o{};
+  o.contrib = reinterpret_cast<double*>(scr + L.contrib);
+  o.keys = reinterpret_cast<int*>(scr + L.keys);
+  o.iters = iters;
+  if (grad) {
+    o.seed_q = reinterpret_cast<V4<T>*>(scr + L.seed_q);
+    o.seed_L = reinterpret_cast<T*>(scr + L.seed_L);
+    o.ck = reinterpret_cast<V4<T>*>(scr + L.ck);
+  }
+  cudaError_t e = cudaMemsetAsync(claim, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  const size_t sh_roots = sizeof(T) * 5 * nr;
+  // persistent forward grid: as many blocks as stay resident
+  int per_sm = 0;
+  if (grad)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sq_fwd_kernel<T, true>, SQF_T, sh_roots);
+  else
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sq_fwd_kernel<T, false>, SQF_T, sh_roots);
+  if (e != cudaSuccess) return e;
+  const long long need = (n + SQF_T - 1) / SQF_T;
+  const int fblocks = (int)std::max<long long>(1, std::min<long long>((long long)sms * std::max(per_sm, 1), need));
+  if (grad)
+    sq_fwd_kernel<T, true><<<fblocks, SQF_T, sh_roots, s>>>(params, nt, nb, xyz, target, n, slice,
+                                                            max_it, escape, d_sat, claim, o);
+  else
+    sq_fwd_kernel<T, false><<<fblocks, SQF_T, sh_roots, s>>>(params, nt, nb, xyz, target, n, slice,
+                                                             max_it, escape, d_sat, claim, o);
+  int* hist = grad ? reinterpret_cast<int*>(scr + L.hist) : nullptr;
+  sq_chunk_kernel<<<L.nchunks, SQC_T, 0, s>>>(o.contrib, grad ? o.keys : nullptr, n, max_it,
+                                              L.nchunks, hist, partials, L.slots, L.nbwd);
+  *launches = 3;
+  if (grad) {
+    unsigned* perm = reinterpret_cast<unsigned*>(scr + L.perm);
+    sq_scan_kernel<<<1, 1024, 0, s>>>(hist, (long long)(max_it + 1) * L.nchunks, total);
+    sq_scatter_kernel<<<L.nchunks, 32, 0, s>>>(o.keys, n, max_it, L.nchunks, hist, perm);
+    const size_t sh = ((sizeof(T) * 5 * nr + 15) / 16) * 16 + sizeof(double) * (SQ_T / 32) * L.slots;
+    sq_bwd_kernel<T><<<L.nbwd, SQ_T, sh, s>>>(params, nt, nb, n, perm, total, o.keys, o.seed_q,
+                                              o.seed_L, o.ck, partials, L.slots);
+    *launches += 3;
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  sq_reduce_kernel<<<(L.slots * 32 + 255) / 256, 256, 0, s>>>(partials, L.nbwd + L.nchunks, L.slots,
+                                                              reinterpret_cast<double*>(scr + L.out));
+  return cudaGetLastError();
+}
+
 }  // namespace
 
 int sq_max_iterations() { return SQ_MAXIT; }
 
+size_t sq_scratch_bytes(bool fp64, bool grad, long long n, int max_it, int nt, int nb) {
+  return sq_layout(fp64, grad, n, max_it, nt, nb, sm_count()).bytes;
+}
+
 cudaError_t launch_sq_energy(bool fp64, bool grad, const double* params, int nt, int nb,
                              const double* xyz, const double* target, long long n, double slice,
-                             int max_it, double escape, double d_sat, double* partials,
-                             int nblocks, double* out, int* iters, cudaStream_t s) {
-  const int nr = nt + nb;
-  const int slots = 1 + 5 * nr + 1 + 1;  // energy, gradient, skipped-sample count
-  const size_t elem = fp64 ? sizeof(double) : sizeof(float);
-  const size_t sh = ((elem * 5 * nr + 15) / 16) * 16 + sizeof(double) * (SQ_T / 32) * slots;
-  if (fp64) {
-    if (grad)
-      sq_energy_kernel<double, true><<<nblocks, SQ_T, sh, s>>>(params, nt, nb, xyz, target, n, slice,
-                                                               max_it, escape, d_sat, partials, slots, iters);
-    else
-      sq_energy_kernel<double, false><<<nblocks, SQ_T, sh, s>>>(params, nt, nb, xyz, target, n, slice,
-                                                                max_it, escape, d_sat, partials, slots, iters);
-  } else {
-    if (grad)
-      sq_energy_kernel<float, true><<<nblocks, SQ_T, sh, s>>>(params, nt, nb, xyz, target, n, slice,
-                                                              max_it, escape, d_sat, partials, slots, iters);
-    else
-      sq_energy_kernel<float, false><<<nblocks, SQ_T, sh, s>>>(params, nt, nb, xyz, target, n, slice,
-                                                               max_it, escape, d_sat, partials, slots, iters);
-  }
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  reduce_partials_kernel<<<(slots + 255) / 256, 256, 0, s>>>(partials, nblocks, slots, out);
-  return cudaGetLastError();
+                             int max_it, double escape, double d_sat, void* scratch,
+                             double** out, int* iters, cudaStream_t s, int* launches) {
+  const int sms = sm_count();
+  const SqLayout L = sq_layout(fp64, grad, n, max_it, nt, nb, sms);
+  unsigned char* scr = static_cast<unsigned char*>(scratch);
+  *out = reinterpret_cast<double*>(scr + L.out);
+  if (fp64)
+    return sq_launch<double>(grad, params, nt, nb, xyz, target, n, slice, max_it, escape, d_sat,
+                             scr, L, iters, sms, s, launches);
+  return sq_launch<float>(grad, params, nt, nb, xyz, target, n, slice, max_it, escape, d_sat, scr,
+                          L, iters, sms, s, launches);
 }
 
 }  // namespace qj

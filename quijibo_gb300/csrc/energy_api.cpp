@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <vector>
 
@@ -85,24 +86,22 @@ static int sq_energy(qjg_ctx* ctx, const double* d_params, int32_t nt, int32_t n
     return fail(ctx, QJG_ERR_ARG, "energy precision must be QJG_FP32 or QJG_FP64");
   cudaStream_t s = (cudaStream_t)stream;
   QJ_CUDA(ctx, cudaSetDevice(ctx->device));
-  int sms = 0;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-  const int nblocks = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * 8, (n + 63) / 64));
+  if (n > INT32_MAX) return fail(ctx, QJG_ERR_ARG, "energy: %lld samples (at most 2^31 - 1)", (long long)n);
+  const bool fp64 = precision == QJG_FP64, grad = d_grad != nullptr;
   const int P = 5 * (nt + nb) + 1;
-  const int slots = 1 + P + 1;  // energy, gradient, samples left out of the gradient
-  double* d_part = nullptr;
-  QJ_CUDA(ctx, cudaMallocAsync((void**)&d_part, sizeof(double) * ((size_t)nblocks + 1) * slots, s));
-  double* d_out = d_part + (size_t)nblocks * slots;
-  cudaError_t e = qj::launch_sq_energy(precision == QJG_FP64, d_grad != nullptr, d_params, nt, nb,
-                                       d_xyz, d_target, n, slice, max_it, escape, d_sat, d_part,
-                                       nblocks, d_out, d_iters, s);
+  void* d_scr = nullptr;
+  QJ_CUDA(ctx, cudaMallocAsync(&d_scr, qj::sq_scratch_bytes(fp64, grad, n, max_it, nt, nb), s));
+  double* d_out = nullptr;
+  int launched = 0;
+  cudaError_t e = qj::launch_sq_energy(fp64, grad, d_params, nt, nb, d_xyz, d_target, n, slice,
+                                       max_it, escape, d_sat, d_scr, &d_out, d_iters, s, &launched);
   if (e == cudaSuccess && d_grad)
     e = cudaMemcpyAsync(d_grad, d_out + 1, sizeof(double) * P, cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(energy, d_out, sizeof(double), cudaMemcpyDeviceToHost, s);
-  cudaFreeAsync(d_part, s);
+  cudaFreeAsync(d_scr, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return fail(ctx, QJG_ERR_CUDA, "energy: %s", cudaGetErrorString(e));
-  ctx->launches += 2;
+  ctx->launches += launched;
   return QJG_OK;
 }
 

@@ -1,6 +1,7 @@
 // Host-side launchers of the energy kernels (energy.cu).
 #pragma once
 #include <cuda_runtime.h>
+#include <stddef.h>
 
 #include "qj_params.h"
 
@@ -20,9 +21,13 @@ cudaError_t launch_tanh_grad(const MapParams& m, const GridParams& g, const Weig
                              double* out, cudaStream_t s);
 
 int sq_max_iterations();
+// Device scratch of one energy call (forward, or forward + gradient).
+size_t sq_scratch_bytes(bool fp64, bool grad, long long n, int max_it, int nt, int nb);
+// *out (in the scratch): [energy, gradient (5 (nt + nb) + 1), samples left
+// out of the gradient]; *launches: kernels launched.
 cudaError_t launch_sq_energy(bool fp64, bool grad, const double* params, int nt, int nb,
                              const double* xyz, const double* target, long long n, double slice,
-                             int max_it, double escape, double d_sat, double* partials,
-                             int nblocks, double* out, int* iters, cudaStream_t s);
+                             int max_it, double escape, double d_sat, void* scratch,
+                             double** out, int* iters, cudaStream_t s, int* launches);
 
 }  // namespace qj
