@@ -275,17 +275,25 @@ __global__ void borders_kernel(double* __restrict__ f, int X, int Y, int Z, doub
   }
 }
 
-// Block partials summed in block order (Neumaier compensation).
+// Block partials summed in block order (Neumaier compensation); the loads of
+// 16 rows are issued before their additions.
 __global__ void reduce_cols_kernel(const double* __restrict__ part, int nblk, int ncol,
                                    double* __restrict__ out) {
+  constexpr int U = 16;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncol) return;
   double s = 0.0, comp = 0.0;
-  for (int b = 0; b < nblk; b++) {
-    const double v = part[(long long)b * ncol + c];
-    const double t = s + v;
-    comp += fabs(s) >= fabs(v) ? (s - t) + v : (v - t) + s;
-    s = t;
+  for (int b0 = 0; b0 < nblk; b0 += U) {
+    double v[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) v[u] = b0 + u < nblk ? part[(long long)(b0 + u) * ncol + c] : 0.0;
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      if (b0 + u >= nblk) break;
+      const double t = s + v[u];
+      comp += fabs(s) >= fabs(v[u]) ? (s - t) + v[u] : (v[u] - t) + s;
+      s = t;
+    }
   }
   out[c] = s + comp;
 }

@@ -634,15 +634,25 @@ __global__ void __launch_bounds__(EN_T, 4) tanh_grad_kernel(const __grid_constan
 }
 
 // Neumaier-compensated sum of partials[b][k] over blocks b, in block order.
+// The loads of 16 rows are issued before their additions (same additions in
+// the same order), so the loop waits on memory once per 16 rows.
 __global__ void reduce_partials_kernel(const double* __restrict__ partials, int nblocks,
                                        int slots, double* __restrict__ out) {
+  constexpr int U = 16;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < slots; k += gridDim.x * blockDim.x) {
     double s = 0, c = 0;
-    for (int b = 0; b < nblocks; b++) {
-      const double v = partials[(long long)b * slots + k];
-      const double t = s + v;
-      c += (fabs(s) >= fabs(v)) ? (s - t) + v : (v - t) + s;
-      s = t;
+    for (int b0 = 0; b0 < nblocks; b0 += U) {
+      double v[U];
+#pragma unroll
+      for (int u = 0; u < U; u++)
+        v[u] = b0 + u < nblocks ? partials[(long long)(b0 + u) * slots + k] : 0.0;
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        if (b0 + u >= nblocks) break;
+        const double t = s + v[u];
+        c += (fabs(s) >= fabs(v[u])) ? (s - t) + v[u] : (v[u] - t) + s;
+        s = t;
+      }
     }
     out[k] = s + c;
   }
@@ -991,7 +1001,9 @@ __global__ void __launch_bounds__(SQF_T) sq_fwd_kernel(
 }
 
 // Per chunk of SQ_CH samples: the energy and the left-out count summed in a
-// fixed tree (one partial row per chunk, after the backward pass's rows), and
+// fixed tree (one partial row per chunk; the backward pass's rows follow, so a
+// chunk's row index, and with it the energy's bits, is the same with or
+// without the gradient), and
 // (gradient pass) the histogram of orbit lengths for the sort, bucket
 // max_it - N so that long orbits come first: hist[bucket * nchunks + chunk].
 __global__ void __launch_bounds__(SQC_T) sq_chunk_kernel(const double* __restrict__ contrib,
@@ -1315,7 +1327,7 @@ cudaError_t sq_launch(bool grad, const double* params, int nt, int nb, const dou
                                                              max_it, escape, d_sat, claim, o);
   int* hist = grad ? reinterpret_cast<int*>(scr + L.hist) : nullptr;
   sq_chunk_kernel<<<L.nchunks, SQC_T, 0, s>>>(o.contrib, grad ? o.keys : nullptr, n, max_it,
-                                              L.nchunks, hist, partials, L.slots, L.nbwd);
+                                              L.nchunks, hist, partials, L.slots, 0);
   *launches = 3;
   if (grad) {
     unsigned* perm = reinterpret_cast<unsigned*>(scr + L.perm);
@@ -1323,7 +1335,8 @@ cudaError_t sq_launch(bool grad, const double* params, int nt, int nb, const dou
     sq_scatter_kernel<<<L.nchunks, 32, 0, s>>>(o.keys, n, max_it, L.nchunks, hist, perm);
     const size_t sh = ((sizeof(T) * 5 * nr + 15) / 16) * 16 + sizeof(double) * (SQ_T / 32) * L.slots;
     sq_bwd_kernel<T><<<L.nbwd, SQ_T, sh, s>>>(params, nt, nb, n, perm, total, o.keys, o.seed_q,
-                                              o.seed_L, o.ck, partials, L.slots);
+                                              o.seed_L, o.ck,
+                                              partials + (size_t)L.nchunks * L.slots, L.slots);
     *launches += 3;
   }
   e = cudaGetLastError();

@@ -119,3 +119,34 @@ def test_device_lbfgs_decreases_energy(ctx, precision):
     assert np.all(np.diff(en) <= 0)
     assert en[-1] < 0.9 * en[0]
     assert not torch.equal(p, p0)
+
+
+@pytest.mark.parametrize("precision", [lib.QJG_FP32, lib.QJG_FP64])
+def test_energy_sizes_split_and_repeat(ctx, precision):
+    """Empty, single-sample and chunk-boundary sample counts; the energy of
+    two disjoint halves adds up to the whole; a repeated call gives the same
+    bits (the sums do not depend on which lane took which sample)."""
+    rs, xyz, t = small_case(n=4500)
+    p = dev(lib.params_of(rs))
+    nt, nb = rs.n_top, rs.n_bottom
+
+    def run(lo, hi, grad=True):
+        X, T = dev(xyz[lo:hi].reshape(-1, 3)), dev(t[lo:hi])
+        g = torch.full((len(p),), 7.0, dtype=torch.float64, device="cuda")
+        e = ctx.energy(p.data_ptr(), nt, nb, hi - lo, X.data_ptr(), T.data_ptr(), 6, 2.0,
+                       precision=precision, d_grad=g.data_ptr() if grad else 0)
+        return e, g.cpu().numpy()
+
+    e0, g0 = run(0, 0)
+    assert e0 == 0.0 and not g0.any()
+    e1, g1 = run(0, 1)
+    assert e1 == run(0, 1, grad=False)[0] and np.all(np.isfinite(g1))
+    ea, ga = run(0, 2049)
+    eb, gb = run(2049, len(t))
+    ew, gw = run(0, len(t))
+    assert abs((ea + eb) - ew) <= 1e-12 * abs(ew)
+    assert np.linalg.norm((ga + gb) - gw) <= (1e-6 if precision == lib.QJG_FP32 else 1e-12) * np.linalg.norm(gw)
+    ew2, gw2 = run(0, len(t))
+    assert ew2 == ew and np.array_equal(gw2, gw)
+    # the forward alone gives the energy of the gradient call
+    assert run(0, len(t), grad=False)[0] == ew
