@@ -87,8 +87,9 @@ def bench_energy(args):
     G = torch.empty_like(P)
     n = len(t)
     out = {"samples": n, "params": int(P.numel()), "max_it": p["max_it"]}
-    for name, prec, grad in (("forward_fp32", lib.QJG_FP32, False), ("adjoint_fp32", lib.QJG_FP32, True),
-                             ("forward_fp64", lib.QJG_FP64, False), ("adjoint_fp64", lib.QJG_FP64, True)):
+    forms = (("forward_fp32", lib.QJG_FP32, False), ("adjoint_fp32", lib.QJG_FP32, True),
+             ("forward_fp64", lib.QJG_FP64, False), ("adjoint_fp64", lib.QJG_FP64, True))
+    for name, prec, grad in forms[:2] if args.fp32_only else forms:
         kw = dict(precision=prec, d_grad=G.data_ptr() if grad else 0)
         ctx.energy(P.data_ptr(), rs.n_top, rs.n_bottom, n, X.data_ptr(), T.data_ptr(), p["max_it"],
                    p["escape"], **kw)
@@ -101,6 +102,8 @@ def bench_energy(args):
         dt = (time.perf_counter() - t0) / reps
         out[name] = {"s": dt, "samples_per_s": n / dt, "energy": e}
     out["gradients_per_s"] = 1.0 / out["adjoint_fp32"]["s"]
+    if args.steps <= 0:
+        return out
     Pfit = P.clone()
     t0 = time.perf_counter()
     en, st = ctx.fit_lbfgs(Pfit.data_ptr(), rs.n_top, rs.n_bottom, n, X.data_ptr(), T.data_ptr(),
@@ -514,6 +517,7 @@ def main():
     ap.add_argument("--tri-cap", type=int, default=0)
     ap.add_argument("--samples", type=int, default=200_000)
     ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--fp32-only", action="store_true", help="energy: skip the FP64 forms")
     ap.add_argument("--requests", type=int, default=400)
     ap.add_argument("--scale", type=float, default=0.25)
     ap.add_argument("--span", type=float, default=20.0)
