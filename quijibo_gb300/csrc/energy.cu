@@ -1095,11 +1095,22 @@ __global__ void __launch_bounds__(32) sq_scatter_kernel(const int* __restrict__ 
 }
 
 // Backward pass over the sorted gradient samples: warp w takes groups of 32
-// consecutive entries w, w + W, ... (equal orbit lengths within a group, so
-// no lane waits on another's longer orbit).  It stores no trajectory: from
-// each checkpoint it recomputes the segment forward before reversing it.
-// Each thread's sums run over a fixed set of samples, so the gradient is the
-// same on every run.
+// consecutive entries w, w + W, ... (equal orbit lengths within a group but
+// at bucket edges, so lanes seldom wait on a longer orbit).  It stores no
+// trajectory: from each checkpoint it recomputes the segment forward before
+// reversing it.  The steps run warp-uniformly down from the group's longest
+// orbit (a lane takes part in the steps below its own length), so that every
+// root term's five gradient components are summed over the warp with
+// shuffles and added to the warp's double accumulators in shared memory:
+// no per-thread gradient array in local memory, and the sums run in a fixed
+// order (the gradient is the same on every run).
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
 template <class T>
 __global__ void __launch_bounds__(SQ_T) sq_bwd_kernel(
     const double* __restrict__ params, int nt, int nb, long long n_samples,
@@ -1117,101 +1128,115 @@ __global__ void __launch_bounds__(SQ_T) sq_bwd_kernel(
   for (int k = threadIdx.x; k < (SQ_T / 32) * slots; k += SQ_T) acc_sh[k] = 0.0;
   __syncthreads();
   const T s = (T)exp(params[5 * nr]);
+  // this warp's sums: acc[1 + 4 i + c] root positions, acc[1 + 4 nr + i]
+  // exponents, acc[1 + 5 nr] log s
   double* acc = acc_sh + (threadIdx.x >> 5) * slots;
   // per-thread scratch (local memory)
   V4<T> seg[SQ_CK];
   V4<T> F[QJ_MAX_ROOTS];
-  T gacc[5 * QJ_MAX_ROOTS + 1];
-  for (int k = 0; k <= 5 * nr; k++) gacc[k] = T(0);
+  const V4<T> zero{T(0), T(0), T(0), T(0)};
   const int count = *total;
   const int lane = threadIdx.x & 31;
   const long long W = ((long long)gridDim.x * SQ_T) >> 5;
   for (long long grp = ((long long)blockIdx.x * SQ_T + threadIdx.x) >> 5; grp * 32 < count;
        grp += W) {
     const long long j = grp * 32 + lane;
-    if (j >= count) continue;
-    const long long k = perm[j];
-    const int N = keys[k];
-    V4<T> qb = seed_q[k];
-    const T Lb = seed_L[k];
+    const bool in = j < count;
+    const long long k = in ? (long long)perm[j] : 0;
+    const int N = in ? keys[k] : 0;
+    V4<T> qb = in ? seed_q[k] : zero;
+    const T Lb = in ? seed_L[k] : T(0);
+    const int Nmax = __reduce_max_sync(0xffffffffu, N);
     // segments in reverse
-    for (int sgi = (N - 1) / SQ_CK; sgi >= 0; sgi--) {
-      const int n0 = sgi * SQ_CK, n1 = min(N, n0 + SQ_CK);
-      V4<T> q = ck[(long long)sgi * n_samples + k];
+    for (int sgi = (Nmax - 1) / SQ_CK; sgi >= 0; sgi--) {
+      const int n0 = sgi * SQ_CK, n1 = min(N, n0 + SQ_CK), n1max = min(Nmax, n0 + SQ_CK);
+      V4<T> q = n1 > n0 ? ck[(long long)sgi * n_samples + k] : zero;
       for (int n = n0; n < n1; n++) {
         seg[n - n0] = q;
         T lg;
         q = sq_apply<T>(rp, ep, nt, nb, s, q, &lg, nullptr, nullptr, nullptr, nullptr);
       }
-      for (int n = n1 - 1; n >= n0; n--) {
-        const V4<T> qn = seg[n - n0];
-        T lg;
-        V4<T> Tq, Bq;
-        const V4<T> Q = sq_apply<T>(rp, ep, nt, nb, s, qn, &lg, F, nullptr, &Tq, &Bq);
-        // L_{n+1} = L_n + log|g| + log|Q|
-        V4<T> Qb = v4add(qb, v4scale(Q, Lb / v4dot(Q, Q)));
-        // d/d log s: <Qbar, Q>
-        gacc[5 * nr] += v4dot(Qb, Q);
-        V4<T> Tb, Bb = {T(0), T(0), T(0), T(0)};
-        if (nb > 0) {
-          const V4<T> W4 = v4scale(v4conj(Bq), T(1) / v4dot(Bq, Bq));
-          Tb = v4scale(v4mul(Qb, v4conj(W4)), s);
-          const V4<T> Wb = v4scale(v4mul(v4conj(Tq), Qb), s);
-          Bb = v4scale(v4mul(v4mul(v4conj(W4), Wb), v4conj(W4)), T(-1));
-        } else {
-          Tb = v4scale(Qb, s);
+      for (int n = n1max - 1; n >= n0; n--) {
+        const bool on = n < n1;  // this lane's orbit has step n
+        V4<T> qn = zero, Tb = zero, Bb = zero, gb = zero;
+        T dls = T(0);
+        if (on) {
+          qn = seg[n - n0];
+          T lg;
+          V4<T> Tq, Bq;
+          const V4<T> Q = sq_apply<T>(rp, ep, nt, nb, s, qn, &lg, F, nullptr, &Tq, &Bq);
+          // L_{n+1} = L_n + log|g| + log|Q|
+          const V4<T> Qb = v4add(qb, v4scale(Q, Lb / v4dot(Q, Q)));
+          // d/d log s: <Qbar, Q>
+          dls = v4dot(Qb, Q);
+          if (nb > 0) {
+            const V4<T> W4 = v4scale(v4conj(Bq), T(1) / v4dot(Bq, Bq));
+            Tb = v4scale(v4mul(Qb, v4conj(W4)), s);
+            const V4<T> Wb = v4scale(v4mul(v4conj(Tq), Qb), s);
+            Bb = v4scale(v4mul(v4mul(v4conj(W4), Wb), v4conj(W4)), T(-1));
+          } else {
+            Tb = v4scale(Qb, s);
+          }
+          // gradient of log|g| w.r.t. g
+          V4<T> g = zero;
+          for (int i = 0; i < nr; i++) {
+            const V4<T> d{qn.w - rp[4 * i], qn.x - rp[4 * i + 1], qn.y - rp[4 * i + 2],
+                          qn.z - rp[4 * i + 3]};
+            g = v4add(g, v4scale(d, (i >= nt ? -ep[i] : ep[i]) / v4dot(d, d)));
+          }
+          gb = v4scale(g, Lb / v4dot(g, g));
         }
-        // gradient of log|g| w.r.t. g
-        V4<T> g = {T(0), T(0), T(0), T(0)};
-        for (int i = 0; i < nr; i++) {
-          const V4<T> d{qn.w - rp[4 * i], qn.x - rp[4 * i + 1], qn.y - rp[4 * i + 2],
-                        qn.z - rp[4 * i + 3]};
-          g = v4add(g, v4scale(d, (i >= nt ? -ep[i] : ep[i]) / v4dot(d, d)));
-        }
-        const V4<T> gb = v4scale(g, Lb / v4dot(g, g));
-        V4<T> qbn = {T(0), T(0), T(0), T(0)};
+        dls = warp_sum(dls);
+        if (lane == 0) acc[1 + 5 * nr] += (double)dls;
+        V4<T> qbn = zero;
         // products: Pbar_i = conj(F_{i-1}) U, U <- U conj(P_i), from the end
         for (int side = 1; side >= 0; side--) {
           const int lo = side ? nt : 0, hi = side ? nr : nt;
           if (hi == lo) continue;
           V4<T> U = side ? Bb : Tb;
           for (int i = hi - 1; i >= lo; i--) {
-            const V4<T> d{qn.w - rp[4 * i], qn.x - rp[4 * i + 1], qn.y - rp[4 * i + 2],
-                          qn.z - rp[4 * i + 3]};
-            PowParts<T> pp;
-            const V4<T> P = powv<T>(d, ep[i], &pp);
-            const V4<T> Pb = (i == lo) ? U : v4mul(v4conj(F[i - 1]), U);
-            U = v4mul(U, v4conj(P));
-            T eb = T(0);
-            V4<T> dbar = powv_vjp<T>(d, ep[i], pp, Pb, &eb);
-            // g term: sgn e d/|d|^2
-            const T sgn = side ? T(-1) : T(1);
-            const T d2 = v4dot(d, d);
-            const T dg = v4dot(d, gb);
-            dbar = v4add(dbar, v4scale(v4add(v4scale(gb, T(1) / d2), v4scale(d, T(-2) * dg / (d2 * d2))),
-                                       sgn * ep[i]));
-            eb += sgn * dg / d2;
-            gacc[4 * nr + i] += eb;
-            gacc[4 * i] -= dbar.w;
-            gacc[4 * i + 1] -= dbar.x;
-            gacc[4 * i + 2] -= dbar.y;
-            gacc[4 * i + 3] -= dbar.z;
-            qbn = v4add(qbn, dbar);
+            T c0 = T(0), c1 = T(0), c2 = T(0), c3 = T(0), c4 = T(0);
+            if (on) {
+              const V4<T> d{qn.w - rp[4 * i], qn.x - rp[4 * i + 1], qn.y - rp[4 * i + 2],
+                            qn.z - rp[4 * i + 3]};
+              PowParts<T> pp;
+              const V4<T> P = powv<T>(d, ep[i], &pp);
+              const V4<T> Pb = (i == lo) ? U : v4mul(v4conj(F[i - 1]), U);
+              U = v4mul(U, v4conj(P));
+              T eb = T(0);
+              V4<T> dbar = powv_vjp<T>(d, ep[i], pp, Pb, &eb);
+              // g term: sgn e d/|d|^2
+              const T sgn = side ? T(-1) : T(1);
+              const T d2 = v4dot(d, d);
+              const T dg = v4dot(d, gb);
+              dbar = v4add(dbar, v4scale(v4add(v4scale(gb, T(1) / d2),
+                                               v4scale(d, T(-2) * dg / (d2 * d2))),
+                                         sgn * ep[i]));
+              eb += sgn * dg / d2;
+              c0 = -dbar.w;
+              c1 = -dbar.x;
+              c2 = -dbar.y;
+              c3 = -dbar.z;
+              c4 = eb;
+              qbn = v4add(qbn, dbar);
+            }
+            c0 = warp_sum(c0);
+            c1 = warp_sum(c1);
+            c2 = warp_sum(c2);
+            c3 = warp_sum(c3);
+            c4 = warp_sum(c4);
+            if (lane < 5) {
+              const T v = lane == 0 ? c0 : lane == 1 ? c1 : lane == 2 ? c2 : lane == 3 ? c3 : c4;
+              acc[1 + (lane < 4 ? 4 * i + lane : 4 * nr + i)] += (double)v;
+            }
           }
         }
-        qb = qbn;
+        if (on) qb = qbn;
       }
     }
   }
-  // deterministic reduction: warp trees, warps in order (the energy and the
-  // left-out count are in the chunk rows)
-  for (int k = 0; k < slots; k++) {
-    double v = (k == 0 || k == slots - 1) ? 0.0 : (double)gacc[k - 1];
-#pragma unroll
-    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0) acc[k] += v;
-  }
   __syncthreads();
+  // warps in order (the energy and the left-out count are in the chunk rows)
   for (int k = threadIdx.x; k < slots; k += SQ_T) {
     double v = 0;
     for (int w = 0; w < SQ_T / 32; w++) v += acc_sh[w * slots + k];
