@@ -155,24 +155,34 @@ __global__ void __launch_bounds__(SCAN_T) emit_kernel(Op op, long long n, const 
 
 // ------------------------------------------------------------ classify
 
-// flags[l * XY + y * X + x] for layers l of `src` planes l and l+1.
-__global__ void flags_kernel(const double* __restrict__ src, int X, int Y, long long n_layers,
-                             uint8_t* __restrict__ flags) {
+// flags[l * XY + y * X + x] for layers l of `src` planes l and l+1.  One
+// thread per (x, y) walks the layers: the four corners of plane l+1 are
+// loaded once and reused as the lower corners of the next layer (4 loads per
+// cube instead of 8, of which the x+1 pair hits L1 behind the neighbouring
+// lane; rows are read coalesced across the warp).
+__device__ __forceinline__ int plane_bits(const double* u, int X) {
+  // corner weights NNN=1 NNP=2 NPN=4 NPP=8 PNN=16 PNP=32 PPN=64 PPP=128
+  // (TRIANGLE_MESH.cpp:4929-4931; letters x, y, z): the z-lower corners
+  return (u[0] > 0) | ((u[X] > 0) << 2) | ((u[1] > 0) << 4) | ((u[1 + X] > 0) << 6);
+}
+
+__global__ void __launch_bounds__(128) flags_kernel(const double* __restrict__ src, int X, int Y,
+                                                    long long n_layers,
+                                                    uint8_t* __restrict__ flags) {
   const long long XY = (long long)X * Y;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_layers * XY;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int x = (int)(i % X);
-    const int y = (int)((i / X) % Y);
-    int f = 0;
-    if (x < X - 1 && y < Y - 1) {
-      const double* v = src + i;
-      // corner weights NNN=1 NNP=2 NPN=4 NPP=8 PNN=16 PNP=32 PPN=64 PPP=128
-      // (TRIANGLE_MESH.cpp:4929-4931; letters x, y, z)
-      f = (v[0] > 0) | ((v[XY] > 0) << 1) | ((v[X] > 0) << 2) | ((v[X + XY] > 0) << 3) |
-          ((v[1] > 0) << 4) | ((v[1 + XY] > 0) << 5) | ((v[1 + X] > 0) << 6) |
-          ((v[1 + X + XY] > 0) << 7);
-    }
-    flags[i] = (uint8_t)f;
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= XY) return;
+  const int y = (int)(p / X), x = (int)(p - (long long)y * X);
+  if (x >= X - 1 || y >= Y - 1) {
+    for (long long l = 0; l < n_layers; l++) flags[l * XY + p] = 0;
+    return;
+  }
+  int lo = plane_bits(src + p, X);
+#pragma unroll 4
+  for (long long l = 0; l < n_layers; l++) {
+    const int hi = plane_bits(src + (l + 1) * XY + p, X);
+    flags[l * XY + p] = (uint8_t)(lo | (hi << 1));
+    lo = hi;
   }
 }
 
@@ -189,11 +199,9 @@ struct MaskCount {
     if (j < lay_lo || j >= lay_hi || x < 0 || y < 0 || x > X - 2 || y > Y - 2) return 0;
     return flags[((long long)j * Y + y) * X + x];
   }
-  __device__ int count(long long i) const {
+  // item i at window plane j, column x, row y
+  __device__ int count_at(long long i, int j, int x, int y) const {
     const long long XY = (long long)X * Y;
-    const int j = j0 + (int)(i / XY);
-    const int r = (int)(i % XY);
-    const int x = r % X, y = r / X;
     // x-edge: edges 10 (cube x,y,j), 9 (x,y-1,j), 11 (x,y,j-1), 12 (x,y-1,j-1)
     const bool ex = (QJ_MC_EDGEMASK[flag(j, x, y)] >> 9 & 1) |
                     (QJ_MC_EDGEMASK[flag(j, x, y - 1)] >> 8 & 1) |
@@ -214,6 +222,35 @@ struct MaskCount {
     return __popc(m);
   }
 };
+
+// Pass 1 of the vertex-id scan over MaskCount, with the item coordinates
+// advanced along x from one division per thread instead of three per item.
+__global__ void __launch_bounds__(SCAN_T) mask_count_kernel(MaskCount op, long long n,
+                                                            long long* bsum) {
+  const long long base = (long long)blockIdx.x * SCAN_B + (long long)threadIdx.x * SCAN_V;
+  long long c = 0;
+  if (base < n) {
+    const long long XY = (long long)op.X * op.Y;
+    int j = (int)(base / XY);
+    const int r = (int)(base - j * XY);
+    int y = r / op.X, x = r - y * op.X;
+    j += op.j0;
+#pragma unroll
+    for (int k = 0; k < SCAN_V; k++) {
+      if (base + k < n) c += op.count_at(base + k, j, x, y);
+      if (++x == op.X) {
+        x = 0;
+        if (++y == op.Y) {
+          y = 0;
+          j++;
+        }
+      }
+    }
+  }
+  long long total;
+  block_exclusive_scan(c, &total);
+  if (threadIdx.x == 0) bsum[blockIdx.x] = total;
+}
 
 // Vertex ids (global) of window planes [j0, ...) and the list of their edges
 // (window voxel index * 4 + axis) in id order.
@@ -760,8 +797,9 @@ cudaError_t mesh_flags(const double* src, int X, int Y, long long n_layers, uint
                        cudaStream_t s) {
   if (n_layers <= 0) return cudaSuccess;
   const long long n = n_layers * X * Y;
-  const int blocks = (int)std::min<long long>((n + 255) / 256, (long long)sm_count() * 16);
-  flags_kernel<<<blocks, 256, 0, s>>>(src, X, Y, n_layers, flags);
+  (void)n;
+  const long long XY = (long long)X * Y;
+  flags_kernel<<<(unsigned)((XY + 127) / 128), 128, 0, s>>>(src, X, Y, n_layers, flags);
   return cudaGetLastError();
 }
 
@@ -778,7 +816,7 @@ cudaError_t mesh_vertex_ids(MeshWindow& w, int j0, int j1, int lay_lo, int lay_h
     *n_new = 0;
     return cudaSuccess;
   }
-  count_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(mc, n, w.bsum);
+  mask_count_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(mc, n, w.bsum);
   scan_bsum_kernel<<<1, 1024, 0, s>>>(w.bsum, nb);
   if ((err = cudaMemcpyAsync(n_new, w.bsum + nb, sizeof(long long), cudaMemcpyDeviceToHost, s)))
     return err;

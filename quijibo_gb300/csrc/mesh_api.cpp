@@ -20,9 +20,10 @@ namespace {
 
 // Grow a device buffer to hold n elements, keeping the first `keep`.
 template <class T>
-int grow_keep(qjg_ctx* ctx, T** buf, size_t* cap, size_t n, size_t keep, cudaStream_t s) {
+int grow_keep(qjg_ctx* ctx, T** buf, size_t* cap, size_t n, size_t keep, cudaStream_t s,
+              size_t hint = 0) {
   if (*cap >= n && *buf) return QJG_OK;
-  size_t want = std::max(n, *cap + *cap / 2);
+  size_t want = std::max(std::max(n, *cap + *cap / 2), hint);
   T* nb = nullptr;
   QJ_CUDA(ctx, cudaMalloc((void**)&nb, want * sizeof(T)));
   if (*buf && keep) QJ_CUDA(ctx, cudaMemcpyAsync(nb, *buf, keep * sizeof(T), cudaMemcpyDeviceToDevice, s));
@@ -157,7 +158,11 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
     const int j1 = L + 1 + (last ? 1 : 0);
     long long n_new = 0;
     auto ensure_list = [&](long long n) -> cudaError_t {
-      if (ensure(ctx, &ctx->m_list, &ctx->m_list_cap, (size_t)std::max<long long>(n, 1)))
+      // grows by half again at least: the per-slab vertex count rises with the surface
+      const size_t want = (size_t)std::max<long long>(n, 1);
+      if (ensure(ctx, &ctx->m_list, &ctx->m_list_cap,
+                 want > ctx->m_list_cap ? std::max(want, ctx->m_list_cap + ctx->m_list_cap / 2)
+                                        : want))
         return cudaErrorMemoryAllocation;
       w.list = ctx->m_list;
       return cudaSuccess;
@@ -166,8 +171,16 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
     ctx->launches += 3;
     if (nv + n_new > INT32_MAX)
       return fail(ctx, QJG_ERR_CAPACITY, "more than 2^31 vertices; int32 indices cannot hold them");
+    // per-vertex buffers grow to the vertex count extrapolated from the layers
+    // meshed so far (+25%; at most 4x the count so far, and no more than the
+    // caller's vertex capacity), so that a large mesh reallocates (cudaMalloc,
+    // copy, cudaFree) a few times instead of once per slab
+    const double need = (double)(nv + n_new);
+    double vh = std::min(need * (Z - 1) / c1 * 1.25, 4.0 * need);
+    if (vcap > 0) vh = std::min(vh, std::max((double)vcap, need));
+    const size_t vhint = (size_t)vh + 1;
     if ((rc = grow_keep(ctx, &ctx->m_verts, &ctx->m_verts_cap, (size_t)(nv + n_new) * 3,
-                        (size_t)nv * 3, s)))
+                        (size_t)nv * 3, s, vhint * 3)))
       return rc;
     QJ_CUDA(ctx, mark(2));
     // FP32-first bisection unless the plain FP64 form is asked for
@@ -178,9 +191,9 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
       // edge states by global vertex id; parked ids accumulate over slabs
       const size_t eb = qj::mesh_edge_state_bytes();
       if ((rc = grow_keep(ctx, &ctx->m_estate, &ctx->m_estate_cap, (size_t)(nv + n_new) * eb,
-                          (size_t)nv * eb, s)) ||
+                          (size_t)nv * eb, s, vhint * eb)) ||
           (rc = grow_keep(ctx, &ctx->m_epark, &ctx->m_epark_cap, (size_t)(nv + n_new),
-                          (size_t)nv, s)))
+                          (size_t)nv, s, vhint)))
         return rc;
       esc.state = ctx->m_estate;
       esc.list[0] = ctx->m_epark;
