@@ -235,7 +235,27 @@ def run_ours(args, world, rank, local):
                 "sign_map_disagreements": sign_diff, "max_rel_err": float(rel.max().item()),
                 "rms_rel_err": float(rel.pow(2).mean().sqrt().item()),
                 "frac_rel_err_le_1e-6": float((rel <= 1e-6).double().mean().item()),
-                "voxel_iters": st64["voxel_iters"]}
+                "voxel_iters": st64["voxel_iters"],
+                "form": "plain FP64: the reference's polar QUATERNION::pow per root term"}
+        del rel
+        # the same algebra as the precision form (integer powers as repeated
+        # products) in FP64: splits the speed-up into algorithm and precision
+        iti = ctx.iter_params(p["max_it"], p["escape"], precision=lib.QJG_FP64,
+                              refine_pow=lib.QJG_REFINE_INT)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.field(h, g, iti, f64.data_ptr(), stream=sptr)
+        e1.record(stream)
+        e1.synchronize()
+        msi = e0.elapsed_time(e1)
+        rel = (field - f64).abs() / f64.abs().clamp_min(1e-300)
+        fp64["int_powers"] = {
+            "form": "FP64 with integer powers as repeated products (the precision form's algebra)",
+            "gvox_s": n / (msi * 1e-3) / 1e9, "ms": msi, "speedup_fp32_refine": msi / ms,
+            "speedup_algorithm_int_over_pow": ms64 / msi,
+            "sign_map_disagreements": int(((field > 0) != (f64 > 0)).sum().item()),
+            "max_rel_err": float(rel.max().item()),
+            "rms_rel_err": float(rel.pow(2).mean().sqrt().item())}
         del f64, rel
 
     # roofline of the FP32 bulk kernel (FMA-pipe bound)
@@ -270,6 +290,17 @@ def run_ours(args, world, rank, local):
                                    workers=8, budget_gb=64.0, baseline_sample=10)
         serving = bench_serve(sargs)
 
+    # the large-grid configuration (48/24 roots, 60 iterations, 2200^3 in
+    # 64-slice slabs): one streamed field + mesh pass, its FMA roofline and
+    # mesher GB/s, and sampled slices against both FP64 forms
+    large = None
+    if rank == 0 and not args.no_large:
+        from quijibo_gb300.benchmarks import bench_large, hbm_peak_gbs
+        largs = argparse.Namespace(res=args.large_res, slab=64, rel_tol=args.rel_tol, vert_cap=0,
+                                   tri_cap=0, no_mesh=False, field_pass=False,
+                                   check_slices=args.large_slices, hbm_gbs=hbm_peak_gbs()[0])
+        large = bench_large(largs)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         slices = [int(v) for v in np.linspace(0, g.res[2] - 1, args.cpu_slices)]
@@ -300,6 +331,7 @@ def run_ours(args, world, rank, local):
                      "flops_per_launch": flops},
         "cpu_baseline": cpu,
         "serving": serving,
+        "large": large,
         "e2e": e2e,
         "gpu_launches": launches,
         "clocks": clk,
@@ -323,6 +355,9 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 plain-form comparison")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving stream")
     ap.add_argument("--serve-requests", type=int, default=200)
+    ap.add_argument("--no-large", action="store_true", help="skip the 2200^3 large-grid record")
+    ap.add_argument("--large-res", type=int, default=2200)
+    ap.add_argument("--large-slices", type=int, default=4)
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.impl == "reference":

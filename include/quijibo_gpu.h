@@ -117,18 +117,21 @@ int qjg_field_host(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg
 /* Counters of the last qjg_field call on ctx; synchronizes `stream`. */
 int qjg_field_stats_read(qjg_ctx* ctx, void* stream, qjg_field_stats* out);
 
-/* The field, for callers that cannot allocate device memory: code running
- * while a stream is captured into a CUDA graph, plugins whose host runtime
- * owns every device allocation, real-time loops that must not reach the
- * allocator.  No counterpart in the reference.  The map comes as host arrays
+/* The field, for callers that cannot allocate device memory: plugins whose
+ * host application owns every device allocation (its own pool, nothing left
+ * for a library to cudaMalloc), real-time loops that must not reach the
+ * allocator, processes held to a fixed device-memory quota.  No counterpart
+ * in the reference.  The map comes as host arrays
  * (as in qjg_rootset_upload), the output is a device buffer as in qjg_field;
- * no context is needed and nothing is allocated: the counters and the FP64
- * refine list live in a fixed scratch array inside the library (about
- * 16 MiB, held on every device that loads the library until the process
- * exits).  One call covers at most QJG_NOALLOC_MAX_VOXELS voxels (X*Y*(z1-z0));
+ * no context is needed and nothing is allocated: the counters, the FP64
+ * refine list and the double-float re-run list live in a fixed scratch array
+ * inside the library (about 32 MiB, held on every device that loads the
+ * library until the process exits).  The field has the bits of qjg_field's
+ * for the same inputs, rel_tol included.  One call covers at most QJG_NOALLOC_MAX_VOXELS voxels (X*Y*(z1-z0));
  * larger slab ranges return QJG_ERR_CAPACITY before anything is launched.
- * The first call on a device looks up the scratch array's device address, so
- * make it before any stream capture.  Every call shares the scratch array:
+ * The first call on a device looks up the scratch array's device address
+ * (with that device current), so make that first call before any stream
+ * capture.  Every call shares the scratch array:
  * calls whose work overlaps on the GPU (different streams or host threads)
  * race on it and must be serialised by the caller. */
 #define QJG_NOALLOC_MAX_VOXELS (1 << 22)
@@ -161,6 +164,7 @@ typedef struct {
   double ms_vertices;    /* vertex placement (interpolation or bisection) */
   double ms_triangles;   /* triangle emission */
   double ms_filter;      /* degenerate-triangle filter and output conversion */
+  double ms_field_bulk;  /* qjg_mesh_stream: the FP32 bulk kernel's part of ms_field */
 } qjg_mesh_stats;
 
 /* Marching cubes on a stored device field (X*Y*Z doubles).  Corners are

@@ -82,6 +82,10 @@ class Oracle:
         L.qjo_field.argtypes = [C.POINTER(_Map), C.POINTER(_Grid), C.c_int, C.c_double, C.c_int,
                                 C.c_int, _dp, _dp, C.POINTER(C.c_int32), C.c_int]
         L.qjo_field.restype = C.c_int64
+        L.qjo_field_window.argtypes = [C.POINTER(_Map), C.POINTER(_Grid), C.c_int, C.c_double,
+                                       C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _dp,
+                                       C.c_int]
+        L.qjo_field_window.restype = None
         L.qjo_nonlinear_value.argtypes = [C.POINTER(_Map), _dp, C.c_double, C.c_int, C.c_double,
                                           C.c_double]
         L.qjo_nonlinear_value.restype = C.c_double
@@ -134,6 +138,14 @@ class Oracle:
         if iters:
             out["iters"] = it.reshape(shape)
         return out
+
+    def field_window(self, rootset, grid, max_it, escape, x0, x1, y0, y1, z0, z1, nthreads=0):
+        """log|q_N| on the cells [x0,x1) x [y0,y1) x [z0,z1) of `grid` (cell
+        centres of the full grid), shaped (z, y, x)."""
+        f = np.empty((z1 - z0) * (y1 - y0) * (x1 - x0))
+        self.L.qjo_field_window(C.byref(make_map(rootset)), C.byref(make_grid(grid)), max_it,
+                                escape, x0, x1, y0, y1, z0, z1, _ptr(f), nthreads)
+        return f.reshape(z1 - z0, y1 - y0, x1 - x0)
 
     def nonlinear_value(self, rootset, p, slice_, max_it, escape, iso=0.0):
         p = np.ascontiguousarray(p, dtype=np.float64)

@@ -268,6 +268,28 @@ int64_t qjo_field(const qjo_map* m, const qjo_grid* g, int max_it, double escape
   return terms;
 }
 
+/* qjo_field over the window x in [x0, x1), y in [y0, y1) of slices
+ * [z0, z1): the same cells of the same grid (cell centres of the full grid),
+ * field[((z-z0)*(y1-y0) + (y-y0))*(x1-x0) + (x-x0)]. */
+void qjo_field_window(const qjo_map* m, const qjo_grid* g, int max_it, double escape, int x0,
+                      int x1, int y0, int y1, int z0, int z1, double* field, int nthreads) {
+  const int W = x1 - x0, H = y1 - y0;
+  const int rows = (z1 - z0) * H;
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_num_procs();
+#pragma omp parallel for schedule(dynamic) num_threads(nthreads)
+#endif
+  for (int r = 0; r < rows; r++) {
+    const int z = z0 + r / H, y = y0 + r % H;
+    for (int x = x0; x < x1; x++) {
+      double p[3];
+      int32_t n;
+      qjo_cell_center(g, x, y, z, p);
+      field[(int64_t)r * W + (x - x0)] = escape_value(m, p, g->slice, max_it, escape, NULL, &n);
+    }
+  }
+}
+
 /* TRIANGLE_MESH::lagrangeNonlinearValue, TRIANGLE_MESH.cpp:1684-1747: an
  * overflowing iterate reverts to the previous one and stops; an infinite
  * value returns FLT_MAX.  (The reference leaves the "previous" magnitude

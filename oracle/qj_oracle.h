@@ -72,6 +72,11 @@ int64_t qjo_field(const qjo_map* m, const qjo_grid* g, int max_it, double escape
                   int z0, int z1, double* field, double* de, int32_t* iters,
                   int nthreads);
 
+/* qjo_field restricted to the cells x in [x0, x1), y in [y0, y1) of slices
+ * [z0, z1) of the same grid; field is (z1-z0) x (y1-y0) x (x1-x0). */
+void qjo_field_window(const qjo_map* m, const qjo_grid* g, int max_it, double escape, int x0,
+                      int x1, int y0, int y1, int z0, int z1, double* field, int nthreads);
+
 /* log|q_N| - iso at an arbitrary point (TRIANGLE_MESH::nonlinearValue). */
 double qjo_nonlinear_value(const qjo_map* m, const double p[3], double slice,
                            int max_it, double escape, double iso);

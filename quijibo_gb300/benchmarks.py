@@ -16,6 +16,19 @@ import time
 import numpy as np
 
 
+def hbm_peak_gbs():
+    """(GB/s, source): the measured copy bandwidth of MEASURED_PEAKS.json at
+    the repository root, else the pool's earlier GB300 measurement."""
+    import os
+    path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                        "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback (earlier GB300 copy measurement)"
+
+
 def _events(torch):
     return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
@@ -228,15 +241,25 @@ def bench_serve(args):
     return out
 
 
+def mesh_algorithmic_bytes(n_voxels, n_verts, n_tris):
+    """Algorithmic HBM bytes of the mesher's classify and triangle phases:
+    the FP64 field read once (8 B per voxel) plus the FP32 vertices and
+    int32 triangles written (12 B each)."""
+    return 8 * n_voxels + 12 * n_verts + 12 * n_tris
+
+
 def bench_large(args):
     """The large-grid configuration: 48 top / 24 bottom roots, 60 iterations,
-    a res^3 grid (2200 by default) in 64-slice z-slabs.  (1) The precision
-    field (FP32 bulk, double-float re-run at rel_tol, FP64 band) streamed
-    through the mesher to FP32 vertices and int32 triangles, with the device
-    time of each mesher phase; (2) the field alone over the same slabs, for
-    the FMA-pipe roofline of the bulk kernel; (3) evenly spaced z-slices in
-    both the precision form and the plain FP64 form: sign map, error, and
-    the FP64 form's speed."""
+    a res^3 grid (2200 by default) in 64-slice z-slabs.  (1) ONE pass of the
+    precision field (FP32 bulk, double-float re-run at rel_tol, FP64 band)
+    streamed through the mesher to FP32 vertices and int32 triangles, with
+    the device time of each phase and the FP32 bulk kernel's FMA roofline
+    from the same pass; (2) optionally (args.field_pass) the field alone over
+    the same slabs; (3) evenly spaced z-slices in the precision form, the
+    plain FP64 form (the reference's polar pow per root term) and the FP64
+    form with integer powers as repeated products (the precision form's
+    algebra in FP64): sign map, error, and the speed of each, so the
+    speed-up splits into algorithm (pow -> products) and precision."""
     import torch
 
     from . import lib
@@ -260,94 +283,123 @@ def bench_large(args):
     ctx.field(h, small, it, ws.data_ptr())
     torch.cuda.synchronize()
     del ws
+    peak = lib.fma_probe(0)
+    field_gvox = None
 
-    # (1) streamed field + mesh
+    # (1) one streamed field + mesh pass
     if not args.no_mesh:
         vcap = int(args.vert_cap or 40 * XY)
         tcap = int(args.tri_cap or 80 * XY)
         v32 = torch.empty(3 * vcap, dtype=torch.float32, device="cuda")
         tris = torch.empty(3 * tcap, dtype=torch.int32, device="cuda")
         ctx.set_timing(True)
+        torch.cuda.synchronize()
+        e0, e1 = _events(torch)
         t0 = time.perf_counter()
+        e0.record()
         rc, st = ctx.mesh_stream(h, g, it, check=False, d_verts32=v32.data_ptr(), vert_cap=vcap,
                                  d_tris=tris.data_ptr(), tri_cap=tcap, slab_nz=args.slab)
+        e1.record()
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
         if rc == -5:
             raise SystemExit("raise --vert-cap/--tri-cap: needs %d / %d" % (st["n_verts"], st["n_tris"]))
         V, T = st["n_verts"], st["n_tris"] + st["n_degenerate"]
-        # algorithmic HBM bytes of classify + id + triangle phases: the FP64
-        # field read once, flags / masks / id bases written and read, edge
-        # list entries, triangles
-        cls_bytes = n * (8 + 1 + 1 + 4) + 4 * V
-        tri_bytes = n * 1 + 12 * T
         mesh_ms = st["ms_classify"] + st["ms_triangles"]
-        out["mesh"] = {"triangles": st["n_tris"], "vertices": V, "degenerate": st["n_degenerate"],
-                       "unbracketed": st["n_unbracketed"], "wall_s": wall,
+        alg = mesh_algorithmic_bytes(n, V, T)
+        fs = st["field"]
+        flops = field_flops(rs, fs["voxel_iters"])
+        bulk = st["ms_field_bulk"]
+        field_gvox = n / (st["ms_field"] * 1e-3) / 1e9
+        out["mesh"] = {"passes": 1, "triangles": st["n_tris"], "vertices": V,
+                       "degenerate": st["n_degenerate"], "unbracketed": st["n_unbracketed"],
+                       "wall_s": wall, "device_ms": e0.elapsed_time(e1),
                        "triangles_per_s": st["n_tris"] / wall,
-                       "ms_field": st["ms_field"], "ms_classify": st["ms_classify"],
-                       "ms_vertices": st["ms_vertices"], "ms_triangles": st["ms_triangles"],
-                       "ms_filter": st["ms_filter"],
-                       "classify_emit_gb_s": (cls_bytes + tri_bytes) / (mesh_ms * 1e-3) / 1e9,
+                       "ms_field": st["ms_field"], "ms_field_bulk": bulk,
+                       "ms_classify": st["ms_classify"], "ms_vertices": st["ms_vertices"],
+                       "ms_triangles": st["ms_triangles"], "ms_filter": st["ms_filter"],
+                       "classify_emit_algorithmic_bytes": alg,
+                       "classify_emit_gb_s": alg / (mesh_ms * 1e-3) / 1e9,
+                       "classify_emit_frac_hbm": alg / (mesh_ms * 1e-3) / 1e9 / args.hbm_gbs,
+                       "hbm_peak_gb_s": args.hbm_gbs,
                        "bisection_map_evals_fp64": st["map_evals"],
                        "bisection_map_evals_fp32": st["map_evals_fp32"],
                        "bisection_map_evals_ff": st["map_evals_ff"], "slabs": st["slabs"],
-                       "field": st["field"]}
+                       "field": fs}
+        out["field"] = {"gvox_s": field_gvox, "source": "the streamed pass's field phase "
+                        "(65 slices computed per 64-slice slab: one-plane overlap)",
+                        "gvoxel_iterations_s": fs["voxel_iters"] / (st["ms_field"] * 1e-3) / 1e9,
+                        "roofline": {"bound": "fma", "kernel": "field32x2_kernel",
+                                     "achieved_tflops": flops / (bulk * 1e-3) / 1e12,
+                                     "peak_tflops": peak,
+                                     "frac": flops / (bulk * 1e-3) / 1e12 / peak},
+                        "lane_efficiency": fs["voxel_iters"] / max(1, fs["lane_iters"])}
         del v32, tris
         torch.cuda.empty_cache()
 
     # (2) the field alone, slab by slab
-    ctx.set_timing(True)
-    buf = torch.empty(args.slab * XY, dtype=torch.float64, device="cuda")
-    bulk = rest = 0.0
-    tot = {}
-    for z0 in range(0, g.res[2], args.slab):
-        z1 = min(z0 + args.slab, g.res[2])
-        ctx.field(h, g, it, buf.data_ptr(), z0=z0, z1=z1)
-        b, r = ctx.last_timings()
-        bulk, rest = bulk + b, rest + r
-        for k, v in ctx.stats().items():
-            tot[k] = tot.get(k, 0) + v
-    del buf
-    flops = field_flops(rs, tot["voxel_iters"])
-    peak = lib.fma_probe(0)
-    out["field"] = {"gvox_s": n / ((bulk + rest) * 1e-3) / 1e9, "bulk_ms": bulk, "rest_ms": rest,
-                    "gvoxel_iterations_s": tot["voxel_iters"] / ((bulk + rest) * 1e-3) / 1e9,
-                    "roofline": {"achieved_tflops": flops / (bulk * 1e-3) / 1e12,
-                                 "peak_tflops": peak, "frac": flops / (bulk * 1e-3) / 1e12 / peak},
-                    "stats": tot, "lane_efficiency": tot["voxel_iters"] / max(1, tot["lane_iters"])}
+    if args.field_pass or args.no_mesh:
+        ctx.set_timing(True)
+        buf = torch.empty(args.slab * XY, dtype=torch.float64, device="cuda")
+        bulk = rest = 0.0
+        tot = {}
+        for z0 in range(0, g.res[2], args.slab):
+            z1 = min(z0 + args.slab, g.res[2])
+            ctx.field(h, g, it, buf.data_ptr(), z0=z0, z1=z1)
+            b, r = ctx.last_timings()
+            bulk, rest = bulk + b, rest + r
+            for k, v in ctx.stats().items():
+                tot[k] = tot.get(k, 0) + v
+        del buf
+        flops = field_flops(rs, tot["voxel_iters"])
+        field_gvox = n / ((bulk + rest) * 1e-3) / 1e9
+        out["field_alone"] = {
+            "gvox_s": field_gvox, "bulk_ms": bulk, "rest_ms": rest,
+            "gvoxel_iterations_s": tot["voxel_iters"] / ((bulk + rest) * 1e-3) / 1e9,
+            "roofline": {"achieved_tflops": flops / (bulk * 1e-3) / 1e12, "peak_tflops": peak,
+                         "frac": flops / (bulk * 1e-3) / 1e12 / peak},
+            "stats": tot, "lane_efficiency": tot["voxel_iters"] / max(1, tot["lane_iters"])}
 
-    # (3) sampled slices against the plain FP64 form
-    it64 = ctx.iter_params(p["max_it"], p["escape"], precision=lib.QJG_FP64)
-    zs = [int(v) for v in np.linspace(0, g.res[2] - 1, args.check_slices)]
-    a = torch.empty(XY, dtype=torch.float64, device="cuda")
-    b64 = torch.empty(XY, dtype=torch.float64, device="cuda")
-    ms64 = ms32 = 0.0
-    sign = 0
-    mx = 0.0
-    ss = 0.0
-    for z in zs:
-        e0, e1 = _events(torch)
-        e0.record()
-        ctx.field(h, g, it64, b64.data_ptr(), z0=z, z1=z + 1)
-        e1.record()
-        e1.synchronize()
-        ms64 += e0.elapsed_time(e1)
-        e0.record()
-        ctx.field(h, g, it, a.data_ptr(), z0=z, z1=z + 1)
-        e1.record()
-        e1.synchronize()
-        ms32 += e0.elapsed_time(e1)
-        sign += int(((a > 0) != (b64 > 0)).sum().item())
-        rel = (a - b64).abs() / b64.abs().clamp_min(1e-300)
-        mx = max(mx, float(rel.max().item()))
-        ss += float(rel.pow(2).sum().item())
-    nv = len(zs) * XY
-    fp64_gvox = nv / (ms64 * 1e-3) / 1e9
-    out["fp64_check"] = {"slices": zs, "voxels": nv, "sign_map_disagreements": sign,
-                         "max_rel_err": mx, "rms_rel_err": (ss / nv) ** 0.5,
-                         "fp64_gvox_s": fp64_gvox, "fp64_full_grid_s_est": n / fp64_gvox / 1e9,
-                         "speedup_field_vs_fp64": out["field"]["gvox_s"] / fp64_gvox}
+    # (3) sampled slices: precision form against both FP64 forms
+    if args.check_slices > 0:
+        forms = {"fp64_pow": ctx.iter_params(p["max_it"], p["escape"], precision=lib.QJG_FP64),
+                 "fp64_int": ctx.iter_params(p["max_it"], p["escape"], precision=lib.QJG_FP64,
+                                             refine_pow=lib.QJG_REFINE_INT),
+                 "fp32_refine": it}
+        zs = [int(v) for v in np.linspace(0, g.res[2] - 1, args.check_slices)]
+        buf = {k: torch.empty(XY, dtype=torch.float64, device="cuda") for k in forms}
+        ms = {k: 0.0 for k in forms}
+        acc = {k: dict(sign=0, mx=0.0, ss=0.0) for k in ("fp64_pow", "fp64_int")}
+        for z in zs:
+            for k, itk in forms.items():
+                e0, e1 = _events(torch)
+                e0.record()
+                ctx.field(h, g, itk, buf[k].data_ptr(), z0=z, z1=z + 1)
+                e1.record()
+                e1.synchronize()
+                ms[k] += e0.elapsed_time(e1)
+            a = buf["fp32_refine"]
+            for k in acc:
+                b = buf[k]
+                acc[k]["sign"] += int(((a > 0) != (b > 0)).sum().item())
+                rel = (a - b).abs() / b.abs().clamp_min(1e-300)
+                acc[k]["mx"] = max(acc[k]["mx"], float(rel.max().item()))
+                acc[k]["ss"] += float(rel.pow(2).sum().item())
+        nv = len(zs) * XY
+        gv = {k: nv / (ms[k] * 1e-3) / 1e9 for k in forms}
+        ref_gvox = field_gvox or gv["fp32_refine"]
+        chk = {"slices": zs, "voxels": nv}
+        for k in acc:
+            chk["vs_" + k] = {"sign_map_disagreements": acc[k]["sign"],
+                              "max_rel_err": acc[k]["mx"], "rms_rel_err": (acc[k]["ss"] / nv) ** 0.5}
+        chk.update({"gvox_s": gv,
+                    "fp64_pow_full_grid_s_est": n / gv["fp64_pow"] / 1e9,
+                    "speedup_vs_fp64_pow": ref_gvox / gv["fp64_pow"],
+                    "speedup_vs_fp64_int": ref_gvox / gv["fp64_int"],
+                    "speedup_algorithm_fp64_int_over_pow": gv["fp64_int"] / gv["fp64_pow"]})
+        out["fp64_check"] = chk
+    ctx.free(h)
+    ctx.close()
     return out
 
 
@@ -528,7 +580,11 @@ def main():
     ap.add_argument("--rel-tol", type=float, default=1e-6)
     ap.add_argument("--check-slices", type=int, default=4)
     ap.add_argument("--no-mesh", action="store_true")
+    ap.add_argument("--field-pass", action="store_true", help="large: also time the field alone")
+    ap.add_argument("--hbm-gbs", type=float, default=0.0,
+                    help="HBM roofline denominator (default: MEASURED_PEAKS.json, else 6800)")
     args = ap.parse_args()
+    args.hbm_gbs = args.hbm_gbs or hbm_peak_gbs()[0]
     fn = {"mesh": bench_mesh, "energy": bench_energy, "serve": bench_serve,
           "large": bench_large, "tooth": bench_tooth, "tanh": bench_tanh}[args.what]
     print(json.dumps(fn(args)), flush=True)

@@ -1,15 +1,15 @@
 // Field entry point that allocates no device memory.
 //
 // Some callers of this library cannot allocate device memory on the path
-// that computes a field: code running while a stream is being captured into
-// a CUDA graph (where cudaMalloc is not allowed), plugins hosted by a runtime
-// that owns every device allocation, and real-time loops that must not hit
-// the allocator.  qjg_field_noalloc serves them.  The caller passes the map
+// that computes a field: plugins hosted by an application that owns every
+// device allocation (its own memory pool, no room for a library's
+// cudaMalloc), real-time loops that must not reach the allocator, and
+// processes held to a fixed device-memory quota.  qjg_field_noalloc serves them.  The caller passes the map
 // (host arrays), the grid, the iteration settings and a device output
 // buffer; the only device memory the call touches besides that buffer is a
-// fixed scratch array of this file (the refine list and the counters of the
-// FP32 + FP64-refine form), which lives for as long as the library is loaded
-// on a device.  Every call shares that array, so calls whose work overlaps
+// fixed scratch array of this file (the counters, the FP64 refine list and
+// the double-float re-run list of the FP32 + FP64-refine form, about 32 MiB),
+// which lives for as long as the library is loaded on a device.  Every call shares that array, so calls whose work overlaps
 // on the GPU (different streams, or different host threads) race on it and
 // must be serialised by the caller.
 #include <cuda_runtime.h>
@@ -26,10 +26,13 @@ namespace {
 
 constexpr int kMaxDevices = 64;
 
-// [0, 256): the counters (qj::DevStats, padded); then one uint32 list entry
-// per voxel of the largest launch.
+// [0, 256): the counters (qj::DevStats, padded); then two lists of one
+// uint32 entry per voxel of the largest launch: the FP64 refine list and the
+// double-float re-run list (the same two lists qjg_field fills).
 constexpr size_t kStatsBytes = 256;
-constexpr size_t kScratchBytes = kStatsBytes + sizeof(uint32_t) * (size_t)QJG_NOALLOC_MAX_VOXELS;
+static_assert(sizeof(qj::DevStats) <= kStatsBytes, "the counters overlap the refine list");
+constexpr size_t kListBytes = sizeof(uint32_t) * (size_t)QJG_NOALLOC_MAX_VOXELS;
+constexpr size_t kScratchBytes = kStatsBytes + 2 * kListBytes;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -77,6 +80,7 @@ extern "C" int qjg_field_noalloc(int32_t n_top, const double* top_roots, const d
   if ((rc = scratch_for_current_device(&scratch))) return rc;
   qj::DevStats* st = reinterpret_cast<qj::DevStats*>(scratch);
   uint32_t* list = reinterpret_cast<uint32_t*>(scratch + kStatsBytes);
+  uint32_t* ff_list = reinterpret_cast<uint32_t*>(scratch + kStatsBytes + kListBytes);
 
   cudaStream_t s = (cudaStream_t)stream;
   const qj::GridParams g = qj_grid_params(grid, z0, z1);
@@ -85,11 +89,17 @@ extern "C" int qjg_field_noalloc(int32_t n_top, const double* top_roots, const d
   const bool pow_ref = iter->refine_pow == QJG_REFINE_POW || !m.all_int;
   // the counters (work-queue position, refine-list length) start at zero
   if (cudaMemsetAsync(st, 0, sizeof(qj::DevStats), s) != cudaSuccess) return QJG_ERR_CUDA;
+  // voxels whose tracked FP32 error exceeds rel_tol are re-run with a
+  // double-float head first, as in qjg_field, so both give the same bits
+  const bool rerun = refine && it.est_tol > 0.0 && m.all_int;
   cudaError_t e;
   if (iter->precision == QJG_FP64)
     e = qj::launch_field64(m, g, it, pow_ref, d_field, d_de, st, s);
   else
-    e = qj::launch_field32(m, g, it, refine, d_field, d_de, list, nullptr, nullptr, st, s);
+    e = qj::launch_field32(m, g, it, refine, d_field, d_de, list, nullptr,
+                           rerun ? ff_list : nullptr, st, s);
+  if (e == cudaSuccess && rerun)
+    e = qj::launch_rerun_ff(m, g, it, ff_list, d_field, d_de, list, nullptr, st, s);
   if (e == cudaSuccess && refine)
     e = qj::launch_refine64(m, g, it, pow_ref, list, nullptr, nullptr, nullptr, d_field, d_de, st,
                             s);

@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cstring>
 
+#include "../../include/quijibo_gpu_bench.h"
 #include "qj_ctx.h"
 #include "qj_kernels.h"
 #include "qj_mesh.h"
@@ -128,6 +129,11 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
           return rc;
       }
       if ((rc = qjg_field_stats_read(ctx, s, &fs))) return rc;
+      if (timed) {
+        float ms_bulk = 0.f, ms_rest = 0.f;
+        if ((rc = qjg_last_timings(ctx, &ms_bulk, &ms_rest))) return rc;
+        st.ms_field_bulk += ms_bulk;
+      }
       st.field.voxels += fs.voxels;
       st.field.voxel_iters += fs.voxel_iters;
       st.field.root_terms += fs.root_terms;

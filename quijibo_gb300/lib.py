@@ -68,7 +68,7 @@ class QjgMeshStats(C.Structure):
                 ("map_evals_fp32", C.c_int64), ("map_evals_ff", C.c_int64), ("slabs", C.c_int64),
                 ("field", QjgFieldStats), ("ms_field", C.c_double), ("ms_classify", C.c_double),
                 ("ms_vertices", C.c_double), ("ms_triangles", C.c_double),
-                ("ms_filter", C.c_double)]
+                ("ms_filter", C.c_double), ("ms_field_bulk", C.c_double)]
 
     def as_dict(self):
         d = {k: int(getattr(self, k)) for k, t in self._fields_

@@ -9,10 +9,11 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
+REF = os.environ.get("QUIJIBO_REF", "")
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src")), reason="reference sources absent")
+@pytest.mark.skipif(not REF or not os.path.isdir(os.path.join(REF, "src")),
+                    reason="reference sources absent (QUIJIBO_REF unset)")
 def test_reference_drivers_link_through_adapter():
     from quijibo_gb300 import build
     build.build()
