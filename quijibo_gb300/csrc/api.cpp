@@ -216,7 +216,12 @@ void qjg_destroy(qjg_ctx* ctx) {
   cudaFree(ctx->d_de);
   cudaFree(ctx->d_mstats);
   cudaFree(ctx->m_field);
-  cudaFree(ctx->m_flags);
+  cudaFree(ctx->m_bits);
+  cudaFree(ctx->m_code);
+  cudaFree(ctx->m_ucount);
+  cudaFree(ctx->m_tot);
+  cudaFree(ctx->m_cubes[0]);
+  cudaFree(ctx->m_cubes[1]);
   cudaFree(ctx->m_masks);
   cudaFree(ctx->m_vbase);
   cudaFree(ctx->m_list);

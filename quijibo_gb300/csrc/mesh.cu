@@ -54,29 +54,32 @@ __device__ __forceinline__ int ntri_of(int flag) {
 }
 
 // Exclusive scan across a block of SCAN_T threads; returns the thread's
-// exclusive prefix and writes the block total to *total.
-__device__ __forceinline__ long long block_exclusive_scan(long long v, long long* total) {
-  __shared__ long long warp_sums[SCAN_T / 32];
+// exclusive prefix and writes the block total to *total.  T is long long or
+// unsigned long long (packed counters whose fields never carry into each
+// other).
+template <class T>
+__device__ __forceinline__ T block_exclusive_scan(T v, T* total) {
+  __shared__ T warp_sums[SCAN_T / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  long long inc = v;
+  T inc = v;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    const long long n = __shfl_up_sync(0xffffffffu, inc, o);
+    const T n = __shfl_up_sync(0xffffffffu, inc, o);
     if (lane >= o) inc += n;
   }
   if (lane == 31) warp_sums[warp] = inc;
   __syncthreads();
   if (warp == 0) {
-    long long w = lane < SCAN_T / 32 ? warp_sums[lane] : 0;
+    T w = lane < SCAN_T / 32 ? warp_sums[lane] : 0;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const long long n = __shfl_up_sync(0xffffffffu, w, o);
+      const T n = __shfl_up_sync(0xffffffffu, w, o);
       if (lane >= o) w += n;
     }
     if (lane < SCAN_T / 32) warp_sums[lane] = w;  // inclusive warp prefix
   }
   __syncthreads();
-  const long long warp_base = warp ? warp_sums[warp - 1] : 0;
+  const T warp_base = warp ? warp_sums[warp - 1] : 0;
   *total = warp_sums[SCAN_T / 32 - 1];
   __syncthreads();
   return warp_base + inc - v;
@@ -155,159 +158,390 @@ __global__ void __launch_bounds__(SCAN_T) emit_kernel(Op op, long long n, const 
 
 // ------------------------------------------------------------ classify
 
-// flags[l * XY + y * X + x] for layers l of `src` planes l and l+1.  One
-// thread per (x, y) walks the layers: the four corners of plane l+1 are
-// loaded once and reused as the lower corners of the next layer (4 loads per
-// cube instead of 8, of which the x+1 pair hits L1 behind the neighbouring
-// lane; rows are read coalesced across the warp).
-__device__ __forceinline__ int plane_bits(const double* u, int X) {
-  // corner weights NNN=1 NNP=2 NPN=4 NPP=8 PNN=16 PNP=32 PPN=64 PPP=128
-  // (TRIANGLE_MESH.cpp:4929-4931; letters x, y, z): the z-lower corners
-  return (u[0] > 0) | ((u[X] > 0) << 2) | ((u[1] > 0) << 4) | ((u[1 + X] > 0) << 6);
+// The vertex of an edge: the reference places one on every edge that a
+// triangle of some cube uses.  Every case of its table uses exactly the edges
+// whose endpoint signs differ, except case 158, which leaves out the three
+// edges of its isolated corner (edges 10, 5, 6: the x-, y- and z-edges at the
+// cube's (1, 0, 0) corner).  An interior edge always has another cube that
+// uses it, so the sign changes give the vertex set except on three lines of
+// the grid where the case-158 cube is the edge's only cube: x-edges at
+// (y, z) = (0, 0), y-edges at (x, z) = (X-1, 0), z-edges at (x, y) = (X-1, 0)
+// (mc_fix158_kernel).
+//
+// Classification of one slab (mc_classify_kernel) reads the FP64 field once:
+// a block takes a row segment of MC_SEG voxels and walks the slab's planes,
+// each thread two voxels (one 16-byte load per row and plane), keeping the
+// corner signs of the plane below in registers.  Per voxel it forms the
+// 3-bit edge mask (x, y, z edges from the voxel) and the flag of the cube at
+// the voxel (corner weights NNN=1 NNP=2 NPN=4 NPP=8 PNN=16 PNP=32 PPN=64
+// PPP=128 with letters x, y, z, TRIANGLE_MESH.cpp:4929-4931).  It writes:
+// one bit per voxel (active: an edge with a vertex or a cube with
+// triangles); for active voxels only, a 16-bit code (mask | flag << 3); and
+// per unit (row segment of one plane) the packed counts of vertices,
+// triangles and cubes with triangles.  Units are numbered in scan order
+// (plane, row, segment), so an exclusive scan of their counts gives every
+// voxel's first vertex id and every cube's first triangle in the reference's
+// order (vertices by (z, y, x, axis) of the edge's lower endpoint, triangles
+// by cube).
+constexpr int MC_SEG = 256;                // voxels per unit (one block's row segment)
+constexpr int MC_WORDS = MC_SEG / 32;      // activity words per unit
+constexpr int MC_T = MC_SEG / 2;           // classify threads per block
+static_assert(MC_WORDS == MESH_UNIT_WORDS, "activity words per unit");
+// packed unit counts: vertices (10 bits), triangles (11), cubes (9)
+__device__ __forceinline__ uint32_t unit_pack(int nv, int nt, int nc) {
+  return (uint32_t)nv | (uint32_t)nt << 10 | (uint32_t)nc << 21;
+}
+// widened for sums over a scan block of SCAN_B units: 21 / 22 / 21 bits
+__device__ __forceinline__ unsigned long long unit_widen(uint32_t c) {
+  return (unsigned long long)(c & 1023u) | (unsigned long long)(c >> 10 & 2047u) << 21 |
+         (unsigned long long)(c >> 21) << 43;
+}
+__device__ __forceinline__ long long wide_nv(unsigned long long w) { return (long long)(w & 0x1FFFFFull); }
+__device__ __forceinline__ long long wide_nt(unsigned long long w) { return (long long)(w >> 21 & 0x3FFFFFull); }
+__device__ __forceinline__ long long wide_nc(unsigned long long w) { return (long long)(w >> 43); }
+
+// bit i of v (< 2^16) to bit 2i
+__device__ __forceinline__ uint32_t spread16(uint32_t v) {
+  v = (v | (v << 8)) & 0x00FF00FFu;
+  v = (v | (v << 4)) & 0x0F0F0F0Fu;
+  v = (v | (v << 2)) & 0x33333333u;
+  v = (v | (v << 1)) & 0x55555555u;
+  return v;
 }
 
-__global__ void __launch_bounds__(128) flags_kernel(const double* __restrict__ src, int X, int Y,
-                                                    long long n_layers,
-                                                    uint8_t* __restrict__ flags) {
-  const long long XY = (long long)X * Y;
-  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= XY) return;
-  const int y = (int)(p / X), x = (int)(p - (long long)y * X);
-  if (x >= X - 1 || y >= Y - 1) {
-    for (long long l = 0; l < n_layers; l++) flags[l * XY + p] = 0;
-    return;
+// Signs (> 0) of the values at x0, x0 + 1, x0 + 2 of one row as bits 0..2;
+// values beyond the row read as 0 (their edges and cubes are masked).  x0 + 2
+// is the next lane's x0; lane 31 loads it.  All lanes of the warp call this.
+template <bool VEC>
+__device__ __forceinline__ int row_signs(const double* __restrict__ row, int x0, int X, int lane) {
+  double a = 0.0, b = 0.0;
+  if (VEC) {
+    if (x0 < X) {  // X even: x0 + 1 < X too
+      const double2 v = __ldg(reinterpret_cast<const double2*>(row + x0));
+      a = v.x;
+      b = v.y;
+    }
+  } else {
+    if (x0 < X) a = __ldg(row + x0);
+    if (x0 + 1 < X) b = __ldg(row + x0 + 1);
   }
-  int lo = plane_bits(src + p, X);
-#pragma unroll 4
-  for (long long l = 0; l < n_layers; l++) {
-    const int hi = plane_bits(src + (l + 1) * XY + p, X);
-    flags[l * XY + p] = (uint8_t)(lo | (hi << 1));
-    lo = hi;
-  }
+  const int s = (int)(a > 0.0) | (int)(b > 0.0) << 1;
+  int nxt = __shfl_down_sync(0xffffffffu, s, 1) & 1;
+  if (lane == 31) nxt = x0 + 2 < X && __ldg(row + x0 + 2) > 0.0;
+  return s | nxt << 2;
 }
 
-// Edge masks of window planes [j0, j0 + n/XY): bit a set when the edge from
-// the voxel along axis a carries a vertex.  Flags window layer j-1 and j are
-// the cube layers below and above plane j; layers outside [lay_lo, lay_hi)
-// do not exist.
-struct MaskCount {
-  const uint8_t* flags;
-  uint8_t* masks;
-  int X, Y;
-  int j0, lay_lo, lay_hi;
-  __device__ int flag(int j, int x, int y) const {
-    if (j < lay_lo || j >= lay_hi || x < 0 || y < 0 || x > X - 2 || y > Y - 2) return 0;
-    return flags[((long long)j * Y + y) * X + x];
-  }
-  // item i at window plane j, column x, row y
-  __device__ int count_at(long long i, int j, int x, int y) const {
-    const long long XY = (long long)X * Y;
-    // x-edge: edges 10 (cube x,y,j), 9 (x,y-1,j), 11 (x,y,j-1), 12 (x,y-1,j-1)
-    const bool ex = (QJ_MC_EDGEMASK[flag(j, x, y)] >> 9 & 1) |
-                    (QJ_MC_EDGEMASK[flag(j, x, y - 1)] >> 8 & 1) |
-                    (QJ_MC_EDGEMASK[flag(j - 1, x, y)] >> 10 & 1) |
-                    (QJ_MC_EDGEMASK[flag(j - 1, x, y - 1)] >> 11 & 1);
-    // y-edge: edges 1 (x,y,j), 5 (x-1,y,j), 3 (x,y,j-1), 7 (x-1,y,j-1)
-    const bool ey = (QJ_MC_EDGEMASK[flag(j, x, y)] >> 0 & 1) |
-                    (QJ_MC_EDGEMASK[flag(j, x - 1, y)] >> 4 & 1) |
-                    (QJ_MC_EDGEMASK[flag(j - 1, x, y)] >> 2 & 1) |
-                    (QJ_MC_EDGEMASK[flag(j - 1, x - 1, y)] >> 6 & 1);
-    // z-edge: edges 2 (x,y,j), 6 (x-1,y,j), 4 (x,y-1,j), 8 (x-1,y-1,j)
-    const bool ez = (QJ_MC_EDGEMASK[flag(j, x, y)] >> 1 & 1) |
-                    (QJ_MC_EDGEMASK[flag(j, x - 1, y)] >> 5 & 1) |
-                    (QJ_MC_EDGEMASK[flag(j, x, y - 1)] >> 3 & 1) |
-                    (QJ_MC_EDGEMASK[flag(j, x - 1, y - 1)] >> 7 & 1);
-    const int m = (int)ex | ((int)ey << 1) | ((int)ez << 2);
-    masks[(long long)j0 * XY + i] = (uint8_t)m;
-    return __popc(m);
-  }
+struct McSlab {
+  const double* src;  // field planes gz0 .. gz0 + P - 1 (plane stride XY)
+  int X, Y, S;        // S: units per row
+  int P, Pv;          // planes in src; voxel planes classified (P - 1, or P on the last slab)
+  int gz0;            // global index of src plane 0
+  long long XY;
+  uint32_t* bits;     // [unit][MC_WORDS] activity bits, x ascending
+  uint16_t* code;     // [Pv][XY]: edge mask | cube flag << 3, written for active voxels
+  uint32_t* ucount;   // [unit]: packed counts
 };
 
-// Pass 1 of the vertex-id scan over MaskCount, with the item coordinates
-// advanced along x from one division per thread instead of three per item.
-__global__ void __launch_bounds__(SCAN_T) mask_count_kernel(MaskCount op, long long n,
-                                                            long long* bsum) {
-  const long long base = (long long)blockIdx.x * SCAN_B + (long long)threadIdx.x * SCAN_V;
-  long long c = 0;
-  if (base < n) {
-    const long long XY = (long long)op.X * op.Y;
-    int j = (int)(base / XY);
-    const int r = (int)(base - j * XY);
-    int y = r / op.X, x = r - y * op.X;
-    j += op.j0;
+template <bool VEC>
+__global__ void __launch_bounds__(MC_T) mc_classify_kernel(const McSlab c) {
+  __shared__ uint8_t ntri[256];
+  __shared__ uint32_t part[2][MC_T / 32];
+  for (int f = threadIdx.x; f < 256; f += MC_T) ntri[f] = (uint8_t)ntri_of(f);
+  const int seg = blockIdx.x % c.S;
+  const int y = blockIdx.x / c.S;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int x0 = seg * MC_SEG + 2 * threadIdx.x;
+  const bool hy = y + 1 < c.Y;  // uniform over the block
+  const double* row = c.src + (long long)y * c.X;
+  __syncthreads();
+  int lo0 = row_signs<VEC>(row, x0, c.X, lane);                 // plane p, row y
+  int lo1 = hy ? row_signs<VEC>(row + c.X, x0, c.X, lane) : 0;  // plane p, row y + 1
+  for (int p = 0; p < c.Pv; p++) {
+    const bool hz = p + 1 < c.P;  // plane p + 1 exists (uniform)
+    int hi0 = 0, hi1 = 0;
+    if (hz) {
+      const double* up = row + (long long)(p + 1) * c.XY;
+      hi0 = row_signs<VEC>(up, x0, c.X, lane);
+      hi1 = hy ? row_signs<VEC>(up + c.X, x0, c.X, lane) : 0;
+    }
+    uint32_t cnt = 0;
+    int act = 0;
 #pragma unroll
-    for (int k = 0; k < SCAN_V; k++) {
-      if (base + k < n) c += op.count_at(base + k, j, x, y);
-      if (++x == op.X) {
-        x = 0;
-        if (++y == op.Y) {
-          y = 0;
-          j++;
+    for (int i = 0; i < 2; i++) {
+      const int x = x0 + i;
+      if (x >= c.X) continue;
+      const bool hx = x + 1 < c.X;
+      const int s = lo0 >> i & 1;
+      const int m = (int)(hx & (s != (lo0 >> (i + 1) & 1))) |
+                    (int)(hy & (s != (lo1 >> i & 1))) << 1 |
+                    (int)(hz & (s != (hi0 >> i & 1))) << 2;
+      int f = 0;
+      if (hx && hy && hz)
+        f = (lo0 >> i & 1) | (hi0 >> i & 1) << 1 | (lo1 >> i & 1) << 2 | (hi1 >> i & 1) << 3 |
+            (lo0 >> (i + 1) & 1) << 4 | (hi0 >> (i + 1) & 1) << 5 | (lo1 >> (i + 1) & 1) << 6 |
+            (hi1 >> (i + 1) & 1) << 7;
+      const bool cube = f != 0 && f != 255;
+      if (m || cube) {
+        act |= 1 << i;
+        c.code[(long long)p * c.XY + (long long)y * c.X + x] = (uint16_t)(m | f << 3);
+        cnt += unit_pack(__popc(m), cube ? ntri[f] : 0, cube ? 1 : 0);
+      }
+    }
+    const long long u = ((long long)p * c.Y + y) * c.S + seg;
+    const uint32_t ev = __ballot_sync(0xffffffffu, act & 1);
+    const uint32_t od = __ballot_sync(0xffffffffu, act >> 1 & 1);
+    if (lane == 0) {
+      uint32_t* b = c.bits + u * MC_WORDS + 2 * warp;
+      b[0] = spread16(ev & 0xFFFFu) | spread16(od & 0xFFFFu) << 1;
+      b[1] = spread16(ev >> 16) | spread16(od >> 16) << 1;
+    }
+    cnt = __reduce_add_sync(0xffffffffu, cnt);
+    if (lane == 0) part[p & 1][warp] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint32_t t = 0;
+#pragma unroll
+      for (int w = 0; w < MC_T / 32; w++) t += part[p & 1][w];
+      c.ucount[u] = t;
+    }
+    lo0 = hi0;
+    lo1 = hi1;
+  }
+}
+
+// The edges case 158 leaves without a vertex: candidates k < X-1 are the
+// x-edges at (k, 0, 0), the next Y-1 the y-edges at (X-1, k, 0) (both on
+// the grid's first plane), the next Pv the z-edges at (X-1, 0, p).  An edge
+// loses its vertex when its one cube has flag 158.
+__global__ void mc_fix158_kernel(const McSlab c) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  int x, y, p, cx, bit;
+  if (k < c.X - 1) {
+    x = k, y = 0, p = 0, cx = k, bit = 1;
+  } else if (k < c.X - 1 + c.Y - 1) {
+    x = c.X - 1, y = k - (c.X - 1), p = 0, cx = c.X - 2, bit = 2;
+  } else if (k < c.X - 1 + c.Y - 1 + c.Pv) {
+    x = c.X - 1, y = 0, p = k - (c.X - 1 + c.Y - 1), cx = c.X - 2, bit = 4;
+  } else {
+    return;
+  }
+  if (bit != 4 && c.gz0 != 0) return;  // only the grid's first plane
+  if (p + 1 >= c.P) return;            // no cube above this plane
+  const int cy = bit == 2 ? y : 0;
+  int f = 0;
+#pragma unroll
+  for (int dx = 0; dx < 2; dx++)
+#pragma unroll
+    for (int dy = 0; dy < 2; dy++)
+#pragma unroll
+      for (int dz = 0; dz < 2; dz++)
+        f |= (int)(c.src[(long long)(p + dz) * c.XY + (long long)(cy + dy) * c.X + cx + dx] > 0.0)
+             << (4 * dx + 2 * dy + dz);
+  if (f != 158) return;
+  // the omitted edge changes sign, so the voxel is active and has a code
+  const long long v = (long long)p * c.XY + (long long)y * c.X + x;
+  const int code = c.code[v];
+  if (!(code & bit)) return;
+  c.code[v] = (uint16_t)(code & ~bit);
+  atomicSub(&c.ucount[((long long)p * c.Y + y) * c.S + x / MC_SEG], 1u);
+}
+
+// Per scan block of SCAN_B units: the sums of the three counts.
+__global__ void __launch_bounds__(SCAN_T) mc_unit_sums_kernel(const uint32_t* __restrict__ ucount,
+                                                              long long U, long long* bsum3) {
+  const long long base = (long long)blockIdx.x * SCAN_B + (long long)threadIdx.x * SCAN_V;
+  unsigned long long w = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_V; k++)
+    if (base + k < U) w += unit_widen(ucount[base + k]);
+  unsigned long long total;
+  block_exclusive_scan(w, &total);
+  if (threadIdx.x == 0) {
+    bsum3[3 * blockIdx.x] = wide_nv(total);
+    bsum3[3 * blockIdx.x + 1] = wide_nt(total);
+    bsum3[3 * blockIdx.x + 2] = wide_nc(total);
+  }
+}
+
+// Exclusive scan of the nb block sums (three counts) in place; the totals go
+// to tot->nv, nt, nc.
+__global__ void __launch_bounds__(1024) mc_scan_sums_kernel(long long* bsum3, long long nb,
+                                                            McTotals* tot) {
+  __shared__ long long sh[3][32];
+  __shared__ long long carry[3];
+  if (threadIdx.x < 3) carry[threadIdx.x] = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (long long c0 = 0; c0 < nb; c0 += 1024) {
+    const long long i = c0 + threadIdx.x;
+    long long v[3], inc[3];
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      v[q] = i < nb ? bsum3[3 * i + q] : 0;
+      inc[q] = v[q];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const long long t = __shfl_up_sync(0xffffffffu, inc[q], o);
+        if (lane >= o) inc[q] += t;
+      }
+      if (lane == 31) sh[q][warp] = inc[q];
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        long long w = sh[q][lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const long long t = __shfl_up_sync(0xffffffffu, w, o);
+          if (lane >= o) w += t;
+        }
+        sh[q][lane] = w;
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 3; q++)
+      if (i < nb) bsum3[3 * i + q] = carry[q] + (warp ? sh[q][warp - 1] : 0) + inc[q] - v[q];
+    __syncthreads();
+    if (threadIdx.x < 3) carry[threadIdx.x] += sh[threadIdx.x][31];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    tot->nv = carry[0];
+    tot->nt = carry[1];
+    tot->nc = carry[2];
+  }
+}
+
+// Pass 3: the slab's vertices and cubes in scan order.  Each thread takes
+// SCAN_V consecutive units; for their active voxels it writes the vertex id
+// base and edge mask of the voxel (window plane p + 1), one edge-list entry
+// per vertex (window voxel index * 4 + axis) and one entry per cube with
+// triangles (its cell, global plane, flag and first triangle).
+struct McEmit {
+  McSlab c;
+  const long long* bpre;  // exclusive prefixes of the scan blocks (3 per block)
+  uint8_t* masks;
+  int32_t* vbase;
+  uint32_t* list;         // this slab's vertices, from list[0]
+  McCube* cubes;          // this slab's cube entries, from cubes[0]
+  long long id0;          // global id of the slab's first vertex
+  long long t0;           // global index of the slab's first triangle
+  long long u_split;      // first unit of the slab's last cube layer (-1: none)
+  McTotals* tot;
+};
+
+__global__ void __launch_bounds__(SCAN_T) mc_emit_kernel(const McEmit e, long long U) {
+  __shared__ uint8_t ntri[256];
+  for (int f = threadIdx.x; f < 256; f += SCAN_T) ntri[f] = (uint8_t)ntri_of(f);
+  const McSlab& c = e.c;
+  const long long base = (long long)blockIdx.x * SCAN_B + (long long)threadIdx.x * SCAN_V;
+  uint32_t cnt[SCAN_V];
+  unsigned long long w = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_V; k++) {
+    cnt[k] = base + k < U ? c.ucount[base + k] : 0u;
+    w += unit_widen(cnt[k]);
+  }
+  unsigned long long total;
+  const unsigned long long ex = block_exclusive_scan(w, &total);  // also syncs ntri
+  long long vp = e.bpre[3 * blockIdx.x] + wide_nv(ex);
+  long long tp = e.bpre[3 * blockIdx.x + 1] + wide_nt(ex);
+  long long cp = e.bpre[3 * blockIdx.x + 2] + wide_nc(ex);
+  for (int k = 0; k < SCAN_V; k++) {
+    const long long u = base + k;
+    if (u == e.u_split) e.tot->split = cp;
+    if (!cnt[k]) continue;
+    const int seg = (int)(u % c.S);
+    const long long py = u / c.S;
+    const int y = (int)(py % c.Y);
+    const int p = (int)(py / c.Y);
+    const long long r0 = (long long)y * c.X;
+    for (int wd = 0; wd < MC_WORDS; wd++) {
+      uint32_t word = c.bits[u * MC_WORDS + wd];
+      while (word) {
+        const int b = __ffs(word) - 1;
+        word &= word - 1;
+        const int x = seg * MC_SEG + wd * 32 + b;
+        const int code = c.code[(long long)p * c.XY + r0 + x];
+        const int m = code & 7, f = code >> 3;
+        const long long wv = (long long)(p + 1) * c.XY + r0 + x;
+        if (m) {
+          e.vbase[wv] = (int32_t)(e.id0 + vp);
+          e.masks[wv] = (uint8_t)m;
+#pragma unroll
+          for (int a = 0; a < 3; a++)
+            if (m >> a & 1) e.list[vp++] = (uint32_t)(wv * 4 + a);
+        }
+        if (f != 0 && f != 255) {
+          McCube q;
+          q.r = (uint32_t)(r0 + x);
+          q.gzf = (uint32_t)(c.gz0 + p) | (uint32_t)f << 24;
+          q.tb = e.t0 + tp;
+          e.cubes[cp++] = q;
+          tp += ntri[f];
         }
       }
     }
   }
-  long long total;
-  block_exclusive_scan(c, &total);
-  if (threadIdx.x == 0) bsum[blockIdx.x] = total;
 }
 
-// Vertex ids (global) of window planes [j0, ...) and the list of their edges
-// (window voxel index * 4 + axis) in id order.
-struct VertexEmit {
-  const uint8_t* masks;
-  int32_t* vbase;
-  uint32_t* list;
-  long long list_base;  // global id of list[0]
-  long long XY;
-  int j0;
-  __device__ int count(long long i) const { return __popc(masks[j0 * XY + i]); }
-  __device__ void emit(long long i, long long k) const {
-    const long long w = j0 * XY + i;
-    const int m = masks[w];
-    vbase[w] = (int32_t)k;
-    long long o = k - list_base;
-#pragma unroll
-    for (int a = 0; a < 3; a++)
-      if (m >> a & 1) list[o++] = (uint32_t)(w * 4 + a);
-  }
-};
-
-struct TriCount {
-  const uint8_t* flags;
-  long long XY;
-  int j0;
-  __device__ int count(long long i) const { return ntri_of(flags[j0 * XY + i]); }
-};
-
-struct TriEmit {
-  const uint8_t* flags;
+// Pass 4: the triangles of cube entries [0, n) with n = n_carry + the
+// slab's entries below its last cube layer (all of them on the last slab):
+// vertex id of edge (voxel v, axis a) = vbase[v] + the set mask bits of v
+// below a.  The case table is staged in shared memory (lanes read different
+// cases).
+struct McTris {
+  const McCube* cubes;
+  long long n_carry;
+  int last;
+  const McTotals* tot;
   const uint8_t* masks;
   const int32_t* vbase;
   int32_t* tris;
   long long cap;
   int X;
   long long XY;
-  int j0;
-  __device__ int count(long long i) const { return ntri_of(flags[j0 * XY + i]); }
-  __device__ void emit(long long i, long long k) const {
-    const long long w = j0 * XY + i;
-    const int f = flags[w];
-    const int r = (int)(i % XY);
-    const int x = r % X, y = r / X, j = j0 + (int)(i / XY);
-    for (int t = 0; t < QJ_MC_MAX_TRIS && QJ_MC_CASES[f][3 * t]; t++, k++) {
-      if (k >= cap) continue;
+  int zbase;  // global plane of window plane 0
+};
+
+__global__ void __launch_bounds__(128) mc_tris_kernel(const McTris t, long long n_all) {
+  __shared__ uint8_t cases[256][16];
+  for (int i = threadIdx.x; i < 256 * 16; i += blockDim.x) cases[i >> 4][i & 15] = QJ_MC_CASES[i >> 4][i & 15];
+  __syncthreads();
+  const long long n = t.last ? n_all : t.n_carry + t.tot->split;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const McCube q = t.cubes[i];
+    const int f = (int)(q.gzf >> 24);
+    const int j = (int)(q.gzf & 0xFFFFFFu) - t.zbase;
+    const int y = (int)(q.r / (uint32_t)t.X), x = (int)(q.r - (uint32_t)y * (uint32_t)t.X);
+    long long k = q.tb;
+    for (int tr = 0; tr < QJ_MC_MAX_TRIS && cases[f][3 * tr]; tr++, k++) {
+      if (k >= t.cap) continue;
 #pragma unroll
-      for (int c = 0; c < 3; c++) {
-        const int e = QJ_MC_CASES[f][3 * t + c];
-        const long long v = ((long long)(j + c_edge_off[e][2]) * XY) +
-                            (long long)(y + c_edge_off[e][1]) * X + (x + c_edge_off[e][0]);
-        const int a = c_edge_axis[e];
-        tris[3 * k + c] = vbase[v] + __popc(masks[v] & ((1 << a) - 1));
+      for (int cc = 0; cc < 3; cc++) {
+        const int ed = cases[f][3 * tr + cc];
+        const long long v = (long long)(j + c_edge_off[ed][2]) * t.XY +
+                            (long long)(y + c_edge_off[ed][1]) * t.X + (x + c_edge_off[ed][0]);
+        const int a = c_edge_axis[ed];
+        t.tris[3 * k + cc] = t.vbase[v] + __popc(t.masks[v] & ((1 << a) - 1));
       }
     }
   }
-};
+}
+
+// The entries of the slab's last cube layer move to the front of the other
+// cube list for the next slab: [n_carry + split, n_carry + nc) -> [0, ...).
+__global__ void mc_carry_kernel(const McCube* __restrict__ src, McCube* __restrict__ dst,
+                                long long n_carry, long long nc, const McTotals* tot) {
+  const long long s0 = n_carry + tot->split;
+  const long long n = n_carry + nc - s0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    dst[i] = src[s0 + i];
+}
 
 // Degenerate-triangle filter of TRIANGLE_MESH.cpp:737-756 (edge < 1e-7).
 __device__ __forceinline__ double edge_len(const double* a, const double* b) {
@@ -793,37 +1027,93 @@ size_t mesh_edge_state_bytes() { return sizeof(EdgeState); }
 
 long long mesh_scan_blocks(long long n) { return (n + SCAN_B - 1) / SCAN_B + 1; }
 
-cudaError_t mesh_flags(const double* src, int X, int Y, long long n_layers, uint8_t* flags,
-                       cudaStream_t s) {
-  if (n_layers <= 0) return cudaSuccess;
-  const long long n = n_layers * X * Y;
-  (void)n;
-  const long long XY = (long long)X * Y;
-  flags_kernel<<<(unsigned)((XY + 127) / 128), 128, 0, s>>>(src, X, Y, n_layers, flags);
+long long mesh_units(int X, int Y, int planes) {
+  return (long long)planes * Y * ((X + MC_SEG - 1) / MC_SEG);
+}
+
+cudaError_t mesh_classify(const MeshWindow& w, const double* src, int P, int Pv, int gz0,
+                          cudaStream_t s) {
+  McSlab c;
+  c.src = src;
+  c.X = w.X;
+  c.Y = w.Y;
+  c.S = (w.X + MC_SEG - 1) / MC_SEG;
+  c.P = P;
+  c.Pv = Pv;
+  c.gz0 = gz0;
+  c.XY = (long long)w.X * w.Y;
+  c.bits = w.bits;
+  c.code = w.code;
+  c.ucount = w.ucount;
+  const unsigned blocks = (unsigned)((long long)c.S * c.Y);
+  const bool vec = (w.X % 2 == 0) && ((reinterpret_cast<uintptr_t>(src) & 15u) == 0);
+  if (vec)
+    mc_classify_kernel<true><<<blocks, MC_T, 0, s>>>(c);
+  else
+    mc_classify_kernel<false><<<blocks, MC_T, 0, s>>>(c);
+  const int nfix = w.X - 1 + w.Y - 1 + Pv;
+  mc_fix158_kernel<<<(nfix + 127) / 128, 128, 0, s>>>(c);
+  const long long U = mesh_units(w.X, w.Y, Pv);
+  const long long nb = (U + SCAN_B - 1) / SCAN_B;
+  mc_unit_sums_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(w.ucount, U, w.bsum);
+  mc_scan_sums_kernel<<<1, 1024, 0, s>>>(w.bsum, nb, w.tot);
   return cudaGetLastError();
 }
 
-cudaError_t mesh_vertex_ids(MeshWindow& w, int j0, int j1, int lay_lo, int lay_hi,
-                            long long running, long long* n_new, cudaStream_t s,
-                            const std::function<cudaError_t(long long)>& ensure_list) {
-  const long long XY = (long long)w.X * w.Y;
-  const long long n = (long long)(j1 - j0) * XY;
-  MaskCount mc{w.flags, w.masks, w.X, w.Y, j0, lay_lo, lay_hi};
-  // the emit pass needs the list buffer, which ensure_list sizes first
-  cudaError_t err = cudaSuccess;
-  const long long nb = (n + SCAN_B - 1) / SCAN_B;
-  if (n == 0) {
-    *n_new = 0;
-    return cudaSuccess;
+cudaError_t mesh_emit(const MeshWindow& w, const double* src, int P, int Pv, int gz0,
+                      long long u_split, long long id0, long long t0, McCube* cubes,
+                      cudaStream_t s) {
+  McEmit e;
+  e.c.src = src;
+  e.c.X = w.X;
+  e.c.Y = w.Y;
+  e.c.S = (w.X + MC_SEG - 1) / MC_SEG;
+  e.c.P = P;
+  e.c.Pv = Pv;
+  e.c.gz0 = gz0;
+  e.c.XY = (long long)w.X * w.Y;
+  e.c.bits = w.bits;
+  e.c.code = w.code;
+  e.c.ucount = w.ucount;
+  e.bpre = w.bsum;
+  e.masks = w.masks;
+  e.vbase = w.vbase;
+  e.list = w.list;
+  e.cubes = cubes;
+  e.id0 = id0;
+  e.t0 = t0;
+  e.u_split = u_split;
+  e.tot = w.tot;
+  const long long U = mesh_units(w.X, w.Y, Pv);
+  const long long nb = (U + SCAN_B - 1) / SCAN_B;
+  mc_emit_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(e, U);
+  return cudaGetLastError();
+}
+
+cudaError_t mesh_triangles(const MeshWindow& w, const McCube* cubes, long long n_carry,
+                           long long nc, bool last, int zbase, McCube* next, int32_t* tris,
+                           long long cap, cudaStream_t s) {
+  const long long n_all = n_carry + nc;
+  if (n_all > 0) {
+    McTris t;
+    t.cubes = cubes;
+    t.n_carry = n_carry;
+    t.last = last ? 1 : 0;
+    t.tot = w.tot;
+    t.masks = w.masks;
+    t.vbase = w.vbase;
+    t.tris = tris;
+    t.cap = cap;
+    t.X = w.X;
+    t.XY = (long long)w.X * w.Y;
+    t.zbase = zbase;
+    const int blocks = (int)std::min<long long>((n_all + 127) / 128, (long long)sm_count() * 16);
+    mc_tris_kernel<<<blocks, 128, 0, s>>>(t, n_all);
   }
-  mask_count_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(mc, n, w.bsum);
-  scan_bsum_kernel<<<1, 1024, 0, s>>>(w.bsum, nb);
-  if ((err = cudaMemcpyAsync(n_new, w.bsum + nb, sizeof(long long), cudaMemcpyDeviceToHost, s)))
-    return err;
-  if ((err = cudaStreamSynchronize(s))) return err;
-  if ((err = ensure_list(*n_new))) return err;
-  VertexEmit ve{w.masks, w.vbase, w.list, running, XY, j0};
-  emit_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(ve, n, w.bsum, running);
+  if (!last && nc > 0) {
+    const int blocks = (int)std::min<long long>((nc + 255) / 256, (long long)sm_count() * 8);
+    mc_carry_kernel<<<blocks, 256, 0, s>>>(cubes, next, n_carry, nc, w.tot);
+  }
   return cudaGetLastError();
 }
 
@@ -897,27 +1187,6 @@ cudaError_t mesh_vertices(const MapParams& m, const GridParams& g, const IterPar
     hybrid ? QJ_VK(true, false, true) : QJ_VK(true, false, false);
 #undef QJ_VK
   return cudaGetLastError();
-}
-
-cudaError_t mesh_triangles(MeshWindow& w, int j0, int j1, long long running, int32_t* tris,
-                           long long cap, long long* n_new, cudaStream_t s) {
-  const long long XY = (long long)w.X * w.Y;
-  const long long n = (long long)(j1 - j0) * XY;
-  if (n <= 0) {
-    *n_new = 0;
-    return cudaSuccess;
-  }
-  const long long nb = (n + SCAN_B - 1) / SCAN_B;
-  TriCount tc{w.flags, XY, j0};
-  count_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(tc, n, w.bsum);
-  scan_bsum_kernel<<<1, 1024, 0, s>>>(w.bsum, nb);
-  cudaError_t err;
-  if ((err = cudaMemcpyAsync(n_new, w.bsum + nb, sizeof(long long), cudaMemcpyDeviceToHost, s)))
-    return err;
-  TriEmit te{w.flags, w.masks, w.vbase, tris, cap, w.X, XY, j0};
-  emit_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(te, n, w.bsum, running);
-  if ((err = cudaGetLastError())) return err;
-  return cudaStreamSynchronize(s);
 }
 
 cudaError_t mesh_filter(const int32_t* tris, long long n, const double* verts, int32_t* out,

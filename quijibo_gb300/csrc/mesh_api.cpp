@@ -68,17 +68,24 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
   nz = std::max(1, std::min(nz, std::max(Z - 1, 1)));
   QJ_CUDA(ctx, cudaSetDevice(ctx->device));
 
+  // without a cube (a grid one cell thin) there is no triangle and no vertex
+  if (X < 2 || Y < 2) {
+    if (out) *out = st;
+    return QJG_OK;
+  }
   const size_t wplanes = (size_t)(nz + 2) * XY;
-  if ((rc = ensure(ctx, &ctx->m_flags, &ctx->m_flags_cap, wplanes)) ||
-      (rc = ensure(ctx, &ctx->m_masks, &ctx->m_masks_cap, wplanes)) ||
+  const long long units = qj::mesh_units(X, Y, nz + 1);
+  if ((rc = ensure(ctx, &ctx->m_masks, &ctx->m_masks_cap, wplanes)) ||
       (rc = ensure(ctx, &ctx->m_vbase, &ctx->m_vbase_cap, wplanes)) ||
-      (rc = ensure(ctx, &ctx->m_bsum, &ctx->m_bsum_cap, (size_t)qj::mesh_scan_blocks(wplanes))))
+      (rc = ensure(ctx, &ctx->m_code, &ctx->m_code_cap, (size_t)(nz + 1) * XY)) ||
+      (rc = ensure(ctx, &ctx->m_bits, &ctx->m_bits_cap, (size_t)units * qj::MESH_UNIT_WORDS)) ||
+      (rc = ensure(ctx, &ctx->m_ucount, &ctx->m_ucount_cap, (size_t)units)) ||
+      (rc = ensure(ctx, &ctx->m_tot, &ctx->m_tot_cap, (size_t)1)) ||
+      (rc = ensure(ctx, &ctx->m_bsum, &ctx->m_bsum_cap,
+                   (size_t)std::max(3 * qj::mesh_scan_blocks(units), (long long)1))))
     return rc;
   if (streaming && (rc = ensure(ctx, &ctx->m_field, &ctx->m_field_cap, (size_t)(nz + 1) * XY)))
     return rc;
-  QJ_CUDA(ctx, cudaMemsetAsync(ctx->m_flags, 0, XY, s));
-  QJ_CUDA(ctx, cudaMemsetAsync(ctx->m_masks, 0, XY, s));
-  QJ_CUDA(ctx, cudaMemsetAsync(ctx->m_vbase, 0, XY * sizeof(int32_t), s));
   QJ_CUDA(ctx, cudaMemsetAsync(ctx->d_mstats, 0, sizeof(qj::DevStats), s));
   if ((rc = ensure(ctx, &ctx->m_ecount, &ctx->m_ecount_cap, (size_t)3))) return rc;
   QJ_CUDA(ctx, cudaMemsetAsync(ctx->m_ecount, 0, 3 * sizeof(unsigned long long), s));
@@ -86,17 +93,23 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
   qj::MeshWindow w;
   w.X = X;
   w.Y = Y;
-  w.flags = ctx->m_flags;
   w.masks = ctx->m_masks;
   w.vbase = ctx->m_vbase;
   w.list = ctx->m_list;
   w.bsum = ctx->m_bsum;
+  w.bits = ctx->m_bits;
+  w.code = ctx->m_code;
+  w.ucount = ctx->m_ucount;
+  w.tot = ctx->m_tot;
   const GridParams g = qj_grid_params(grid, 0, Z);
   IterParams it{};
   if (iter) it = qj_iter_params(iter, grid);
   const bool pow_ref = !iter || iter->refine_pow == QJG_REFINE_POW || !m->all_int;
+  const long long S = (X + 255) / 256;  // units per row (qj::mesh_units)
 
   long long nv = 0, nt = 0;
+  long long n_carry = 0, prev_nc = 0;  // cube entries carried into the slab; the last slab's count
+  int cur = 0;                         // cube list of this slab (the other takes the carry)
   int prevL = 0;
   // phase timing (qjg_set_timing): events mev[0..4] bracket the phases of a slab
   const bool timed = ctx->timing;
@@ -147,36 +160,43 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
     } else {
       src = d_field + (size_t)c0 * XY;
     }
-    // carry layer/plane c0-1 into window index 0
+    // carry the vertex ids and masks of plane c0-1 into window plane 0
     if (c0 > 0) {
-      QJ_CUDA(ctx, cudaMemcpyAsync(ctx->m_flags, ctx->m_flags + (size_t)prevL * XY, XY,
-                                   cudaMemcpyDeviceToDevice, s));
       QJ_CUDA(ctx, cudaMemcpyAsync(ctx->m_masks, ctx->m_masks + (size_t)prevL * XY, XY,
                                    cudaMemcpyDeviceToDevice, s));
       QJ_CUDA(ctx, cudaMemcpyAsync(ctx->m_vbase, ctx->m_vbase + (size_t)prevL * XY,
                                    XY * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
     }
-    // classify cube layers [c0, c1) into window layers 1..L
+    // classify voxel planes [c0, c1) (+ Z-1 on the last slab) from field planes [c0, c1]
     QJ_CUDA(ctx, mark(1));
-    QJ_CUDA(ctx, qj::mesh_flags(src, X, Y, L, ctx->m_flags + XY, s));
-    ctx->launches++;
-    // vertex ids of planes [c0, c1) (+ Z-1 on the last slab) = window planes [1, j1)
-    const int j1 = L + 1 + (last ? 1 : 0);
-    long long n_new = 0;
-    auto ensure_list = [&](long long n) -> cudaError_t {
-      // grows by half again at least: the per-slab vertex count rises with the surface
-      const size_t want = (size_t)std::max<long long>(n, 1);
-      if (ensure(ctx, &ctx->m_list, &ctx->m_list_cap,
-                 want > ctx->m_list_cap ? std::max(want, ctx->m_list_cap + ctx->m_list_cap / 2)
-                                        : want))
-        return cudaErrorMemoryAllocation;
-      w.list = ctx->m_list;
-      return cudaSuccess;
-    };
-    QJ_CUDA(ctx, qj::mesh_vertex_ids(w, 1, j1, c0 == 0 ? 1 : 0, L + 1, nv, &n_new, s, ensure_list));
-    ctx->launches += 3;
+    const int P = L + 1, Pv = L + (last ? 1 : 0);
+    QJ_CUDA(ctx, qj::mesh_classify(w, src, P, Pv, c0, s));
+    ctx->launches += 4;
+    qj::McTotals tot;
+    QJ_CUDA(ctx, cudaMemcpyAsync(&tot, ctx->m_tot, sizeof tot, cudaMemcpyDeviceToHost, s));
+    QJ_CUDA(ctx, cudaStreamSynchronize(s));
+    // the previous slab's last cube layer (its split is still in tot)
+    n_carry = c0 > 0 ? prev_nc - tot.split : 0;
+    const long long n_new = tot.nv, nc = tot.nc;
     if (nv + n_new > INT32_MAX)
       return fail(ctx, QJG_ERR_CAPACITY, "more than 2^31 vertices; int32 indices cannot hold them");
+    // the edge list grows by half again at least: the per-slab vertex count rises with the surface
+    {
+      const size_t want = (size_t)std::max<long long>(n_new, 1);
+      if ((rc = ensure(ctx, &ctx->m_list, &ctx->m_list_cap,
+                       want > ctx->m_list_cap ? std::max(want, ctx->m_list_cap + ctx->m_list_cap / 2)
+                                              : want)))
+        return rc;
+      w.list = ctx->m_list;
+    }
+    if ((rc = grow_keep(ctx, &ctx->m_cubes[cur], &ctx->m_cubes_cap[cur],
+                        (size_t)std::max<long long>(n_carry + nc, 1), (size_t)n_carry, s)) ||
+        (rc = grow_keep(ctx, &ctx->m_cubes[cur ^ 1], &ctx->m_cubes_cap[cur ^ 1],
+                        (size_t)std::max<long long>(nc, 1), 0, s)))
+      return rc;
+    const long long u_split = last ? -1 : (long long)(L - 1) * Y * S;
+    QJ_CUDA(ctx, qj::mesh_emit(w, src, P, Pv, c0, u_split, nv, nt, ctx->m_cubes[cur] + n_carry, s));
+    ctx->launches++;
     // per-vertex buffers grow to the vertex count extrapolated from the layers
     // meshed so far (+25%; at most 4x the count so far, and no more than the
     // caller's vertex capacity), so that a large mesh reallocates (cudaMalloc,
@@ -210,18 +230,20 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
     if (n_new) ctx->launches++;
     nv += n_new;
     QJ_CUDA(ctx, mark(3));
-    // triangles of layers [c0-1, c1-1) (+ c1-1 on the last slab)
-    const int jt0 = c0 == 0 ? 1 : 0, jt1 = last ? L + 1 : L;
-    long long t_new = 0;
-    QJ_CUDA(ctx, qj::mesh_triangles(w, jt0, jt1, nt, tris, tcap, &t_new, s));
-    ctx->launches += 3;
+    // triangles of cube layers [c0-1, c1-1) (+ c1-1 on the last slab); the
+    // entries of layer c1-1 move to the other list for the next slab
+    QJ_CUDA(ctx, qj::mesh_triangles(w, ctx->m_cubes[cur], n_carry, nc, last, c0 - 1,
+                                    ctx->m_cubes[cur ^ 1], tris, tcap, s));
+    ctx->launches += 2;
     QJ_CUDA(ctx, mark(4));
     QJ_CUDA(ctx, span(0, 1, &st.ms_field));
     QJ_CUDA(ctx, span(1, 2, &st.ms_classify));
     QJ_CUDA(ctx, span(2, 3, &st.ms_vertices));
     QJ_CUDA(ctx, span(3, 4, &st.ms_triangles));
-    nt += t_new;
+    nt += tot.nt;
+    prev_nc = nc;
     prevL = L;
+    cur ^= 1;
     st.slabs++;
     c0 = c1;
   }

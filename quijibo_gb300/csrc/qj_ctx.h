@@ -49,8 +49,16 @@ struct qjg_ctx {
   qj::DevStats* d_mstats = nullptr;
   double* m_field = nullptr;    // slab field window
   size_t m_field_cap = 0;
-  uint8_t* m_flags = nullptr;
-  size_t m_flags_cap = 0;
+  uint32_t* m_bits = nullptr;   // activity bits of the classified planes
+  size_t m_bits_cap = 0;
+  uint16_t* m_code = nullptr;   // sparse voxel codes of the classified planes
+  size_t m_code_cap = 0;
+  uint32_t* m_ucount = nullptr; // unit counts
+  size_t m_ucount_cap = 0;
+  qj::McTotals* m_tot = nullptr;
+  size_t m_tot_cap = 0;
+  qj::McCube* m_cubes[2] = {nullptr, nullptr};  // cube lists of alternate slabs
+  size_t m_cubes_cap[2] = {0, 0};
   uint8_t* m_masks = nullptr;
   size_t m_masks_cap = 0;
   int32_t* m_vbase = nullptr;

@@ -9,24 +9,59 @@
 
 namespace qj {
 
-// Scratch of one z-slab: cube flags per window layer, edge masks and vertex
-// ids per window plane, the edge list of the slab's vertices, scan blocks.
+// A cube with triangles, in scan order: its cell (y * X + x), its global
+// plane with the case flag in the top byte, and the global index of its
+// first triangle.
+struct McCube {
+  uint32_t r;
+  uint32_t gzf;
+  long long tb;
+};
+
+// Device-side counts of one slab's classification.
+struct McTotals {
+  long long nv, nt, nc;  // vertices, triangles, cubes with triangles of the slab
+  long long split;       // the slab's cube entries below its last cube layer
+};
+
+// Scratch of one z-slab.  Window planes j <-> global plane c0 - 1 + j: edge
+// masks and vertex ids per window plane (plane c0 - 1 carried over from the
+// previous slab); per classified plane the activity bits, sparse voxel codes
+// and unit counts; the edge list of the slab's vertices; scan blocks.
 struct MeshWindow {
   int X = 0, Y = 0;
-  uint8_t* flags = nullptr;
   uint8_t* masks = nullptr;
   int32_t* vbase = nullptr;
   uint32_t* list = nullptr;
-  long long* bsum = nullptr;
+  long long* bsum = nullptr;  // 3 per scan block
+  uint32_t* bits = nullptr;
+  uint16_t* code = nullptr;
+  uint32_t* ucount = nullptr;
+  McTotals* tot = nullptr;
 };
 
 long long mesh_scan_blocks(long long n);
+// classification units (row segments of one plane) of `planes` planes
+long long mesh_units(int X, int Y, int planes);
+// Words of activity bits per unit.
+constexpr int MESH_UNIT_WORDS = 8;
 
-cudaError_t mesh_flags(const double* src, int X, int Y, long long n_layers, uint8_t* flags,
-                       cudaStream_t s);
-cudaError_t mesh_vertex_ids(MeshWindow& w, int j0, int j1, int lay_lo, int lay_hi,
-                            long long running, long long* n_new, cudaStream_t s,
-                            const std::function<cudaError_t(long long)>& ensure_list);
+// Classify voxel planes [0, Pv) of src (P planes, global plane gz0 first;
+// Pv = P - 1, or P on the grid's last plane): codes, bits and unit counts,
+// their scan, the slab totals in w.tot (nv, nt, nc).
+cudaError_t mesh_classify(const MeshWindow& w, const double* src, int P, int Pv, int gz0,
+                          cudaStream_t s);
+// The slab's vertex ids, masks and edge list (window planes 1..Pv) and its
+// cube entries (written from `cubes`); u_split = the first unit of the last
+// cube layer (-1 on the last slab), whose entry offset goes to w.tot->split.
+cudaError_t mesh_emit(const MeshWindow& w, const double* src, int P, int Pv, int gz0,
+                      long long u_split, long long id0, long long t0, McCube* cubes,
+                      cudaStream_t s);
+// Triangles of cube entries [0, n_carry + split) (all on the last slab);
+// unless last, the remaining entries move to the front of `next`.
+cudaError_t mesh_triangles(const MeshWindow& w, const McCube* cubes, long long n_carry,
+                           long long nc, bool last, int zbase, McCube* next, int32_t* tris,
+                           long long cap, cudaStream_t s);
 // Scratch of the FP32-first bisection with parked FP64 evaluations: one
 // edge state per vertex of the mesh (mesh_edge_state_bytes() each, indexed
 // by global vertex id), two parking lists of global vertex ids (list 0
@@ -49,8 +84,6 @@ cudaError_t mesh_vertices(const MapParams& m, const GridParams& g, const IterPar
 cudaError_t mesh_parked_finish(const MapParams& m, const GridParams& g, const IterParams& it,
                                bool pow_ref, double* verts, double iso, DevStats* st,
                                const EdgeScratch& sc, cudaStream_t s);
-cudaError_t mesh_triangles(MeshWindow& w, int j0, int j1, long long running, int32_t* tris,
-                           long long cap, long long* n_new, cudaStream_t s);
 cudaError_t mesh_filter(const int32_t* tris, long long n, const double* verts, int32_t* out,
                         long long* bsum, long long* n_keep, cudaStream_t s);
 cudaError_t mesh_to_float(const double* a, float* b, long long n, cudaStream_t s);
