@@ -5,6 +5,7 @@ which measures the headline field).  Each prints one JSON object.
     python -m quijibo_gb300.benchmarks energy [--samples 200000] [--steps 50]
     python -m quijibo_gb300.benchmarks serve  [--requests 400] [--scale 0.25]
     python -m quijibo_gb300.benchmarks large  [--res 2200] [--slab 64] [--check-slices 4]
+    python -m quijibo_gb300.benchmarks classify [--res 2200] [--slab 64] [--reps 5]
 
 All inputs are synthetic (quijibo_gb300/rootsets.py, samples.py).
 """
@@ -82,6 +83,58 @@ def bench_mesh(args):
             "degenerate": st["n_degenerate"], "slabs": st["slabs"],
             "refined": st["field"]["refined"],
             "lane_efficiency": st["field"]["voxel_iters"] / max(1, st["field"]["lane_iters"])}
+
+
+def bench_classify(args):
+    """The mesher's classification alone on one stored slab of the large
+    workload: the precision field of 65 planes of the 2200^3 grid (48/24
+    roots, 60 iterations) computed once, then meshed repeatedly as a stored
+    field with linear edge vertices, so the classify and triangle phases are
+    timed without the field and the bisection.  Algorithmic bytes: the FP64
+    field read once (8 B per voxel), 12 B per vertex and per triangle."""
+    import torch
+
+    from . import lib
+    from .rootsets import Grid, large_workload
+    ctx = lib.Context(0)
+    res = args.res or 2200
+    rs, g, p = large_workload(res)
+    h = ctx.upload(rs)
+    planes = args.slab + 1
+    z0 = args.z0 if args.z0 >= 0 else res // 2
+    XY = g.res[0] * g.res[1]
+    f = torch.empty(planes * XY, dtype=torch.float64, device="cuda")
+    it = ctx.iter_params(p["max_it"], p["escape"], precision=lib.QJG_FP32_REFINE,
+                         refine_pow=lib.QJG_REFINE_INT, rel_tol=args.rel_tol)
+    ctx.field(h, g, it, f.data_ptr(), z0=z0, z1=z0 + planes)
+    torch.cuda.synchronize()
+    slab = Grid((g.res[0], g.res[1], planes), lengths=(g.lengths[0], g.lengths[1],
+                                                      g.lengths[2] * planes / res))
+    vcap, tcap = 8 * XY, 16 * XY
+    v32 = torch.empty(3 * vcap, dtype=torch.float32, device="cuda")
+    tris = torch.empty(3 * tcap, dtype=torch.int32, device="cuda")
+    ctx.set_timing(True)
+    runs = []
+    for k in range(args.reps + 1):
+        _, st = ctx.mesh_field(None, slab, None, f.data_ptr(), lib.QJG_EDGE_LINEAR,
+                               d_verts32=v32.data_ptr(), vert_cap=vcap, d_tris=tris.data_ptr(),
+                               tri_cap=tcap, slab_nz=args.slab)
+        if k:
+            runs.append(st)
+    n = slab.n_voxels
+    cls = statistics.median(r["ms_classify"] for r in runs)
+    tri = statistics.median(r["ms_triangles"] for r in runs)
+    st = runs[-1]
+    alg = mesh_algorithmic_bytes(n, st["n_verts"], st["n_tris"] + st["n_degenerate"])
+    out = {"workload": "large workload, planes [%d, %d) of the %d^3 grid as one stored slab"
+                       % (z0, z0 + planes, res),
+           "voxels": n, "vertices": st["n_verts"], "triangles": st["n_tris"],
+           "ms_classify": cls, "ms_triangles": tri, "ms_vertices": st["ms_vertices"],
+           "algorithmic_bytes": alg, "gb_s": alg / ((cls + tri) * 1e-3) / 1e9,
+           "frac_hbm": alg / ((cls + tri) * 1e-3) / 1e9 / args.hbm_gbs, "hbm_peak_gb_s": args.hbm_gbs}
+    ctx.free(h)
+    ctx.close()
+    return out
 
 
 def bench_energy(args):
@@ -561,7 +614,8 @@ def bench_tanh(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["mesh", "energy", "serve", "large", "tooth", "tanh"])
+    ap.add_argument("what", choices=["mesh", "energy", "serve", "large", "tooth", "tanh",
+                                     "classify"])
     ap.add_argument("--res", type=int, default=0, help="grid edge (mesh: 512, large: 2200)")
     ap.add_argument("--workload", default="precision", choices=["precision", "large"])
     ap.add_argument("--slab", type=int, default=64)
@@ -581,12 +635,15 @@ def main():
     ap.add_argument("--check-slices", type=int, default=4)
     ap.add_argument("--no-mesh", action="store_true")
     ap.add_argument("--field-pass", action="store_true", help="large: also time the field alone")
+    ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--z0", type=int, default=-1, help="classify: first plane of the slab")
     ap.add_argument("--hbm-gbs", type=float, default=0.0,
                     help="HBM roofline denominator (default: MEASURED_PEAKS.json, else 6800)")
     args = ap.parse_args()
     args.hbm_gbs = args.hbm_gbs or hbm_peak_gbs()[0]
     fn = {"mesh": bench_mesh, "energy": bench_energy, "serve": bench_serve,
-          "large": bench_large, "tooth": bench_tooth, "tanh": bench_tanh}[args.what]
+          "large": bench_large, "tooth": bench_tooth, "tanh": bench_tanh,
+          "classify": bench_classify}[args.what]
     print(json.dumps(fn(args)), flush=True)
 
 

@@ -217,7 +217,7 @@ void qjg_destroy(qjg_ctx* ctx) {
   cudaFree(ctx->d_mstats);
   cudaFree(ctx->m_field);
   cudaFree(ctx->m_bits);
-  cudaFree(ctx->m_code);
+  cudaFree(ctx->m_sign);
   cudaFree(ctx->m_ucount);
   cudaFree(ctx->m_tot);
   cudaFree(ctx->m_cubes[0]);

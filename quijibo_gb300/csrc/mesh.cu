@@ -168,37 +168,43 @@ __global__ void __launch_bounds__(SCAN_T) emit_kernel(Op op, long long n, const 
 // (y, z) = (0, 0), y-edges at (x, z) = (X-1, 0), z-edges at (x, y) = (X-1, 0)
 // (mc_fix158_kernel).
 //
-// Classification of one slab (mc_classify_kernel) reads the FP64 field once:
-// a block takes a row segment of MC_SEG voxels and walks the slab's planes,
-// each thread two voxels (one 16-byte load per row and plane), keeping the
-// corner signs of the plane below in registers.  Per voxel it forms the
-// 3-bit edge mask (x, y, z edges from the voxel) and the flag of the cube at
-// the voxel (corner weights NNN=1 NNP=2 NPN=4 NPP=8 PNN=16 PNP=32 PPN=64
-// PPP=128 with letters x, y, z, TRIANGLE_MESH.cpp:4929-4931).  It writes:
-// one bit per voxel (active: an edge with a vertex or a cube with
-// triangles); for active voxels only, a 16-bit code (mask | flag << 3); and
-// per unit (row segment of one plane) the packed counts of vertices,
-// triangles and cubes with triangles.  Units are numbered in scan order
-// (plane, row, segment), so an exclusive scan of their counts gives every
-// voxel's first vertex id and every cube's first triangle in the reference's
-// order (vertices by (z, y, x, axis) of the edge's lower endpoint, triangles
-// by cube).
-constexpr int MC_SEG = 256;                // voxels per unit (one block's row segment)
-constexpr int MC_WORDS = MC_SEG / 32;      // activity words per unit
-constexpr int MC_T = MC_SEG / 2;           // classify threads per block
-static_assert(MC_WORDS == MESH_UNIT_WORDS, "activity words per unit");
-// packed unit counts: vertices (10 bits), triangles (11), cubes (9)
-__device__ __forceinline__ uint32_t unit_pack(int nv, int nt, int nc) {
-  return (uint32_t)nv | (uint32_t)nt << 10 | (uint32_t)nc << 21;
+// Classification of one slab reads the FP64 field once and works on sign
+// bits only.  A warp takes a row segment of MC_SEG = 64 voxels of MC_ROWS
+// rows and walks the slab's planes; per plane it loads MC_ROWS + 1 rows
+// (one 16-byte load per lane and row: x = xb + 2 lane and xb + 2 lane + 1)
+// and turns each into two 32-bit sign words with __ballot_sync, E (even x)
+// and O (odd x), plus the sign at xb + 64.  Edge masks and mixed cubes
+// (neither all inside nor all outside) come from word-wide bit operations,
+// identical in every lane, with the words of the plane below kept in
+// registers, so no lane works per voxel here.  Outputs per unit (64 voxels
+// of one row of one plane, numbered in scan order (plane, row, segment)):
+// the sign words (every unit), and for units with activity (an edge with a
+// vertex or a cube with triangles) the packed counts of vertices and of
+// mixed cubes and the two activity words.  The unit counts start at zero.
+// An exclusive scan of the counts gives every voxel's first vertex id and
+// every cube's place in the cube list in the reference's order (vertices by
+// (z, y, x, axis) of the edge's lower endpoint, cubes in scan order); the
+// sparse pass (mc_emit_kernel) forms edge masks and cube flags (corner
+// weights NNN=1 NNP=2 NPN=4 NPP=8 PNN=16 PNP=32 PPN=64 PPP=128 with letters
+// x, y, z, TRIANGLE_MESH.cpp:4929-4931) of the active voxels from the sign
+// words, and a scan over the cube list gives each cube's first triangle.
+//
+// Plain 16-byte loads are used: on the large workload's slab (2200^2 x 65
+// planes) they stream the field at about 7.6 TB/s with the classification
+// taken out, where per-warp TMA boxes of 66 x 5 doubles reached 2.6 TB/s.
+constexpr int MC_SEG = 64;     // voxels per unit (one warp's row segment)
+constexpr int MC_WORDS = 2;    // words per unit: even x, odd x
+constexpr int MC_ROWS = 4;     // rows per warp
+constexpr int MC_WARPS = 4;    // warps per classify block
+static_assert(MC_WORDS == MESH_UNIT_WORDS, "words per unit");
+// packed unit counts: vertices (<= 192) | mixed cubes (<= 64) << 8
+__device__ __forceinline__ uint32_t unit_pack(int nv, int nc) {
+  return (uint32_t)nv | (uint32_t)nc << 8;
 }
-// widened for sums over a scan block of SCAN_B units: 21 / 22 / 21 bits
+// widened for sums over a scan block of SCAN_B units
 __device__ __forceinline__ unsigned long long unit_widen(uint32_t c) {
-  return (unsigned long long)(c & 1023u) | (unsigned long long)(c >> 10 & 2047u) << 21 |
-         (unsigned long long)(c >> 21) << 43;
+  return (unsigned long long)(c & 255u) | (unsigned long long)(c >> 8) << 32;
 }
-__device__ __forceinline__ long long wide_nv(unsigned long long w) { return (long long)(w & 0x1FFFFFull); }
-__device__ __forceinline__ long long wide_nt(unsigned long long w) { return (long long)(w >> 21 & 0x3FFFFFull); }
-__device__ __forceinline__ long long wide_nc(unsigned long long w) { return (long long)(w >> 43); }
 
 // bit i of v (< 2^16) to bit 2i
 __device__ __forceinline__ uint32_t spread16(uint32_t v) {
@@ -208,27 +214,11 @@ __device__ __forceinline__ uint32_t spread16(uint32_t v) {
   v = (v | (v << 1)) & 0x55555555u;
   return v;
 }
-
-// Signs (> 0) of the values at x0, x0 + 1, x0 + 2 of one row as bits 0..2;
-// values beyond the row read as 0 (their edges and cubes are masked).  x0 + 2
-// is the next lane's x0; lane 31 loads it.  All lanes of the warp call this.
-template <bool VEC>
-__device__ __forceinline__ int row_signs(const double* __restrict__ row, int x0, int X, int lane) {
-  double a = 0.0, b = 0.0;
-  if (VEC) {
-    if (x0 < X) {  // X even: x0 + 1 < X too
-      const double2 v = __ldg(reinterpret_cast<const double2*>(row + x0));
-      a = v.x;
-      b = v.y;
-    }
-  } else {
-    if (x0 < X) a = __ldg(row + x0);
-    if (x0 + 1 < X) b = __ldg(row + x0 + 1);
-  }
-  const int s = (int)(a > 0.0) | (int)(b > 0.0) << 1;
-  int nxt = __shfl_down_sync(0xffffffffu, s, 1) & 1;
-  if (lane == 31) nxt = x0 + 2 < X && __ldg(row + x0 + 2) > 0.0;
-  return s | nxt << 2;
+// the even/odd words of a unit as 64 bits in x order
+__device__ __forceinline__ unsigned long long natural64(uint2 w) {
+  const uint32_t lo = spread16(w.x & 0xFFFFu) | spread16(w.y & 0xFFFFu) << 1;
+  const uint32_t hi = spread16(w.x >> 16) | spread16(w.y >> 16) << 1;
+  return (unsigned long long)lo | (unsigned long long)hi << 32;
 }
 
 struct McSlab {
@@ -237,97 +227,300 @@ struct McSlab {
   int P, Pv;          // planes in src; voxel planes classified (P - 1, or P on the last slab)
   int gz0;            // global index of src plane 0
   long long XY;
-  uint32_t* bits;     // [unit][MC_WORDS] activity bits, x ascending
-  uint16_t* code;     // [Pv][XY]: edge mask | cube flag << 3, written for active voxels
-  uint32_t* ucount;   // [unit]: packed counts
+  uint2* sign;        // [plane < P][Y][S]: sign words of every unit
+  uint2* bits;        // [Pv][Y][S]: activity words of units with activity
+  uint32_t* ucount;   // [Pv][Y][S]: packed counts (zero where nothing is active)
 };
 
+// Column validity of a segment starting at xb: x < X for even (vE) and odd
+// (vO) bits, x + 1 < X (v1E, v1O).
+struct McCols {
+  uint32_t vE, vO, v1E, v1O;
+};
+__device__ __forceinline__ uint32_t low_bits(int n) {
+  return n >= 32 ? 0xffffffffu : n <= 0 ? 0u : (1u << n) - 1u;
+}
+__device__ __forceinline__ McCols mc_cols(int X, int xb) {
+  McCols v;
+  v.vE = low_bits((X - xb + 1) / 2);   // xb + 2k < X
+  v.vO = low_bits((X - xb) / 2);       // xb + 2k + 1 < X
+  v.v1E = v.vO;
+  v.v1O = low_bits((X - xb - 1) / 2);  // xb + 2k + 2 < X
+  return v;
+}
+
+// v > 0.0 with integer operations (GB300's FP64 pipe, which a double
+// comparison would use, is narrow): positive values from the smallest
+// denormal up to +inf are the bit patterns 1 .. 0x7FF0000000000000; zeros,
+// negatives and NaNs fall outside.
+__device__ __forceinline__ bool positive(double v) {
+  return (unsigned long long)__double_as_longlong(v) - 1ull < 0x7FF0000000000000ull;
+}
+
+// Sign words of rows y0 .. y0 + MC_ROWS of one plane: E[r] bit k = (value at
+// xb + 2k > 0), O[r] the same at xb + 2k + 1, bit r of *N the sign at
+// xb + 64.  Values outside the grid read as 0 (their edges and cubes are
+// masked).  Every load is issued before the first ballot.
 template <bool VEC>
-__global__ void __launch_bounds__(MC_T) mc_classify_kernel(const McSlab c) {
-  __shared__ uint8_t ntri[256];
-  __shared__ uint32_t part[2][MC_T / 32];
-  for (int f = threadIdx.x; f < 256; f += MC_T) ntri[f] = (uint8_t)ntri_of(f);
-  const int seg = blockIdx.x % c.S;
-  const int y = blockIdx.x / c.S;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int x0 = seg * MC_SEG + 2 * threadIdx.x;
-  const bool hy = y + 1 < c.Y;  // uniform over the block
-  const double* row = c.src + (long long)y * c.X;
-  __syncthreads();
-  int lo0 = row_signs<VEC>(row, x0, c.X, lane);                 // plane p, row y
-  int lo1 = hy ? row_signs<VEC>(row + c.X, x0, c.X, lane) : 0;  // plane p, row y + 1
-  for (int p = 0; p < c.Pv; p++) {
-    const bool hz = p + 1 < c.P;  // plane p + 1 exists (uniform)
-    int hi0 = 0, hi1 = 0;
-    if (hz) {
-      const double* up = row + (long long)(p + 1) * c.XY;
-      hi0 = row_signs<VEC>(up, x0, c.X, lane);
-      hi1 = hy ? row_signs<VEC>(up + c.X, x0, c.X, lane) : 0;
-    }
-    uint32_t cnt = 0;
-    int act = 0;
+__device__ __forceinline__ void plane_signs(const double* __restrict__ plane, int X, int Y, int y0,
+                                            int xb, int lane, uint32_t (&E)[MC_ROWS + 1],
+                                            uint32_t (&O)[MC_ROWS + 1], uint32_t* N) {
+  const int x = xb + 2 * lane;
+  double a[MC_ROWS + 1], b[MC_ROWS + 1];
 #pragma unroll
-    for (int i = 0; i < 2; i++) {
-      const int x = x0 + i;
-      if (x >= c.X) continue;
-      const bool hx = x + 1 < c.X;
-      const int s = lo0 >> i & 1;
-      const int m = (int)(hx & (s != (lo0 >> (i + 1) & 1))) |
-                    (int)(hy & (s != (lo1 >> i & 1))) << 1 |
-                    (int)(hz & (s != (hi0 >> i & 1))) << 2;
-      int f = 0;
-      if (hx && hy && hz)
-        f = (lo0 >> i & 1) | (hi0 >> i & 1) << 1 | (lo1 >> i & 1) << 2 | (hi1 >> i & 1) << 3 |
-            (lo0 >> (i + 1) & 1) << 4 | (hi0 >> (i + 1) & 1) << 5 | (lo1 >> (i + 1) & 1) << 6 |
-            (hi1 >> (i + 1) & 1) << 7;
-      const bool cube = f != 0 && f != 255;
-      if (m || cube) {
-        act |= 1 << i;
-        c.code[(long long)p * c.XY + (long long)y * c.X + x] = (uint16_t)(m | f << 3);
-        cnt += unit_pack(__popc(m), cube ? ntri[f] : 0, cube ? 1 : 0);
+  for (int r = 0; r <= MC_ROWS; r++) {
+    a[r] = 0.0;
+    b[r] = 0.0;
+    if (y0 + r < Y) {
+      const double* row = plane + (long long)(y0 + r) * X;
+      if (VEC) {
+        if (x < X) {  // X even: x + 1 < X too
+          const double2 v = __ldg(reinterpret_cast<const double2*>(row + x));
+          a[r] = v.x;
+          b[r] = v.y;
+        }
+      } else {
+        if (x < X) a[r] = __ldg(row + x);
+        if (x + 1 < X) b[r] = __ldg(row + x + 1);
       }
     }
-    const long long u = ((long long)p * c.Y + y) * c.S + seg;
-    const uint32_t ev = __ballot_sync(0xffffffffu, act & 1);
-    const uint32_t od = __ballot_sync(0xffffffffu, act >> 1 & 1);
-    if (lane == 0) {
-      uint32_t* b = c.bits + u * MC_WORDS + 2 * warp;
-      b[0] = spread16(ev & 0xFFFFu) | spread16(od & 0xFFFFu) << 1;
-      b[1] = spread16(ev >> 16) | spread16(od >> 16) << 1;
-    }
-    cnt = __reduce_add_sync(0xffffffffu, cnt);
-    if (lane == 0) part[p & 1][warp] = cnt;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      uint32_t t = 0;
+  }
+  double nx = 0.0;
+  if (lane <= MC_ROWS && y0 + lane < Y && xb + MC_SEG < X)
+    nx = __ldg(plane + (long long)(y0 + lane) * X + xb + MC_SEG);
 #pragma unroll
-      for (int w = 0; w < MC_T / 32; w++) t += part[p & 1][w];
-      c.ucount[u] = t;
+  for (int r = 0; r <= MC_ROWS; r++) {
+    E[r] = __ballot_sync(0xffffffffu, positive(a[r]));
+    O[r] = __ballot_sync(0xffffffffu, positive(b[r]));
+  }
+  *N = __ballot_sync(0xffffffffu, positive(nx));
+}
+
+// lanes 0 .. MC_ROWS - 1: the sign words of their row of plane p
+__device__ __forceinline__ void store_signs(const McSlab& c, int p, int y0, int seg, int lane,
+                                            const uint32_t (&E)[MC_ROWS + 1],
+                                            const uint32_t (&O)[MC_ROWS + 1]) {
+  uint2 w = make_uint2(0u, 0u);
+#pragma unroll
+  for (int r = 0; r < MC_ROWS; r++)
+    if (lane == r) w = make_uint2(E[r], O[r]);
+  if (lane < MC_ROWS && y0 + lane < c.Y) c.sign[((long long)p * c.Y + y0 + lane) * c.S + seg] = w;
+}
+
+// Voxel plane p of rows y0 .. y0 + MC_ROWS - 1 of segment seg, from the sign
+// words of planes p (l*) and p + 1 (h*, zero when the plane does not exist).
+// A cube is mixed when its eight corners are neither all inside nor all
+// outside: with the z-pair words zo = l | h and za = l & h per row, the
+// corners of the cube at (x, y) are the bits x and x + 1 of rows y and y + 1.
+__device__ __forceinline__ void mc_classify_plane(const McSlab& c, int p, bool hz, int y0, int seg,
+                                                  int lane, const McCols& v,
+                                                  const uint32_t (&lE)[MC_ROWS + 1],
+                                                  const uint32_t (&lO)[MC_ROWS + 1], uint32_t lN,
+                                                  const uint32_t (&hE)[MC_ROWS + 1],
+                                                  const uint32_t (&hO)[MC_ROWS + 1], uint32_t hN) {
+  const int xb = seg * MC_SEG;
+  // Where all MC_ROWS + 1 rows and the next column exist, a block whose two
+  // planes are all inside or all outside has no vertex and no mixed cube
+  if (hz && y0 + MC_ROWS < c.Y && xb + MC_SEG < c.X) {
+    uint32_t any = 0u, all = 0xffffffffu;
+#pragma unroll
+    for (int r = 0; r <= MC_ROWS; r++) {
+      any |= lE[r] | lO[r] | hE[r] | hO[r];
+      all &= lE[r] & lO[r] & hE[r] & hO[r];
     }
-    lo0 = hi0;
-    lo1 = hi1;
+    constexpr uint32_t rows = (1u << (MC_ROWS + 1)) - 1u;
+    if ((any == 0u && ((lN | hN) & rows) == 0u) || (all == 0xffffffffu && (lN & hN & rows) == rows))
+      return;
+  }
+  // the x + 1 neighbour of even bit k is odd bit k, of odd bit k even bit
+  // k + 1 (bit 31: the next segment's first column, from the N words)
+  uint32_t l1[MC_ROWS + 1], anyE[MC_ROWS + 1], anyO[MC_ROWS + 1], allE[MC_ROWS + 1],
+      allO[MC_ROWS + 1];
+#pragma unroll
+  for (int r = 0; r <= MC_ROWS; r++) {
+    l1[r] = (lE[r] >> 1) | (lN << (31 - r) & 0x80000000u);
+    anyE[r] = anyO[r] = allE[r] = allO[r] = 0u;
+    if (hz) {
+      const uint32_t h1 = (hE[r] >> 1) | (hN << (31 - r) & 0x80000000u);
+      const uint32_t zoE = lE[r] | hE[r], zoO = lO[r] | hO[r], zo1 = l1[r] | h1;
+      const uint32_t zaE = lE[r] & hE[r], zaO = lO[r] & hO[r], za1 = l1[r] & h1;
+      anyE[r] = zoE | zoO;  // columns x, x+1 of an even voxel
+      allE[r] = zaE & zaO;
+      anyO[r] = zoO | zo1;  // columns x, x+1 of an odd voxel
+      allO[r] = zaO & za1;
+    }
+  }
+  uint32_t cnt_lane = 0;       // lane r: the packed counts of row r
+  uint2 bits_lane = {0u, 0u};  // lane r: the activity words of row r
+#pragma unroll
+  for (int r = 0; r < MC_ROWS; r++) {
+    const int y = y0 + r;
+    if (y >= c.Y) break;
+    const bool hy = y + 1 < c.Y;
+    const uint32_t AE = lE[r], AO = lO[r];
+    const uint32_t xeE = (AE ^ AO) & v.v1E, xeO = (AO ^ l1[r]) & v.v1O;
+    const uint32_t yeE = hy ? (AE ^ lE[r + 1]) & v.vE : 0u, yeO = hy ? (AO ^ lO[r + 1]) & v.vO : 0u;
+    const uint32_t zeE = hz ? (AE ^ hE[r]) & v.vE : 0u, zeO = hz ? (AO ^ hO[r]) & v.vO : 0u;
+    uint32_t mxE = 0u, mxO = 0u;
+    if (hy && hz) {
+      mxE = (anyE[r] | anyE[r + 1]) & ~(allE[r] & allE[r + 1]) & v.v1E;
+      mxO = (anyO[r] | anyO[r + 1]) & ~(allO[r] & allO[r + 1]) & v.v1O;
+    }
+    const uint32_t actE = xeE | yeE | zeE | mxE, actO = xeO | yeO | zeO | mxO;
+    if (!(actE | actO)) continue;  // uniform over the warp
+    const int nv = __popc(xeE) + __popc(xeO) + __popc(yeE) + __popc(yeO) + __popc(zeE) + __popc(zeO);
+    const int nc = __popc(mxE) + __popc(mxO);
+    if (lane == r) {
+      cnt_lane = unit_pack(nv, nc);
+      bits_lane = make_uint2(actE, actO);
+    }
+  }
+  if (lane < MC_ROWS && cnt_lane) {
+    const long long u = ((long long)p * c.Y + y0 + lane) * c.S + seg;
+    c.ucount[u] = cnt_lane;
+    c.bits[u] = bits_lane;
   }
 }
 
-// The edges case 158 leaves without a vertex: candidates k < X-1 are the
-// x-edges at (k, 0, 0), the next Y-1 the y-edges at (X-1, k, 0) (both on
-// the grid's first plane), the next Pv the z-edges at (X-1, 0, p).  An edge
-// loses its vertex when its one cube has flag 158.
-__global__ void mc_fix158_kernel(const McSlab c) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  int x, y, p, cx, bit;
-  if (k < c.X - 1) {
-    x = k, y = 0, p = 0, cx = k, bit = 1;
-  } else if (k < c.X - 1 + c.Y - 1) {
-    x = c.X - 1, y = k - (c.X - 1), p = 0, cx = c.X - 2, bit = 2;
-  } else if (k < c.X - 1 + c.Y - 1 + c.Pv) {
-    x = c.X - 1, y = 0, p = k - (c.X - 1 + c.Y - 1), cx = c.X - 2, bit = 4;
-  } else {
-    return;
+// One warp per task (segment, row group).
+template <bool VEC>
+__global__ void __launch_bounds__(32 * MC_WARPS) mc_classify_kernel(const McSlab c) {
+  const int lane = threadIdx.x & 31;
+  const long long task = (long long)blockIdx.x * MC_WARPS + (threadIdx.x >> 5);
+  const int groups = (c.Y + MC_ROWS - 1) / MC_ROWS;
+  if (task >= (long long)groups * c.S) return;  // the whole warp
+  const int seg = (int)(task % c.S);
+  const int y0 = (int)(task / c.S) * MC_ROWS;
+  const int xb = seg * MC_SEG;
+  const McCols v = mc_cols(c.X, xb);
+  uint32_t lE[MC_ROWS + 1], lO[MC_ROWS + 1], lN;
+  plane_signs<VEC>(c.src, c.X, c.Y, y0, xb, lane, lE, lO, &lN);
+  for (int p = 0; p < c.Pv; p++) {
+    const bool hz = p + 1 < c.P;
+    uint32_t hE[MC_ROWS + 1], hO[MC_ROWS + 1], hN = 0;
+#pragma unroll
+    for (int r = 0; r <= MC_ROWS; r++) hE[r] = hO[r] = 0u;
+    if (hz) plane_signs<VEC>(c.src + (long long)(p + 1) * c.XY, c.X, c.Y, y0, xb, lane, hE, hO, &hN);
+    store_signs(c, p, y0, seg, lane, lE, lO);
+    mc_classify_plane(c, p, hz, y0, seg, lane, v, lE, lO, lN, hE, hO, hN);
+#pragma unroll
+    for (int r = 0; r <= MC_ROWS; r++) {
+      lE[r] = hE[r];
+      lO[r] = hO[r];
+    }
+    lN = hN;
   }
-  if (bit != 4 && c.gz0 != 0) return;  // only the grid's first plane
-  if (p + 1 >= c.P) return;            // no cube above this plane
-  const int cy = bit == 2 ? y : 0;
+  // the window's top plane when it is not classified itself (the emit pass
+  // reads it as the plane above)
+  if (c.Pv < c.P) store_signs(c, c.Pv, y0, seg, lane, lE, lO);
+}
+
+// Form for fields whose rows are 16-byte aligned (X even): each lane copies
+// its own values of MC_ASTAGES planes ahead into a shared-memory ring with
+// cp.async (16 bytes per row; lanes 0 .. MC_ROWS also the next column's 8
+// bytes; zero-filled outside the grid), so a warp keeps several planes of
+// loads in flight without holding them in registers.  A lane reads back only
+// what it copied itself, so cp.async.wait_group alone orders the reads.
+constexpr int MC_ASTAGES = 4;
+constexpr int MC_NEXT_OFF = (MC_ROWS + 1) * 32 * 16;        // next-column values
+constexpr int MC_ASTAGE_BYTES = MC_NEXT_OFF + 8 * (MC_ROWS + 1 + 1) / 16 * 16 + 16;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, bool valid) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src),
+               "r"(valid ? 16 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src, bool valid) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(smem_u32(dst)), "l"(src),
+               "r"(valid ? 8 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_ahead() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(MC_ASTAGES - 1) : "memory");
+}
+
+// this lane's copies of plane q (q >= n_load: an empty group)
+__device__ __forceinline__ void async_plane(const McSlab& c, unsigned char* stage, int q, int n_load,
+                                            int y0, int xb, int lane) {
+  if (q < n_load) {
+    const double* plane = c.src + (long long)q * c.XY;
+    const int x = xb + 2 * lane;
+#pragma unroll
+    for (int r = 0; r <= MC_ROWS; r++) {
+      const bool ok = y0 + r < c.Y && x < c.X;
+      cp_async16(stage + (r * 32 + lane) * 16, ok ? plane + (long long)(y0 + r) * c.X + x : c.src, ok);
+    }
+    if (lane <= MC_ROWS) {
+      const bool ok = y0 + lane < c.Y && xb + MC_SEG < c.X;
+      cp_async8(stage + MC_NEXT_OFF + lane * 8,
+                ok ? plane + (long long)(y0 + lane) * c.X + xb + MC_SEG : c.src, ok);
+    }
+  }
+  cp_async_commit();
+}
+
+__device__ __forceinline__ void stage_signs(const unsigned char* stage, int lane,
+                                            uint32_t (&E)[MC_ROWS + 1], uint32_t (&O)[MC_ROWS + 1],
+                                            uint32_t* N) {
+#pragma unroll
+  for (int r = 0; r <= MC_ROWS; r++) {
+    const double2 v = *reinterpret_cast<const double2*>(stage + (r * 32 + lane) * 16);
+    E[r] = __ballot_sync(0xffffffffu, positive(v.x));
+    O[r] = __ballot_sync(0xffffffffu, positive(v.y));
+  }
+  const double nx = lane <= MC_ROWS ? *reinterpret_cast<const double*>(stage + MC_NEXT_OFF + lane * 8) : 0.0;
+  *N = __ballot_sync(0xffffffffu, positive(nx));
+}
+
+__global__ void __launch_bounds__(32 * MC_WARPS) mc_classify_async_kernel(const McSlab c) {
+  __shared__ __align__(16) unsigned char ring[MC_WARPS][MC_ASTAGES][MC_ASTAGE_BYTES];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long long task = (long long)blockIdx.x * MC_WARPS + warp;
+  const int groups = (c.Y + MC_ROWS - 1) / MC_ROWS;
+  if (task >= (long long)groups * c.S) return;  // the whole warp
+  const int seg = (int)(task % c.S);
+  const int y0 = (int)(task / c.S) * MC_ROWS;
+  const int xb = seg * MC_SEG;
+  const McCols v = mc_cols(c.X, xb);
+  const int n_load = min(c.Pv + 1, c.P);  // planes read
+#pragma unroll
+  for (int q = 0; q < MC_ASTAGES; q++) async_plane(c, ring[warp][q], q, n_load, y0, xb, lane);
+  uint32_t lE[MC_ROWS + 1], lO[MC_ROWS + 1], lN = 0;
+  for (int q = 0; q < n_load; q++) {
+    unsigned char* st = ring[warp][q % MC_ASTAGES];
+    cp_async_wait_ahead();  // plane q has landed (this lane's copies)
+    uint32_t hE[MC_ROWS + 1], hO[MC_ROWS + 1], hN;
+    stage_signs(st, lane, hE, hO, &hN);
+    async_plane(c, st, q + MC_ASTAGES, n_load, y0, xb, lane);
+    if (q > 0) {  // voxel plane q - 1 between planes q - 1 and q
+      store_signs(c, q - 1, y0, seg, lane, lE, lO);
+      mc_classify_plane(c, q - 1, true, y0, seg, lane, v, lE, lO, lN, hE, hO, hN);
+    }
+#pragma unroll
+    for (int r = 0; r <= MC_ROWS; r++) {
+      lE[r] = hE[r];
+      lO[r] = hO[r];
+    }
+    lN = hN;
+  }
+  // the last plane read: classified itself on the grid's last slab (no plane
+  // above), else stored as the window's top plane
+  store_signs(c, n_load - 1, y0, seg, lane, lE, lO);
+  if (c.Pv == n_load) {
+    uint32_t zE[MC_ROWS + 1], zO[MC_ROWS + 1];
+#pragma unroll
+    for (int r = 0; r <= MC_ROWS; r++) zE[r] = zO[r] = 0u;
+    mc_classify_plane(c, n_load - 1, false, y0, seg, lane, v, lE, lO, lN, zE, zO, 0u);
+  }
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
+// Flag of the cube at (cx, cy) of window plane p, from the field.
+__device__ __forceinline__ int cube_flag_src(const McSlab& c, int cx, int cy, int p) {
   int f = 0;
 #pragma unroll
   for (int dx = 0; dx < 2; dx++)
@@ -337,18 +530,37 @@ __global__ void mc_fix158_kernel(const McSlab c) {
       for (int dz = 0; dz < 2; dz++)
         f |= (int)(c.src[(long long)(p + dz) * c.XY + (long long)(cy + dy) * c.X + cx + dx] > 0.0)
              << (4 * dx + 2 * dy + dz);
-  if (f != 158) return;
-  // the omitted edge changes sign, so the voxel is active and has a code
-  const long long v = (long long)p * c.XY + (long long)y * c.X + x;
-  const int code = c.code[v];
-  if (!(code & bit)) return;
-  c.code[v] = (uint16_t)(code & ~bit);
+  return f;
+}
+
+// The edges case 158 leaves without a vertex: candidates k < X-1 are the
+// x-edges at (k, 0, 0), the next Y-1 the y-edges at (X-1, k, 0) (both on
+// the grid's first plane), the next Pv the z-edges at (X-1, 0, p).  An edge
+// loses its vertex when its one cube has flag 158; the edge changes sign, so
+// its voxel's unit counted it, and the count drops by one (the emit pass
+// applies the same rule).
+__global__ void mc_fix158_kernel(const McSlab c) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  int x, y, p, cx;
+  bool zline = false;
+  if (k < c.X - 1) {
+    x = k, y = 0, p = 0, cx = k;
+  } else if (k < c.X - 1 + c.Y - 1) {
+    x = c.X - 1, y = k - (c.X - 1), p = 0, cx = c.X - 2;
+  } else if (k < c.X - 1 + c.Y - 1 + c.Pv) {
+    x = c.X - 1, y = 0, p = k - (c.X - 1 + c.Y - 1), cx = c.X - 2, zline = true;
+  } else {
+    return;
+  }
+  if (!zline && c.gz0 != 0) return;  // only the grid's first plane
+  if (p + 1 >= c.P) return;          // no cube above this plane
+  if (cube_flag_src(c, cx, y, p) != 158) return;
   atomicSub(&c.ucount[((long long)p * c.Y + y) * c.S + x / MC_SEG], 1u);
 }
 
-// Per scan block of SCAN_B units: the sums of the three counts.
+// Per scan block of SCAN_B units: the sums of the two counts.
 __global__ void __launch_bounds__(SCAN_T) mc_unit_sums_kernel(const uint32_t* __restrict__ ucount,
-                                                              long long U, long long* bsum3) {
+                                                              long long U, long long* bsum2) {
   const long long base = (long long)blockIdx.x * SCAN_B + (long long)threadIdx.x * SCAN_V;
   unsigned long long w = 0;
 #pragma unroll
@@ -357,27 +569,26 @@ __global__ void __launch_bounds__(SCAN_T) mc_unit_sums_kernel(const uint32_t* __
   unsigned long long total;
   block_exclusive_scan(w, &total);
   if (threadIdx.x == 0) {
-    bsum3[3 * blockIdx.x] = wide_nv(total);
-    bsum3[3 * blockIdx.x + 1] = wide_nt(total);
-    bsum3[3 * blockIdx.x + 2] = wide_nc(total);
+    bsum2[2 * blockIdx.x] = (long long)(total & 0xFFFFFFFFull);
+    bsum2[2 * blockIdx.x + 1] = (long long)(total >> 32);
   }
 }
 
-// Exclusive scan of the nb block sums (three counts) in place; the totals go
-// to tot->nv, nt, nc.
-__global__ void __launch_bounds__(1024) mc_scan_sums_kernel(long long* bsum3, long long nb,
+// Exclusive scan of the nb block sums (two counts) in place; the totals go
+// to tot->nv and tot->nc.
+__global__ void __launch_bounds__(1024) mc_scan_sums_kernel(long long* bsum2, long long nb,
                                                             McTotals* tot) {
-  __shared__ long long sh[3][32];
-  __shared__ long long carry[3];
-  if (threadIdx.x < 3) carry[threadIdx.x] = 0;
+  __shared__ long long sh[2][32];
+  __shared__ long long carry[2];
+  if (threadIdx.x < 2) carry[threadIdx.x] = 0;
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (long long c0 = 0; c0 < nb; c0 += 1024) {
     const long long i = c0 + threadIdx.x;
-    long long v[3], inc[3];
+    long long v[2], inc[2];
 #pragma unroll
-    for (int q = 0; q < 3; q++) {
-      v[q] = i < nb ? bsum3[3 * i + q] : 0;
+    for (int q = 0; q < 2; q++) {
+      v[q] = i < nb ? bsum2[2 * i + q] : 0;
       inc[q] = v[q];
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
@@ -389,7 +600,7 @@ __global__ void __launch_bounds__(1024) mc_scan_sums_kernel(long long* bsum3, lo
     __syncthreads();
     if (warp == 0) {
 #pragma unroll
-      for (int q = 0; q < 3; q++) {
+      for (int q = 0; q < 2; q++) {
         long long w = sh[q][lane];
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -401,40 +612,56 @@ __global__ void __launch_bounds__(1024) mc_scan_sums_kernel(long long* bsum3, lo
     }
     __syncthreads();
 #pragma unroll
-    for (int q = 0; q < 3; q++)
-      if (i < nb) bsum3[3 * i + q] = carry[q] + (warp ? sh[q][warp - 1] : 0) + inc[q] - v[q];
+    for (int q = 0; q < 2; q++)
+      if (i < nb) bsum2[2 * i + q] = carry[q] + (warp ? sh[q][warp - 1] : 0) + inc[q] - v[q];
     __syncthreads();
-    if (threadIdx.x < 3) carry[threadIdx.x] += sh[threadIdx.x][31];
+    if (threadIdx.x < 2) carry[threadIdx.x] += sh[threadIdx.x][31];
     __syncthreads();
   }
   if (threadIdx.x == 0) {
     tot->nv = carry[0];
-    tot->nt = carry[1];
-    tot->nc = carry[2];
+    tot->nc = carry[1];
   }
 }
 
 // Pass 3: the slab's vertices and cubes in scan order.  Each thread takes
-// SCAN_V consecutive units; for their active voxels it writes the vertex id
-// base and edge mask of the voxel (window plane p + 1), one edge-list entry
-// per vertex (window voxel index * 4 + axis) and one entry per cube with
-// triangles (its cell, global plane, flag and first triangle).
+// SCAN_V consecutive units; for the active voxels of its units it forms the
+// edge mask and cube flag from the sign words of the voxel's unit, the unit
+// above it (y + 1), the units of the plane above, and the first column of the
+// next unit of each, and writes the vertex id base and mask of the voxel
+// (window plane p + 1), one edge-list entry per vertex (window voxel index
+// * 4 + axis) and one entry per mixed cube (its cell, global plane and
+// flag; the first triangle comes from the cube scan).
 struct McEmit {
   McSlab c;
-  const long long* bpre;  // exclusive prefixes of the scan blocks (3 per block)
+  const long long* bpre;  // exclusive prefixes of the scan blocks (2 per block)
   uint8_t* masks;
   int32_t* vbase;
   uint32_t* list;         // this slab's vertices, from list[0]
   McCube* cubes;          // this slab's cube entries, from cubes[0]
   long long id0;          // global id of the slab's first vertex
-  long long t0;           // global index of the slab's first triangle
   long long u_split;      // first unit of the slab's last cube layer (-1: none)
   McTotals* tot;
 };
 
+// the unit's sign words in x order, with the next unit's first sign as bit 64
+struct McRow {
+  unsigned long long w;
+  uint32_t next;
+};
+__device__ __forceinline__ McRow load_row(const McSlab& c, int p, int y, int seg) {
+  McRow r{0ull, 0u};
+  if (p >= c.P || y >= c.Y) return r;
+  const long long u = ((long long)p * c.Y + y) * c.S + seg;
+  r.w = natural64(c.sign[u]);
+  if (seg + 1 < c.S) r.next = c.sign[u + 1].x & 1u;
+  return r;
+}
+__device__ __forceinline__ uint32_t bit_at(const McRow& r, int i) {
+  return i < 64 ? (uint32_t)(r.w >> i) & 1u : r.next;
+}
+
 __global__ void __launch_bounds__(SCAN_T) mc_emit_kernel(const McEmit e, long long U) {
-  __shared__ uint8_t ntri[256];
-  for (int f = threadIdx.x; f < 256; f += SCAN_T) ntri[f] = (uint8_t)ntri_of(f);
   const McSlab& c = e.c;
   const long long base = (long long)blockIdx.x * SCAN_B + (long long)threadIdx.x * SCAN_V;
   uint32_t cnt[SCAN_V];
@@ -445,10 +672,9 @@ __global__ void __launch_bounds__(SCAN_T) mc_emit_kernel(const McEmit e, long lo
     w += unit_widen(cnt[k]);
   }
   unsigned long long total;
-  const unsigned long long ex = block_exclusive_scan(w, &total);  // also syncs ntri
-  long long vp = e.bpre[3 * blockIdx.x] + wide_nv(ex);
-  long long tp = e.bpre[3 * blockIdx.x + 1] + wide_nt(ex);
-  long long cp = e.bpre[3 * blockIdx.x + 2] + wide_nc(ex);
+  const unsigned long long ex = block_exclusive_scan(w, &total);
+  long long vp = e.bpre[2 * blockIdx.x] + (long long)(ex & 0xFFFFFFFFull);
+  long long cp = e.bpre[2 * blockIdx.x + 1] + (long long)(ex >> 32);
   for (int k = 0; k < SCAN_V; k++) {
     const long long u = base + k;
     if (u == e.u_split) e.tot->split = cp;
@@ -457,35 +683,56 @@ __global__ void __launch_bounds__(SCAN_T) mc_emit_kernel(const McEmit e, long lo
     const long long py = u / c.S;
     const int y = (int)(py % c.Y);
     const int p = (int)(py / c.Y);
+    const int gz = c.gz0 + p;
+    const int xb = seg * MC_SEG;
+    const McRow A = load_row(c, p, y, seg), C = load_row(c, p, y + 1, seg);
+    const McRow B = load_row(c, p + 1, y, seg), D = load_row(c, p + 1, y + 1, seg);
+    const bool hy = y + 1 < c.Y, hz = p + 1 < c.P;
     const long long r0 = (long long)y * c.X;
-    for (int wd = 0; wd < MC_WORDS; wd++) {
-      uint32_t word = c.bits[u * MC_WORDS + wd];
-      while (word) {
-        const int b = __ffs(word) - 1;
-        word &= word - 1;
-        const int x = seg * MC_SEG + wd * 32 + b;
-        const int code = c.code[(long long)p * c.XY + r0 + x];
-        const int m = code & 7, f = code >> 3;
-        const long long wv = (long long)(p + 1) * c.XY + r0 + x;
-        if (m) {
-          e.vbase[wv] = (int32_t)(e.id0 + vp);
-          e.masks[wv] = (uint8_t)m;
+    unsigned long long act = natural64(c.bits[u]);
+    while (act) {
+      const int i = __ffsll((long long)act) - 1;
+      act &= act - 1;
+      const int x = xb + i;
+      const bool hx = x + 1 < c.X;
+      const uint32_t a0 = bit_at(A, i), a1 = bit_at(A, i + 1);
+      const uint32_t b0 = bit_at(B, i), c0 = bit_at(C, i);
+      int m = (int)(hx & (a0 != a1)) | (int)(hy & (a0 != c0)) << 1 | (int)(hz & (a0 != b0)) << 2;
+      int f = 0;
+      if (hx && hy && hz)
+        f = (int)(a0 | b0 << 1 | c0 << 2 | bit_at(D, i) << 3 | a1 << 4 | bit_at(B, i + 1) << 5 |
+                  bit_at(C, i + 1) << 6 | bit_at(D, i + 1) << 7);
+      // the case-158 edges on the grid's boundary lines (mc_fix158_kernel)
+      if ((m & 1) && y == 0 && gz == 0 && f == 158) m &= ~1;
+      if (x == c.X - 1 && (m & 6)) {
+        if ((m & 2) && gz == 0 && cube_flag_src(c, x - 1, y, p) == 158) m &= ~2;
+        if ((m & 4) && y == 0 && cube_flag_src(c, x - 1, 0, p) == 158) m &= ~4;
+      }
+      const long long wv = (long long)(p + 1) * c.XY + r0 + x;
+      if (m) {
+        e.vbase[wv] = (int32_t)(e.id0 + vp);
+        e.masks[wv] = (uint8_t)m;
 #pragma unroll
-          for (int a = 0; a < 3; a++)
-            if (m >> a & 1) e.list[vp++] = (uint32_t)(wv * 4 + a);
-        }
-        if (f != 0 && f != 255) {
-          McCube q;
-          q.r = (uint32_t)(r0 + x);
-          q.gzf = (uint32_t)(c.gz0 + p) | (uint32_t)f << 24;
-          q.tb = e.t0 + tp;
-          e.cubes[cp++] = q;
-          tp += ntri[f];
-        }
+        for (int a = 0; a < 3; a++)
+          if (m >> a & 1) e.list[vp++] = (uint32_t)(wv * 4 + a);
+      }
+      if (f != 0 && f != 255) {
+        McCube q;
+        q.r = (uint32_t)(r0 + x);
+        q.gzf = (uint32_t)gz | (uint32_t)f << 24;
+        q.tb = 0;
+        e.cubes[cp++] = q;
       }
     }
   }
 }
+
+// The cube scan: each cube's first triangle, in cube-list order.
+struct CubeTris {
+  McCube* cubes;
+  __device__ int count(long long i) const { return ntri_of((int)(cubes[i].gzf >> 24)); }
+  __device__ void emit(long long i, long long k) const { cubes[i].tb = k; }
+};
 
 // Pass 4: the triangles of cube entries [0, n) with n = n_carry + the
 // slab's entries below its last cube layer (all of them on the last slab):
@@ -1031,8 +1278,7 @@ long long mesh_units(int X, int Y, int planes) {
   return (long long)planes * Y * ((X + MC_SEG - 1) / MC_SEG);
 }
 
-cudaError_t mesh_classify(const MeshWindow& w, const double* src, int P, int Pv, int gz0,
-                          cudaStream_t s) {
+static McSlab slab_of(const MeshWindow& w, const double* src, int P, int Pv, int gz0) {
   McSlab c;
   c.src = src;
   c.X = w.X;
@@ -1042,18 +1288,27 @@ cudaError_t mesh_classify(const MeshWindow& w, const double* src, int P, int Pv,
   c.Pv = Pv;
   c.gz0 = gz0;
   c.XY = (long long)w.X * w.Y;
-  c.bits = w.bits;
-  c.code = w.code;
+  c.sign = reinterpret_cast<uint2*>(w.sign);
+  c.bits = reinterpret_cast<uint2*>(w.bits);
   c.ucount = w.ucount;
-  const unsigned blocks = (unsigned)((long long)c.S * c.Y);
-  const bool vec = (w.X % 2 == 0) && ((reinterpret_cast<uintptr_t>(src) & 15u) == 0);
-  if (vec)
-    mc_classify_kernel<true><<<blocks, MC_T, 0, s>>>(c);
+  return c;
+}
+
+cudaError_t mesh_classify(const MeshWindow& w, const double* src, int P, int Pv, int gz0,
+                          cudaStream_t s) {
+  const McSlab c = slab_of(w, src, P, Pv, gz0);
+  const long long U = mesh_units(w.X, w.Y, Pv);
+  cudaError_t err;
+  // units without activity keep these zero counts (the kernel stores the others)
+  if ((err = cudaMemsetAsync(w.ucount, 0, (size_t)U * sizeof(uint32_t), s))) return err;
+  const long long tasks = (long long)c.S * ((c.Y + MC_ROWS - 1) / MC_ROWS);
+  const unsigned blocks = (unsigned)((tasks + MC_WARPS - 1) / MC_WARPS);
+  if ((w.X % 2 == 0) && ((reinterpret_cast<uintptr_t>(src) & 15u) == 0))
+    mc_classify_async_kernel<<<blocks, 32 * MC_WARPS, 0, s>>>(c);
   else
-    mc_classify_kernel<false><<<blocks, MC_T, 0, s>>>(c);
+    mc_classify_kernel<false><<<blocks, 32 * MC_WARPS, 0, s>>>(c);
   const int nfix = w.X - 1 + w.Y - 1 + Pv;
   mc_fix158_kernel<<<(nfix + 127) / 128, 128, 0, s>>>(c);
-  const long long U = mesh_units(w.X, w.Y, Pv);
   const long long nb = (U + SCAN_B - 1) / SCAN_B;
   mc_unit_sums_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(w.ucount, U, w.bsum);
   mc_scan_sums_kernel<<<1, 1024, 0, s>>>(w.bsum, nb, w.tot);
@@ -1061,33 +1316,34 @@ cudaError_t mesh_classify(const MeshWindow& w, const double* src, int P, int Pv,
 }
 
 cudaError_t mesh_emit(const MeshWindow& w, const double* src, int P, int Pv, int gz0,
-                      long long u_split, long long id0, long long t0, McCube* cubes,
-                      cudaStream_t s) {
+                      long long u_split, long long id0, McCube* cubes, cudaStream_t s) {
   McEmit e;
-  e.c.src = src;
-  e.c.X = w.X;
-  e.c.Y = w.Y;
-  e.c.S = (w.X + MC_SEG - 1) / MC_SEG;
-  e.c.P = P;
-  e.c.Pv = Pv;
-  e.c.gz0 = gz0;
-  e.c.XY = (long long)w.X * w.Y;
-  e.c.bits = w.bits;
-  e.c.code = w.code;
-  e.c.ucount = w.ucount;
+  e.c = slab_of(w, src, P, Pv, gz0);
   e.bpre = w.bsum;
   e.masks = w.masks;
   e.vbase = w.vbase;
   e.list = w.list;
   e.cubes = cubes;
   e.id0 = id0;
-  e.t0 = t0;
   e.u_split = u_split;
   e.tot = w.tot;
   const long long U = mesh_units(w.X, w.Y, Pv);
   const long long nb = (U + SCAN_B - 1) / SCAN_B;
   mc_emit_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(e, U);
   return cudaGetLastError();
+}
+
+cudaError_t mesh_cube_scan(const MeshWindow& w, McCube* cubes, long long nc, long long t0,
+                           cudaStream_t s) {
+  if (nc <= 0) return cudaMemsetAsync(&w.tot->nt, 0, sizeof(long long), s);
+  const long long nb = (nc + SCAN_B - 1) / SCAN_B;
+  CubeTris op{cubes};
+  count_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(op, nc, w.bsum);
+  scan_bsum_kernel<<<1, 1024, 0, s>>>(w.bsum, nb);
+  emit_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(op, nc, w.bsum, t0);
+  cudaError_t err = cudaGetLastError();
+  if (err) return err;
+  return cudaMemcpyAsync(&w.tot->nt, w.bsum + nb, sizeof(long long), cudaMemcpyDeviceToDevice, s);
 }
 
 cudaError_t mesh_triangles(const MeshWindow& w, const McCube* cubes, long long n_carry,

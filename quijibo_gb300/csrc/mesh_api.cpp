@@ -77,12 +77,12 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
   const long long units = qj::mesh_units(X, Y, nz + 1);
   if ((rc = ensure(ctx, &ctx->m_masks, &ctx->m_masks_cap, wplanes)) ||
       (rc = ensure(ctx, &ctx->m_vbase, &ctx->m_vbase_cap, wplanes)) ||
-      (rc = ensure(ctx, &ctx->m_code, &ctx->m_code_cap, (size_t)(nz + 1) * XY)) ||
+      (rc = ensure(ctx, &ctx->m_sign, &ctx->m_sign_cap, (size_t)units * qj::MESH_UNIT_WORDS)) ||
       (rc = ensure(ctx, &ctx->m_bits, &ctx->m_bits_cap, (size_t)units * qj::MESH_UNIT_WORDS)) ||
       (rc = ensure(ctx, &ctx->m_ucount, &ctx->m_ucount_cap, (size_t)units)) ||
       (rc = ensure(ctx, &ctx->m_tot, &ctx->m_tot_cap, (size_t)1)) ||
       (rc = ensure(ctx, &ctx->m_bsum, &ctx->m_bsum_cap,
-                   (size_t)std::max(3 * qj::mesh_scan_blocks(units), (long long)1))))
+                   (size_t)std::max(2 * qj::mesh_scan_blocks(units), (long long)1))))
     return rc;
   if (streaming && (rc = ensure(ctx, &ctx->m_field, &ctx->m_field_cap, (size_t)(nz + 1) * XY)))
     return rc;
@@ -98,14 +98,14 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
   w.list = ctx->m_list;
   w.bsum = ctx->m_bsum;
   w.bits = ctx->m_bits;
-  w.code = ctx->m_code;
+  w.sign = ctx->m_sign;
   w.ucount = ctx->m_ucount;
   w.tot = ctx->m_tot;
   const GridParams g = qj_grid_params(grid, 0, Z);
   IterParams it{};
   if (iter) it = qj_iter_params(iter, grid);
   const bool pow_ref = !iter || iter->refine_pow == QJG_REFINE_POW || !m->all_int;
-  const long long S = (X + 255) / 256;  // units per row (qj::mesh_units)
+  const long long S = (X + 63) / 64;  // units per row (qj::mesh_units)
 
   long long nv = 0, nt = 0;
   long long n_carry = 0, prev_nc = 0;  // cube entries carried into the slab; the last slab's count
@@ -175,8 +175,10 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
     qj::McTotals tot;
     QJ_CUDA(ctx, cudaMemcpyAsync(&tot, ctx->m_tot, sizeof tot, cudaMemcpyDeviceToHost, s));
     QJ_CUDA(ctx, cudaStreamSynchronize(s));
-    // the previous slab's last cube layer (its split is still in tot)
+    // the previous slab's last cube layer (its split is still in tot) and
+    // the triangles of the previous slab's cubes
     n_carry = c0 > 0 ? prev_nc - tot.split : 0;
+    if (c0 > 0) nt += tot.nt;
     const long long n_new = tot.nv, nc = tot.nc;
     if (nv + n_new > INT32_MAX)
       return fail(ctx, QJG_ERR_CAPACITY, "more than 2^31 vertices; int32 indices cannot hold them");
@@ -195,8 +197,9 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
                         (size_t)std::max<long long>(nc, 1), 0, s)))
       return rc;
     const long long u_split = last ? -1 : (long long)(L - 1) * Y * S;
-    QJ_CUDA(ctx, qj::mesh_emit(w, src, P, Pv, c0, u_split, nv, nt, ctx->m_cubes[cur] + n_carry, s));
-    ctx->launches++;
+    QJ_CUDA(ctx, qj::mesh_emit(w, src, P, Pv, c0, u_split, nv, ctx->m_cubes[cur] + n_carry, s));
+    QJ_CUDA(ctx, qj::mesh_cube_scan(w, ctx->m_cubes[cur] + n_carry, nc, nt, s));
+    ctx->launches += nc > 0 ? 4 : 1;
     // per-vertex buffers grow to the vertex count extrapolated from the layers
     // meshed so far (+25%; at most 4x the count so far, and no more than the
     // caller's vertex capacity), so that a large mesh reallocates (cudaMalloc,
@@ -240,7 +243,6 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
     QJ_CUDA(ctx, span(1, 2, &st.ms_classify));
     QJ_CUDA(ctx, span(2, 3, &st.ms_vertices));
     QJ_CUDA(ctx, span(3, 4, &st.ms_triangles));
-    nt += tot.nt;
     prev_nc = nc;
     prevL = L;
     cur ^= 1;
@@ -248,6 +250,13 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
     c0 = c1;
   }
 
+  // the triangles of the last slab's cubes
+  if (st.slabs > 0) {
+    long long nt_last = 0;
+    QJ_CUDA(ctx, cudaMemcpyAsync(&nt_last, &ctx->m_tot->nt, sizeof nt_last, cudaMemcpyDeviceToHost, s));
+    QJ_CUDA(ctx, cudaStreamSynchronize(s));
+    nt += nt_last;
+  }
   // the parked edges of every slab, resolved together
   const bool any_parked = iter && iter->precision != QJG_FP64 && bisect && nv > 0;
   if (any_parked) {

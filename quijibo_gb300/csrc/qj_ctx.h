@@ -51,8 +51,8 @@ struct qjg_ctx {
   size_t m_field_cap = 0;
   uint32_t* m_bits = nullptr;   // activity bits of the classified planes
   size_t m_bits_cap = 0;
-  uint16_t* m_code = nullptr;   // sparse voxel codes of the classified planes
-  size_t m_code_cap = 0;
+  uint32_t* m_sign = nullptr;   // sign words of the window's planes
+  size_t m_sign_cap = 0;
   uint32_t* m_ucount = nullptr; // unit counts
   size_t m_ucount_cap = 0;
   qj::McTotals* m_tot = nullptr;

@@ -20,8 +20,9 @@ struct McCube {
 
 // Device-side counts of one slab's classification.
 struct McTotals {
-  long long nv, nt, nc;  // vertices, triangles, cubes with triangles of the slab
-  long long split;       // the slab's cube entries below its last cube layer
+  long long nv, nc;  // vertices and cubes with triangles of the slab
+  long long nt;      // triangles of the cubes of the last cube scan
+  long long split;   // the slab's cube entries below its last cube layer
 };
 
 // Scratch of one z-slab.  Window planes j <-> global plane c0 - 1 + j: edge
@@ -33,9 +34,9 @@ struct MeshWindow {
   uint8_t* masks = nullptr;
   int32_t* vbase = nullptr;
   uint32_t* list = nullptr;
-  long long* bsum = nullptr;  // 3 per scan block
-  uint32_t* bits = nullptr;
-  uint16_t* code = nullptr;
+  long long* bsum = nullptr;  // 2 per scan block
+  uint32_t* sign = nullptr;   // MESH_UNIT_WORDS per unit, every plane of the window
+  uint32_t* bits = nullptr;   // MESH_UNIT_WORDS per unit
   uint32_t* ucount = nullptr;
   McTotals* tot = nullptr;
 };
@@ -43,20 +44,24 @@ struct MeshWindow {
 long long mesh_scan_blocks(long long n);
 // classification units (row segments of one plane) of `planes` planes
 long long mesh_units(int X, int Y, int planes);
-// Words of activity bits per unit.
-constexpr int MESH_UNIT_WORDS = 8;
+// Words of activity bits per unit (64 voxels: even x, odd x).
+constexpr int MESH_UNIT_WORDS = 2;
 
 // Classify voxel planes [0, Pv) of src (P planes, global plane gz0 first;
-// Pv = P - 1, or P on the grid's last plane): codes, bits and unit counts,
-// their scan, the slab totals in w.tot (nv, nt, nc).
+// Pv = P - 1, or P on the grid's last plane): sign words of every plane,
+// activity words and unit counts, their scan, the slab totals in w.tot (nv,
+// nc).
 cudaError_t mesh_classify(const MeshWindow& w, const double* src, int P, int Pv, int gz0,
                           cudaStream_t s);
 // The slab's vertex ids, masks and edge list (window planes 1..Pv) and its
 // cube entries (written from `cubes`); u_split = the first unit of the last
 // cube layer (-1 on the last slab), whose entry offset goes to w.tot->split.
 cudaError_t mesh_emit(const MeshWindow& w, const double* src, int P, int Pv, int gz0,
-                      long long u_split, long long id0, long long t0, McCube* cubes,
-                      cudaStream_t s);
+                      long long u_split, long long id0, McCube* cubes, cudaStream_t s);
+// The first triangle of each of the nc cube entries (global index, from t0);
+// their triangle count goes to w.tot->nt.
+cudaError_t mesh_cube_scan(const MeshWindow& w, McCube* cubes, long long nc, long long t0,
+                           cudaStream_t s);
 // Triangles of cube entries [0, n_carry + split) (all on the last slab);
 // unless last, the remaining entries move to the front of `next`.
 cudaError_t mesh_triangles(const MeshWindow& w, const McCube* cubes, long long n_carry,
