@@ -198,6 +198,24 @@ int qjg_mesh_stream(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qj
                     int64_t vert_cap, int32_t* d_tris, int64_t tri_cap, qjg_mesh_stats* stats,
                     void* stream);
 
+/* Edge-cache bookkeeping of the meshers.  With capture on, qjg_mesh_stream
+ * and qjg_mesh_field keep, per call, the edge of every vertex (its two grid
+ * corners, in vertex order) and every cube whose corners are neither all
+ * inside nor all outside (flag and corner index, in scan order): the two
+ * lists of the reference's edge cache.  qjg_mesh_edge_cache_write writes the
+ * last captured call in the reference's cache-file format, byte for byte
+ * (TRIANGLE_MESH::writeEdgeCacheHuge, src/geometry/TRIANGLE_MESH.cpp:535-586,
+ * the file computeNonlinearMarchingCubesLowMemoryHuge (:681-768) leaves at
+ * the streaming constructor's cacheFilename): int count, 6 ints per edge;
+ * int count, 4 ints (flag, x, y, z) per cube.  qjg_mesh_edge_cache_read reads
+ * such a file (TRIANGLE_MESH::readEdgeCacheHuge, :431-482) into caller
+ * arrays (NULL arrays: counts only).  Capture costs one device-to-host copy
+ * of the vertices' edges and the cubes per slab. */
+int qjg_mesh_capture(qjg_ctx* ctx, int32_t on);
+int qjg_mesh_edge_cache_write(qjg_ctx* ctx, const char* path);
+int qjg_mesh_edge_cache_read(const char* path, int32_t* edges, int64_t edge_cap, int64_t* n_edges,
+                             int32_t* cubes, int64_t cube_cap, int64_t* n_cubes);
+
 /* ---- fitting energy and gradients ------------------------------------- */
 
 typedef struct {

@@ -31,6 +31,7 @@
 #include <vector>
 
 #include <cuda_runtime.h>
+#include <unistd.h>
 
 #include "OPTIMIZE_3D.h"
 #include "TRIANGLE_MESH.h"
@@ -181,6 +182,47 @@ void run_mesher(TRIANGLE_MESH* self, int64_t n_vox, Call call) {
   fill_mesh(self, out, st);
 }
 
+// The streaming mesher's edge cache (TRIANGLE_MESH.cpp:681-768): the
+// reference writes it after classifying when the file is absent
+// (writeEdgeCacheHuge, :535-586), and when it exists takes its cube flags and
+// edges instead of classifying again (readEdgeCacheHuge, :431-482).  Here the
+// grid is always classified on the GPU (it costs milliseconds); an absent
+// file is written with the same bytes, an existing one is compared with the
+// lists just computed and reported when it does not match them (a cache left
+// by another map or grid, which the reference would mesh from).
+std::vector<char> file_bytes(const std::string& path, bool* ok) {
+  std::vector<char> b;
+  *ok = false;
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) return b;
+  char buf[1 << 16];
+  size_t n;
+  while ((n = std::fread(buf, 1, sizeof buf, f)) > 0) b.insert(b.end(), buf, buf + n);
+  std::fclose(f);
+  *ok = true;
+  return b;
+}
+
+void edge_cache(const std::string& path) {
+  bool exists;
+  const std::vector<char> old = file_bytes(path, &exists);
+  if (!exists) {
+    const int rc = qjg_mesh_edge_cache_write(gpu(), path.c_str());
+    if (rc) std::printf(" FAILED TO CACHE OUT EDGES: %s\n", path.c_str());
+    return;
+  }
+  char tmp[] = "/tmp/qja_edgecacheXXXXXX";
+  const int fd = mkstemp(tmp);
+  if (fd < 0) return;
+  close(fd);
+  bool ok = qjg_mesh_edge_cache_write(gpu(), tmp) == 0;
+  const std::vector<char> now = ok ? file_bytes(tmp, &ok) : std::vector<char>();
+  unlink(tmp);
+  if (ok && now != old)
+    std::printf(" Cache file %s does not match this grid and map; the mesh is the recomputed one\n",
+                path.c_str());
+}
+
 // The state of the last GPU score, for the gradient calls that follow it.
 struct ScoreCache {
   std::vector<double> grad;  // [log s, bottom, top, sigma_t, sigma_b]
@@ -256,15 +298,20 @@ void qja_mesh_stream(TRIANGLE_MESH* self, const VEC3F& center, const VEC3F& leng
                      const VEC3I& res, const POLYNOMIAL_4D& top, const POLYNOMIAL_4D& bottom,
                      Real expScaling, int maxIterations, Real slice, Real isosurface,
                      const QUATERNION& rotation, const std::string& cacheFilename) {
-  (void)cacheFilename;  // the edge cache of the two-slab mesher has no use here
   const qjg_rootset h = upload(top, bottom, expScaling);
   const qjg_grid g = grid_of(res, center, lengths, rotation, slice);
   const qjg_iter it = iter_of(maxIterations, 2000.0, precision());
+  const bool cache = !cacheFilename.empty();
+  if (cache) qjg_mesh_capture(gpu(), 1);
   run_mesher(self, (int64_t)res[0] * res[1] * 8, [&](MeshOut& o, qjg_mesh_stats* st) {
     return qjg_mesh_stream(gpu(), h, &g, &it, (double)isosurface, 0, o.v, nullptr, o.vcap, o.t,
                            o.tcap, st, nullptr);
   });
   qjg_rootset_free(gpu(), h);
+  if (cache) {
+    edge_cache(cacheFilename);
+    qjg_mesh_capture(gpu(), 0);
+  }
 }
 
 // TRIANGLE_MESH(center, lengths, res, top, bottom, expScaling, maxIterations,

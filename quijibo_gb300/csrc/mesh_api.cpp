@@ -35,6 +35,39 @@ int grow_keep(qjg_ctx* ctx, T** buf, size_t* cap, size_t n, size_t keep, cudaStr
   return QJG_OK;
 }
 
+// Edge-cache capture of one slab: its vertices' edges (window-encoded list
+// entries: window voxel index * 4 + axis, window plane 0 = global c0 - 1)
+// and its new cube entries, appended in order.
+int capture_slab(qjg_ctx* ctx, const uint32_t* d_list, long long n_new, const qj::McCube* d_cubes,
+                 long long nc, int X, int Y, int c0, cudaStream_t s) {
+  std::vector<uint32_t> list((size_t)n_new);
+  std::vector<qj::McCube> cubes((size_t)nc);
+  if (n_new)
+    QJ_CUDA(ctx, cudaMemcpyAsync(list.data(), d_list, (size_t)n_new * sizeof(uint32_t),
+                                 cudaMemcpyDeviceToHost, s));
+  if (nc)
+    QJ_CUDA(ctx, cudaMemcpyAsync(cubes.data(), d_cubes, (size_t)nc * sizeof(qj::McCube),
+                                 cudaMemcpyDeviceToHost, s));
+  QJ_CUDA(ctx, cudaStreamSynchronize(s));
+  const long long XY = (long long)X * Y;
+  for (uint32_t e : list) {
+    const long long wv = e >> 2;
+    const int a = (int)(e & 3u);
+    const int z = c0 - 1 + (int)(wv / XY);
+    const int r = (int)(wv % XY);
+    const int p[3] = {r % X, r / X, z};
+    for (int k = 0; k < 3; k++) ctx->cap_edges.push_back(p[k]);
+    for (int k = 0; k < 3; k++) ctx->cap_edges.push_back(p[k] + (k == a));
+  }
+  for (const qj::McCube& q : cubes) {
+    ctx->cap_cubes.push_back((int32_t)(q.gzf >> 24));
+    ctx->cap_cubes.push_back((int32_t)(q.r % (uint32_t)X));
+    ctx->cap_cubes.push_back((int32_t)(q.r / (uint32_t)X));
+    ctx->cap_cubes.push_back((int32_t)(q.gzf & 0xFFFFFFu));
+  }
+  return QJG_OK;
+}
+
 int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter* iter,
               bool streaming, const double* d_field, int edge_mode, double iso, int slab_nz,
               double* v64, float* v32, int64_t vcap, int32_t* tris, int64_t tcap,
@@ -57,6 +90,8 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
   if (vcap < 0 || tcap < 0) return fail(ctx, QJG_ERR_ARG, "negative capacity");
   qjg_mesh_stats st;
   std::memset(&st, 0, sizeof st);
+  ctx->cap_edges.clear();
+  ctx->cap_cubes.clear();
 
   const int X = grid->res[0], Y = grid->res[1], Z = grid->res[2];
   const long long XY = (long long)X * Y;
@@ -198,6 +233,9 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
       return rc;
     const long long u_split = last ? -1 : (long long)(L - 1) * Y * S;
     QJ_CUDA(ctx, qj::mesh_emit(w, src, P, Pv, c0, u_split, nv, ctx->m_cubes[cur] + n_carry, s));
+    if (ctx->m_capture && (rc = capture_slab(ctx, w.list, n_new, ctx->m_cubes[cur] + n_carry, nc,
+                                             X, Y, c0, s)))
+      return rc;
     QJ_CUDA(ctx, qj::mesh_cube_scan(w, ctx->m_cubes[cur] + n_carry, nc, nt, s));
     ctx->launches += nc > 0 ? 4 : 1;
     // per-vertex buffers grow to the vertex count extrapolated from the layers
@@ -334,6 +372,51 @@ int qjg_mesh_stream(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qj
   if (!ctx) return QJG_ERR_ARG;
   return mesh_core(ctx, rs, grid, iter, true, nullptr, QJG_EDGE_BISECT, iso, slab_nz, d_verts64,
                    d_verts32, vert_cap, d_tris, tri_cap, stats, (cudaStream_t)stream);
+}
+
+int qjg_mesh_capture(qjg_ctx* ctx, int32_t on) {
+  if (!ctx) return QJG_ERR_ARG;
+  ctx->m_capture = on != 0;
+  return QJG_OK;
+}
+
+int qjg_mesh_edge_cache_write(qjg_ctx* ctx, const char* path) {
+  if (!ctx || !path) return QJG_ERR_ARG;
+  if (!ctx->m_capture) return fail(ctx, QJG_ERR_ARG, "edge capture is off (qjg_mesh_capture)");
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return fail(ctx, QJG_ERR_ARG, "cannot write %s", path);
+  const int32_t ne = (int32_t)(ctx->cap_edges.size() / 6), nc = (int32_t)(ctx->cap_cubes.size() / 4);
+  bool ok = std::fwrite(&ne, sizeof ne, 1, f) == 1 &&
+            std::fwrite(ctx->cap_edges.data(), sizeof(int32_t), ctx->cap_edges.size(), f) ==
+                ctx->cap_edges.size() &&
+            std::fwrite(&nc, sizeof nc, 1, f) == 1 &&
+            std::fwrite(ctx->cap_cubes.data(), sizeof(int32_t), ctx->cap_cubes.size(), f) ==
+                ctx->cap_cubes.size();
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? QJG_OK : fail(ctx, QJG_ERR_ARG, "short write to %s", path);
+}
+
+int qjg_mesh_edge_cache_read(const char* path, int32_t* edges, int64_t edge_cap, int64_t* n_edges,
+                             int32_t* cubes, int64_t cube_cap, int64_t* n_cubes) {
+  if (!path || !n_edges || !n_cubes) return QJG_ERR_ARG;
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return QJG_ERR_ARG;
+  int32_t ne = 0, nc = 0;
+  int rc = QJG_OK;
+  if (std::fread(&ne, sizeof ne, 1, f) != 1 || ne < 0) rc = QJG_ERR_ARG;
+  std::vector<int32_t> e(rc ? 0 : (size_t)ne * 6);
+  if (!rc && std::fread(e.data(), sizeof(int32_t), e.size(), f) != e.size()) rc = QJG_ERR_ARG;
+  if (!rc && (std::fread(&nc, sizeof nc, 1, f) != 1 || nc < 0)) rc = QJG_ERR_ARG;
+  std::vector<int32_t> c(rc ? 0 : (size_t)nc * 4);
+  if (!rc && std::fread(c.data(), sizeof(int32_t), c.size(), f) != c.size()) rc = QJG_ERR_ARG;
+  std::fclose(f);
+  if (rc) return rc;
+  *n_edges = ne;
+  *n_cubes = nc;
+  if ((edges && edge_cap < ne) || (cubes && cube_cap < nc)) return QJG_ERR_CAPACITY;
+  if (edges) std::memcpy(edges, e.data(), e.size() * sizeof(int32_t));
+  if (cubes) std::memcpy(cubes, c.data(), c.size() * sizeof(int32_t));
+  return QJG_OK;
 }
 
 }  // extern "C"

@@ -77,6 +77,11 @@ struct qjg_ctx {
   size_t m_epark_cap = 0;
   unsigned long long* m_ecount = nullptr;
   size_t m_ecount_cap = 0;
+  // edge-cache capture (qjg_mesh_capture): per vertex its edge's two corners
+  // (6 ints), per mixed cube (flag, x, y, z), of the last mesher call
+  bool m_capture = false;
+  std::vector<int32_t> cap_edges;
+  std::vector<int32_t> cap_cubes;
 };
 
 

@@ -193,6 +193,11 @@ EXPORTS = {
     "qjg_mesh_stream": ([C.c_void_p, C.c_int32, C.POINTER(QjgGrid), C.POINTER(QjgIter), C.c_double,
                          C.c_int32, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
                          C.POINTER(QjgMeshStats), C.c_void_p], C.c_int),
+    "qjg_mesh_capture": ([C.c_void_p, C.c_int32], C.c_int),
+    "qjg_mesh_edge_cache_write": ([C.c_void_p, C.c_char_p], C.c_int),
+    "qjg_mesh_edge_cache_read": ([C.c_char_p, C.POINTER(C.c_int32), C.c_int64,
+                                  C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.c_int64,
+                                  C.POINTER(C.c_int64)], C.c_int),
     "qjg_tanh_score_grad": ([C.c_void_p, C.c_int32, C.POINTER(QjgGrid), C.c_int32,
                              C.POINTER(QjgGrid), C.c_void_p, C.c_double, C.c_double, _dp, _dp,
                              C.c_void_p, C.POINTER(QjgTanhStats), C.c_void_p], C.c_int),
@@ -401,6 +406,23 @@ def o3d_write(path, rs, grid_res, center, lengths, fields, history=0):
                                    *data), "qjg_o3d_write")
 
 
+def mesh_edge_cache_read(path):
+    """(edges [n, 2, 3] corner pairs, cubes [m, 4] (flag, x, y, z)) of an edge-cache file."""
+    L = load()
+    ne, nc = C.c_int64(), C.c_int64()
+    rc = L.qjg_mesh_edge_cache_read(str(path).encode(), None, 0, C.byref(ne), None, 0, C.byref(nc))
+    if rc:
+        raise QjgError("qjg_mesh_edge_cache_read(%s) failed (%d)" % (path, rc))
+    e = np.zeros(6 * ne.value, dtype=np.int32)
+    c = np.zeros(4 * nc.value, dtype=np.int32)
+    rc = L.qjg_mesh_edge_cache_read(str(path).encode(), e.ctypes.data_as(C.POINTER(C.c_int32)),
+                                    ne.value, C.byref(ne), c.ctypes.data_as(C.POINTER(C.c_int32)),
+                                    nc.value, C.byref(nc))
+    if rc:
+        raise QjgError("qjg_mesh_edge_cache_read(%s) failed (%d)" % (path, rc))
+    return e.reshape(-1, 2, 3), c.reshape(-1, 4)
+
+
 def set_field32_pairs(on):
     """Process-wide FP32 bulk kernel form: True two voxels per lane (default)."""
     load().qjg_set_field32_pairs(int(bool(on)))
@@ -602,6 +624,15 @@ class Context:
         if check:
             self._check(rc, "qjg_mesh_stream")
         return rc, st.as_dict()
+
+    def mesh_capture(self, on=True):
+        """Keep each mesher call's edge-cache lists (qjg_mesh_capture)."""
+        self._check(self.L.qjg_mesh_capture(self.h, int(bool(on))), "qjg_mesh_capture")
+
+    def mesh_edge_cache_write(self, path):
+        """The last captured mesher call as the reference's edge-cache file."""
+        self._check(self.L.qjg_mesh_edge_cache_write(self.h, str(path).encode()),
+                    "qjg_mesh_edge_cache_write")
 
     def tanh_score_grad(self, handle, grid: Grid, max_it, wgrid: Grid, d_weights, n_params,
                         alpha=10.0, threshold=0.0, d_field=0, stream=None):
