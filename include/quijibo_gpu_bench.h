@@ -32,6 +32,17 @@ int64_t qjg_launch_count(qjg_ctx* ctx);
  * bits.  Set it while no field call is in flight. */
 int qjg_set_field32_pairs(int on);
 
+/* Process-wide choice of the squared-error energy's forward kernel, for A/B
+ * timing: 1 two samples per lane sharing one walk over the roots, 0 (the
+ * default) one sample per lane.  Set it while no energy call is in flight. */
+int qjg_set_energy_pairs(int on);
+
+/* Work of the last qjg_energy_forward/backward call on ctx: the map
+ * applications of its forward pass (orbit steps of every sample) and the
+ * orbit steps its adjoint ran back over (gradient samples only; 0 for a
+ * forward call): the units of the energy kernels' algorithmic FLOP counts. */
+int qjg_energy_last_work(qjg_ctx* ctx, int64_t* applications, int64_t* steps);
+
 /* FP32 FMA-pipe probe: runs a kernel of independent FMA chains on every SM
  * of `device` and returns the achieved FP32 TFLOP/s (2 flops per FMA). */
 int qjg_fma_probe(int device, double* tflops);

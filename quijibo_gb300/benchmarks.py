@@ -153,8 +153,13 @@ def bench_energy(args):
     G = torch.empty_like(P)
     n = len(t)
     out = {"samples": n, "params": int(P.numel()), "max_it": p["max_it"]}
+    from .roofline import energy_flops
+    peak = lib.fma_probe(0)
     forms = (("forward_fp32", lib.QJG_FP32, False), ("adjoint_fp32", lib.QJG_FP32, True),
              ("forward_fp64", lib.QJG_FP64, False), ("adjoint_fp64", lib.QJG_FP64, True))
+    if args.energy_pairs:
+        lib.set_energy_pairs(True)
+        out["forward_kernel"] = "two samples per lane"
     for name, prec, grad in forms[:2] if args.fp32_only else forms:
         kw = dict(precision=prec, d_grad=G.data_ptr() if grad else 0)
         ctx.energy(P.data_ptr(), rs.n_top, rs.n_bottom, n, X.data_ptr(), T.data_ptr(), p["max_it"],
@@ -167,6 +172,16 @@ def bench_energy(args):
                            p["max_it"], p["escape"], **kw)
         dt = (time.perf_counter() - t0) / reps
         out[name] = {"s": dt, "samples_per_s": n / dt, "energy": e}
+        # algorithmic work of the call (counted on the device) against the
+        # FP32 FMA probe: per-call wall time, so a lower bound of the kernels'
+        apps, steps = ctx.energy_last_work()
+        fl, sp = energy_flops(rs.n_top, rs.n_bottom, apps, steps)
+        out[name].update({"map_applications": apps, "adjoint_steps": steps,
+                          "root_terms": apps * (rs.n_top + rs.n_bottom), "flops": fl,
+                          "special_ops": sp, "tflops": fl / dt / 1e12})
+        if prec == lib.QJG_FP32:
+            out[name]["frac_fma_probe"] = fl / dt / 1e12 / peak
+    out["fma_probe_tflops"] = peak
     out["gradients_per_s"] = 1.0 / out["adjoint_fp32"]["s"]
     if args.steps <= 0:
         return out
@@ -636,6 +651,8 @@ def main():
     ap.add_argument("--no-mesh", action="store_true")
     ap.add_argument("--field-pass", action="store_true", help="large: also time the field alone")
     ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--energy-pairs", action="store_true",
+                    help="energy: the forward kernel with two samples per lane")
     ap.add_argument("--z0", type=int, default=-1, help="classify: first plane of the slab")
     ap.add_argument("--hbm-gbs", type=float, default=0.0,
                     help="HBM roofline denominator (default: MEASURED_PEAKS.json, else 6800)")

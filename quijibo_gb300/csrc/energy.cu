@@ -21,6 +21,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <atomic>
 #include <type_traits>
 
 #include "qj_device.cuh"
@@ -1000,6 +1001,150 @@ __global__ void __launch_bounds__(SQF_T) sq_fwd_kernel(
   }
 }
 
+// Two map applications that share the walk over the roots: the same
+// arithmetic as sq_apply for each of qa and qb, so each keeps its bits, with
+// the root constants read once and two independent dependency chains.
+template <class T>
+__device__ __forceinline__ void sq_apply2(const T* __restrict__ rp, const T* __restrict__ ep,
+                                          int nt, int nb, T s, V4<T>& qa, T* lga, V4<T>& qb,
+                                          T* lgb) {
+  V4<T> acc[2][2] = {{{T(1), T(0), T(0), T(0)}, {T(1), T(0), T(0), T(0)}},
+                     {{T(1), T(0), T(0), T(0)}, {T(1), T(0), T(0), T(0)}}};
+  V4<T> ga = {T(0), T(0), T(0), T(0)}, gb = ga;
+#pragma unroll
+  for (int side = 0; side < 2; side++) {
+    const int lo = side ? nt : 0, hi = side ? nt + nb : nt;
+    V4<T> a = acc[0][side], b = acc[1][side];
+    for (int i = lo; i < hi; i++) {
+      const T r0 = rp[4 * i], r1 = rp[4 * i + 1], r2 = rp[4 * i + 2], r3 = rp[4 * i + 3];
+      const T e = ep[i];
+      const V4<T> da{qa.w - r0, qa.x - r1, qa.y - r2, qa.z - r3};
+      const V4<T> db{qb.w - r0, qb.x - r1, qb.y - r2, qb.z - r3};
+      const T ka = (side ? -e : e) / v4dot(da, da);
+      const T kb = (side ? -e : e) / v4dot(db, db);
+      ga = v4add(ga, v4scale(da, ka));
+      gb = v4add(gb, v4scale(db, kb));
+      const V4<T> Pa = powv<T>(da, e, nullptr);
+      const V4<T> Pb = powv<T>(db, e, nullptr);
+      a = i == lo ? Pa : v4mul(a, Pa);
+      b = i == lo ? Pb : v4mul(b, Pb);
+    }
+    acc[0][side] = a;
+    acc[1][side] = b;
+  }
+  if (nb > 0) {
+    const V4<T> Wa = v4scale(v4conj(acc[0][1]), T(1) / v4dot(acc[0][1], acc[0][1]));
+    const V4<T> Wb = v4scale(v4conj(acc[1][1]), T(1) / v4dot(acc[1][1], acc[1][1]));
+    qa = v4scale(v4mul(acc[0][0], Wa), s);
+    qb = v4scale(v4mul(acc[1][0], Wb), s);
+  } else {
+    qa = v4scale(acc[0][0], s);
+    qb = v4scale(acc[1][0], s);
+  }
+  *lga = T(0.5) * log(v4dot(ga, ga));
+  *lgb = T(0.5) * log(v4dot(gb, gb));
+}
+
+// The forward pass with two samples per lane (slots 0 and 1), each refilled
+// as in sq_fwd_kernel; both slots step through one sq_apply2.  A slot without
+// a sample steps a dummy point whose results are not used.
+template <class T, bool GRAD>
+__global__ void __launch_bounds__(SQF_T) sq_fwd2_kernel(
+    const double* __restrict__ params, int nt, int nb, const double* __restrict__ xyz,
+    const double* __restrict__ target, long long n_samples, double slice, int max_it,
+    double escape, double d_sat, unsigned long long* __restrict__ claim, SqFwdOut<T> o) {
+  extern __shared__ unsigned char sh_raw[];
+  const int nr = nt + nb;
+  T* rp = reinterpret_cast<T*>(sh_raw);
+  T* ep = rp + 4 * nr;
+  for (int k = threadIdx.x; k < 4 * nr; k += SQF_T) rp[k] = (T)params[k];
+  for (int k = threadIdx.x; k < nr; k += SQF_T) ep[k] = (T)params[4 * nr + k];
+  __syncthreads();
+  const T s = (T)exp(params[5 * nr]);
+  const T esc = (T)escape, dsat = (T)d_sat;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  auto finish = [&](long long k, const V4<T>& q, T L, int n) {
+    const T m = sqrt(v4dot(q, q));
+    const T lm = log(m);
+    const T ld = log(fabs(lm)) + lm - L;
+    if (o.iters) o.iters[k] = n;
+    T val, dval, dval_dd;
+    sq_saturate<T>(lm, ld, dsat, &val, &dval, &dval_dd);
+    const T r = val - (T)target[k];
+    o.contrib[k] = (double)(r * r);
+    if (!GRAD) return;
+    int key = -1;
+    if (dval_dd != T(0)) {
+      const T db = T(2) * r * dval_dd;
+      const T kq = db * (lm + T(1)) * exp(ld - log(m) - log(fabs(lm)));
+      if (!isfinite(kq) || !isfinite(db * dval)) {
+        key = -2;
+      } else if (n > 0) {
+        o.seed_q[k] = v4scale(q, kq / m);
+        o.seed_L[k] = -db * dval;
+        key = n;
+      }
+    }
+    o.keys[k] = key;
+  };
+  long long k[2] = {0, 0};
+  bool live[2] = {false, false};
+  bool done = false;
+  V4<T> q[2] = {{T(0), T(0), T(0), T(0)}, {T(0), T(0), T(0), T(0)}};
+  T L[2] = {T(0), T(0)};
+  int n[2] = {0, 0};
+  for (;;) {
+#pragma unroll
+    for (int sl = 0; sl < 2; sl++) {
+      unsigned want = __ballot_sync(0xffffffffu, !live[sl] && !done);
+      while (want) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(claim, (unsigned long long)__popc(want));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (!live[sl] && !done) {
+          k[sl] = (long long)(base + __popc(want & lt));
+          if (k[sl] >= n_samples) {
+            done = true;
+          } else {
+            const long long kk = k[sl];
+            q[sl] = V4<T>{(T)xyz[3 * kk], (T)xyz[3 * kk + 1], (T)xyz[3 * kk + 2], (T)slice};
+            L[sl] = T(0);
+            n[sl] = 0;
+            if (sqrt(v4dot(q[sl], q[sl])) < esc && n[sl] < max_it)
+              live[sl] = true;
+            else
+              finish(kk, q[sl], L[sl], n[sl]);
+          }
+        }
+        want = __ballot_sync(0xffffffffu, !live[sl] && !done);
+      }
+    }
+    if (!__any_sync(0xffffffffu, live[0] || live[1])) break;
+#pragma unroll
+    for (int sl = 0; sl < 2; sl++)
+      if (GRAD && live[sl] && n[sl] % SQ_CK == 0)
+        o.ck[(long long)(n[sl] / SQ_CK) * n_samples + k[sl]] = q[sl];
+    V4<T> qa = live[0] ? q[0] : V4<T>{T(0.5), T(0.5), T(0.5), T(0.5)};
+    V4<T> qb = live[1] ? q[1] : V4<T>{T(0.5), T(0.5), T(0.5), T(0.5)};
+    T lga, lgb;
+    sq_apply2<T>(rp, ep, nt, nb, s, qa, &lga, qb, &lgb);
+#pragma unroll
+    for (int sl = 0; sl < 2; sl++) {
+      if (!live[sl]) continue;
+      const V4<T>& qn = sl ? qb : qa;
+      q[sl] = qn;
+      L[sl] += (sl ? lgb : lga) + T(0.5) * log(v4dot(qn, qn));
+      n[sl]++;
+      const T m = sqrt(v4dot(qn, qn));
+      if (!(m < esc && n[sl] < max_it) || m < T(1.1754943508e-37)) {
+        finish(k[sl], qn, L[sl], n[sl]);
+        live[sl] = false;
+      }
+    }
+  }
+}
+
 // Per chunk of SQ_CH samples: the energy and the left-out count summed in a
 // fixed tree (one partial row per chunk; the backward pass's rows follow, so a
 // chunk's row index, and with it the energy's bits, is the same with or
@@ -1008,25 +1153,38 @@ __global__ void __launch_bounds__(SQF_T) sq_fwd_kernel(
 // max_it - N so that long orbits come first: hist[bucket * nchunks + chunk].
 __global__ void __launch_bounds__(SQC_T) sq_chunk_kernel(const double* __restrict__ contrib,
                                                          const int* __restrict__ keys,
+                                                         const int* __restrict__ iters,
                                                          long long n, int max_it, int nchunks,
                                                          int* __restrict__ hist,
                                                          double* __restrict__ partials, int slots,
-                                                         int row0) {
+                                                         int row0,
+                                                         unsigned long long* __restrict__ work) {
   __shared__ double red_e[SQC_T], red_b[SQC_T];
   __shared__ int h[SQ_MAXIT + 1];
   const int c = blockIdx.x, t = threadIdx.x;
   for (int b = t; b <= max_it; b += SQC_T) h[b] = 0;
   __syncthreads();
   double e = 0.0, bad = 0.0;
+  unsigned long long apps = 0, steps = 0;  // map applications (forward), orbit steps (adjoint)
   for (int i = t; i < SQ_CH; i += SQC_T) {
     const long long k = (long long)c * SQ_CH + i;
     if (k >= n) break;
     e += contrib[k];
+    apps += (unsigned long long)iters[k];
     if (keys) {
       const int key = keys[k];
       if (key == -2) bad += 1.0;
-      else if (key > 0) atomicAdd(&h[max_it - key], 1);
+      else if (key > 0) {
+        atomicAdd(&h[max_it - key], 1);
+        steps += (unsigned long long)key;
+      }
     }
+  }
+  apps = __reduce_add_sync(0xffffffffu, (unsigned)apps);
+  steps = __reduce_add_sync(0xffffffffu, (unsigned)steps);
+  if ((t & 31) == 0 && (apps | steps)) {
+    atomicAdd(&work[0], apps);
+    atomicAdd(&work[1], steps);
   }
   red_e[t] = e;
   red_b[t] = bad;
@@ -1270,9 +1428,13 @@ __global__ void __launch_bounds__(256) sq_reduce_kernel(const double* __restrict
   if (lane == 0) out[k] = sum + c;
 }
 
+// Forward kernel choice (qjg_set_energy_pairs): two samples per lane or one.
+std::atomic<int> g_sq_pairs{0};
+
 // Byte layout of the energy scratch (each piece 256-byte aligned).
 struct SqLayout {
-  size_t claim, total, contrib, keys, perm, hist, seed_q, seed_L, ck, partials, out, bytes;
+  size_t claim, work, total, contrib, keys, iters, perm, hist, seed_q, seed_L, ck, partials, out,
+      bytes;
   int nchunks, nbwd, nck, slots;
 };
 
@@ -1291,9 +1453,11 @@ SqLayout sq_layout(bool fp64, bool grad, long long n, int max_it, int nt, int nb
   };
   const size_t nn = (size_t)std::max<long long>(n, 0);
   L.claim = take(sizeof(unsigned long long));
+  L.work = take(2 * sizeof(unsigned long long));
   L.total = take(sizeof(int));
   L.contrib = take(sizeof(double) * nn);
   L.keys = take(sizeof(int) * nn);
+  L.iters = take(sizeof(int) * nn);
   if (grad) {
     L.perm = take(sizeof(unsigned) * nn);
     L.hist = take(sizeof(int) * (size_t)(max_it + 1) * L.nchunks);
@@ -1326,13 +1490,15 @@ cudaError_t sq_launch(bool grad, const double* params, int nt, int nb, const dou
   SqFwdOut<T> o{};
   o.contrib = reinterpret_cast<double*>(scr + L.contrib);
   o.keys = reinterpret_cast<int*>(scr + L.keys);
-  o.iters = iters;
+  o.iters = iters ? iters : reinterpret_cast<int*>(scr + L.iters);
+  unsigned long long* work = reinterpret_cast<unsigned long long*>(scr + L.work);
   if (grad) {
     o.seed_q = reinterpret_cast<V4<T>*>(scr + L.seed_q);
     o.seed_L = reinterpret_cast<T*>(scr + L.seed_L);
     o.ck = reinterpret_cast<V4<T>*>(scr + L.ck);
   }
   cudaError_t e = cudaMemsetAsync(claim, 0, sizeof(unsigned long long), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(work, 0, 2 * sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
   const size_t sh_roots = sizeof(T) * 5 * nr;
   // persistent forward grid: as many blocks as stay resident
@@ -1351,15 +1517,23 @@ cudaError_t sq_launch(bool grad, const double* params, int nt, int nb, const dou
   const long long need = (n + SQF_T - 1) / SQF_T;
   const int fblocks = (int)std::max<long long>(
       1, std::min<long long>((long long)sms * std::min<long long>(std::max(per_sm, 1), want), need));
-  if (grad)
+  if (g_sq_pairs.load(std::memory_order_relaxed)) {
+    if (grad)
+      sq_fwd2_kernel<T, true><<<fblocks, SQF_T, sh_roots, s>>>(params, nt, nb, xyz, target, n,
+                                                               slice, max_it, escape, d_sat, claim, o);
+    else
+      sq_fwd2_kernel<T, false><<<fblocks, SQF_T, sh_roots, s>>>(params, nt, nb, xyz, target, n,
+                                                                slice, max_it, escape, d_sat, claim, o);
+  } else if (grad) {
     sq_fwd_kernel<T, true><<<fblocks, SQF_T, sh_roots, s>>>(params, nt, nb, xyz, target, n, slice,
                                                             max_it, escape, d_sat, claim, o);
-  else
+  } else {
     sq_fwd_kernel<T, false><<<fblocks, SQF_T, sh_roots, s>>>(params, nt, nb, xyz, target, n, slice,
                                                              max_it, escape, d_sat, claim, o);
+  }
   int* hist = grad ? reinterpret_cast<int*>(scr + L.hist) : nullptr;
-  sq_chunk_kernel<<<L.nchunks, SQC_T, 0, s>>>(o.contrib, grad ? o.keys : nullptr, n, max_it,
-                                              L.nchunks, hist, partials, L.slots, 0);
+  sq_chunk_kernel<<<L.nchunks, SQC_T, 0, s>>>(o.contrib, grad ? o.keys : nullptr, o.iters, n,
+                                              max_it, L.nchunks, hist, partials, L.slots, 0, work);
   *launches = 3;
   if (grad) {
     unsigned* perm = reinterpret_cast<unsigned*>(scr + L.perm);
@@ -1382,6 +1556,8 @@ cudaError_t sq_launch(bool grad, const double* params, int nt, int nb, const dou
 
 int sq_max_iterations() { return SQ_MAXIT; }
 
+void set_energy_pairs(int on) { g_sq_pairs.store(on ? 1 : 0); }
+
 size_t sq_scratch_bytes(bool fp64, bool grad, long long n, int max_it, int nt, int nb) {
   return sq_layout(fp64, grad, n, max_it, nt, nb, sm_count()).bytes;
 }
@@ -1389,11 +1565,13 @@ size_t sq_scratch_bytes(bool fp64, bool grad, long long n, int max_it, int nt, i
 cudaError_t launch_sq_energy(bool fp64, bool grad, const double* params, int nt, int nb,
                              const double* xyz, const double* target, long long n, double slice,
                              int max_it, double escape, double d_sat, void* scratch,
-                             double** out, int* iters, cudaStream_t s, int* launches) {
+                             double** out, int* iters, cudaStream_t s, int* launches,
+                             unsigned long long** work) {
   const int sms = sm_count();
   const SqLayout L = sq_layout(fp64, grad, n, max_it, nt, nb, sms);
   unsigned char* scr = static_cast<unsigned char*>(scratch);
   *out = reinterpret_cast<double*>(scr + L.out);
+  *work = reinterpret_cast<unsigned long long*>(scr + L.work);
   if (fp64)
     return sq_launch<double>(grad, params, nt, nb, xyz, target, n, slice, max_it, escape, d_sat,
                              scr, L, iters, sms, s, launches);

@@ -7,6 +7,7 @@
 #include <cstring>
 #include <vector>
 
+#include "../../include/quijibo_gpu_bench.h"
 #include "qj_ctx.h"
 #include "qj_energy.h"
 #include "qj_lbfgs.h"
@@ -28,6 +29,18 @@ qj::WeightGrid qj_weight_grid(const qjg_grid* g) {
 }
 
 extern "C" {
+
+int qjg_set_energy_pairs(int on) {
+  qj::set_energy_pairs(on);
+  return QJG_OK;
+}
+
+int qjg_energy_last_work(qjg_ctx* ctx, int64_t* applications, int64_t* steps) {
+  if (!ctx || !applications || !steps) return QJG_ERR_ARG;
+  *applications = ctx->sq_applications;
+  *steps = ctx->sq_steps;
+  return QJG_OK;
+}
 
 int qjg_tanh_score_grad(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, int32_t max_it,
                         const qjg_grid* weight_grid, const double* d_weights, double alpha,
@@ -92,9 +105,14 @@ static int sq_energy(qjg_ctx* ctx, const double* d_params, int32_t nt, int32_t n
   void* d_scr = nullptr;
   QJ_CUDA(ctx, cudaMallocAsync(&d_scr, qj::sq_scratch_bytes(fp64, grad, n, max_it, nt, nb), s));
   double* d_out = nullptr;
+  unsigned long long* d_work = nullptr;
   int launched = 0;
   cudaError_t e = qj::launch_sq_energy(fp64, grad, d_params, nt, nb, d_xyz, d_target, n, slice,
-                                       max_it, escape, d_sat, d_scr, &d_out, d_iters, s, &launched);
+                                       max_it, escape, d_sat, d_scr, &d_out, d_iters, s, &launched,
+                                       &d_work);
+  unsigned long long work[2] = {0, 0};
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(work, d_work, sizeof work, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess && d_grad)
     e = cudaMemcpyAsync(d_grad, d_out + 1, sizeof(double) * P, cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(energy, d_out, sizeof(double), cudaMemcpyDeviceToHost, s);
@@ -102,6 +120,8 @@ static int sq_energy(qjg_ctx* ctx, const double* d_params, int32_t nt, int32_t n
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return fail(ctx, QJG_ERR_CUDA, "energy: %s", cudaGetErrorString(e));
   ctx->launches += launched;
+  ctx->sq_applications = (int64_t)work[0];
+  ctx->sq_steps = (int64_t)work[1];
   return QJG_OK;
 }
 

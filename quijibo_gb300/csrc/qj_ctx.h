@@ -45,6 +45,8 @@ struct qjg_ctx {
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
   cudaEvent_t mev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // mesher phases
   int64_t launches = 0;
+  int64_t sq_applications = 0;  // work of the last energy call: forward map applications
+  int64_t sq_steps = 0;         // ... and adjoint orbit steps
   // marching-cubes scratch
   qj::DevStats* d_mstats = nullptr;
   double* m_field = nullptr;    // slab field window

@@ -25,9 +25,14 @@ int sq_max_iterations();
 size_t sq_scratch_bytes(bool fp64, bool grad, long long n, int max_it, int nt, int nb);
 // *out (in the scratch): [energy, gradient (5 (nt + nb) + 1), samples left
 // out of the gradient]; *launches: kernels launched.
+// process-wide choice of the energy forward kernel: 1 two samples per lane
+void set_energy_pairs(int on);
+// *work: two counters in the scratch, the map applications of the forward
+// pass and the orbit steps of the adjoint (read after the call completes)
 cudaError_t launch_sq_energy(bool fp64, bool grad, const double* params, int nt, int nb,
                              const double* xyz, const double* target, long long n, double slice,
                              int max_it, double escape, double d_sat, void* scratch,
-                             double** out, int* iters, cudaStream_t s, int* launches);
+                             double** out, int* iters, cudaStream_t s, int* launches,
+                             unsigned long long** work);
 
 }  // namespace qj

@@ -193,6 +193,8 @@ EXPORTS = {
     "qjg_mesh_stream": ([C.c_void_p, C.c_int32, C.POINTER(QjgGrid), C.POINTER(QjgIter), C.c_double,
                          C.c_int32, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
                          C.POINTER(QjgMeshStats), C.c_void_p], C.c_int),
+    "qjg_set_energy_pairs": ([C.c_int], C.c_int),
+    "qjg_energy_last_work": ([C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)], C.c_int),
     "qjg_mesh_capture": ([C.c_void_p, C.c_int32], C.c_int),
     "qjg_mesh_edge_cache_write": ([C.c_void_p, C.c_char_p], C.c_int),
     "qjg_mesh_edge_cache_read": ([C.c_char_p, C.POINTER(C.c_int32), C.c_int64,
@@ -423,6 +425,11 @@ def mesh_edge_cache_read(path):
     return e.reshape(-1, 2, 3), c.reshape(-1, 4)
 
 
+def set_energy_pairs(on):
+    """Energy forward kernel: two samples per lane (True) or one (False)."""
+    load().qjg_set_energy_pairs(int(bool(on)))
+
+
 def set_field32_pairs(on):
     """Process-wide FP32 bulk kernel form: True two voxels per lane (default)."""
     load().qjg_set_field32_pairs(int(bool(on)))
@@ -624,6 +631,13 @@ class Context:
         if check:
             self._check(rc, "qjg_mesh_stream")
         return rc, st.as_dict()
+
+    def energy_last_work(self):
+        """(forward map applications, adjoint orbit steps) of the last energy call."""
+        a, b = C.c_int64(), C.c_int64()
+        self._check(self.L.qjg_energy_last_work(self.h, C.byref(a), C.byref(b)),
+                    "qjg_energy_last_work")
+        return a.value, b.value
 
     def mesh_capture(self, on=True):
         """Keep each mesher call's edge-cache lists (qjg_mesh_capture)."""

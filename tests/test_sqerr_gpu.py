@@ -186,3 +186,28 @@ def test_energy_sizes_split_and_repeat(ctx, precision):
     assert ew2 == ew and np.array_equal(gw2, gw)
     # the forward alone gives the energy of the gradient call
     assert run(0, len(t), grad=False)[0] == ew
+
+
+@pytest.mark.parametrize("precision", [lib.QJG_FP32, lib.QJG_FP64])
+def test_forward_with_two_samples_per_lane(ctx, precision):
+    """The forward kernel with two samples per lane runs the same orbits:
+    the same map applications and adjoint steps, the energy and gradient
+    within rounding of the one-sample kernel's."""
+    rs, xyz, t = small_case(n=3000)
+    p = dev(lib.params_of(rs))
+    X, T = dev(xyz), dev(t)
+    out = []
+    try:
+        for pairs in (False, True):
+            lib.set_energy_pairs(pairs)
+            g = torch.empty(len(p), dtype=torch.float64, device="cuda")
+            e = ctx.energy(p.data_ptr(), rs.n_top, rs.n_bottom, len(t), X.data_ptr(), T.data_ptr(),
+                           10, 2.0, precision=precision, d_grad=g.data_ptr())
+            out.append((e, g.cpu().numpy(), ctx.energy_last_work()))
+    finally:
+        lib.set_energy_pairs(False)
+    (e0, g0, w0), (e1, g1, w1) = out
+    assert w0 == w1 and w0[0] > 0 and w0[1] > 0
+    tol = 1e-5 if precision == lib.QJG_FP32 else 1e-12
+    assert abs(e1 - e0) <= tol * abs(e0)
+    assert np.linalg.norm(g1 - g0) <= tol * np.linalg.norm(g0)
