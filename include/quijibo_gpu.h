@@ -66,7 +66,7 @@ typedef struct {
                         if still above it, in FP64.  0 = the band rule alone. */
   int32_t form;      /* QJG_FORM_QUOTIENT: T(q) / B(q) (computeLogScaledPowerRationalMap);
                         QJG_FORM_LAGRANGE: RATIONAL_4D::evaluateLagrange order, top and bottom
-                        factors interleaved (RATIONAL_4D.cpp:27-73; QJG_FP64 only) */
+                        factors interleaved (RATIONAL_4D.cpp:27-73), in every precision form */
   int32_t pad_;
 } qjg_iter;
 

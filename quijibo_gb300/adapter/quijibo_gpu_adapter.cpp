@@ -316,7 +316,7 @@ void qja_mesh_stream(TRIANGLE_MESH* self, const VEC3F& center, const VEC3F& leng
 
 // TRIANGLE_MESH(center, lengths, res, top, bottom, expScaling, maxIterations,
 // slice, isosurface, rotation): the Lagrange streaming mesher
-// (TRIANGLE_MESH.cpp:106-123), always in the FP64 form.
+// (TRIANGLE_MESH.cpp:106-123), in the form QJG_PRECISION selects.
 void qja_mesh_lagrange(TRIANGLE_MESH* self, const VEC3F& center, const VEC3F& lengths,
                        const VEC3I& res, const POLYNOMIAL_4D& top, const POLYNOMIAL_4D& bottom,
                        Real expScaling, int maxIterations, Real slice, Real isosurface,
@@ -327,7 +327,7 @@ void qja_mesh_lagrange(TRIANGLE_MESH* self, const VEC3F& center, const VEC3F& le
                        const QUATERNION& rotation) {
   const qjg_rootset h = upload(top, bottom, expScaling);
   const qjg_grid g = grid_of(res, center, lengths, rotation, slice);
-  qjg_iter it = iter_of(maxIterations, 2000.0, QJG_FP64);
+  qjg_iter it = iter_of(maxIterations, 2000.0, precision());
   it.form = QJG_FORM_LAGRANGE;
   run_mesher(self, (int64_t)res[0] * res[1] * 8, [&](MeshOut& o, qjg_mesh_stats* st) {
     return qjg_mesh_stream(gpu(), h, &g, &it, (double)isosurface, 0, o.v, nullptr, o.vcap, o.t,

@@ -6,6 +6,7 @@ which measures the headline field).  Each prints one JSON object.
     python -m quijibo_gb300.benchmarks serve  [--requests 400] [--scale 0.25]
     python -m quijibo_gb300.benchmarks large  [--res 2200] [--slab 64] [--check-slices 4]
     python -m quijibo_gb300.benchmarks classify [--res 2200] [--slab 64] [--reps 5]
+    python -m quijibo_gb300.benchmarks lagrange [--res 256]
 
 All inputs are synthetic (quijibo_gb300/rootsets.py, samples.py).
 """
@@ -132,6 +133,50 @@ def bench_classify(args):
            "ms_classify": cls, "ms_triangles": tri, "ms_vertices": st["ms_vertices"],
            "algorithmic_bytes": alg, "gb_s": alg / ((cls + tri) * 1e-3) / 1e9,
            "frac_hbm": alg / ((cls + tri) * 1e-3) / 1e9 / args.hbm_gbs, "hbm_peak_gb_s": args.hbm_gbs}
+    ctx.free(h)
+    ctx.close()
+    return out
+
+
+def bench_lagrange(args):
+    """The Lagrange order of the map (RATIONAL_4D::evaluateLagrange, the
+    lagrangeBunny3D driver's) on the precision workload's map (16 top / 8
+    bottom roots, 40 iterations, escape 2) at res^3: the plain FP64 form
+    against the precision form (FP32 bulk, double-float re-run at rel_tol,
+    FP64 band): time, sign map, error."""
+    import torch
+
+    from . import lib
+    from .rootsets import precision_workload
+    ctx = lib.Context(0)
+    res = args.res or 256
+    rs, g, p = precision_workload(res)
+    h = ctx.upload(rs)
+    n = g.n_voxels
+    a = torch.empty(n, dtype=torch.float64, device="cuda")
+    b = torch.empty(n, dtype=torch.float64, device="cuda")
+    forms = {"fp64": ctx.iter_params(p["max_it"], p["escape"], refine_pow=lib.QJG_REFINE_INT,
+                                     lagrange=True),
+             "fp32_refine": ctx.iter_params(p["max_it"], p["escape"], precision=lib.QJG_FP32_REFINE,
+                                            refine_pow=lib.QJG_REFINE_INT, rel_tol=args.rel_tol,
+                                            lagrange=True)}
+    out = {"workload": "Lagrange order, precision workload map, %d^3, 40 iterations" % res,
+           "voxels": n, "rel_tol": args.rel_tol}
+    for name, it in forms.items():
+        buf = a if name == "fp64" else b
+        ctx.field(h, g, it, buf.data_ptr())  # warm
+        torch.cuda.synchronize()
+        e0, e1 = _events(torch)
+        e0.record()
+        ctx.field(h, g, it, buf.data_ptr())
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[name] = {"ms": ms, "gvox_s": n / (ms * 1e-3) / 1e9, "stats": ctx.stats()}
+    rel = (b - a).abs() / a.abs().clamp_min(1e-300)
+    out["sign_map_disagreements"] = int(((a > 0) != (b > 0)).sum().item())
+    out["max_rel_err"] = float(rel.max().item())
+    out["speedup"] = out["fp64"]["ms"] / out["fp32_refine"]["ms"]
     ctx.free(h)
     ctx.close()
     return out
@@ -630,7 +675,7 @@ def bench_tanh(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("what", choices=["mesh", "energy", "serve", "large", "tooth", "tanh",
-                                     "classify"])
+                                     "classify", "lagrange"])
     ap.add_argument("--res", type=int, default=0, help="grid edge (mesh: 512, large: 2200)")
     ap.add_argument("--workload", default="precision", choices=["precision", "large"])
     ap.add_argument("--slab", type=int, default=64)
@@ -660,7 +705,7 @@ def main():
     args.hbm_gbs = args.hbm_gbs or hbm_peak_gbs()[0]
     fn = {"mesh": bench_mesh, "energy": bench_energy, "serve": bench_serve,
           "large": bench_large, "tooth": bench_tooth, "tanh": bench_tanh,
-          "classify": bench_classify}[args.what]
+          "classify": bench_classify, "lagrange": bench_lagrange}[args.what]
     print(json.dumps(fn(args)), flush=True)
 
 

@@ -108,8 +108,6 @@ int qj_check_iter(qjg_ctx* ctx, const qjg_iter* it) {
     return fail(ctx, QJG_ERR_ARG, "unknown refine_pow %d", it->refine_pow);
   if (it->form != QJG_FORM_QUOTIENT && it->form != QJG_FORM_LAGRANGE)
     return fail(ctx, QJG_ERR_ARG, "unknown form %d", it->form);
-  if (it->form == QJG_FORM_LAGRANGE && it->precision != QJG_FP64)
-    return fail(ctx, QJG_ERR_ARG, "the Lagrange form is computed in the plain FP64 form only");
   return QJG_OK;
 }
 
@@ -270,7 +268,16 @@ int qjg_rootset_free(qjg_ctx* ctx, qjg_rootset rs) {
 int qjg_field(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter* iter,
               int32_t z0, int32_t z1, double* d_field, float* d_de, void* stream) {
   if (!ctx) return QJG_ERR_ARG;
-  const MapParams* m = qj_lookup(ctx, rs);
+  const MapParams* m0 = qj_lookup(ctx, rs);
+  // the Lagrange order rides with the launch copy of the map (FP32 and
+  // double-float tiers); the resident map keeps the quotient default
+  std::unique_ptr<MapParams> mcopy;
+  const MapParams* m = m0;
+  if (m0 && iter && iter->form == QJG_FORM_LAGRANGE) {
+    mcopy.reset(new MapParams(*m0));
+    mcopy->lagrange = 1;
+    m = mcopy.get();
+  }
   if (!m) return fail(ctx, QJG_ERR_HANDLE, "unknown root set %d", rs);
   int rc;
   if ((rc = qj_check_grid(ctx, grid)) || (rc = qj_check_iter(ctx, iter))) return rc;

@@ -643,7 +643,9 @@ cudaError_t launch_field32(const MapParams& m, const GridParams& g, const IterPa
     else                                                                                   \
       field32x2_kernel<false, NT, NB><<<blocks, 128, 0, s>>>(m, g, it, field, de, rl, 0, st); \
   } while (0)
-    if (m.nt == 16 && m.nb == 8)
+    if (m.lagrange)
+      QJ_F32X2(0, 0);
+    else if (m.nt == 16 && m.nb == 8)
       QJ_F32X2(16, 8);
     else if (m.nt == 8 && m.nb == 0)
       QJ_F32X2(8, 0);

@@ -76,6 +76,8 @@ extern "C" int qjg_field_noalloc(int32_t n_top, const double* top_roots, const d
                   sigma_bot, scale) >= 0)
     return QJG_ERR_ARG;
 
+  m.lagrange = iter->form == QJG_FORM_LAGRANGE ? 1 : 0;
+
   unsigned char* scratch = nullptr;
   if ((rc = scratch_for_current_device(&scratch))) return rc;
   qj::DevStats* st = reinterpret_cast<qj::DevStats*>(scratch);

@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <memory>
 
 #include "../../include/quijibo_gpu_bench.h"
 #include "qj_ctx.h"
@@ -80,10 +81,16 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
   MapParams zero_map;
   std::memset(&zero_map, 0, sizeof zero_map);
   const MapParams* m = &zero_map;
+  std::unique_ptr<MapParams> mcopy;  // the Lagrange order rides with a launch copy
   if (bisect || streaming) {
     m = qj_lookup(ctx, rs);
     if (!m) return fail(ctx, QJG_ERR_HANDLE, "unknown root set %d", rs);
     if ((rc = qj_check_iter(ctx, iter))) return rc;
+    if (iter->form == QJG_FORM_LAGRANGE) {
+      mcopy.reset(new MapParams(*m));
+      mcopy->lagrange = 1;
+      m = mcopy.get();
+    }
   }
   if (!streaming && !d_field) return fail(ctx, QJG_ERR_ARG, "d_field is NULL");
   if (!tris) return fail(ctx, QJG_ERR_ARG, "d_tris is NULL");

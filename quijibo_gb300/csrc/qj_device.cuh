@@ -502,10 +502,47 @@ __device__ __forceinline__ q32::Q product32(const MapParams& m, const q32::Q& q,
   return r;
 }
 
+// RATIONAL_4D::evaluateLagrange's order in FP32 (RATIONAL_4D.cpp:27-73):
+// times top term k, then divided by bottom term k (r conj(b) / |b|^2) for
+// the common k, then the longer side's leftovers; with bottom roots only.
+template <bool DE>
+__device__ __forceinline__ q32::Q lagrange32(const MapParams& m, const q32::Q& q, q32::Q& g) {
+  using namespace q32;
+  const int same = m.nt < m.nb ? m.nt : m.nb;
+  auto divide = [&](const Q& r, int i) {
+    const Q b = root_term32<DE>(m, q, i, g);
+    const float inv = rcp_approx(norm2(b));
+    Q o = qmul_conj(r, b);
+    o.w *= inv;
+    o.x *= inv;
+    o.y *= inv;
+    o.z *= inv;
+    return o;
+  };
+  Q r = root_term32<DE>(m, q, 0, g);
+  r = divide(r, m.nt);
+#pragma unroll 1
+  for (int k = 1; k < same; k++) r = divide(qmul(r, root_term32<DE>(m, q, k, g)), m.nt + k);
+#pragma unroll 1
+  for (int k = same; k < m.nt; k++) r = qmul(r, root_term32<DE>(m, q, k, g));
+#pragma unroll 1
+  for (int k = same; k < m.nb; k++) r = divide(r, m.nt + k);
+  return r;
+}
+
 template <bool DE>
 __device__ __forceinline__ q32::Q apply32(const MapParams& m, const q32::Q& q, float* g2) {
   using namespace q32;
   Q g = {0.f, 0.f, 0.f, 0.f};
+  if (m.lagrange && m.nb > 0) {
+    Q out = lagrange32<DE>(m, q, g);
+    out.w *= m.scalef;
+    out.x *= m.scalef;
+    out.y *= m.scalef;
+    out.z *= m.scalef;
+    if (DE) *g2 = norm2(g);
+    return out;
+  }
   const Q top = product32<DE>(m, q, 0, m.nt, g);
   Q out;
   if (m.nb > 0) {
@@ -595,13 +632,51 @@ __device__ __forceinline__ q32x2::Q2 product32x2_fixed(const MapParams& m, const
   return r;
 }
 
+// lagrange32 on a voxel pair
+template <bool DE>
+__device__ __forceinline__ q32x2::Q2 lagrange32x2(const MapParams& m, const q32x2::Q2& q,
+                                                  q32x2::Q2& g) {
+  using namespace q32x2;
+  const int same = m.nt < m.nb ? m.nt : m.nb;
+  auto divide = [&](const Q2& r, int i) {
+    const Q2 b = root_term32x2<DE>(m, q, i, g);
+    const float2 n = norm2(b);
+    const float2 inv = make_float2(q32::rcp_approx(n.x), q32::rcp_approx(n.y));
+    Q2 o = qmul_conj(r, b);
+    o.w = mul2(o.w, inv);
+    o.x = mul2(o.x, inv);
+    o.y = mul2(o.y, inv);
+    o.z = mul2(o.z, inv);
+    return o;
+  };
+  Q2 r = root_term32x2<DE>(m, q, 0, g);
+  r = divide(r, m.nt);
+#pragma unroll 1
+  for (int k = 1; k < same; k++) r = divide(qmul(r, root_term32x2<DE>(m, q, k, g)), m.nt + k);
+#pragma unroll 1
+  for (int k = same; k < m.nt; k++) r = qmul(r, root_term32x2<DE>(m, q, k, g));
+#pragma unroll 1
+  for (int k = same; k < m.nb; k++) r = divide(r, m.nt + k);
+  return r;
+}
+
 // NT, NB > 0: the root counts are compile-time constants (they must equal
-// m.nt and m.nb); 0: read from m.
+// m.nt and m.nb; the quotient order only); 0: read from m.
 template <bool DE, int NT = 0, int NB = 0>
 __device__ __forceinline__ q32x2::Q2 apply32x2(const MapParams& m, const q32x2::Q2& q,
                                                float2* g2) {
   using namespace q32x2;
   Q2 g = {pair(0.f), pair(0.f), pair(0.f), pair(0.f)};
+  if (NT == 0 && m.lagrange && m.nb > 0) {
+    Q2 out = lagrange32x2<DE>(m, q, g);
+    const float2 s = pair(m.scalef);
+    out.w = mul2(out.w, s);
+    out.x = mul2(out.x, s);
+    out.y = mul2(out.y, s);
+    out.z = mul2(out.z, s);
+    if (DE) *g2 = norm2(g);
+    return out;
+  }
   const Q2 top = NT > 0 ? product32x2_fixed<DE, 0, (NT > 0 ? NT : 1)>(m, q, g)
                         : product32x2<DE>(m, q, 0, m.nt, g);
   Q2 out;

@@ -208,12 +208,48 @@ __device__ __forceinline__ qff::Q product_ff(const MapParams& m, const qff::Q& q
   return r;
 }
 
+// The Lagrange order (lagrange32) in double-float.
+template <bool DE>
+__device__ __forceinline__ qff::Q lagrange_ff(const MapParams& m, const qff::Q& q, q32::Q& g) {
+  using namespace qff;
+  const int same = m.nt < m.nb ? m.nt : m.nb;
+  auto divide = [&](const Q& r, int i) {
+    const Q b = root_term_ff<DE>(m, q, i, g);
+    const F inv = recip(norm2(b));
+    Q o = qmul_conj(r, b);
+    o.w = mul(o.w, inv);
+    o.x = mul(o.x, inv);
+    o.y = mul(o.y, inv);
+    o.z = mul(o.z, inv);
+    return o;
+  };
+  Q r = root_term_ff<DE>(m, q, 0, g);
+  r = divide(r, m.nt);
+#pragma unroll 1
+  for (int k = 1; k < same; k++) r = divide(qmul(r, root_term_ff<DE>(m, q, k, g)), m.nt + k);
+#pragma unroll 1
+  for (int k = same; k < m.nt; k++) r = qmul(r, root_term_ff<DE>(m, q, k, g));
+#pragma unroll 1
+  for (int k = same; k < m.nb; k++) r = divide(r, m.nt + k);
+  return r;
+}
+
 // One map application in double-float; *g2 = |grad log|R||^2 in FP32.
 // Requires m.all_int (integer effective exponents).
 template <bool DE>
 __device__ __forceinline__ qff::Q apply_ff(const MapParams& m, const qff::Q& q, float* g2) {
   using namespace qff;
   q32::Q g = {0.f, 0.f, 0.f, 0.f};
+  if (m.lagrange && m.nb > 0) {
+    Q out = lagrange_ff<DE>(m, q, g);
+    const F s = {m.scale_ff[0], m.scale_ff[1]};
+    out.w = mul(out.w, s);
+    out.x = mul(out.x, s);
+    out.y = mul(out.y, s);
+    out.z = mul(out.z, s);
+    if (DE) *g2 = q32::norm2(g);
+    return out;
+  }
   const Q top = product_ff<DE>(m, q, 0, m.nt, g);
   Q out;
   if (m.nb > 0) {
@@ -453,13 +489,49 @@ __device__ __forceinline__ qff2::Q product_ff2(const MapParams& m, const qff2::Q
   return r;
 }
 
+// lagrange_ff for two voxels
+template <bool DE>
+__device__ __forceinline__ qff2::Q lagrange_ff2(const MapParams& m, const qff2::Q& q,
+                                                q32x2::Q2& g) {
+  using namespace qff2;
+  const int same = m.nt < m.nb ? m.nt : m.nb;
+  auto divide = [&](const Q& r, int i) {
+    const Q b = root_term_ff2<DE>(m, q, i, g);
+    const F2 inv = recip(norm2(b));
+    Q o = qmul_conj(r, b);
+    o.w = mul(o.w, inv);
+    o.x = mul(o.x, inv);
+    o.y = mul(o.y, inv);
+    o.z = mul(o.z, inv);
+    return o;
+  };
+  Q r = root_term_ff2<DE>(m, q, 0, g);
+  r = divide(r, m.nt);
+#pragma unroll 1
+  for (int k = 1; k < same; k++) r = divide(qmul(r, root_term_ff2<DE>(m, q, k, g)), m.nt + k);
+#pragma unroll 1
+  for (int k = same; k < m.nt; k++) r = qmul(r, root_term_ff2<DE>(m, q, k, g));
+#pragma unroll 1
+  for (int k = same; k < m.nb; k++) r = divide(r, m.nt + k);
+  return r;
+}
+
 // apply_ff for two voxels; *g2 = each one's |grad log|R||^2 in FP32
 template <bool DE>
 __device__ __forceinline__ qff2::Q apply_ff2(const MapParams& m, const qff2::Q& q, float2* g2) {
   using namespace qff2;
   q32x2::Q2 g = {pair(0.f), pair(0.f), pair(0.f), pair(0.f)};
-  const Q top = product_ff2<DE>(m, q, 0, m.nt, g);
   const F2 s = {pair(m.scale_ff[0]), pair(m.scale_ff[1])};
+  if (m.lagrange && m.nb > 0) {
+    Q out = lagrange_ff2<DE>(m, q, g);
+    out.w = mul(out.w, s);
+    out.x = mul(out.x, s);
+    out.y = mul(out.y, s);
+    out.z = mul(out.z, s);
+    if (DE) *g2 = q32x2::norm2(g);
+    return out;
+  }
+  const Q top = product_ff2<DE>(m, q, 0, m.nt, g);
   Q out;
   if (m.nb > 0) {
     const Q bot = product_ff2<DE>(m, q, m.nt, m.nt + m.nb, g);

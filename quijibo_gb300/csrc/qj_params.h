@@ -16,7 +16,9 @@ namespace qj {
 struct MapParams {
   int nt, nb;
   int all_int;                  // every effective exponent is an integer in [1, QJ_MAX_INT_EXP]
-  int pad_;
+  int lagrange;                 // the FP32 and double-float tiers apply the map in
+                                // RATIONAL_4D::evaluateLagrange order (set per call from
+                                // the iteration form; the FP64 tier reads IterParams)
   double scale;                 // s (OPTIMIZE_3D::_expScaling)
   float scalef;
   float pad2_;
