@@ -272,6 +272,29 @@ int qjg_energy_backward(qjg_ctx* ctx, const double* d_params, int32_t n_top, int
                         int32_t max_it, double escape, double d_sat, int32_t precision,
                         double* energy, double* d_grad, void* stream);
 
+/* Several squared-error energy + gradient calls in one pass (FP32 only; no
+ * reference counterpart: the serving form's batches).  Each item is the
+ * argument set of a qjg_energy_backward call; the items' samples are
+ * iterated by one persistent forward kernel and their gradient samples by
+ * one persistent adjoint kernel, and each item's energy and gradient are
+ * summed in a fixed order (the same values on every run, within FP32
+ * rounding of the item's own qjg_energy_backward).  Writes each item's
+ * energy and d_grad; synchronizes `stream`. */
+typedef struct {
+  const double* d_params; /* 5 (n_top + n_bot) + 1 doubles, layout of qjg_energy_backward */
+  int32_t n_top, n_bot;
+  int64_t n;              /* samples */
+  const double* d_xyz;    /* n x 3 */
+  const double* d_target; /* n */
+  double slice;
+  int32_t max_it;
+  int32_t pad_;
+  double escape, d_sat;
+  double* d_grad;         /* device output */
+  double energy;          /* output */
+} qjg_energy_item;
+int qjg_energy_backward_batch(qjg_ctx* ctx, int32_t n_items, qjg_energy_item* items, void* stream);
+
 typedef struct {
   int32_t steps;          /* L-BFGS iterations taken */
   int32_t energy_evals;   /* forward evaluations (line search) */

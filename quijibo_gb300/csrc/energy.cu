@@ -22,6 +22,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <vector>
 #include <type_traits>
 
 #include "qj_device.cuh"
@@ -1428,6 +1429,274 @@ __global__ void __launch_bounds__(256) sq_reduce_kernel(const double* __restrict
   if (lane == 0) out[k] = sum + c;
 }
 
+// ---- batches of energy + gradient requests (FP32), one pass for all.
+// Items' samples sit in one flat index space, each item's range starting on
+// a chunk boundary (SQ_CH), so that a chunk belongs to one item.  The
+// forward pass is the refill kernel over the flat space: a lane finds its
+// sample's item from the chunk table and reads that item's roots (FP32,
+// converted once) from global memory.  Chunk sums, the orbit-length sort and
+// the final reduction run per item; the adjoint's warps walk every item's
+// sorted groups in turn and write one partial row per group, so each item's
+// energy and gradient are sums in a fixed order.
+struct SqItem {
+  const double* xyz;     // the item's samples (n x 3) and targets
+  const double* target;
+  const float* rp;       // the item's roots (4 nr) then exponents (nr), FP32
+  const double* params;  // the item's parameter vector (for log s)
+  int nt, nb, max_it, slots;
+  double slice, escape, d_sat;
+  long long s0, n;       // first flat sample, samples
+  long long c0;          // first chunk
+  long long rows0;       // first partial row: the item's chunks, then its groups
+  int* total;            // the item's gradient samples (the sort's count)
+  unsigned* perm;        // the item's sorted gradient samples (local indices)
+  double* partials;      // the item's partial rows
+};
+
+__global__ void sq_item_roots_kernel(const SqItem* __restrict__ items, int K) {
+  const SqItem& it = items[blockIdx.x];
+  const int nr = it.nt + it.nb;
+  float* rp = const_cast<float*>(it.rp);
+  for (int k = threadIdx.x; k < 5 * nr; k += blockDim.x) rp[k] = (float)it.params[k];
+  (void)K;
+}
+
+__global__ void __launch_bounds__(SQF_T) sq_fwd_batch_kernel(
+    const SqItem* __restrict__ items, const int* __restrict__ chunk_item, long long n_flat,
+    unsigned long long* __restrict__ claim, SqFwdOut<float> o) {
+  using T = float;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  long long k = 0;       // flat sample
+  int item = -1;
+  bool live = false, done = false;
+  V4<T> q{T(0), T(0), T(0), T(0)};
+  T L = T(0);
+  int n = 0;
+  const SqItem* it = nullptr;
+  auto finish = [&](long long kf, const V4<T>& qf, T Lf, int nf) {
+    const long long kl = kf - it->s0;
+    const T m = sqrt(v4dot(qf, qf));
+    const T lm = log(m);
+    const T ld = log(fabs(lm)) + lm - Lf;
+    o.iters[kf] = nf;
+    T val, dval, dval_dd;
+    sq_saturate<T>(lm, ld, (T)it->d_sat, &val, &dval, &dval_dd);
+    const T r = val - (T)it->target[kl];
+    o.contrib[kf] = (double)(r * r);
+    int key = -1;
+    if (dval_dd != T(0)) {
+      const T db = T(2) * r * dval_dd;
+      const T kq = db * (lm + T(1)) * exp(ld - log(m) - log(fabs(lm)));
+      if (!isfinite(kq) || !isfinite(db * dval)) {
+        key = -2;
+      } else if (nf > 0) {
+        o.seed_q[kf] = v4scale(qf, kq / m);
+        o.seed_L[kf] = -db * dval;
+        key = nf;
+      }
+    }
+    o.keys[kf] = key;
+  };
+  for (;;) {
+    unsigned want = __ballot_sync(0xffffffffu, !live && !done);
+    while (want) {
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(claim, (unsigned long long)__popc(want));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (!live && !done) {
+        k = (long long)(base + __popc(want & lt));
+        if (k >= n_flat) {
+          done = true;
+        } else {
+          item = chunk_item[k / SQ_CH];
+          it = &items[item];
+          if (k - it->s0 < it->n) {  // not the padding after the item's samples
+            const long long kl = k - it->s0;
+            q = V4<T>{(T)it->xyz[3 * kl], (T)it->xyz[3 * kl + 1], (T)it->xyz[3 * kl + 2],
+                      (T)it->slice};
+            L = T(0);
+            n = 0;
+            if (sqrt(v4dot(q, q)) < (T)it->escape && n < it->max_it)
+              live = true;
+            else
+              finish(k, q, L, n);
+          }
+        }
+      }
+      want = __ballot_sync(0xffffffffu, !live && !done);
+    }
+    if (!__any_sync(0xffffffffu, live)) break;
+    if (live) {
+      if (n % SQ_CK == 0) o.ck[(long long)(n / SQ_CK) * n_flat + k] = q;
+      const int nr = it->nt + it->nb;
+      const T s = (T)exp(it->params[5 * nr]);
+      T lg;
+      q = sq_apply<T>(it->rp, it->rp + 4 * nr, it->nt, it->nb, s, q, &lg, nullptr, nullptr,
+                      nullptr, nullptr);
+      L += lg + T(0.5) * log(v4dot(q, q));
+      n++;
+      const T m = sqrt(v4dot(q, q));
+      if (!(m < (T)it->escape && n < it->max_it) || m < T(1.1754943508e-37)) {
+        finish(k, q, L, n);
+        live = false;
+      }
+    }
+  }
+}
+
+// The adjoint of a batch: warp w takes groups w, w + W, ... of item 0, then
+// of item 1, and so on (the items' sorted gradient samples in groups of 32);
+// per group it sums the root terms' gradient components over the warp into
+// shared double accumulators as sq_bwd_kernel does and writes them as the
+// group's partial row.
+__global__ void __launch_bounds__(SQ_T) sq_bwd_batch_kernel(
+    const SqItem* __restrict__ items, int K, long long n_flat, const int* __restrict__ keys,
+    const V4<float>* __restrict__ seed_q, const float* __restrict__ seed_L,
+    const V4<float>* __restrict__ ck, int max_slots) {
+  using T = float;
+  extern __shared__ unsigned char sh_raw[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double* acc = reinterpret_cast<double*>(sh_raw) + (size_t)warp * max_slots;
+  V4<T> seg[SQ_CK];
+  V4<T> F[QJ_MAX_ROOTS];
+  const V4<T> zero{T(0), T(0), T(0), T(0)};
+  const long long W = ((long long)gridDim.x * SQ_T) >> 5;
+  const long long w0 = ((long long)blockIdx.x * SQ_T + threadIdx.x) >> 5;
+  for (int item = 0; item < K; item++) {
+    const SqItem& it = items[item];
+    const int nt = it.nt, nb = it.nb, nr = nt + nb, slots = it.slots;
+    const T* rp = it.rp;
+    const T* ep = it.rp + 4 * nr;
+    const T s = (T)exp(it.params[5 * nr]);
+    const int count = *it.total;
+    const long long nchunks = (it.n + SQ_CH - 1) / SQ_CH;
+    for (long long grp = w0; grp * 32 < count; grp += W) {
+      for (int j = lane; j < slots; j += 32) acc[j] = 0.0;
+      __syncwarp();
+      const long long j = grp * 32 + lane;
+      const bool in = j < count;
+      const long long k = in ? it.s0 + (long long)it.perm[j] : 0;  // flat index
+      const int N = in ? keys[k] : 0;
+      V4<T> qb = in ? seed_q[k] : zero;
+      const T Lb = in ? seed_L[k] : T(0);
+      const int Nmax = __reduce_max_sync(0xffffffffu, N);
+      for (int sgi = (Nmax - 1) / SQ_CK; sgi >= 0; sgi--) {
+        const int n0 = sgi * SQ_CK, n1 = min(N, n0 + SQ_CK), n1max = min(Nmax, n0 + SQ_CK);
+        V4<T> q = n1 > n0 ? ck[(long long)sgi * n_flat + k] : zero;
+        for (int n = n0; n < n1; n++) {
+          seg[n - n0] = q;
+          T lg;
+          q = sq_apply<T>(rp, ep, nt, nb, s, q, &lg, nullptr, nullptr, nullptr, nullptr);
+        }
+        for (int n = n1max - 1; n >= n0; n--) {
+          const bool on = n < n1;
+          V4<T> qn = zero, Tb = zero, Bb = zero, gb = zero;
+          T dls = T(0);
+          if (on) {
+            qn = seg[n - n0];
+            T lg;
+            V4<T> Tq, Bq;
+            const V4<T> Q = sq_apply<T>(rp, ep, nt, nb, s, qn, &lg, F, nullptr, &Tq, &Bq);
+            const V4<T> Qb = v4add(qb, v4scale(Q, Lb / v4dot(Q, Q)));
+            dls = v4dot(Qb, Q);
+            if (nb > 0) {
+              const V4<T> W4 = v4scale(v4conj(Bq), T(1) / v4dot(Bq, Bq));
+              Tb = v4scale(v4mul(Qb, v4conj(W4)), s);
+              const V4<T> Wb = v4scale(v4mul(v4conj(Tq), Qb), s);
+              Bb = v4scale(v4mul(v4mul(v4conj(W4), Wb), v4conj(W4)), T(-1));
+            } else {
+              Tb = v4scale(Qb, s);
+            }
+            V4<T> g = zero;
+            for (int i = 0; i < nr; i++) {
+              const V4<T> d{qn.w - rp[4 * i], qn.x - rp[4 * i + 1], qn.y - rp[4 * i + 2],
+                            qn.z - rp[4 * i + 3]};
+              g = v4add(g, v4scale(d, (i >= nt ? -ep[i] : ep[i]) / v4dot(d, d)));
+            }
+            gb = v4scale(g, Lb / v4dot(g, g));
+          }
+          dls = warp_sum(dls);
+          if (lane == 0) acc[1 + 5 * nr] += (double)dls;
+          V4<T> qbn = zero;
+          for (int side = 1; side >= 0; side--) {
+            const int lo = side ? nt : 0, hi = side ? nr : nt;
+            if (hi == lo) continue;
+            V4<T> U = side ? Bb : Tb;
+            for (int i = hi - 1; i >= lo; i--) {
+              T c0 = T(0), c1 = T(0), c2 = T(0), c3 = T(0), c4 = T(0);
+              if (on) {
+                const V4<T> d{qn.w - rp[4 * i], qn.x - rp[4 * i + 1], qn.y - rp[4 * i + 2],
+                              qn.z - rp[4 * i + 3]};
+                PowParts<T> pp;
+                const V4<T> P = powv<T>(d, ep[i], &pp);
+                const V4<T> Pb = (i == lo) ? U : v4mul(v4conj(F[i - 1]), U);
+                U = v4mul(U, v4conj(P));
+                T eb = T(0);
+                V4<T> dbar = powv_vjp<T>(d, ep[i], pp, Pb, &eb);
+                const T sgn = side ? T(-1) : T(1);
+                const T d2 = v4dot(d, d);
+                const T dg = v4dot(d, gb);
+                dbar = v4add(dbar, v4scale(v4add(v4scale(gb, T(1) / d2),
+                                                 v4scale(d, T(-2) * dg / (d2 * d2))),
+                                           sgn * ep[i]));
+                eb += sgn * dg / d2;
+                c0 = -dbar.w;
+                c1 = -dbar.x;
+                c2 = -dbar.y;
+                c3 = -dbar.z;
+                c4 = eb;
+                qbn = v4add(qbn, dbar);
+              }
+              c0 = warp_sum(c0);
+              c1 = warp_sum(c1);
+              c2 = warp_sum(c2);
+              c3 = warp_sum(c3);
+              c4 = warp_sum(c4);
+              if (lane < 5) {
+                const T v = lane == 0 ? c0 : lane == 1 ? c1 : lane == 2 ? c2 : lane == 3 ? c3 : c4;
+                acc[1 + (lane < 4 ? 4 * i + lane : 4 * nr + i)] += (double)v;
+              }
+            }
+          }
+          if (on) qb = qbn;
+        }
+      }
+      __syncwarp();
+      double* row = it.partials + (nchunks + grp) * slots;
+      for (int jj = lane; jj < slots; jj += 32) row[jj] = acc[jj];
+      __syncwarp();
+    }
+  }
+}
+
+// The final sums of one item: its chunk rows and as many group rows as its
+// sort produced (read on the device), as sq_reduce_kernel.
+__global__ void __launch_bounds__(256) sq_reduce_item_kernel(const double* __restrict__ partials,
+                                                             int chunk_rows,
+                                                             const int* __restrict__ total,
+                                                             int slots, double* __restrict__ out) {
+  const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (k >= slots) return;
+  const int rows = chunk_rows + (*total + 31) / 32;
+  double sum = 0, c = 0;
+  for (int b = lane; b < rows; b += 32) {
+    const double v = partials[(long long)b * slots + k];
+    const double t = sum + v;
+    c += (fabs(sum) >= fabs(v)) ? (sum - t) + v : (v - t) + sum;
+    sum = t;
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    const double s2 = __shfl_down_sync(0xffffffffu, sum, o);
+    const double c2 = __shfl_down_sync(0xffffffffu, c, o);
+    const double t = sum + s2;
+    c += c2 + ((fabs(sum) >= fabs(s2)) ? (sum - t) + s2 : (s2 - t) + sum);
+    sum = t;
+  }
+  if (lane == 0) out[k] = sum + c;
+}
+
 // Forward kernel choice (qjg_set_energy_pairs): two samples per lane or one.
 std::atomic<int> g_sq_pairs{0};
 
@@ -1552,7 +1821,150 @@ cudaError_t sq_launch(bool grad, const double* params, int nt, int nb, const dou
   return cudaGetLastError();
 }
 
+// Byte layout of a batch's scratch (each piece 256-byte aligned).
+struct SqBatchLayout {
+  size_t items, chunk_item, claim, work, contrib, keys, iters, seed_q, seed_L, ck, bytes;
+  std::vector<size_t> rp, hist, total, perm, partials, out;
+  std::vector<long long> s0, c0, nchunks;
+  std::vector<int> slots;
+  long long n_flat = 0, chunks = 0;
+  int nck = 0, max_slots = 0;
+};
+
+SqBatchLayout sq_batch_layout(const SqBatchReq* r, int K) {
+  SqBatchLayout L;
+  size_t at = 0;
+  auto take = [&](size_t b) {
+    const size_t o = at;
+    at += (b + 255) / 256 * 256;
+    return o;
+  };
+  for (int i = 0; i < K; i++) {
+    const long long nc = std::max<long long>(1, (r[i].n + SQ_CH - 1) / SQ_CH);
+    L.s0.push_back(L.n_flat);
+    L.c0.push_back(L.chunks);
+    L.nchunks.push_back(nc);
+    L.n_flat += nc * SQ_CH;
+    L.chunks += nc;
+    L.nck = std::max(L.nck, r[i].max_it > 0 ? (r[i].max_it - 1) / SQ_CK + 1 : 0);
+    L.slots.push_back(1 + 5 * (r[i].nt + r[i].nb) + 1 + 1);
+    L.max_slots = std::max(L.max_slots, L.slots.back());
+  }
+  const size_t nf = (size_t)L.n_flat;
+  L.items = take(sizeof(SqItem) * (size_t)K);
+  L.chunk_item = take(sizeof(int) * (size_t)L.chunks);
+  L.claim = take(sizeof(unsigned long long));
+  L.work = take(2 * sizeof(unsigned long long));
+  L.contrib = take(sizeof(double) * nf);
+  L.keys = take(sizeof(int) * nf);
+  L.iters = take(sizeof(int) * nf);
+  L.seed_q = take(sizeof(V4<float>) * nf);
+  L.seed_L = take(sizeof(float) * nf);
+  L.ck = take(sizeof(V4<float>) * nf * (size_t)std::max(L.nck, 1));
+  for (int i = 0; i < K; i++) {
+    const size_t nr = (size_t)(r[i].nt + r[i].nb), n = (size_t)std::max<long long>(r[i].n, 0);
+    L.rp.push_back(take(sizeof(float) * 5 * nr));
+    L.hist.push_back(take(sizeof(int) * (size_t)(r[i].max_it + 1) * (size_t)L.nchunks[i]));
+    L.total.push_back(take(sizeof(int)));
+    L.perm.push_back(take(sizeof(unsigned) * std::max<size_t>(n, 1)));
+    L.partials.push_back(
+        take(sizeof(double) * (size_t)(L.nchunks[i] + (long long)(n + 31) / 32) * L.slots[i]));
+    L.out.push_back(take(sizeof(double) * L.slots[i]));
+  }
+  L.bytes = at;
+  return L;
+}
+
 }  // namespace
+
+size_t sq_batch_scratch_bytes(const SqBatchReq* r, int K) { return sq_batch_layout(r, K).bytes; }
+
+cudaError_t launch_sq_energy_batch(const SqBatchReq* r, int K, void* scratch, double** outs,
+                                   cudaStream_t s, int* launches) {
+  if (K <= 0) return cudaSuccess;
+  const SqBatchLayout L = sq_batch_layout(r, K);
+  unsigned char* scr = static_cast<unsigned char*>(scratch);
+  std::vector<SqItem> items((size_t)K);
+  std::vector<int> chunk_item((size_t)L.chunks);
+  for (int i = 0; i < K; i++) {
+    SqItem& it = items[(size_t)i];
+    it.xyz = r[i].xyz;
+    it.target = r[i].target;
+    it.rp = reinterpret_cast<const float*>(scr + L.rp[(size_t)i]);
+    it.params = r[i].params;
+    it.nt = r[i].nt;
+    it.nb = r[i].nb;
+    it.max_it = r[i].max_it;
+    it.slots = L.slots[(size_t)i];
+    it.slice = r[i].slice;
+    it.escape = r[i].escape;
+    it.d_sat = r[i].d_sat;
+    it.s0 = L.s0[(size_t)i];
+    it.n = r[i].n;
+    it.c0 = L.c0[(size_t)i];
+    it.rows0 = 0;
+    it.total = reinterpret_cast<int*>(scr + L.total[(size_t)i]);
+    it.perm = reinterpret_cast<unsigned*>(scr + L.perm[(size_t)i]);
+    it.partials = reinterpret_cast<double*>(scr + L.partials[(size_t)i]);
+    for (long long c = 0; c < L.nchunks[(size_t)i]; c++) chunk_item[(size_t)(L.c0[(size_t)i] + c)] = i;
+    outs[i] = reinterpret_cast<double*>(scr + L.out[(size_t)i]);
+  }
+  SqItem* d_items = reinterpret_cast<SqItem*>(scr + L.items);
+  int* d_chunk_item = reinterpret_cast<int*>(scr + L.chunk_item);
+  unsigned long long* claim = reinterpret_cast<unsigned long long*>(scr + L.claim);
+  unsigned long long* work = reinterpret_cast<unsigned long long*>(scr + L.work);
+  cudaError_t e;
+  // pageable sources: each copy has left the host buffer when it returns
+  if ((e = cudaMemcpyAsync(d_items, items.data(), sizeof(SqItem) * (size_t)K,
+                           cudaMemcpyHostToDevice, s)) ||
+      (e = cudaMemcpyAsync(d_chunk_item, chunk_item.data(), sizeof(int) * chunk_item.size(),
+                           cudaMemcpyHostToDevice, s)) ||
+      (e = cudaMemsetAsync(claim, 0, sizeof(unsigned long long), s)) ||
+      (e = cudaMemsetAsync(work, 0, 2 * sizeof(unsigned long long), s)))
+    return e;
+  int n_launch = 0;
+  sq_item_roots_kernel<<<K, 128, 0, s>>>(d_items, K);
+  n_launch++;
+  SqFwdOut<float> o{};
+  o.contrib = reinterpret_cast<double*>(scr + L.contrib);
+  o.keys = reinterpret_cast<int*>(scr + L.keys);
+  o.iters = reinterpret_cast<int*>(scr + L.iters);
+  o.seed_q = reinterpret_cast<V4<float>*>(scr + L.seed_q);
+  o.seed_L = reinterpret_cast<float*>(scr + L.seed_L);
+  o.ck = reinterpret_cast<V4<float>*>(scr + L.ck);
+  const int sms = sm_count();
+  // persistent forward grid: three blocks per SM (the single-request choice
+  // for long orbit mixes), fewer when the batch is small
+  const long long need = (L.n_flat + SQF_T - 1) / SQF_T;
+  const int fblocks = (int)std::max<long long>(1, std::min<long long>((long long)sms * 3, need));
+  sq_fwd_batch_kernel<<<fblocks, SQF_T, 0, s>>>(d_items, d_chunk_item, L.n_flat, claim, o);
+  n_launch++;
+  // per item: chunk sums and histogram, the sort's scan and scatter
+  for (int i = 0; i < K; i++) {
+    const long long s0 = L.s0[(size_t)i];
+    int* hist = reinterpret_cast<int*>(scr + L.hist[(size_t)i]);
+    sq_chunk_kernel<<<(unsigned)L.nchunks[(size_t)i], SQC_T, 0, s>>>(
+        o.contrib + s0, o.keys + s0, o.iters + s0, r[i].n, r[i].max_it, (int)L.nchunks[(size_t)i],
+        hist, items[(size_t)i].partials, L.slots[(size_t)i], 0, work);
+    sq_scan_kernel<<<1, 1024, 0, s>>>(hist, (long long)(r[i].max_it + 1) * L.nchunks[(size_t)i],
+                                      items[(size_t)i].total);
+    sq_scatter_kernel<<<(unsigned)L.nchunks[(size_t)i], 32, 0, s>>>(
+        o.keys + s0, r[i].n, r[i].max_it, (int)L.nchunks[(size_t)i], hist, items[(size_t)i].perm);
+    n_launch += 3;
+  }
+  const size_t sh = sizeof(double) * (SQ_T / 32) * (size_t)L.max_slots;
+  sq_bwd_batch_kernel<<<sms * SQ_BWD_PER_SM, SQ_T, sh, s>>>(d_items, K, L.n_flat, o.keys, o.seed_q,
+                                                              o.seed_L, o.ck, L.max_slots);
+  n_launch++;
+  for (int i = 0; i < K; i++) {
+    sq_reduce_item_kernel<<<(L.slots[(size_t)i] * 32 + 255) / 256, 256, 0, s>>>(
+        items[(size_t)i].partials, (int)L.nchunks[(size_t)i], items[(size_t)i].total,
+        L.slots[(size_t)i], outs[i]);
+    n_launch++;
+  }
+  if (launches) *launches = n_launch;
+  return cudaGetLastError();
+}
 
 int sq_max_iterations() { return SQ_MAXIT; }
 

@@ -30,6 +30,49 @@ qj::WeightGrid qj_weight_grid(const qjg_grid* g) {
 
 extern "C" {
 
+int qjg_energy_backward_batch(qjg_ctx* ctx, int32_t n_items, qjg_energy_item* items,
+                              void* stream) {
+  if (!ctx) return QJG_ERR_ARG;
+  if (n_items < 0 || (n_items > 0 && !items)) return fail(ctx, QJG_ERR_ARG, "no items");
+  if (n_items == 0) return QJG_OK;
+  std::vector<qj::SqBatchReq> req((size_t)n_items);
+  for (int i = 0; i < n_items; i++) {
+    const qjg_energy_item& it = items[i];
+    if (it.n_top < 1 || it.n_bot < 0 || it.n_top + it.n_bot > QJG_MAX_ROOTS)
+      return fail(ctx, QJG_ERR_ARG, "item %d: root counts top=%d bottom=%d", i, it.n_top, it.n_bot);
+    if (it.n < 0 || it.n > INT32_MAX || !it.d_params || !it.d_grad ||
+        (it.n > 0 && (!it.d_xyz || !it.d_target)))
+      return fail(ctx, QJG_ERR_ARG, "item %d: NULL or out-of-range arguments", i);
+    if (it.max_it < 0 || it.max_it > qj::sq_max_iterations())
+      return fail(ctx, QJG_ERR_ARG, "item %d: max_it = %d", i, it.max_it);
+    if (!(it.escape > 0)) return fail(ctx, QJG_ERR_ARG, "item %d: escape radius must be > 0", i);
+    req[(size_t)i] = qj::SqBatchReq{it.d_params, it.n_top, it.n_bot, it.n, it.d_xyz, it.d_target,
+                                    it.slice, it.max_it, it.escape, it.d_sat};
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  QJ_CUDA(ctx, cudaSetDevice(ctx->device));
+  void* d_scr = nullptr;
+  QJ_CUDA(ctx, cudaMallocAsync(&d_scr, qj::sq_batch_scratch_bytes(req.data(), n_items), s));
+  std::vector<double*> outs((size_t)n_items);
+  std::vector<double> energies((size_t)n_items);
+  int launched = 0;
+  cudaError_t e = qj::launch_sq_energy_batch(req.data(), n_items, d_scr, outs.data(), s, &launched);
+  for (int i = 0; i < n_items && e == cudaSuccess; i++) {
+    const int P = 5 * (items[i].n_top + items[i].n_bot) + 1;
+    e = cudaMemcpyAsync(items[i].d_grad, outs[(size_t)i] + 1, sizeof(double) * P,
+                        cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(&energies[(size_t)i], outs[(size_t)i], sizeof(double),
+                          cudaMemcpyDeviceToHost, s);
+  }
+  cudaFreeAsync(d_scr, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return fail(ctx, QJG_ERR_CUDA, "energy batch: %s", cudaGetErrorString(e));
+  for (int i = 0; i < n_items; i++) items[i].energy = energies[(size_t)i];
+  ctx->launches += launched;
+  return QJG_OK;
+}
+
 int qjg_set_energy_pairs(int on) {
   qj::set_energy_pairs(on);
   return QJG_OK;

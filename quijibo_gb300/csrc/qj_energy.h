@@ -35,4 +35,23 @@ cudaError_t launch_sq_energy(bool fp64, bool grad, const double* params, int nt,
                              double** out, int* iters, cudaStream_t s, int* launches,
                              unsigned long long** work);
 
+// One request of a batch of FP32 energy + gradient calls: device pointers
+// as for launch_sq_energy.
+struct SqBatchReq {
+  const double* params;
+  int nt, nb;
+  long long n;
+  const double* xyz;
+  const double* target;
+  double slice;
+  int max_it;
+  double escape, d_sat;
+};
+size_t sq_batch_scratch_bytes(const SqBatchReq* r, int K);
+// The K requests in one pass (FP32 forward and adjoint); outs[i] (in the
+// scratch) receives request i's [energy, gradient, samples left out], as
+// launch_sq_energy's out.
+cudaError_t launch_sq_energy_batch(const SqBatchReq* r, int K, void* scratch, double** outs,
+                                   cudaStream_t s, int* launches);
+
 }  // namespace qj

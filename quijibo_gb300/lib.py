@@ -83,6 +83,14 @@ class QjgTanhStats(C.Structure):
                 ("band_voxels", C.c_int64)]
 
 
+class QjgEnergyItem(C.Structure):
+    _fields_ = [("d_params", C.c_void_p), ("n_top", C.c_int32), ("n_bot", C.c_int32),
+                ("n", C.c_int64), ("d_xyz", C.c_void_p), ("d_target", C.c_void_p),
+                ("slice", C.c_double), ("max_it", C.c_int32), ("pad_", C.c_int32),
+                ("escape", C.c_double), ("d_sat", C.c_double), ("d_grad", C.c_void_p),
+                ("energy", C.c_double)]
+
+
 class QjgFitStats(C.Structure):
     _fields_ = [("steps", C.c_int32), ("energy_evals", C.c_int32), ("gradient_evals", C.c_int32),
                 ("energy0", C.c_double), ("energy", C.c_double)]
@@ -194,6 +202,8 @@ EXPORTS = {
                          C.c_int32, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
                          C.POINTER(QjgMeshStats), C.c_void_p], C.c_int),
     "qjg_set_energy_pairs": ([C.c_int], C.c_int),
+    "qjg_energy_backward_batch": ([C.c_void_p, C.c_int32, C.POINTER(QjgEnergyItem), C.c_void_p],
+                                  C.c_int),
     "qjg_energy_last_work": ([C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)], C.c_int),
     "qjg_mesh_capture": ([C.c_void_p, C.c_int32], C.c_int),
     "qjg_mesh_edge_cache_write": ([C.c_void_p, C.c_char_p], C.c_int),
@@ -631,6 +641,20 @@ class Context:
         if check:
             self._check(rc, "qjg_mesh_stream")
         return rc, st.as_dict()
+
+    def energy_batch(self, items, stream=None):
+        """qjg_energy_backward_batch over dicts with d_params, n_top, n_bot, n,
+        d_xyz, d_target, max_it, escape, d_sat, slice, d_grad (device
+        addresses as ints); returns the energies."""
+        arr = (QjgEnergyItem * len(items))()
+        for a, it in zip(arr, items):
+            a.d_params, a.n_top, a.n_bot, a.n = it["d_params"], it["n_top"], it["n_bot"], it["n"]
+            a.d_xyz, a.d_target, a.slice = it["d_xyz"], it["d_target"], it.get("slice", 0.0)
+            a.max_it, a.escape, a.d_sat = it["max_it"], it["escape"], it.get("d_sat", 1.0)
+            a.d_grad = it["d_grad"]
+        self._check(self.L.qjg_energy_backward_batch(self.h, len(items), arr, C.c_void_p(stream or 0)),
+                    "qjg_energy_backward_batch")
+        return [a.energy for a in arr]
 
     def energy_last_work(self):
         """(forward map applications, adjoint orbit steps) of the last energy call."""
