@@ -326,7 +326,9 @@ int qjg_fit_lbfgs(qjg_ctx* ctx, double* d_params, int32_t n_top, int32_t n_bot, 
  * with integer exponents and at most 2^26 voxels are served by a batch
  * worker instead: every such request waiting when it becomes free (up to 64
  * and the batch arena) runs in one multi-request pass, replayed from a
- * captured CUDA graph.  Inputs are copied at submission; output buffers
+ * captured CUDA graph.  FP32 energy + gradient requests go to an energy
+ * batch worker, which runs every such request waiting when it is free as
+ * one qjg_energy_backward_batch pass.  Inputs are copied at submission; output buffers
  * (host) must stay valid until the request completes. */
 #define QJG_REQ_FIELD 0  /* field of a map on a grid (out_field: X*Y*Z doubles, optional) */
 #define QJG_REQ_MESH 1   /* streaming field + marching cubes (out_verts / out_tris optional) */
@@ -386,6 +388,9 @@ typedef struct {
   int64_t batched;               /* field requests served inside multi-request batches */
   int64_t batches;               /* batch passes (one CUDA-graph replay each) */
   int64_t max_batch;             /* most requests in one batch */
+  int64_t energy_batched;        /* FP32 energy requests served inside energy batches */
+  int64_t energy_batches;        /* energy batch passes */
+  int64_t max_energy_batch;      /* most requests in one energy batch */
 } qjg_server_stats;
 
 int qjg_server_create(int device, int32_t workers, int64_t hbm_budget_bytes, qjg_server** out);

@@ -43,7 +43,8 @@ struct Job {
   std::vector<double> top_roots, top_powers, bot_roots, bot_powers, xyz, target, params;
   int64_t est_bytes = 0;
   int64_t voxels = 0;
-  bool batchable = false;
+  bool batchable = false;   // field request for the field batch worker
+  bool ebatchable = false;  // FP32 energy request for the energy batch worker
   Clock::time_point t_submit, t_admit, t_done;
   qjg_result res;
 };
@@ -125,8 +126,13 @@ int64_t estimate_bytes(const qjg_request& r) {
       const int64_t nz = 64;
       return slab * (nz + 2) * (8 + 1 + 1 + 4 + 12) + r.vert_cap * 36 + r.tri_cap * 24 + (1 << 20);
     }
-    default:
-      return r.n_samples * 40 + (1 << 20);
+    default: {
+      // inputs and gradient, per-sample results and sort, checkpoints every
+      // 8 steps (16 B each), partial rows of the sums
+      const int64_t nck = r.max_it > 0 ? (r.max_it - 1) / 8 + 1 : 0;
+      const int64_t slots = 5 * (int64_t)(r.n_top + r.n_bot) + 3;
+      return r.n_samples * (32 + 48 + 16 * nck) + (r.n_samples / 32 + 1) * slots * 8 + (1 << 20);
+    }
   }
 }
 
@@ -162,6 +168,13 @@ struct qjg_server {
   std::vector<std::shared_ptr<Job>> batch_q;
   std::condition_variable batch_cv;
   int64_t batched = 0, batches = 0, max_batch = 0;
+
+  // energy batch worker
+  bool ebatch_on = false;
+  bool ebatch_idle = false;
+  std::vector<std::shared_ptr<Job>> ebatch_q;
+  std::condition_variable ebatch_cv;
+  int64_t ebatched = 0, ebatches = 0, max_ebatch = 0;
 
   explicit qjg_server(int workers) : idle(workers, 0), worker_q(workers), worker_cv(workers) {}
 };
@@ -412,6 +425,100 @@ void batch_main(qjg_server* srv) {
   }
 }
 
+// One pass over FP32 energy + gradient jobs: their inputs to the device,
+// qjg_energy_backward_batch, the gradients back.
+int run_energy_batch(qjg_ctx* ctx, cudaStream_t s, std::vector<std::shared_ptr<Job>>& jobs) {
+  const int K = (int)jobs.size();
+  int64_t doubles = 0;
+  for (auto& j : jobs) {
+    const qjg_request& r = j->req;
+    doubles += 2 * (5 * (int64_t)(r.n_top + r.n_bot) + 1) + 4 * r.n_samples;
+  }
+  double* arena = nullptr;
+  if (cudaMallocAsync((void**)&arena, (size_t)std::max<int64_t>(doubles, 1) * sizeof(double), s))
+    return QJG_ERR_NOMEM;
+  std::vector<qjg_energy_item> items((size_t)K);
+  int rc = QJG_OK;
+  double* at = arena;
+  for (int k = 0; k < K && rc == QJG_OK; k++) {
+    Job& j = *jobs[(size_t)k];
+    const qjg_request& r = j.req;
+    const int64_t P = 5 * (int64_t)(r.n_top + r.n_bot) + 1;
+    qjg_energy_item& it = items[(size_t)k];
+    std::memset(&it, 0, sizeof it);
+    double* dp = at;
+    double* dg = dp + P;
+    double* dx = dg + P;
+    double* dt = dx + 3 * r.n_samples;
+    at = dt + r.n_samples;
+    if (cudaMemcpyAsync(dp, j.params.data(), P * sizeof(double), cudaMemcpyHostToDevice, s) ||
+        (r.n_samples &&
+         (cudaMemcpyAsync(dx, j.xyz.data(), 3 * r.n_samples * sizeof(double), cudaMemcpyHostToDevice, s) ||
+          cudaMemcpyAsync(dt, j.target.data(), r.n_samples * sizeof(double), cudaMemcpyHostToDevice, s))))
+      rc = QJG_ERR_CUDA;
+    it.d_params = dp;
+    it.n_top = r.n_top;
+    it.n_bot = r.n_bot;
+    it.n = r.n_samples;
+    it.d_xyz = dx;
+    it.d_target = dt;
+    it.slice = r.grid.slice;
+    it.max_it = r.max_it;
+    it.escape = r.escape;
+    it.d_sat = r.d_sat;
+    it.d_grad = dg;
+  }
+  if (rc == QJG_OK) rc = qjg_energy_backward_batch(ctx, K, items.data(), s);
+  for (int k = 0; k < K && rc == QJG_OK; k++) {
+    Job& j = *jobs[(size_t)k];
+    j.res.energy = items[(size_t)k].energy;
+    const int64_t P = 5 * (int64_t)(j.req.n_top + j.req.n_bot) + 1;
+    if (j.req.out_grad && cudaMemcpyAsync(j.req.out_grad, items[(size_t)k].d_grad, P * sizeof(double),
+                                          cudaMemcpyDeviceToHost, s))
+      rc = QJG_ERR_CUDA;
+  }
+  cudaFreeAsync(arena, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess && rc == QJG_OK) rc = QJG_ERR_CUDA;
+  return rc;
+}
+
+void ebatch_main(qjg_server* srv) {
+  cudaSetDevice(srv->device);
+  qjg_ctx* ctx = nullptr;
+  const int crc = qjg_create(srv->device, &ctx);
+  cudaStream_t s = nullptr;
+  cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  for (;;) {
+    std::vector<std::shared_ptr<Job>> jobs;
+    {
+      std::unique_lock<std::mutex> lk(srv->mu);
+      srv->ebatch_idle = true;
+      srv->cv_dispatch.notify_one();
+      srv->ebatch_cv.wait(lk, [&] { return srv->stop || !srv->ebatch_q.empty(); });
+      srv->ebatch_idle = false;
+      if (srv->ebatch_q.empty()) break;  // stopping
+      jobs.swap(srv->ebatch_q);
+      for (auto& j : jobs) j->res.status = QJG_STATUS_RUNNING;
+    }
+    const int rc = crc != QJG_OK ? crc : run_energy_batch(ctx, s, jobs);
+    {
+      std::lock_guard<std::mutex> lk(srv->mu);
+      const Clock::time_point now = Clock::now();
+      srv->ebatches++;
+      srv->ebatched += (int64_t)jobs.size();
+      srv->max_ebatch = std::max<int64_t>(srv->max_ebatch, (int64_t)jobs.size());
+      for (auto& j : jobs) {
+        j->res.error = rc;
+        finish_job(srv, *j, now);
+      }
+      srv->cv_done.notify_all();
+      srv->cv_dispatch.notify_one();
+    }
+  }
+  if (s) cudaStreamDestroy(s);
+  if (ctx) qjg_destroy(ctx);
+}
+
 void dispatcher_main(qjg_server* srv) {
   std::unique_lock<std::mutex> lk(srv->mu);
   const int nw = (int)srv->worker_q.size();
@@ -439,6 +546,33 @@ void dispatcher_main(qjg_server* srv) {
         admitted = true;
       }
     }
+    // the energy batch worker takes the FP32 energy requests waiting when it
+    // is free (up to BATCH_MAX items and 2^23 samples) that fit the budget
+    if (srv->ebatch_on && srv->ebatch_idle && srv->ebatch_q.empty()) {
+      int64_t samples = 0;
+      for (size_t i = 0; i < srv->waiting.size() && (int)srv->ebatch_q.size() < qj::BATCH_MAX;) {
+        auto job = srv->waiting[i];
+        const bool fits = srv->in_use + job->est_bytes <= srv->budget || srv->in_use == 0;
+        const bool room = srv->ebatch_q.empty() || samples + job->req.n_samples <= (1ll << 23);
+        if (!job->ebatchable || !room || !fits) {
+          i++;
+          continue;
+        }
+        srv->waiting.erase(srv->waiting.begin() + (long)i);
+        samples += job->req.n_samples;
+        srv->in_use += job->est_bytes;
+        srv->peak_in_use = std::max(srv->peak_in_use, srv->in_use);
+        job->t_admit = Clock::now();
+        srv->ebatch_q.push_back(job);
+        srv->running++;
+      }
+      if (!srv->ebatch_q.empty()) {
+        srv->peak_running = std::max(srv->peak_running, srv->running);
+        srv->ebatch_idle = false;
+        srv->ebatch_cv.notify_one();
+        admitted = true;
+      }
+    }
     // admit while a worker is idle and the head (or a request within the
     // lookahead window) fits the budget
     int w = -1;
@@ -452,6 +586,7 @@ void dispatcher_main(qjg_server* srv) {
       for (size_t i = 0; i < srv->waiting.size() && seen < srv->lookahead; i++) {
         auto job = srv->waiting[i];
         if (job->batchable && srv->batcher) continue;  // the batch worker's
+        if (job->ebatchable && srv->ebatch_on) continue;  // the energy batch worker's
         seen++;
         // a request larger than the whole budget runs alone
         if (srv->in_use + job->est_bytes <= srv->budget || srv->in_use == 0) {
@@ -502,6 +637,8 @@ int qjg_server_create(int device, int32_t workers, int64_t hbm_budget_bytes, qjg
   }
   for (int w = 0; w < workers; w++) srv->threads.emplace_back(worker_main, srv, w);
   if (srv->batcher) srv->threads.emplace_back(batch_main, srv);
+  srv->ebatch_on = true;
+  srv->threads.emplace_back(ebatch_main, srv);
   srv->threads.emplace_back(dispatcher_main, srv);
   *out = srv;
   return QJG_OK;
@@ -547,6 +684,8 @@ int qjg_server_submit(qjg_server* srv, const qjg_request* req, int64_t* ticket) 
     j->batchable = ints;
     if (ints) j->est_bytes = 0;  // inside the batch arena
   }
+  j->ebatchable = req->kind == QJG_REQ_ENERGY && req->precision != QJG_FP64 &&
+                  req->max_it >= 0 && req->escape > 0;
   std::memset(&j->res, 0, sizeof j->res);
   j->res.status = QJG_STATUS_QUEUED;
   {
@@ -595,7 +734,7 @@ int qjg_server_drain(qjg_server* srv) {
     if (!srv->waiting.empty()) return false;
     for (auto& q : srv->worker_q)
       if (!q.empty()) return false;
-    if (!srv->batch_q.empty()) return false;
+    if (!srv->batch_q.empty() || !srv->ebatch_q.empty()) return false;
     for (auto& kv : srv->jobs)
       if (kv.second->res.status == QJG_STATUS_QUEUED || kv.second->res.status == QJG_STATUS_RUNNING)
         return false;
@@ -627,6 +766,9 @@ int qjg_server_read_stats(qjg_server* srv, qjg_server_stats* out) {
   out->batched = srv->batched;
   out->batches = srv->batches;
   out->max_batch = srv->max_batch;
+  out->energy_batched = srv->ebatched;
+  out->energy_batches = srv->ebatches;
+  out->max_energy_batch = srv->max_ebatch;
   return QJG_OK;
 }
 
@@ -639,6 +781,7 @@ void qjg_server_destroy(qjg_server* srv) {
   }
   srv->cv_dispatch.notify_all();
   srv->batch_cv.notify_all();
+  srv->ebatch_cv.notify_all();
   for (auto& cv : srv->worker_cv) cv.notify_all();
   for (auto& t : srv->threads) t.join();
   srv->batcher.reset();

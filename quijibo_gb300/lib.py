@@ -127,7 +127,9 @@ class QjgServerStats(C.Structure):
                 ("p99_ms", C.c_double), ("max_ms", C.c_double), ("span_s", C.c_double),
                 ("in_use_bytes", C.c_int64), ("peak_in_use_bytes", C.c_int64),
                 ("peak_running", C.c_int32), ("pad_", C.c_int32), ("batched", C.c_int64),
-                ("batches", C.c_int64), ("max_batch", C.c_int64)]
+                ("batches", C.c_int64), ("max_batch", C.c_int64),
+                ("energy_batched", C.c_int64), ("energy_batches", C.c_int64),
+                ("max_energy_batch", C.c_int64)]
 
 
 class QjgBlmvmSettings(C.Structure):

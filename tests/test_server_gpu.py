@@ -140,3 +140,40 @@ def test_batched_field_requests_equal_direct_calls(ctx):
         ctx.free(h)
         np.testing.assert_array_equal(f.reshape(-1), o["field"])
         assert rr["voxel_iters"] == fs["voxel_iters"]
+
+
+def test_batched_energy_requests_equal_direct_calls(ctx):
+    """FP32 energy + gradient requests submitted together are served in
+    multi-request energy batches (one forward and one adjoint pass over all
+    of them); each result is its own qjg_energy_backward's within FP32
+    rounding.  FP64 energy requests take the per-request workers."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.RandomState(7)
+    reqs = []
+    for i in range(14):
+        nt, nb = int(rng.randint(4, 17)), int(rng.randint(0, 6))
+        rs = draw_rootset(500 + i, nt, nb, -1.2, 1.2, exps=(1, 2))
+        rs.scale = conformal_scale(rs, Grid((16, 16, 16), lengths=(2.0, 2.0, 2.0)), 16)
+        xyz, _ = poisson_disk(int(rng.randint(300, 3000)), seed=40 + i)
+        reqs.append(dict(kind=lib.QJG_REQ_ENERGY, rs=rs, params=lib.params_of(rs), xyz=xyz,
+                         target=ShapeSDF(i)(xyz), max_it=int(rng.randint(5, 21)),
+                         precision=lib.QJG_FP64 if i % 7 == 6 else lib.QJG_FP32))
+    srv = lib.Server(workers=2)
+    outs, res = run(srv, reqs)
+    st = srv.stats()
+    srv.close()
+    n32 = sum(1 for r in reqs if r["precision"] == lib.QJG_FP32)
+    assert st["energy_batched"] == n32 and st["failed"] == 0
+    assert st["max_energy_batch"] > 1 and st["energy_batches"] < n32
+    for r, o in zip(reqs, outs):
+        P = torch.from_numpy(r["params"]).cuda()
+        X = torch.from_numpy(np.ascontiguousarray(r["xyz"])).cuda()
+        T = torch.from_numpy(r["target"]).cuda()
+        G = torch.empty_like(P)
+        e = ctx.energy(P.data_ptr(), r["rs"].n_top, r["rs"].n_bottom, len(r["target"]),
+                       X.data_ptr(), T.data_ptr(), r["max_it"], 2.0, precision=r["precision"],
+                       d_grad=G.data_ptr())
+        g = G.cpu().numpy()
+        tol = 1e-5 if r["precision"] == lib.QJG_FP32 else 1e-12
+        assert abs(o["energy"] - e) <= tol * abs(e)
+        assert np.linalg.norm(o["grad"] - g) <= tol * np.linalg.norm(g)
