@@ -287,7 +287,8 @@ def run_ours(args, world, rank, local):
     if rank == 0 and not args.no_serve:
         from quijibo_gb300.benchmarks import bench_serve
         sargs = argparse.Namespace(seed=0, requests=args.serve_requests, scale=0.25, span=10.0,
-                                   workers=8, budget_gb=64.0, baseline_sample=10)
+                                   workers=8, budget_gb=64.0, baseline_sample=10,
+                                   baseline_max_voxels=1 << 24)
         serving = bench_serve(sargs)
 
     # the large-grid configuration (48/24 roots, 60 iterations, 2200^3 in

@@ -248,6 +248,12 @@ def _stream(seed, n, scale):
     from .samples import ShapeSDF, poisson_disk
     rng = np.random.RandomState(seed)
     reqs = []
+    # sample sets: two seeded Poisson-disk sets of the largest size, each
+    # with its own target shape; a request takes a prefix of one (dart
+    # throwing accepts points uniformly over the box, so a prefix is spread
+    # over it too)
+    big = int(200_000 * scale)
+    pools = {}
     for i in range(n):
         kind = rng.choice([lib.QJG_REQ_FIELD, lib.QJG_REQ_MESH, lib.QJG_REQ_ENERGY], p=[0.5, 0.2, 0.3])
         nr = int(rng.randint(4, 65))
@@ -255,11 +261,15 @@ def _stream(seed, n, scale):
         rs = draw_rootset(1000 + i, nr - nb if nr - nb >= 1 else 1, nb, -1.2, 1.2, exps=(1, 2))
         max_it = int(rng.randint(10, 61))
         if kind == lib.QJG_REQ_ENERGY:
-            ns = int(np.exp(rng.uniform(np.log(10_000), np.log(200_000))) * scale)
-            xyz, _ = poisson_disk(max(ns, 64), seed=i)
+            ns = max(64, int(np.exp(rng.uniform(np.log(10_000), np.log(200_000))) * scale))
+            pool = i % 2
+            if pool not in pools:
+                xyz = poisson_disk(max(big, 64), seed=pool)[0]
+                pools[pool] = (xyz, ShapeSDF(pool)(xyz))
+            xyz, target = pools[pool][0][:ns], pools[pool][1][:ns]
             rs.scale = conformal_scale(rs, Grid((16, 16, 16), lengths=(2.0, 2.0, 2.0)), 16)
             reqs.append(dict(kind=kind, rs=rs, params=lib.params_of(rs), xyz=xyz,
-                             target=ShapeSDF(i)(xyz), max_it=max_it, precision=lib.QJG_FP32))
+                             target=target, max_it=max_it, precision=lib.QJG_FP32))
         else:
             lo, hi = (32, 512) if kind == lib.QJG_REQ_FIELD else (128, 1024)
             res = max(8, int(np.exp(rng.uniform(np.log(lo), np.log(hi))) * scale))
@@ -267,9 +277,21 @@ def _stream(seed, n, scale):
             rs.scale = conformal_scale(rs, g, 16)
             r = dict(kind=kind, rs=rs, grid=g, max_it=max_it, precision=lib.QJG_FP32_REFINE)
             if kind == lib.QJG_REQ_MESH:
-                r.update(vert_cap=12 * res * res + 1024, tri_cap=24 * res * res + 1024)
+                r.update(vert_cap=24 * res * res + 4096, tri_cap=48 * res * res + 4096)
             reqs.append(r)
     return reqs
+
+
+def _failures(reqs, results):
+    """Requests that did not complete: index, kind, size, status and error."""
+    from . import lib
+    out = []
+    for i, (q, r) in enumerate(zip(reqs, results)):
+        if r["status"] != lib.QJG_STATUS_DONE:
+            size = q["grid"].res[0] if "grid" in q else len(q["target"])
+            out.append({"i": i, "kind": int(q["kind"]), "size": int(size), "roots": q["rs"].n_top +
+                        q["rs"].n_bottom, "status": int(r["status"]), "error": int(r["error"])})
+    return out
 
 
 def bench_serve(args):
@@ -302,7 +324,15 @@ def bench_serve(args):
            "max_ms": float(lat.max()), "throughput_req_s": len(reqs) / span,
            "gvox_s": vox / span / 1e9, "span_s": span, "peak_running": st["peak_running"],
            "failed": st["failed"], "batched": st["batched"], "batches": st["batches"],
-           "max_batch": st["max_batch"]}
+           "max_batch": st["max_batch"], "energy_batched": st["energy_batched"],
+           "energy_batches": st["energy_batches"], "max_energy_batch": st["max_energy_batch"],
+           "by_kind": {}, "failures": _failures(reqs, results)}
+    for kind, name in ((lib.QJG_REQ_FIELD, "field"), (lib.QJG_REQ_MESH, "mesh"),
+                       (lib.QJG_REQ_ENERGY, "energy")):
+        lk = np.array([r["latency_ms"] for r, q in zip(results, reqs) if q["kind"] == kind])
+        if len(lk):
+            out["by_kind"][name] = {"n": int(len(lk)), "p50_ms": float(np.percentile(lk, 50)),
+                                    "p99_ms": float(np.percentile(lk, 99))}
     # capacity: the same requests submitted at once
     srv = lib.Server(workers=args.workers, hbm_budget=int(args.budget_gb * (1 << 30)))
     srv.wait(srv.submit(**reqs[0]))
@@ -317,10 +347,17 @@ def bench_serve(args):
                     "span_s": span_b, "p50_ms": float(np.percentile(lat_b, 50)),
                     "p99_ms": float(np.percentile(lat_b, 99)), "peak_running": st_b["peak_running"],
                     "batched": st_b["batched"], "batches": st_b["batches"],
-                    "max_batch": st_b["max_batch"], "failed": st_b["failed"]}
+                    "max_batch": st_b["max_batch"], "energy_batched": st_b["energy_batched"],
+                    "energy_batches": st_b["energy_batches"],
+                    "max_energy_batch": st_b["max_energy_batch"], "failed": st_b["failed"],
+                    "failures": _failures(reqs, results_b)}
     # baseline: a sample of the same requests, plain FP64, one at a time
     ctx = lib.Context(0)
-    idx = list(range(0, len(reqs), max(1, len(reqs) // args.baseline_sample)))
+    # evenly spaced requests, leaving out grids above baseline_max_voxels (a
+    # 1024^3 mesh in the plain FP64 form runs for many minutes)
+    small = [i for i, r in enumerate(reqs)
+             if "grid" not in r or r["grid"].n_voxels <= args.baseline_max_voxels]
+    idx = small[::max(1, len(small) // args.baseline_sample)]
     base_t, serve_t = [], []
     for i in idx:
         r = reqs[i]
@@ -348,7 +385,8 @@ def bench_serve(args):
         base_t.append(time.perf_counter() - t1)
         serve_t.append(results[i]["run_ms"] / 1e3)
     out["baseline_fp64_serial"] = {
-        "sampled_requests": len(idx), "mean_s": statistics.mean(base_t),
+        "sampled_requests": len(idx), "max_voxels": args.baseline_max_voxels,
+        "mean_s": statistics.mean(base_t),
         "throughput_req_s_est": 1.0 / statistics.mean(base_t),
         "served_run_s_same_requests": statistics.mean(serve_t)}
     return out
@@ -690,6 +728,7 @@ def main():
     ap.add_argument("--workers", type=int, default=8)
     ap.add_argument("--budget-gb", type=float, default=64.0)
     ap.add_argument("--baseline-sample", type=int, default=40)
+    ap.add_argument("--baseline-max-voxels", type=int, default=1 << 24)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--rel-tol", type=float, default=1e-6)
     ap.add_argument("--check-slices", type=int, default=4)
