@@ -38,6 +38,11 @@ extern "C" {
 #define QJG_REFINE_POW 0 /* the reference's polar QUATERNION::pow (reference rounding) */
 #define QJG_REFINE_INT 1 /* repeated products when every exponent is an integer */
 
+/* Transcendentals of the reference's QUATERNION::pow in the FP64 forms. */
+#define QJG_LIBM_DEVICE 0 /* the CUDA device library's acos/log/exp/sin/cos */
+#define QJG_LIBM_CR 1     /* correctly rounded acos/log/exp/sin/cos (slower): the values a C
+                             library with correctly rounded functions gives */
+
 typedef struct qjg_ctx qjg_ctx;
 typedef int32_t qjg_rootset;
 
@@ -67,7 +72,10 @@ typedef struct {
   int32_t form;      /* QJG_FORM_QUOTIENT: T(q) / B(q) (computeLogScaledPowerRationalMap);
                         QJG_FORM_LAGRANGE: RATIONAL_4D::evaluateLagrange order, top and bottom
                         factors interleaved (RATIONAL_4D.cpp:27-73), in every precision form */
-  int32_t pad_;
+  int32_t libm;      /* QJG_LIBM_DEVICE / QJG_LIBM_CR: the transcendentals of every FP64
+                        QUATERNION::pow (plain FP64 form, FP64 refine with QJG_REFINE_POW,
+                        the meshers' FP64 evaluations) and the final log|q_N| of those
+                        evaluations */
 } qjg_iter;
 
 typedef struct {

@@ -43,6 +43,16 @@ int qjg_set_energy_pairs(int on);
  * forward call): the units of the energy kernels' algorithmic FLOP counts. */
 int qjg_energy_last_work(qjg_ctx* ctx, int64_t* applications, int64_t* steps);
 
+/* The correctly rounded FP64 transcendentals of the QJG_LIBM_CR form, element
+ * by element on the device: y[i] = f(x[i]) for n device doubles on `stream`
+ * (for bit-for-bit comparison with the same functions built for the host). */
+#define QJG_CRM_EXP 0
+#define QJG_CRM_LOG 1
+#define QJG_CRM_SIN 2
+#define QJG_CRM_COS 3
+#define QJG_CRM_ACOS 4
+int qjg_crmath_eval(int fn, const double* d_x, double* d_y, int64_t n, void* stream);
+
 /* FP32 FMA-pipe probe: runs a kernel of independent FMA chains on every SM
  * of `device` and returns the achieved FP32 TFLOP/s (2 flops per FMA). */
 int qjg_fma_probe(int device, double* tflops);

@@ -79,6 +79,10 @@ class Oracle:
         L = C.CDLL(path)
         L.qjo_mt_rand.argtypes = [C.c_uint32, C.c_int, _dp]
         L.qjo_quat_pow.argtypes = [_dp, C.c_double, _dp]
+        L.qjo_set_libm.argtypes = [C.c_int]
+        L.qjo_set_libm.restype = None
+        L.qjo_crm.argtypes = [C.c_int, C.c_double]
+        L.qjo_crm.restype = C.c_double
         L.qjo_field.argtypes = [C.POINTER(_Map), C.POINTER(_Grid), C.c_int, C.c_double, C.c_int,
                                 C.c_int, _dp, _dp, C.POINTER(C.c_int32), C.c_int]
         L.qjo_field.restype = C.c_int64
@@ -108,6 +112,19 @@ class Oracle:
         out = np.empty(n)
         self.L.qjo_mt_rand(seed, n, _ptr(out))
         return out
+
+    def set_libm(self, correctly_rounded):
+        """Transcendentals of the map's QUATERNION::pow: False the C library's
+        (the reference build's), True the correctly rounded ones."""
+        self.L.qjo_set_libm(int(bool(correctly_rounded)))
+
+    CRM = ("exp", "log", "sin", "cos", "acos")
+
+    def crm(self, name, x):
+        """The correctly rounded function `name` on each element of x."""
+        fn = self.CRM.index(name)
+        x = np.ascontiguousarray(x, dtype=np.float64).ravel()
+        return np.array([self.L.qjo_crm(fn, float(v)) for v in x])
 
     def quat_pow(self, q, e):
         q = np.ascontiguousarray(q, dtype=np.float64)
@@ -405,6 +422,19 @@ class Reference:
         out = np.empty(n)
         self.L.ref_mt_rand(seed, n, _ptr(out))
         return out
+
+    def set_libm(self, correctly_rounded):
+        """Transcendentals of the map's QUATERNION::pow: False the C library's
+        (the reference build's), True the correctly rounded ones."""
+        self.L.qjo_set_libm(int(bool(correctly_rounded)))
+
+    CRM = ("exp", "log", "sin", "cos", "acos")
+
+    def crm(self, name, x):
+        """The correctly rounded function `name` on each element of x."""
+        fn = self.CRM.index(name)
+        x = np.ascontiguousarray(x, dtype=np.float64).ravel()
+        return np.array([self.L.qjo_crm(fn, float(v)) for v in x])
 
     def quat_pow(self, q, e):
         q = np.ascontiguousarray(q, dtype=np.float64)

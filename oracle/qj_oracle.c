@@ -17,6 +17,23 @@
 #endif
 
 #include "../quijibo_gb300/csrc/mc_cases.h"
+#include "../quijibo_gb300/csrc/qj_crmath.h"
+
+/* Transcendentals of qjo_quat_pow and of the escape loops' final log: the
+ * C library's (the reference build's) or, with qjo_set_libm(1), the
+ * correctly rounded ones of qj_crmath.h. */
+static int g_libm_cr = 0;
+void qjo_set_libm(int correctly_rounded) { g_libm_cr = correctly_rounded != 0; }
+
+double qjo_crm(int fn, double x) {
+  switch (fn) {
+    case 0: return crm_exp(x);
+    case 1: return crm_log(x);
+    case 2: return crm_sin(x);
+    case 3: return crm_cos(x);
+    default: return crm_acos(x);
+  }
+}
 
 /* SETTINGS.h:60 -- REAL_MIN is FLT_MIN whatever Real is. */
 #define QJO_REAL_MIN ((double)FLT_MIN)
@@ -80,12 +97,19 @@ void qjo_quat_pow(const double q[4], double e, double out[4]) {
   const double qm = sqrt(partial + q[0] * q[0]);
   const double vm = sqrt(partial);
   const double vminv = (vm > 0.0) ? 1.0 / vm : 0.0;
-  const double scale = e * acos(q[0] / qm) * vminv;
+  const double scale = e * (g_libm_cr ? crm_acos(q[0] / qm) : acos(q[0] / qm)) * vminv;
   const double mag = scale * vm;
   const double maginv = (mag > 0.0) ? 1.0 / mag : 0.0;
-  const double exps = exp(e * log(qm));
-  const double scale2 = scale * exps * maginv * sin(mag);
-  out[0] = exps * cos(mag);
+  const double exps = g_libm_cr ? crm_exp(e * crm_log(qm)) : exp(e * log(qm));
+  double sn, cs;
+  if (g_libm_cr) {
+    crm_sincos(mag, &sn, &cs);
+  } else {
+    sn = sin(mag);
+    cs = cos(mag);
+  }
+  const double scale2 = scale * exps * maginv * sn;
+  out[0] = exps * cs;
   out[1] = scale2 * q[1];
   out[2] = scale2 * q[2];
   out[3] = scale2 * q[3];
@@ -236,7 +260,7 @@ static double escape_value(const qjo_map* m, const double p[3], double slice, in
     executed++;
     if (mag < 10.0 * QJO_REAL_MIN) it = max_it;
   }
-  const double f = log(mag);
+  const double f = g_libm_cr ? crm_log(mag) : log(mag);
   if (de) *de = mag * f / dnorm;
   if (iters) *iters = executed;
   return f;
@@ -315,7 +339,7 @@ static double lagrange_value(const qjo_map* m, const double p[3], double slice, 
     it++;
     if (mag < 10.0 * QJO_REAL_MIN) it = max_it;
   }
-  const double f = log(mag) - iso;
+  const double f = (g_libm_cr ? crm_log(mag) : log(mag)) - iso;
   return isinf(f) ? 3.40282346638528859812e+38 : f;
 }
 

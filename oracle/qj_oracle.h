@@ -58,6 +58,14 @@ void qjo_cell_center(const qjo_grid* g, int x, int y, int z, double out[3]);
 /* Quaternion power (w,x,y,z) -> q^e. */
 void qjo_quat_pow(const double q[4], double e, double out[4]);
 
+/* 0: qjo_quat_pow and the escape loops call the C library's acos/log/exp/sin/cos (as the
+ * reference does); 1: the correctly rounded functions of qj_crmath.h. */
+void qjo_set_libm(int correctly_rounded);
+
+/* The correctly rounded functions themselves: fn 0 exp, 1 log, 2 sin,
+ * 3 cos, 4 acos. */
+double qjo_crm(int fn, double x);
+
 /* prod_i (q - r_i)^(sigma e_i), left to right. */
 void qjo_eval_factored(const qjo_poly* p, const double q[4], double out[4]);
 

@@ -294,6 +294,27 @@ def _failures(reqs, results):
     return out
 
 
+def _retry_capacity(srv, reqs, results):
+    """Mesh requests whose mesh outgrew their caps come back failed with
+    QJG_ERR_CAPACITY and the counts they need; a client resubmits them with
+    those caps.  The retried request's latency is both attempts' (the retry
+    runs after the stream).  Returns how many were retried."""
+    from . import lib
+    idx = [i for i, r in enumerate(results) if r["status"] != lib.QJG_STATUS_DONE and
+           r["error"] == lib.QJG_ERR_CAPACITY and reqs[i]["kind"] == lib.QJG_REQ_MESH]
+    tickets = []
+    for i in idx:
+        q = dict(reqs[i])
+        q["vert_cap"] = max(q["vert_cap"], int(results[i]["n_verts"]))
+        q["tri_cap"] = max(q["tri_cap"], int(results[i]["n_tris"]))
+        tickets.append(srv.submit(**q))
+    for i, t in zip(idx, tickets):
+        r = srv.wait(t)
+        r["latency_ms"] += results[i]["latency_ms"]
+        results[i] = r
+    return len(idx)
+
+
 def bench_serve(args):
     """Serving: Poisson arrivals into the continuous-batching server vs the
     same requests as plain FP64 launches one after another."""
@@ -315,6 +336,7 @@ def bench_serve(args):
     results = [srv.wait(t) for t in tickets]
     span = time.perf_counter() - t0
     st = srv.stats()
+    retried = _retry_capacity(srv, reqs, results)
     srv.close()
     lat = np.array([r["latency_ms"] for r in results])
     vox = sum(r["grid"].n_voxels for r in reqs if "grid" in r)
@@ -326,7 +348,7 @@ def bench_serve(args):
            "failed": st["failed"], "batched": st["batched"], "batches": st["batches"],
            "max_batch": st["max_batch"], "energy_batched": st["energy_batched"],
            "energy_batches": st["energy_batches"], "max_energy_batch": st["max_energy_batch"],
-           "by_kind": {}, "failures": _failures(reqs, results)}
+           "by_kind": {}, "capacity_retries": retried, "failures": _failures(reqs, results)}
     for kind, name in ((lib.QJG_REQ_FIELD, "field"), (lib.QJG_REQ_MESH, "mesh"),
                        (lib.QJG_REQ_ENERGY, "energy")):
         lk = np.array([r["latency_ms"] for r, q in zip(results, reqs) if q["kind"] == kind])
@@ -341,6 +363,7 @@ def bench_serve(args):
     results_b = [srv.wait(t) for t in tickets]
     span_b = time.perf_counter() - t0
     st_b = srv.stats()
+    retried_b = _retry_capacity(srv, reqs, results_b)
     srv.close()
     lat_b = np.array([r["latency_ms"] for r in results_b])
     out["burst"] = {"throughput_req_s": len(reqs) / span_b, "gvox_s": vox / span_b / 1e9,
@@ -350,7 +373,7 @@ def bench_serve(args):
                     "max_batch": st_b["max_batch"], "energy_batched": st_b["energy_batched"],
                     "energy_batches": st_b["energy_batches"],
                     "max_energy_batch": st_b["max_energy_batch"], "failed": st_b["failed"],
-                    "failures": _failures(reqs, results_b)}
+                    "capacity_retries": retried_b, "failures": _failures(reqs, results_b)}
     # baseline: a sample of the same requests, plain FP64, one at a time
     ctx = lib.Context(0)
     # evenly spaced requests, leaving out grids above baseline_max_voxels (a

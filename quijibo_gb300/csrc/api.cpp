@@ -108,6 +108,8 @@ int qj_check_iter(qjg_ctx* ctx, const qjg_iter* it) {
     return fail(ctx, QJG_ERR_ARG, "unknown refine_pow %d", it->refine_pow);
   if (it->form != QJG_FORM_QUOTIENT && it->form != QJG_FORM_LAGRANGE)
     return fail(ctx, QJG_ERR_ARG, "unknown form %d", it->form);
+  if (it->libm != QJG_LIBM_DEVICE && it->libm != QJG_LIBM_CR)
+    return fail(ctx, QJG_ERR_ARG, "unknown libm %d", it->libm);
   return QJG_OK;
 }
 
@@ -293,7 +295,7 @@ int qjg_field(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
   cudaStream_t s = (cudaStream_t)stream;
   const GridParams g = qj_grid_params(grid, z0, z1);
   IterParams it = qj_iter_params(iter, grid);
-  const bool pow_ref = iter->refine_pow == QJG_REFINE_POW || !m->all_int;
+  const int pow_mode = qj_pow_mode(iter, m->all_int);
   if (refine && ((rc = ensure(ctx, &ctx->d_list, &ctx->list_cap, (size_t)n)) ||
                  (rc = ensure(ctx, &ctx->d_sorted, &ctx->sorted_cap, (size_t)n)) ||
                  (rc = ensure(ctx, &ctx->d_keys, &ctx->keys_cap, (size_t)n)) ||
@@ -304,7 +306,7 @@ int qjg_field(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
   QJ_CUDA(ctx, cudaMemsetAsync(ctx->d_stats, 0, sizeof(DevStats), s));
   if (ctx->timing) QJ_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
   if (iter->precision == QJG_FP64) {
-    QJ_CUDA(ctx, qj::launch_field64(*m, g, it, pow_ref, d_field, d_de, ctx->d_stats, s));
+    QJ_CUDA(ctx, qj::launch_field64(*m, g, it, pow_mode, d_field, d_de, ctx->d_stats, s));
   } else {
     QJ_CUDA(ctx, qj::launch_field32(*m, g, it, refine, d_field, d_de, ctx->d_list, ctx->d_keys,
                                     rerun ? ctx->d_ff : nullptr, ctx->d_stats, s));
@@ -317,7 +319,7 @@ int qjg_field(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
     ctx->launches++;
   }
   if (refine) {
-    QJ_CUDA(ctx, qj::launch_refine64(*m, g, it, pow_ref, ctx->d_list, ctx->d_keys,
+    QJ_CUDA(ctx, qj::launch_refine64(*m, g, it, pow_mode, ctx->d_list, ctx->d_keys,
                                      ctx->d_sorted, ctx->d_hist, d_field, d_de, ctx->d_stats, s));
     ctx->launches += 4;  // histogram, offsets, scatter, refine
   }

@@ -56,7 +56,7 @@ __device__ __forceinline__ void warp_add(unsigned long long* dst, unsigned long 
 
 // One application of the map in reference order (OPTIMIZE_3D.cpp:1331-1350),
 // plus |grad log|R|| for the distance estimate when DE is set.
-template <bool POW_REF, bool DE>
+template <int POW_REF, bool DE>
 __global__ void __launch_bounds__(128) field64_kernel(const __grid_constant__ MapParams m,
                                                       const GridParams g, const IterParams it, double* __restrict__ field,
                                                       float* __restrict__ de, DevStats* st) {
@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(128) field64_kernel(const __grid_constant__ Ma
 }
 
 // FP64 recomputation of the voxels in `list` (local linear indices).
-template <bool POW_REF>
+template <int POW_REF>
 __global__ void __launch_bounds__(128) refine64_kernel(const __grid_constant__ MapParams m,
                                                        const GridParams g,
                                                        const IterParams it, const uint32_t* list,
@@ -594,25 +594,25 @@ static int grid_blocks(const void* fn, int threads) {
 }
 
 cudaError_t launch_field64(const MapParams& m, const GridParams& g, const IterParams& it,
-                           bool pow_ref, double* field, float* de, DevStats* st,
+                           int pow_mode, double* field, float* de, DevStats* st,
                            cudaStream_t s) {
-  const void* fn;
-  if (pow_ref)
-    fn = it.want_de ? (const void*)field64_kernel<true, true> : (const void*)field64_kernel<true, false>;
+#define QJ_F64(P)                                                                              \
+  do {                                                                                         \
+    const void* fn = it.want_de ? (const void*)field64_kernel<P, true>                          \
+                                : (const void*)field64_kernel<P, false>;                       \
+    const int blocks = grid_blocks(fn, 128);                                                   \
+    if (it.want_de)                                                                            \
+      field64_kernel<P, true><<<blocks, 128, 0, s>>>(m, g, it, field, de, st);                 \
+    else                                                                                       \
+      field64_kernel<P, false><<<blocks, 128, 0, s>>>(m, g, it, field, de, st);                \
+  } while (0)
+  if (pow_mode == 2)
+    QJ_F64(2);
+  else if (pow_mode == 1)
+    QJ_F64(1);
   else
-    fn = it.want_de ? (const void*)field64_kernel<false, true> : (const void*)field64_kernel<false, false>;
-  const int blocks = grid_blocks(fn, 128);
-  if (pow_ref) {
-    if (it.want_de)
-      field64_kernel<true, true><<<blocks, 128, 0, s>>>(m, g, it, field, de, st);
-    else
-      field64_kernel<true, false><<<blocks, 128, 0, s>>>(m, g, it, field, de, st);
-  } else {
-    if (it.want_de)
-      field64_kernel<false, true><<<blocks, 128, 0, s>>>(m, g, it, field, de, st);
-    else
-      field64_kernel<false, false><<<blocks, 128, 0, s>>>(m, g, it, field, de, st);
-  }
+    QJ_F64(0);
+#undef QJ_F64
   return cudaGetLastError();
 }
 
@@ -743,7 +743,7 @@ static int sm_count() {
 }
 
 cudaError_t launch_refine64(const MapParams& m, const GridParams& g, const IterParams& it,
-                            bool pow_ref, const uint32_t* list, const uint8_t* keys,
+                            int pow_mode, const uint32_t* list, const uint8_t* keys,
                             uint32_t* sorted, unsigned* hist, double* field, float* de,
                             DevStats* st, cudaStream_t s) {
   if (keys) {
@@ -755,12 +755,18 @@ cudaError_t launch_refine64(const MapParams& m, const GridParams& g, const IterP
     refine_scatter_kernel<<<blocks, 256, 0, s>>>(list, keys, st, hist, sorted);
     list = sorted;
   }
-  const void* fn = pow_ref ? (const void*)refine64_kernel<true> : (const void*)refine64_kernel<false>;
-  const int blocks = grid_blocks(fn, 128);
-  if (pow_ref)
-    refine64_kernel<true><<<blocks, 128, 0, s>>>(m, g, it, list, st, field, de, st);
+#define QJ_R64(P)                                                                    \
+  do {                                                                               \
+    const int blocks = grid_blocks((const void*)refine64_kernel<P>, 128);            \
+    refine64_kernel<P><<<blocks, 128, 0, s>>>(m, g, it, list, st, field, de, st);    \
+  } while (0)
+  if (pow_mode == 2)
+    QJ_R64(2);
+  else if (pow_mode == 1)
+    QJ_R64(1);
   else
-    refine64_kernel<false><<<blocks, 128, 0, s>>>(m, g, it, list, st, field, de, st);
+    QJ_R64(0);
+#undef QJ_R64
   return cudaGetLastError();
 }
 

@@ -88,7 +88,7 @@ extern "C" int qjg_field_noalloc(int32_t n_top, const double* top_roots, const d
   const qj::GridParams g = qj_grid_params(grid, z0, z1);
   const qj::IterParams it = qj_iter_params(iter, grid);
   const bool refine = iter->precision == QJG_FP32_REFINE;
-  const bool pow_ref = iter->refine_pow == QJG_REFINE_POW || !m.all_int;
+  const int pow_mode = qj_pow_mode(iter, m.all_int);
   // the counters (work-queue position, refine-list length) start at zero
   if (cudaMemsetAsync(st, 0, sizeof(qj::DevStats), s) != cudaSuccess) return QJG_ERR_CUDA;
   // voxels whose tracked FP32 error exceeds rel_tol are re-run with a
@@ -96,14 +96,14 @@ extern "C" int qjg_field_noalloc(int32_t n_top, const double* top_roots, const d
   const bool rerun = refine && it.est_tol > 0.0 && m.all_int;
   cudaError_t e;
   if (iter->precision == QJG_FP64)
-    e = qj::launch_field64(m, g, it, pow_ref, d_field, d_de, st, s);
+    e = qj::launch_field64(m, g, it, pow_mode, d_field, d_de, st, s);
   else
     e = qj::launch_field32(m, g, it, refine, d_field, d_de, list, nullptr,
                            rerun ? ff_list : nullptr, st, s);
   if (e == cudaSuccess && rerun)
     e = qj::launch_rerun_ff(m, g, it, ff_list, d_field, d_de, list, nullptr, st, s);
   if (e == cudaSuccess && refine)
-    e = qj::launch_refine64(m, g, it, pow_ref, list, nullptr, nullptr, nullptr, d_field, d_de, st,
+    e = qj::launch_refine64(m, g, it, pow_mode, list, nullptr, nullptr, nullptr, d_field, d_de, st,
                             s);
   return e == cudaSuccess ? QJG_OK : QJG_ERR_CUDA;
 }

@@ -826,7 +826,7 @@ struct DegenEmit : DegenCount {
 // first and trusted when its value clears its error bound and the 1e-8 stop
 // test by a margin: then the FP64 value has the same sign and also fails the
 // stop test, so every decision of the search is the one FP64 would make.
-template <bool POW_REF>
+template <int POW_REF>
 __device__ __forceinline__ double value64(const MapParams& m, const GridParams& g,
                                           const IterParams& it, const double p[3], double iso,
                                           unsigned long long* e64) {
@@ -837,7 +837,7 @@ __device__ __forceinline__ double value64(const MapParams& m, const GridParams& 
   return q64::sub(escape64<POW_REF, false>(m, it, p, g.slice, &ni, &dd), iso);
 }
 
-template <bool POW_REF, bool HYBRID>
+template <int POW_REF, bool HYBRID>
 __device__ __forceinline__ double bisect_value(const MapParams& m, const GridParams& g,
                                                const IterParams& it, const double p[3], double iso,
                                                unsigned long long* e32, unsigned long long* e64) {
@@ -853,7 +853,7 @@ __device__ __forceinline__ double bisect_value(const MapParams& m, const GridPar
   return value64<POW_REF>(m, g, it, p, iso, e64);
 }
 
-template <bool BISECT, bool POW_REF, bool HYBRID>
+template <bool BISECT, int POW_REF, bool HYBRID>
 __global__ void __launch_bounds__(128) vertex_kernel(const __grid_constant__ MapParams m,
                                                      const GridParams g, const IterParams it,
                                                      const uint32_t* __restrict__ list, long long n,
@@ -983,7 +983,7 @@ __device__ __forceinline__ void edge_point(const EdgeState& e, double p[3]) {
 
 // Runs the edge until it is done (returns false; the vertex is written and
 // *bad set) or needs an FP64 value (returns true).
-template <bool POW_REF>
+template <int POW_REF>
 __device__ bool edge_advance(const MapParams& m, const GridParams& g, const IterParams& it,
                              EdgeState& e, double iso, double* vert, bool* bad,
                              unsigned long long* e32) {
@@ -1113,7 +1113,7 @@ __device__ __forceinline__ void edge_counts(unsigned long long e32, unsigned lon
 }
 
 // Starts every edge of the slab; edges that need FP64 go to `park`.
-template <bool POW_REF>
+template <int POW_REF>
 __global__ void __launch_bounds__(128) edge_start_kernel(const __grid_constant__ MapParams m,
                                                          const GridParams g, const IterParams it,
                                                          const uint32_t* __restrict__ list,
@@ -1202,7 +1202,7 @@ __global__ void __launch_bounds__(128) edge_ff_kernel(const __grid_constant__ Ma
 }
 
 // The FP64 value of every parked edge's point.
-template <bool POW_REF>
+template <int POW_REF>
 __global__ void __launch_bounds__(128) edge_fp64_kernel(const __grid_constant__ MapParams m,
                                                         const GridParams g, const IterParams it,
                                                         const uint32_t* __restrict__ park,
@@ -1224,7 +1224,7 @@ __global__ void __launch_bounds__(128) edge_fp64_kernel(const __grid_constant__ 
 }
 
 // Resumes the parked edges; those that need FP64 again go to `next`.
-template <bool POW_REF>
+template <int POW_REF>
 __global__ void __launch_bounds__(128) edge_resume_kernel(const __grid_constant__ MapParams m,
                                                           const GridParams g, const IterParams it,
                                                           const uint32_t* __restrict__ park,
@@ -1373,7 +1373,7 @@ cudaError_t mesh_triangles(const MeshWindow& w, const McCube* cubes, long long n
   return cudaGetLastError();
 }
 
-template <bool POW_REF>
+template <int POW_REF>
 static cudaError_t parked_start(const MapParams& m, const GridParams& g, const IterParams& it,
                                 const MeshWindow& w, long long n, long long id0, int c0,
                                 double* verts, double iso, DevStats* st, const EdgeScratch& sc,
@@ -1385,7 +1385,7 @@ static cudaError_t parked_start(const MapParams& m, const GridParams& g, const I
   return cudaGetLastError();
 }
 
-template <bool POW_REF>
+template <int POW_REF>
 static cudaError_t parked_finish(const MapParams& m, const GridParams& g, const IterParams& it,
                                  double* verts, double iso, DevStats* st, const EdgeScratch& sc,
                                  cudaStream_t s) {
@@ -1418,29 +1418,33 @@ static cudaError_t parked_finish(const MapParams& m, const GridParams& g, const 
 }
 
 cudaError_t mesh_parked_finish(const MapParams& m, const GridParams& g, const IterParams& it,
-                               bool pow_ref, double* verts, double iso, DevStats* st,
+                               int pow_mode, double* verts, double iso, DevStats* st,
                                const EdgeScratch& sc, cudaStream_t s) {
-  return pow_ref ? parked_finish<true>(m, g, it, verts, iso, st, sc, s)
-                 : parked_finish<false>(m, g, it, verts, iso, st, sc, s);
+  return pow_mode == 2 ? parked_finish<2>(m, g, it, verts, iso, st, sc, s)
+         : pow_mode   ? parked_finish<1>(m, g, it, verts, iso, st, sc, s)
+                      : parked_finish<0>(m, g, it, verts, iso, st, sc, s);
 }
 
 cudaError_t mesh_vertices(const MapParams& m, const GridParams& g, const IterParams& it,
-                          int edge_mode, bool pow_ref, bool hybrid, const MeshWindow& w,
+                          int edge_mode, int pow_mode, bool hybrid, const MeshWindow& w,
                           long long n, long long id0, int c0, const double* src, double* verts,
                           double iso, DevStats* st, const EdgeScratch* scratch, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   if (edge_mode != 0 && hybrid && scratch)
-    return pow_ref ? parked_start<true>(m, g, it, w, n, id0, c0, verts, iso, st, *scratch, s)
-                   : parked_start<false>(m, g, it, w, n, id0, c0, verts, iso, st, *scratch, s);
+    return pow_mode == 2 ? parked_start<2>(m, g, it, w, n, id0, c0, verts, iso, st, *scratch, s)
+           : pow_mode   ? parked_start<1>(m, g, it, w, n, id0, c0, verts, iso, st, *scratch, s)
+                        : parked_start<0>(m, g, it, w, n, id0, c0, verts, iso, st, *scratch, s);
   const int blocks = (int)std::min<long long>((n + 127) / 128, (long long)sm_count() * 32);
 #define QJ_VK(B, P, H) \
   vertex_kernel<B, P, H><<<blocks, 128, 0, s>>>(m, g, it, w.list, n, id0, c0, src, verts, iso, st)
   if (edge_mode == 0)
-    QJ_VK(false, false, false);
-  else if (pow_ref)
-    hybrid ? QJ_VK(true, true, true) : QJ_VK(true, true, false);
+    QJ_VK(false, 0, false);
+  else if (pow_mode == 2)
+    hybrid ? QJ_VK(true, 2, true) : QJ_VK(true, 2, false);
+  else if (pow_mode)
+    hybrid ? QJ_VK(true, 1, true) : QJ_VK(true, 1, false);
   else
-    hybrid ? QJ_VK(true, false, true) : QJ_VK(true, false, false);
+    hybrid ? QJ_VK(true, 0, true) : QJ_VK(true, 0, false);
 #undef QJ_VK
   return cudaGetLastError();
 }

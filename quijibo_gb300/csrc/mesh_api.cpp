@@ -146,7 +146,7 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
   const GridParams g = qj_grid_params(grid, 0, Z);
   IterParams it{};
   if (iter) it = qj_iter_params(iter, grid);
-  const bool pow_ref = !iter || iter->refine_pow == QJG_REFINE_POW || !m->all_int;
+  const int pow_mode = qj_pow_mode(iter, m->all_int);
   const long long S = (X + 63) / 64;  // units per row (qj::mesh_units)
 
   long long nv = 0, nt = 0;
@@ -273,7 +273,7 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
       esc.list[0] = ctx->m_epark;
       esc.count = ctx->m_ecount;
     }
-    QJ_CUDA(ctx, qj::mesh_vertices(*m, g, it, edge_mode, pow_ref, hybrid, w, n_new, nv, c0, src,
+    QJ_CUDA(ctx, qj::mesh_vertices(*m, g, it, edge_mode, pow_mode, hybrid, w, n_new, nv, c0, src,
                                    ctx->m_verts, iso, ctx->d_mstats, parked ? &esc : nullptr, s));
     if (n_new) ctx->launches++;
     nv += n_new;
@@ -314,7 +314,7 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
     esc.list[1] = ctx->m_epark + nv;
     esc.list[2] = ctx->m_epark + 2 * nv;
     esc.count = ctx->m_ecount;
-    QJ_CUDA(ctx, qj::mesh_parked_finish(*m, g, it, pow_ref, ctx->m_verts, iso, ctx->d_mstats, esc,
+    QJ_CUDA(ctx, qj::mesh_parked_finish(*m, g, it, pow_mode, ctx->m_verts, iso, ctx->d_mstats, esc,
                                         s));
     QJ_CUDA(ctx, mark(1));
     QJ_CUDA(ctx, span(0, 1, &st.ms_vertices));

@@ -128,6 +128,12 @@ int qj_fill_map(qj::MapParams* m, int n_top, const double* top_roots, const doub
                 double sigma_bot, double scale);
 int qj_check_grid(qjg_ctx* ctx, const qjg_grid* g);
 int qj_check_iter(qjg_ctx* ctx, const qjg_iter* it);
+// pow_mode of the FP64 kernels (qj_kernels.h) for these settings: the
+// reference's polar pow unless integer products were asked for and apply
+inline int qj_pow_mode(const qjg_iter* it, bool all_int) {
+  const bool pow_ref = !it || it->refine_pow == QJG_REFINE_POW || !all_int;
+  return pow_ref ? (it && it->libm == QJG_LIBM_CR ? 2 : 1) : 0;
+}
 qj::GridParams qj_grid_params(const qjg_grid* g, int z0, int z1);
 qj::IterParams qj_iter_params(const qjg_iter* it, const qjg_grid* g);
 qj::MapParams* qj_lookup(qjg_ctx* ctx, qjg_rootset rs);

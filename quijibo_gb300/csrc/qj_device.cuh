@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "qj_crmath.h"
 #include "qj_params.h"
 
 namespace qj {
@@ -67,6 +68,30 @@ __device__ __forceinline__ Q qpow(const Q& q, double e) {
   const double exps = exp(mul(e, log(qm)));
   double s, c;
   sincos(m, &s, &c);
+  const double scale2 = mul(mul(mul(scale, exps), minv), s);
+  Q o;
+  o.w = mul(exps, c);
+  o.x = mul(scale2, q.x);
+  o.y = mul(scale2, q.y);
+  o.z = mul(scale2, q.z);
+  return o;
+}
+
+// QUATERNION::pow with correctly rounded acos, log, exp, sin and cos
+// (qj_crmath.h) in place of the device library's: the reference's operation
+// order, and the values a C library with correctly rounded transcendentals
+// would give.
+__device__ __forceinline__ Q qpow_cr(const Q& q, double e) {
+  const double partial = add(add(mul(q.x, q.x), mul(q.y, q.y)), mul(q.z, q.z));
+  const double qm = __dsqrt_rn(add(partial, mul(q.w, q.w)));
+  const double vm = __dsqrt_rn(partial);
+  const double vminv = (vm > 0.0) ? __ddiv_rn(1.0, vm) : 0.0;
+  const double scale = mul(mul(e, crm_acos(__ddiv_rn(q.w, qm))), vminv);
+  const double m = mul(scale, vm);
+  const double minv = (m > 0.0) ? __ddiv_rn(1.0, m) : 0.0;
+  const double exps = crm_exp(mul(e, crm_log(qm)));
+  double s, c;
+  crm_sincos(m, &s, &c);
   const double scale2 = mul(mul(mul(scale, exps), minv), s);
   Q o;
   o.w = mul(exps, c);
@@ -312,7 +337,7 @@ __device__ __forceinline__ double trilinear(const WeightGrid& wg, const double* 
 // with DE, adds sign * sum e_i (q - r_i) / |q - r_i|^2 to g.
 // One root term (q - r_i)^(e_i) (POLYNOMIAL_4D::evaluateRoot,
 // POLYNOMIAL_4D.cpp:928-940); with DE, adds sign * e_i d/|d|^2 to g.
-template <bool POW_REF, bool DE>
+template <int POW_REF, bool DE>
 __device__ __forceinline__ q64::Q term64(const MapParams& m, const q64::Q& q, int i, double sign,
                                          q64::Q& g) {
   using namespace q64;
@@ -329,10 +354,10 @@ __device__ __forceinline__ q64::Q term64(const MapParams& m, const q64::Q& q, in
     g.y += k * d.y;
     g.z += k * d.z;
   }
-  return POW_REF ? qpow(d, m.e64[i]) : qpow_int(d, m.ie[i]);
+  return POW_REF == 2 ? qpow_cr(d, m.e64[i]) : POW_REF ? qpow(d, m.e64[i]) : qpow_int(d, m.ie[i]);
 }
 
-template <bool POW_REF, bool DE>
+template <int POW_REF, bool DE>
 __device__ __forceinline__ q64::Q product64(const MapParams& m, const q64::Q& q, int lo, int hi,
                                             double sign, q64::Q& g) {
   using namespace q64;
@@ -348,7 +373,7 @@ __device__ __forceinline__ q64::Q product64(const MapParams& m, const q64::Q& q,
 // RATIONAL_4D::evaluateLagrange (RATIONAL_4D.cpp:27-73): from 1, times top
 // term k then divided by bottom term k for the common k, then the longer
 // side's leftovers; without bottom roots the plain factored top.
-template <bool POW_REF, bool DE>
+template <int POW_REF, bool DE>
 __device__ __forceinline__ q64::Q lagrange64(const MapParams& m, const q64::Q& q, q64::Q& g) {
   using namespace q64;
   if (m.nb == 0) return product64<POW_REF, DE>(m, q, 0, m.nt, 1.0, g);
@@ -369,7 +394,7 @@ __device__ __forceinline__ q64::Q lagrange64(const MapParams& m, const q64::Q& q
 // One application of the map in reference order (OPTIMIZE_3D.cpp:1331-1350),
 // plus |grad log|R|| for the distance estimate when DE is set.
 // With `lagrange`, the map in the Lagrange order (TRIANGLE_MESH.cpp:281-322).
-template <bool POW_REF, bool DE>
+template <int POW_REF, bool DE>
 __device__ __forceinline__ q64::Q apply64(const MapParams& m, const q64::Q& q, double* gnorm,
                                           bool lagrange = false) {
   using namespace q64;
@@ -395,7 +420,7 @@ __device__ __forceinline__ q64::Q apply64(const MapParams& m, const q64::Q& q, d
 
 // The escape loop for one start point; returns log|q_N| and the executed
 // iteration count; *de = |q_N| log|q_N| / |q_N'| when DE.
-template <bool POW_REF, bool DE>
+template <int POW_REF, bool DE>
 __device__ __forceinline__ double escape64(const MapParams& m, const IterParams& it,
                                            const double p[3], double slice, int* iters,
                                            double* de) {
@@ -414,7 +439,7 @@ __device__ __forceinline__ double escape64(const MapParams& m, const IterParams&
     executed++;
     if (mg < tiny) n = it.max_it;  // the "black hole" exit, OPTIMIZE_3D.cpp:1358-1359
   }
-  const double f = log(mg);
+  const double f = POW_REF == 2 ? crm_log(mg) : log(mg);
   *iters = executed;
   if (DE) *de = mg * f / dn;
   return f;
@@ -425,7 +450,7 @@ __device__ __forceinline__ double escape64(const MapParams& m, const IterParams&
 // the previous one and stops, and an infinite value becomes FLT_MAX.  (The
 // reference leaves the previous magnitude unset when the first application
 // overflows; here it is |q_0|.)
-template <bool POW_REF>
+template <int POW_REF>
 __device__ __forceinline__ double lagrange_value64(const MapParams& m, const IterParams& it,
                                                    const double p[3], double slice, double iso) {
   using namespace q64;
@@ -448,7 +473,7 @@ __device__ __forceinline__ double lagrange_value64(const MapParams& m, const Ite
     n++;
     if (mg < tiny) n = it.max_it;
   }
-  const double f = sub(log(mg), iso);
+  const double f = sub(POW_REF == 2 ? crm_log(mg) : log(mg), iso);
   return isinf(f) ? 3.40282346638528859812e+38 : f;
 }
 

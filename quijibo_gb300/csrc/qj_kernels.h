@@ -67,8 +67,11 @@ long long batch_item_tiles(int X, int Y, int Z);
 cudaError_t launch_field_batch(const BatchBuffers& b, const BatchShapes& sh, cudaStream_t s);
 
 // field.cu
+// pow_mode of the FP64 kernels: 0 integer powers as repeated products, 1 the
+// reference's polar QUATERNION::pow with the device library's transcendentals,
+// 2 the same with correctly rounded ones (qj_crmath.h).
 cudaError_t launch_field64(const MapParams& m, const GridParams& g, const IterParams& it,
-                           bool pow_ref, double* field, float* de, DevStats* st, cudaStream_t s);
+                           int pow_mode, double* field, float* de, DevStats* st, cudaStream_t s);
 // FP32 bulk pass; with refine, appends the voxels to re-evaluate in FP64 to
 // `list` (with each one's FP32 orbit length in `keys` when not null) and,
 // when `ff_list` is not null, it.est_tol > 0 and the exponents are integers,
@@ -88,7 +91,7 @@ void set_field32_pairs(int on);
 // REFINE_KEYS counters) so that each warp gets orbits of one length.
 constexpr int REFINE_KEYS = 256;
 cudaError_t launch_refine64(const MapParams& m, const GridParams& g, const IterParams& it,
-                            bool pow_ref, const uint32_t* list, const uint8_t* keys,
+                            int pow_mode, const uint32_t* list, const uint8_t* keys,
                             uint32_t* sorted, unsigned* hist, double* field, float* de,
                             DevStats* st, cudaStream_t s);
 

@@ -77,17 +77,17 @@ struct EdgeScratch {
   unsigned long long* count;  // their three lengths
 };
 size_t mesh_edge_state_bytes();
-// Vertex placement.  With hybrid bisection and a scratch, the edges that
+// Vertex placement (pow_mode as for launch_field64).  With hybrid bisection and a scratch, the edges that
 // need FP64 values are parked and their vertices written by
 // mesh_parked_finish after the last slab.
 cudaError_t mesh_vertices(const MapParams& m, const GridParams& g, const IterParams& it,
-                          int edge_mode, bool pow_ref, bool hybrid, const MeshWindow& w,
+                          int edge_mode, int pow_mode, bool hybrid, const MeshWindow& w,
                           long long n, long long id0, int c0, const double* src, double* verts,
                           double iso, DevStats* st, const EdgeScratch* scratch, cudaStream_t s);
 // Resolves every parked edge: rounds of one batched FP64 evaluation per
 // parked edge and a resumption (host reads of the list sizes in between).
 cudaError_t mesh_parked_finish(const MapParams& m, const GridParams& g, const IterParams& it,
-                               bool pow_ref, double* verts, double iso, DevStats* st,
+                               int pow_mode, double* verts, double iso, DevStats* st,
                                const EdgeScratch& sc, cudaStream_t s);
 cudaError_t mesh_filter(const int32_t* tris, long long n, const double* verts, int32_t* out,
                         long long* bsum, long long* n_keep, cudaStream_t s);

@@ -13,8 +13,11 @@ from .rootsets import Grid, RootSet
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libquijibo_gpu.so")
 
+QJG_OK, QJG_ERR_ARG, QJG_ERR_CUDA, QJG_ERR_NOMEM, QJG_ERR_HANDLE, QJG_ERR_CAPACITY = 0, -1, -2, -3, -4, -5
 QJG_FP64, QJG_FP32, QJG_FP32_REFINE = 0, 1, 2
 QJG_REFINE_POW, QJG_REFINE_INT = 0, 1
+QJG_LIBM_DEVICE, QJG_LIBM_CR = 0, 1
+CRM_FUNCTIONS = ("exp", "log", "sin", "cos", "acos")  # qjg_crmath_eval's fn order
 
 _dp = C.POINTER(C.c_double)
 _fp = C.POINTER(C.c_float)
@@ -39,7 +42,7 @@ class QjgIter(C.Structure):
     _fields_ = [("max_it", C.c_int32), ("precision", C.c_int32), ("refine_pow", C.c_int32),
                 ("want_de", C.c_int32), ("escape", C.c_double), ("band_h", C.c_double),
                 ("field_tol", C.c_double), ("rel_tol", C.c_double), ("form", C.c_int32),
-                ("pad_", C.c_int32)]
+                ("libm", C.c_int32)]
 
 
 class QjgFieldStats(C.Structure):
@@ -262,6 +265,7 @@ EXPORTS = {
     "qjg_last_timings": ([C.c_void_p, _fp, _fp], C.c_int),
     "qjg_launch_count": ([C.c_void_p], C.c_int64),
     "qjg_fma_probe": ([C.c_int, _dp], C.c_int),
+    "qjg_crmath_eval": ([C.c_int, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p], C.c_int),
     "qjg_set_field32_pairs": ([C.c_int], C.c_int),
 }
 
@@ -447,6 +451,15 @@ def set_field32_pairs(on):
     load().qjg_set_field32_pairs(int(bool(on)))
 
 
+def crmath_eval(name, d_x, d_y, n, stream=None):
+    """y[i] = f(x[i]) on the device with the correctly rounded FP64 function
+    `name` (one of CRM_FUNCTIONS) of the QJG_LIBM_CR form; device pointers."""
+    rc = load().qjg_crmath_eval(CRM_FUNCTIONS.index(name), C.c_void_p(d_x), C.c_void_p(d_y),
+                                int(n), C.c_void_p(stream or 0))
+    if rc != 0:
+        raise QjgError("qjg_crmath_eval failed (%d)" % rc)
+
+
 def fma_probe(device=0):
     """Achieved FP32 TFLOP/s of an FMA-chain probe kernel on every SM."""
     v = C.c_double()
@@ -558,10 +571,11 @@ class Context:
 
     @staticmethod
     def iter_params(max_it, escape, precision=QJG_FP64, refine_pow=QJG_REFINE_POW, want_de=False,
-                    band_h=2.0, field_tol=1e-3, rel_tol=0.0, lagrange=False):
+                    band_h=2.0, field_tol=1e-3, rel_tol=0.0, lagrange=False,
+                    libm=QJG_LIBM_DEVICE):
         return QjgIter(int(max_it), int(precision), int(refine_pow), int(bool(want_de)),
                        float(escape), float(band_h), float(field_tol), float(rel_tol),
-                       int(bool(lagrange)), 0)
+                       int(bool(lagrange)), int(libm))
 
     def field(self, handle, grid: Grid, it: QjgIter, d_field, d_de=None, z0=0, z1=None,
               stream=None):
