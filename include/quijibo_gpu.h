@@ -410,6 +410,30 @@ int qjg_server_wait(qjg_server* srv, int64_t ticket, qjg_result* out);
 int qjg_server_drain(qjg_server* srv);
 int qjg_server_read_stats(qjg_server* srv, qjg_server_stats* out);
 
+/* ---- finite-difference root gradients ---------------------------------- */
+
+/* Central differences, step eps = lengths[0] / res[0], of OPTIMIZE_3D's
+ * binary-score objectives with respect to every root component (entry
+ * 4 k + c for root k, component c of (w, x, y, z)); every moved map is
+ * evaluated in one pass, FP64 in the reference's operation order, so the
+ * scores and gradients are the reference's.  The map takes the root set's
+ * roots and scale s (_expScaling); exponents and power scalars are unused.
+ * d_dist (and d_curv) are X*Y*Z device doubles on `grid` (the reference's
+ * _distanceField and _curvatureField share the fractal's grid).  grad is a
+ * host array; *score (optional) receives the unmoved map's score. */
+#define QJG_FD_LOG_RATIONAL 0        /* computeLogRationalCenteredGradient
+                                        (src/solvers/OPTIMIZE_3D.cpp:2872-2951): binary score
+                                        (:2275-2297) of computeLogRationalMap (:1907-1985);
+                                        4 (nt + nb) entries, top roots first */
+#define QJG_FD_LOG_RATIONAL_BOTTOM 1 /* computeLogRationalBottomCenteredGradient (:2956-3008):
+                                        the same, bottom roots only; 4 nb entries */
+#define QJG_FD_POLYNOMIAL 2          /* computeCenteredGradient (:2761-2812): (binary + curvature
+                                        score (:2497-2537)) / 2 of computeMap (:853-980), the
+                                        top polynomial alone; 4 nt entries; needs d_curv */
+int qjg_centered_gradient(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, int32_t max_it,
+                          int32_t kind, const double* d_dist, const double* d_curv, double* grad,
+                          double* score, void* stream);
+
 /* ---- optimizer set-up passes ------------------------------------------ */
 
 /* The weight field of a signed distance field (X*Y*Z doubles, device):

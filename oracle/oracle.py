@@ -103,6 +103,9 @@ class Oracle:
         L.qjo_tanh_score_grad.argtypes = [C.POINTER(_Map), C.POINTER(_Grid), C.POINTER(_Grid), _dp,
                                           C.c_int, C.c_double, C.c_double, _dp, _dp]
         L.qjo_tanh_score_grad.restype = C.c_double
+        L.qjo_centered_gradient.argtypes = [C.POINTER(_Map), C.POINTER(_Grid), C.c_int, C.c_int,
+                                            _dp, _dp, _dp, _dp]
+        L.qjo_centered_gradient.restype = None
         L.qjo_sqerr_energy.argtypes = [C.POINTER(_Map), C.c_int64, _dp, _dp, C.c_double, C.c_int,
                                        C.c_double, C.c_double, C.POINTER(C.c_int32)]
         L.qjo_sqerr_energy.restype = C.c_double
@@ -194,6 +197,18 @@ class Oracle:
                                         threshold, _ptr(grad), _ptr(field))
         return sc, grad, field.reshape(grid.res[::-1])
 
+    def centered_gradient(self, rootset, grid, max_it, kind, dist, curv=None):
+        """(score, gradient) of the centered root gradients (kind 0 log-rational,
+        1 its bottom-root form, 2 computeCenteredGradient)."""
+        d = np.ascontiguousarray(dist, dtype=np.float64).reshape(-1)
+        cv = None if curv is None else np.ascontiguousarray(curv, dtype=np.float64).reshape(-1)
+        nt, nb = rootset.n_top, rootset.n_bottom
+        grad = np.empty(4 * (nt + nb if kind == 0 else nb if kind == 1 else nt))
+        sc = np.empty(1)
+        self.L.qjo_centered_gradient(C.byref(make_map(rootset)), C.byref(make_grid(grid)), max_it,
+                                     kind, _ptr(d), _ptr(cv), _ptr(grad), _ptr(sc))
+        return float(sc[0]), grad
+
     def sqerr_energy(self, rootset, xyz, target, max_it, escape, slice_=0.0, iters=False,
                      d_sat=1.0):
         xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
@@ -275,6 +290,8 @@ class Reference:
         L.ref_o3d_write.argtypes = [C.c_char_p, A, _ip, _dp, _dp, _dp, _ip, _dp, _dp, _dp, _dp]
         L.ref_o3d_read.argtypes = [C.c_char_p, _ip, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
         L.ref_inverted_distance.argtypes = [_ip, _dp, _dp, _dp, C.c_int, _dp]
+        L.ref_centered_gradient.argtypes = [A, _ip, _dp, _dp, C.c_double, C.c_int, C.c_int, _dp,
+                                            _dp, _dp, _dp]
         L.ref_conformal_radius.argtypes = [A, _ip, _dp, _dp, C.c_double, _ip, _dp, _dp, _dp, _dp]
         L.ref_conformal_radius.restype = C.c_double
         L.ref_blmvm.argtypes = [C.c_int, _dp, _dp, _dp, _REF_OBJECTIVE]
@@ -484,6 +501,21 @@ class Reference:
         f = np.ascontiguousarray(field, dtype=np.float64).reshape(-1)
         return self._mesh_out(self.L.ref_mesh_linear, _ptr(res, _ip), _ptr(c), _ptr(l), _ptr(f),
                               n=f.size)
+
+    def centered_gradient(self, rs, grid, max_it, kind, dist, curv=None):
+        """(score, gradient) of OPTIMIZE_3D's centered root gradients (kind 0
+        log-rational, 1 its bottom-root form, 2 computeCenteredGradient)."""
+        res, c, l, _ = self._g(grid)
+        d = np.ascontiguousarray(dist, dtype=np.float64).reshape(-1)
+        cv = None if curv is None else np.ascontiguousarray(curv, dtype=np.float64).reshape(-1)
+        n = 4 * (rs.n_top + rs.n_bottom if kind == 0 else rs.n_bottom if kind == 1 else rs.n_top)
+        grad = np.empty(n)
+        sc = np.empty(1)
+        with _quiet():
+            self.L.ref_centered_gradient(C.byref(_map_args(rs)), _ptr(res, _ip), _ptr(c), _ptr(l),
+                                         grid.slice, max_it, kind, _ptr(d), _ptr(cv), _ptr(grad),
+                                         _ptr(sc))
+        return float(sc[0]), grad
 
     def tanh_score_grad(self, rs, grid, wgrid, weights, max_it):
         res, c, l, _ = self._g(grid)

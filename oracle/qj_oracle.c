@@ -802,3 +802,134 @@ double qjo_sqerr_energy(const qjo_map* m, int64_t n, const double* xyz, const do
   return e;
 }
 
+/* ------------------------------------------------------------------ */
+/* Central-difference root gradients (qjo_centered_gradient). */
+
+/* POLYNOMIAL_4D::evaluateFactored (POLYNOMIAL_4D.cpp:1080-1088): the roots'
+ * plain product (q - r_0)(q - r_1)..., left to right. */
+static void fd_factored(const double* roots, int n, const double q[4], double out[4]) {
+  double r[4], d[4], t[4];
+  for (int c = 0; c < 4; c++) r[c] = q[c] - roots[c];
+  for (int i = 1; i < n; i++) {
+    for (int c = 0; c < 4; c++) d[c] = q[c] - roots[4 * i + c];
+    qmul(r, d, t);
+    memcpy(r, t, sizeof r);
+  }
+  memcpy(out, r, sizeof r);
+}
+
+/* computeLogRationalMap (OPTIMIZE_3D.cpp:1907-1985) at one cell: escape 20,
+ * iterate = s * (q top(q)) / (q bottom(q)); returns log|q|. */
+static double fd_lograt_value(const double* top, int nt, const double* bot, int nb, double s,
+                              const double p[3], double slice, int max_it) {
+  double q[4] = {p[0], p[1], p[2], slice}, f[4], T[4], B[4], o[4];
+  double mag = qmag(q);
+  int it = 0;
+  while (mag < 20.0 && it < max_it) {
+    fd_factored(top, nt, q, f);
+    qmul(q, f, T);
+    if (nb > 0) {
+      fd_factored(bot, nb, q, f);
+      qmul(q, f, B);
+      qdiv(T, B, o);
+    } else {
+      memcpy(o, T, sizeof o);
+    }
+    for (int c = 0; c < 4; c++) q[c] = o[c] * s;
+    mag = qmag(q);
+    it++;
+  }
+  return log(mag);
+}
+
+/* computeMap (OPTIMIZE_3D.cpp:853-980) at one cell: escape 10, iterate =
+ * top.evaluateFactored(iterate); -1 if the orbit stays, else +1. */
+static double fd_poly_value(const double* top, int nt, const double p[3], double slice,
+                            int max_it) {
+  double q[4] = {p[0], p[1], p[2], slice}, o[4];
+  double mag = qmag(q);
+  int it = 0;
+  while (mag < 10.0 && it < max_it) {
+    fd_factored(top, nt, q, o);
+    memcpy(q, o, sizeof q);
+    mag = qmag(q);
+    it++;
+  }
+  return (it == max_it || mag < 10.0) ? -1.0 : 1.0;
+}
+
+/* OPTIMIZE_3D::kahanAdd (OPTIMIZE_3D.cpp:2486-2492) */
+static void fd_kahan(double* sum, double add, double* err) {
+  const double y = add - *err;
+  const double t = *sum + y;
+  *err = (t - *sum) - y;
+  *sum = t;
+}
+
+/* computeScore / computeLogRationalScore of one root placement: the field,
+ * then computeBinaryScore (:2275-2297) and, for kind 2,
+ * computeCurvatureScore (:2497-2537). */
+static double fd_score(const qjo_map* m, const double* top, const double* bot,
+                       const qjo_grid* g, int max_it, int kind, const double* dist,
+                       const double* curv, double* fractal) {
+  const int X = g->res[0], Y = g->res[1], Z = g->res[2];
+  const int64_t N = (int64_t)X * Y * Z;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic)
+#endif
+  for (int64_t i = 0; i < N; i++) {
+    double p[3];
+    qjo_cell_center(g, (int)(i % X), (int)((i / X) % Y), (int)(i / ((int64_t)X * Y)), p);
+    fractal[i] = kind == 2 ? fd_poly_value(top, m->top.n, p, g->slice, max_it)
+                           : fd_lograt_value(top, m->top.n, bot, m->bottom.n, m->scale, p,
+                                             g->slice, max_it);
+  }
+  double score = 0.0;
+  for (int64_t i = 0; i < N; i++) {
+    double p[3];
+    qjo_cell_center(g, (int)(i % X), (int)((i / X) % Y), (int)(i / ((int64_t)X * Y)), p);
+    const double dt = (qjo_trilinear(g, dist, p) < 0) ? -1 : 1;
+    const double ft = (fractal[i] > 0) ? -1 : 1;
+    score += ft * dt;
+  }
+  const double binary = score / (double)N;
+  if (kind != 2) return binary;
+  double cs = 0.0, cs_err = 0.0, sum = 0.0, sum_err = 0.0;
+  for (int64_t i = 0; i < N; i++) {
+    const double sign = (dist[i] < 0) ? 1 : -1;
+    const double adding = sign * curv[i];
+    fd_kahan(&cs, adding * fractal[i], &cs_err);
+    fd_kahan(&sum, fabs(adding), &sum_err);
+  }
+  return (binary + cs / sum) * 0.5;
+}
+
+void qjo_centered_gradient(const qjo_map* m, const qjo_grid* g, int max_it, int kind,
+                           const double* dist, const double* curv, double* grad, double* score) {
+  const int nt = m->top.n, nb = m->bottom.n;
+  const int64_t N = (int64_t)g->res[0] * g->res[1] * g->res[2];
+  const double eps = g->lengths[0] / g->res[0];
+  double* top = (double*)malloc(sizeof(double) * 4 * (nt > 0 ? nt : 1));
+  double* bot = (double*)malloc(sizeof(double) * 4 * (nb > 0 ? nb : 1));
+  double* fractal = (double*)malloc(sizeof(double) * (size_t)N);
+  if (nt > 0) memcpy(top, m->top.roots, sizeof(double) * 4 * (size_t)nt);
+  if (nb > 0) memcpy(bot, m->bottom.roots, sizeof(double) * 4 * (size_t)nb);
+  const int k0 = kind == 1 ? nt : 0;
+  const int nk = kind == 0 ? nt + nb : kind == 1 ? nb : nt;
+  for (int k = 0; k < nk; k++) {
+    double* root = (k0 + k < nt) ? top + 4 * (k0 + k) : bot + 4 * (k0 + k - nt);
+    for (int c = 0; c < 4; c++) {
+      const double keep = root[c];
+      root[c] = keep + eps;
+      const double right = fd_score(m, top, bot, g, max_it, kind, dist, curv, fractal);
+      root[c] = keep - eps;
+      const double left = fd_score(m, top, bot, g, max_it, kind, dist, curv, fractal);
+      root[c] = keep;
+      grad[4 * k + c] = (right - left) / (2.0 * eps);
+    }
+  }
+  if (score) *score = fd_score(m, top, bot, g, max_it, kind, dist, curv, fractal);
+  free(top);
+  free(bot);
+  free(fractal);
+}

@@ -114,6 +114,18 @@ double qjo_tanh_score_grad(const qjo_map* m, const qjo_grid* g, const qjo_grid* 
                            const double* weights, int max_it, double alpha,
                            double threshold, double* grad, double* field);
 
+/* Central-difference root gradients of OPTIMIZE_3D's binary-score
+ * objectives, step eps = lengths[0] / res[0], entry 4 k + c:
+ *   kind 0: computeLogRationalCenteredGradient (OPTIMIZE_3D.cpp:2872-2951),
+ *           top then bottom roots; kind 1: computeLogRationalBottomCenteredGradient
+ *           (:2956-3008); both the binary score (:2275-2297) of
+ *           computeLogRationalMap (:1907-1985);
+ *   kind 2: computeCenteredGradient (:2761-2812), (binary + curvature score
+ *           (:2497-2537)) / 2 of computeMap (:853-980), top roots.
+ * dist / curv are fields on g.  *score (optional): the unmoved map's score. */
+void qjo_centered_gradient(const qjo_map* m, const qjo_grid* g, int max_it, int kind,
+                           const double* dist, const double* curv, double* grad, double* score);
+
 /* Squared-error energy sum_k (D tanh(d(x_k)/D) - t_k)^2 of the distance
  * estimate d, D = d_sat (d_sat <= 0: sum (d - t)^2). */
 double qjo_sqerr_energy(const qjo_map* m, int64_t n, const double* xyz, const double* target,

@@ -492,6 +492,40 @@ int ref_mesh_lagrange(const MapArgs* a, const int* res, const double* center,
   return export_mesh(mesh, verts, max_v, tris, max_t, nv, nt);
 }
 
+// OPTIMIZE_3D's central-difference root gradients, unmodified: kind 0
+// computeLogRationalCenteredGradient (OPTIMIZE_3D.cpp:2872-2951), 1
+// computeLogRationalBottomCenteredGradient (:2956-3008), 2
+// computeCenteredGradient (:2761-2812).  The distance and curvature fields
+// share the fractal's grid, as setScoreFields makes them; *score gets the
+// unmoved map's score (computeLogRationalScore / ...BottomScore / computeScore).
+void ref_centered_gradient(const MapArgs* a, const int* res, const double* center,
+                           const double* lengths, double slice, int max_it, int kind,
+                           const double* dist, const double* curv, double* grad, double* score) {
+  OPTIMIZE_3D opt(res[0], res[1], res[2], VEC3F(center[0], center[1], center[2]),
+                  VEC3F(lengths[0], lengths[1], lengths[2]));
+  opt.top() = make_poly(a->nt, a->troots, a->tpows, a->tsig);
+  opt.bottom() = make_poly(a->nb, a->broots, a->bpows, a->bsig);
+  opt.maxIterations() = max_it;
+  opt.expScaling() = a->s;
+  opt.slice() = slice;
+  FIELD_3D d(res[0], res[1], res[2], VEC3F(center[0], center[1], center[2]),
+             VEC3F(lengths[0], lengths[1], lengths[2]));
+  for (int i = 0; i < d.totalCells(); i++) d[i] = dist[i];
+  opt.distanceField() = d;
+  FIELD_3D c = d;
+  if (curv)
+    for (int i = 0; i < c.totalCells(); i++) c[i] = curv[i];
+  opt.curvatureField() = c;
+  VECTOR g = kind == 0   ? opt.computeLogRationalCenteredGradient()
+             : kind == 1 ? opt.computeLogRationalBottomCenteredGradient()
+                         : opt.computeCenteredGradient();
+  for (int i = 0; i < (int)g.size(); i++) grad[i] = (double)g[i];
+  FIELD_3D f = opt.fractal();
+  *score = (double)(kind == 0   ? opt.computeLogRationalScore(opt.top(), opt.bottom(), f)
+                    : kind == 1 ? opt.computeLogRationalBottomScore(opt.bottom(), f)
+                                : opt.computeScore(opt.top(), f));
+}
+
 // FIELD_3D::invertedDistance / invertedDistanceNormalized (FIELD_3D.cpp:5241-5352).
 void ref_inverted_distance(const int* res, const double* center, const double* lengths,
                            const double* dist, int normalized, double* out) {

@@ -156,6 +156,7 @@ class QjgMapState(C.Structure):
                 ("sigma_top", C.c_double), ("sigma_bot", C.c_double), ("scale", C.c_double)]
 
 
+QJG_FD_LOG_RATIONAL, QJG_FD_LOG_RATIONAL_BOTTOM, QJG_FD_POLYNOMIAL = 0, 1, 2
 QJG_FIT_SCALED_ONLY = 0
 QJG_FIT_SCALED = 1
 OBJECTIVE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int32, _dp, _dp, _dp)
@@ -215,6 +216,8 @@ EXPORTS = {
     "qjg_mesh_edge_cache_read": ([C.c_char_p, C.POINTER(C.c_int32), C.c_int64,
                                   C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.c_int64,
                                   C.POINTER(C.c_int64)], C.c_int),
+    "qjg_centered_gradient": ([C.c_void_p, C.c_int32, C.POINTER(QjgGrid), C.c_int32, C.c_int32,
+                               C.c_void_p, C.c_void_p, _dp, _dp, C.c_void_p], C.c_int),
     "qjg_tanh_score_grad": ([C.c_void_p, C.c_int32, C.POINTER(QjgGrid), C.c_int32,
                              C.POINTER(QjgGrid), C.c_void_p, C.c_double, C.c_double, _dp, _dp,
                              C.c_void_p, C.POINTER(QjgTanhStats), C.c_void_p], C.c_int),
@@ -687,6 +690,19 @@ class Context:
         """The last captured mesher call as the reference's edge-cache file."""
         self._check(self.L.qjg_mesh_edge_cache_write(self.h, str(path).encode()),
                     "qjg_mesh_edge_cache_write")
+
+    def centered_gradient(self, handle, grid: Grid, max_it, kind, d_dist, n_entries, d_curv=0,
+                          stream=None):
+        """OPTIMIZE_3D's central-difference root gradients (QJG_FD_*): (score
+        of the unmoved map, gradient of n_entries = 4 x the moved roots)."""
+        score = C.c_double()
+        grad = np.empty(n_entries)
+        self._check(self.L.qjg_centered_gradient(self.h, handle, C.byref(QjgGrid.of(grid)),
+                                                 int(max_it), int(kind), C.c_void_p(d_dist),
+                                                 C.c_void_p(d_curv or 0), grad.ctypes.data_as(_dp),
+                                                 C.byref(score), C.c_void_p(stream or 0)),
+                    "qjg_centered_gradient")
+        return score.value, grad
 
     def tanh_score_grad(self, handle, grid: Grid, max_it, wgrid: Grid, d_weights, n_params,
                         alpha=10.0, threshold=0.0, d_field=0, stream=None):
