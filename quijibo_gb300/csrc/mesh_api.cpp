@@ -243,6 +243,15 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
     if (ctx->m_capture && (rc = capture_slab(ctx, w.list, n_new, ctx->m_cubes[cur] + n_carry, nc,
                                              X, Y, c0, s)))
       return rc;
+    // the cube scan's block sums (one per scan block of cubes, and the
+    // total) outgrow the unit scan's when a slab has many triangle-bearing
+    // cubes per unit; emit has read the unit sums once the stream is synced
+    if ((size_t)qj::mesh_scan_blocks(nc) > ctx->m_bsum_cap) {
+      if ((rc = grow_keep(ctx, &ctx->m_bsum, &ctx->m_bsum_cap,
+                          (size_t)qj::mesh_scan_blocks(nc), 0, s)))
+        return rc;
+      w.bsum = ctx->m_bsum;
+    }
     QJ_CUDA(ctx, qj::mesh_cube_scan(w, ctx->m_cubes[cur] + n_carry, nc, nt, s));
     ctx->launches += nc > 0 ? 4 : 1;
     // per-vertex buffers grow to the vertex count extrapolated from the layers

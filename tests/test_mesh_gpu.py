@@ -109,6 +109,25 @@ def test_mesh_matches_oracle_64(ctx, oracle, wl):
     ctx.free(h)
 
 
+@pytest.mark.parametrize("res,slab_nz", [((48, 40, 37), 0), ((130, 24, 70), 16)])
+def test_dense_random_sign_field_matches_oracle(ctx, oracle, res, slab_nz):
+    """A field of random signs: about half of the cubes carry triangles, many
+    more per 64-voxel unit than a surface gives, so a slab's cube scan needs
+    more block sums than its unit scan (the buffer grows for them); the
+    linear mesh equals the oracle's."""
+    g = Grid(res)
+    f = np.random.RandomState(sum(res)).uniform(-1.0, 1.0, g.n_voxels)
+    fd = torch.from_numpy(f).cuda()
+    out = Out(g.n_voxels)
+    _, st = ctx.mesh_field(None, g, None, fd.data_ptr(), lib.QJG_EDGE_LINEAR, slab_nz=slab_nz,
+                           **out.kw())
+    v64, _, tris = out.result(st)
+    o = oracle.mesh(None, g, f, lib.QJG_EDGE_LINEAR, 1, 2.0)
+    assert len(tris) > 2 * g.n_voxels // 3
+    np.testing.assert_array_equal(tris, o["tris"])
+    np.testing.assert_allclose(v64, o["verts"], rtol=0, atol=1e-12)
+
+
 @pytest.mark.parametrize("res", [64, 160])
 def test_fp32_refine_stream_topology_matches_fp64(ctx, res):
     rs, g, p = precision_workload(res)
