@@ -282,11 +282,13 @@ def run_ours(args, world, rank, local):
                "unit": "Gvox/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 8 * n}
 
     # serving: a Poisson-arrival stream of field / field+mesh / energy+gradient
-    # requests (sizes scaled down so the stream takes about 10 s), p50/p99
+    # requests at the serving configuration's sizes (fields 32^3-512^3, meshes
+    # 128^3-1024^3, 10k-200k samples) and its offered rate (22 req/s), p50/p99
     serving = None
     if rank == 0 and not args.no_serve:
         from quijibo_gb300.benchmarks import bench_serve
-        sargs = argparse.Namespace(seed=0, requests=args.serve_requests, scale=0.25, span=10.0,
+        sargs = argparse.Namespace(seed=0, requests=args.serve_requests, scale=1.0,
+                                   span=args.serve_requests / 22.2,
                                    workers=8, budget_gb=64.0, baseline_sample=10,
                                    baseline_max_voxels=1 << 24)
         serving = bench_serve(sargs)
@@ -355,7 +357,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 plain-form comparison")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving stream")
-    ap.add_argument("--serve-requests", type=int, default=200)
+    ap.add_argument("--serve-requests", type=int, default=400)
     ap.add_argument("--no-large", action="store_true", help="skip the 2200^3 large-grid record")
     ap.add_argument("--large-res", type=int, default=2200)
     ap.add_argument("--large-slices", type=int, default=4)
