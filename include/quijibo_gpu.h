@@ -206,6 +206,26 @@ int qjg_mesh_stream(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qj
                     int64_t vert_cap, int32_t* d_tris, int64_t tri_cap, qjg_mesh_stats* stats,
                     void* stream);
 
+/* qjg_mesh_stream as a fixed launch sequence: every count stays in device
+ * memory, so no host read, host wait or allocation sits between its kernels
+ * and a caller may capture the call into a CUDA graph (same vertices and
+ * triangles as qjg_mesh_stream).  qjg_mesh_prepare sizes the context for
+ * meshes up to the grid's X, Y, the slab depth and the capacities (device
+ * allocations: call it before a capture); qjg_mesh_stream_async enqueues one
+ * mesh on `stream` and returns (vert_cap and tri_cap > 0, at most the
+ * prepared ones; d_tris also holds the unfiltered triangles);
+ * qjg_mesh_async_result reads its stats once the stream (or graph) has run.
+ * A mesh that outgrows a capacity stops writing and reads back as
+ * QJG_ERR_CAPACITY without the counts it needs (qjg_mesh_stream reports
+ * them).  No edge-cache capture or phase timing on this path. */
+int qjg_mesh_prepare(qjg_ctx* ctx, const qjg_grid* grid, int32_t slab_nz, int64_t vert_cap,
+                     int64_t tri_cap);
+int qjg_mesh_stream_async(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid,
+                          const qjg_iter* iter, double iso, int32_t slab_nz, double* d_verts64,
+                          float* d_verts32, int64_t vert_cap, int32_t* d_tris, int64_t tri_cap,
+                          void* stream);
+int qjg_mesh_async_result(qjg_ctx* ctx, qjg_mesh_stats* stats);
+
 /* Edge-cache bookkeeping of the meshers.  With capture on, qjg_mesh_stream
  * and qjg_mesh_field keep, per call, the edge of every vertex (its two grid
  * corners, in vertex order) and every cube whose corners are neither all

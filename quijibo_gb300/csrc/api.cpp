@@ -231,6 +231,8 @@ void qjg_destroy(qjg_ctx* ctx) {
   cudaFree(ctx->m_estate);
   cudaFree(ctx->m_epark);
   cudaFree(ctx->m_ecount);
+  cudaFree(ctx->m_run);
+  cudaFree(ctx->m_fstats);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   for (cudaEvent_t e : ctx->ev)
     if (e) cudaEventDestroy(e);

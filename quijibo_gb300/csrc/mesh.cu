@@ -85,9 +85,12 @@ __device__ __forceinline__ T block_exclusive_scan(T v, T* total) {
   return warp_base + inc - v;
 }
 
-// Generic pass 1: per-block sums of op.count(i) over items [0, n).
+// Generic pass 1: per-block sums of op.count(i) over items [0, n) (n read
+// from n_dev when given).
 template <class Op>
-__global__ void __launch_bounds__(SCAN_T) count_kernel(Op op, long long n, long long* bsum) {
+__global__ void __launch_bounds__(SCAN_T) count_kernel(Op op, long long n, long long* bsum,
+                                                       const long long* n_dev) {
+  if (n_dev) n = *n_dev;
   const long long base = (long long)blockIdx.x * SCAN_B + (long long)threadIdx.x * SCAN_V;
   long long c = 0;
 #pragma unroll
@@ -135,10 +138,14 @@ __global__ void __launch_bounds__(1024) scan_bsum_kernel(long long* bsum, long l
 }
 
 // Generic pass 3: op.emit(i, k) with k = running + exclusive prefix of
-// op.count over items [0, n).
+// op.count over items [0, n) (n and running read from n_dev and run_dev
+// when given).
 template <class Op>
 __global__ void __launch_bounds__(SCAN_T) emit_kernel(Op op, long long n, const long long* bsum,
-                                                      long long running) {
+                                                      long long running, const long long* n_dev,
+                                                      const long long* run_dev) {
+  if (n_dev) n = *n_dev;
+  if (run_dev) running = *run_dev;
   const long long base = (long long)blockIdx.x * SCAN_B + (long long)threadIdx.x * SCAN_V;
   int c[SCAN_V];
   long long s = 0;
@@ -642,6 +649,7 @@ struct McEmit {
   long long id0;          // global id of the slab's first vertex
   long long u_split;      // first unit of the slab's last cube layer (-1: none)
   McTotals* tot;
+  const McRun* run;       // when set: id0 = run->nv, cubes from cubes + run->n_carry
 };
 
 // the unit's sign words in x order, with the next unit's first sign as bit 64
@@ -663,6 +671,13 @@ __device__ __forceinline__ uint32_t bit_at(const McRow& r, int i) {
 
 __global__ void __launch_bounds__(SCAN_T) mc_emit_kernel(const McEmit e, long long U) {
   const McSlab& c = e.c;
+  long long id0 = e.id0;
+  McCube* cubes = e.cubes;
+  if (e.run) {
+    if (e.run->overflow) return;
+    id0 = e.run->nv;
+    cubes += e.run->n_carry;
+  }
   const long long base = (long long)blockIdx.x * SCAN_B + (long long)threadIdx.x * SCAN_V;
   uint32_t cnt[SCAN_V];
   unsigned long long w = 0;
@@ -710,7 +725,7 @@ __global__ void __launch_bounds__(SCAN_T) mc_emit_kernel(const McEmit e, long lo
       }
       const long long wv = (long long)(p + 1) * c.XY + r0 + x;
       if (m) {
-        e.vbase[wv] = (int32_t)(e.id0 + vp);
+        e.vbase[wv] = (int32_t)(id0 + vp);
         e.masks[wv] = (uint8_t)m;
 #pragma unroll
         for (int a = 0; a < 3; a++)
@@ -721,7 +736,7 @@ __global__ void __launch_bounds__(SCAN_T) mc_emit_kernel(const McEmit e, long lo
         q.r = (uint32_t)(r0 + x);
         q.gzf = (uint32_t)gz | (uint32_t)f << 24;
         q.tb = 0;
-        e.cubes[cp++] = q;
+        cubes[cp++] = q;
       }
     }
   }
@@ -732,6 +747,15 @@ struct CubeTris {
   McCube* cubes;
   __device__ int count(long long i) const { return ntri_of((int)(cubes[i].gzf >> 24)); }
   __device__ void emit(long long i, long long k) const { cubes[i].tb = k; }
+};
+// ... over the run's new entries (from cubes + run->n_carry)
+struct CubeTrisRun {
+  McCube* cubes;
+  const McRun* run;
+  __device__ int count(long long i) const {
+    return ntri_of((int)(cubes[run->n_carry + i].gzf >> 24));
+  }
+  __device__ void emit(long long i, long long k) const { cubes[run->n_carry + i].tb = k; }
 };
 
 // Pass 4: the triangles of cube entries [0, n) with n = n_carry + the
@@ -751,13 +775,20 @@ struct McTris {
   int X;
   long long XY;
   int zbase;  // global plane of window plane 0
+  const McRun* run;  // when set: n_carry and the entry count from here
 };
 
 __global__ void __launch_bounds__(128) mc_tris_kernel(const McTris t, long long n_all) {
   __shared__ uint8_t cases[256][16];
+  long long n_carry = t.n_carry;
+  if (t.run) {
+    if (t.run->overflow) return;
+    n_carry = t.run->n_carry;
+    n_all = n_carry + t.run->nc;
+  }
   for (int i = threadIdx.x; i < 256 * 16; i += blockDim.x) cases[i >> 4][i & 15] = QJ_MC_CASES[i >> 4][i & 15];
   __syncthreads();
-  const long long n = t.last ? n_all : t.n_carry + t.tot->split;
+  const long long n = t.last ? n_all : n_carry + t.tot->split;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     const McCube q = t.cubes[i];
@@ -782,7 +813,13 @@ __global__ void __launch_bounds__(128) mc_tris_kernel(const McTris t, long long 
 // The entries of the slab's last cube layer move to the front of the other
 // cube list for the next slab: [n_carry + split, n_carry + nc) -> [0, ...).
 __global__ void mc_carry_kernel(const McCube* __restrict__ src, McCube* __restrict__ dst,
-                                long long n_carry, long long nc, const McTotals* tot) {
+                                long long n_carry, long long nc, const McTotals* tot,
+                                const McRun* run) {
+  if (run) {
+    if (run->overflow) return;
+    n_carry = run->n_carry;
+    nc = run->nc;
+  }
   const long long s0 = n_carry + tot->split;
   const long long n = n_carry + nc - s0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
@@ -860,7 +897,12 @@ __global__ void __launch_bounds__(128) vertex_kernel(const __grid_constant__ Map
                                                      long long id0, int c0,
                                                      const double* __restrict__ src,
                                                      double* __restrict__ verts, double iso,
-                                                     DevStats* st) {
+                                                     DevStats* st, const McRun* run) {
+  if (run) {
+    if (run->overflow) return;
+    n = run->n_new;
+    id0 = run->nv;
+  }
   const long long XY = (long long)g.X * g.Y;
   unsigned long long evals = 0, evals32 = 0, unbracketed = 0;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
@@ -1122,7 +1164,12 @@ __global__ void __launch_bounds__(128) edge_start_kernel(const __grid_constant__
                                                          double* __restrict__ verts, double iso,
                                                          uint32_t* park,
                                                          unsigned long long* n_park,
-                                                         DevStats* st) {
+                                                         DevStats* st, const McRun* run) {
+  if (run) {
+    if (run->overflow) return;
+    n = run->n_new;
+    id0 = run->nv;
+  }
   const long long XY = (long long)g.X * g.Y;
   unsigned long long e32 = 0, nbad = 0;
   const long long stride = (long long)gridDim.x * blockDim.x;
@@ -1261,6 +1308,76 @@ __global__ void to_float_kernel(const double* __restrict__ a, float* __restrict_
     b[i] = (float)a[i];
 }
 
+// ------------------------------------------------ the run's bookkeeping
+
+__global__ void mc_run_init_kernel(McRun* r, long long cap_v, long long cap_list,
+                                   long long cap_cubes, long long cap_t) {
+  McRun z{};
+  z.cap_v = cap_v;
+  z.cap_list = cap_list;
+  z.cap_cubes = cap_cubes;
+  z.cap_t = cap_t;
+  *r = z;
+}
+
+__global__ void mc_run_slab_kernel(McRun* r, const McTotals* tot, int first) {
+  if (!r->overflow) {
+    const long long n_carry = first ? 0 : r->prev_nc - tot->split;
+    if (!first) r->nt += tot->nt;
+    const long long n_new = tot->nv, nc = tot->nc;
+    if (r->nv + n_new > r->cap_v || n_new > r->cap_list || n_carry + nc > r->cap_cubes ||
+        r->nv + n_new > 0x7FFFFFFFll) {
+      r->overflow = 1;
+    } else {
+      r->n_carry = n_carry;
+      r->n_new = n_new;
+      r->nc = nc;
+      return;
+    }
+  }
+  // nothing more is written: every later phase sees empty counts
+  r->n_carry = r->n_new = r->nc = 0;
+}
+
+__global__ void mc_run_next_kernel(McRun* r) {
+  if (r->overflow) return;
+  r->nv += r->n_new;
+  r->prev_nc = r->nc;
+}
+
+__global__ void mc_run_final_kernel(McRun* r, const McTotals* tot, int any_slab) {
+  if (!r->overflow && any_slab) r->nt += tot->nt;
+  if (r->nt > r->cap_t) r->overflow = 1;
+  r->n_filter = r->overflow ? 0 : r->nt;
+}
+
+// the run's outputs: vertices (FP64 and/or FP32) and the kept triangles
+__global__ void mc_copy_out_kernel(const double* __restrict__ verts, double* __restrict__ v64,
+                                   float* __restrict__ v32, const int32_t* __restrict__ kept,
+                                   int32_t* __restrict__ tris, const McRun* run) {
+  if (run->overflow) return;
+  const long long nv3 = 3 * run->nv, nt3 = 3 * run->keep;
+  const long long n = nv3 > nt3 ? nv3 : nt3;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    if (i < nv3) {
+      if (v64) v64[i] = verts[i];
+      if (v32) v32[i] = (float)verts[i];
+    }
+    if (i < nt3) tris[i] = kept[i];
+  }
+}
+
+__global__ void mc_stats_add_kernel(DevStats* acc, const DevStats* st) {
+  acc->voxel_iters += st->voxel_iters;
+  acc->refined += st->refined;
+  acc->nonfinite += st->nonfinite;
+  for (int k = 0; k < 4; k++) acc->aux[k] += st->aux[k];
+  acc->rerun += st->rerun;
+  acc->rerun_iters += st->rerun_iters;
+  acc->ff_evals += st->ff_evals;
+}
+
 int sm_count() {
   int dev = 0, n = 0;
   cudaGetDevice(&dev);
@@ -1327,6 +1444,7 @@ cudaError_t mesh_emit(const MeshWindow& w, const double* src, int P, int Pv, int
   e.id0 = id0;
   e.u_split = u_split;
   e.tot = w.tot;
+  e.run = nullptr;
   const long long U = mesh_units(w.X, w.Y, Pv);
   const long long nb = (U + SCAN_B - 1) / SCAN_B;
   mc_emit_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(e, U);
@@ -1338,9 +1456,9 @@ cudaError_t mesh_cube_scan(const MeshWindow& w, McCube* cubes, long long nc, lon
   if (nc <= 0) return cudaMemsetAsync(&w.tot->nt, 0, sizeof(long long), s);
   const long long nb = (nc + SCAN_B - 1) / SCAN_B;
   CubeTris op{cubes};
-  count_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(op, nc, w.bsum);
+  count_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(op, nc, w.bsum, nullptr);
   scan_bsum_kernel<<<1, 1024, 0, s>>>(w.bsum, nb);
-  emit_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(op, nc, w.bsum, t0);
+  emit_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(op, nc, w.bsum, t0, nullptr, nullptr);
   cudaError_t err = cudaGetLastError();
   if (err) return err;
   return cudaMemcpyAsync(&w.tot->nt, w.bsum + nb, sizeof(long long), cudaMemcpyDeviceToDevice, s);
@@ -1363,12 +1481,13 @@ cudaError_t mesh_triangles(const MeshWindow& w, const McCube* cubes, long long n
     t.X = w.X;
     t.XY = (long long)w.X * w.Y;
     t.zbase = zbase;
+    t.run = nullptr;
     const int blocks = (int)std::min<long long>((n_all + 127) / 128, (long long)sm_count() * 16);
     mc_tris_kernel<<<blocks, 128, 0, s>>>(t, n_all);
   }
   if (!last && nc > 0) {
     const int blocks = (int)std::min<long long>((nc + 255) / 256, (long long)sm_count() * 8);
-    mc_carry_kernel<<<blocks, 256, 0, s>>>(cubes, next, n_carry, nc, w.tot);
+    mc_carry_kernel<<<blocks, 256, 0, s>>>(cubes, next, n_carry, nc, w.tot, nullptr);
   }
   return cudaGetLastError();
 }
@@ -1381,7 +1500,7 @@ static cudaError_t parked_start(const MapParams& m, const GridParams& g, const I
   const int blocks = (int)std::min<long long>((n + 127) / 128, (long long)sm_count() * 32);
   edge_start_kernel<POW_REF><<<blocks, 128, 0, s>>>(m, g, it, w.list, n, id0, c0,
                                                     static_cast<EdgeState*>(sc.state), verts, iso,
-                                                    sc.list[0], sc.count, st);
+                                                    sc.list[0], sc.count, st, nullptr);
   return cudaGetLastError();
 }
 
@@ -1436,7 +1555,8 @@ cudaError_t mesh_vertices(const MapParams& m, const GridParams& g, const IterPar
                         : parked_start<0>(m, g, it, w, n, id0, c0, verts, iso, st, *scratch, s);
   const int blocks = (int)std::min<long long>((n + 127) / 128, (long long)sm_count() * 32);
 #define QJ_VK(B, P, H) \
-  vertex_kernel<B, P, H><<<blocks, 128, 0, s>>>(m, g, it, w.list, n, id0, c0, src, verts, iso, st)
+  vertex_kernel<B, P, H><<<blocks, 128, 0, s>>>(m, g, it, w.list, n, id0, c0, src, verts, iso, st, \
+                                                nullptr)
   if (edge_mode == 0)
     QJ_VK(false, 0, false);
   else if (pow_mode == 2)
@@ -1457,13 +1577,13 @@ cudaError_t mesh_filter(const int32_t* tris, long long n, const double* verts, i
   }
   const long long nb = (n + SCAN_B - 1) / SCAN_B;
   DegenCount dc{tris, verts};
-  count_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(dc, n, bsum);
+  count_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(dc, n, bsum, nullptr);
   scan_bsum_kernel<<<1, 1024, 0, s>>>(bsum, nb);
   DegenEmit de;
   de.tris = tris;
   de.v = verts;
   de.out = out;
-  emit_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(de, n, bsum, 0);
+  emit_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(de, n, bsum, 0, nullptr, nullptr);
   cudaError_t err;
   if ((err = cudaMemcpyAsync(n_keep, bsum + nb, sizeof(long long), cudaMemcpyDeviceToHost, s)))
     return err;
@@ -1474,6 +1594,175 @@ cudaError_t mesh_to_float(const double* a, float* b, long long n, cudaStream_t s
   if (n == 0) return cudaSuccess;
   const int blocks = (int)std::min<long long>((n + 255) / 256, (long long)sm_count() * 16);
   to_float_kernel<<<blocks, 256, 0, s>>>(a, b, n);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------- the fixed launch sequence
+
+cudaError_t mesh_run_init(McRun* run, long long cap_v, long long cap_list, long long cap_cubes,
+                          long long cap_t, cudaStream_t s) {
+  mc_run_init_kernel<<<1, 1, 0, s>>>(run, cap_v, cap_list, cap_cubes, cap_t);
+  return cudaGetLastError();
+}
+
+cudaError_t mesh_run_slab(McRun* run, const McTotals* tot, bool first, cudaStream_t s) {
+  mc_run_slab_kernel<<<1, 1, 0, s>>>(run, tot, first ? 1 : 0);
+  return cudaGetLastError();
+}
+
+cudaError_t mesh_run_next(McRun* run, cudaStream_t s) {
+  mc_run_next_kernel<<<1, 1, 0, s>>>(run);
+  return cudaGetLastError();
+}
+
+cudaError_t mesh_run_final(McRun* run, const McTotals* tot, bool any_slab, cudaStream_t s) {
+  mc_run_final_kernel<<<1, 1, 0, s>>>(run, tot, any_slab ? 1 : 0);
+  return cudaGetLastError();
+}
+
+cudaError_t mesh_emit_run(const MeshWindow& w, const double* src, int P, int Pv, int gz0,
+                          long long u_split, McCube* cubes, const McRun* run, cudaStream_t s) {
+  McEmit e;
+  e.c = slab_of(w, src, P, Pv, gz0);
+  e.bpre = w.bsum;
+  e.masks = w.masks;
+  e.vbase = w.vbase;
+  e.list = w.list;
+  e.cubes = cubes;
+  e.id0 = 0;
+  e.u_split = u_split;
+  e.tot = w.tot;
+  e.run = run;
+  const long long U = mesh_units(w.X, w.Y, Pv);
+  const long long nb = (U + SCAN_B - 1) / SCAN_B;
+  mc_emit_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(e, U);
+  return cudaGetLastError();
+}
+
+// The scan runs over as many blocks as the list could hold; blocks past the
+// run's count sum to zero.  w.bsum holds mesh_scan_blocks(cap_cubes).
+cudaError_t mesh_cube_scan_run(const MeshWindow& w, McCube* cubes, McRun* run,
+                               long long cap_cubes, cudaStream_t s) {
+  const long long nb = (std::max(cap_cubes, 1ll) + SCAN_B - 1) / SCAN_B;
+  CubeTrisRun op{cubes, run};
+  count_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(op, 0, w.bsum, &run->nc);
+  scan_bsum_kernel<<<1, 1024, 0, s>>>(w.bsum, nb);
+  emit_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(op, 0, w.bsum, 0, &run->nc, &run->nt);
+  cudaError_t err = cudaGetLastError();
+  if (err) return err;
+  return cudaMemcpyAsync(&w.tot->nt, w.bsum + nb, sizeof(long long), cudaMemcpyDeviceToDevice, s);
+}
+
+cudaError_t mesh_vertices_run(const MapParams& m, const GridParams& g, const IterParams& it,
+                              int edge_mode, int pow_mode, bool hybrid, const MeshWindow& w,
+                              int c0, const double* src, double* verts, double iso, DevStats* st,
+                              const EdgeScratch* scratch, const McRun* run, cudaStream_t s) {
+  const int blocks = sm_count() * 32;
+  if (edge_mode != 0 && hybrid && scratch) {
+#define QJ_ES(P)                                                                              \
+  edge_start_kernel<P><<<blocks, 128, 0, s>>>(m, g, it, w.list, 0, 0, c0,                    \
+                                              static_cast<EdgeState*>(scratch->state), verts, \
+                                              iso, scratch->list[0], scratch->count, st, run)
+    if (pow_mode == 2)
+      QJ_ES(2);
+    else if (pow_mode)
+      QJ_ES(1);
+    else
+      QJ_ES(0);
+#undef QJ_ES
+    return cudaGetLastError();
+  }
+#define QJ_VK(B, P, H) \
+  vertex_kernel<B, P, H><<<blocks, 128, 0, s>>>(m, g, it, w.list, 0, 0, c0, src, verts, iso, st, run)
+  if (edge_mode == 0)
+    QJ_VK(false, 0, false);
+  else if (pow_mode == 2)
+    hybrid ? QJ_VK(true, 2, true) : QJ_VK(true, 2, false);
+  else if (pow_mode)
+    hybrid ? QJ_VK(true, 1, true) : QJ_VK(true, 1, false);
+  else
+    hybrid ? QJ_VK(true, 0, true) : QJ_VK(true, 0, false);
+#undef QJ_VK
+  return cudaGetLastError();
+}
+
+template <int POW_REF>
+static cudaError_t parked_finish_fixed(const MapParams& m, const GridParams& g,
+                                       const IterParams& it, double* verts, double iso,
+                                       DevStats* st, const EdgeScratch& sc, cudaStream_t s) {
+  EdgeState* es = static_cast<EdgeState*>(sc.state);
+  const int pb = sm_count() * 32;
+  cudaError_t err;
+  // each round gives every parked edge one value; no edge needs more than 8
+  for (int round = 0, cur = 0; round < 8; round++, cur ^= 1) {
+    if ((err = cudaMemsetAsync(sc.count + 2, 0, sizeof(unsigned long long), s))) return err;
+    edge_ff_kernel<<<pb, 128, 0, s>>>(m, g, it, sc.list[cur], sc.count + cur, es, iso,
+                                      sc.list[2], sc.count + 2, st);
+    edge_fp64_kernel<POW_REF><<<pb, 128, 0, s>>>(m, g, it, sc.list[2], sc.count + 2, es, iso,
+                                                 st);
+    if ((err = cudaMemsetAsync(sc.count + (cur ^ 1), 0, sizeof(unsigned long long), s)))
+      return err;
+    edge_resume_kernel<POW_REF><<<pb, 128, 0, s>>>(m, g, it, sc.list[cur], sc.count + cur, es,
+                                                   verts, iso, sc.list[cur ^ 1],
+                                                   sc.count + (cur ^ 1), st);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t mesh_parked_finish_fixed(const MapParams& m, const GridParams& g,
+                                     const IterParams& it, int pow_mode, double* verts,
+                                     double iso, DevStats* st, const EdgeScratch& sc,
+                                     cudaStream_t s) {
+  return pow_mode == 2 ? parked_finish_fixed<2>(m, g, it, verts, iso, st, sc, s)
+         : pow_mode   ? parked_finish_fixed<1>(m, g, it, verts, iso, st, sc, s)
+                      : parked_finish_fixed<0>(m, g, it, verts, iso, st, sc, s);
+}
+
+cudaError_t mesh_triangles_run(const MeshWindow& w, const McCube* cubes, bool last, int zbase,
+                               McCube* next, int32_t* tris, long long cap, const McRun* run,
+                               cudaStream_t s) {
+  McTris t;
+  t.cubes = cubes;
+  t.n_carry = 0;
+  t.last = last ? 1 : 0;
+  t.tot = w.tot;
+  t.masks = w.masks;
+  t.vbase = w.vbase;
+  t.tris = tris;
+  t.cap = cap;
+  t.X = w.X;
+  t.XY = (long long)w.X * w.Y;
+  t.zbase = zbase;
+  t.run = run;
+  mc_tris_kernel<<<sm_count() * 16, 128, 0, s>>>(t, 0);
+  if (!last) mc_carry_kernel<<<sm_count() * 8, 256, 0, s>>>(cubes, next, 0, 0, w.tot, run);
+  return cudaGetLastError();
+}
+
+cudaError_t mesh_filter_run(const int32_t* tris, const double* verts, int32_t* out,
+                            long long* bsum, McRun* run, long long cap_t, cudaStream_t s) {
+  const long long nb = (std::max(cap_t, 1ll) + SCAN_B - 1) / SCAN_B;
+  DegenCount dc{tris, verts};
+  count_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(dc, 0, bsum, &run->n_filter);
+  scan_bsum_kernel<<<1, 1024, 0, s>>>(bsum, nb);
+  DegenEmit de;
+  de.tris = tris;
+  de.v = verts;
+  de.out = out;
+  emit_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(de, 0, bsum, 0, &run->n_filter, nullptr);
+  cudaError_t err = cudaGetLastError();
+  if (err) return err;
+  return cudaMemcpyAsync(&run->keep, bsum + nb, sizeof(long long), cudaMemcpyDeviceToDevice, s);
+}
+
+cudaError_t mesh_copy_out_run(const double* verts, double* v64, float* v32, const int32_t* kept,
+                              int32_t* tris, const McRun* run, cudaStream_t s) {
+  mc_copy_out_kernel<<<sm_count() * 8, 256, 0, s>>>(verts, v64, v32, kept, tris, run);
+  return cudaGetLastError();
+}
+
+cudaError_t mesh_stats_add(DevStats* acc, const DevStats* st, cudaStream_t s) {
+  mc_stats_add_kernel<<<1, 1, 0, s>>>(acc, st);
   return cudaGetLastError();
 }
 

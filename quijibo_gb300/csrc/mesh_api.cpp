@@ -368,6 +368,140 @@ int mesh_core(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter
   return QJG_OK;
 }
 
+// Slab depth of the streaming mesher for a grid (mesh_core's rule).
+long long slab_depth(const qjg_grid* grid, int slab_nz) {
+  const long long XY = (long long)grid->res[0] * grid->res[1];
+  int nz = slab_nz > 0 ? slab_nz : 64;
+  const long long nz_max = (long long)(UINT32_MAX / 4) / XY - 2;
+  if (nz_max < 1) return 0;
+  nz = (int)std::min<long long>(nz, nz_max);
+  return std::max(1, std::min(nz, std::max(grid->res[2] - 1, 1)));
+}
+
+// Buffer sizes of the fixed launch sequence.
+struct RunCaps {
+  long long list, cubes, bsum, field_vox;
+};
+RunCaps run_caps(long long X, long long Y, long long nz, int64_t vcap, int64_t tcap) {
+  const long long XY = X * Y;
+  RunCaps c;
+  c.list = std::max<long long>(1, std::min<long long>(vcap, 3 * XY * (nz + 1)));
+  c.cubes = std::max<long long>(1, std::min<long long>(tcap, XY * (nz + 1)));
+  const long long units = qj::mesh_units((int)X, (int)Y, (int)nz + 1);
+  c.bsum = std::max({2 * qj::mesh_scan_blocks(units), qj::mesh_scan_blocks(c.cubes),
+                     qj::mesh_scan_blocks(std::max<long long>(tcap, 1))});
+  c.field_vox = (nz + 1) * XY;
+  return c;
+}
+
+// The streaming mesher as a fixed launch sequence: every count stays on the
+// device (McRun), so nothing between the kernels reads the host or waits.
+int mesh_core_async(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qjg_iter* iter,
+                    double iso, int slab_nz, double* v64, float* v32, int64_t vcap,
+                    int32_t* tris, int64_t tcap, cudaStream_t s) {
+  int rc;
+  if ((rc = qj_check_grid(ctx, grid))) return rc;
+  const MapParams* m = qj_lookup(ctx, rs);
+  if (!m) return fail(ctx, QJG_ERR_HANDLE, "unknown root set %d", rs);
+  if ((rc = qj_check_iter(ctx, iter))) return rc;
+  std::unique_ptr<MapParams> mcopy;
+  if (iter->form == QJG_FORM_LAGRANGE) {
+    mcopy.reset(new MapParams(*m));
+    mcopy->lagrange = 1;
+    m = mcopy.get();
+  }
+  if (!tris || vcap <= 0 || tcap <= 0)
+    return fail(ctx, QJG_ERR_ARG, "the fixed sequence needs d_tris and positive capacities");
+  const int X = grid->res[0], Y = grid->res[1], Z = grid->res[2];
+  const long long XY = (long long)X * Y;
+  const long long nz = slab_depth(grid, slab_nz);
+  if (nz < 1) return fail(ctx, QJG_ERR_ARG, "a %d x %d slice is too large", X, Y);
+  if (!ctx->m_run || X > ctx->m_prep_X || Y > ctx->m_prep_Y || XY > ctx->m_prep_X * ctx->m_prep_Y ||
+      nz > ctx->m_prep_nz || vcap > ctx->m_prep_vcap || tcap > ctx->m_prep_tcap)
+    return fail(ctx, QJG_ERR_ARG, "qjg_mesh_prepare has not sized this context for the mesh");
+  const RunCaps caps = run_caps(X, Y, nz, vcap, tcap);
+  QJ_CUDA(ctx, cudaSetDevice(ctx->device));
+  QJ_CUDA(ctx, qj::mesh_run_init(ctx->m_run, vcap, caps.list, caps.cubes, tcap, s));
+  ctx->m_async_slabs = 0;
+  if (X < 2 || Y < 2) {  // no cube
+    QJ_CUDA(ctx, qj::mesh_run_final(ctx->m_run, ctx->m_tot, false, s));
+    return QJG_OK;
+  }
+  QJ_CUDA(ctx, cudaMemsetAsync(ctx->d_mstats, 0, sizeof(qj::DevStats), s));
+  QJ_CUDA(ctx, cudaMemsetAsync(ctx->m_fstats, 0, sizeof(qj::DevStats), s));
+  QJ_CUDA(ctx, cudaMemsetAsync(ctx->m_ecount, 0, 3 * sizeof(unsigned long long), s));
+  qj::MeshWindow w;
+  w.X = X;
+  w.Y = Y;
+  w.masks = ctx->m_masks;
+  w.vbase = ctx->m_vbase;
+  w.list = ctx->m_list;
+  w.bsum = ctx->m_bsum;
+  w.bits = ctx->m_bits;
+  w.sign = ctx->m_sign;
+  w.ucount = ctx->m_ucount;
+  w.tot = ctx->m_tot;
+  const GridParams g = qj_grid_params(grid, 0, Z);
+  const IterParams it = qj_iter_params(iter, grid);
+  const int pow_mode = qj_pow_mode(iter, m->all_int);
+  const bool hybrid = iter->precision != QJG_FP64;
+  const long long S = (X + 63) / 64;
+  qj::EdgeScratch esc{};
+  esc.state = ctx->m_estate;
+  esc.list[0] = ctx->m_epark;
+  esc.list[1] = ctx->m_epark + vcap;
+  esc.list[2] = ctx->m_epark + 2 * vcap;
+  esc.count = ctx->m_ecount;
+  int cur = 0, prevL = 0, slabs = 0;
+  for (int c0 = 0; c0 < Z - 1;) {
+    const int c1 = (int)std::min<long long>(c0 + nz, Z - 1);
+    const bool last = c1 == Z - 1;
+    const int L = c1 - c0;
+    if (c0 == 0) {
+      if ((rc = qjg_field(ctx, rs, grid, iter, 0, c1 + 1, ctx->m_field, nullptr, s))) return rc;
+    } else {
+      QJ_CUDA(ctx, cudaMemcpyAsync(ctx->m_field, ctx->m_field + (size_t)prevL * XY,
+                                   XY * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      if ((rc = qjg_field(ctx, rs, grid, iter, c0 + 1, c1 + 1, ctx->m_field + XY, nullptr, s)))
+        return rc;
+      QJ_CUDA(ctx, cudaMemcpyAsync(ctx->m_masks, ctx->m_masks + (size_t)prevL * XY, XY,
+                                   cudaMemcpyDeviceToDevice, s));
+      QJ_CUDA(ctx, cudaMemcpyAsync(ctx->m_vbase, ctx->m_vbase + (size_t)prevL * XY,
+                                   XY * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+    }
+    QJ_CUDA(ctx, qj::mesh_stats_add(ctx->m_fstats, ctx->d_stats, s));
+    const double* src = ctx->m_field;
+    const int P = L + 1, Pv = L + (last ? 1 : 0);
+    QJ_CUDA(ctx, qj::mesh_classify(w, src, P, Pv, c0, s));
+    QJ_CUDA(ctx, qj::mesh_run_slab(ctx->m_run, w.tot, c0 == 0, s));
+    const long long u_split = last ? -1 : (long long)(L - 1) * Y * S;
+    QJ_CUDA(ctx, qj::mesh_emit_run(w, src, P, Pv, c0, u_split, ctx->m_cubes[cur], ctx->m_run, s));
+    QJ_CUDA(ctx, qj::mesh_cube_scan_run(w, ctx->m_cubes[cur], ctx->m_run, caps.cubes, s));
+    QJ_CUDA(ctx, qj::mesh_vertices_run(*m, g, it, QJG_EDGE_BISECT, pow_mode, hybrid, w, c0, src,
+                                       ctx->m_verts, iso, ctx->d_mstats, hybrid ? &esc : nullptr,
+                                       ctx->m_run, s));
+    QJ_CUDA(ctx, qj::mesh_run_next(ctx->m_run, s));
+    QJ_CUDA(ctx, qj::mesh_triangles_run(w, ctx->m_cubes[cur], last, c0 - 1, ctx->m_cubes[cur ^ 1],
+                                        tris, tcap, ctx->m_run, s));
+    ctx->launches += 12;
+    prevL = L;
+    cur ^= 1;
+    slabs++;
+    c0 = c1;
+  }
+  QJ_CUDA(ctx, qj::mesh_run_final(ctx->m_run, w.tot, slabs > 0, s));
+  if (hybrid)
+    QJ_CUDA(ctx, qj::mesh_parked_finish_fixed(*m, g, it, pow_mode, ctx->m_verts, iso,
+                                              ctx->d_mstats, esc, s));
+  QJ_CUDA(ctx, qj::mesh_filter_run(tris, ctx->m_verts, ctx->m_tris, ctx->m_bsum, ctx->m_run, tcap, s));
+  QJ_CUDA(ctx, qj::mesh_copy_out_run(ctx->m_verts, v64, v32, ctx->m_tris, tris, ctx->m_run, s));
+  ctx->launches += hybrid ? 30 : 6;
+  ctx->m_async_slabs = slabs;
+  ctx->m_async_voxels = slabs > 0 ? (int64_t)Z * XY : 0;  // every plane computed once
+  ctx->m_async_roots = m->nt + m->nb;
+  return QJG_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -388,6 +522,103 @@ int qjg_mesh_stream(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qj
   if (!ctx) return QJG_ERR_ARG;
   return mesh_core(ctx, rs, grid, iter, true, nullptr, QJG_EDGE_BISECT, iso, slab_nz, d_verts64,
                    d_verts32, vert_cap, d_tris, tri_cap, stats, (cudaStream_t)stream);
+}
+
+int qjg_mesh_prepare(qjg_ctx* ctx, const qjg_grid* grid, int32_t slab_nz, int64_t vert_cap,
+                     int64_t tri_cap) {
+  if (!ctx) return QJG_ERR_ARG;
+  int rc;
+  if ((rc = qj_check_grid(ctx, grid))) return rc;
+  if (vert_cap <= 0 || tri_cap <= 0) return fail(ctx, QJG_ERR_ARG, "capacities must be positive");
+  const long long X = grid->res[0], Y = grid->res[1], XY = X * Y;
+  const long long nz = slab_depth(grid, slab_nz);
+  if (nz < 1) return fail(ctx, QJG_ERR_ARG, "a %lld x %lld slice is too large", X, Y);
+  const RunCaps caps = run_caps(X, Y, nz, vert_cap, tri_cap);
+  const size_t wplanes = (size_t)(nz + 2) * XY;
+  const long long units = qj::mesh_units((int)X, (int)Y, (int)nz + 1);
+  const size_t fv = (size_t)caps.field_vox;
+  QJ_CUDA(ctx, cudaSetDevice(ctx->device));
+  if ((rc = ensure(ctx, &ctx->m_masks, &ctx->m_masks_cap, wplanes)) ||
+      (rc = ensure(ctx, &ctx->m_vbase, &ctx->m_vbase_cap, wplanes)) ||
+      (rc = ensure(ctx, &ctx->m_sign, &ctx->m_sign_cap, (size_t)units * qj::MESH_UNIT_WORDS)) ||
+      (rc = ensure(ctx, &ctx->m_bits, &ctx->m_bits_cap, (size_t)units * qj::MESH_UNIT_WORDS)) ||
+      (rc = ensure(ctx, &ctx->m_ucount, &ctx->m_ucount_cap, (size_t)units)) ||
+      (rc = ensure(ctx, &ctx->m_tot, &ctx->m_tot_cap, (size_t)1)) ||
+      (rc = ensure(ctx, &ctx->m_bsum, &ctx->m_bsum_cap, (size_t)caps.bsum)) ||
+      (rc = ensure(ctx, &ctx->m_field, &ctx->m_field_cap, fv)) ||
+      (rc = ensure(ctx, &ctx->d_list, &ctx->list_cap, fv)) ||
+      (rc = ensure(ctx, &ctx->d_sorted, &ctx->sorted_cap, fv)) ||
+      (rc = ensure(ctx, &ctx->d_keys, &ctx->keys_cap, fv)) ||
+      (rc = ensure(ctx, &ctx->d_hist, &ctx->hist_cap, (size_t)qj::REFINE_KEYS)) ||
+      (rc = ensure(ctx, &ctx->d_ff, &ctx->ff_cap, fv)) ||
+      (rc = ensure(ctx, &ctx->m_ecount, &ctx->m_ecount_cap, (size_t)3)) ||
+      (rc = ensure(ctx, &ctx->m_list, &ctx->m_list_cap, (size_t)caps.list)) ||
+      (rc = ensure(ctx, &ctx->m_cubes[0], &ctx->m_cubes_cap[0], (size_t)caps.cubes)) ||
+      (rc = ensure(ctx, &ctx->m_cubes[1], &ctx->m_cubes_cap[1], (size_t)caps.cubes)) ||
+      (rc = ensure(ctx, &ctx->m_verts, &ctx->m_verts_cap, (size_t)(3 * vert_cap))) ||
+      (rc = ensure(ctx, &ctx->m_estate, &ctx->m_estate_cap,
+                   (size_t)vert_cap * qj::mesh_edge_state_bytes())) ||
+      (rc = ensure(ctx, &ctx->m_epark, &ctx->m_epark_cap, (size_t)(3 * vert_cap))) ||
+      (rc = ensure(ctx, &ctx->m_tris, &ctx->m_tris_cap, (size_t)(3 * tri_cap))))
+    return rc;
+  if (!ctx->m_run) QJ_CUDA(ctx, cudaMalloc((void**)&ctx->m_run, sizeof(qj::McRun)));
+  if (!ctx->m_fstats) QJ_CUDA(ctx, cudaMalloc((void**)&ctx->m_fstats, sizeof(qj::DevStats)));
+  ctx->m_prep_X = X;
+  ctx->m_prep_Y = Y;
+  ctx->m_prep_nz = nz;
+  ctx->m_prep_vcap = vert_cap;
+  ctx->m_prep_tcap = tri_cap;
+  return QJG_OK;
+}
+
+int qjg_mesh_stream_async(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid,
+                          const qjg_iter* iter, double iso, int32_t slab_nz, double* d_verts64,
+                          float* d_verts32, int64_t vert_cap, int32_t* d_tris, int64_t tri_cap,
+                          void* stream) {
+  if (!ctx) return QJG_ERR_ARG;
+  ctx->m_async_slabs = -1;
+  return mesh_core_async(ctx, rs, grid, iter, iso, slab_nz, d_verts64, d_verts32, vert_cap,
+                         d_tris, tri_cap, (cudaStream_t)stream);
+}
+
+int qjg_mesh_async_result(qjg_ctx* ctx, qjg_mesh_stats* stats) {
+  if (!ctx || !stats) return QJG_ERR_ARG;
+  if (ctx->m_async_slabs < 0 || !ctx->m_run)
+    return fail(ctx, QJG_ERR_ARG, "no qjg_mesh_stream_async run to read");
+  qj::McRun run;
+  qj::DevStats ds, fs;
+  QJ_CUDA(ctx, cudaSetDevice(ctx->device));
+  QJ_CUDA(ctx, cudaMemcpy(&run, ctx->m_run, sizeof run, cudaMemcpyDeviceToHost));
+  std::memset(&ds, 0, sizeof ds);
+  std::memset(&fs, 0, sizeof fs);
+  if (ctx->m_async_slabs > 0) {
+    QJ_CUDA(ctx, cudaMemcpy(&ds, ctx->d_mstats, sizeof ds, cudaMemcpyDeviceToHost));
+    QJ_CUDA(ctx, cudaMemcpy(&fs, ctx->m_fstats, sizeof fs, cudaMemcpyDeviceToHost));
+  }
+  qjg_mesh_stats st;
+  std::memset(&st, 0, sizeof st);
+  st.n_verts = run.nv;
+  st.n_tris = run.keep;
+  st.n_degenerate = run.overflow ? 0 : run.nt - run.keep;
+  st.slabs = ctx->m_async_slabs;
+  st.map_evals = (int64_t)ds.aux[1];
+  st.n_unbracketed = (int64_t)ds.aux[2];
+  st.map_evals_fp32 = (int64_t)ds.aux[3];
+  st.map_evals_ff = (int64_t)ds.ff_evals;
+  // the slab fields' counters, as qjg_field_stats_read reads them
+  st.field.voxels = ctx->m_async_voxels;
+  st.field.voxel_iters = (int64_t)fs.voxel_iters;
+  st.field.root_terms = (int64_t)fs.voxel_iters * ctx->m_async_roots;
+  st.field.refined = (int64_t)fs.refined;
+  st.field.refined_iters = (int64_t)fs.aux[0];
+  st.field.nonfinite = (int64_t)fs.nonfinite;
+  st.field.lane_iters = (int64_t)fs.aux[3];
+  st.field.rerun = (int64_t)fs.rerun;
+  st.field.rerun_iters = (int64_t)fs.rerun_iters;
+  *stats = st;
+  if (run.overflow)
+    return fail(ctx, QJG_ERR_CAPACITY, "the mesh outgrew the capacities of the fixed sequence");
+  return QJG_OK;
 }
 
 int qjg_mesh_capture(qjg_ctx* ctx, int32_t on) {

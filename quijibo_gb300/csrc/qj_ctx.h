@@ -79,6 +79,14 @@ struct qjg_ctx {
   size_t m_epark_cap = 0;
   unsigned long long* m_ecount = nullptr;
   size_t m_ecount_cap = 0;
+  // the fixed launch sequence (qjg_mesh_prepare / qjg_mesh_stream_async)
+  qj::McRun* m_run = nullptr;        // device counts of the run
+  qj::DevStats* m_fstats = nullptr;  // the slab fields' counters, summed on the device
+  long long m_prep_X = 0, m_prep_Y = 0, m_prep_nz = 0;  // what qjg_mesh_prepare sized for
+  int64_t m_prep_vcap = 0, m_prep_tcap = 0;
+  int32_t m_async_slabs = -1;  // slabs of the last enqueued run (-1: none)
+  int64_t m_async_voxels = 0;  // its field voxels
+  int m_async_roots = 0;       // its map's roots
   // edge-cache capture (qjg_mesh_capture): per vertex its edge's two corners
   // (6 ints), per mixed cube (flag, x, y, z), of the last mesher call
   bool m_capture = false;

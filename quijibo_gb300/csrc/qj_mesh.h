@@ -25,6 +25,24 @@ struct McTotals {
   long long split;   // the slab's cube entries below its last cube layer
 };
 
+// The counts of a mesh run kept on the device, for the fixed launch
+// sequence (qjg_mesh_stream_async): every launcher below that takes a run
+// reads its counts and offsets from here instead of from host arguments, so
+// no host read sits between the kernels.
+struct McRun {
+  long long nv;       // vertices of the slabs so far (first id of the slab's vertices)
+  long long nt;       // triangles of the cube entries scanned so far
+  long long n_carry;  // cube entries carried into the slab's list
+  long long prev_nc;  // the previous slab's new cube entries
+  long long n_new;    // the slab's vertices
+  long long nc;       // the slab's new cube entries
+  long long n_filter; // triangles the degenerate filter reads (0 after an overflow)
+  long long keep;     // triangles kept by the degenerate filter
+  long long cap_v, cap_list, cap_cubes, cap_t;  // capacities of the run's buffers
+  int overflow;       // a count outgrew a capacity: nothing more is written
+  int pad;
+};
+
 // Scratch of one z-slab.  Window planes j <-> global plane c0 - 1 + j: edge
 // masks and vertex ids per window plane (plane c0 - 1 carried over from the
 // previous slab); per classified plane the activity bits, sparse voxel codes
@@ -92,5 +110,41 @@ cudaError_t mesh_parked_finish(const MapParams& m, const GridParams& g, const It
 cudaError_t mesh_filter(const int32_t* tris, long long n, const double* verts, int32_t* out,
                         long long* bsum, long long* n_keep, cudaStream_t s);
 cudaError_t mesh_to_float(const double* a, float* b, long long n, cudaStream_t s);
+
+// ---- the same phases with the counts on the device (McRun) ----
+// run <- zero counts and the capacities
+cudaError_t mesh_run_init(McRun* run, long long cap_v, long long cap_list, long long cap_cubes,
+                          long long cap_t, cudaStream_t s);
+// after a slab's classification: its counts and carry from w.tot, the
+// previous slab's triangles added, capacities checked (first: c0 == 0)
+cudaError_t mesh_run_slab(McRun* run, const McTotals* tot, bool first, cudaStream_t s);
+// after a slab's vertices: vertex base and previous cube count advance
+cudaError_t mesh_run_next(McRun* run, cudaStream_t s);
+// after the last slab: its triangles added, the triangle capacity checked
+cudaError_t mesh_run_final(McRun* run, const McTotals* tot, bool any_slab, cudaStream_t s);
+cudaError_t mesh_emit_run(const MeshWindow& w, const double* src, int P, int Pv, int gz0,
+                          long long u_split, McCube* cubes, const McRun* run, cudaStream_t s);
+cudaError_t mesh_cube_scan_run(const MeshWindow& w, McCube* cubes, McRun* run,
+                               long long cap_cubes, cudaStream_t s);
+cudaError_t mesh_vertices_run(const MapParams& m, const GridParams& g, const IterParams& it,
+                              int edge_mode, int pow_mode, bool hybrid, const MeshWindow& w,
+                              int c0, const double* src, double* verts, double iso, DevStats* st,
+                              const EdgeScratch* scratch, const McRun* run, cudaStream_t s);
+// the parked edges in a fixed number of rounds (8, the most any edge needs)
+cudaError_t mesh_parked_finish_fixed(const MapParams& m, const GridParams& g,
+                                     const IterParams& it, int pow_mode, double* verts,
+                                     double iso, DevStats* st, const EdgeScratch& sc,
+                                     cudaStream_t s);
+cudaError_t mesh_triangles_run(const MeshWindow& w, const McCube* cubes, bool last, int zbase,
+                               McCube* next, int32_t* tris, long long cap, const McRun* run,
+                               cudaStream_t s);
+// degenerate filter of run->nt triangles (at most cap_t) into out; run->keep
+cudaError_t mesh_filter_run(const int32_t* tris, const double* verts, int32_t* out,
+                            long long* bsum, McRun* run, long long cap_t, cudaStream_t s);
+// the run's vertices (FP64 and/or FP32) and kept triangles to the caller's buffers
+cudaError_t mesh_copy_out_run(const double* verts, double* v64, float* v32, const int32_t* kept,
+                              int32_t* tris, const McRun* run, cudaStream_t s);
+// acc += the field call's counters (every field counter but the tile position)
+cudaError_t mesh_stats_add(DevStats* acc, const DevStats* st, cudaStream_t s);
 
 }  // namespace qj

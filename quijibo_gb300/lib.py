@@ -207,6 +207,12 @@ EXPORTS = {
     "qjg_mesh_stream": ([C.c_void_p, C.c_int32, C.POINTER(QjgGrid), C.POINTER(QjgIter), C.c_double,
                          C.c_int32, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
                          C.POINTER(QjgMeshStats), C.c_void_p], C.c_int),
+    "qjg_mesh_prepare": ([C.c_void_p, C.POINTER(QjgGrid), C.c_int32, C.c_int64, C.c_int64],
+                         C.c_int),
+    "qjg_mesh_stream_async": ([C.c_void_p, C.c_int32, C.POINTER(QjgGrid), C.POINTER(QjgIter),
+                               C.c_double, C.c_int32, C.c_void_p, C.c_void_p, C.c_int64,
+                               C.c_void_p, C.c_int64, C.c_void_p], C.c_int),
+    "qjg_mesh_async_result": ([C.c_void_p, C.POINTER(QjgMeshStats)], C.c_int),
     "qjg_set_energy_pairs": ([C.c_int], C.c_int),
     "qjg_energy_backward_batch": ([C.c_void_p, C.c_int32, C.POINTER(QjgEnergyItem), C.c_void_p],
                                   C.c_int),
@@ -659,6 +665,30 @@ class Context:
                                     int(tri_cap), C.byref(st), C.c_void_p(stream or 0))
         if check:
             self._check(rc, "qjg_mesh_stream")
+        return rc, st.as_dict()
+
+    def mesh_prepare(self, grid: Grid, vert_cap, tri_cap, slab_nz=0):
+        """Size the context for qjg_mesh_stream_async (device allocations)."""
+        self._check(self.L.qjg_mesh_prepare(self.h, C.byref(QjgGrid.of(grid)), int(slab_nz),
+                                            int(vert_cap), int(tri_cap)), "qjg_mesh_prepare")
+
+    def mesh_stream_async(self, handle, grid: Grid, it, iso=0.0, slab_nz=0, d_verts64=0,
+                          d_verts32=0, vert_cap=0, d_tris=0, tri_cap=0, stream=None):
+        """Enqueue the streaming mesher as a fixed launch sequence (no host
+        wait inside; capturable); read the stats with mesh_async_result."""
+        self._check(self.L.qjg_mesh_stream_async(self.h, handle, C.byref(QjgGrid.of(grid)),
+                                                 C.byref(it), float(iso), int(slab_nz),
+                                                 C.c_void_p(d_verts64), C.c_void_p(d_verts32),
+                                                 int(vert_cap), C.c_void_p(d_tris), int(tri_cap),
+                                                 C.c_void_p(stream or 0)),
+                    "qjg_mesh_stream_async")
+
+    def mesh_async_result(self, check=True):
+        """(rc, stats dict) of the last mesh_stream_async run (after its stream ran)."""
+        st = QjgMeshStats()
+        rc = self.L.qjg_mesh_async_result(self.h, C.byref(st))
+        if check:
+            self._check(rc, "qjg_mesh_async_result")
         return rc, st.as_dict()
 
     def energy_batch(self, items, stream=None):
