@@ -223,7 +223,21 @@ void run_job(qjg_ctx* ctx, cudaStream_t s, Job& j) {
         cudaMallocAsync((void**)&tris, tcap * 3 * sizeof(int32_t), s) != cudaSuccess)
       rc = QJG_ERR_NOMEM;
     qjg_mesh_stats ms = {};
-    if (rc == QJG_OK)
+    // meshes up to 2^24 voxels run as the fixed launch sequence (one wait at
+    // the end instead of host reads between slabs; the context's buffers are
+    // sized to the request's capacities, so larger meshes keep the path whose
+    // buffers grow with the actual counts); a mesh that outgrows its
+    // capacities is re-run on that path for the counts it needs
+    const int64_t vox = (int64_t)r.grid.res[0] * r.grid.res[1] * r.grid.res[2];
+    const bool fixed = vox <= (int64_t)1 << 24;
+    if (rc == QJG_OK && fixed) {
+      rc = qjg_mesh_prepare(ctx, &r.grid, 0, vcap, tcap);
+      if (rc == QJG_OK)
+        rc = qjg_mesh_stream_async(ctx, h, &r.grid, &it, r.iso, 0, v64, nullptr, vcap, tris, tcap, s);
+      if (rc == QJG_OK) rc = cudaStreamSynchronize(s) == cudaSuccess ? QJG_OK : QJG_ERR_CUDA;
+      if (rc == QJG_OK) rc = qjg_mesh_async_result(ctx, &ms);
+    }
+    if ((rc == QJG_OK && !fixed) || rc == QJG_ERR_CAPACITY)
       rc = qjg_mesh_stream(ctx, h, &r.grid, &it, r.iso, 0, v64, nullptr, vcap, tris, tcap, &ms, s);
     out.n_verts = ms.n_verts;
     out.n_tris = ms.n_tris;
