@@ -32,7 +32,11 @@ extern "C" int qjg_crmath_eval(int fn, const double* d_x, double* d_y, int64_t n
   if (fn < QJG_CRM_EXP || fn > QJG_CRM_ACOS || n < 0 || (n > 0 && (!d_x || !d_y)))
     return QJG_ERR_ARG;
   if (n == 0) return QJG_OK;
-  const long long blocks = (n + 255) / 256 < 152 * 8 ? (n + 255) / 256 : 152 * 8;
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long most = 8ll * sms;  // grid-stride beyond eight blocks per SM
+  const long long blocks = (n + 255) / 256 < most ? (n + 255) / 256 : most;
   crmath_kernel<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(fn, d_x, d_y, (long long)n);
   return cudaGetLastError() == cudaSuccess ? QJG_OK : QJG_ERR_CUDA;
 }
