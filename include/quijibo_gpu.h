@@ -217,7 +217,11 @@ int qjg_mesh_stream(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, const qj
  * qjg_mesh_async_result reads its stats once the stream (or graph) has run.
  * A mesh that outgrows a capacity stops writing and reads back as
  * QJG_ERR_CAPACITY without the counts it needs (qjg_mesh_stream reports
- * them).  No edge-cache capture or phase timing on this path. */
+ * them).  No edge-cache capture or phase timing on this path.  A captured
+ * graph holds the context's buffers: a later call on the context that grows
+ * them (qjg_mesh_prepare with larger sizes, qjg_mesh_stream or qjg_field on
+ * more voxels) leaves the graph pointing at freed memory, so capture again
+ * after such a call. */
 int qjg_mesh_prepare(qjg_ctx* ctx, const qjg_grid* grid, int32_t slab_nz, int64_t vert_cap,
                      int64_t tri_cap);
 int qjg_mesh_stream_async(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid,

@@ -138,7 +138,64 @@ def bench_classify(args):
     return out
 
 
-def bench_lagrange(args):
+def bench_mesh_fixed(args):
+    """The streaming mesher three ways on the precision workload at small
+    grids (a mesh request's sizes): qjg_mesh_stream (host reads between
+    slabs), qjg_mesh_stream_async (the fixed launch sequence, one wait) and
+    that sequence replayed from a captured CUDA graph; wall-clock ms per mesh
+    (median of --reps), same mesh each way."""
+    import torch
+
+    from . import lib
+    from .rootsets import precision_workload
+    ctx = lib.Context(0)
+    out = {"workload": "precision workload map, FP32 + double-float + FP64 band, rel_tol 1e-6"}
+    for res in (64, 128, 256):
+        rs, g, p = precision_workload(res)
+        h = ctx.upload(rs)
+        it = ctx.iter_params(p["max_it"], p["escape"], precision=lib.QJG_FP32_REFINE,
+                             refine_pow=lib.QJG_REFINE_INT, rel_tol=1e-6)
+        vcap, tcap = 12 * res * res + 4096, 24 * res * res + 4096
+        v64 = torch.empty(3 * vcap, dtype=torch.float64, device="cuda")
+        tris = torch.empty(3 * tcap, dtype=torch.int32, device="cuda")
+        kw = dict(d_verts64=v64.data_ptr(), vert_cap=vcap, d_tris=tris.data_ptr(), tri_cap=tcap)
+        s = torch.cuda.Stream()
+        ctx.mesh_prepare(g, vcap, tcap)
+
+        def timed(fn):
+            fn()
+            torch.cuda.synchronize()
+            ts = []
+            for _ in range(args.reps):
+                t0 = time.perf_counter()
+                fn()
+                torch.cuda.synchronize()
+                ts.append(1e3 * (time.perf_counter() - t0))
+            return float(np.median(ts))
+
+        def host():
+            ctx.mesh_stream(h, g, it, stream=s.cuda_stream, **kw)
+
+        def fixed():
+            ctx.mesh_stream_async(h, g, it, stream=s.cuda_stream, **kw)
+            s.synchronize()
+
+        r = {"host_ms": timed(host)}
+        _, st_h = ctx.mesh_stream(h, g, it, stream=s.cuda_stream, **kw)
+        r["fixed_ms"] = timed(fixed)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=s, capture_error_mode="thread_local"):
+            ctx.mesh_stream_async(h, g, it, stream=s.cuda_stream, **kw)
+        r["graph_ms"] = timed(graph.replay)
+        _, st = ctx.mesh_async_result()
+        r.update(triangles=st["n_tris"], same_counts=st["n_tris"] == st_h["n_tris"] and
+                 st["n_verts"] == st_h["n_verts"], slabs=st["slabs"])
+        out["%d^3" % res] = r
+        ctx.free(h)
+    return out
+
+
+def bench_lagrange(args):def bench_lagrange(args):
     """The Lagrange order of the map (RATIONAL_4D::evaluateLagrange, the
     lagrangeBunny3D driver's) on the precision workload's map (16 top / 8
     bottom roots, 40 iterations, escape 2) at res^3: the plain FP64 form
@@ -736,7 +793,7 @@ def bench_tanh(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("what", choices=["mesh", "energy", "serve", "large", "tooth", "tanh",
-                                     "classify", "lagrange"])
+                                     "classify", "lagrange", "mesh_fixed"])
     ap.add_argument("--res", type=int, default=0, help="grid edge (mesh: 512, large: 2200)")
     ap.add_argument("--workload", default="precision", choices=["precision", "large"])
     ap.add_argument("--slab", type=int, default=64)
@@ -767,7 +824,8 @@ def main():
     args.hbm_gbs = args.hbm_gbs or hbm_peak_gbs()[0]
     fn = {"mesh": bench_mesh, "energy": bench_energy, "serve": bench_serve,
           "large": bench_large, "tooth": bench_tooth, "tanh": bench_tanh,
-          "classify": bench_classify, "lagrange": bench_lagrange}[args.what]
+          "classify": bench_classify, "lagrange": bench_lagrange,
+          "mesh_fixed": bench_mesh_fixed}[args.what]
     print(json.dumps(fn(args)), flush=True)
 
 
