@@ -195,7 +195,7 @@ def bench_mesh_fixed(args):
     return out
 
 
-def bench_lagrange(args):def bench_lagrange(args):
+def bench_lagrange(args):
     """The Lagrange order of the map (RATIONAL_4D::evaluateLagrange, the
     lagrangeBunny3D driver's) on the precision workload's map (16 top / 8
     bottom roots, 40 iterations, escape 2) at res^3: the plain FP64 form
