@@ -1,18 +1,22 @@
 """Generate the drop-in fixtures: the reference's own bunnyMarchingCubes3D
-driver, unmodified (projects/bunnyMarchingCubes3D/bunnyMarchingCubes3D.cpp,
-built by `make -C oracle driver` in the Real=double flavour), run on a small
-configuration.  The driver reads an optimizer state (.o3d), moves the roots
-and the field centre by the root translation, meshes the map with the
-streaming marching-cubes constructor (which writes its edge cache) and writes
-the OBJ.  tests/test_dropin_gpu.py runs the same driver linked against the
-GPU library through the adapter and compares both files with these.
+and lagrangeBunny3D drivers, unmodified
+(projects/bunnyMarchingCubes3D/bunnyMarchingCubes3D.cpp,
+projects/lagrangeBunny3D/lagrangeBunny3D.cpp, built by `make -C oracle
+driver` in the Real=double flavour), run on a small configuration.  Each
+driver reads an optimizer state (.o3d), moves the roots and the field centre
+by the root translation, meshes the map with the streaming marching-cubes
+constructor (bunny: the quotient map, writing its edge cache; lagrange: the
+Lagrange order) and writes the OBJ.  tests/test_dropin_gpu.py runs the same
+drivers linked against the GPU library through the adapter and compares
+their files with these.
 
     QUIJIBO_REF=<QUIJIBO checkout> make -C oracle ref driver
     python tests/golden/gen_dropin.py
 
 Outputs (committed): dropin_state.o3d (written by the reference's
 OPTIMIZE_3D::write), dropin.cfg, dropin_ref.npz (the OBJ's vertices and faces
-and the cache file's bytes).
+and the cache file's bytes), dropin_lagrange.cfg, dropin_lagrange_ref.npz
+(the Lagrange driver's OBJ).
 """
 import os
 import shutil
@@ -30,6 +34,7 @@ from quijibo_gb300.rootsets import Grid, precision_workload  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
 DRIVER = os.path.join(ROOT, "oracle", "_ref", "bunnyMarchingCubes3D_ref")
+LAGRANGE_DRIVER = os.path.join(ROOT, "oracle", "_ref", "lagrangeBunny3D_ref")
 RES, MAX_IT = 40, 20
 CFG = """root translation = (0.0,0.0,0.05)
 optimization file = dropin_state.o3d
@@ -40,6 +45,9 @@ output prefix = ./dropin
 # the driver's output names (bunnyMarchingCubes3D.cpp:75-78, 456-466)
 OBJ = "dropin.res.%d.iterations.%d_translationz.obj" % (RES, MAX_IT)
 CACHE = "dropin.res.%d.iterations.%d.cache" % (RES, MAX_IT)
+# lagrangeBunny3D.cpp:124-129 reads the same keys; its OBJ name: :101-104
+LAGRANGE_CFG = CFG.replace("./dropin", "./dropin_lagrange")
+LAGRANGE_OBJ = "dropin_lagrange.res.%d.iterations.%d_translationz.obj" % (RES, MAX_IT)
 
 
 def read_obj(path):
@@ -86,6 +94,17 @@ def main():
     np.savez_compressed(os.path.join(OUT, "dropin_ref.npz"), verts=verts, faces=faces, cache=cache,
                         res=RES, max_it=MAX_IT, lengths=3.0)
     print("dropin: %d vertices, %d faces, cache %d bytes" % (len(verts), len(faces), len(cache)))
+    with open(os.path.join(OUT, "dropin_lagrange.cfg"), "w") as f:
+        f.write(LAGRANGE_CFG)
+    with tempfile.TemporaryDirectory() as d:
+        shutil.copy(o3d, d)
+        shutil.copy(os.path.join(OUT, "dropin_lagrange.cfg"), d)
+        subprocess.run([LAGRANGE_DRIVER, "dropin_lagrange.cfg"], cwd=d, check=True,
+                       stdout=subprocess.DEVNULL)
+        verts, faces = read_obj(os.path.join(d, LAGRANGE_OBJ))
+    np.savez_compressed(os.path.join(OUT, "dropin_lagrange_ref.npz"), verts=verts, faces=faces,
+                        res=RES, max_it=MAX_IT, lengths=3.0)
+    print("dropin lagrange: %d vertices, %d faces" % (len(verts), len(faces)))
 
 
 if __name__ == "__main__":

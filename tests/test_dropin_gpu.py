@@ -5,7 +5,10 @@ bindings, run on the committed configuration, against the unmodified
 driver's own outputs (tests/golden/gen_dropin.py): the OBJ has the
 reference's faces, its vertices within half a voxel (the field and the
 bisection run in FP64 where the reference uses glibc's transcendentals), and
-the edge-cache file has the reference's bytes.
+the edge-cache file has the reference's bytes.  The same for the
+lagrangeBunny3D driver (projects/lagrangeBunny3D/lagrangeBunny3D.cpp, the
+Lagrange-order streaming mesher), in the plain FP64 form and the precision
+form (QJG_PRECISION=fp32refine).
 
 The edge cache is also checked through the C ABI alone (qjg_mesh_capture,
 qjg_mesh_edge_cache_write) on the driver's inputs, which needs no reference
@@ -134,3 +137,29 @@ def test_wrapped_driver_matches_reference_driver(tmp_path):
     assert r.returncode == 0 and "does not match" not in r.stdout
     verts2, faces2 = read_obj(tmp_path / ("dropin.res.%d.iterations.%d_translationz.obj" % (res, it)))
     assert np.array_equal(faces2, faces) and np.array_equal(verts2, verts)
+
+
+@pytest.mark.skipif(_reference_tree() is None,
+                    reason="reference sources absent (QUIJIBO_REF unset, no oracle/_ref/src_stage)")
+@pytest.mark.parametrize("precision", ["", "fp32refine"])
+def test_wrapped_lagrange_driver_matches_reference_driver(tmp_path, precision):
+    from quijibo_gb300 import build
+    build.build()
+    adir = os.path.join(ROOT, "quijibo_gb300", "adapter")
+    subprocess.run(["make", "-s", "-j16", "-C", adir, "lagrange", "FLAVOUR=double",
+                    "REF=" + _reference_tree()], check=True, timeout=900)
+    exe = os.path.join(adir, "_build_double", "lagrangeBunny3D_gpu")
+    for name in ("dropin_state.o3d", "dropin_lagrange.cfg"):
+        shutil.copy(os.path.join(GOLDEN, name), tmp_path)
+    d = dict(np.load(os.path.join(GOLDEN, "dropin_lagrange_ref.npz")))
+    res, it = int(d["res"]), int(d["max_it"])
+    env = dict(os.environ)
+    env.pop("QJG_PRECISION", None)
+    if precision:
+        env["QJG_PRECISION"] = precision
+    r = subprocess.run([exe, "dropin_lagrange.cfg"], cwd=tmp_path, env=env, capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    verts, faces = read_obj(tmp_path / ("dropin_lagrange.res.%d.iterations.%d_translationz.obj"
+                                        % (res, it)))
+    check_mesh(verts, faces, d)
