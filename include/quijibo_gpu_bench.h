@@ -37,6 +37,12 @@ int qjg_set_field32_pairs(int on);
  * default) one sample per lane.  Set it while no energy call is in flight. */
 int qjg_set_energy_pairs(int on);
 
+/* Process-wide form of the FP32 energy's polar power: 1 (the default) the
+ * fast form (hardware approximations of log2 and of sin/cos, a polynomial
+ * atan: about 1e-6 relative per power), 0 the accurate device library
+ * functions.  Set it while no energy call is in flight. */
+int qjg_set_energy_fast(int on);
+
 /* Work of the last qjg_energy_forward/backward call on ctx: the map
  * applications of its forward pass (orbit steps of every sample) and the
  * orbit steps its adjoint ran back over (gradient samples only; 0 for a

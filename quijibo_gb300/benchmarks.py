@@ -262,6 +262,9 @@ def bench_energy(args):
     if args.energy_pairs:
         lib.set_energy_pairs(True)
         out["forward_kernel"] = "two samples per lane"
+    lib.set_energy_fast(not args.energy_accurate)
+    out["polar_power"] = ("accurate device functions" if args.energy_accurate else
+                          "fast: hardware log2 and sin/cos, polynomial atan")
     for name, prec, grad in forms[:2] if args.fp32_only else forms:
         kw = dict(precision=prec, d_grad=G.data_ptr() if grad else 0)
         ctx.energy(P.data_ptr(), rs.n_top, rs.n_bottom, n, X.data_ptr(), T.data_ptr(), p["max_it"],
@@ -815,6 +818,8 @@ def main():
     ap.add_argument("--no-mesh", action="store_true")
     ap.add_argument("--field-pass", action="store_true", help="large: also time the field alone")
     ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--energy-accurate", action="store_true",
+                    help="energy: the FP32 polar power with the accurate device functions")
     ap.add_argument("--energy-pairs", action="store_true",
                     help="energy: the forward kernel with two samples per lane")
     ap.add_argument("--z0", type=int, default=-1, help="classify: first plane of the slab")

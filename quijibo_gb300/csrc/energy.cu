@@ -762,6 +762,39 @@ struct PowParts {
   T rho, vm, theta, A, c, s;
 };
 
+// The FP32 polar power's fast form (the default; qjg_set_energy_fast(0)
+// selects the accurate device functions): the angle from a polynomial atan
+// and the hardware approximations of log2 and of sin/cos.  On the
+// differentiation workload (200k samples, 64/16 roots, 30 iterations) it
+// moves the FP32 energy from 3e-9 to 8e-8 of the FP64 form's and the FP32
+// gradient from 2e-7 to 9e-7, for a 21% faster forward kernel.
+__constant__ int c_sq_fast = 1;
+
+// atan(t) for 0 <= t <= 1 as t P(t^2), P of degree 7 fitted for this
+// library (weighted least squares on Chebyshev nodes of t^2 in [0, 1]; max
+// relative error 2.3e-7 evaluated in FP32)
+__device__ __forceinline__ float atan01_fast(float t) {
+  const float u = t * t;
+  float p = -0.004780514165759087f;
+  p = fmaf(p, u, 0.024557340890169144f);
+  p = fmaf(p, u, -0.0599050298333168f);
+  p = fmaf(p, u, 0.09942781925201416f);
+  p = fmaf(p, u, -0.14029428362846375f);
+  p = fmaf(p, u, 0.19971376657485962f);
+  p = fmaf(p, u, -0.3333209455013275f);
+  p = fmaf(p, u, 0.9999999403953552f);
+  return p * t;
+}
+
+// atan2(y, x) for y >= 0, in [0, pi]
+__device__ __forceinline__ float atan2_pos_fast(float y, float x) {
+  const float ax = fabsf(x);
+  const float mx = fmaxf(ax, y), mn = fminf(ax, y);
+  float a = mx > 0.f ? atan01_fast(__fdividef(mn, mx)) : 0.f;
+  if (y > ax) a = 1.57079632679489662f - a;
+  return x < 0.f ? 3.14159265358979324f - a : a;
+}
+
 template <class T>
 __device__ __forceinline__ V4<T> powv(const V4<T>& d, T e, PowParts<T>* pp) {
   if constexpr (std::is_same<T, float>::value) {
@@ -772,10 +805,16 @@ __device__ __forceinline__ V4<T> powv(const V4<T>& d, T e, PowParts<T>* pp) {
     const float r2 = v2 + d.w * d.w;
     const float rv = v2 > 0.f ? rsqrtf(v2) : 0.f;
     const float vm = v2 * rv;
-    const float theta = atan2f(vm, d.w);
-    const float A = exp2f(0.5f * e * log2f(r2));
-    float s, c;
-    sincospif(e * theta * 0.318309886183790672f, &s, &c);
+    float theta, A, s, c;
+    if (c_sq_fast) {
+      theta = atan2_pos_fast(vm, d.w);
+      A = exp2f(0.5f * e * __log2f(r2));
+      __sincosf(e * theta, &s, &c);
+    } else {
+      theta = atan2f(vm, d.w);
+      A = exp2f(0.5f * e * log2f(r2));
+      sincospif(e * theta * 0.318309886183790672f, &s, &c);
+    }
     const float k = A * s * rv;
     if (pp) *pp = PowParts<T>{sqrtf(r2), vm, theta, A, c, s};
     return V4<T>{A * c, k * d.x, k * d.y, k * d.z};
@@ -1969,6 +2008,11 @@ cudaError_t launch_sq_energy_batch(const SqBatchReq* r, int K, void* scratch, do
 int sq_max_iterations() { return SQ_MAXIT; }
 
 void set_energy_pairs(int on) { g_sq_pairs.store(on ? 1 : 0); }
+
+cudaError_t set_energy_fast(int on) {
+  const int v = on ? 1 : 0;
+  return cudaMemcpyToSymbol(c_sq_fast, &v, sizeof v);
+}
 
 size_t sq_scratch_bytes(bool fp64, bool grad, long long n, int max_it, int nt, int nb) {
   return sq_layout(fp64, grad, n, max_it, nt, nb, sm_count()).bytes;

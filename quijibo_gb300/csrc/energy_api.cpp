@@ -78,6 +78,10 @@ int qjg_set_energy_pairs(int on) {
   return QJG_OK;
 }
 
+int qjg_set_energy_fast(int on) {
+  return qj::set_energy_fast(on) == cudaSuccess ? QJG_OK : QJG_ERR_CUDA;
+}
+
 int qjg_energy_last_work(qjg_ctx* ctx, int64_t* applications, int64_t* steps) {
   if (!ctx || !applications || !steps) return QJG_ERR_ARG;
   *applications = ctx->sq_applications;

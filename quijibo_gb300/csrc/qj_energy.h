@@ -27,6 +27,8 @@ size_t sq_scratch_bytes(bool fp64, bool grad, long long n, int max_it, int nt, i
 // out of the gradient]; *launches: kernels launched.
 // process-wide choice of the energy forward kernel: 1 two samples per lane
 void set_energy_pairs(int on);
+// the FP32 polar power's fast form (hardware log2 and sin/cos, polynomial atan)
+cudaError_t set_energy_fast(int on);
 // *work: two counters in the scratch, the map applications of the forward
 // pass and the orbit steps of the adjoint (read after the call completes)
 cudaError_t launch_sq_energy(bool fp64, bool grad, const double* params, int nt, int nb,

@@ -214,6 +214,7 @@ EXPORTS = {
                                C.c_void_p, C.c_int64, C.c_void_p], C.c_int),
     "qjg_mesh_async_result": ([C.c_void_p, C.POINTER(QjgMeshStats)], C.c_int),
     "qjg_set_energy_pairs": ([C.c_int], C.c_int),
+    "qjg_set_energy_fast": ([C.c_int], C.c_int),
     "qjg_energy_backward_batch": ([C.c_void_p, C.c_int32, C.POINTER(QjgEnergyItem), C.c_void_p],
                                   C.c_int),
     "qjg_energy_last_work": ([C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)], C.c_int),
@@ -453,6 +454,13 @@ def mesh_edge_cache_read(path):
 def set_energy_pairs(on):
     """Energy forward kernel: two samples per lane (True) or one (False)."""
     load().qjg_set_energy_pairs(int(bool(on)))
+
+
+def set_energy_fast(on):
+    """FP32 energy's polar power: fast hardware approximations (True, the
+    default) or the accurate device functions (False)."""
+    if load().qjg_set_energy_fast(int(bool(on))) != 0:
+        raise QjgError("qjg_set_energy_fast failed")
 
 
 def set_field32_pairs(on):
