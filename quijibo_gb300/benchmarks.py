@@ -288,6 +288,20 @@ def bench_energy(args):
             out[name]["frac_fma_probe"] = fl / dt / 1e12 / peak
     out["fma_probe_tflops"] = peak
     out["gradients_per_s"] = 1.0 / out["adjoint_fp32"]["s"]
+    # the FP32 adjoint with one lane per sample walking the roots, for comparison
+    lib.set_energy_adjoint_roots(False)
+    try:
+        kw = dict(precision=lib.QJG_FP32, d_grad=G.data_ptr())
+        args_e = (P.data_ptr(), rs.n_top, rs.n_bottom, n, X.data_ptr(), T.data_ptr(), p["max_it"],
+                  p["escape"])
+        ctx.energy(*args_e, **kw)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(3):
+            ctx.energy(*args_e, **kw)
+        out["adjoint_fp32_one_lane"] = {"s": (time.perf_counter() - t0) / 3}
+    finally:
+        lib.set_energy_adjoint_roots(True)
     if args.steps <= 0:
         return out
     Pfit = P.clone()

@@ -194,7 +194,31 @@ int qjg_create(int device, qjg_ctx** out) {
   if (cudaMalloc((void**)&ctx->d_mstats, sizeof(DevStats)) != cudaSuccess) return QJG_ERR_NOMEM;
   if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
     return QJG_ERR_CUDA;
+  cudaMemPoolProps props = {};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.handleTypes = cudaMemHandleTypeNone;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = device;
+  if (cudaMemPoolCreate(&ctx->pool, &props) != cudaSuccess) {
+    cudaStreamDestroy(ctx->stream);
+    return QJG_ERR_CUDA;
+  }
+  // Keep freed scratch for the next calls: returning it at every
+  // synchronization cost 0.4 ms per energy + gradient call (200k samples,
+  // 30 iterations: 2.21 ms against 1.81 ms).
+  if (qj_pool_keep(ctx.get(), true) != cudaSuccess) {
+    cudaMemPoolDestroy(ctx->pool);
+    cudaStreamDestroy(ctx->stream);
+    return QJG_ERR_CUDA;
+  }
   *out = ctx.release();
+  return QJG_OK;
+}
+
+int qjg_trim(qjg_ctx* ctx) {
+  if (!ctx) return QJG_ERR_ARG;
+  QJ_CUDA(ctx, cudaSetDevice(ctx->device));
+  QJ_CUDA(ctx, cudaMemPoolTrimTo(ctx->pool, 0));
   return QJG_OK;
 }
 
@@ -234,6 +258,7 @@ void qjg_destroy(qjg_ctx* ctx) {
   cudaFree(ctx->m_run);
   cudaFree(ctx->m_fstats);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
   for (cudaEvent_t e : ctx->ev)
     if (e) cudaEventDestroy(e);
   for (cudaEvent_t e : ctx->mev)

@@ -16,13 +16,14 @@ namespace {
 
 // Scratch freed on every exit path.
 struct Scratch {
+  qjg_ctx* ctx;
   cudaStream_t s;
   std::vector<void*> ptrs;
-  explicit Scratch(cudaStream_t st) : s(st) {}
+  Scratch(qjg_ctx* c, cudaStream_t st) : ctx(c), s(st) {}
   template <class T>
   T* get(size_t n) {
     void* p = nullptr;
-    if (cudaMallocAsync(&p, (n ? n : 1) * sizeof(T), s) != cudaSuccess) return nullptr;
+    if (qj_malloc_async(ctx, &p, (n ? n : 1) * sizeof(T), s) != cudaSuccess) return nullptr;
     ptrs.push_back(p);
     return static_cast<T*>(p);
   }
@@ -95,7 +96,7 @@ int qjg_inverted_distance(qjg_ctx* ctx, const int32_t res[3], const double* d_di
     return fail(ctx, QJG_ERR_ARG, "bad resolution or NULL buffer");
   QJ_CUDA(ctx, cudaSetDevice(ctx->device));
   cudaStream_t s = (cudaStream_t)stream;
-  Scratch sc(s);
+  Scratch sc(ctx, s);
   return inverted_distance(ctx, res, d_dist, normalized != 0, d_out, s, sc);
 }
 
@@ -111,7 +112,7 @@ int qjg_conformal_radius(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid,
     return fail(ctx, QJG_ERR_ARG, "NULL distance field or output");
   QJ_CUDA(ctx, cudaSetDevice(ctx->device));
   cudaStream_t s = (cudaStream_t)stream;
-  Scratch sc(s);
+  Scratch sc(ctx, s);
   const long long n = (long long)grid->res[0] * grid->res[1] * grid->res[2];
   const long long nd = (long long)dist_grid->res[0] * dist_grid->res[1] * dist_grid->res[2];
 

@@ -716,8 +716,9 @@ cudaError_t launch_tanh_grad(const MapParams& m, const GridParams& g, const Weig
 // Parameters: root positions (4 each), effective exponents, log s, laid out
 // [top roots 4nt | bottom roots 4nb | top exps nt | bottom exps nb | log s].
 // The forward pass keeps q at every SQ_CK-th iteration of the samples whose
-// gradient is wanted; the backward pass stores no trajectory: it recomputes
-// each segment forward from its checkpoint before reversing it.
+// gradient is wanted (every iteration: SQ_CK = 1); the backward pass
+// recomputes each segment forward from its first kept point before
+// reversing it (nothing to recompute at SQ_CK = 1).
 // ===========================================================================
 namespace {
 
@@ -726,7 +727,13 @@ constexpr int SQ_BWD_PER_SM = 8;  // backward blocks per SM
 constexpr int SQF_T = 128;  // threads per block of the forward pass
 constexpr int SQC_T = 256;  // threads per chunk block
 constexpr int SQ_CH = 2048; // samples per chunk (sums and sort)
-constexpr int SQ_CK = 8;    // checkpoint spacing (iterations)
+// Spacing of the kept orbit points (iterations).  1: the adjoint evaluates
+// every Jacobian at the forward pass's own orbit.  A wider spacing saves
+// memory, but its recomputed segments must reproduce the forward's rounding
+// bit for bit: with the roots of a step spread over lanes (products in
+// another order) a recomputed orbit drifts from the forward's and the FP32
+// gradient lost a factor of 10-40 in accuracy at spacing 8.
+constexpr int SQ_CK = 1;
 constexpr int SQ_MAXIT = 256;
 
 template <class T>
@@ -1352,7 +1359,8 @@ __global__ void __launch_bounds__(SQ_T) sq_bwd_kernel(
       for (int n = n0; n < n1; n++) {
         seg[n - n0] = q;
         T lg;
-        q = sq_apply<T>(rp, ep, nt, nb, s, q, &lg, nullptr, nullptr, nullptr, nullptr);
+        if (n + 1 < n1)
+          q = sq_apply<T>(rp, ep, nt, nb, s, q, &lg, nullptr, nullptr, nullptr, nullptr);
       }
       for (int n = n1max - 1; n >= n0; n--) {
         const bool on = n < n1;  // this lane's orbit has step n
@@ -1442,30 +1450,318 @@ __global__ void __launch_bounds__(SQ_T) sq_bwd_kernel(
   }
 }
 
-// Compensated sum of partials[b][k] over rows b, one warp per slot k: each
-// lane a Neumaier sum over rows lane, lane + 32, ..., then the 32 (sum,
-// compensation) pairs in a fixed tree, so the result is the same on every run.
-__global__ void __launch_bounds__(256) sq_reduce_kernel(const double* __restrict__ partials,
-                                                        int rows, int slots,
-                                                        double* __restrict__ out) {
-  const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (k >= slots) return;
-  double sum = 0, c = 0;
-  for (int b = lane; b < rows; b += 32) {
-    const double v = partials[(long long)b * slots + k];
-    const double t = sum + v;
-    c += (fabs(sum) >= fabs(v)) ? (sum - t) + v : (v - t) + sum;
-    sum = t;
+// ---- the backward pass with the roots spread over lanes ----
+//
+// sq_bwd_kernel gives each lane a sample and walks the 80 roots of a step in
+// series; the gradient samples are few (the others saturate or escape at
+// once), so a few hundred warps run long serial chains and most of the GPU
+// idles.  Here a group of G lanes takes one sample and lane l of the group
+// owns a contiguous run of at most CT top and CB bottom roots.  A map
+// application is a per-lane product of the run's polar powers and a scan of
+// those products over the group's lanes in lane order (quaternion products
+// do not commute).  The adjoint of root i needs the product of the side's
+// factors before it and the conjugate of the product after it:
+//   Pbar_i = conj(F_{i-1}) Ubar conj(S_{i+1}),
+// F from the group's exclusive prefix times the lane's own factors, S from
+// the exclusive suffix.  Each lane sums its own roots' five components over
+// the sample's steps in registers and adds them to its group's double
+// accumulators in shared memory when the sample ends; the group sums only
+// qbar and the log-gradient vector per step (butterflies, so that every lane
+// of the group holds the same bits).  The groups of a warp run their steps
+// together down from the warp's longest orbit (the samples are sorted by
+// orbit length, so a warp's groups seldom differ); a group whose orbit has
+// no step n computes alongside and adds nothing.  Each step starts from the
+// forward pass's own q_n: a recomputed orbit, its products taken in this
+// order, would drift from the forward's in FP32.
+template <class T, int G>
+__device__ __forceinline__ V4<T> shfl4_up(const V4<T>& v, int o) {
+  return V4<T>{__shfl_up_sync(0xffffffffu, v.w, o, G), __shfl_up_sync(0xffffffffu, v.x, o, G),
+               __shfl_up_sync(0xffffffffu, v.y, o, G), __shfl_up_sync(0xffffffffu, v.z, o, G)};
+}
+template <class T, int G>
+__device__ __forceinline__ V4<T> shfl4_down(const V4<T>& v, int o) {
+  return V4<T>{__shfl_down_sync(0xffffffffu, v.w, o, G), __shfl_down_sync(0xffffffffu, v.x, o, G),
+               __shfl_down_sync(0xffffffffu, v.y, o, G), __shfl_down_sync(0xffffffffu, v.z, o, G)};
+}
+template <class T, int G>
+__device__ __forceinline__ V4<T> shfl4_idx(const V4<T>& v, int src) {
+  return V4<T>{__shfl_sync(0xffffffffu, v.w, src, G), __shfl_sync(0xffffffffu, v.x, src, G),
+               __shfl_sync(0xffffffffu, v.y, src, G), __shfl_sync(0xffffffffu, v.z, src, G)};
+}
+template <class T, int G>
+__device__ __forceinline__ V4<T> group_sum4(V4<T> v) {
+#pragma unroll
+  for (int o = G / 2; o; o >>= 1)
+    v = v4add(v, V4<T>{__shfl_xor_sync(0xffffffffu, v.w, o, G),
+                       __shfl_xor_sync(0xffffffffu, v.x, o, G),
+                       __shfl_xor_sync(0xffffffffu, v.y, o, G),
+                       __shfl_xor_sync(0xffffffffu, v.z, o, G)});
+  return v;
+}
+
+// A lane's run of one side's roots (first root a, cnt <= C of them; cnt 0
+// for lanes past the side), its factors at the current q, the products of
+// the factors of the group's lower lanes (E) and higher lanes (X), the
+// side's full product, and the run's gradient sums over the current sample
+// (four position components and the exponent per root).
+template <class T, int C>
+struct SideRun {
+  int a, cnt;
+  V4<T> P[C];
+  V4<T> E, X, tot;
+  T acc[C][5];
+};
+
+template <class T, int G, int C>
+__device__ __forceinline__ void side_init(SideRun<T, C>& r, int lo, int ns, int gl) {
+  const int c = (ns + G - 1) / G;
+  r.a = lo + gl * c;
+  r.cnt = max(0, min(c, ns - gl * c));
+#pragma unroll
+  for (int j = 0; j < C; j++)
+#pragma unroll
+    for (int m = 0; m < 5; m++) r.acc[j][m] = T(0);
+}
+
+// The side's factors at q, the scans over the group's lanes; the side's
+// log-gradient terms added to gp.
+template <class T, int G, int C>
+__device__ __forceinline__ void side_fwd(const T* __restrict__ rp, const T* __restrict__ ep,
+                                         T sgn, int gl, const V4<T>& q, SideRun<T, C>& r,
+                                         V4<T>& gp) {
+  const V4<T> one{T(1), T(0), T(0), T(0)};
+  V4<T> Cp = one;
+#pragma unroll
+  for (int j = 0; j < C; j++) {
+    if (j < r.cnt) {
+      const int i = r.a + j;
+      const V4<T> d{q.w - rp[4 * i], q.x - rp[4 * i + 1], q.y - rp[4 * i + 2],
+                    q.z - rp[4 * i + 3]};
+      const V4<T> P = powv<T>(d, ep[i], nullptr);
+      r.P[j] = P;
+      Cp = j ? v4mul(Cp, P) : P;
+      gp = v4add(gp, v4scale(d, sgn * ep[i] / v4dot(d, d)));
+    }
   }
+  // inclusive prefix over the group's lanes: x_l = C_0 C_1 ... C_l
+  V4<T> x = Cp;
+#pragma unroll
+  for (int o = 1; o < G; o <<= 1) {
+    const V4<T> y = shfl4_up<T, G>(x, o);
+    if (gl >= o) x = v4mul(y, x);
+  }
+  r.tot = shfl4_idx<T, G>(x, G - 1);
+  const V4<T> e = shfl4_up<T, G>(x, 1);
+  r.E = gl ? e : one;
+  // inclusive suffix: z_l = C_l C_{l+1} ... C_{G-1}
+  V4<T> z = Cp;
+#pragma unroll
+  for (int o = 1; o < G; o <<= 1) {
+    const V4<T> y = shfl4_down<T, G>(z, o);
+    if (gl + o < G) z = v4mul(z, y);
+  }
+  const V4<T> xx = shfl4_down<T, G>(z, 1);
+  r.X = gl < G - 1 ? xx : one;
+}
+
+// The side's adjoint at qn given Ubar (the adjoint of its full product) and
+// gbar (of the log-gradient vector): each root's terms added to the run's
+// sums when `on`, and to qbp (this lane's share of qbar).
+template <class T, int C>
+__device__ __forceinline__ void side_adj(const T* __restrict__ rp, const T* __restrict__ ep,
+                                         T sgn, const V4<T>& qn, SideRun<T, C>& r,
+                                         const V4<T>& Ub, const V4<T>& gb, bool on, V4<T>& qbp) {
+  // Fa[j] = F_{a+j-1}: the side's factors before root a + j
+  V4<T> Fa[C];
+  Fa[0] = r.E;
+#pragma unroll
+  for (int j = 1; j < C; j++)
+    if (j < r.cnt) Fa[j] = v4mul(Fa[j - 1], r.P[j - 1]);
+  // V = Ubar conj(S_{a+j+1}), walked down from the run's end
+  V4<T> V = v4mul(Ub, v4conj(r.X));
+#pragma unroll
+  for (int j = C - 1; j >= 0; j--) {
+    if (j < r.cnt) {
+      const int i = r.a + j;
+      const V4<T> d{qn.w - rp[4 * i], qn.x - rp[4 * i + 1], qn.y - rp[4 * i + 2],
+                    qn.z - rp[4 * i + 3]};
+      PowParts<T> pp;
+      powv<T>(d, ep[i], &pp);
+      const V4<T> Pb = v4mul(v4conj(Fa[j]), V);
+      V = v4mul(V, v4conj(r.P[j]));
+      T eb = T(0);
+      V4<T> dbar = powv_vjp<T>(d, ep[i], pp, Pb, &eb);
+      // g term: sgn e d/|d|^2
+      const T d2 = v4dot(d, d);
+      const T dg = v4dot(d, gb);
+      dbar = v4add(dbar, v4scale(v4add(v4scale(gb, T(1) / d2),
+                                       v4scale(d, T(-2) * dg / (d2 * d2))),
+                                 sgn * ep[i]));
+      eb += sgn * dg / d2;
+      if (on) {
+        r.acc[j][0] -= dbar.w;
+        r.acc[j][1] -= dbar.x;
+        r.acc[j][2] -= dbar.y;
+        r.acc[j][3] -= dbar.z;
+        r.acc[j][4] += eb;
+      }
+      qbp = v4add(qbp, dbar);
+    }
+  }
+}
+
+// The run's sums of the finished sample into the group's accumulators.
+template <class T, int C>
+__device__ __forceinline__ void side_flush(SideRun<T, C>& r, double* acc, int nr) {
+#pragma unroll
+  for (int j = 0; j < C; j++) {
+    if (j < r.cnt) {
+      const int i = r.a + j;
+#pragma unroll
+      for (int m = 0; m < 4; m++) acc[1 + 4 * i + m] += (double)r.acc[j][m];
+      acc[1 + 4 * nr + i] += (double)r.acc[j][4];
+    }
+#pragma unroll
+    for (int m = 0; m < 5; m++) r.acc[j][m] = T(0);
+  }
+}
+
+static_assert(SQ_CK == 1, "sq_bwd_roots_kernel reads the forward pass's q at every step");
+
+template <class T, int G, int CT, int CB, int MINB>
+__global__ void __launch_bounds__(SQ_T, MINB) sq_bwd_roots_kernel(
+    const double* __restrict__ params, int nt, int nb, long long n_samples,
+    const unsigned* __restrict__ perm, const int* __restrict__ total,
+    const int* __restrict__ keys, const V4<T>* __restrict__ seed_q,
+    const T* __restrict__ seed_L, const V4<T>* __restrict__ ck, double* __restrict__ partials,
+    int slots) {
+  constexpr int NG = SQ_T / G;  // groups per block
+  extern __shared__ unsigned char sh_raw[];
+  const int nr = nt + nb;
+  T* rp = reinterpret_cast<T*>(sh_raw);  // 4 nr
+  T* ep = rp + 4 * nr;                   // nr
+  double* acc_sh = reinterpret_cast<double*>(sh_raw + ((sizeof(T) * 5 * nr + 15) / 16) * 16);
+  for (int k = threadIdx.x; k < 4 * nr; k += SQ_T) rp[k] = (T)params[k];
+  for (int k = threadIdx.x; k < nr; k += SQ_T) ep[k] = (T)params[4 * nr + k];
+  for (int k = threadIdx.x; k < NG * slots; k += SQ_T) acc_sh[k] = 0.0;
+  __syncthreads();
+  const T s = (T)exp(params[5 * nr]);
+  const int lane = threadIdx.x & 31, gl = lane & (G - 1);
+  // this group's sums: acc[1 + 4 i + c] root positions, acc[1 + 4 nr + i]
+  // exponents, acc[1 + 5 nr] log s
+  double* acc = acc_sh + (threadIdx.x / G) * slots;
+  SideRun<T, CT> top;
+  SideRun<T, CB> bot;
+  side_init<T, G, CT>(top, 0, nt, gl);
+  side_init<T, G, CB>(bot, nt, nb, gl);
+  const V4<T> zero{T(0), T(0), T(0), T(0)};
+  const int count = *total;
+  const long long stride = (long long)gridDim.x * NG;
+  // the warp's first group in the sorted list; its groups take consecutive entries
+  for (long long base = ((long long)blockIdx.x * SQ_T + (threadIdx.x & ~31)) / G; base < count;
+       base += stride) {
+    const long long j = base + lane / G;
+    const bool in = j < count;
+    const long long k = in ? (long long)perm[j] : 0;
+    const int N = in ? keys[k] : 0;
+    V4<T> qb = in ? seed_q[k] : zero;
+    const T Lb = in ? seed_L[k] : T(0);
+    const int Nmax = __reduce_max_sync(0xffffffffu, N);
+    T dls = T(0);
+    for (int n = Nmax - 1; n >= 0; n--) {
+      const bool on = n < N;  // this group's orbit has step n
+      // the forward pass's own q_n (SQ_CK = 1)
+      const V4<T> qn = on ? ck[(long long)n * n_samples + k] : zero;
+      V4<T> gp = zero;
+      side_fwd<T, G, CT>(rp, ep, T(1), gl, qn, top, gp);
+      side_fwd<T, G, CB>(rp, ep, T(-1), gl, qn, bot, gp);
+      const V4<T> g = group_sum4<T, G>(gp);
+      V4<T> Q, Tb, Bb;
+      if (nb > 0) {
+        const V4<T> W4 = v4scale(v4conj(bot.tot), T(1) / v4dot(bot.tot, bot.tot));
+        Q = v4scale(v4mul(top.tot, W4), s);
+        // L_{n+1} = L_n + log|g| + log|Q|
+        const V4<T> Qb = v4add(qb, v4scale(Q, Lb / v4dot(Q, Q)));
+        if (on) dls += v4dot(Qb, Q);
+        Tb = v4scale(v4mul(Qb, v4conj(W4)), s);
+        const V4<T> Wb = v4scale(v4mul(v4conj(top.tot), Qb), s);
+        Bb = v4scale(v4mul(v4mul(v4conj(W4), Wb), v4conj(W4)), T(-1));
+      } else {
+        Q = v4scale(top.tot, s);
+        const V4<T> Qb = v4add(qb, v4scale(Q, Lb / v4dot(Q, Q)));
+        if (on) dls += v4dot(Qb, Q);
+        Tb = v4scale(Qb, s);
+        Bb = zero;
+      }
+      const V4<T> gb = v4scale(g, Lb / v4dot(g, g));
+      V4<T> qbp = zero;
+      side_adj<T, CT>(rp, ep, T(1), qn, top, Tb, gb, on, qbp);
+      side_adj<T, CB>(rp, ep, T(-1), qn, bot, Bb, gb, on, qbp);
+      qbp = group_sum4<T, G>(qbp);
+      if (on) qb = qbp;
+    }
+    if (in) {
+      side_flush<T, CT>(top, acc, nr);
+      side_flush<T, CB>(bot, acc, nr);
+      if (gl == 0) acc[1 + 5 * nr] += (double)dls;
+    }
+  }
+  __syncthreads();
+  // groups in order (the energy and the left-out count are in the chunk rows)
+  for (int k = threadIdx.x; k < slots; k += SQ_T) {
+    double v = 0;
+    for (int w = 0; w < NG; w++) v += acc_sh[w * slots + k];
+    partials[(long long)blockIdx.x * slots + k] = v;
+  }
+}
+
+// Compensated sum of partials[b][k] over rows b, one block of SQR_W warps
+// per slot k: each thread a Neumaier sum over rows t, t + 32 SQR_W, ...,
+// each warp's 32 (sum, compensation) pairs in a fixed tree, then the warps'
+// pairs in order, so the result is the same on every run.  The sums are
+// FP64-bound, so they are spread over many warps (one warp per slot in
+// 256-thread blocks: 30 us for 1 000 rows x 403 slots).
+constexpr int SQR_W = 4;
+
+__device__ __forceinline__ void neumaier_add(double& sum, double& c, double v) {
+  const double t = sum + v;
+  c += (fabs(sum) >= fabs(v)) ? (sum - t) + v : (v - t) + sum;
+  sum = t;
+}
+
+__device__ __forceinline__ void reduce_slot(const double* __restrict__ partials, int rows,
+                                            int slots, int k, double* __restrict__ out) {
+  __shared__ double ws[SQR_W], wc[SQR_W];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  double sum = 0, c = 0;
+  for (int b = threadIdx.x; b < rows; b += 32 * SQR_W)
+    neumaier_add(sum, c, partials[(long long)b * slots + k]);
 #pragma unroll
   for (int o = 16; o; o >>= 1) {
     const double s2 = __shfl_down_sync(0xffffffffu, sum, o);
     const double c2 = __shfl_down_sync(0xffffffffu, c, o);
-    const double t = sum + s2;
-    c += c2 + ((fabs(sum) >= fabs(s2)) ? (sum - t) + s2 : (s2 - t) + sum);
-    sum = t;
+    c += c2;
+    neumaier_add(sum, c, s2);
   }
-  if (lane == 0) out[k] = sum + c;
+  if (lane == 0) {
+    ws[w] = sum;
+    wc[w] = c;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s0 = ws[0], c0 = wc[0];
+    for (int i = 1; i < SQR_W; i++) {
+      c0 += wc[i];
+      neumaier_add(s0, c0, ws[i]);
+    }
+    out[k] = s0 + c0;
+  }
+}
+
+__global__ void __launch_bounds__(32 * SQR_W) sq_reduce_kernel(const double* __restrict__ partials,
+                                                               int rows, int slots,
+                                                               double* __restrict__ out) {
+  reduce_slot(partials, rows, slots, blockIdx.x, out);
 }
 
 // ---- batches of energy + gradient requests (FP32), one pass for all.
@@ -1626,7 +1922,8 @@ __global__ void __launch_bounds__(SQ_T) sq_bwd_batch_kernel(
         for (int n = n0; n < n1; n++) {
           seg[n - n0] = q;
           T lg;
-          q = sq_apply<T>(rp, ep, nt, nb, s, q, &lg, nullptr, nullptr, nullptr, nullptr);
+          if (n + 1 < n1)
+            q = sq_apply<T>(rp, ep, nt, nb, s, q, &lg, nullptr, nullptr, nullptr, nullptr);
         }
         for (int n = n1max - 1; n >= n0; n--) {
           const bool on = n < n1;
@@ -1711,33 +2008,17 @@ __global__ void __launch_bounds__(SQ_T) sq_bwd_batch_kernel(
 
 // The final sums of one item: its chunk rows and as many group rows as its
 // sort produced (read on the device), as sq_reduce_kernel.
-__global__ void __launch_bounds__(256) sq_reduce_item_kernel(const double* __restrict__ partials,
-                                                             int chunk_rows,
-                                                             const int* __restrict__ total,
-                                                             int slots, double* __restrict__ out) {
-  const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (k >= slots) return;
-  const int rows = chunk_rows + (*total + 31) / 32;
-  double sum = 0, c = 0;
-  for (int b = lane; b < rows; b += 32) {
-    const double v = partials[(long long)b * slots + k];
-    const double t = sum + v;
-    c += (fabs(sum) >= fabs(v)) ? (sum - t) + v : (v - t) + sum;
-    sum = t;
-  }
-#pragma unroll
-  for (int o = 16; o; o >>= 1) {
-    const double s2 = __shfl_down_sync(0xffffffffu, sum, o);
-    const double c2 = __shfl_down_sync(0xffffffffu, c, o);
-    const double t = sum + s2;
-    c += c2 + ((fabs(sum) >= fabs(s2)) ? (sum - t) + s2 : (s2 - t) + sum);
-    sum = t;
-  }
-  if (lane == 0) out[k] = sum + c;
+__global__ void __launch_bounds__(32 * SQR_W) sq_reduce_item_kernel(
+    const double* __restrict__ partials, int chunk_rows, const int* __restrict__ total, int slots,
+    double* __restrict__ out) {
+  reduce_slot(partials, chunk_rows + (*total + 31) / 32, slots, blockIdx.x, out);
 }
 
 // Forward kernel choice (qjg_set_energy_pairs): two samples per lane or one.
 std::atomic<int> g_sq_pairs{0};
+// FP32 adjoint choice (qjg_set_energy_adjoint_roots): the roots of a step
+// spread over a group of lanes (sq_bwd_roots_kernel) or walked by one lane.
+std::atomic<int> g_sq_bwd_roots{1};
 
 // Byte layout of the energy scratch (each piece 256-byte aligned).
 struct SqLayout {
@@ -1784,6 +2065,24 @@ int sm_count() {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   return sms;
+}
+
+// The root-group adjoint on as many blocks as stay resident (at most the
+// layout's L.nbwd rows of partials): a second wave of blocks would start its
+// long orbits only as blocks of the first wave end.
+template <int G, int CT, int CB, int MINB>
+cudaError_t launch_bwd_roots(size_t sh_r, const SqLayout& L, int sms, const double* params, int nt,
+                             int nb, long long n, const unsigned* perm, const int* total,
+                             const SqFwdOut<float>& o, double* rows, int* blocks, cudaStream_t s) {
+  const size_t sh = sh_r + sizeof(double) * (SQ_T / G) * L.slots;
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &per_sm, sq_bwd_roots_kernel<float, G, CT, CB, MINB>, SQ_T, sh);
+  if (e != cudaSuccess) return e;
+  *blocks = std::max(1, std::min(L.nbwd, std::max(per_sm, 1) * sms));
+  sq_bwd_roots_kernel<float, G, CT, CB, MINB><<<*blocks, SQ_T, sh, s>>>(
+      params, nt, nb, n, perm, total, o.keys, o.seed_q, o.seed_L, o.ck, rows, L.slots);
+  return cudaGetLastError();
 }
 
 template <class T>
@@ -1843,20 +2142,40 @@ cudaError_t sq_launch(bool grad, const double* params, int nt, int nb, const dou
   sq_chunk_kernel<<<L.nchunks, SQC_T, 0, s>>>(o.contrib, grad ? o.keys : nullptr, o.iters, n,
                                               max_it, L.nchunks, hist, partials, L.slots, 0, work);
   *launches = 3;
+  int bwd_blocks = L.nbwd;  // rows of backward partials written
   if (grad) {
     unsigned* perm = reinterpret_cast<unsigned*>(scr + L.perm);
     sq_scan_kernel<<<1, 1024, 0, s>>>(hist, (long long)(max_it + 1) * L.nchunks, total);
     sq_scatter_kernel<<<L.nchunks, 32, 0, s>>>(o.keys, n, max_it, L.nchunks, hist, perm);
-    const size_t sh = ((sizeof(T) * 5 * nr + 15) / 16) * 16 + sizeof(double) * (SQ_T / 32) * L.slots;
-    sq_bwd_kernel<T><<<L.nbwd, SQ_T, sh, s>>>(params, nt, nb, n, perm, total, o.keys, o.seed_q,
-                                              o.seed_L, o.ck,
-                                              partials + (size_t)L.nchunks * L.slots, L.slots);
+    const size_t sh_r = ((sizeof(T) * 5 * nr + 15) / 16) * 16;
+    double* bwd_rows = partials + (size_t)L.nchunks * L.slots;
+    bool done = false;
+    if constexpr (std::is_same<T, float>::value) {
+      // groups of 16 lanes while each side has at most 64 roots (4 per
+      // lane); maps with more roots on a side keep one lane per sample,
+      // which measured faster there than whole-warp groups (90/10 and 100/28
+      // roots, 200k samples: 0.89 vs 0.99 ms, 1.17 vs 1.22 ms)
+      const int ct = (nt + 15) / 16, cb = (nb + 15) / 16;
+      if (g_sq_bwd_roots.load(std::memory_order_relaxed) && ct <= 4 && cb <= 4) {
+        if (cb <= 1)  // at most 16 bottom roots: one per lane, 8 blocks per SM
+          e = launch_bwd_roots<16, 4, 1, 8>(sh_r, L, sms, params, nt, nb, n, perm, total, o,
+                                            bwd_rows, &bwd_blocks, s);
+        else
+          e = launch_bwd_roots<16, 4, 4, 1>(sh_r, L, sms, params, nt, nb, n, perm, total, o,
+                                            bwd_rows, &bwd_blocks, s);
+        if (e != cudaSuccess) return e;
+        done = true;
+      }
+    }
+    if (!done)
+      sq_bwd_kernel<T><<<L.nbwd, SQ_T, sh_r + sizeof(double) * (SQ_T / 32) * L.slots, s>>>(
+          params, nt, nb, n, perm, total, o.keys, o.seed_q, o.seed_L, o.ck, bwd_rows, L.slots);
     *launches += 3;
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  sq_reduce_kernel<<<(L.slots * 32 + 255) / 256, 256, 0, s>>>(partials, L.nbwd + L.nchunks, L.slots,
-                                                              reinterpret_cast<double*>(scr + L.out));
+  sq_reduce_kernel<<<L.slots, 32 * SQR_W, 0, s>>>(partials, bwd_blocks + L.nchunks, L.slots,
+                                                  reinterpret_cast<double*>(scr + L.out));
   return cudaGetLastError();
 }
 
@@ -1996,7 +2315,7 @@ cudaError_t launch_sq_energy_batch(const SqBatchReq* r, int K, void* scratch, do
                                                               o.seed_L, o.ck, L.max_slots);
   n_launch++;
   for (int i = 0; i < K; i++) {
-    sq_reduce_item_kernel<<<(L.slots[(size_t)i] * 32 + 255) / 256, 256, 0, s>>>(
+    sq_reduce_item_kernel<<<L.slots[(size_t)i], 32 * SQR_W, 0, s>>>(
         items[(size_t)i].partials, (int)L.nchunks[(size_t)i], items[(size_t)i].total,
         L.slots[(size_t)i], outs[i]);
     n_launch++;
@@ -2008,6 +2327,8 @@ cudaError_t launch_sq_energy_batch(const SqBatchReq* r, int K, void* scratch, do
 int sq_max_iterations() { return SQ_MAXIT; }
 
 void set_energy_pairs(int on) { g_sq_pairs.store(on ? 1 : 0); }
+
+void set_energy_adjoint_roots(int on) { g_sq_bwd_roots.store(on ? 1 : 0); }
 
 cudaError_t set_energy_fast(int on) {
   const int v = on ? 1 : 0;

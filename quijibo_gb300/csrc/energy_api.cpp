@@ -52,7 +52,7 @@ int qjg_energy_backward_batch(qjg_ctx* ctx, int32_t n_items, qjg_energy_item* it
   cudaStream_t s = (cudaStream_t)stream;
   QJ_CUDA(ctx, cudaSetDevice(ctx->device));
   void* d_scr = nullptr;
-  QJ_CUDA(ctx, cudaMallocAsync(&d_scr, qj::sq_batch_scratch_bytes(req.data(), n_items), s));
+  QJ_CUDA(ctx, qj_malloc_async(ctx, &d_scr, qj::sq_batch_scratch_bytes(req.data(), n_items), s));
   std::vector<double*> outs((size_t)n_items);
   std::vector<double> energies((size_t)n_items);
   int launched = 0;
@@ -75,6 +75,11 @@ int qjg_energy_backward_batch(qjg_ctx* ctx, int32_t n_items, qjg_energy_item* it
 
 int qjg_set_energy_pairs(int on) {
   qj::set_energy_pairs(on);
+  return QJG_OK;
+}
+
+int qjg_set_energy_adjoint_roots(int on) {
+  qj::set_energy_adjoint_roots(on);
   return QJG_OK;
 }
 
@@ -107,7 +112,7 @@ int qjg_tanh_score_grad(qjg_ctx* ctx, qjg_rootset rs, const qjg_grid* grid, int3
   const int nblocks = qj::tanh_blocks();
   const int slots = qj::tanh_slots(m->nt, m->nb);
   double* d_part = nullptr;
-  QJ_CUDA(ctx, cudaMallocAsync((void**)&d_part, sizeof(double) * ((size_t)nblocks + 1) * slots, s));
+  QJ_CUDA(ctx, qj_malloc_async(ctx, &d_part, sizeof(double) * ((size_t)nblocks + 1) * slots, s));
   double* d_out = d_part + (size_t)nblocks * slots;
   cudaError_t e = qj::launch_tanh_grad(*m, g, wg, d_weights, max_it, alpha, threshold, true,
                                        d_field, d_part, nblocks, d_out, s);
@@ -150,7 +155,7 @@ static int sq_energy(qjg_ctx* ctx, const double* d_params, int32_t nt, int32_t n
   const bool fp64 = precision == QJG_FP64, grad = d_grad != nullptr;
   const int P = 5 * (nt + nb) + 1;
   void* d_scr = nullptr;
-  QJ_CUDA(ctx, cudaMallocAsync(&d_scr, qj::sq_scratch_bytes(fp64, grad, n, max_it, nt, nb), s));
+  QJ_CUDA(ctx, qj_malloc_async(ctx, &d_scr, qj::sq_scratch_bytes(fp64, grad, n, max_it, nt, nb), s));
   double* d_out = nullptr;
   unsigned long long* d_work = nullptr;
   int launched = 0;
@@ -204,7 +209,7 @@ int qjg_fit_lbfgs(qjg_ctx* ctx, double* d_params, int32_t nt, int32_t nb, int64_
   // x1 g0 g1 d | S Y (m x P) | rho alpha (m) | gd
   const size_t total = (size_t)P * 4 + (size_t)2 * m * P + 2 * (size_t)m + 1;
   double* buf = nullptr;
-  QJ_CUDA(ctx, cudaMallocAsync((void**)&buf, total * sizeof(double), s));
+  QJ_CUDA(ctx, qj_malloc_async(ctx, &buf, total * sizeof(double), s));
   double *x = d_params, *x1 = buf, *g0 = x1 + P, *g1 = g0 + P, *d = g1 + P;
   double *S = d + P, *Y = S + (size_t)m * P, *rho = Y + (size_t)m * P, *alpha = rho + m;
   double* gd_dev = alpha + m;

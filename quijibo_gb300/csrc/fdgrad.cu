@@ -238,7 +238,7 @@ extern "C" int qjg_centered_gradient(qjg_ctx* ctx, qjg_rootset rs, const qjg_gri
   const size_t add_bytes = curv ? sizeof(double) * (size_t)f.n : 0;
   const size_t out_bytes = sizeof(unsigned long long) * f.variants + sizeof(double) * f.variants;
   unsigned char* scratch = nullptr;
-  QJ_CUDA(ctx, cudaMallocAsync((void**)&scratch, bits_bytes + add_bytes + out_bytes, s));
+  QJ_CUDA(ctx, qj_malloc_async(ctx, &scratch, bits_bytes + add_bytes + out_bytes, s));
   uint32_t* bits = reinterpret_cast<uint32_t*>(scratch);
   uint32_t* dbits = bits + (size_t)f.words * f.variants;
   double* adding = curv ? reinterpret_cast<double*>(scratch + bits_bytes) : nullptr;

@@ -15,6 +15,9 @@
 struct qjg_ctx {
   int device = 0;
   std::string err;
+  // stream-ordered memory of the calls' scratch; keeps what they free for
+  // the next calls (qjg_trim returns it to the device)
+  cudaMemPool_t pool = nullptr;
   std::vector<std::unique_ptr<qj::MapParams>> rootsets;
   qj::DevStats* d_stats = nullptr;  // counters of the current call
   uint32_t* d_list = nullptr;   // FP64 refine list
@@ -138,6 +141,19 @@ int qj_check_grid(qjg_ctx* ctx, const qjg_grid* g);
 int qj_check_iter(qjg_ctx* ctx, const qjg_iter* it);
 // pow_mode of the FP64 kernels (qj_kernels.h) for these settings: the
 // reference's polar pow unless integer products were asked for and apply
+// Stream-ordered allocation from the context's pool.
+template <class T>
+inline cudaError_t qj_malloc_async(qjg_ctx* ctx, T** p, size_t bytes, cudaStream_t s) {
+  return cudaMallocFromPoolAsync(reinterpret_cast<void**>(p), bytes, ctx->pool, s);
+}
+
+// Whether the context's pool keeps freed memory past a synchronization (the
+// default) or returns it to the device then.
+inline cudaError_t qj_pool_keep(qjg_ctx* ctx, bool keep) {
+  uint64_t thr = keep ? ~0ull : 0ull;
+  return cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &thr);
+}
+
 inline int qj_pow_mode(const qjg_iter* it, bool all_int) {
   const bool pow_ref = !it || it->refine_pow == QJG_REFINE_POW || !all_int;
   return pow_ref ? (it && it->libm == QJG_LIBM_CR ? 2 : 1) : 0;

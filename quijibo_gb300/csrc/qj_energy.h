@@ -27,6 +27,9 @@ size_t sq_scratch_bytes(bool fp64, bool grad, long long n, int max_it, int nt, i
 // out of the gradient]; *launches: kernels launched.
 // process-wide choice of the energy forward kernel: 1 two samples per lane
 void set_energy_pairs(int on);
+// process-wide choice of the FP32 adjoint: 1 (default) the roots of a step
+// spread over a group of lanes where the map fits, 0 one lane per sample
+void set_energy_adjoint_roots(int on);
 // the FP32 polar power's fast form (hardware log2 and sin/cos, polynomial atan)
 cudaError_t set_energy_fast(int on);
 // *work: two counters in the scratch, the map applications of the forward

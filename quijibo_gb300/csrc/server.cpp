@@ -203,7 +203,7 @@ void run_job(qjg_ctx* ctx, cudaStream_t s, Job& j) {
   if (rc == QJG_OK && r.kind == QJG_REQ_FIELD) {
     const int64_t vox = (int64_t)r.grid.res[0] * r.grid.res[1] * r.grid.res[2];
     double* d_field = nullptr;
-    if (cudaMallocAsync((void**)&d_field, vox * sizeof(double), s) != cudaSuccess) rc = QJG_ERR_NOMEM;
+    if (qj_malloc_async(ctx, &d_field, vox * sizeof(double), s) != cudaSuccess) rc = QJG_ERR_NOMEM;
     if (rc == QJG_OK) rc = qjg_field(ctx, h, &r.grid, &it, 0, r.grid.res[2], d_field, nullptr, s);
     qjg_field_stats fs = {};
     if (rc == QJG_OK) rc = qjg_field_stats_read(ctx, s, &fs);
@@ -219,8 +219,8 @@ void run_job(qjg_ctx* ctx, cudaStream_t s, Job& j) {
     double* v64 = nullptr;
     int32_t* tris = nullptr;
     int64_t vcap = std::max<int64_t>(r.vert_cap, 1), tcap = std::max<int64_t>(r.tri_cap, 1);
-    if (cudaMallocAsync((void**)&v64, vcap * 3 * sizeof(double), s) != cudaSuccess ||
-        cudaMallocAsync((void**)&tris, tcap * 3 * sizeof(int32_t), s) != cudaSuccess)
+    if (qj_malloc_async(ctx, &v64, vcap * 3 * sizeof(double), s) != cudaSuccess ||
+        qj_malloc_async(ctx, &tris, tcap * 3 * sizeof(int32_t), s) != cudaSuccess)
       rc = QJG_ERR_NOMEM;
     qjg_mesh_stats ms = {};
     // meshes up to 2^24 voxels run as the fixed launch sequence (one wait at
@@ -257,10 +257,10 @@ void run_job(qjg_ctx* ctx, cudaStream_t s, Job& j) {
   } else if (rc == QJG_OK && r.kind == QJG_REQ_ENERGY) {
     const int64_t P = 5 * (r.n_top + r.n_bot) + 1;
     double *d_p = nullptr, *d_x = nullptr, *d_t = nullptr, *d_g = nullptr;
-    if (cudaMallocAsync((void**)&d_p, P * sizeof(double), s) != cudaSuccess ||
-        cudaMallocAsync((void**)&d_g, P * sizeof(double), s) != cudaSuccess ||
-        cudaMallocAsync((void**)&d_x, std::max<int64_t>(r.n_samples, 1) * 3 * sizeof(double), s) != cudaSuccess ||
-        cudaMallocAsync((void**)&d_t, std::max<int64_t>(r.n_samples, 1) * sizeof(double), s) != cudaSuccess)
+    if (qj_malloc_async(ctx, &d_p, P * sizeof(double), s) != cudaSuccess ||
+        qj_malloc_async(ctx, &d_g, P * sizeof(double), s) != cudaSuccess ||
+        qj_malloc_async(ctx, &d_x, std::max<int64_t>(r.n_samples, 1) * 3 * sizeof(double), s) != cudaSuccess ||
+        qj_malloc_async(ctx, &d_t, std::max<int64_t>(r.n_samples, 1) * sizeof(double), s) != cudaSuccess)
       rc = QJG_ERR_NOMEM;
     if (rc == QJG_OK &&
         (cudaMemcpyAsync(d_p, j.params.data(), P * sizeof(double), cudaMemcpyHostToDevice, s) ||
@@ -308,6 +308,9 @@ void worker_main(qjg_server* srv, int w) {
   qjg_ctx* ctx = nullptr;
   cudaSetDevice(srv->device);
   const int crc = qjg_create(srv->device, &ctx);
+  // requests' buffers go back to the device when a request ends, so that
+  // the HBM budget of admitted requests is what the workers hold
+  if (crc == QJG_OK) qj_pool_keep(ctx, false);
   cudaStream_t s = nullptr;
   cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
   for (;;) {
@@ -449,7 +452,7 @@ int run_energy_batch(qjg_ctx* ctx, cudaStream_t s, std::vector<std::shared_ptr<J
     doubles += 2 * (5 * (int64_t)(r.n_top + r.n_bot) + 1) + 4 * r.n_samples;
   }
   double* arena = nullptr;
-  if (cudaMallocAsync((void**)&arena, (size_t)std::max<int64_t>(doubles, 1) * sizeof(double), s))
+  if (qj_malloc_async(ctx, &arena, (size_t)std::max<int64_t>(doubles, 1) * sizeof(double), s))
     return QJG_ERR_NOMEM;
   std::vector<qjg_energy_item> items((size_t)K);
   int rc = QJG_OK;
@@ -500,6 +503,7 @@ void ebatch_main(qjg_server* srv) {
   cudaSetDevice(srv->device);
   qjg_ctx* ctx = nullptr;
   const int crc = qjg_create(srv->device, &ctx);
+  if (crc == QJG_OK) qj_pool_keep(ctx, false);
   cudaStream_t s = nullptr;
   cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
   for (;;) {

@@ -102,7 +102,7 @@ int qjg_tanh_fit(qjg_ctx* ctx, int32_t mode, qjg_map_state* state, const qjg_gri
   const int nblocks = qj::tanh_blocks();
   const int slots = qj::tanh_slots(nt, nb);
   double* d_part = nullptr;
-  QJ_CUDA(ctx, cudaMallocAsync((void**)&d_part, sizeof(double) * ((size_t)nblocks + 1) * slots, s));
+  QJ_CUDA(ctx, qj_malloc_async(ctx, &d_part, sizeof(double) * ((size_t)nblocks + 1) * slots, s));
   double* d_out = d_part + (size_t)nblocks * slots;
   double* h_out = nullptr;
   if (cudaMallocHost((void**)&h_out, sizeof(double) * slots) != cudaSuccess) {
@@ -190,7 +190,7 @@ int qjg_tanh_max_score(qjg_ctx* ctx, const qjg_grid* grid, const qjg_grid* weigh
   const long long n = (long long)grid->res[0] * grid->res[1] * grid->res[2];
   const int nb = qj::conformal_blocks(n);
   double* d_w = nullptr;
-  QJ_CUDA(ctx, cudaMallocAsync((void**)&d_w, sizeof(double) * ((size_t)n + 3 * (size_t)nb + 3), s));
+  QJ_CUDA(ctx, qj_malloc_async(ctx, &d_w, sizeof(double) * ((size_t)n + 3 * (size_t)nb + 3), s));
   double* part = d_w + n;
   double* sums = part + 3 * (size_t)nb;
   double h[3];
@@ -443,7 +443,7 @@ int qjg_reweight_inside(qjg_ctx* ctx, int64_t n, const double* d_md, const doubl
   QJ_CUDA(ctx, cudaSetDevice(ctx->device));
   const int nb = qj::conformal_blocks(n);
   double* d_part = nullptr;
-  QJ_CUDA(ctx, cudaMallocAsync((void**)&d_part, sizeof(double) * (3 * (size_t)nb + 3), s));
+  QJ_CUDA(ctx, qj_malloc_async(ctx, &d_part, sizeof(double) * (3 * (size_t)nb + 3), s));
   double h[3];
   cudaError_t e = qj::launch_region_sums(d_md, d_fd, d_w, n, d_part, d_part + 3 * nb, s);
   if (e == cudaSuccess)

@@ -214,6 +214,8 @@ EXPORTS = {
                                C.c_void_p, C.c_int64, C.c_void_p], C.c_int),
     "qjg_mesh_async_result": ([C.c_void_p, C.POINTER(QjgMeshStats)], C.c_int),
     "qjg_set_energy_pairs": ([C.c_int], C.c_int),
+    "qjg_set_energy_adjoint_roots": ([C.c_int], C.c_int),
+    "qjg_trim": ([C.c_void_p], C.c_int),
     "qjg_set_energy_fast": ([C.c_int], C.c_int),
     "qjg_energy_backward_batch": ([C.c_void_p, C.c_int32, C.POINTER(QjgEnergyItem), C.c_void_p],
                                   C.c_int),
@@ -456,6 +458,13 @@ def set_energy_pairs(on):
     load().qjg_set_energy_pairs(int(bool(on)))
 
 
+def set_energy_adjoint_roots(on):
+    """FP32 adjoint: roots spread over a group of 16 lanes per sample (True,
+    the default, for maps of at most 64 roots a side) or one lane per sample
+    walking the roots (False)."""
+    load().qjg_set_energy_adjoint_roots(int(bool(on)))
+
+
 def set_energy_fast(on):
     """FP32 energy's polar power: fast hardware approximations (True, the
     default) or the accurate device functions (False)."""
@@ -562,6 +571,10 @@ class Context:
         if self.h:
             self.L.qjg_destroy(self.h)
             self.h = None
+
+    def trim(self):
+        """Return the device memory the context's pool keeps to the device."""
+        self._check(self.L.qjg_trim(self.h), "qjg_trim")
 
     def __del__(self):
         try:

@@ -211,3 +211,70 @@ def test_forward_with_two_samples_per_lane(ctx, precision):
     tol = 1e-5 if precision == lib.QJG_FP32 else 1e-12
     assert abs(e1 - e0) <= tol * abs(e0)
     assert np.linalg.norm(g1 - g0) <= tol * np.linalg.norm(g0)
+
+
+@pytest.mark.parametrize("nt,nb,exps", [(64, 16, (1,)), (48, 24, (1,)), (8, 4, (1, 2)),
+                                         (12, 0, (1, 2))])
+def test_adjoint_root_groups_match_one_lane(ctx, nt, nb, exps):
+    """The FP32 adjoint with the roots spread over groups of 16 lanes (one
+    bottom root per lane up to 16, four above) against
+    the one-lane adjoint: within 1e-6 (vector norm; the products and sums run
+    in another order), as close to the FP64 adjoint as the one-lane form
+    (the 8/4 map with exponents 2 is 3e-4 from FP64 in either FP32 form), the
+    same bits on a repeated call, the same orbit steps."""
+    rs = draw_rootset(5, nt, nb, -1.2, 1.2, exps=exps)
+    rs.scale = conformal_scale(rs, Grid((24, 24, 24), lengths=(2.0, 2.0, 2.0)))
+    xyz, _ = poisson_disk(6000, seed=5)
+    t = ShapeSDF(5)(xyz)
+    p = dev(lib.params_of(rs))
+    X, T = dev(xyz), dev(t)
+
+    def run(precision):
+        g = torch.empty(len(p), dtype=torch.float64, device="cuda")
+        e = ctx.energy(p.data_ptr(), nt, nb, len(t), X.data_ptr(), T.data_ptr(), 12, 2.0,
+                       precision=precision, d_grad=g.data_ptr())
+        return e, g.cpu().numpy(), ctx.energy_last_work()
+
+    try:
+        lib.set_energy_adjoint_roots(False)
+        e_one, g_one, w_one = run(lib.QJG_FP32)
+        lib.set_energy_adjoint_roots(True)
+        e_grp, g_grp, w_grp = run(lib.QJG_FP32)
+        e_grp2, g_grp2, _ = run(lib.QJG_FP32)
+    finally:
+        lib.set_energy_adjoint_roots(True)
+    e64, g64, _ = run(lib.QJG_FP64)
+    assert w_one == w_grp and w_grp[1] > 0
+    assert e_grp == e_one and e_grp2 == e_grp and np.array_equal(g_grp2, g_grp)
+    assert np.all(np.isfinite(g_grp)) and np.linalg.norm(g64) > 0
+    rel = lambda a, b: np.linalg.norm(a - b) / np.linalg.norm(b)
+    assert rel(g_grp, g_one) <= 1e-6, rel(g_grp, g_one)
+    assert rel(g_grp, g64) <= 1.1 * rel(g_one, g64) + 1e-6, (rel(g_grp, g64), rel(g_one, g64))
+
+
+def test_context_pool_keeps_scratch_until_trim(ctx, config4):
+    """The context keeps the scratch its calls free (its memory pool) and
+    qjg_trim returns it: a repeated gradient call gives the same bits, and
+    trimming frees at least the orbit the forward pass kept (samples x
+    iterations x 16 bytes)."""
+    rs, xyz, t, p = config4
+    P = dev(lib.params_of(rs))
+    X, T = dev(xyz), dev(t)
+    g = torch.empty(len(P), dtype=torch.float64, device="cuda")
+
+    def run():
+        e = ctx.energy(P.data_ptr(), rs.n_top, rs.n_bottom, len(t), X.data_ptr(), T.data_ptr(),
+                       p["max_it"], p["escape"], precision=lib.QJG_FP32, d_grad=g.data_ptr())
+        return e, g.cpu().numpy()
+
+    e0, g0 = run()
+    torch.cuda.synchronize()
+    kept = torch.cuda.mem_get_info()[0]
+    e1, g1 = run()
+    assert e1 == e0 and np.array_equal(g1, g0)
+    assert torch.cuda.mem_get_info()[0] >= kept - (2 << 20)  # nothing new mapped
+    ctx.trim()
+    freed = torch.cuda.mem_get_info()[0] - kept
+    assert freed >= 0.9 * len(t) * p["max_it"] * 16, freed
+    e2, g2 = run()
+    assert e2 == e0 and np.array_equal(g2, g0)
