@@ -43,12 +43,12 @@ def sq_forward_app_flops(nt, nb):
     return per
 
 
-# Adjoint, per orbit step: the step is recomputed twice (the segment's
-# forward sweep and the application that keeps the prefix products), then
-# per root term: the log|g| gradient loop 20, q - r 4, polar power 18, the
-# prefix-product adjoint conj(F) U 28 and U conj(P) 28, the polar power's
-# vector-Jacobian product 57, the log|g| term 40, the warp sums of the five
-# components 5, the running q-bar 4; per step: Q-bar 16, d/d log s 7, the
+# Adjoint, per orbit step: the step's map application at the forward pass's
+# kept q_n (its factors and prefix products), then per root term: the
+# log|g| gradient loop 20, q - r 4, polar power 18, the prefix-product
+# adjoint conj(F) U 28 and U conj(P) 28, the polar power's vector-Jacobian
+# product 57, the log|g| term 40, the sums of the five components over the
+# samples 5, the running q-bar 4; per step: Q-bar 16, d/d log s 7, the
 # quotient's adjoint (conj(B) / |B|^2, two products, B-bar) 136 with bottom
 # roots, g-bar 12.
 SQ_BWD_ROOT = 20 + 4 + 18 + 28 + 28 + 57 + 40 + 5 + 4
@@ -56,7 +56,7 @@ SQ_BWD_SPECIAL_ROOT = 6
 
 
 def sq_backward_step_flops(nt, nb):
-    return 2 * sq_forward_app_flops(nt, nb) + SQ_BWD_ROOT * (nt + nb) + 16 + 7 + (136 if nb else 0) + 12
+    return sq_forward_app_flops(nt, nb) + SQ_BWD_ROOT * (nt + nb) + 16 + 7 + (136 if nb else 0) + 12
 
 
 def energy_flops(nt, nb, applications, steps=0):
@@ -65,5 +65,5 @@ def energy_flops(nt, nb, applications, steps=0):
     nr = nt + nb
     flops = applications * sq_forward_app_flops(nt, nb) + steps * sq_backward_step_flops(nt, nb)
     special = applications * (SQ_FWD_SPECIAL_ROOT * nr + 4)
-    special += steps * (2 * (SQ_FWD_SPECIAL_ROOT * nr + 4) + SQ_BWD_SPECIAL_ROOT * nr)
+    special += steps * ((SQ_FWD_SPECIAL_ROOT * nr + 4) + SQ_BWD_SPECIAL_ROOT * nr)
     return flops, special
