@@ -47,10 +47,11 @@ int qjg_set_energy_pairs(int on);
  * orders).  Set it while no energy call is in flight. */
 int qjg_set_energy_adjoint_roots(int on);
 
-/* Process-wide form of the FP32 energy's polar power: 1 (the default) the
- * fast form (hardware approximations of log2 and of sin/cos, a polynomial
- * atan: about 1e-6 relative per power), 0 the accurate device library
- * functions.  Set it while no energy call is in flight. */
+/* Process-wide form of the FP32 energy's arithmetic: 1 (the default) the
+ * fast form (hardware approximations of log2, of sin/cos and of the
+ * reciprocal for every division, a polynomial atan: about 1e-6 relative per
+ * power), 0 the accurate device library functions and IEEE divisions.  Set
+ * it while no energy call is in flight. */
 int qjg_set_energy_fast(int on);
 
 /* Work of the last qjg_energy_forward/backward call on ctx: the map

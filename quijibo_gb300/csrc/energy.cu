@@ -771,10 +771,12 @@ struct PowParts {
 
 // The FP32 polar power's fast form (the default; qjg_set_energy_fast(0)
 // selects the accurate device functions): the angle from a polynomial atan
-// and the hardware approximations of log2 and of sin/cos.  On the
-// differentiation workload (200k samples, 64/16 roots, 30 iterations) it
-// moves the FP32 energy from 3e-9 to 8e-8 of the FP64 form's and the FP32
-// gradient from 2e-7 to 9e-7, for a 21% faster forward kernel.
+// and the hardware approximations of log2, of sin/cos and of the reciprocal
+// (divisions and the square root of |d|^2).  On the differentiation
+// workload (200k samples, 64/16 roots, 30 iterations) it moves the FP32
+// energy from 3e-9 to 8e-8 of the FP64 form's and the FP32 gradient from
+// 2e-7 to 9e-7, for a forward kernel 1.715 -> 1.162 ms and an adjoint
+// kernel 0.45 -> 0.35 ms.
 __constant__ int c_sq_fast = 1;
 
 // atan(t) for 0 <= t <= 1 as t P(t^2), P of degree 7 fitted for this
@@ -802,6 +804,17 @@ __device__ __forceinline__ float atan2_pos_fast(float y, float x) {
   return x < 0.f ? 3.14159265358979324f - a : a;
 }
 
+// a / b: FP64 and the accurate FP32 form divide (IEEE); the fast FP32 form
+// takes the hardware reciprocal (__fdividef, 2 ulp), whose IEEE division
+// sequence was a tenth of the adjoint's instructions.
+template <class T>
+__device__ __forceinline__ T sq_div(T a, T b) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (c_sq_fast) return __fdividef(a, b);
+  }
+  return a / b;
+}
+
 template <class T>
 __device__ __forceinline__ V4<T> powv(const V4<T>& d, T e, PowParts<T>* pp) {
   if constexpr (std::is_same<T, float>::value) {
@@ -823,7 +836,11 @@ __device__ __forceinline__ V4<T> powv(const V4<T>& d, T e, PowParts<T>* pp) {
       sincospif(e * theta * 0.318309886183790672f, &s, &c);
     }
     const float k = A * s * rv;
-    if (pp) *pp = PowParts<T>{sqrtf(r2), vm, theta, A, c, s};
+    if (pp) {
+      // rho = sqrt(r2), as r2 rsqrt(r2) in the fast form
+      const float rho = c_sq_fast ? (r2 > 0.f ? r2 * rsqrtf(r2) : 0.f) : sqrtf(r2);
+      *pp = PowParts<T>{rho, vm, theta, A, c, s};
+    }
     return V4<T>{A * c, k * d.x, k * d.y, k * d.z};
   }
   const T v2 = d.x * d.x + d.y * d.y + d.z * d.z;
@@ -841,19 +858,21 @@ __device__ __forceinline__ V4<T> powv(const V4<T>& d, T e, PowParts<T>* pp) {
 template <class T>
 __device__ __forceinline__ V4<T> powv_vjp(const V4<T>& d, T e, const PowParts<T>& p,
                                           const V4<T>& Pb, T* ebar) {
-  const T ux = p.vm > T(0) ? d.x / p.vm : T(0), uy = p.vm > T(0) ? d.y / p.vm : T(0),
-          uz = p.vm > T(0) ? d.z / p.vm : T(0);
+  // 1/|v| and 1/rho once (FP64: IEEE divisions)
+  const T ivm = p.vm > T(0) ? sq_div(T(1), p.vm) : T(0);
+  const T irho = sq_div(T(1), p.rho);
+  const T ux = d.x * ivm, uy = d.y * ivm, uz = d.z * ivm;
   const T pu = Pb.x * ux + Pb.y * uy + Pb.z * uz;
   const T Ab = Pb.w * p.c + pu * p.s;
   const T phib = p.A * (pu * p.c - Pb.w * p.s);
-  const T rhob = Ab * e * p.A / p.rho;
+  const T rhob = Ab * e * p.A * irho;
   const T thetab = phib * e;
   *ebar += Ab * p.A * log(p.rho) + phib * p.theta;
-  const T r2 = p.rho * p.rho;
+  const T ir2 = irho * irho;
   V4<T> db;
-  db.w = rhob * d.w / p.rho - thetab * p.vm / r2;
-  const T kv = rhob / p.rho;
-  const T kt = thetab * d.w / r2;
+  db.w = rhob * d.w * irho - thetab * p.vm * ir2;
+  const T kv = rhob * irho;
+  const T kt = thetab * d.w * ir2;
   db.x = kv * d.x + kt * ux;
   db.y = kv * d.y + kt * uy;
   db.z = kv * d.z + kt * uz;
@@ -862,9 +881,9 @@ __device__ __forceinline__ V4<T> powv_vjp(const V4<T>& d, T e, const PowParts<T>
     const T ub = p.A * p.s;
     const T ubx = ub * Pb.x, uby = ub * Pb.y, ubz = ub * Pb.z;
     const T proj = ubx * ux + uby * uy + ubz * uz;
-    db.x += (ubx - proj * ux) / p.vm;
-    db.y += (uby - proj * uy) / p.vm;
-    db.z += (ubz - proj * uz) / p.vm;
+    db.x += (ubx - proj * ux) * ivm;
+    db.y += (uby - proj * uy) * ivm;
+    db.z += (ubz - proj * uz) * ivm;
   }
   return db;
 }
@@ -886,7 +905,7 @@ __device__ __forceinline__ V4<T> sq_apply(const T* __restrict__ rp, const T* __r
     for (int i = lo; i < hi; i++) {
       const V4<T> d{q.w - rp[4 * i], q.x - rp[4 * i + 1], q.y - rp[4 * i + 2], q.z - rp[4 * i + 3]};
       const T e = ep[i];
-      const T k = (side ? -e : e) / v4dot(d, d);
+      const T k = sq_div(side ? -e : e, v4dot(d, d));
       g = v4add(g, v4scale(d, k));
       const V4<T> P = powv<T>(d, e, nullptr);
       a = i == lo ? P : v4mul(a, P);
@@ -897,7 +916,7 @@ __device__ __forceinline__ V4<T> sq_apply(const T* __restrict__ rp, const T* __r
   }
   V4<T> Q;
   if (nb > 0) {
-    const V4<T> W = v4scale(v4conj(acc[1]), T(1) / v4dot(acc[1], acc[1]));
+    const V4<T> W = v4scale(v4conj(acc[1]), sq_div(T(1), v4dot(acc[1], acc[1])));
     Q = v4scale(v4mul(acc[0], W), s);
   } else {
     Q = v4scale(acc[0], s);
@@ -1067,8 +1086,8 @@ __device__ __forceinline__ void sq_apply2(const T* __restrict__ rp, const T* __r
       const T e = ep[i];
       const V4<T> da{qa.w - r0, qa.x - r1, qa.y - r2, qa.z - r3};
       const V4<T> db{qb.w - r0, qb.x - r1, qb.y - r2, qb.z - r3};
-      const T ka = (side ? -e : e) / v4dot(da, da);
-      const T kb = (side ? -e : e) / v4dot(db, db);
+      const T ka = sq_div(side ? -e : e, v4dot(da, da));
+      const T kb = sq_div(side ? -e : e, v4dot(db, db));
       ga = v4add(ga, v4scale(da, ka));
       gb = v4add(gb, v4scale(db, kb));
       const V4<T> Pa = powv<T>(da, e, nullptr);
@@ -1080,8 +1099,8 @@ __device__ __forceinline__ void sq_apply2(const T* __restrict__ rp, const T* __r
     acc[1][side] = b;
   }
   if (nb > 0) {
-    const V4<T> Wa = v4scale(v4conj(acc[0][1]), T(1) / v4dot(acc[0][1], acc[0][1]));
-    const V4<T> Wb = v4scale(v4conj(acc[1][1]), T(1) / v4dot(acc[1][1], acc[1][1]));
+    const V4<T> Wa = v4scale(v4conj(acc[0][1]), sq_div(T(1), v4dot(acc[0][1], acc[0][1])));
+    const V4<T> Wb = v4scale(v4conj(acc[1][1]), sq_div(T(1), v4dot(acc[1][1], acc[1][1])));
     qa = v4scale(v4mul(acc[0][0], Wa), s);
     qb = v4scale(v4mul(acc[1][0], Wb), s);
   } else {
@@ -1372,11 +1391,11 @@ __global__ void __launch_bounds__(SQ_T) sq_bwd_kernel(
           V4<T> Tq, Bq;
           const V4<T> Q = sq_apply<T>(rp, ep, nt, nb, s, qn, &lg, F, nullptr, &Tq, &Bq);
           // L_{n+1} = L_n + log|g| + log|Q|
-          const V4<T> Qb = v4add(qb, v4scale(Q, Lb / v4dot(Q, Q)));
+          const V4<T> Qb = v4add(qb, v4scale(Q, sq_div(Lb, v4dot(Q, Q))));
           // d/d log s: <Qbar, Q>
           dls = v4dot(Qb, Q);
           if (nb > 0) {
-            const V4<T> W4 = v4scale(v4conj(Bq), T(1) / v4dot(Bq, Bq));
+            const V4<T> W4 = v4scale(v4conj(Bq), sq_div(T(1), v4dot(Bq, Bq)));
             Tb = v4scale(v4mul(Qb, v4conj(W4)), s);
             const V4<T> Wb = v4scale(v4mul(v4conj(Tq), Qb), s);
             Bb = v4scale(v4mul(v4mul(v4conj(W4), Wb), v4conj(W4)), T(-1));
@@ -1388,9 +1407,9 @@ __global__ void __launch_bounds__(SQ_T) sq_bwd_kernel(
           for (int i = 0; i < nr; i++) {
             const V4<T> d{qn.w - rp[4 * i], qn.x - rp[4 * i + 1], qn.y - rp[4 * i + 2],
                           qn.z - rp[4 * i + 3]};
-            g = v4add(g, v4scale(d, (i >= nt ? -ep[i] : ep[i]) / v4dot(d, d)));
+            g = v4add(g, v4scale(d, sq_div(i >= nt ? -ep[i] : ep[i], v4dot(d, d))));
           }
-          gb = v4scale(g, Lb / v4dot(g, g));
+          gb = v4scale(g, sq_div(Lb, v4dot(g, g)));
         }
         dls = warp_sum(dls);
         if (lane == 0) acc[1 + 5 * nr] += (double)dls;
@@ -1415,10 +1434,10 @@ __global__ void __launch_bounds__(SQ_T) sq_bwd_kernel(
               const T sgn = side ? T(-1) : T(1);
               const T d2 = v4dot(d, d);
               const T dg = v4dot(d, gb);
-              dbar = v4add(dbar, v4scale(v4add(v4scale(gb, T(1) / d2),
-                                               v4scale(d, T(-2) * dg / (d2 * d2))),
+              const T id2 = sq_div(T(1), d2);
+              dbar = v4add(dbar, v4scale(v4add(v4scale(gb, id2), v4scale(d, T(-2) * dg * id2 * id2)),
                                          sgn * ep[i]));
-              eb += sgn * dg / d2;
+              eb += sgn * dg * id2;
               c0 = -dbar.w;
               c1 = -dbar.x;
               c2 = -dbar.y;
@@ -1540,7 +1559,7 @@ __device__ __forceinline__ void side_fwd(const T* __restrict__ rp, const T* __re
       const V4<T> P = powv<T>(d, ep[i], nullptr);
       r.P[j] = P;
       Cp = j ? v4mul(Cp, P) : P;
-      gp = v4add(gp, v4scale(d, sgn * ep[i] / v4dot(d, d)));
+      gp = v4add(gp, v4scale(d, sq_div(sgn * ep[i], v4dot(d, d))));
     }
   }
   // inclusive prefix over the group's lanes: x_l = C_0 C_1 ... C_l
@@ -1594,10 +1613,10 @@ __device__ __forceinline__ void side_adj(const T* __restrict__ rp, const T* __re
       // g term: sgn e d/|d|^2
       const T d2 = v4dot(d, d);
       const T dg = v4dot(d, gb);
-      dbar = v4add(dbar, v4scale(v4add(v4scale(gb, T(1) / d2),
-                                       v4scale(d, T(-2) * dg / (d2 * d2))),
+      const T id2 = sq_div(T(1), d2);
+      dbar = v4add(dbar, v4scale(v4add(v4scale(gb, id2), v4scale(d, T(-2) * dg * id2 * id2)),
                                  sgn * ep[i]));
-      eb += sgn * dg / d2;
+      eb += sgn * dg * id2;
       if (on) {
         r.acc[j][0] -= dbar.w;
         r.acc[j][1] -= dbar.x;
@@ -1678,22 +1697,22 @@ __global__ void __launch_bounds__(SQ_T, MINB) sq_bwd_roots_kernel(
       const V4<T> g = group_sum4<T, G>(gp);
       V4<T> Q, Tb, Bb;
       if (nb > 0) {
-        const V4<T> W4 = v4scale(v4conj(bot.tot), T(1) / v4dot(bot.tot, bot.tot));
+        const V4<T> W4 = v4scale(v4conj(bot.tot), sq_div(T(1), v4dot(bot.tot, bot.tot)));
         Q = v4scale(v4mul(top.tot, W4), s);
         // L_{n+1} = L_n + log|g| + log|Q|
-        const V4<T> Qb = v4add(qb, v4scale(Q, Lb / v4dot(Q, Q)));
+        const V4<T> Qb = v4add(qb, v4scale(Q, sq_div(Lb, v4dot(Q, Q))));
         if (on) dls += v4dot(Qb, Q);
         Tb = v4scale(v4mul(Qb, v4conj(W4)), s);
         const V4<T> Wb = v4scale(v4mul(v4conj(top.tot), Qb), s);
         Bb = v4scale(v4mul(v4mul(v4conj(W4), Wb), v4conj(W4)), T(-1));
       } else {
         Q = v4scale(top.tot, s);
-        const V4<T> Qb = v4add(qb, v4scale(Q, Lb / v4dot(Q, Q)));
+        const V4<T> Qb = v4add(qb, v4scale(Q, sq_div(Lb, v4dot(Q, Q))));
         if (on) dls += v4dot(Qb, Q);
         Tb = v4scale(Qb, s);
         Bb = zero;
       }
-      const V4<T> gb = v4scale(g, Lb / v4dot(g, g));
+      const V4<T> gb = v4scale(g, sq_div(Lb, v4dot(g, g)));
       V4<T> qbp = zero;
       side_adj<T, CT>(rp, ep, T(1), qn, top, Tb, gb, on, qbp);
       side_adj<T, CB>(rp, ep, T(-1), qn, bot, Bb, gb, on, qbp);
@@ -1934,10 +1953,10 @@ __global__ void __launch_bounds__(SQ_T) sq_bwd_batch_kernel(
             T lg;
             V4<T> Tq, Bq;
             const V4<T> Q = sq_apply<T>(rp, ep, nt, nb, s, qn, &lg, F, nullptr, &Tq, &Bq);
-            const V4<T> Qb = v4add(qb, v4scale(Q, Lb / v4dot(Q, Q)));
+            const V4<T> Qb = v4add(qb, v4scale(Q, sq_div(Lb, v4dot(Q, Q))));
             dls = v4dot(Qb, Q);
             if (nb > 0) {
-              const V4<T> W4 = v4scale(v4conj(Bq), T(1) / v4dot(Bq, Bq));
+              const V4<T> W4 = v4scale(v4conj(Bq), sq_div(T(1), v4dot(Bq, Bq)));
               Tb = v4scale(v4mul(Qb, v4conj(W4)), s);
               const V4<T> Wb = v4scale(v4mul(v4conj(Tq), Qb), s);
               Bb = v4scale(v4mul(v4mul(v4conj(W4), Wb), v4conj(W4)), T(-1));
@@ -1948,9 +1967,9 @@ __global__ void __launch_bounds__(SQ_T) sq_bwd_batch_kernel(
             for (int i = 0; i < nr; i++) {
               const V4<T> d{qn.w - rp[4 * i], qn.x - rp[4 * i + 1], qn.y - rp[4 * i + 2],
                             qn.z - rp[4 * i + 3]};
-              g = v4add(g, v4scale(d, (i >= nt ? -ep[i] : ep[i]) / v4dot(d, d)));
+              g = v4add(g, v4scale(d, sq_div(i >= nt ? -ep[i] : ep[i], v4dot(d, d))));
             }
-            gb = v4scale(g, Lb / v4dot(g, g));
+            gb = v4scale(g, sq_div(Lb, v4dot(g, g)));
           }
           dls = warp_sum(dls);
           if (lane == 0) acc[1 + 5 * nr] += (double)dls;
@@ -1973,10 +1992,11 @@ __global__ void __launch_bounds__(SQ_T) sq_bwd_batch_kernel(
                 const T sgn = side ? T(-1) : T(1);
                 const T d2 = v4dot(d, d);
                 const T dg = v4dot(d, gb);
-                dbar = v4add(dbar, v4scale(v4add(v4scale(gb, T(1) / d2),
-                                                 v4scale(d, T(-2) * dg / (d2 * d2))),
+                const T id2 = sq_div(T(1), d2);
+                dbar = v4add(dbar, v4scale(v4add(v4scale(gb, id2),
+                                                 v4scale(d, T(-2) * dg * id2 * id2)),
                                            sgn * ep[i]));
-                eb += sgn * dg / d2;
+                eb += sgn * dg * id2;
                 c0 = -dbar.w;
                 c1 = -dbar.x;
                 c2 = -dbar.y;
