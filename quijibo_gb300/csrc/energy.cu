@@ -1482,9 +1482,9 @@ __global__ void __launch_bounds__(SQ_T) sq_bwd_kernel(
 // factors before it and the conjugate of the product after it:
 //   Pbar_i = conj(F_{i-1}) Ubar conj(S_{i+1}),
 // F from the group's exclusive prefix times the lane's own factors, S from
-// the exclusive suffix.  Each lane sums its own roots' five components over
-// the sample's steps in registers and adds them to its group's double
-// accumulators in shared memory when the sample ends; the group sums only
+// the exclusive suffix.  Each lane sums its own roots' five components in
+// FP32 registers over the steps of up to SQ_FLUSH samples and then adds them
+// to its group's double accumulators in shared memory; the group sums only
 // qbar and the log-gradient vector per step (butterflies, so that every lane
 // of the group holds the same bits).  The groups of a warp run their steps
 // together down from the warp's longest orbit (the samples are sorted by
@@ -1629,7 +1629,7 @@ __device__ __forceinline__ void side_adj(const T* __restrict__ rp, const T* __re
   }
 }
 
-// The run's sums of the finished sample into the group's accumulators.
+// The run's register sums into the group's accumulators (and reset).
 template <class T, int C>
 __device__ __forceinline__ void side_flush(SideRun<T, C>& r, double* acc, int nr) {
 #pragma unroll
@@ -1646,6 +1646,7 @@ __device__ __forceinline__ void side_flush(SideRun<T, C>& r, double* acc, int nr
 }
 
 static_assert(SQ_CK == 1, "sq_bwd_roots_kernel reads the forward pass's q at every step");
+constexpr int SQ_FLUSH = 16;  // samples a lane sums in FP32 before adding to the double sums
 
 template <class T, int G, int CT, int CB, int MINB>
 __global__ void __launch_bounds__(SQ_T, MINB) sq_bwd_roots_kernel(
@@ -1676,6 +1677,8 @@ __global__ void __launch_bounds__(SQ_T, MINB) sq_bwd_roots_kernel(
   const V4<T> zero{T(0), T(0), T(0), T(0)};
   const int count = *total;
   const long long stride = (long long)gridDim.x * NG;
+  T dls = T(0);
+  int since = 0;  // samples summed in registers since the last flush
   // the warp's first group in the sorted list; its groups take consecutive entries
   for (long long base = ((long long)blockIdx.x * SQ_T + (threadIdx.x & ~31)) / G; base < count;
        base += stride) {
@@ -1686,7 +1689,6 @@ __global__ void __launch_bounds__(SQ_T, MINB) sq_bwd_roots_kernel(
     V4<T> qb = in ? seed_q[k] : zero;
     const T Lb = in ? seed_L[k] : T(0);
     const int Nmax = __reduce_max_sync(0xffffffffu, N);
-    T dls = T(0);
     for (int n = Nmax - 1; n >= 0; n--) {
       const bool on = n < N;  // this group's orbit has step n
       // the forward pass's own q_n (SQ_CK = 1)
@@ -1719,12 +1721,21 @@ __global__ void __launch_bounds__(SQ_T, MINB) sq_bwd_roots_kernel(
       qbp = group_sum4<T, G>(qbp);
       if (on) qb = qbp;
     }
-    if (in) {
+    // most gradient samples run one or two steps, so a flush per sample (25
+    // FP64 additions and conversions per lane) kept the FP64 pipe 41% busy
+    // and took 40% of the kernel; sums of at most SQ_FLUSH samples stay in
+    // FP32 registers
+    if (++since == SQ_FLUSH) {
       side_flush<T, CT>(top, acc, nr);
       side_flush<T, CB>(bot, acc, nr);
       if (gl == 0) acc[1 + 5 * nr] += (double)dls;
+      dls = T(0);
+      since = 0;
     }
   }
+  side_flush<T, CT>(top, acc, nr);
+  side_flush<T, CB>(bot, acc, nr);
+  if (gl == 0) acc[1 + 5 * nr] += (double)dls;
   __syncthreads();
   // groups in order (the energy and the left-out count are in the chunk rows)
   for (int k = threadIdx.x; k < slots; k += SQ_T) {
