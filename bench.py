@@ -304,6 +304,17 @@ def run_ours(args, world, rank, local):
                                    check_slices=args.large_slices, hbm_gbs=hbm_peak_gbs()[0])
         large = bench_large(largs)
 
+    # the differentiation configuration (200k Poisson-disk samples, 64 top /
+    # 16 bottom roots, 30 iterations): FP32 forward + recompute-free adjoint
+    # per call (gradients/s), both FP64 forms beside it, the algorithmic FLOP
+    # rate of each against the FMA probe, and 50 device L-BFGS steps
+    energy = None
+    if rank == 0 and not args.no_energy:
+        from quijibo_gb300.benchmarks import bench_energy
+        eargs = argparse.Namespace(samples=200_000, steps=50, fp32_only=False,
+                                   energy_pairs=False, energy_accurate=False)
+        energy = bench_energy(eargs)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         slices = [int(v) for v in np.linspace(0, g.res[2] - 1, args.cpu_slices)]
@@ -335,6 +346,7 @@ def run_ours(args, world, rank, local):
         "cpu_baseline": cpu,
         "serving": serving,
         "large": large,
+        "energy": energy,
         "e2e": e2e,
         "gpu_launches": launches,
         "clocks": clk,
@@ -361,6 +373,8 @@ def main():
     ap.add_argument("--no-large", action="store_true", help="skip the 2200^3 large-grid record")
     ap.add_argument("--large-res", type=int, default=2200)
     ap.add_argument("--large-slices", type=int, default=4)
+    ap.add_argument("--no-energy", action="store_true",
+                    help="skip the 200k-sample energy + gradient record")
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.impl == "reference":

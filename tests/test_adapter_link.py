@@ -18,7 +18,7 @@ def test_reference_drivers_link_through_adapter():
     from quijibo_gb300 import build
     build.build()
     adir = os.path.join(ROOT, "quijibo_gb300", "adapter")
-    subprocess.run(["make", "-s", "-j8", "-C", adir, "REF=" + REF], check=True)
+    subprocess.run(["make", "-s", "-j8", "-C", adir, "all", "REF=" + REF], check=True)
     for exe in ("bunnyMarchingCubes3D_gpu", "toothOptimizer_gpu", "lagrangeBunny3D_gpu"):
         path = os.path.join(adir, "_build", exe)
         assert os.path.exists(path)
