@@ -48,10 +48,11 @@ int qjg_set_energy_pairs(int on);
 int qjg_set_energy_adjoint_roots(int on);
 
 /* Process-wide form of the FP32 energy's arithmetic: 1 (the default) the
- * fast form (hardware approximations of log2, of sin/cos and of the
- * reciprocal for every division, a polynomial atan: about 1e-6 relative per
- * power), 0 the accurate device library functions and IEEE divisions.  Set
- * it while no energy call is in flight. */
+ * fast form (the PTX approximations of log2, exp2, sin/cos, the reciprocal
+ * for every division and the reciprocal square root, denormals flushed, and
+ * a polynomial atan: about 1e-6 relative per power), 0 the accurate device
+ * library functions and IEEE divisions.  Set it while no energy call is in
+ * flight. */
 int qjg_set_energy_fast(int on);
 
 /* Work of the last qjg_energy_forward/backward call on ctx: the map

@@ -771,13 +771,66 @@ struct PowParts {
 
 // The FP32 polar power's fast form (the default; qjg_set_energy_fast(0)
 // selects the accurate device functions): the angle from a polynomial atan
-// and the hardware approximations of log2, of sin/cos and of the reciprocal
-// (divisions and the square root of |d|^2).  On the differentiation
-// workload (200k samples, 64/16 roots, 30 iterations) it moves the FP32
-// energy from 3e-9 to 8e-8 of the FP64 form's and the FP32 gradient from
-// 2e-7 to 9e-7, for a forward kernel 1.715 -> 1.162 ms and an adjoint
-// kernel 0.45 -> 0.35 ms.
+// and the PTX approximations of log2, exp2, sin/cos, the reciprocal (every
+// division) and the reciprocal square root, with denormals flushed.  On the
+// differentiation workload (200k samples, 64/16 roots, 30 iterations) it
+// moves the FP32 energy from 3e-9 to 8e-8 of the FP64 form's; the FP32
+// gradient stays within 1e-5 of the FP64 form's (about 1e-6 measured).
 __constant__ int c_sq_fast = 1;
+
+// How a device function picks the FP32 form: SQM_RT reads the switch
+// (c_sq_fast) where it is used; SQM_FAST and SQM_ACC fix the form at compile
+// time, so that a kernel instantiated for one form runs its root loop as
+// straight-line code (the forward kernel tests the switch once, at entry).
+// The FP64 form ignores the mode.
+constexpr int SQM_RT = 0, SQM_FAST = 1, SQM_ACC = 2;
+
+template <int M>
+__device__ __forceinline__ bool sq_fast() {
+  if constexpr (M == SQM_FAST) return true;
+  if constexpr (M == SQM_ACC) return false;
+  return c_sq_fast != 0;
+}
+
+// The fast form's transcendentals: the PTX approximations with denormal
+// inputs and results flushed to zero, one special-function instruction each
+// (the device library's __log2f, rsqrtf and exp2f add a denormal range fix-up
+// around the same approximation).  Accuracy as documented for the PTX
+// instructions: ex2 and lg2 about 2^-22 relative / absolute, rsqrt and rcp
+// about 1 ulp, sin and cos 2^-20.5 absolute for arguments within [-pi, pi]
+// (|e theta| stays within a few pi here).
+__device__ __forceinline__ float lg2_ftz(float x) {
+  float y;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float ex2_ftz(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float rcp_ftz(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float sin_ftz(float x) {
+  float y;
+  asm("sin.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float cos_ftz(float x) {
+  float y;
+  asm("cos.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+// smallest normal FP32 value: below it the flushed approximations read 0
+constexpr float SQ_FLT_MIN = 1.17549435e-38f;
 
 // atan(t) for 0 <= t <= 1 as t P(t^2), P of degree 7 fitted for this
 // library (weighted least squares on Chebyshev nodes of t^2 in [0, 1]; max
@@ -799,46 +852,53 @@ __device__ __forceinline__ float atan01_fast(float t) {
 __device__ __forceinline__ float atan2_pos_fast(float y, float x) {
   const float ax = fabsf(x);
   const float mx = fmaxf(ax, y), mn = fminf(ax, y);
-  float a = mx > 0.f ? atan01_fast(__fdividef(mn, mx)) : 0.f;
+  float a = mx > SQ_FLT_MIN ? atan01_fast(mn * rcp_ftz(mx)) : 0.f;
   if (y > ax) a = 1.57079632679489662f - a;
   return x < 0.f ? 3.14159265358979324f - a : a;
 }
 
 // a / b: FP64 and the accurate FP32 form divide (IEEE); the fast FP32 form
-// takes the hardware reciprocal (__fdividef, 2 ulp), whose IEEE division
-// sequence was a tenth of the adjoint's instructions.
-template <class T>
+// multiplies by the hardware reciprocal, whose IEEE division sequence was a
+// tenth of the adjoint's instructions.
+template <class T, int M = SQM_RT>
 __device__ __forceinline__ T sq_div(T a, T b) {
   if constexpr (std::is_same<T, float>::value) {
-    if (c_sq_fast) return __fdividef(a, b);
+    if (sq_fast<M>()) return a * rcp_ftz(b);
   }
   return a / b;
 }
 
-template <class T>
-__device__ __forceinline__ V4<T> powv(const V4<T>& d, T e, PowParts<T>* pp) {
+// The polar power d^e (the form of QUATERNION::pow).  The fast FP32 form
+// also returns |d|^2 through r2out (the log-gradient term divides by it).
+template <class T, int M = SQM_RT>
+__device__ __forceinline__ V4<T> powv(const V4<T>& d, T e, PowParts<T>* pp,
+                                      T* r2out = nullptr) {
   if constexpr (std::is_same<T, float>::value) {
     // FP32: the same polar form through base-2 logarithm and exponential,
-    // the angle as atan2(|v|, w) and its multiple in half-turns (sincospif),
-    // and 1/|v| as one reciprocal square root
+    // the angle as atan2(|v|, w), and 1/|v| as one reciprocal square root
     const float v2 = d.x * d.x + d.y * d.y + d.z * d.z;
     const float r2 = v2 + d.w * d.w;
-    const float rv = v2 > 0.f ? rsqrtf(v2) : 0.f;
-    const float vm = v2 * rv;
-    float theta, A, s, c;
-    if (c_sq_fast) {
-      theta = atan2_pos_fast(vm, d.w);
-      A = exp2f(0.5f * e * __log2f(r2));
-      __sincosf(e * theta, &s, &c);
+    if (r2out) *r2out = r2;
+    float theta, A, s, c, rv;
+    if (sq_fast<M>()) {
+      rv = v2 > SQ_FLT_MIN ? rsqrt_ftz(v2) : 0.f;
+      theta = atan2_pos_fast(v2 * rv, d.w);
+      A = ex2_ftz(0.5f * e * lg2_ftz(r2));
+      const float ang = e * theta;
+      s = sin_ftz(ang);
+      c = cos_ftz(ang);
     } else {
-      theta = atan2f(vm, d.w);
+      rv = v2 > 0.f ? rsqrtf(v2) : 0.f;
+      theta = atan2f(v2 * rv, d.w);
       A = exp2f(0.5f * e * log2f(r2));
       sincospif(e * theta * 0.318309886183790672f, &s, &c);
     }
+    const float vm = v2 * rv;
     const float k = A * s * rv;
     if (pp) {
       // rho = sqrt(r2), as r2 rsqrt(r2) in the fast form
-      const float rho = c_sq_fast ? (r2 > 0.f ? r2 * rsqrtf(r2) : 0.f) : sqrtf(r2);
+      const float rho =
+          sq_fast<M>() ? (r2 > SQ_FLT_MIN ? r2 * rsqrt_ftz(r2) : 0.f) : sqrtf(r2);
       *pp = PowParts<T>{rho, vm, theta, A, c, s};
     }
     return V4<T>{A * c, k * d.x, k * d.y, k * d.z};
@@ -855,19 +915,26 @@ __device__ __forceinline__ V4<T> powv(const V4<T>& d, T e, PowParts<T>* pp) {
 }
 
 // given Pbar, accumulate dbar (returned) and ebar
-template <class T>
+template <class T, int M = SQM_RT>
 __device__ __forceinline__ V4<T> powv_vjp(const V4<T>& d, T e, const PowParts<T>& p,
                                           const V4<T>& Pb, T* ebar) {
   // 1/|v| and 1/rho once (FP64: IEEE divisions)
-  const T ivm = p.vm > T(0) ? sq_div(T(1), p.vm) : T(0);
-  const T irho = sq_div(T(1), p.rho);
+  const T ivm = p.vm > T(0) ? sq_div<T, M>(T(1), p.vm) : T(0);
+  const T irho = sq_div<T, M>(T(1), p.rho);
   const T ux = d.x * ivm, uy = d.y * ivm, uz = d.z * ivm;
   const T pu = Pb.x * ux + Pb.y * uy + Pb.z * uz;
   const T Ab = Pb.w * p.c + pu * p.s;
   const T phib = p.A * (pu * p.c - Pb.w * p.s);
   const T rhob = Ab * e * p.A * irho;
   const T thetab = phib * e;
-  *ebar += Ab * p.A * log(p.rho) + phib * p.theta;
+  T lrho;
+  if constexpr (std::is_same<T, float>::value) {
+    // log(rho) = ln 2 log2(rho): the fast form's approximation
+    lrho = sq_fast<M>() ? 0.693147180559945309f * lg2_ftz(p.rho) : logf(p.rho);
+  } else {
+    lrho = log(p.rho);
+  }
+  *ebar += Ab * p.A * lrho + phib * p.theta;
   const T ir2 = irho * irho;
   V4<T> db;
   db.w = rhob * d.w * irho - thetab * p.vm * ir2;
@@ -889,8 +956,9 @@ __device__ __forceinline__ V4<T> powv_vjp(const V4<T>& d, T e, const PowParts<T>
 }
 
 // One map application q -> Q with log|g|; fills prefix products F (per
-// side) and factors P when `keep` is set.
-template <class T>
+// side) and factors P when given.  The first root of each side starts the
+// side's running product (no multiply by one, no select in the loop).
+template <class T, int M = SQM_RT>
 __device__ __forceinline__ V4<T> sq_apply(const T* __restrict__ rp, const T* __restrict__ ep,
                                           int nt, int nb, T s, const V4<T>& q, T* lg,
                                           V4<T>* F, V4<T>* Pf, V4<T>* Tout, V4<T>* Bout) {
@@ -898,25 +966,43 @@ __device__ __forceinline__ V4<T> sq_apply(const T* __restrict__ rp, const T* __r
   // running products stay in registers)
   V4<T> acc[2] = {{T(1), T(0), T(0), T(0)}, {T(1), T(0), T(0), T(0)}};
   V4<T> g = {T(0), T(0), T(0), T(0)};
+  // root i's factor; its log-gradient term sgn e d / |d|^2 added to g
+  auto term = [&](int i, bool bottom) -> V4<T> {
+    const V4<T> d{q.w - rp[4 * i], q.x - rp[4 * i + 1], q.y - rp[4 * i + 2], q.z - rp[4 * i + 3]};
+    const T e = ep[i];
+    const T se = bottom ? -e : e;
+    V4<T> P;
+    T k;
+    bool fast = false;
+    if constexpr (std::is_same<T, float>::value) fast = sq_fast<M>();
+    if (fast) {
+      // |d|^2 from the polar power's own sum
+      T r2;
+      P = powv<T, M>(d, e, nullptr, &r2);
+      k = sq_div<T, M>(se, r2);
+    } else {
+      k = sq_div<T, M>(se, v4dot(d, d));
+      P = powv<T, M>(d, e, nullptr);
+    }
+    g = v4add(g, v4scale(d, k));
+    if (Pf) Pf[i] = P;
+    return P;
+  };
 #pragma unroll
   for (int side = 0; side < 2; side++) {
     const int lo = side ? nt : 0, hi = side ? nt + nb : nt;
-    V4<T> a = acc[side];
-    for (int i = lo; i < hi; i++) {
-      const V4<T> d{q.w - rp[4 * i], q.x - rp[4 * i + 1], q.y - rp[4 * i + 2], q.z - rp[4 * i + 3]};
-      const T e = ep[i];
-      const T k = sq_div(side ? -e : e, v4dot(d, d));
-      g = v4add(g, v4scale(d, k));
-      const V4<T> P = powv<T>(d, e, nullptr);
-      a = i == lo ? P : v4mul(a, P);
+    if (lo == hi) continue;
+    V4<T> a = term(lo, side != 0);
+    if (F) F[lo] = a;
+    for (int i = lo + 1; i < hi; i++) {
+      a = v4mul(a, term(i, side != 0));
       if (F) F[i] = a;
-      if (Pf) Pf[i] = P;
     }
     acc[side] = a;
   }
   V4<T> Q;
   if (nb > 0) {
-    const V4<T> W = v4scale(v4conj(acc[1]), sq_div(T(1), v4dot(acc[1], acc[1])));
+    const V4<T> W = v4scale(v4conj(acc[1]), sq_div<T, M>(T(1), v4dot(acc[1], acc[1])));
     Q = v4scale(v4mul(acc[0], W), s);
   } else {
     Q = v4scale(acc[0], s);
@@ -974,11 +1060,11 @@ struct SqFwdOut {
 // orbit ends, so a warp's lanes stay busy however the orbit lengths differ.
 // The per-sample results go to SqFwdOut; the sums are formed afterwards in
 // sample order, so they do not depend on which lane took which sample.
-template <class T, bool GRAD>
-__global__ void __launch_bounds__(SQF_T) sq_fwd_kernel(
+template <class T, bool GRAD, int M>
+__device__ __forceinline__ void sq_fwd_body(
     const double* __restrict__ params, int nt, int nb, const double* __restrict__ xyz,
     const double* __restrict__ target, long long n_samples, double slice, int max_it,
-    double escape, double d_sat, unsigned long long* __restrict__ claim, SqFwdOut<T> o) {
+    double escape, double d_sat, unsigned long long* __restrict__ claim, const SqFwdOut<T>& o) {
   extern __shared__ unsigned char sh_raw[];
   const int nr = nt + nb;
   T* rp = reinterpret_cast<T*>(sh_raw);  // 4 nr
@@ -1054,7 +1140,7 @@ __global__ void __launch_bounds__(SQF_T) sq_fwd_kernel(
     if (live) {
       if (GRAD && n % SQ_CK == 0) o.ck[(long long)(n / SQ_CK) * n_samples + k] = q;
       T lg;
-      q = sq_apply<T>(rp, ep, nt, nb, s, q, &lg, nullptr, nullptr, nullptr, nullptr);
+      q = sq_apply<T, M>(rp, ep, nt, nb, s, q, &lg, nullptr, nullptr, nullptr, nullptr);
       L += lg + T(0.5) * log(v4dot(q, q));
       n++;
       // 10 * FLT_MIN exit of the field loop
@@ -1065,6 +1151,24 @@ __global__ void __launch_bounds__(SQF_T) sq_fwd_kernel(
       }
     }
   }
+}
+
+// The FP32 form is chosen once per launch, so that each form's root loop is
+// compiled as straight-line code.
+template <class T, bool GRAD>
+__global__ void __launch_bounds__(SQF_T) sq_fwd_kernel(
+    const double* __restrict__ params, int nt, int nb, const double* __restrict__ xyz,
+    const double* __restrict__ target, long long n_samples, double slice, int max_it,
+    double escape, double d_sat, unsigned long long* __restrict__ claim, SqFwdOut<T> o) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (c_sq_fast) {
+      sq_fwd_body<T, GRAD, SQM_FAST>(params, nt, nb, xyz, target, n_samples, slice, max_it,
+                                     escape, d_sat, claim, o);
+      return;
+    }
+  }
+  sq_fwd_body<T, GRAD, SQM_ACC>(params, nt, nb, xyz, target, n_samples, slice, max_it, escape,
+                                d_sat, claim, o);
 }
 
 // Two map applications that share the walk over the roots: the same
@@ -1544,7 +1648,7 @@ __device__ __forceinline__ void side_init(SideRun<T, C>& r, int lo, int ns, int 
 
 // The side's factors at q, the scans over the group's lanes; the side's
 // log-gradient terms added to gp.
-template <class T, int G, int C>
+template <class T, int G, int C, int M>
 __device__ __forceinline__ void side_fwd(const T* __restrict__ rp, const T* __restrict__ ep,
                                          T sgn, int gl, const V4<T>& q, SideRun<T, C>& r,
                                          V4<T>& gp) {
@@ -1556,10 +1660,14 @@ __device__ __forceinline__ void side_fwd(const T* __restrict__ rp, const T* __re
       const int i = r.a + j;
       const V4<T> d{q.w - rp[4 * i], q.x - rp[4 * i + 1], q.y - rp[4 * i + 2],
                     q.z - rp[4 * i + 3]};
-      const V4<T> P = powv<T>(d, ep[i], nullptr);
+      T r2 = T(0);
+      const V4<T> P = powv<T, M>(d, ep[i], nullptr, &r2);
       r.P[j] = P;
       Cp = j ? v4mul(Cp, P) : P;
-      gp = v4add(gp, v4scale(d, sq_div(sgn * ep[i], v4dot(d, d))));
+      bool fast = false;
+      if constexpr (std::is_same<T, float>::value) fast = sq_fast<M>();
+      // the fast form divides by the polar power's own |d|^2
+      gp = v4add(gp, v4scale(d, sq_div<T, M>(sgn * ep[i], fast ? r2 : v4dot(d, d))));
     }
   }
   // inclusive prefix over the group's lanes: x_l = C_0 C_1 ... C_l
@@ -1586,7 +1694,7 @@ __device__ __forceinline__ void side_fwd(const T* __restrict__ rp, const T* __re
 // The side's adjoint at qn given Ubar (the adjoint of its full product) and
 // gbar (of the log-gradient vector): each root's terms added to the run's
 // sums when `on`, and to qbp (this lane's share of qbar).
-template <class T, int C>
+template <class T, int C, int M>
 __device__ __forceinline__ void side_adj(const T* __restrict__ rp, const T* __restrict__ ep,
                                          T sgn, const V4<T>& qn, SideRun<T, C>& r,
                                          const V4<T>& Ub, const V4<T>& gb, bool on, V4<T>& qbp) {
@@ -1605,15 +1713,18 @@ __device__ __forceinline__ void side_adj(const T* __restrict__ rp, const T* __re
       const V4<T> d{qn.w - rp[4 * i], qn.x - rp[4 * i + 1], qn.y - rp[4 * i + 2],
                     qn.z - rp[4 * i + 3]};
       PowParts<T> pp;
-      powv<T>(d, ep[i], &pp);
+      T r2 = T(0);
+      powv<T, M>(d, ep[i], &pp, &r2);
       const V4<T> Pb = v4mul(v4conj(Fa[j]), V);
       V = v4mul(V, v4conj(r.P[j]));
       T eb = T(0);
-      V4<T> dbar = powv_vjp<T>(d, ep[i], pp, Pb, &eb);
+      V4<T> dbar = powv_vjp<T, M>(d, ep[i], pp, Pb, &eb);
       // g term: sgn e d/|d|^2
-      const T d2 = v4dot(d, d);
+      bool fast = false;
+      if constexpr (std::is_same<T, float>::value) fast = sq_fast<M>();
+      const T d2 = fast ? r2 : v4dot(d, d);
       const T dg = v4dot(d, gb);
-      const T id2 = sq_div(T(1), d2);
+      const T id2 = sq_div<T, M>(T(1), d2);
       dbar = v4add(dbar, v4scale(v4add(v4scale(gb, id2), v4scale(d, T(-2) * dg * id2 * id2)),
                                  sgn * ep[i]));
       eb += sgn * dg * id2;
@@ -1648,8 +1759,8 @@ __device__ __forceinline__ void side_flush(SideRun<T, C>& r, double* acc, int nr
 static_assert(SQ_CK == 1, "sq_bwd_roots_kernel reads the forward pass's q at every step");
 constexpr int SQ_FLUSH = 16;  // samples a lane sums in FP32 before adding to the double sums
 
-template <class T, int G, int CT, int CB, int MINB>
-__global__ void __launch_bounds__(SQ_T, MINB) sq_bwd_roots_kernel(
+template <class T, int G, int CT, int CB, int M>
+__device__ __forceinline__ void sq_bwd_roots_body(
     const double* __restrict__ params, int nt, int nb, long long n_samples,
     const unsigned* __restrict__ perm, const int* __restrict__ total,
     const int* __restrict__ keys, const V4<T>* __restrict__ seed_q,
@@ -1694,30 +1805,30 @@ __global__ void __launch_bounds__(SQ_T, MINB) sq_bwd_roots_kernel(
       // the forward pass's own q_n (SQ_CK = 1)
       const V4<T> qn = on ? ck[(long long)n * n_samples + k] : zero;
       V4<T> gp = zero;
-      side_fwd<T, G, CT>(rp, ep, T(1), gl, qn, top, gp);
-      side_fwd<T, G, CB>(rp, ep, T(-1), gl, qn, bot, gp);
+      side_fwd<T, G, CT, M>(rp, ep, T(1), gl, qn, top, gp);
+      side_fwd<T, G, CB, M>(rp, ep, T(-1), gl, qn, bot, gp);
       const V4<T> g = group_sum4<T, G>(gp);
       V4<T> Q, Tb, Bb;
       if (nb > 0) {
-        const V4<T> W4 = v4scale(v4conj(bot.tot), sq_div(T(1), v4dot(bot.tot, bot.tot)));
+        const V4<T> W4 = v4scale(v4conj(bot.tot), sq_div<T, M>(T(1), v4dot(bot.tot, bot.tot)));
         Q = v4scale(v4mul(top.tot, W4), s);
         // L_{n+1} = L_n + log|g| + log|Q|
-        const V4<T> Qb = v4add(qb, v4scale(Q, sq_div(Lb, v4dot(Q, Q))));
+        const V4<T> Qb = v4add(qb, v4scale(Q, sq_div<T, M>(Lb, v4dot(Q, Q))));
         if (on) dls += v4dot(Qb, Q);
         Tb = v4scale(v4mul(Qb, v4conj(W4)), s);
         const V4<T> Wb = v4scale(v4mul(v4conj(top.tot), Qb), s);
         Bb = v4scale(v4mul(v4mul(v4conj(W4), Wb), v4conj(W4)), T(-1));
       } else {
         Q = v4scale(top.tot, s);
-        const V4<T> Qb = v4add(qb, v4scale(Q, sq_div(Lb, v4dot(Q, Q))));
+        const V4<T> Qb = v4add(qb, v4scale(Q, sq_div<T, M>(Lb, v4dot(Q, Q))));
         if (on) dls += v4dot(Qb, Q);
         Tb = v4scale(Qb, s);
         Bb = zero;
       }
-      const V4<T> gb = v4scale(g, sq_div(Lb, v4dot(g, g)));
+      const V4<T> gb = v4scale(g, sq_div<T, M>(Lb, v4dot(g, g)));
       V4<T> qbp = zero;
-      side_adj<T, CT>(rp, ep, T(1), qn, top, Tb, gb, on, qbp);
-      side_adj<T, CB>(rp, ep, T(-1), qn, bot, Bb, gb, on, qbp);
+      side_adj<T, CT, M>(rp, ep, T(1), qn, top, Tb, gb, on, qbp);
+      side_adj<T, CB, M>(rp, ep, T(-1), qn, bot, Bb, gb, on, qbp);
       qbp = group_sum4<T, G>(qbp);
       if (on) qb = qbp;
     }
@@ -1743,6 +1854,22 @@ __global__ void __launch_bounds__(SQ_T, MINB) sq_bwd_roots_kernel(
     for (int w = 0; w < NG; w++) v += acc_sh[w * slots + k];
     partials[(long long)blockIdx.x * slots + k] = v;
   }
+}
+
+// The FP32 form is chosen once per launch (straight-line root loops).
+template <class T, int G, int CT, int CB, int MINB>
+__global__ void __launch_bounds__(SQ_T, MINB) sq_bwd_roots_kernel(
+    const double* __restrict__ params, int nt, int nb, long long n_samples,
+    const unsigned* __restrict__ perm, const int* __restrict__ total,
+    const int* __restrict__ keys, const V4<T>* __restrict__ seed_q,
+    const T* __restrict__ seed_L, const V4<T>* __restrict__ ck, double* __restrict__ partials,
+    int slots) {
+  if (c_sq_fast)
+    sq_bwd_roots_body<T, G, CT, CB, SQM_FAST>(params, nt, nb, n_samples, perm, total, keys,
+                                              seed_q, seed_L, ck, partials, slots);
+  else
+    sq_bwd_roots_body<T, G, CT, CB, SQM_ACC>(params, nt, nb, n_samples, perm, total, keys,
+                                             seed_q, seed_L, ck, partials, slots);
 }
 
 // Compensated sum of partials[b][k] over rows b, one block of SQR_W warps
