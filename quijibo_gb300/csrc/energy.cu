@@ -1174,7 +1174,7 @@ __global__ void __launch_bounds__(SQF_T) sq_fwd_kernel(
 // Two map applications that share the walk over the roots: the same
 // arithmetic as sq_apply for each of qa and qb, so each keeps its bits, with
 // the root constants read once and two independent dependency chains.
-template <class T>
+template <class T, int M = SQM_RT>
 __device__ __forceinline__ void sq_apply2(const T* __restrict__ rp, const T* __restrict__ ep,
                                           int nt, int nb, T s, V4<T>& qa, T* lga, V4<T>& qb,
                                           T* lgb) {
@@ -1190,12 +1190,12 @@ __device__ __forceinline__ void sq_apply2(const T* __restrict__ rp, const T* __r
       const T e = ep[i];
       const V4<T> da{qa.w - r0, qa.x - r1, qa.y - r2, qa.z - r3};
       const V4<T> db{qb.w - r0, qb.x - r1, qb.y - r2, qb.z - r3};
-      const T ka = sq_div(side ? -e : e, v4dot(da, da));
-      const T kb = sq_div(side ? -e : e, v4dot(db, db));
+      const T ka = sq_div<T, M>(side ? -e : e, v4dot(da, da));
+      const T kb = sq_div<T, M>(side ? -e : e, v4dot(db, db));
       ga = v4add(ga, v4scale(da, ka));
       gb = v4add(gb, v4scale(db, kb));
-      const V4<T> Pa = powv<T>(da, e, nullptr);
-      const V4<T> Pb = powv<T>(db, e, nullptr);
+      const V4<T> Pa = powv<T, M>(da, e, nullptr);
+      const V4<T> Pb = powv<T, M>(db, e, nullptr);
       a = i == lo ? Pa : v4mul(a, Pa);
       b = i == lo ? Pb : v4mul(b, Pb);
     }
@@ -1203,8 +1203,8 @@ __device__ __forceinline__ void sq_apply2(const T* __restrict__ rp, const T* __r
     acc[1][side] = b;
   }
   if (nb > 0) {
-    const V4<T> Wa = v4scale(v4conj(acc[0][1]), sq_div(T(1), v4dot(acc[0][1], acc[0][1])));
-    const V4<T> Wb = v4scale(v4conj(acc[1][1]), sq_div(T(1), v4dot(acc[1][1], acc[1][1])));
+    const V4<T> Wa = v4scale(v4conj(acc[0][1]), sq_div<T, M>(T(1), v4dot(acc[0][1], acc[0][1])));
+    const V4<T> Wb = v4scale(v4conj(acc[1][1]), sq_div<T, M>(T(1), v4dot(acc[1][1], acc[1][1])));
     qa = v4scale(v4mul(acc[0][0], Wa), s);
     qb = v4scale(v4mul(acc[1][0], Wb), s);
   } else {
@@ -1218,8 +1218,8 @@ __device__ __forceinline__ void sq_apply2(const T* __restrict__ rp, const T* __r
 // The forward pass with two samples per lane (slots 0 and 1), each refilled
 // as in sq_fwd_kernel; both slots step through one sq_apply2.  A slot without
 // a sample steps a dummy point whose results are not used.
-template <class T, bool GRAD>
-__global__ void __launch_bounds__(SQF_T) sq_fwd2_kernel(
+template <class T, bool GRAD, int M>
+__device__ __forceinline__ void sq_fwd2_body(
     const double* __restrict__ params, int nt, int nb, const double* __restrict__ xyz,
     const double* __restrict__ target, long long n_samples, double slice, int max_it,
     double escape, double d_sat, unsigned long long* __restrict__ claim, SqFwdOut<T> o) {
@@ -1298,7 +1298,7 @@ __global__ void __launch_bounds__(SQF_T) sq_fwd2_kernel(
     V4<T> qa = live[0] ? q[0] : V4<T>{T(0.5), T(0.5), T(0.5), T(0.5)};
     V4<T> qb = live[1] ? q[1] : V4<T>{T(0.5), T(0.5), T(0.5), T(0.5)};
     T lga, lgb;
-    sq_apply2<T>(rp, ep, nt, nb, s, qa, &lga, qb, &lgb);
+    sq_apply2<T, M>(rp, ep, nt, nb, s, qa, &lga, qb, &lgb);
 #pragma unroll
     for (int sl = 0; sl < 2; sl++) {
       if (!live[sl]) continue;
@@ -1313,6 +1313,23 @@ __global__ void __launch_bounds__(SQF_T) sq_fwd2_kernel(
       }
     }
   }
+}
+
+// The FP32 form is chosen once per launch (straight-line root loops).
+template <class T, bool GRAD>
+__global__ void __launch_bounds__(SQF_T) sq_fwd2_kernel(
+    const double* __restrict__ params, int nt, int nb, const double* __restrict__ xyz,
+    const double* __restrict__ target, long long n_samples, double slice, int max_it,
+    double escape, double d_sat, unsigned long long* __restrict__ claim, SqFwdOut<T> o) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (c_sq_fast) {
+      sq_fwd2_body<T, GRAD, SQM_FAST>(params, nt, nb, xyz, target, n_samples, slice, max_it,
+                                      escape, d_sat, claim, o);
+      return;
+    }
+  }
+  sq_fwd2_body<T, GRAD, SQM_ACC>(params, nt, nb, xyz, target, n_samples, slice, max_it, escape,
+                                 d_sat, claim, o);
 }
 
 // Per chunk of SQ_CH samples: the energy and the left-out count summed in a
@@ -1439,8 +1456,8 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
-template <class T>
-__global__ void __launch_bounds__(SQ_T) sq_bwd_kernel(
+template <class T, int M>
+__device__ __forceinline__ void sq_bwd_body(
     const double* __restrict__ params, int nt, int nb, long long n_samples,
     const unsigned* __restrict__ perm, const int* __restrict__ total,
     const int* __restrict__ keys, const V4<T>* __restrict__ seed_q,
@@ -1483,7 +1500,7 @@ __global__ void __launch_bounds__(SQ_T) sq_bwd_kernel(
         seg[n - n0] = q;
         T lg;
         if (n + 1 < n1)
-          q = sq_apply<T>(rp, ep, nt, nb, s, q, &lg, nullptr, nullptr, nullptr, nullptr);
+          q = sq_apply<T, M>(rp, ep, nt, nb, s, q, &lg, nullptr, nullptr, nullptr, nullptr);
       }
       for (int n = n1max - 1; n >= n0; n--) {
         const bool on = n < n1;  // this lane's orbit has step n
@@ -1493,13 +1510,13 @@ __global__ void __launch_bounds__(SQ_T) sq_bwd_kernel(
           qn = seg[n - n0];
           T lg;
           V4<T> Tq, Bq;
-          const V4<T> Q = sq_apply<T>(rp, ep, nt, nb, s, qn, &lg, F, nullptr, &Tq, &Bq);
+          const V4<T> Q = sq_apply<T, M>(rp, ep, nt, nb, s, qn, &lg, F, nullptr, &Tq, &Bq);
           // L_{n+1} = L_n + log|g| + log|Q|
-          const V4<T> Qb = v4add(qb, v4scale(Q, sq_div(Lb, v4dot(Q, Q))));
+          const V4<T> Qb = v4add(qb, v4scale(Q, sq_div<T, M>(Lb, v4dot(Q, Q))));
           // d/d log s: <Qbar, Q>
           dls = v4dot(Qb, Q);
           if (nb > 0) {
-            const V4<T> W4 = v4scale(v4conj(Bq), sq_div(T(1), v4dot(Bq, Bq)));
+            const V4<T> W4 = v4scale(v4conj(Bq), sq_div<T, M>(T(1), v4dot(Bq, Bq)));
             Tb = v4scale(v4mul(Qb, v4conj(W4)), s);
             const V4<T> Wb = v4scale(v4mul(v4conj(Tq), Qb), s);
             Bb = v4scale(v4mul(v4mul(v4conj(W4), Wb), v4conj(W4)), T(-1));
@@ -1511,9 +1528,9 @@ __global__ void __launch_bounds__(SQ_T) sq_bwd_kernel(
           for (int i = 0; i < nr; i++) {
             const V4<T> d{qn.w - rp[4 * i], qn.x - rp[4 * i + 1], qn.y - rp[4 * i + 2],
                           qn.z - rp[4 * i + 3]};
-            g = v4add(g, v4scale(d, sq_div(i >= nt ? -ep[i] : ep[i], v4dot(d, d))));
+            g = v4add(g, v4scale(d, sq_div<T, M>(i >= nt ? -ep[i] : ep[i], v4dot(d, d))));
           }
-          gb = v4scale(g, sq_div(Lb, v4dot(g, g)));
+          gb = v4scale(g, sq_div<T, M>(Lb, v4dot(g, g)));
         }
         dls = warp_sum(dls);
         if (lane == 0) acc[1 + 5 * nr] += (double)dls;
@@ -1529,16 +1546,16 @@ __global__ void __launch_bounds__(SQ_T) sq_bwd_kernel(
               const V4<T> d{qn.w - rp[4 * i], qn.x - rp[4 * i + 1], qn.y - rp[4 * i + 2],
                             qn.z - rp[4 * i + 3]};
               PowParts<T> pp;
-              const V4<T> P = powv<T>(d, ep[i], &pp);
+              const V4<T> P = powv<T, M>(d, ep[i], &pp);
               const V4<T> Pb = (i == lo) ? U : v4mul(v4conj(F[i - 1]), U);
               U = v4mul(U, v4conj(P));
               T eb = T(0);
-              V4<T> dbar = powv_vjp<T>(d, ep[i], pp, Pb, &eb);
+              V4<T> dbar = powv_vjp<T, M>(d, ep[i], pp, Pb, &eb);
               // g term: sgn e d/|d|^2
               const T sgn = side ? T(-1) : T(1);
               const T d2 = v4dot(d, d);
               const T dg = v4dot(d, gb);
-              const T id2 = sq_div(T(1), d2);
+              const T id2 = sq_div<T, M>(T(1), d2);
               dbar = v4add(dbar, v4scale(v4add(v4scale(gb, id2), v4scale(d, T(-2) * dg * id2 * id2)),
                                          sgn * ep[i]));
               eb += sgn * dg * id2;
@@ -1571,6 +1588,25 @@ __global__ void __launch_bounds__(SQ_T) sq_bwd_kernel(
     for (int w = 0; w < SQ_T / 32; w++) v += acc_sh[w * slots + k];
     partials[(long long)blockIdx.x * slots + k] = v;
   }
+}
+
+// The FP32 form is chosen once per launch (straight-line root loops).
+template <class T>
+__global__ void __launch_bounds__(SQ_T) sq_bwd_kernel(
+    const double* __restrict__ params, int nt, int nb, long long n_samples,
+    const unsigned* __restrict__ perm, const int* __restrict__ total,
+    const int* __restrict__ keys, const V4<T>* __restrict__ seed_q,
+    const T* __restrict__ seed_L, const V4<T>* __restrict__ ck, double* __restrict__ partials,
+    int slots) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (c_sq_fast) {
+      sq_bwd_body<T, SQM_FAST>(params, nt, nb, n_samples, perm, total, keys, seed_q, seed_L, ck,
+                               partials, slots);
+      return;
+    }
+  }
+  sq_bwd_body<T, SQM_ACC>(params, nt, nb, n_samples, perm, total, keys, seed_q, seed_L, ck,
+                          partials, slots);
 }
 
 // ---- the backward pass with the roots spread over lanes ----
@@ -1953,7 +1989,8 @@ __global__ void sq_item_roots_kernel(const SqItem* __restrict__ items, int K) {
   (void)K;
 }
 
-__global__ void __launch_bounds__(SQF_T) sq_fwd_batch_kernel(
+template <int M>
+__device__ __forceinline__ void sq_fwd_batch_body(
     const SqItem* __restrict__ items, const int* __restrict__ chunk_item, long long n_flat,
     unsigned long long* __restrict__ claim, SqFwdOut<float> o) {
   using T = float;
@@ -2024,7 +2061,7 @@ __global__ void __launch_bounds__(SQF_T) sq_fwd_batch_kernel(
       const int nr = it->nt + it->nb;
       const T s = (T)exp(it->params[5 * nr]);
       T lg;
-      q = sq_apply<T>(it->rp, it->rp + 4 * nr, it->nt, it->nb, s, q, &lg, nullptr, nullptr,
+      q = sq_apply<T, M>(it->rp, it->rp + 4 * nr, it->nt, it->nb, s, q, &lg, nullptr, nullptr,
                       nullptr, nullptr);
       L += lg + T(0.5) * log(v4dot(q, q));
       n++;
@@ -2037,12 +2074,23 @@ __global__ void __launch_bounds__(SQF_T) sq_fwd_batch_kernel(
   }
 }
 
+// The FP32 form is chosen once per launch (straight-line root loops).
+__global__ void __launch_bounds__(SQF_T) sq_fwd_batch_kernel(
+    const SqItem* __restrict__ items, const int* __restrict__ chunk_item, long long n_flat,
+    unsigned long long* __restrict__ claim, SqFwdOut<float> o) {
+  if (c_sq_fast)
+    sq_fwd_batch_body<SQM_FAST>(items, chunk_item, n_flat, claim, o);
+  else
+    sq_fwd_batch_body<SQM_ACC>(items, chunk_item, n_flat, claim, o);
+}
+
 // The adjoint of a batch: warp w takes groups w, w + W, ... of item 0, then
 // of item 1, and so on (the items' sorted gradient samples in groups of 32);
 // per group it sums the root terms' gradient components over the warp into
 // shared double accumulators as sq_bwd_kernel does and writes them as the
 // group's partial row.
-__global__ void __launch_bounds__(SQ_T) sq_bwd_batch_kernel(
+template <int M>
+__device__ __forceinline__ void sq_bwd_batch_body(
     const SqItem* __restrict__ items, int K, long long n_flat, const int* __restrict__ keys,
     const V4<float>* __restrict__ seed_q, const float* __restrict__ seed_L,
     const V4<float>* __restrict__ ck, int max_slots) {
@@ -2080,7 +2128,7 @@ __global__ void __launch_bounds__(SQ_T) sq_bwd_batch_kernel(
           seg[n - n0] = q;
           T lg;
           if (n + 1 < n1)
-            q = sq_apply<T>(rp, ep, nt, nb, s, q, &lg, nullptr, nullptr, nullptr, nullptr);
+            q = sq_apply<T, M>(rp, ep, nt, nb, s, q, &lg, nullptr, nullptr, nullptr, nullptr);
         }
         for (int n = n1max - 1; n >= n0; n--) {
           const bool on = n < n1;
@@ -2090,11 +2138,11 @@ __global__ void __launch_bounds__(SQ_T) sq_bwd_batch_kernel(
             qn = seg[n - n0];
             T lg;
             V4<T> Tq, Bq;
-            const V4<T> Q = sq_apply<T>(rp, ep, nt, nb, s, qn, &lg, F, nullptr, &Tq, &Bq);
-            const V4<T> Qb = v4add(qb, v4scale(Q, sq_div(Lb, v4dot(Q, Q))));
+            const V4<T> Q = sq_apply<T, M>(rp, ep, nt, nb, s, qn, &lg, F, nullptr, &Tq, &Bq);
+            const V4<T> Qb = v4add(qb, v4scale(Q, sq_div<T, M>(Lb, v4dot(Q, Q))));
             dls = v4dot(Qb, Q);
             if (nb > 0) {
-              const V4<T> W4 = v4scale(v4conj(Bq), sq_div(T(1), v4dot(Bq, Bq)));
+              const V4<T> W4 = v4scale(v4conj(Bq), sq_div<T, M>(T(1), v4dot(Bq, Bq)));
               Tb = v4scale(v4mul(Qb, v4conj(W4)), s);
               const V4<T> Wb = v4scale(v4mul(v4conj(Tq), Qb), s);
               Bb = v4scale(v4mul(v4mul(v4conj(W4), Wb), v4conj(W4)), T(-1));
@@ -2105,9 +2153,9 @@ __global__ void __launch_bounds__(SQ_T) sq_bwd_batch_kernel(
             for (int i = 0; i < nr; i++) {
               const V4<T> d{qn.w - rp[4 * i], qn.x - rp[4 * i + 1], qn.y - rp[4 * i + 2],
                             qn.z - rp[4 * i + 3]};
-              g = v4add(g, v4scale(d, sq_div(i >= nt ? -ep[i] : ep[i], v4dot(d, d))));
+              g = v4add(g, v4scale(d, sq_div<T, M>(i >= nt ? -ep[i] : ep[i], v4dot(d, d))));
             }
-            gb = v4scale(g, sq_div(Lb, v4dot(g, g)));
+            gb = v4scale(g, sq_div<T, M>(Lb, v4dot(g, g)));
           }
           dls = warp_sum(dls);
           if (lane == 0) acc[1 + 5 * nr] += (double)dls;
@@ -2122,15 +2170,15 @@ __global__ void __launch_bounds__(SQ_T) sq_bwd_batch_kernel(
                 const V4<T> d{qn.w - rp[4 * i], qn.x - rp[4 * i + 1], qn.y - rp[4 * i + 2],
                               qn.z - rp[4 * i + 3]};
                 PowParts<T> pp;
-                const V4<T> P = powv<T>(d, ep[i], &pp);
+                const V4<T> P = powv<T, M>(d, ep[i], &pp);
                 const V4<T> Pb = (i == lo) ? U : v4mul(v4conj(F[i - 1]), U);
                 U = v4mul(U, v4conj(P));
                 T eb = T(0);
-                V4<T> dbar = powv_vjp<T>(d, ep[i], pp, Pb, &eb);
+                V4<T> dbar = powv_vjp<T, M>(d, ep[i], pp, Pb, &eb);
                 const T sgn = side ? T(-1) : T(1);
                 const T d2 = v4dot(d, d);
                 const T dg = v4dot(d, gb);
-                const T id2 = sq_div(T(1), d2);
+                const T id2 = sq_div<T, M>(T(1), d2);
                 dbar = v4add(dbar, v4scale(v4add(v4scale(gb, id2),
                                                  v4scale(d, T(-2) * dg * id2 * id2)),
                                            sgn * ep[i]));
@@ -2164,6 +2212,17 @@ __global__ void __launch_bounds__(SQ_T) sq_bwd_batch_kernel(
   }
 }
 
+// The FP32 form is chosen once per launch (straight-line root loops).
+__global__ void __launch_bounds__(SQ_T) sq_bwd_batch_kernel(
+    const SqItem* __restrict__ items, int K, long long n_flat, const int* __restrict__ keys,
+    const V4<float>* __restrict__ seed_q, const float* __restrict__ seed_L,
+    const V4<float>* __restrict__ ck, int max_slots) {
+  if (c_sq_fast)
+    sq_bwd_batch_body<SQM_FAST>(items, K, n_flat, keys, seed_q, seed_L, ck, max_slots);
+  else
+    sq_bwd_batch_body<SQM_ACC>(items, K, n_flat, keys, seed_q, seed_L, ck, max_slots);
+}
+
 // The final sums of one item: its chunk rows and as many group rows as its
 // sort produced (read on the device), as sq_reduce_kernel.
 __global__ void __launch_bounds__(32 * SQR_W) sq_reduce_item_kernel(
@@ -2174,6 +2233,10 @@ __global__ void __launch_bounds__(32 * SQR_W) sq_reduce_item_kernel(
 
 // Forward kernel choice (qjg_set_energy_pairs): two samples per lane or one.
 std::atomic<int> g_sq_pairs{0};
+// Forward blocks per SM (qjg_set_energy_forward_blocks): 0 the rule in
+// sq_launch, else that many (capped by residency), for sweeps.
+std::atomic<int> g_sq_fwd_blocks{0};
+
 // FP32 adjoint choice (qjg_set_energy_adjoint_roots): the roots of a step
 // spread over a group of lanes (sq_bwd_roots_kernel) or walked by one lane.
 std::atomic<int> g_sq_bwd_roots{1};
@@ -2247,7 +2310,7 @@ template <class T>
 cudaError_t sq_launch(bool grad, const double* params, int nt, int nb, const double* xyz,
                       const double* target, long long n, double slice, int max_it, double escape,
                       double d_sat, unsigned char* scr, const SqLayout& L, int* iters, int sms,
-                      cudaStream_t s, int* launches) {
+                      cudaStream_t s, int* launches, long long steps_hint) {
   const int nr = nt + nb;
   unsigned long long* claim = reinterpret_cast<unsigned long long*>(scr + L.claim);
   int* total = reinterpret_cast<int*>(scr + L.total);
@@ -2273,12 +2336,27 @@ cudaError_t sq_launch(bool grad, const double* params, int nt, int nb, const dou
   else
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sq_fwd_kernel<T, false>, SQF_T, sh_roots);
   if (e != cudaSuccess) return e;
-  // Blocks per SM: enough warps to keep the issue slots busy, few enough that
-  // each lane runs about four samples, so that refill evens out the orbit
-  // lengths (200k samples, 30 steps: 3 blocks per SM 1.94 ms, 5 2.09 ms, 9
-  // (all resident) 2.47 ms).
+  // Blocks per SM.  The kernel ends when the lane with the most orbit steps
+  // ends, so the grid is sized from the orbit steps of the call: with as
+  // many lanes as total steps / max_it, a lane runs about one full-length
+  // orbit (or its equivalent in short ones) and no lane is left with two
+  // full-length orbits, while each extra warp costs issue slots.  On the
+  // differentiation workload (200k samples, 30 iterations, 3.06 M steps,
+  // 49% of the orbits at the cap; forward kernel, ms) 2 blocks per SM 1.22,
+  // 3 0.96, 4 1.01, 5 0.96, 6 0.83, 8 1.03: 6 is the first count with a lane
+  // per full-length orbit.  The steps are those of an earlier call on the
+  // same samples (steps_hint); without one, or in FP64 (bound by the FP64
+  // pipe rather than by the longest lane), about four samples per lane and
+  // at least 3 blocks per SM.
   const long long lanes_per_sm = (long long)sms * SQF_T;
-  const long long want = std::max<long long>(3, ((n + 3) / 4 + lanes_per_sm - 1) / lanes_per_sm);
+  const int fixed = g_sq_fwd_blocks.load(std::memory_order_relaxed);
+  long long want = std::max<long long>(3, ((n + 3) / 4 + lanes_per_sm - 1) / lanes_per_sm);
+  if (fixed > 0) {
+    want = fixed;
+  } else if (std::is_same<T, float>::value && steps_hint > 0 && max_it > 0) {
+    const long long lanes = (steps_hint + max_it - 1) / max_it;
+    want = std::max<long long>(3, (lanes + lanes_per_sm - 1) / lanes_per_sm);
+  }
   const long long need = (n + SQF_T - 1) / SQF_T;
   const int fblocks = (int)std::max<long long>(
       1, std::min<long long>((long long)sms * std::min<long long>(std::max(per_sm, 1), want), need));
@@ -2488,6 +2566,8 @@ void set_energy_pairs(int on) { g_sq_pairs.store(on ? 1 : 0); }
 
 void set_energy_adjoint_roots(int on) { g_sq_bwd_roots.store(on ? 1 : 0); }
 
+void set_energy_forward_blocks(int per_sm) { g_sq_fwd_blocks.store(per_sm > 0 ? per_sm : 0); }
+
 cudaError_t set_energy_fast(int on) {
   const int v = on ? 1 : 0;
   return cudaMemcpyToSymbol(c_sq_fast, &v, sizeof v);
@@ -2501,7 +2581,7 @@ cudaError_t launch_sq_energy(bool fp64, bool grad, const double* params, int nt,
                              const double* xyz, const double* target, long long n, double slice,
                              int max_it, double escape, double d_sat, void* scratch,
                              double** out, int* iters, cudaStream_t s, int* launches,
-                             unsigned long long** work) {
+                             unsigned long long** work, long long steps_hint) {
   const int sms = sm_count();
   const SqLayout L = sq_layout(fp64, grad, n, max_it, nt, nb, sms);
   unsigned char* scr = static_cast<unsigned char*>(scratch);
@@ -2509,9 +2589,9 @@ cudaError_t launch_sq_energy(bool fp64, bool grad, const double* params, int nt,
   *work = reinterpret_cast<unsigned long long*>(scr + L.work);
   if (fp64)
     return sq_launch<double>(grad, params, nt, nb, xyz, target, n, slice, max_it, escape, d_sat,
-                             scr, L, iters, sms, s, launches);
+                             scr, L, iters, sms, s, launches, steps_hint);
   return sq_launch<float>(grad, params, nt, nb, xyz, target, n, slice, max_it, escape, d_sat, scr,
-                          L, iters, sms, s, launches);
+                          L, iters, sms, s, launches, steps_hint);
 }
 
 }  // namespace qj

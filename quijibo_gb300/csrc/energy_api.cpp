@@ -83,6 +83,12 @@ int qjg_set_energy_adjoint_roots(int on) {
   return QJG_OK;
 }
 
+int qjg_set_energy_forward_blocks(int per_sm) {
+  if (per_sm < 0) return QJG_ERR_ARG;
+  qj::set_energy_forward_blocks(per_sm);
+  return QJG_OK;
+}
+
 int qjg_set_energy_fast(int on) {
   return qj::set_energy_fast(on) == cudaSuccess ? QJG_OK : QJG_ERR_CUDA;
 }
@@ -159,9 +165,13 @@ static int sq_energy(qjg_ctx* ctx, const double* d_params, int32_t nt, int32_t n
   double* d_out = nullptr;
   unsigned long long* d_work = nullptr;
   int launched = 0;
+  // the previous call's work sizes the forward grid when it ran on as many
+  // samples with the same iteration cap (the optimizer's repeated calls)
+  const long long hint =
+      (ctx->sq_last_n == n && ctx->sq_last_max_it == max_it) ? ctx->sq_applications : 0;
   cudaError_t e = qj::launch_sq_energy(fp64, grad, d_params, nt, nb, d_xyz, d_target, n, slice,
                                        max_it, escape, d_sat, d_scr, &d_out, d_iters, s, &launched,
-                                       &d_work);
+                                       &d_work, hint);
   unsigned long long work[2] = {0, 0};
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(work, d_work, sizeof work, cudaMemcpyDeviceToHost, s);
@@ -174,6 +184,8 @@ static int sq_energy(qjg_ctx* ctx, const double* d_params, int32_t nt, int32_t n
   ctx->launches += launched;
   ctx->sq_applications = (int64_t)work[0];
   ctx->sq_steps = (int64_t)work[1];
+  ctx->sq_last_n = n;
+  ctx->sq_last_max_it = max_it;
   return QJG_OK;
 }
 

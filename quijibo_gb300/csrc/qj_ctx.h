@@ -50,6 +50,8 @@ struct qjg_ctx {
   int64_t launches = 0;
   int64_t sq_applications = 0;  // work of the last energy call: forward map applications
   int64_t sq_steps = 0;         // ... and adjoint orbit steps
+  int64_t sq_last_n = -1;       // sample count and iteration cap of that call
+  int32_t sq_last_max_it = -1;
   // marching-cubes scratch
   qj::DevStats* d_mstats = nullptr;
   double* m_field = nullptr;    // slab field window

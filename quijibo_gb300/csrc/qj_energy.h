@@ -30,15 +30,19 @@ void set_energy_pairs(int on);
 // process-wide choice of the FP32 adjoint: 1 (default) the roots of a step
 // spread over a group of lanes where the map fits, 0 one lane per sample
 void set_energy_adjoint_roots(int on);
+// FP32/FP64 forward blocks per SM (0: the sizing rule).
+void set_energy_forward_blocks(int per_sm);
 // the FP32 polar power's fast form (hardware log2 and sin/cos, polynomial atan)
 cudaError_t set_energy_fast(int on);
 // *work: two counters in the scratch, the map applications of the forward
-// pass and the orbit steps of the adjoint (read after the call completes)
+// pass and the orbit steps of the adjoint (read after the call completes).
+// steps_hint: the forward map applications of an earlier call on the same
+// samples (0 if none), which sizes the FP32 forward grid.
 cudaError_t launch_sq_energy(bool fp64, bool grad, const double* params, int nt, int nb,
                              const double* xyz, const double* target, long long n, double slice,
                              int max_it, double escape, double d_sat, void* scratch,
                              double** out, int* iters, cudaStream_t s, int* launches,
-                             unsigned long long** work);
+                             unsigned long long** work, long long steps_hint);
 
 // One request of a batch of FP32 energy + gradient calls: device pointers
 // as for launch_sq_energy.

@@ -217,6 +217,7 @@ EXPORTS = {
     "qjg_set_energy_adjoint_roots": ([C.c_int], C.c_int),
     "qjg_trim": ([C.c_void_p], C.c_int),
     "qjg_set_energy_fast": ([C.c_int], C.c_int),
+    "qjg_set_energy_forward_blocks": ([C.c_int], C.c_int),
     "qjg_energy_backward_batch": ([C.c_void_p, C.c_int32, C.POINTER(QjgEnergyItem), C.c_void_p],
                                   C.c_int),
     "qjg_energy_last_work": ([C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)], C.c_int),
@@ -470,6 +471,12 @@ def set_energy_fast(on):
     default) or the accurate device functions (False)."""
     if load().qjg_set_energy_fast(int(bool(on))) != 0:
         raise QjgError("qjg_set_energy_fast failed")
+
+
+def set_energy_forward_blocks(per_sm):
+    """Energy forward kernel's blocks per SM (0: the sizing rule), for sweeps."""
+    if load().qjg_set_energy_forward_blocks(int(per_sm)) != 0:
+        raise QjgError("qjg_set_energy_forward_blocks(%d) failed" % per_sm)
 
 
 def set_field32_pairs(on):
