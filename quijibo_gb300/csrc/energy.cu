@@ -2345,16 +2345,18 @@ cudaError_t sq_launch(bool grad, const double* params, int nt, int nb, const dou
   // 49% of the orbits at the cap; forward kernel, ms) 2 blocks per SM 1.22,
   // 3 0.96, 4 1.01, 5 0.96, 6 0.83, 8 1.03: 6 is the first count with a lane
   // per full-length orbit.  The steps are those of an earlier call on the
-  // same samples (steps_hint); without one, or in FP64 (bound by the FP64
-  // pipe rather than by the longest lane), about four samples per lane and
-  // at least 3 blocks per SM.
+  // same samples (steps_hint), else half the iteration cap per sample (a
+  // lane per two samples); at least 3 blocks per SM.  FP64 (bound by the
+  // FP64 pipe rather than by the longest lane) keeps about four samples per
+  // lane.
   const long long lanes_per_sm = (long long)sms * SQF_T;
   const int fixed = g_sq_fwd_blocks.load(std::memory_order_relaxed);
   long long want = std::max<long long>(3, ((n + 3) / 4 + lanes_per_sm - 1) / lanes_per_sm);
   if (fixed > 0) {
     want = fixed;
-  } else if (std::is_same<T, float>::value && steps_hint > 0 && max_it > 0) {
-    const long long lanes = (steps_hint + max_it - 1) / max_it;
+  } else if (std::is_same<T, float>::value && max_it > 0) {
+    const long long steps = steps_hint > 0 ? steps_hint : (n * max_it + 1) / 2;
+    const long long lanes = (steps + max_it - 1) / max_it;
     want = std::max<long long>(3, (lanes + lanes_per_sm - 1) / lanes_per_sm);
   }
   const long long need = (n + SQF_T - 1) / SQF_T;
@@ -2527,10 +2529,20 @@ cudaError_t launch_sq_energy_batch(const SqBatchReq* r, int K, void* scratch, do
   o.seed_L = reinterpret_cast<float*>(scr + L.seed_L);
   o.ck = reinterpret_cast<V4<float>*>(scr + L.ck);
   const int sms = sm_count();
-  // persistent forward grid: three blocks per SM (the single-request choice
-  // for long orbit mixes), fewer when the batch is small
+  // persistent forward grid: as the single request's first call, a lane per
+  // two samples of the batch (at least 3 blocks per SM, at most the resident
+  // count), fewer when the batch is small
+  int per_sm = 0;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sq_fwd_batch_kernel, SQF_T, 0)))
+    return e;
   const long long need = (L.n_flat + SQF_T - 1) / SQF_T;
-  const int fblocks = (int)std::max<long long>(1, std::min<long long>((long long)sms * 3, need));
+  long long total_n = 0;
+  for (int i = 0; i < K; i++) total_n += r[i].n;
+  const long long lanes_per_sm = (long long)sms * SQF_T;
+  const long long want = std::min<long long>(
+      std::max(per_sm, 1),
+      std::max<long long>(3, ((total_n + 1) / 2 + lanes_per_sm - 1) / lanes_per_sm));
+  const int fblocks = (int)std::max<long long>(1, std::min<long long>((long long)sms * want, need));
   sq_fwd_batch_kernel<<<fblocks, SQF_T, 0, s>>>(d_items, d_chunk_item, L.n_flat, claim, o);
   n_launch++;
   // per item: chunk sums and histogram, the sort's scan and scatter

@@ -278,3 +278,32 @@ def test_context_pool_keeps_scratch_until_trim(ctx, config4):
     assert freed >= 0.9 * len(t) * p["max_it"] * 16, freed
     e2, g2 = run()
     assert e2 == e0 and np.array_equal(g2, g0)
+
+
+@pytest.mark.parametrize("precision", [lib.QJG_FP32, lib.QJG_FP64])
+def test_forward_grid_does_not_change_results(ctx, precision):
+    """The forward kernel's grid (the sizing rule on a first call, the earlier
+    call's orbit steps on a repeated one, or a fixed block count) decides
+    only which lane runs which sample: each sample's value is its own and the
+    sums run in sample order, so the energy and the gradient keep their bits
+    at every block count."""
+    rs, xyz, t = small_case(n=20000)
+    p = dev(lib.params_of(rs))
+    X, T = dev(xyz), dev(t)
+
+    def run():
+        g = torch.empty(len(p), dtype=torch.float64, device="cuda")
+        e = ctx.energy(p.data_ptr(), rs.n_top, rs.n_bottom, len(t), X.data_ptr(), T.data_ptr(),
+                       20, 2.0, precision=precision, d_grad=g.data_ptr())
+        return e, g.cpu().numpy(), ctx.energy_last_work()
+
+    first = run()  # sized by the rule (or by an earlier test's call on as many samples)
+    out = [run()]  # sized by the first call's orbit steps
+    try:
+        for per_sm in (1, 2, 6, 9):
+            lib.set_energy_forward_blocks(per_sm)
+            out.append(run())
+    finally:
+        lib.set_energy_forward_blocks(0)
+    for e, g, w in out:
+        assert e == first[0] and np.array_equal(g, first[1]) and w == first[2]
