@@ -365,7 +365,10 @@ int qjg_fit_lbfgs(qjg_ctx* ctx, double* d_params, int32_t n_top, int32_t n_bot, 
  * with integer exponents and at most 2^26 voxels are served by a batch
  * worker instead: every such request waiting when it becomes free (up to 64
  * and the batch arena) runs in one multi-request pass, replayed from a
- * captured CUDA graph.  FP32 energy + gradient requests go to an energy
+ * captured CUDA graph.  Mesh requests of the same form with at most 2^22
+ * voxels take their field from that pass as well; a worker then meshes that
+ * field (qjg_mesh_field with the map's bisection: the vertices and triangles
+ * qjg_mesh_stream gives them).  FP32 energy + gradient requests go to an energy
  * batch worker, which runs every such request waiting when it is free as
  * one qjg_energy_backward_batch pass.  Inputs are copied at submission; output buffers
  * (host) must stay valid until the request completes. */
@@ -424,12 +427,13 @@ typedef struct {
   int64_t peak_in_use_bytes;
   int32_t peak_running;          /* most requests running at once */
   int32_t pad_;
-  int64_t batched;               /* field requests served inside multi-request batches */
+  int64_t batched;               /* field (and mesh) requests served inside multi-request batches */
   int64_t batches;               /* batch passes (one CUDA-graph replay each) */
   int64_t max_batch;             /* most requests in one batch */
   int64_t energy_batched;        /* FP32 energy requests served inside energy batches */
   int64_t energy_batches;        /* energy batch passes */
   int64_t max_energy_batch;      /* most requests in one energy batch */
+  int64_t mesh_batched;          /* mesh requests among `batched` (field from the batch pass) */
 } qjg_server_stats;
 
 int qjg_server_create(int device, int32_t workers, int64_t hbm_budget_bytes, qjg_server** out);

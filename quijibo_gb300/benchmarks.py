@@ -422,7 +422,7 @@ def bench_serve(args):
            "failed": st["failed"], "batched": st["batched"], "batches": st["batches"],
            "max_batch": st["max_batch"], "energy_batched": st["energy_batched"],
            "energy_batches": st["energy_batches"], "max_energy_batch": st["max_energy_batch"],
-           "by_kind": {}, "capacity_retries": retried, "failures": _failures(reqs, results)}
+           "mesh_batched": st["mesh_batched"], "by_kind": {}, "capacity_retries": retried, "failures": _failures(reqs, results)}
     for kind, name in ((lib.QJG_REQ_FIELD, "field"), (lib.QJG_REQ_MESH, "mesh"),
                        (lib.QJG_REQ_ENERGY, "energy")):
         lk = np.array([r["latency_ms"] for r, q in zip(results, reqs) if q["kind"] == kind])
@@ -446,7 +446,8 @@ def bench_serve(args):
                     "batched": st_b["batched"], "batches": st_b["batches"],
                     "max_batch": st_b["max_batch"], "energy_batched": st_b["energy_batched"],
                     "energy_batches": st_b["energy_batches"],
-                    "max_energy_batch": st_b["max_energy_batch"], "failed": st_b["failed"],
+                    "max_energy_batch": st_b["max_energy_batch"],
+                    "mesh_batched": st_b["mesh_batched"], "failed": st_b["failed"],
                     "capacity_retries": retried_b, "failures": _failures(reqs, results_b)}
     # baseline: a sample of the same requests, plain FP64, one at a time
     ctx = lib.Context(0)

@@ -12,8 +12,12 @@
 // worker: all that wait when it frees up run as one multi-request pass (one
 // tile queue over every item, field.cu's batch kernels), replayed from a
 // CUDA graph captured on the first batch, with the batch table rewritten in
-// place each time.  Results are copied to caller buffers; latencies are
-// measured from submission to completion on the host clock.
+// place each time.  Small mesh requests of the same form take their field
+// from that pass too (an item of the batch); the field is copied out of the
+// arena and the request goes back to the dispatcher, which hands it to a
+// worker to mesh (so meshes still overlap one another).  Results are copied
+// to caller buffers; latencies are measured from submission to completion
+// on the host clock.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -36,6 +40,9 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
+// Largest mesh request (voxels) whose field joins the field batch pass.
+constexpr int64_t kMeshBatchVoxels = 1ll << 22;
+
 struct Job {
   int64_t ticket;
   qjg_request req;
@@ -43,7 +50,10 @@ struct Job {
   std::vector<double> top_roots, top_powers, bot_roots, bot_powers, xyz, target, params;
   int64_t est_bytes = 0;
   int64_t voxels = 0;
-  bool batchable = false;   // field request for the field batch worker
+  bool batchable = false;   // field (or mesh) request for the field batch worker
+  bool mbatch = false;      // a mesh request whose field runs in the field batch
+  bool staged = false;      // ... whose field has run: a worker meshes d_staged
+  double* d_staged = nullptr;  // that field (X*Y*Z doubles, freed by the worker)
   bool ebatchable = false;  // FP32 energy request for the energy batch worker
   Clock::time_point t_submit, t_admit, t_done;
   qjg_result res;
@@ -112,7 +122,10 @@ struct FieldBatcher {
     return b;
   }
 
-  // One pass over `jobs` (each batchable; their voxels sum to <= cap).
+  // One pass over `jobs` (each batchable; their voxels sum to <= cap); the
+  // fields of the mesh jobs among them are copied to their own device
+  // buffers (Job::d_staged).  Returns the pass's status; a mesh job whose
+  // copy failed has its own status in its result.
   int run(std::vector<std::shared_ptr<Job>>& jobs);
 };
 
@@ -167,7 +180,7 @@ struct qjg_server {
   bool batch_idle = false;
   std::vector<std::shared_ptr<Job>> batch_q;
   std::condition_variable batch_cv;
-  int64_t batched = 0, batches = 0, max_batch = 0;
+  int64_t batched = 0, batches = 0, max_batch = 0, mesh_batched = 0;
 
   // energy batch worker
   bool ebatch_on = false;
@@ -181,9 +194,19 @@ struct qjg_server {
 
 namespace {
 
+void mesh_from_field(qjg_ctx* mctx, cudaStream_t s, Job& j, const double* d_field);
+
 void run_job(qjg_ctx* ctx, cudaStream_t s, Job& j) {
   qjg_request& r = j.req;
   qjg_result& out = j.res;
+  if (j.staged) {
+    // a mesh whose field the batch pass computed
+    mesh_from_field(ctx, s, j, j.d_staged);
+    cudaFreeAsync(j.d_staged, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess && out.error == QJG_OK) out.error = QJG_ERR_CUDA;
+    j.d_staged = nullptr;
+    return;
+  }
   int rc = QJG_OK;
   qjg_rootset h = -1;
   if (r.kind == QJG_REQ_FIELD || r.kind == QJG_REQ_MESH) {
@@ -341,6 +364,54 @@ void worker_main(qjg_server* srv, int w) {
   if (ctx) qjg_destroy(ctx);
 }
 
+// The mesh of a mesh job from its field computed by the batch pass
+// (d_field): the bisection evaluates the map as the streaming mesher does,
+// so the vertices and triangles are the ones qjg_mesh_stream gives for the
+// request.
+void mesh_from_field(qjg_ctx* mctx, cudaStream_t s, Job& j, const double* d_field) {
+  qjg_request& r = j.req;
+  qjg_result& out = j.res;
+  qjg_rootset h = -1;
+  int rc = qjg_rootset_upload(mctx, r.n_top, j.top_roots.data(), j.top_powers.data(), r.sigma_top,
+                              r.n_bot, j.bot_roots.empty() ? nullptr : j.bot_roots.data(),
+                              j.bot_powers.empty() ? nullptr : j.bot_powers.data(), r.sigma_bot,
+                              r.scale, &h);
+  qjg_iter it = {};
+  it.max_it = r.max_it;
+  it.precision = r.precision;
+  it.refine_pow = QJG_REFINE_INT;
+  it.escape = r.escape;
+  it.band_h = 2.0;
+  it.field_tol = 1e-3;
+  it.rel_tol = r.precision == QJG_FP32_REFINE ? r.rel_tol : 0.0;
+  double* v64 = nullptr;
+  int32_t* tris = nullptr;
+  const int64_t vcap = std::max<int64_t>(r.vert_cap, 1), tcap = std::max<int64_t>(r.tri_cap, 1);
+  if (rc == QJG_OK && (qj_malloc_async(mctx, &v64, vcap * 3 * sizeof(double), s) != cudaSuccess ||
+                       qj_malloc_async(mctx, &tris, tcap * 3 * sizeof(int32_t), s) != cudaSuccess))
+    rc = QJG_ERR_NOMEM;
+  qjg_mesh_stats ms = {};
+  if (rc == QJG_OK)
+    rc = qjg_mesh_field(mctx, h, &r.grid, &it, d_field, QJG_EDGE_BISECT, r.iso, 0, v64, nullptr,
+                        vcap, tris, tcap, &ms, s);
+  // a mesh that outgrows its capacities reports the counts it needs
+  out.n_verts = ms.n_verts;
+  out.n_tris = ms.n_tris;
+  if (rc == QJG_OK && r.out_verts &&
+      cudaMemcpyAsync(r.out_verts, v64, ms.n_verts * 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                      s) != cudaSuccess)
+    rc = QJG_ERR_CUDA;
+  if (rc == QJG_OK && r.out_tris &&
+      cudaMemcpyAsync(r.out_tris, tris, ms.n_tris * 3 * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                      s) != cudaSuccess)
+    rc = QJG_ERR_CUDA;
+  if (v64) cudaFreeAsync(v64, s);
+  if (tris) cudaFreeAsync(tris, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess && rc == QJG_OK) rc = QJG_ERR_CUDA;
+  if (h >= 0) qjg_rootset_free(mctx, h);
+  out.error = rc;
+}
+
 int FieldBatcher::run(std::vector<std::shared_ptr<Job>>& jobs) {
   const int n = (int)jobs.size();
   int64_t off = 0, tiles = 0;
@@ -400,7 +471,7 @@ int FieldBatcher::run(std::vector<std::shared_ptr<Job>>& jobs) {
   off = 0;
   for (int k = 0; k < n; k++) {
     Job& j = *jobs[k];
-    if (j.req.out_field &&
+    if (!j.mbatch && j.req.out_field &&
         cudaMemcpyAsync(j.req.out_field, d_arena + off, (size_t)j.voxels * sizeof(double),
                         cudaMemcpyDeviceToHost, s))
       return QJG_ERR_CUDA;
@@ -408,6 +479,23 @@ int FieldBatcher::run(std::vector<std::shared_ptr<Job>>& jobs) {
   }
   if (cudaStreamSynchronize(s)) return QJG_ERR_CUDA;
   for (int k = 0; k < n; k++) jobs[k]->res.voxel_iters = (int64_t)h_counts[k].voxel_iters;
+  // the mesh jobs' fields out of the arena (the next pass reuses it)
+  off = 0;
+  for (int k = 0; k < n; k++) {
+    Job& j = *jobs[k];
+    if (j.mbatch) {
+      const size_t bytes = (size_t)j.voxels * sizeof(double);
+      if (cudaMallocAsync((void**)&j.d_staged, bytes, s) != cudaSuccess) {
+        j.d_staged = nullptr;
+        j.res.error = QJG_ERR_NOMEM;
+      } else if (cudaMemcpyAsync(j.d_staged, d_arena + off, bytes, cudaMemcpyDeviceToDevice, s) !=
+                 cudaSuccess) {
+        j.res.error = QJG_ERR_CUDA;
+      }
+    }
+    off += j.voxels;
+  }
+  if (cudaStreamSynchronize(s)) return QJG_ERR_CUDA;
   return QJG_OK;
 }
 
@@ -433,11 +521,26 @@ void batch_main(qjg_server* srv) {
       srv->batched += (int64_t)jobs.size();
       srv->max_batch = std::max<int64_t>(srv->max_batch, (int64_t)jobs.size());
       for (auto& j : jobs) {
-        j->res.error = rc;
+        // a failed pass fails every job; after it, a mesh job has its own status
+        if (rc != QJG_OK) j->res.error = rc;
+        if (j->mbatch) {
+          srv->mesh_batched++;
+          j->mbatch = false;
+          if (j->res.error == QJG_OK && j->d_staged) {
+            // to the front of the queue: a worker meshes it (its bytes stay
+            // counted in the budget from its admission to the batch)
+            j->staged = true;
+            srv->running--;
+            srv->waiting.push_front(j);
+            continue;
+          }
+          if (j->d_staged) cudaFree(j->d_staged);
+          j->d_staged = nullptr;
+        }
         finish_job(srv, *j, now);
       }
       srv->cv_done.notify_all();
-      srv->cv_dispatch.notify_one();
+      srv->cv_dispatch.notify_all();
     }
   }
 }
@@ -547,12 +650,16 @@ void dispatcher_main(qjg_server* srv) {
       int64_t vox = 0;
       for (size_t i = 0; i < srv->waiting.size() && (int)srv->batch_q.size() < qj::BATCH_MAX;) {
         auto job = srv->waiting[i];
-        if (!job->batchable || vox + job->voxels > srv->batch_cap) {
+        // a mesh job's mesher buffers count against the budget
+        const bool fits = srv->in_use + job->est_bytes <= srv->budget || srv->in_use == 0;
+        if (!job->batchable || job->staged || vox + job->voxels > srv->batch_cap || !fits) {
           i++;
           continue;
         }
         srv->waiting.erase(srv->waiting.begin() + (long)i);
         vox += job->voxels;
+        srv->in_use += job->est_bytes;
+        srv->peak_in_use = std::max(srv->peak_in_use, srv->in_use);
         job->t_admit = Clock::now();
         srv->batch_q.push_back(job);
         srv->running++;
@@ -603,13 +710,14 @@ void dispatcher_main(qjg_server* srv) {
       int seen = 0;
       for (size_t i = 0; i < srv->waiting.size() && seen < srv->lookahead; i++) {
         auto job = srv->waiting[i];
-        if (job->batchable && srv->batcher) continue;  // the batch worker's
+        if (job->batchable && !job->staged && srv->batcher) continue;  // the batch worker's
         if (job->ebatchable && srv->ebatch_on) continue;  // the energy batch worker's
         seen++;
-        // a request larger than the whole budget runs alone
-        if (srv->in_use + job->est_bytes <= srv->budget || srv->in_use == 0) {
+        // a request larger than the whole budget runs alone; a staged mesh
+        // has been counted since its admission to the batch
+        if (job->staged || srv->in_use + job->est_bytes <= srv->budget || srv->in_use == 0) {
           srv->waiting.erase(srv->waiting.begin() + (long)i);
-          srv->in_use += job->est_bytes;
+          if (!job->staged) srv->in_use += job->est_bytes;
           srv->peak_in_use = std::max(srv->peak_in_use, srv->in_use);
           srv->running++;
           srv->peak_running = std::max(srv->peak_running, srv->running);
@@ -688,7 +796,8 @@ int qjg_server_submit(qjg_server* srv, const qjg_request* req, int64_t* ticket) 
   }
   j->est_bytes = estimate_bytes(*req);
   j->voxels = (int64_t)req->grid.res[0] * req->grid.res[1] * req->grid.res[2];
-  if (req->kind == QJG_REQ_FIELD && req->precision != QJG_FP64 && req->grid.res[0] > 0 &&
+  if ((req->kind == QJG_REQ_FIELD || req->kind == QJG_REQ_MESH) && req->precision != QJG_FP64 &&
+      req->grid.res[0] > 0 &&
       req->grid.res[1] > 0 && req->grid.res[2] > 0 && j->voxels <= srv->batch_cap &&
       j->voxels <= qj::BATCH_ITEM_VOXELS && req->max_it >= 0 && req->escape > 0) {
     // batch items take integer effective exponents (the double-float head and
@@ -699,8 +808,15 @@ int qjg_server_submit(qjg_server* srv, const qjg_request* req, int64_t* ticket) 
                                : req->sigma_bot * req->bot_powers[i - nt]);
       ints = e == std::floor(e) && e >= 1 && e <= QJ_MAX_INT_EXP;
     }
-    j->batchable = ints;
-    if (ints) j->est_bytes = 0;  // inside the batch arena
+    // meshes join the batch up to kMeshBatchVoxels, so that a large mesh
+    // field does not hold up the small fields of its pass
+    const bool mesh = req->kind == QJG_REQ_MESH;
+    j->batchable = ints && (!mesh || j->voxels <= kMeshBatchVoxels);
+    j->mbatch = j->batchable && mesh;
+    // a field lives inside the batch arena; a mesh job keeps its mesher's
+    // part and the copy of its field
+    if (j->batchable && !mesh) j->est_bytes = 0;
+    if (j->mbatch) j->est_bytes += j->voxels * (int64_t)sizeof(double);
   }
   j->ebatchable = req->kind == QJG_REQ_ENERGY && req->precision != QJG_FP64 &&
                   req->max_it >= 0 && req->escape > 0;
@@ -787,6 +903,7 @@ int qjg_server_read_stats(qjg_server* srv, qjg_server_stats* out) {
   out->energy_batched = srv->ebatched;
   out->energy_batches = srv->ebatches;
   out->max_energy_batch = srv->max_ebatch;
+  out->mesh_batched = srv->mesh_batched;
   return QJG_OK;
 }
 

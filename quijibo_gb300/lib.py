@@ -132,7 +132,7 @@ class QjgServerStats(C.Structure):
                 ("peak_running", C.c_int32), ("pad_", C.c_int32), ("batched", C.c_int64),
                 ("batches", C.c_int64), ("max_batch", C.c_int64),
                 ("energy_batched", C.c_int64), ("energy_batches", C.c_int64),
-                ("max_energy_batch", C.c_int64)]
+                ("max_energy_batch", C.c_int64), ("mesh_batched", C.c_int64)]
 
 
 class QjgBlmvmSettings(C.Structure):

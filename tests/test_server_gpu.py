@@ -177,3 +177,47 @@ def test_batched_energy_requests_equal_direct_calls(ctx):
         tol = 1e-5 if r["precision"] == lib.QJG_FP32 else 1e-12
         assert abs(o["energy"] - e) <= tol * abs(e)
         assert np.linalg.norm(o["grad"] - g) <= tol * np.linalg.norm(g)
+
+
+def test_batched_mesh_requests_equal_direct_calls(ctx):
+    """Precision-form mesh requests with integer exponents take their field
+    from the field batch pass (with the field requests waiting beside them)
+    and are meshed from it: each mesh has the vertices and triangles of its
+    own qjg_mesh_stream call, bit for bit."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.RandomState(7)
+    reqs = []
+    for i in range(12):
+        nt, nb = int(rng.randint(3, 17)), int(rng.randint(0, 7))
+        rs = draw_rootset(500 + i, nt, nb, -1.2, 1.2, exps=(1, 2))
+        res = int(rng.choice([16, 24, 33, 40]))
+        g = Grid((res, res, res))
+        rs.scale = conformal_scale(rs, g, sample_res=16)
+        kind = lib.QJG_REQ_FIELD if i % 4 == 3 else lib.QJG_REQ_MESH
+        reqs.append(dict(kind=kind, rs=rs, grid=g, max_it=int(rng.randint(5, 25)),
+                         precision=lib.QJG_FP32_REFINE, rel_tol=[0.0, 1e-6][i % 2]))
+    srv = lib.Server(workers=4)
+    outs, res = run(srv, reqs)
+    st = srv.stats()
+    srv.close()
+    n_mesh = sum(1 for r in reqs if r["kind"] == lib.QJG_REQ_MESH)
+    assert st["mesh_batched"] == n_mesh and st["batched"] == len(reqs) and st["failed"] == 0
+    assert st["batches"] < len(reqs)
+    tris = 0
+    for r, o, rr in zip(reqs, outs, res):
+        if r["kind"] != lib.QJG_REQ_MESH:
+            continue
+        cap = 3 * r["grid"].n_voxels
+        v = torch.empty(3 * cap, dtype=torch.float64, device="cuda")
+        t = torch.empty(3 * 2 * cap, dtype=torch.int32, device="cuda")
+        h = ctx.upload(r["rs"])
+        it = ctx.iter_params(r["max_it"], 2.0, precision=r["precision"],
+                             refine_pow=lib.QJG_REFINE_INT, rel_tol=r["rel_tol"])
+        _, ms = ctx.mesh_stream(h, r["grid"], it, d_verts64=v.data_ptr(), vert_cap=cap,
+                                d_tris=t.data_ptr(), tri_cap=2 * cap)
+        ctx.free(h)
+        assert rr["n_verts"] == ms["n_verts"] and rr["n_tris"] == ms["n_tris"]
+        tris += ms["n_tris"]
+        np.testing.assert_array_equal(o["verts"], v[:3 * ms["n_verts"]].cpu().numpy())
+        np.testing.assert_array_equal(o["tris"], t[:3 * ms["n_tris"]].cpu().numpy())
+    assert tris > 0
