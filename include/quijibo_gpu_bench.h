@@ -58,9 +58,10 @@ int qjg_set_energy_fast(int on);
 /* Process-wide block count of the energy forward kernel, for sweeps: 0 (the
  * default) the sizing rule (at least 3 blocks of 128 lanes per SM, more when
  * each lane would otherwise take more than about four samples), else that
- * many blocks per SM, capped by residency.  Results do not depend on it (each
- * sample's value is its own; sums run in sample order).  Set it while no
- * energy call is in flight; a negative count returns QJG_ERR_ARG. */
+ * many blocks per SM, capped by residency.  With the one-sample kernel (the
+ * default) results do not depend on it (each sample's value is its own; sums
+ * run in sample order).  Set it while no energy call is in flight; a
+ * negative count returns QJG_ERR_ARG. */
 int qjg_set_energy_forward_blocks(int per_sm);
 
 /* Work of the last qjg_energy_forward/backward call on ctx: the map
