@@ -37,8 +37,8 @@ int qjg_set_field32_pairs(int on);
  * default) one sample per lane.  Set it while no energy call is in flight. */
 int qjg_set_energy_pairs(int on);
 
-/* Process-wide form of the FP32 adjoint of qjg_energy_backward (batches
- * keep the one-lane form), for A/B timing: 1 (the default) each gradient
+/* Process-wide form of the FP32 adjoint of qjg_energy_backward and of
+ * qjg_energy_backward_batch, for A/B timing: 1 (the default) each gradient
  * sample taken by a group of 16 lanes, every lane owning a run of at most 4
  * roots of each side (the products over the roots as scans over the lanes),
  * for maps of at most 64 top and 64 bottom roots (larger maps keep the

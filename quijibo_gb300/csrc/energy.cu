@@ -2223,6 +2223,118 @@ __global__ void __launch_bounds__(SQ_T) sq_bwd_batch_kernel(
     sq_bwd_batch_body<SQM_ACC>(items, K, n_flat, keys, seed_q, seed_L, ck, max_slots);
 }
 
+// The adjoint of a batch with the roots of a step spread over groups of G
+// lanes, as sq_bwd_roots_kernel: the blocks take the items one after the
+// other; per item each block stages the item's roots in shared memory, its
+// groups take the item's sorted gradient samples (flat indices s0 + perm[j])
+// and the block writes one partial row after the item's chunk rows (rows
+// nchunks + blockIdx.x), so an item's rows are its chunks plus gridDim.x.
+constexpr int SQB_ROOT_BYTES = ((5 * QJ_MAX_ROOTS * (int)sizeof(float) + 15) / 16) * 16;
+
+template <int G, int CT, int CB, int M>
+__device__ __forceinline__ void sq_bwd_batch_roots_body(
+    const SqItem* __restrict__ items, int K, long long n_flat, const int* __restrict__ keys,
+    const V4<float>* __restrict__ seed_q, const float* __restrict__ seed_L,
+    const V4<float>* __restrict__ ck) {
+  using T = float;
+  constexpr int NG = SQ_T / G;  // groups per block
+  extern __shared__ unsigned char sh_raw[];
+  T* rp = reinterpret_cast<T*>(sh_raw);  // 4 nr roots, then nr exponents
+  double* acc_sh = reinterpret_cast<double*>(sh_raw + SQB_ROOT_BYTES);
+  const int lane = threadIdx.x & 31, gl = lane & (G - 1);
+  const V4<T> zero{T(0), T(0), T(0), T(0)};
+  const long long stride = (long long)gridDim.x * NG;
+  for (int item = 0; item < K; item++) {
+    const SqItem& it = items[item];
+    const int nt = it.nt, nb = it.nb, nr = nt + nb, slots = it.slots;
+    const T* ep = rp + 4 * nr;
+    __syncthreads();  // the previous item's roots and sums are read
+    for (int k = threadIdx.x; k < 5 * nr; k += SQ_T) rp[k] = it.rp[k];
+    for (int k = threadIdx.x; k < NG * slots; k += SQ_T) acc_sh[k] = 0.0;
+    __syncthreads();
+    const T s = (T)exp(it.params[5 * nr]);
+    double* acc = acc_sh + (threadIdx.x / G) * slots;
+    SideRun<T, CT> top;
+    SideRun<T, CB> bot;
+    side_init<T, G, CT>(top, 0, nt, gl);
+    side_init<T, G, CB>(bot, nt, nb, gl);
+    const int count = *it.total;
+    T dls = T(0);
+    int since = 0;
+    for (long long base = ((long long)blockIdx.x * SQ_T + (threadIdx.x & ~31)) / G; base < count;
+         base += stride) {
+      const long long j = base + lane / G;
+      const bool in = j < count;
+      const long long k = in ? it.s0 + (long long)it.perm[j] : 0;  // flat index
+      const int N = in ? keys[k] : 0;
+      V4<T> qb = in ? seed_q[k] : zero;
+      const T Lb = in ? seed_L[k] : T(0);
+      const int Nmax = __reduce_max_sync(0xffffffffu, N);
+      for (int n = Nmax - 1; n >= 0; n--) {
+        const bool on = n < N;
+        const V4<T> qn = on ? ck[(long long)n * n_flat + k] : zero;
+        V4<T> gp = zero;
+        side_fwd<T, G, CT, M>(rp, ep, T(1), gl, qn, top, gp);
+        side_fwd<T, G, CB, M>(rp, ep, T(-1), gl, qn, bot, gp);
+        const V4<T> g = group_sum4<T, G>(gp);
+        V4<T> Tb, Bb;
+        if (nb > 0) {
+          const V4<T> W4 =
+              v4scale(v4conj(bot.tot), sq_div<T, M>(T(1), v4dot(bot.tot, bot.tot)));
+          const V4<T> Q = v4scale(v4mul(top.tot, W4), s);
+          const V4<T> Qb = v4add(qb, v4scale(Q, sq_div<T, M>(Lb, v4dot(Q, Q))));
+          if (on) dls += v4dot(Qb, Q);
+          Tb = v4scale(v4mul(Qb, v4conj(W4)), s);
+          const V4<T> Wb = v4scale(v4mul(v4conj(top.tot), Qb), s);
+          Bb = v4scale(v4mul(v4mul(v4conj(W4), Wb), v4conj(W4)), T(-1));
+        } else {
+          const V4<T> Q = v4scale(top.tot, s);
+          const V4<T> Qb = v4add(qb, v4scale(Q, sq_div<T, M>(Lb, v4dot(Q, Q))));
+          if (on) dls += v4dot(Qb, Q);
+          Tb = v4scale(Qb, s);
+          Bb = zero;
+        }
+        const V4<T> gb = v4scale(g, sq_div<T, M>(Lb, v4dot(g, g)));
+        V4<T> qbp = zero;
+        side_adj<T, CT, M>(rp, ep, T(1), qn, top, Tb, gb, on, qbp);
+        side_adj<T, CB, M>(rp, ep, T(-1), qn, bot, Bb, gb, on, qbp);
+        qbp = group_sum4<T, G>(qbp);
+        if (on) qb = qbp;
+      }
+      if (++since == SQ_FLUSH) {
+        side_flush<T, CT>(top, acc, nr);
+        side_flush<T, CB>(bot, acc, nr);
+        if (gl == 0) acc[1 + 5 * nr] += (double)dls;
+        dls = T(0);
+        since = 0;
+      }
+    }
+    side_flush<T, CT>(top, acc, nr);
+    side_flush<T, CB>(bot, acc, nr);
+    if (gl == 0) acc[1 + 5 * nr] += (double)dls;
+    __syncthreads();
+    const long long nchunks = max(1LL, (it.n + SQ_CH - 1) / SQ_CH);
+    double* row = it.partials + (nchunks + blockIdx.x) * slots;
+    for (int k = threadIdx.x; k < slots; k += SQ_T) {
+      double v = 0;
+      for (int w = 0; w < NG; w++) v += acc_sh[w * slots + k];
+      row[k] = v;
+    }
+  }
+}
+
+// The FP32 form is chosen once per launch (straight-line root loops).
+template <int G, int CT, int CB, int MINB>
+__global__ void __launch_bounds__(SQ_T, MINB) sq_bwd_batch_roots_kernel(
+    const SqItem* __restrict__ items, int K, long long n_flat, const int* __restrict__ keys,
+    const V4<float>* __restrict__ seed_q, const float* __restrict__ seed_L,
+    const V4<float>* __restrict__ ck) {
+  if (c_sq_fast)
+    sq_bwd_batch_roots_body<G, CT, CB, SQM_FAST>(items, K, n_flat, keys, seed_q, seed_L, ck);
+  else
+    sq_bwd_batch_roots_body<G, CT, CB, SQM_ACC>(items, K, n_flat, keys, seed_q, seed_L, ck);
+}
+
 // The final sums of one item: its chunk rows and as many group rows as its
 // sort produced (read on the device), as sq_reduce_kernel.
 __global__ void __launch_bounds__(32 * SQR_W) sq_reduce_item_kernel(
@@ -2427,7 +2539,7 @@ struct SqBatchLayout {
   int nck = 0, max_slots = 0;
 };
 
-SqBatchLayout sq_batch_layout(const SqBatchReq* r, int K) {
+SqBatchLayout sq_batch_layout(const SqBatchReq* r, int K, int bwd_rows) {
   SqBatchLayout L;
   size_t at = 0;
   auto take = [&](size_t b) {
@@ -2463,8 +2575,10 @@ SqBatchLayout sq_batch_layout(const SqBatchReq* r, int K) {
     L.hist.push_back(take(sizeof(int) * (size_t)(r[i].max_it + 1) * (size_t)L.nchunks[i]));
     L.total.push_back(take(sizeof(int)));
     L.perm.push_back(take(sizeof(unsigned) * std::max<size_t>(n, 1)));
-    L.partials.push_back(
-        take(sizeof(double) * (size_t)(L.nchunks[i] + (long long)(n + 31) / 32) * L.slots[i]));
+    // after the chunk rows: a row per group of 32 samples (one-lane adjoint)
+    // or per block of the grouped adjoint (at most bwd_rows blocks)
+    const long long rows = std::max<long long>((long long)(n + 31) / 32, bwd_rows);
+    L.partials.push_back(take(sizeof(double) * (size_t)(L.nchunks[i] + rows) * L.slots[i]));
     L.out.push_back(take(sizeof(double) * L.slots[i]));
   }
   L.bytes = at;
@@ -2473,12 +2587,15 @@ SqBatchLayout sq_batch_layout(const SqBatchReq* r, int K) {
 
 }  // namespace
 
-size_t sq_batch_scratch_bytes(const SqBatchReq* r, int K) { return sq_batch_layout(r, K).bytes; }
+size_t sq_batch_scratch_bytes(const SqBatchReq* r, int K) {
+  return sq_batch_layout(r, K, sm_count() * SQ_BWD_PER_SM).bytes;
+}
 
 cudaError_t launch_sq_energy_batch(const SqBatchReq* r, int K, void* scratch, double** outs,
                                    cudaStream_t s, int* launches) {
   if (K <= 0) return cudaSuccess;
-  const SqBatchLayout L = sq_batch_layout(r, K);
+  const int sms = sm_count();
+  const SqBatchLayout L = sq_batch_layout(r, K, sms * SQ_BWD_PER_SM);
   unsigned char* scr = static_cast<unsigned char*>(scratch);
   std::vector<SqItem> items((size_t)K);
   std::vector<int> chunk_item((size_t)L.chunks);
@@ -2528,7 +2645,6 @@ cudaError_t launch_sq_energy_batch(const SqBatchReq* r, int K, void* scratch, do
   o.seed_q = reinterpret_cast<V4<float>*>(scr + L.seed_q);
   o.seed_L = reinterpret_cast<float*>(scr + L.seed_L);
   o.ck = reinterpret_cast<V4<float>*>(scr + L.ck);
-  const int sms = sm_count();
   // persistent forward grid: as the single request's first call, a lane per
   // two samples of the batch (at least 3 blocks per SM, at most the resident
   // count), fewer when the batch is small
@@ -2558,14 +2674,46 @@ cudaError_t launch_sq_energy_batch(const SqBatchReq* r, int K, void* scratch, do
         o.keys + s0, r[i].n, r[i].max_it, (int)L.nchunks[(size_t)i], hist, items[(size_t)i].perm);
     n_launch += 3;
   }
-  const size_t sh = sizeof(double) * (SQ_T / 32) * (size_t)L.max_slots;
-  sq_bwd_batch_kernel<<<sms * SQ_BWD_PER_SM, SQ_T, sh, s>>>(d_items, K, L.n_flat, o.keys, o.seed_q,
-                                                              o.seed_L, o.ck, L.max_slots);
+  // the adjoint: the roots over 16-lane groups while every item has at most
+  // 64 roots a side (as a single call), else one lane per sample
+  int ct = 0, cb = 0;
+  for (int i = 0; i < K; i++) {
+    ct = std::max(ct, (r[i].nt + 15) / 16);
+    cb = std::max(cb, (r[i].nb + 15) / 16);
+  }
+  int grp_blocks = 0;  // blocks of the grouped adjoint (0: one-lane form)
+  if (g_sq_bwd_roots.load(std::memory_order_relaxed) && ct <= 4 && cb <= 4) {
+    const size_t shg = SQB_ROOT_BYTES + sizeof(double) * (SQ_T / 16) * (size_t)L.max_slots;
+    int per_sm = 0;
+    if (cb <= 1)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &per_sm, sq_bwd_batch_roots_kernel<16, 4, 1, 8>, SQ_T, shg);
+    else
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &per_sm, sq_bwd_batch_roots_kernel<16, 4, 4, 1>, SQ_T, shg);
+    if (e) return e;
+    grp_blocks = std::max(1, std::min(sms * SQ_BWD_PER_SM, std::max(per_sm, 1) * sms));
+    if (cb <= 1)
+      sq_bwd_batch_roots_kernel<16, 4, 1, 8><<<grp_blocks, SQ_T, shg, s>>>(
+          d_items, K, L.n_flat, o.keys, o.seed_q, o.seed_L, o.ck);
+    else
+      sq_bwd_batch_roots_kernel<16, 4, 4, 1><<<grp_blocks, SQ_T, shg, s>>>(
+          d_items, K, L.n_flat, o.keys, o.seed_q, o.seed_L, o.ck);
+  } else {
+    const size_t sh = sizeof(double) * (SQ_T / 32) * (size_t)L.max_slots;
+    sq_bwd_batch_kernel<<<sms * SQ_BWD_PER_SM, SQ_T, sh, s>>>(d_items, K, L.n_flat, o.keys,
+                                                                o.seed_q, o.seed_L, o.ck, L.max_slots);
+  }
   n_launch++;
   for (int i = 0; i < K; i++) {
-    sq_reduce_item_kernel<<<L.slots[(size_t)i], 32 * SQR_W, 0, s>>>(
-        items[(size_t)i].partials, (int)L.nchunks[(size_t)i], items[(size_t)i].total,
-        L.slots[(size_t)i], outs[i]);
+    if (grp_blocks > 0)
+      sq_reduce_kernel<<<L.slots[(size_t)i], 32 * SQR_W, 0, s>>>(
+          items[(size_t)i].partials, (int)L.nchunks[(size_t)i] + grp_blocks, L.slots[(size_t)i],
+          outs[i]);
+    else
+      sq_reduce_item_kernel<<<L.slots[(size_t)i], 32 * SQR_W, 0, s>>>(
+          items[(size_t)i].partials, (int)L.nchunks[(size_t)i], items[(size_t)i].total,
+          L.slots[(size_t)i], outs[i]);
     n_launch++;
   }
   if (launches) *launches = n_launch;
