@@ -265,6 +265,31 @@ def bench_energy(args):
     lib.set_energy_fast(not args.energy_accurate)
     out["polar_power"] = ("accurate device functions" if args.energy_accurate else
                           "fast: hardware log2 and sin/cos, polynomial atan")
+    if getattr(args, "sweep_blocks", ""):
+        # forward and forward + adjoint calls per forward block count: median
+        # of 7 FP32 calls after one warm-up call (wall clock, ms)
+        sweep = {}
+        fargs = (P.data_ptr(), rs.n_top, rs.n_bottom, n, X.data_ptr(), T.data_ptr(), p["max_it"],
+                 p["escape"])
+        try:
+            for per_sm in [int(v) for v in args.sweep_blocks.split(",")]:
+                lib.set_energy_forward_blocks(per_sm)
+                row = {}
+                for name, g in (("forward_ms", 0), ("gradient_ms", G.data_ptr())):
+                    ctx.energy(*fargs, precision=lib.QJG_FP32, d_grad=g)
+                    torch.cuda.synchronize()
+                    ts = []
+                    for _ in range(7):
+                        t0 = time.perf_counter()
+                        e = ctx.energy(*fargs, precision=lib.QJG_FP32, d_grad=g)
+                        ts.append(time.perf_counter() - t0)
+                    row[name] = sorted(ts)[3] * 1e3
+                    row["energy"] = e
+                sweep[per_sm] = row
+        finally:
+            lib.set_energy_forward_blocks(0)
+        out["forward_blocks_sweep"] = sweep
+        return out
     for name, prec, grad in forms[:2] if args.fp32_only else forms:
         kw = dict(precision=prec, d_grad=G.data_ptr() if grad else 0)
         ctx.energy(P.data_ptr(), rs.n_top, rs.n_bottom, n, X.data_ptr(), T.data_ptr(), p["max_it"],
@@ -837,6 +862,8 @@ def main():
                     help="energy: the FP32 polar power with the accurate device functions")
     ap.add_argument("--energy-pairs", action="store_true",
                     help="energy: the forward kernel with two samples per lane")
+    ap.add_argument("--sweep-blocks", default="",
+                    help="energy: comma-separated forward blocks per SM to time (0: the rule)")
     ap.add_argument("--z0", type=int, default=-1, help="classify: first plane of the slab")
     ap.add_argument("--hbm-gbs", type=float, default=0.0,
                     help="HBM roofline denominator (default: MEASURED_PEAKS.json, else 6800)")
