@@ -338,6 +338,53 @@ def bench_energy(args):
     return out
 
 
+def bench_energy_batch(args):
+    """One qjg_energy_backward_batch pass over 8 FP32 energy + gradient calls
+    (25k Poisson-disk samples each, 64/16, 32/8, 16/4 and 48/12 roots, 30
+    iterations): median of 5 batch calls with the adjoint's roots over
+    16-lane groups and with one lane per sample, and how far apart the two
+    forms' gradients are."""
+    import torch
+
+    from . import lib
+    from .rootsets import Grid, conformal_scale, draw_rootset
+    from .samples import ShapeSDF, poisson_disk
+    ctx = lib.Context(0)
+    items = []
+    for j in range(8):
+        nt, nb = [(64, 16), (32, 8), (16, 4), (48, 12)][j % 4]
+        rs = draw_rootset(40 + j, nt, nb, -1.2, 1.2, exps=(1, 2))
+        rs.scale = conformal_scale(rs, Grid((16, 16, 16), lengths=(2.0, 2.0, 2.0)))
+        xyz, _ = poisson_disk(args.batch_samples, seed=j)
+        t = ShapeSDF(j)(xyz)
+        p = torch.from_numpy(lib.params_of(rs)).cuda()
+        X, T = torch.from_numpy(xyz).cuda(), torch.from_numpy(t).cuda()
+        g = torch.empty(5 * (nt + nb) + 1, dtype=torch.float64, device="cuda")
+        items.append(dict(d_params=p.data_ptr(), n_top=nt, n_bot=nb, n=len(t),
+                          d_xyz=X.data_ptr(), d_target=T.data_ptr(), max_it=30, escape=2.0,
+                          d_sat=1.0, d_grad=g.data_ptr(), keep=(p, X, T, g)))
+    out = {"items": len(items), "samples_per_item": args.batch_samples}
+    grads = {}
+    try:
+        for roots in (False, True):
+            lib.set_energy_adjoint_roots(roots)
+            ctx.energy_batch(items)
+            torch.cuda.synchronize()
+            ts = []
+            for _ in range(5):
+                t0 = time.perf_counter()
+                ctx.energy_batch(items)
+                ts.append(time.perf_counter() - t0)
+            name = "grouped_adjoint_ms" if roots else "one_lane_adjoint_ms"
+            out[name] = sorted(ts)[2] * 1e3
+            grads[roots] = [it["keep"][3].cpu().numpy().copy() for it in items]
+    finally:
+        lib.set_energy_adjoint_roots(True)
+    out["max_rel_gradient_difference"] = max(
+        float(np.linalg.norm(a - b) / np.linalg.norm(a)) for a, b in zip(grads[False], grads[True]))
+    return out
+
+
 def _stream(seed, n, scale):
     """Poisson-arrival mix of field, field+mesh and energy+gradient requests:
     grid sides log-uniform in [32, 512] (field) and [128, 1024] (mesh) times
@@ -836,7 +883,7 @@ def bench_tanh(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("what", choices=["mesh", "energy", "serve", "large", "tooth", "tanh",
-                                     "classify", "lagrange", "mesh_fixed"])
+                                     "classify", "lagrange", "mesh_fixed", "energy_batch"])
     ap.add_argument("--res", type=int, default=0, help="grid edge (mesh: 512, large: 2200)")
     ap.add_argument("--workload", default="precision", choices=["precision", "large"])
     ap.add_argument("--slab", type=int, default=64)
@@ -862,6 +909,8 @@ def main():
                     help="energy: the FP32 polar power with the accurate device functions")
     ap.add_argument("--energy-pairs", action="store_true",
                     help="energy: the forward kernel with two samples per lane")
+    ap.add_argument("--batch-samples", type=int, default=25_000,
+                    help="energy_batch: samples per item")
     ap.add_argument("--sweep-blocks", default="",
                     help="energy: comma-separated forward blocks per SM to time (0: the rule)")
     ap.add_argument("--z0", type=int, default=-1, help="classify: first plane of the slab")
@@ -872,7 +921,7 @@ def main():
     fn = {"mesh": bench_mesh, "energy": bench_energy, "serve": bench_serve,
           "large": bench_large, "tooth": bench_tooth, "tanh": bench_tanh,
           "classify": bench_classify, "lagrange": bench_lagrange,
-          "mesh_fixed": bench_mesh_fixed}[args.what]
+          "mesh_fixed": bench_mesh_fixed, "energy_batch": bench_energy_batch}[args.what]
     print(json.dumps(fn(args)), flush=True)
 
 
